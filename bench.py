@@ -1,0 +1,323 @@
+#!/usr/bin/env python
+"""Benchmark of the GB300 TSQR-SVD hot path (pyLOM.math.tsqr_svd / POD.SVD).
+
+Workload (one "step"): the TSQR-SVD of the large POD snapshot matrix,
+8,388,608 points x 1,024 snapshots, FP32 (32 GiB), temporal mean removed
+before the timed region, mixed precision form (TF32x3 tensor-core tall
+products, FP64 n x n stage).  The matrix is far larger than L2 (129 MB), so no
+flush is needed between steps.
+
+metric "TSQR-SVD GB/s" = algorithmic bytes / time, bytes = s*m*n (read X) +
+s*m*n (write U), s = 4.
+
+Usage: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+Multi-GPU: the path runs one replica per GPU ("replicas only"); value is the
+sum over ranks of matrices processed / max-over-ranks time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+M_FULL = 8_388_608
+N_FULL = 1024
+NMODES = 64
+SEED = 1002
+CPU_SAMPLE_ROWS = 131_072
+FP64_SAMPLE_ROWS = 1_048_576
+
+
+def algorithmic_bytes(m, n, s=4):
+    return 2 * s * m * n
+
+
+def algorithmic_flops(m, n):
+    return 4.0 * m * n * n
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return d.get("hbm_gbs", 6800.0), d.get("bf16_tflops", 1900.0), "measured"
+    except Exception:
+        return 6800.0, 1900.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clock/throttle sampling during the timed region."""
+
+    def __init__(self, gpu_index=0):
+        self.samples = []
+        self.proc = None
+        self.gpu = gpu_index
+
+    def __enter__(self):
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) >= 9:
+                self.samples.append(parts)
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
+        mx = [float(s[2]) for s in self.samples if s[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = set()
+        for s in self.samples:
+            for nm, v in zip(names, s[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": float(np.median(sm)) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(self.samples)}
+
+
+def dist_setup(n_gpus):
+    import torch
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    return rank, world, local
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def max_over_ranks(x, world):
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], device="cuda", dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+# ---------------------------------------------------------------------------
+# CPU baseline (oracle port on the host cores, bounded sample)
+# ---------------------------------------------------------------------------
+
+def cpu_baseline(rows=CPU_SAMPLE_ROWS, reps=1):
+    from oracle import plom_oracle as O
+    from pyloworder_gb300 import datagen
+    nx, ny = datagen.grid_for_points(rows)
+    X = datagen.pod_field_np(nx, ny, N_FULL, NMODES, seed=SEED, noise=1e-5, amp_pow=1.5,
+                             dtype=np.float32, distinct=True)
+    X = X - X.mean(axis=1, keepdims=True)
+    O.tsqr_svd(X[:4096])  # warm the BLAS threads
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        O.tsqr_svd(X)
+    dt = (time.perf_counter() - t0) / reps
+    cores = os.cpu_count()
+    return {"value": algorithmic_bytes(rows, N_FULL) / dt / 1e9, "unit": "GB/s", "cores": cores,
+            "kind": "port",
+            "sample": f"oracle tsqr_svd (numpy/LAPACK, all {cores} host threads) on {rows} x {N_FULL} "
+                      f"FP32 rows of the same field, {dt:.2f} s per call"}
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return 0
+    vals = []
+    for _ in range(max(1, args.warmup)):
+        cpu_baseline(rows=CPU_SAMPLE_ROWS // 4)
+    for _ in range(args.steps):
+        vals.append(cpu_baseline(rows=CPU_SAMPLE_ROWS // 2))
+    v = float(np.median([x["value"] for x in vals]))
+    ms = algorithmic_bytes(CPU_SAMPLE_ROWS // 2, N_FULL) / (v * 1e9) * 1e3
+    line = {"metric": "TSQR-SVD GB/s", "value": v, "unit": "GB/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic", "impl": "reference",
+            "config": {"workload": f"tsqr_svd {M_FULL}x{N_FULL} f32 (sampled rows)",
+                       "sample_rows": CPU_SAMPLE_ROWS // 2},
+            "cpu_baseline": dict(vals[-1], value=v),
+            "e2e": {"value": v, "unit": "GB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+# ---------------------------------------------------------------------------
+# our arm
+# ---------------------------------------------------------------------------
+
+def run_ours(args):
+    import torch
+    rank, world, local = dist_setup(args.gpus)
+    import pyloworder_gb300 as P
+    from pyloworder_gb300 import _lib as L, datagen
+    L.load()
+    m, n = args.m, N_FULL
+    nx, ny = datagen.grid_for_points(m)
+    X = datagen.pod_field_device(nx, ny, n, NMODES, seed=SEED + rank, noise=1e-5, amp_pow=1.5)
+    Y, _, _ = P.vmmath.remove_mean_device(X, n)
+    del X
+    torch.cuda.synchronize()
+    st = torch.cuda.current_stream()
+    prof = L.Profiler() if hasattr(L, "Profiler") else None
+
+    def step():
+        return P.vmmath.tsqr_svd_device(Y, n, "mixed")
+
+    for _ in range(args.warmup):
+        out = step()
+    del out
+    torch.cuda.synchronize()
+    if prof:
+        prof.start()
+    barrier(world)
+    torch.cuda.synchronize()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk:
+        ev0.record(st)
+        for _ in range(args.steps):
+            U, S, V = step()
+        ev1.record(st)
+        torch.cuda.synchronize()
+    barrier(world)
+    ms = ev0.elapsed_time(ev1) / args.steps
+    ms = max_over_ranks(ms, world)
+    kernels = prof.stop() if prof else {}
+    value = algorithmic_bytes(m, n) * world / (ms * 1e-3) / 1e9
+
+    # accuracy of the mixed form against the FP64 form on a row sample
+    acc = {}
+    fp64 = {}
+    if rank == 0 and not args.quick:
+        ms_rows = min(m, FP64_SAMPLE_ROWS)
+        Ys = Y[:ms_rows]
+        torch.cuda.synchronize()
+        P.vmmath.tsqr_svd_device(Ys[:65536], n, "fp64")  # warm
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(st)
+        U64, S64, V64 = P.vmmath.tsqr_svd_device(Ys, n, "fp64")
+        e1.record(st)
+        torch.cuda.synchronize()
+        t64 = e0.elapsed_time(e1)
+        Um, Sm, Vm = P.vmmath.tsqr_svd_device(Ys, n, "mixed")
+        torch.cuda.synchronize()
+        s64 = S64.double().cpu().numpy()
+        sm = Sm.double().cpu().numpy()
+        k = NMODES
+        a = Um[:, :k].double()
+        b = U64[:, :k].double()
+        cosines = torch.linalg.svdvals(a.T @ b).cpu().numpy()
+        acc = {"sample_rows": ms_rows,
+               "sigma_rel_err_retained": float(np.max(np.abs(sm[:k] - s64[:k]) / s64[:k])),
+               "subspace_angle_retained": float(np.arccos(min(1.0, cosines.min()))),
+               "orth_retained": float(torch.linalg.matrix_norm(
+                   torch.eye(k, device="cuda", dtype=torch.float64) - a.T @ a, ord=2)),
+               "sigma_normwise_all": float(np.max(np.abs(sm - s64)) / s64[0])}
+        fp64 = {"value": algorithmic_bytes(ms_rows, n) / (t64 * 1e-3) / 1e9, "unit": "GB/s",
+                "ms": t64, "rows": ms_rows,
+                "note": "plain FP64 GPU form on a row sample (throughput is linear in rows)"}
+        del U64, S64, V64, Um, Sm, Vm
+
+    # end to end through the public API with pinned host buffers
+    e2e = None
+    if rank == 0 and not args.quick:
+        del U, S, V
+        Yh = torch.empty((m, n), dtype=torch.float32, pin_memory=True)
+        Yh.copy_(Y)
+        del Y
+        torch.cuda.empty_cache()
+        steps = max(1, min(args.steps, 3))
+        P.math.tsqr_svd(Yh[:65536])
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(steps):
+            Uh, Sh, Vh = P.math.tsqr_svd(Yh)
+        torch.cuda.synchronize()
+        te = (time.perf_counter() - t0) / steps
+        e2e = {"value": algorithmic_bytes(m, n) / te / 1e9, "unit": "GB/s",
+               "h2d_bytes_per_step": int(4 * m * n),
+               "d2h_bytes_per_step": int(4 * m * n + 4 * n + 4 * n * n),
+               "ms_per_step": te * 1e3}
+        del Yh, Uh
+
+    hbm, bf16, how = peaks()
+    cpu = cpu_baseline() if (rank == 0 and not args.quick and world == 1) else None
+    if rank == 0:
+        roof = None
+        if kernels:
+            top = max(kernels.values(), key=lambda k: k["ms_total"])
+            achieved = top["flops"] / (top["ms_total"] * 1e-3) / 1e12
+            roof = {"bound": "tensor", "kernel": top["name"], "achieved": achieved, "peak": bf16,
+                    "unit": "TFLOP/s", "frac": achieved / bf16, "traffic": None,
+                    "peak_source": how}
+        line = {"metric": "TSQR-SVD GB/s", "value": value, "unit": "GB/s", "n_gpus": world,
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+                "data": "synthetic",
+                "config": {"workload": f"tsqr_svd {m}x{n} f32 (POD config 2, mean removed)",
+                           "precision": "mixed", "l2": "inputs larger than L2 (32 GiB)",
+                           "parallelism": "replicas" if world > 1 else "single"},
+                "clocks": clk.summary(), "gpu_launches": sum(k["count"] for k in kernels.values()) if kernels else None,
+                "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "fp64_form": fp64,
+                "accuracy_vs_fp64": acc, "kernels": kernels}
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--m", type=int, default=M_FULL)
+    ap.add_argument("--quick", action="store_true", help="skip accuracy / e2e / CPU legs")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

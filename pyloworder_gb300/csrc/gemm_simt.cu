@@ -1,0 +1,313 @@
+// CUDA-core (SIMT) GEMMs for the tall-skinny shapes of the SVD path.
+//
+//  * gemm_nn:  C(M x N) = A(M x K) B(K x N), A tall (M = points), B small.
+//              Used for Q = X R^-1, U = Q Ur, Y = A Omega, Phi = Y2 (...).
+//  * gemm_tn:  C(M x N) = A(K x M)^T B(K x N) with K = points (huge): a
+//              split-K reduction over row chunks, partial tiles written to
+//              a workspace slab and summed in FP64 in a fixed order (the
+//              in-GPU replacement of the TSQR butterfly / MPI_Allreduce of
+//              pyLOM/vmmath/src/svd.c:565-676 and vector_matrix.c:330-356).
+//              sym=true computes only the upper block triangle (Gram).
+//
+// These are the plain-FP64 GPU form's products (GB300's FP64 rate bounds
+// them), the n x n FP64 products of the small factorizations, and the
+// fallback of the mixed form for operand shapes the tensor-core kernels do
+// not take.
+#include "plom_common.cuh"
+#include "plom_kernels.cuh"
+
+#include <algorithm>
+
+namespace plom {
+
+// ----------------------------------------------------------------------------
+// NN: BM x BN block tile, BK deep; 256 threads as 16 x 16, TM x TN per thread.
+// ----------------------------------------------------------------------------
+template <typename TA, typename TB, typename TC, typename Acc, int BM, int BN, int BK, int TM,
+          int TN>
+__global__ void __launch_bounds__(256) gemm_nn_kernel(const TA* __restrict__ A, int64_t lda,
+                                                      int64_t sA, const TB* __restrict__ B,
+                                                      int64_t ldb, int64_t sB, TC* __restrict__ C,
+                                                      int64_t ldc, int64_t sC, int64_t M,
+                                                      int64_t N, int64_t K) {
+  static_assert(BM == 16 * TM && BN == 16 * TN, "tile/thread mismatch");
+  A += (int64_t)blockIdx.z * sA;
+  B += (int64_t)blockIdx.z * sB;
+  C += (int64_t)blockIdx.z * sC;
+  __shared__ Acc As[BK][BM + 1];
+  __shared__ Acc Bs[BK][BN];
+  const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+  const int64_t m0 = (int64_t)blockIdx.x * BM;
+  const int64_t n0 = (int64_t)blockIdx.y * BN;
+  Acc acc[TM][TN];
+#pragma unroll
+  for (int i = 0; i < TM; ++i)
+#pragma unroll
+    for (int j = 0; j < TN; ++j) acc[i][j] = Acc(0);
+
+  for (int64_t k0 = 0; k0 < K; k0 += BK) {
+    // A tile: BM rows x BK cols
+    for (int e = threadIdx.x; e < BM * BK; e += 256) {
+      int r = e / BK, c = e % BK;
+      int64_t gr = m0 + r, gc = k0 + c;
+      As[c][r] = (gr < M && gc < K) ? (Acc)A[gr * lda + gc] : Acc(0);
+    }
+    for (int e = threadIdx.x; e < BK * BN; e += 256) {
+      int r = e / BN, c = e % BN;
+      int64_t gr = k0 + r, gc = n0 + c;
+      Bs[r][c] = (gr < K && gc < N) ? (Acc)B[gr * ldb + gc] : Acc(0);
+    }
+    __syncthreads();
+#pragma unroll
+    for (int kk = 0; kk < BK; ++kk) {
+      Acc a[TM], b[TN];
+#pragma unroll
+      for (int i = 0; i < TM; ++i) a[i] = As[kk][ty + 16 * i];
+#pragma unroll
+      for (int j = 0; j < TN; ++j) b[j] = Bs[kk][tx + 16 * j];
+#pragma unroll
+      for (int i = 0; i < TM; ++i)
+#pragma unroll
+        for (int j = 0; j < TN; ++j) acc[i][j] = fma(a[i], b[j], acc[i][j]);
+    }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int i = 0; i < TM; ++i) {
+    int64_t gr = m0 + ty + 16 * i;
+    if (gr >= M) continue;
+#pragma unroll
+    for (int j = 0; j < TN; ++j) {
+      int64_t gc = n0 + tx + 16 * j;
+      if (gc < N) C[gr * ldc + gc] = (TC)acc[i][j];
+    }
+  }
+}
+
+template <typename TA, typename TB, typename TC, typename Acc>
+int gemm_nn_batched(const TA* A, int64_t lda, int64_t sA, const TB* B, int64_t ldb, int64_t sB,
+                    TC* C, int64_t ldc, int64_t sC, int64_t M, int64_t N, int64_t K, int batch,
+                    cudaStream_t st) {
+  if (M == 0 || N == 0 || batch == 0) return PLOM_OK;
+  PLOM_REQUIRE(A && B && C, PLOM_ERR_ARG, "gemm_nn: null operand");
+  constexpr int BM = 128, BN = 64, BK = 8;
+  dim3 grid((unsigned)cdiv(M, BM), (unsigned)cdiv(N, BN), (unsigned)batch);
+  PLOM_REQUIRE(grid.y <= 65535 && batch <= 65535, PLOM_ERR_ARG, "gemm_nn: N or batch too large");
+  gemm_nn_kernel<TA, TB, TC, Acc, BM, BN, BK, 8, 4><<<grid, 256, 0, st>>>(A, lda, sA, B, ldb, sB, C,
+                                                                          ldc, sC, M, N, K);
+  PLOM_CHECK_LAUNCH();
+  return PLOM_OK;
+}
+
+template <typename TA, typename TB, typename TC, typename Acc>
+int gemm_nn(const TA* A, int64_t lda, const TB* B, int64_t ldb, TC* C, int64_t ldc, int64_t M,
+            int64_t N, int64_t K, cudaStream_t st) {
+  return gemm_nn_batched<TA, TB, TC, Acc>(A, lda, 0, B, ldb, 0, C, ldc, 0, M, N, K, 1, st);
+}
+
+// ----------------------------------------------------------------------------
+// TN split-K: partial[b][c](M x N) = sum_{k in chunk c} A_b[k][i] B_b[k][j]
+// ----------------------------------------------------------------------------
+template <typename TA, typename TB, typename Acc, int BM, int BN, int BK>
+__global__ void __launch_bounds__(256) gemm_tn_kernel(const TA* __restrict__ A, int64_t lda,
+                                                      int64_t sA, const TB* __restrict__ B,
+                                                      int64_t ldb, int64_t sB,
+                                                      Acc* __restrict__ part, int64_t M, int64_t N,
+                                                      int64_t K, int64_t kchunk, int nchunks,
+                                                      const int2* __restrict__ tiles) {
+  constexpr int TM = BM / 16, TN = BN / 16;
+  __shared__ Acc As[BK][BM];
+  __shared__ Acc Bs[BK][BN];
+  const int bz = blockIdx.z;
+  A += (int64_t)bz * sA;
+  B += (int64_t)bz * sB;
+  const int2 t = tiles[blockIdx.x];
+  const int64_t i0 = (int64_t)t.x * BM, j0 = (int64_t)t.y * BN;
+  const int64_t kbeg = (int64_t)blockIdx.y * kchunk;
+  const int64_t kend = min(K, kbeg + kchunk);
+  const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+  Acc acc[TM][TN];
+#pragma unroll
+  for (int i = 0; i < TM; ++i)
+#pragma unroll
+    for (int j = 0; j < TN; ++j) acc[i][j] = Acc(0);
+  for (int64_t k0 = kbeg; k0 < kend; k0 += BK) {
+    for (int e = threadIdx.x; e < BK * BM; e += 256) {
+      int r = e / BM, c = e % BM;
+      int64_t gk = k0 + r, gi = i0 + c;
+      As[r][c] = (gk < kend && gi < M) ? (Acc)A[gk * lda + gi] : Acc(0);
+    }
+    for (int e = threadIdx.x; e < BK * BN; e += 256) {
+      int r = e / BN, c = e % BN;
+      int64_t gk = k0 + r, gj = j0 + c;
+      Bs[r][c] = (gk < kend && gj < N) ? (Acc)B[gk * ldb + gj] : Acc(0);
+    }
+    __syncthreads();
+#pragma unroll
+    for (int kk = 0; kk < BK; ++kk) {
+      Acc a[TM], b[TN];
+#pragma unroll
+      for (int i = 0; i < TM; ++i) a[i] = As[kk][ty + 16 * i];
+#pragma unroll
+      for (int j = 0; j < TN; ++j) b[j] = Bs[kk][tx + 16 * j];
+#pragma unroll
+      for (int i = 0; i < TM; ++i)
+#pragma unroll
+        for (int j = 0; j < TN; ++j) acc[i][j] = fma(a[i], b[j], acc[i][j]);
+    }
+    __syncthreads();
+  }
+  Acc* P = part + ((int64_t)bz * nchunks + blockIdx.y) * M * N;
+#pragma unroll
+  for (int i = 0; i < TM; ++i) {
+    int64_t gi = i0 + ty + 16 * i;
+    if (gi >= M) continue;
+#pragma unroll
+    for (int j = 0; j < TN; ++j) {
+      int64_t gj = j0 + tx + 16 * j;
+      if (gj < N) P[gi * N + gj] = acc[i][j];
+    }
+  }
+}
+
+// Sum the chunk partials in a fixed order (deterministic), mirror the upper
+// block triangle for sym, and write C (batch stride sC) in TC.
+template <typename Acc, typename TC>
+__global__ void reduce_partials_kernel(const Acc* __restrict__ part, int nchunks, int64_t M,
+                                       int64_t N, int sym, int bm, int bn, TC* __restrict__ C,
+                                       int64_t ldc, int64_t sC, int batch) {
+  const int64_t total = M * N;
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < total * batch;
+       e += (int64_t)gridDim.x * blockDim.x) {
+    int64_t b = e / total, r = e % total;
+    int64_t i = r / N, j = r % N;
+    int64_t si = i, sj = j;
+    if (sym && (i / bm) > (j / bn)) {  // lower block triangle: read the mirror
+      si = j;
+      sj = i;
+    }
+    const Acc* p = part + b * nchunks * total + si * N + sj;
+    double s = 0.0;
+    for (int c = 0; c < nchunks; ++c) s += (double)p[(int64_t)c * total];
+    C[b * sC + i * ldc + j] = (TC)s;
+  }
+}
+
+__global__ void make_tiles_kernel(int2* tiles, int tm, int tn, int sym) {
+  int idx = 0;
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  for (int i = 0; i < tm; ++i)
+    for (int j = 0; j < tn; ++j)
+      if (!sym || i <= j) tiles[idx++] = make_int2(i, j);
+}
+
+static int tn_chunks(int64_t ntiles, int64_t K, int BK, int batch) {
+  int64_t target = (int64_t)num_sms() * 4;
+  int64_t c = cdiv(target, ntiles * batch);
+  int64_t maxc = cdiv(K, (int64_t)BK * 64);  // at least 64 k-steps per chunk
+  if (c > maxc) c = maxc;
+  if (c < 1) c = 1;
+  if (c > 512) c = 512;
+  return (int)c;
+}
+
+struct TnPlan {
+  int64_t tm, tn, ntiles, kchunk;
+  int chunks;
+};
+static TnPlan tn_plan(int64_t M, int64_t N, int64_t K, bool sym, int batch) {
+  constexpr int BM = 64, BN = 64, BK = 16;
+  TnPlan p;
+  p.tm = cdiv(M, BM);
+  p.tn = cdiv(N, BN);
+  p.ntiles = sym ? p.tm * (p.tm + 1) / 2 : p.tm * p.tn;
+  int c = tn_chunks(p.ntiles, K, BK, batch);
+  int64_t kc = cdiv(std::max<int64_t>(K, 1), c);
+  kc = cdiv(kc, BK) * BK;
+  p.kchunk = kc;
+  p.chunks = (int)std::max<int64_t>(1, cdiv(K, kc));
+  return p;
+}
+
+size_t gemm_tn_workspace_batched(int64_t M, int64_t N, int64_t K, bool sym, size_t acc_bytes,
+                                 int batch) {
+  TnPlan p = tn_plan(M, N, K, sym, batch);
+  Arena a(nullptr, 0);
+  a.take<char>((size_t)batch * p.chunks * M * N * acc_bytes);
+  a.take<int2>((size_t)p.tm * p.tn);
+  return a.off + 256;
+}
+size_t gemm_tn_workspace(int64_t M, int64_t N, int64_t K, bool sym, size_t acc_bytes) {
+  return gemm_tn_workspace_batched(M, N, K, sym, acc_bytes, 1);
+}
+
+template <typename TA, typename TB, typename Acc, typename TC>
+int gemm_tn_batched(const TA* A, int64_t lda, int64_t sA, const TB* B, int64_t ldb, int64_t sB,
+                    TC* C, int64_t ldc, int64_t sC, int64_t M, int64_t N, int64_t K, bool sym,
+                    int batch, Arena& ws, cudaStream_t st) {
+  if (M == 0 || N == 0 || batch == 0) return PLOM_OK;
+  constexpr int BM = 64, BN = 64, BK = 16;
+  PLOM_REQUIRE(!sym || M == N, PLOM_ERR_ARG, "gemm_tn: sym needs a square result");
+  PLOM_REQUIRE(batch <= 65535, PLOM_ERR_ARG, "gemm_tn: batch too large");
+  TnPlan p = tn_plan(M, N, K, sym, batch);
+  Acc* part = ws.take<Acc>((size_t)batch * p.chunks * M * N);
+  int2* tiles = ws.take<int2>((size_t)p.tm * p.tn);
+  if (ws.measuring()) return PLOM_OK;
+  PLOM_REQUIRE(!ws.overflow(), PLOM_ERR_WORKSPACE, "gemm_tn: workspace too small");
+  PLOM_REQUIRE(A && B && C && part, PLOM_ERR_ARG, "gemm_tn: null operand");
+  make_tiles_kernel<<<1, 1, 0, st>>>(tiles, (int)p.tm, (int)p.tn, sym ? 1 : 0);
+  PLOM_CHECK_LAUNCH();
+  if (K > 0) {
+    dim3 grid((unsigned)p.ntiles, (unsigned)p.chunks, (unsigned)batch);
+    gemm_tn_kernel<TA, TB, Acc, BM, BN, BK><<<grid, 256, 0, st>>>(A, lda, sA, B, ldb, sB, part, M,
+                                                                  N, K, p.kchunk, p.chunks, tiles);
+    PLOM_CHECK_LAUNCH();
+  } else {
+    PLOM_CHECK_CUDA(cudaMemsetAsync(part, 0, sizeof(Acc) * M * N * batch * p.chunks, st));
+  }
+  int64_t total = M * N * batch;
+  int blocks = (int)std::min<int64_t>(cdiv(total, 256), (int64_t)num_sms() * 16);
+  reduce_partials_kernel<Acc, TC><<<blocks, 256, 0, st>>>(part, p.chunks, M, N, sym ? 1 : 0, BM, BN,
+                                                          C, ldc, sC, batch);
+  PLOM_CHECK_LAUNCH();
+  return PLOM_OK;
+}
+
+template <typename TA, typename TB, typename Acc, typename TC>
+int gemm_tn(const TA* A, int64_t lda, const TB* B, int64_t ldb, TC* C, int64_t ldc, int64_t M,
+            int64_t N, int64_t K, bool sym, Arena& ws, cudaStream_t st) {
+  return gemm_tn_batched<TA, TB, Acc, TC>(A, lda, 0, B, ldb, 0, C, ldc, 0, M, N, K, sym, 1, ws, st);
+}
+
+// explicit instantiations used across the library
+#define NN(TA, TB, TC, ACC)                                                                  \
+  template int gemm_nn<TA, TB, TC, ACC>(const TA*, int64_t, const TB*, int64_t, TC*, int64_t, \
+                                        int64_t, int64_t, int64_t, cudaStream_t);             \
+  template int gemm_nn_batched<TA, TB, TC, ACC>(const TA*, int64_t, int64_t, const TB*, int64_t, \
+                                                int64_t, TC*, int64_t, int64_t, int64_t, int64_t, \
+                                                int64_t, int, cudaStream_t);
+NN(float, float, float, float)
+NN(float, double, double, double)
+NN(float, double, float, double)
+NN(double, double, double, double)
+NN(double, double, float, double)
+NN(float, double, float, float)
+NN(float, float, float, double)
+#undef NN
+#define TN(TA, TB, ACC, TC)                                                                    \
+  template int gemm_tn<TA, TB, ACC, TC>(const TA*, int64_t, const TB*, int64_t, TC*, int64_t,   \
+                                        int64_t, int64_t, int64_t, bool, Arena&, cudaStream_t); \
+  template int gemm_tn_batched<TA, TB, ACC, TC>(const TA*, int64_t, int64_t, const TB*, int64_t, \
+                                                int64_t, TC*, int64_t, int64_t, int64_t, int64_t, \
+                                                int64_t, bool, int, Arena&, cudaStream_t);
+TN(float, float, float, double)
+TN(float, float, double, double)
+TN(double, double, double, double)
+TN(float, float, float, float)
+TN(float, float, double, float)
+TN(double, double, double, float)
+TN(float, double, double, double)
+TN(double, float, double, double)
+#undef TN
+
+}  // namespace plom

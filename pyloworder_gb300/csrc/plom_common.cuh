@@ -1,0 +1,104 @@
+// Common definitions for libplom: error state, workspace carving, launch
+// helpers and small device utilities shared by every translation unit.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <stddef.h>
+#include <stdio.h>
+#include <stdarg.h>
+#include <string.h>
+
+#include "../../include/plom.h"
+
+namespace plom {
+
+// ---------------------------------------------------------------------------
+// error handling: every C-ABI entry returns an int status; the message of the
+// last failure on the calling host thread is kept for plom_last_error_string.
+// ---------------------------------------------------------------------------
+void set_error(const char* fmt, ...);
+const char* last_error();
+
+#define PLOM_CHECK_CUDA(expr)                                                        \
+  do {                                                                               \
+    cudaError_t _e = (expr);                                                         \
+    if (_e != cudaSuccess) {                                                         \
+      ::plom::set_error("%s:%d: %s -> %s", __FILE__, __LINE__, #expr,                \
+                        cudaGetErrorString(_e));                                     \
+      return PLOM_ERR_CUDA;                                                          \
+    }                                                                                \
+  } while (0)
+
+#define PLOM_CHECK_LAUNCH() PLOM_CHECK_CUDA(cudaGetLastError())
+
+#define PLOM_TRY(expr)                                                               \
+  do {                                                                               \
+    int _s = (expr);                                                                 \
+    if (_s != PLOM_OK) return _s;                                                    \
+  } while (0)
+
+#define PLOM_REQUIRE(cond, code, ...)                                                \
+  do {                                                                               \
+    if (!(cond)) {                                                                   \
+      ::plom::set_error(__VA_ARGS__);                                                \
+      return (code);                                                                 \
+    }                                                                                \
+  } while (0)
+
+// ---------------------------------------------------------------------------
+// workspace: a caller-owned device buffer carved into aligned sub-buffers.
+// Running with base == nullptr only measures (workspace queries).
+// ---------------------------------------------------------------------------
+struct Arena {
+  char* base;
+  size_t cap;
+  size_t off;
+  Arena(void* b, size_t c) : base(static_cast<char*>(b)), cap(c), off(0) {}
+  template <typename T>
+  T* take(size_t count, size_t align = 256) {
+    size_t o = (off + align - 1) / align * align;
+    off = o + count * sizeof(T);
+    if (base == nullptr) return nullptr;
+    return reinterpret_cast<T*>(base + o);
+  }
+  bool measuring() const { return base == nullptr; }
+  bool overflow() const { return base != nullptr && off > cap; }
+};
+
+inline int num_sms() {
+  static int sms = -1;
+  if (sms < 0) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (sms <= 0) sms = 152;
+  }
+  return sms;
+}
+
+inline int64_t cdiv(int64_t a, int64_t b) { return (a + b - 1) / b; }
+
+// ---------------------------------------------------------------------------
+// device helpers
+// ---------------------------------------------------------------------------
+template <typename T>
+__device__ __forceinline__ T warp_sum(T v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+template <typename T>
+__device__ __forceinline__ T warp_max(T v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v = max(v, __shfl_xor_sync(0xffffffffu, v, o));
+  return v;
+}
+
+// status words written by kernels (device side) and read back by the host.
+// Index 0: numerical failure code (0 = ok), 1: count of Cholesky shift
+// escalations, 2: Jacobi sweeps of the last small SVD, 3: non-finite input seen.
+enum { ST_FAIL = 0, ST_SHIFTS = 1, ST_SWEEPS = 2, ST_NONFINITE = 3, ST_WORDS = 8 };
+
+}  // namespace plom

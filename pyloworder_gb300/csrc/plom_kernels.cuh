@@ -1,0 +1,70 @@
+// Internal (C++) interfaces shared between libplom translation units.
+#pragma once
+#include "plom_common.cuh"
+
+namespace plom {
+
+// ---- averaging.cu ----
+int rows_dispatch(int dtype, const void* X, int64_t m, int64_t n, int64_t ldx, const void* mean_in,
+                  const void* var_in, void* mean_out, void* var_out, int want_var, int ymode,
+                  void* Y, int64_t ldy, cudaStream_t st);
+
+// ---- gemm_simt.cu ----
+template <typename TA, typename TB, typename TC, typename Acc>
+int gemm_nn(const TA* A, int64_t lda, const TB* B, int64_t ldb, TC* C, int64_t ldc, int64_t M,
+            int64_t N, int64_t K, cudaStream_t st);
+template <typename TA, typename TB, typename TC, typename Acc>
+int gemm_nn_batched(const TA* A, int64_t lda, int64_t sA, const TB* B, int64_t ldb, int64_t sB,
+                    TC* C, int64_t ldc, int64_t sC, int64_t M, int64_t N, int64_t K, int batch,
+                    cudaStream_t st);
+template <typename TA, typename TB, typename Acc, typename TC>
+int gemm_tn(const TA* A, int64_t lda, const TB* B, int64_t ldb, TC* C, int64_t ldc, int64_t M,
+            int64_t N, int64_t K, bool sym, Arena& ws, cudaStream_t st);
+template <typename TA, typename TB, typename Acc, typename TC>
+int gemm_tn_batched(const TA* A, int64_t lda, int64_t sA, const TB* B, int64_t ldb, int64_t sB,
+                    TC* C, int64_t ldc, int64_t sC, int64_t M, int64_t N, int64_t K, bool sym,
+                    int batch, Arena& ws, cudaStream_t st);
+size_t gemm_tn_workspace(int64_t M, int64_t N, int64_t K, bool sym, size_t acc_bytes);
+size_t gemm_tn_workspace_batched(int64_t M, int64_t N, int64_t K, bool sym, size_t acc_bytes,
+                                 int batch);
+
+// ---- dense.cu (FP64 small dense, batched, cooperative) ----
+// Upper Cholesky R^T R = G + s I of `batch` n x n matrices (stride n*n, ld n).
+// s starts at shift_rel0 * trace(G)/n; on a non-positive pivot the whole
+// factorization restarts with s = max(s*100, shift_rel_fail*trace/n).
+// info[ST_FAIL] = PLOM_NUM_CHOLESKY when all attempts fail.
+int chol_shifted(const double* G, double* R, int n, int batch, double shift_rel0,
+                 double shift_rel_fail, int* info, Arena& ws, cudaStream_t st);
+// W = R^{-1} for upper-triangular R (batch, stride n*n).
+int trtri_upper(const double* R, double* W, int n, int batch, Arena& ws, cudaStream_t st);
+// One-sided Jacobi SVD of `batch` square n x n matrices A (ld n, stride n*n),
+// real (cplx=0) or complex interleaved (cplx=1, A holds n x 2n doubles).
+// Outputs: S (batch x n, descending), U (n x n, row-major, A = U diag(S) V^H),
+// VH (n x n rows = conj of right singular vectors, i.e. V^H).
+int jacobi_svd(const double* A, int n, int batch, int cplx, double* S, double* U, double* VH,
+               int* info, Arena& ws, cudaStream_t st);
+size_t dense_workspace(int n, int batch, int cplx);
+
+// complex <-> real-embedding helpers for n x n matrices (batched)
+//  complexify_gram: H = Zr^T Zr (2n x 2n) of the interleaved real view of a
+//  complex Z -> real_embed(Z^H Z)
+int complexify_gram(const double* H, double* G, int n, int batch, cudaStream_t st);
+//  real_embed(Mc) (column-vector form) -> real_embed(conj(Mc)) (row-vector
+//  form used as the right operand of a real GEMM on interleaved data)
+int embed_to_rowform(const double* E, double* F, int n, int batch, cudaStream_t st);
+//  complex n x n (interleaved) -> real_embed (2n x 2n)
+int complex_to_embed(const double* C, double* E, int n, int batch, cudaStream_t st);
+//  real_embed (2n x 2n) -> complex n x n interleaved
+int embed_to_complex(const double* E, double* C, int n, int batch, cudaStream_t st);
+
+// ---- misc kernels (misc.cu) ----
+template <typename TI, typename TO>
+int convert(const TI* in, TO* out, int64_t count, cudaStream_t st);
+template <typename TI, typename TO>
+int copy2d(const TI* in, int64_t ldi, TO* out, int64_t ldo, int64_t rows, int64_t cols,
+           cudaStream_t st);
+int fill_uniform_dispatch(int dtype, void* out, int64_t count, uint64_t seed, cudaStream_t st);
+int transpose_f64(const double* in, double* out, int64_t rows, int64_t cols, int batch,
+                  cudaStream_t st);
+
+}  // namespace plom

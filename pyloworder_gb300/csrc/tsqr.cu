@@ -1,0 +1,565 @@
+// Host-side orchestration of the tall-skinny QR and SVD (all kernels launched
+// on the caller's stream; nothing allocated, nothing synchronised).
+//
+// Algorithm (GB300 restatement of pyLOM's TSQR-SVD, pyLOM/vmmath/svd.py:
+// 50-118 and 228-252, pyLOM/vmmath/src/svd.c:565-712):
+//   The MPI butterfly that merges per-rank R factors becomes an in-GPU
+//   reduction over row tiles.  Each tile contributes its Gram block
+//   A_t^T A_t (the R-merge in Gram form: R_ab^T R_ab = R_a^T R_a + R_b^T R_b),
+//   the partial Grams are summed in FP64, and the n x n factor comes from a
+//   shifted Cholesky.  Three passes (shifted CholeskyQR3, Fukaya et al.,
+//   SIAM J. Sci. Comput. 42 (2020)) give a backward-stable Q with orthonormal
+//   columns:
+//       G1 = X^T X,   R1 = chol(G1 + s I),  Q1 = X R1^-1
+//       G2 = Q1^T Q1, R2 = chol(G2),        Q2 = Q1 R2^-1
+//       G3 = Q2^T Q2, R3 = chol(G3),        R = R3 R2 R1
+//   then svd(R) = Ur S V^T (FP64 one-sided Jacobi) and U = Q2 (R3^-1 Ur).
+//   The identity GEMM pyLOM runs on one rank (svd.py:117, svd.c:673) is not
+//   performed.
+//
+// Precision forms: PLOM_PREC_FP64 runs every product in FP64 (Q1, Q2 stored
+// in FP64); PLOM_PREC_MIXED stores Q1, Q2 in FP32 and runs the tall products
+// on the tensor cores (gemm_tc.cu; CUDA-core FP32 when the shape does not
+// fit the tensor-core kernels), keeping every n x n step in FP64.
+#include <algorithm>
+#include <cmath>
+#include <type_traits>
+
+#include "plom_common.cuh"
+#include "plom_kernels.cuh"
+#include "plom_tc.cuh"
+
+namespace plom {
+
+static const double U64 = 1.1102230246251565e-16;  // 2^-53
+static const double U32 = 5.9604644775390625e-08;  // 2^-24 (TF32x3 ~ FP32)
+
+// ---------------------------------------------------------------------------
+// tall operations, dispatched on precision
+// ---------------------------------------------------------------------------
+template <typename TA>
+static int tall_gram(int prec, const TA* A, int64_t lda, int64_t m, int64_t N, double* G,
+                     int* err, Arena& ws, cudaStream_t st) {
+  if (prec == PLOM_PREC_FP64)
+    return gemm_tn<TA, TA, double, double>(A, lda, A, lda, G, N, N, N, m, true, ws, st);
+  if constexpr (sizeof(TA) == 4) {
+    if (tc_gram_supported(m, N, lda)) return tc_gram_tf32x3(A, lda, m, N, G, err, ws, st);
+    return gemm_tn<TA, TA, float, double>(A, lda, A, lda, G, N, N, N, m, true, ws, st);
+  } else {
+    return gemm_tn<TA, TA, double, double>(A, lda, A, lda, G, N, N, N, m, true, ws, st);
+  }
+}
+
+// C(m x k) = A(m x N) W(N x k), W in FP64 (converted for the mixed form)
+template <typename TA, typename TO>
+static int tall_apply(int prec, const TA* A, int64_t lda, int64_t m, int64_t N, const double* W,
+                      int64_t k, TO* C, int64_t ldc, int* err, Arena& ws, cudaStream_t st) {
+  if (prec == PLOM_PREC_FP64 || sizeof(TA) == 8) {
+    if (ws.measuring()) return PLOM_OK;  // workspace query: launch nothing
+    return gemm_nn<TA, double, TO, double>(A, lda, W, k, C, ldc, m, k, N, st);
+  }
+  if constexpr (sizeof(TA) == 4 && sizeof(TO) == 4) {
+    if (tc_apply_supported(m, N, k, lda, ldc))
+      return tc_apply_tf32x3<double>(A, lda, m, N, W, k, k, C, ldc, err, ws, st);
+  }
+  float* Wf = ws.take<float>((size_t)N * k);
+  if (ws.measuring()) return PLOM_OK;
+  PLOM_REQUIRE(!ws.overflow(), PLOM_ERR_WORKSPACE, "tall_apply: workspace too small");
+  PLOM_TRY((convert<double, float>(W, Wf, N * k, st)));
+  return gemm_nn<TA, float, TO, float>(A, lda, Wf, k, C, ldc, m, k, N, st);
+}
+
+// Shifts are passed to the Cholesky relative to trace(G)/N; the absolute
+// shift is s = c u trace(G) (trace(G) = ||X||_F^2 >= ||X||_2^2).
+static void shifts_for(int prec, int64_t m, int64_t N, double& rel1, double& relfail) {
+  const double u = (prec == PLOM_PREC_FP64) ? U64 : U32;
+  const double n = (double)N;
+  // FP64: the sCholeskyQR3 bound 11 (mn + n(n+1)) u; mixed: a fixed 16 u,
+  // escalated on breakdown (the bound grows with m far past what the FP64
+  // partial-Gram summation needs).
+  const double c1 = (prec == PLOM_PREC_FP64) ? std::max(11.0 * ((double)m * n + n * (n + 1.0)), 4.0)
+                                             : 16.0;
+  rel1 = c1 * u * n;
+  relfail = 16.0 * u * n;
+}
+
+// ---------------------------------------------------------------------------
+// CholeskyQR3 core.  X: m x N real (complex data as its interleaved real view
+// with N = 2n).  Produces Q2 (m x N, TC), W3e = R3^-1, Re = R3 R2 R1 (N x N,
+// FP64; for complex data these are real embeddings of the complex factors).
+// ---------------------------------------------------------------------------
+template <typename TI, typename TC>
+struct CoreBufs {
+  TC* Q1;
+  TC* Q2;
+  double *G, *H, *R1, *R2, *R3, *W1, *W2, *W3, *Rp, *Re, *F;
+};
+
+template <typename TI, typename TC>
+static int chol_pass(int prec, bool cplx, int n, int64_t m, const TC* Q, int64_t ldq,
+                     const TI* Xin, int64_t ldx, bool first, CoreBufs<TI, TC>& b, double* R,
+                     double* W, double rel0, double relfail, int* info, Arena& ws,
+                     cudaStream_t st) {
+  const int N = cplx ? 2 * n : n;
+  double* Gtarget = cplx ? b.H : b.G;
+  const size_t mark = ws.off;
+  size_t need = mark;
+  if (first)
+    PLOM_TRY(tall_gram<TI>(prec, Xin, ldx, m, N, Gtarget, info, ws, st));
+  else
+    PLOM_TRY(tall_gram<TC>(prec, Q, ldq, m, N, Gtarget, info, ws, st));
+  need = std::max(need, ws.off);
+  ws.off = mark;
+  if (cplx && !ws.measuring()) PLOM_TRY(complexify_gram(b.H, b.G, n, 1, st));
+  PLOM_TRY(chol_shifted(b.G, R, N, 1, rel0, relfail, info, ws, st));
+  need = std::max(need, ws.off);
+  ws.off = mark;
+  PLOM_TRY(trtri_upper(R, W, N, 1, ws, st));
+  need = std::max(need, ws.off);
+  ws.off = need;
+  return PLOM_OK;
+}
+
+// right operand of a real GEMM on interleaved complex data: real_embed(conj(W))
+static const double* rowform(bool cplx, const double* We, double* F, int n, cudaStream_t st,
+                             int& status) {
+  status = PLOM_OK;
+  if (!cplx) return We;
+  status = embed_to_rowform(We, F, n, 1, st);
+  return F;
+}
+
+template <typename TI, typename TC>
+static int cholqr3(int prec, bool cplx, const TI* X, int64_t m, int n, int64_t ldx, TC* q1_store,
+                   int64_t ldq1, CoreBufs<TI, TC>& b, int* info, Arena& ws, cudaStream_t st) {
+  const int N = cplx ? 2 * n : n;
+  double rel1, relfail;
+  shifts_for(prec, m, N, rel1, relfail);
+  const size_t mark = ws.off;
+  size_t need = mark;
+  int s;
+  // pass 1
+  PLOM_TRY((chol_pass<TI, TC>(prec, cplx, n, m, nullptr, 0, X, ldx, true, b, b.R1, b.W1, rel1,
+                              relfail, info, ws, st)));
+  const double* F1 = ws.measuring() ? b.W1 : rowform(cplx, b.W1, b.F, n, st, s);
+  if (!ws.measuring()) PLOM_TRY(s);
+  need = std::max(need, ws.off);
+  ws.off = mark;
+  TC* Q1 = q1_store ? q1_store : b.Q1;
+  int64_t ld1 = q1_store ? ldq1 : N;
+  PLOM_TRY((tall_apply<TI, TC>(prec, X, ldx, m, N, F1, N, Q1, ld1, info, ws, st)));
+  need = std::max(need, ws.off);
+  ws.off = mark;
+  // pass 2
+  PLOM_TRY((chol_pass<TI, TC>(prec, cplx, n, m, Q1, ld1, nullptr, 0, false, b, b.R2, b.W2, 0.0,
+                              relfail, info, ws, st)));
+  need = std::max(need, ws.off);
+  ws.off = mark;
+  const double* F2 = ws.measuring() ? b.W2 : rowform(cplx, b.W2, b.F, n, st, s);
+  if (!ws.measuring()) PLOM_TRY(s);
+  PLOM_TRY((tall_apply<TC, TC>(prec, Q1, ld1, m, N, F2, N, b.Q2, N, info, ws, st)));
+  need = std::max(need, ws.off);
+  ws.off = mark;
+  // pass 3
+  PLOM_TRY((chol_pass<TI, TC>(prec, cplx, n, m, b.Q2, N, nullptr, 0, false, b, b.R3, b.W3, 0.0,
+                              relfail, info, ws, st)));
+  need = std::max(need, ws.off);
+  ws.off = need;
+  // Re = R3 R2 R1
+  if (!ws.measuring()) {
+    PLOM_TRY((gemm_nn<double, double, double, double>(b.R3, N, b.R2, N, b.Rp, N, N, N, N, st)));
+    PLOM_TRY((gemm_nn<double, double, double, double>(b.Rp, N, b.R1, N, b.Re, N, N, N, N, st)));
+  }
+  return PLOM_OK;
+}
+
+template <typename TI, typename TC>
+static void carve_core(Arena& ws, CoreBufs<TI, TC>& b, int64_t m, int N, bool need_q1) {
+  const size_t nn = (size_t)N * N;
+  b.G = ws.take<double>(nn);
+  b.H = ws.take<double>(nn);
+  b.R1 = ws.take<double>(nn);
+  b.R2 = ws.take<double>(nn);
+  b.R3 = ws.take<double>(nn);
+  b.W1 = ws.take<double>(nn);
+  b.W2 = ws.take<double>(nn);
+  b.W3 = ws.take<double>(nn);
+  b.Rp = ws.take<double>(nn);
+  b.Re = ws.take<double>(nn);
+  b.F = ws.take<double>(nn);
+  b.Q1 = need_q1 ? ws.take<TC>((size_t)m * N) : nullptr;
+  b.Q2 = ws.take<TC>((size_t)m * N);
+}
+
+// ---------------------------------------------------------------------------
+// tsqr_svd driver
+// ---------------------------------------------------------------------------
+template <typename TI, typename TC>
+static int tsqr_svd_impl(int prec, bool cplx, const TI* X, int64_t m, int n, int64_t ldx, TI* U,
+                         int64_t ldu, TI* S, TI* VT, int* info, Arena& ws, cudaStream_t st) {
+  const int N = cplx ? 2 * n : n;
+  // Q1 can live in U when U has the compute type and is densely packed
+  const bool q1_in_u = std::is_same<TI, TC>::value && ldu == N;
+  CoreBufs<TI, TC> b;
+  carve_core<TI, TC>(ws, b, m, N, !q1_in_u);
+  const int cw = cplx ? 2 : 1;
+  double* Rc = ws.take<double>((size_t)n * n * cw);
+  double* Ur = ws.take<double>((size_t)n * n * cw);
+  double* VH = ws.take<double>((size_t)n * n * cw);
+  double* S64 = ws.take<double>(n);
+  double* Me = ws.take<double>((size_t)N * N);
+  double* Ue = ws.take<double>((size_t)N * N);
+  if (!ws.measuring())
+    PLOM_REQUIRE(!ws.overflow(), PLOM_ERR_WORKSPACE, "tsqr_svd: workspace too small (%zu > %zu)",
+                 ws.off, ws.cap);
+  size_t scratch_mark = ws.off;
+  PLOM_TRY((cholqr3<TI, TC>(prec, cplx, X, m, n, ldx, q1_in_u ? (TC*)(void*)U : nullptr, N, b,
+                            info, ws, st)));
+  size_t need = ws.off;
+  ws.off = scratch_mark;
+  // small SVD of R (FP64)
+  const double* Rin = b.Re;
+  if (cplx && !ws.measuring()) {
+    PLOM_TRY(embed_to_complex(b.Re, Rc, n, 1, st));
+    Rin = Rc;
+  }
+  PLOM_TRY(jacobi_svd(Rin, n, 1, cplx ? 1 : 0, S64, Ur, VH, info, ws, st));
+  need = std::max(need, ws.off);
+  ws.off = scratch_mark;
+  if (!ws.measuring()) {
+    // M = R3^-1 Ur (embedded for complex), as the right operand of Q2 x M
+    const double* Mop;
+    if (cplx) {
+      PLOM_TRY(complex_to_embed(Ur, Ue, n, 1, st));
+      PLOM_TRY((gemm_nn<double, double, double, double>(b.W3, N, Ue, N, Me, N, N, N, N, st)));
+      PLOM_TRY(embed_to_rowform(Me, b.F, n, 1, st));
+      Mop = b.F;
+    } else {
+      PLOM_TRY((gemm_nn<double, double, double, double>(b.W3, N, Ur, N, Me, N, N, N, N, st)));
+      Mop = Me;
+    }
+    PLOM_TRY((tall_apply<TC, TI>(prec, b.Q2, N, m, N, Mop, N, U, ldu, info, ws, st)));
+    PLOM_TRY((convert<double, TI>(S64, S, n, st)));
+    PLOM_TRY((convert<double, TI>(VH, VT, (int64_t)n * n * cw, st)));
+  } else {
+    PLOM_TRY((tall_apply<TC, TI>(prec, b.Q2, N, m, N, b.F, N, U, ldu, info, ws, st)));
+  }
+  ws.off = std::max(need, ws.off);
+  return PLOM_OK;
+}
+
+template <typename TI, typename TC>
+static int tsqr_impl(int prec, const TI* X, int64_t m, int n, int64_t ldx, TI* Q, int64_t ldq,
+                     TI* R, int* info, Arena& ws, cudaStream_t st) {
+  CoreBufs<TI, TC> b;
+  const bool q1_in_q = std::is_same<TI, TC>::value && ldq == n;
+  carve_core<TI, TC>(ws, b, m, n, !q1_in_q);
+  if (!ws.measuring()) PLOM_REQUIRE(!ws.overflow(), PLOM_ERR_WORKSPACE, "tsqr: workspace too small");
+  PLOM_TRY((cholqr3<TI, TC>(prec, false, X, m, n, ldx, q1_in_q ? (TC*)(void*)Q : nullptr, n, b,
+                            info, ws, st)));
+  size_t need = ws.off;
+  PLOM_TRY((tall_apply<TC, TI>(prec, b.Q2, n, m, n, b.W3, n, Q, ldq, info, ws, st)));
+  if (!ws.measuring()) PLOM_TRY((convert<double, TI>(b.Re, R, (int64_t)n * n, st)));
+  ws.off = std::max(need, ws.off);
+  return PLOM_OK;
+}
+
+// ---------------------------------------------------------------------------
+// randomized SVD (pyLOM/vmmath/svd.py:121-144, 255-273; svd.c:1267-1519)
+// ---------------------------------------------------------------------------
+template <typename TI, typename TC>
+static int rsvd_impl(int prec, const TI* A, int64_t m, int64_t n, int64_t lda, int r, int q,
+                     uint64_t seed, TI* U, int64_t ldu, TI* S, TI* VT, int* info, Arena& ws,
+                     cudaStream_t st) {
+  TI* omega = ws.take<TI>((size_t)n * r);
+  TC* omc = ws.take<TC>((size_t)n * r);
+  TC* Y = ws.take<TC>((size_t)m * r);
+  TC* Qm = ws.take<TC>((size_t)m * r);
+  double* Rr = ws.take<double>((size_t)r * r);
+  TC* Q2 = ws.take<TC>((size_t)n * r);
+  double* B = ws.take<double>((size_t)r * n);
+  double* Bt = ws.take<double>((size_t)n * r);
+  double* Ub = ws.take<double>((size_t)n * r);
+  double* Sb = ws.take<double>(r);
+  double* VbH = ws.take<double>((size_t)r * r);
+  double* Ur = ws.take<double>((size_t)r * r);
+  double* Vo = ws.take<double>((size_t)r * n);
+  TC* Rq = ws.take<TC>((size_t)r * r);
+  size_t mark = ws.off;
+  size_t need = mark;
+  auto sub = [&](auto&& fn) -> int {
+    ws.off = mark;
+    int s = fn();
+    need = std::max(need, ws.off);
+    ws.off = mark;
+    return s;
+  };
+  const bool meas = ws.measuring();
+  if (!meas) {
+    PLOM_REQUIRE(!ws.overflow(), PLOM_ERR_WORKSPACE, "randomized_svd: workspace too small");
+    PLOM_TRY(fill_uniform_dispatch(sizeof(TI) == 8 ? PLOM_F64 : PLOM_F32, omega, n * r, seed, st));
+    PLOM_TRY((convert<TI, TC>(omega, omc, n * r, st)));
+  }
+  // Y = A Omega
+  auto apply_small = [&](const TC* Bm, TC* C) -> int {  // C(m x r) = A(m x n) Bm(n x r)
+    if (prec == PLOM_PREC_FP64 || sizeof(TC) == 8)
+      return gemm_nn<TI, TC, TC, double>(A, lda, Bm, r, C, r, m, r, n, st);
+    return gemm_nn<TI, TC, TC, float>(A, lda, Bm, r, C, r, m, r, n, st);
+  };
+  if (!meas) PLOM_TRY(apply_small(omc, Y));
+  for (int j = 0; j <= q; ++j) {
+    PLOM_TRY(sub([&]() { return tsqr_impl<TC, TC>(prec, Y, m, r, r, Qm, r, Rq, info, ws, st); }));
+    if (j == q) break;
+    // Q2 = A^T Q  (n x r), then Y = A Q2
+    PLOM_TRY(sub([&]() {
+      if (prec == PLOM_PREC_FP64 || sizeof(TC) == 8)
+        return gemm_tn<TI, TC, double, TC>(A, lda, Qm, r, Q2, r, n, r, m, false, ws, st);
+      return gemm_tn<TI, TC, float, TC>(A, lda, Qm, r, Q2, r, n, r, m, false, ws, st);
+    }));
+    if (!meas) PLOM_TRY(apply_small(Q2, Y));
+  }
+  // B = Q^T A  (r x n, FP64)
+  PLOM_TRY(sub([&]() {
+    if (prec == PLOM_PREC_FP64 || sizeof(TC) == 8)
+      return gemm_tn<TC, TI, double, double>(Qm, r, A, lda, B, n, r, n, m, false, ws, st);
+    return gemm_tn<TC, TI, float, double>(Qm, r, A, lda, B, n, r, n, m, false, ws, st);
+  }));
+  // svd(B) through the tall n x r matrix B^T: B^T = Ub Sb VbH -> B = Vb Sb Ub^T
+  if (!meas) PLOM_TRY(transpose_f64(B, Bt, r, n, 1, st));
+  PLOM_TRY(sub([&]() {
+    return tsqr_svd_impl<double, double>(PLOM_PREC_FP64, false, Bt, n, r, r, Ub, r, Sb, VbH,
+                                         info, ws, st);
+  }));
+  if (!meas) {
+    PLOM_TRY(transpose_f64(VbH, Ur, r, r, 1, st));  // Ur = Vb = VbH^T (real)
+    PLOM_TRY(transpose_f64(Ub, Vo, n, r, 1, st));   // V (r x n) = Ub^T
+    PLOM_TRY((convert<double, TI>(Sb, S, r, st)));
+    PLOM_TRY((convert<double, TI>(Vo, VT, (int64_t)r * n, st)));
+  }
+  // U = Q Ur
+  PLOM_TRY(sub([&]() { return tall_apply<TC, TI>(prec, Qm, r, m, r, Ur, r, U, ldu, info, ws, st); }));
+  ws.off = need;
+  return PLOM_OK;
+}
+
+}  // namespace plom
+
+using namespace plom;
+
+static bool prec_ok(int p) { return p == PLOM_PREC_FP64 || p == PLOM_PREC_MIXED; }
+
+// ---------------------------------------------------------------------------
+// C ABI
+// ---------------------------------------------------------------------------
+// Workspace queries run the driver with a null arena: nothing may launch.
+// A failing dry run (a launch attempted, an unsupported shape) reports 0.
+template <typename Fn>
+static int run_measured(size_t* bytes, Fn&& fn) {
+  Arena a(nullptr, 0);
+  int s = fn(a);
+  *bytes = (s == PLOM_OK) ? a.off + 1024 : 0;
+  return s;
+}
+
+static int tsqr_svd_dispatch(int dtype, int prec, const void* X, int64_t m, int64_t n, int64_t ldx,
+                             void* U, int64_t ldu, void* S, void* VT, int* info, Arena& ws,
+                             cudaStream_t st) {
+  const int ni = (int)n;
+  switch (dtype) {
+    case PLOM_F32:
+      if (prec == PLOM_PREC_FP64)
+        return tsqr_svd_impl<float, double>(prec, false, (const float*)X, m, ni, ldx, (float*)U,
+                                            ldu, (float*)S, (float*)VT, info, ws, st);
+      return tsqr_svd_impl<float, float>(prec, false, (const float*)X, m, ni, ldx, (float*)U, ldu,
+                                         (float*)S, (float*)VT, info, ws, st);
+    case PLOM_F64:
+      return tsqr_svd_impl<double, double>(PLOM_PREC_FP64, false, (const double*)X, m, ni, ldx,
+                                           (double*)U, ldu, (double*)S, (double*)VT, info, ws, st);
+    case PLOM_C64:
+      if (prec == PLOM_PREC_FP64)
+        return tsqr_svd_impl<float, double>(prec, true, (const float*)X, m, ni, 2 * ldx,
+                                            (float*)U, 2 * ldu, (float*)S, (float*)VT, info, ws,
+                                            st);
+      return tsqr_svd_impl<float, float>(prec, true, (const float*)X, m, ni, 2 * ldx, (float*)U,
+                                         2 * ldu, (float*)S, (float*)VT, info, ws, st);
+    case PLOM_C128:
+      return tsqr_svd_impl<double, double>(PLOM_PREC_FP64, true, (const double*)X, m, ni, 2 * ldx,
+                                           (double*)U, 2 * ldu, (double*)S, (double*)VT, info, ws,
+                                           st);
+  }
+  set_error("tsqr_svd: unknown dtype %d", dtype);
+  return PLOM_ERR_UNSUPPORTED;
+}
+
+extern "C" size_t plom_tsqr_svd_workspace(int dtype, int prec, int64_t m, int64_t n) {
+  size_t bytes = 0;
+  int dummy[PLOM_INFO_WORDS];
+  run_measured(&bytes, [&](Arena& a) {
+    return tsqr_svd_dispatch(dtype, prec, nullptr, m, n, n, nullptr, n, nullptr, nullptr, dummy, a,
+                             0);
+  });
+  return bytes;
+}
+
+extern "C" int plom_tsqr_svd(int dtype, int prec, const void* X, int64_t m, int64_t n,
+                             int64_t ldx, void* U, int64_t ldu, void* S, void* VT, void* ws,
+                             size_t ws_bytes, int* info, void* stream) {
+  PLOM_REQUIRE(prec_ok(prec), PLOM_ERR_ARG, "bad precision %d", prec);
+  PLOM_REQUIRE(m >= 1 && n >= 1 && n <= 4096, PLOM_ERR_ARG,
+               "tsqr_svd: need m >= 1 and 1 <= n <= 4096 (m=%lld n=%lld)", (long long)m,
+               (long long)n);
+  PLOM_REQUIRE(ldx >= n && ldu >= n, PLOM_ERR_ARG, "tsqr_svd: leading dimension < n");
+  PLOM_REQUIRE(X && U && S && VT && info && ws, PLOM_ERR_ARG, "tsqr_svd: null pointer");
+  size_t need = plom_tsqr_svd_workspace(dtype, prec, m, n);
+  PLOM_REQUIRE(ws_bytes >= need, PLOM_ERR_WORKSPACE, "tsqr_svd: workspace %zu < required %zu",
+               ws_bytes, need);
+  Arena a(ws, ws_bytes);
+  PLOM_CHECK_CUDA(cudaMemsetAsync(info, 0, sizeof(int) * PLOM_INFO_WORDS, (cudaStream_t)stream));
+  return tsqr_svd_dispatch(dtype, prec, X, m, n, ldx, U, ldu, S, VT, info, a, (cudaStream_t)stream);
+}
+
+static int tsqr_dispatch(int dtype, int prec, const void* X, int64_t m, int64_t n, int64_t ldx,
+                         void* Q, int64_t ldq, void* R, int* info, Arena& ws, cudaStream_t st) {
+  if (dtype == PLOM_F32) {
+    if (prec == PLOM_PREC_FP64)
+      return tsqr_impl<float, double>(prec, (const float*)X, m, (int)n, ldx, (float*)Q, ldq,
+                                      (float*)R, info, ws, st);
+    return tsqr_impl<float, float>(prec, (const float*)X, m, (int)n, ldx, (float*)Q, ldq,
+                                   (float*)R, info, ws, st);
+  }
+  if (dtype == PLOM_F64)
+    return tsqr_impl<double, double>(PLOM_PREC_FP64, (const double*)X, m, (int)n, ldx, (double*)Q,
+                                     ldq, (double*)R, info, ws, st);
+  set_error("tsqr: dtype must be F32 or F64");
+  return PLOM_ERR_UNSUPPORTED;
+}
+
+extern "C" size_t plom_tsqr_workspace(int dtype, int prec, int64_t m, int64_t n) {
+  size_t bytes = 0;
+  int dummy[PLOM_INFO_WORDS];
+  run_measured(&bytes, [&](Arena& a) {
+    return tsqr_dispatch(dtype, prec, nullptr, m, n, n, nullptr, n, nullptr, dummy, a, 0);
+  });
+  return bytes;
+}
+
+extern "C" int plom_tsqr(int dtype, int prec, const void* X, int64_t m, int64_t n, int64_t ldx,
+                         void* Q, int64_t ldq, void* R, void* ws, size_t ws_bytes, int* info,
+                         void* stream) {
+  PLOM_REQUIRE(prec_ok(prec), PLOM_ERR_ARG, "bad precision %d", prec);
+  PLOM_REQUIRE(m >= 1 && n >= 1 && n <= 4096, PLOM_ERR_ARG, "tsqr: bad sizes");
+  PLOM_REQUIRE(ldx >= n && ldq >= n, PLOM_ERR_ARG, "tsqr: leading dimension < n");
+  PLOM_REQUIRE(X && Q && R && info && ws, PLOM_ERR_ARG, "tsqr: null pointer");
+  size_t need = plom_tsqr_workspace(dtype, prec, m, n);
+  PLOM_REQUIRE(ws_bytes >= need, PLOM_ERR_WORKSPACE, "tsqr: workspace %zu < required %zu",
+               ws_bytes, need);
+  Arena a(ws, ws_bytes);
+  PLOM_CHECK_CUDA(cudaMemsetAsync(info, 0, sizeof(int) * PLOM_INFO_WORDS, (cudaStream_t)stream));
+  return tsqr_dispatch(dtype, prec, X, m, n, ldx, Q, ldq, R, info, a, (cudaStream_t)stream);
+}
+
+static int rsvd_dispatch(int dtype, int prec, const void* X, int64_t m, int64_t n, int64_t ldx,
+                         int64_t r, int q, uint64_t seed, void* U, int64_t ldu, void* S, void* VT,
+                         int* info, Arena& ws, cudaStream_t st) {
+  if (dtype == PLOM_F32) {
+    if (prec == PLOM_PREC_FP64)
+      return rsvd_impl<float, double>(prec, (const float*)X, m, n, ldx, (int)r, q, seed,
+                                      (float*)U, ldu, (float*)S, (float*)VT, info, ws, st);
+    return rsvd_impl<float, float>(prec, (const float*)X, m, n, ldx, (int)r, q, seed, (float*)U,
+                                   ldu, (float*)S, (float*)VT, info, ws, st);
+  }
+  if (dtype == PLOM_F64)
+    return rsvd_impl<double, double>(PLOM_PREC_FP64, (const double*)X, m, n, ldx, (int)r, q, seed,
+                                     (double*)U, ldu, (double*)S, (double*)VT, info, ws, st);
+  set_error("randomized_svd: dtype must be F32 or F64");
+  return PLOM_ERR_UNSUPPORTED;
+}
+
+extern "C" size_t plom_randomized_svd_workspace(int dtype, int prec, int64_t m, int64_t n,
+                                                int64_t r) {
+  size_t bytes = 0;
+  int dummy[PLOM_INFO_WORDS];
+  run_measured(&bytes, [&](Arena& a) {
+    return rsvd_dispatch(dtype, prec, nullptr, m, n, n, r, 1, 0, nullptr, r, nullptr, nullptr,
+                         dummy, a, 0);
+  });
+  return bytes;
+}
+
+extern "C" int plom_randomized_svd(int dtype, int prec, const void* X, int64_t m, int64_t n,
+                                   int64_t ldx, int64_t r, int q, uint64_t seed, void* U,
+                                   int64_t ldu, void* S, void* VT, void* ws, size_t ws_bytes,
+                                   int* info, void* stream) {
+  PLOM_REQUIRE(prec_ok(prec), PLOM_ERR_ARG, "bad precision %d", prec);
+  PLOM_REQUIRE(m >= 1 && n >= 1 && r >= 1 && r <= n && r <= m && r <= 4096 && q >= 0,
+               PLOM_ERR_ARG, "randomized_svd: need 1 <= r <= min(m, n, 4096), q >= 0");
+  PLOM_REQUIRE(ldx >= n && ldu >= r, PLOM_ERR_ARG, "randomized_svd: leading dimension too small");
+  PLOM_REQUIRE(X && U && S && VT && info && ws, PLOM_ERR_ARG, "randomized_svd: null pointer");
+  size_t need = plom_randomized_svd_workspace(dtype, prec, m, n, r);
+  PLOM_REQUIRE(ws_bytes >= need, PLOM_ERR_WORKSPACE, "randomized_svd: workspace %zu < %zu",
+               ws_bytes, need);
+  Arena a(ws, ws_bytes);
+  PLOM_CHECK_CUDA(cudaMemsetAsync(info, 0, sizeof(int) * PLOM_INFO_WORDS, (cudaStream_t)stream));
+  return rsvd_dispatch(dtype, prec, X, m, n, ldx, r, q, seed, U, ldu, S, VT, info, a,
+                       (cudaStream_t)stream);
+}
+
+// ---------------------------------------------------------------------------
+// matmul / matmulp
+// ---------------------------------------------------------------------------
+template <typename T>
+static int matmul_impl(int prec, int transA, const T* A, int64_t lda, const T* B, int64_t ldb,
+                       T* C, int64_t ldc, int64_t m, int64_t n, int64_t k, Arena& ws,
+                       cudaStream_t st) {
+  const bool fp64 = (prec == PLOM_PREC_FP64) || sizeof(T) == 8;
+  if (transA == 0) {
+    if constexpr (sizeof(T) == 4) {
+      if (!fp64 && tc_apply_supported(m, k, n, lda, ldc))
+        return tc_apply_tf32x3<float>(A, lda, m, k, B, ldb, n, C, ldc, nullptr, ws, st);
+    }
+    if (ws.measuring()) return PLOM_OK;
+    if (fp64) return gemm_nn<T, T, T, double>(A, lda, B, ldb, C, ldc, m, n, k, st);
+    return gemm_nn<T, T, T, float>(A, lda, B, ldb, C, ldc, m, n, k, st);
+  }
+  if (fp64) return gemm_tn<T, T, double, T>(A, lda, B, ldb, C, ldc, m, n, k, false, ws, st);
+  return gemm_tn<T, T, float, T>(A, lda, B, ldb, C, ldc, m, n, k, false, ws, st);
+}
+
+static int matmul_dispatch(int dtype, int prec, int transA, const void* A, int64_t lda,
+                           const void* B, int64_t ldb, void* C, int64_t ldc, int64_t m, int64_t n,
+                           int64_t k, Arena& ws, cudaStream_t st) {
+  if (dtype == PLOM_F32)
+    return matmul_impl<float>(prec, transA, (const float*)A, lda, (const float*)B, ldb, (float*)C,
+                              ldc, m, n, k, ws, st);
+  if (dtype == PLOM_F64)
+    return matmul_impl<double>(prec, transA, (const double*)A, lda, (const double*)B, ldb,
+                               (double*)C, ldc, m, n, k, ws, st);
+  set_error("matmul: dtype must be F32 or F64");
+  return PLOM_ERR_UNSUPPORTED;
+}
+
+extern "C" size_t plom_matmul_workspace(int dtype, int prec, int transA, int64_t m, int64_t n,
+                                        int64_t k) {
+  size_t bytes = 0;
+  run_measured(&bytes, [&](Arena& a) {
+    return matmul_dispatch(dtype, prec, transA, nullptr, m, nullptr, n, nullptr, n, m, n, k, a, 0);
+  });
+  return bytes;
+}
+
+extern "C" int plom_matmul(int dtype, int prec, int transA, const void* A, int64_t lda,
+                           const void* B, int64_t ldb, void* C, int64_t ldc, int64_t m, int64_t n,
+                           int64_t k, void* ws, size_t ws_bytes, void* stream) {
+  PLOM_REQUIRE(prec_ok(prec), PLOM_ERR_ARG, "bad precision %d", prec);
+  PLOM_REQUIRE(transA == 0 || transA == 1, PLOM_ERR_ARG, "transA must be 0 or 1");
+  PLOM_REQUIRE(m >= 0 && n >= 0 && k >= 0, PLOM_ERR_ARG, "negative size");
+  PLOM_REQUIRE(ldb >= n && ldc >= n && lda >= (transA ? m : k), PLOM_ERR_ARG,
+               "matmul: leading dimension too small");
+  PLOM_REQUIRE((A && B && C) || m * n == 0, PLOM_ERR_ARG, "matmul: null pointer");
+  size_t need = plom_matmul_workspace(dtype, prec, transA, m, n, k);
+  PLOM_REQUIRE(ws_bytes >= need, PLOM_ERR_WORKSPACE, "matmul: workspace %zu < %zu", ws_bytes,
+               need);
+  Arena a(ws, ws_bytes);
+  return matmul_dispatch(dtype, prec, transA, A, lda, B, ldb, C, ldc, m, n, k, a,
+                         (cudaStream_t)stream);
+}

@@ -1,0 +1,97 @@
+"""Seeded synthetic snapshot matrices for the benchmark configurations.
+
+No dataset is shipped with the reference for these workloads, so inputs are
+synthetic, seeded and described here:
+
+* POD field (configs 1 and 2): X[i, t] = sum_k a_k sin(kx_k x_i) sin(ky_k y_i)
+  cos(w_k t + th_k) + noise, on an nx x ny grid over [0, 2 pi]^2 (endpoints
+  included), dt = 1.  w_k ~ U[0.1, 2], th_k ~ U[0, 2 pi].  Config 1 uses 10
+  modes, a_k = 2^-k, (kx, ky) ~ U{1..8}, noise 1e-4.  Config 2 uses 64 modes
+  with a_k = k^-1.5 and 1e-5 noise; its (kx, ky) pairs are drawn WITHOUT
+  replacement from {1..16}^2 so that the 64 spatial modes are distinct (with
+  replacement from {1..8}^2 colliding pairs would merge modes and lower the
+  rank).
+* DMD field (config 3) and SPOD field (config 4): see dmd_field / spod_field.
+
+Host (numpy) generators serve the small parity cases; the device generators
+build the large matrices directly in HBM with torch in row chunks.
+"""
+from __future__ import annotations
+
+import math
+
+import numpy as np
+
+
+def _pod_params(nmodes, seed, distinct, kmax):
+    rng = np.random.default_rng(seed)
+    if distinct:
+        pairs = rng.choice(kmax * kmax, size=nmodes, replace=False)
+        kx, ky = pairs // kmax + 1, pairs % kmax + 1
+    else:
+        kx = np.empty(nmodes, dtype=np.int64)
+        ky = np.empty(nmodes, dtype=np.int64)
+    w = np.empty(nmodes)
+    th = np.empty(nmodes)
+    for k in range(nmodes):
+        if not distinct:
+            kx[k], ky[k] = rng.integers(1, 9, size=2)
+        w[k] = rng.uniform(0.1, 2.0)
+        th[k] = rng.uniform(0, 2 * np.pi)
+    return rng, kx, ky, w, th
+
+
+def pod_field_np(nx, ny, nt, nmodes, seed, noise=1e-4, amp_pow=None, dtype=np.float64,
+                 distinct=False, kmax=16):
+    """Config-1 style field on the host (float64 math, cast at the end)."""
+    rng, kx, ky, w, th = _pod_params(nmodes, seed, distinct, kmax)
+    x = np.linspace(0, 2 * np.pi, nx)
+    y = np.linspace(0, 2 * np.pi, ny)
+    XX, YY = np.meshgrid(x, y, indexing="ij")
+    xs, ys = XX.ravel(), YY.ravel()
+    t = np.arange(nt, dtype=np.float64)
+    amps = np.array([2.0 ** (-k) if amp_pow is None else k ** (-amp_pow) for k in range(1, nmodes + 1)])
+    Phi = np.sin(np.outer(xs, kx)) * np.sin(np.outer(ys, ky))          # m x K
+    T = amps[:, None] * np.cos(np.outer(w, t) + th[:, None])           # K x n
+    X = Phi @ T
+    X += noise * rng.standard_normal(X.shape)
+    return X.astype(dtype)
+
+
+def pod_field_device(nx, ny, nt, nmodes, seed, noise=1e-5, amp_pow=1.5, dtype="float32",
+                     distinct=True, kmax=16, chunk_rows=1 << 20):
+    """Config-2 style field generated in HBM (torch, row chunks)."""
+    import torch
+    tdt = getattr(torch, dtype) if isinstance(dtype, str) else dtype
+    rng, kx, ky, w, th = _pod_params(nmodes, seed, distinct, kmax)
+    m = nx * ny
+    amps = np.array([k ** (-amp_pow) for k in range(1, nmodes + 1)])
+    t = np.arange(nt, dtype=np.float64)
+    T = torch.tensor(amps[:, None] * np.cos(np.outer(w, t) + th[:, None]), device="cuda",
+                     dtype=torch.float64)
+    kxt = torch.tensor(kx, device="cuda", dtype=torch.float64)
+    kyt = torch.tensor(ky, device="cuda", dtype=torch.float64)
+    X = torch.empty((m, nt), dtype=tdt, device="cuda")
+    g = torch.Generator(device="cuda")
+    g.manual_seed(int(seed))
+    hx = 2 * math.pi / (nx - 1)
+    hy = 2 * math.pi / (ny - 1)
+    for r0 in range(0, m, chunk_rows):
+        r1 = min(m, r0 + chunk_rows)
+        idx = torch.arange(r0, r1, device="cuda", dtype=torch.int64)
+        xs = (idx // ny).to(torch.float64) * hx
+        ys = (idx % ny).to(torch.float64) * hy
+        Phi = torch.sin(xs[:, None] * kxt[None, :]) * torch.sin(ys[:, None] * kyt[None, :])
+        blk = Phi @ T
+        blk += noise * torch.randn(blk.shape, device="cuda", dtype=torch.float64, generator=g)
+        X[r0:r1].copy_(blk)
+        del Phi, blk
+    return X
+
+
+def grid_for_points(m):
+    """nx, ny with nx * ny = m and nx >= ny, as square as a power-of-two split allows."""
+    ny = 1 << (int(math.log2(m)) // 2) if m & (m - 1) == 0 else int(math.isqrt(m))
+    while m % ny:
+        ny -= 1
+    return m // ny, ny

@@ -1,0 +1,348 @@
+"""pyLOM.math (pyLOM/vmmath) hot-path functions on GB300.
+
+Same names, argument meanings, defaults and return tuples as pyLOM 3.2.8's
+``pyLOM.math``; inputs may be numpy arrays or torch tensors and results come
+back as the same kind (numpy in -> numpy out, CUDA tensor in -> CUDA tensor
+out).  One extra keyword-only argument, ``precision``:
+
+* ``'fp64'``  -- every product and reduction in FP64 on the GPU (default for
+  float64 / complex128 input);
+* ``'mixed'`` -- tall-skinny products on the tensor cores (TF32 split into
+  three terms, FP32 accumulation), n x n factorizations in FP64 (default for
+  float32 / complex64 input, whose reference path runs in single precision).
+"""
+from __future__ import annotations
+
+import time
+
+import numpy as np
+
+from . import _lib as L
+
+__all__ = [
+    "temporal_mean", "subtract_mean", "temporal_variance", "norm_variance",
+    "matmul", "matmulp", "vecmat", "transpose", "tsqr", "tsqr_svd", "randomized_svd",
+    "randomized_qr", "compute_truncation_residual", "energy", "hammwin", "RMSE",
+]
+
+
+# --------------------------------------------------------------------------
+# averaging: pyLOM/vmmath/averaging.py:18-75, src/averaging.c:10-157
+# --------------------------------------------------------------------------
+
+def _rows_in(X):
+    cv = L.to_device(X)
+    x, ld = L.as_rows(cv.t)
+    if x.dim() != 2:
+        raise ValueError("expected a 2-D snapshot matrix (points x snapshots)")
+    if x.dtype not in (L.torch().float32, L.torch().float64):
+        raise TypeError("averaging takes float32 or float64 data")
+    return cv, x, ld
+
+
+def temporal_mean(X):
+    """Mean over snapshots of each point (pyLOM/vmmath/averaging.py:18)."""
+    cv, x, ld = _rows_in(X)
+    t = L.torch()
+    m, n = x.shape
+    out = t.empty(m, dtype=x.dtype, device="cuda")
+    L.call("plom_temporal_mean", L.dtype_code(x), L.ptr(x), m, n, ld, L.ptr(out), L.stream_ptr())
+    return cv.back(out)
+
+
+def subtract_mean(X, X_mean):
+    """X - mean over columns (pyLOM/vmmath/averaging.py:32)."""
+    cv, x, ld = _rows_in(X)
+    t = L.torch()
+    m, n = x.shape
+    mean = L.to_device(X_mean, x.dtype).t.contiguous().reshape(-1)
+    Y = t.empty((m, n), dtype=x.dtype, device="cuda")
+    L.call("plom_subtract_mean", L.dtype_code(x), L.ptr(x), m, n, ld, L.ptr(mean), L.ptr(Y), n,
+           L.stream_ptr())
+    return cv.back(Y)
+
+
+def temporal_variance(X, X_mean):
+    """Population variance over snapshots, shape (m, 1) (averaging.py:47)."""
+    cv, x, ld = _rows_in(X)
+    t = L.torch()
+    m, n = x.shape
+    mean = L.to_device(X_mean, x.dtype).t.contiguous().reshape(-1)
+    var = t.empty((m, 1), dtype=x.dtype, device="cuda")
+    L.call("plom_temporal_variance", L.dtype_code(x), L.ptr(x), m, n, ld, L.ptr(mean), L.ptr(var),
+           L.stream_ptr())
+    return cv.back(var)
+
+
+def norm_variance(X, X_mean, X_var):
+    """(X - mean) / variance (pyLOM/vmmath/averaging.py:62)."""
+    cv, x, ld = _rows_in(X)
+    t = L.torch()
+    m, n = x.shape
+    mean = L.to_device(X_mean, x.dtype).t.contiguous().reshape(-1)
+    var = L.to_device(X_var, x.dtype).t.contiguous().reshape(-1)
+    Y = t.empty((m, n), dtype=x.dtype, device="cuda")
+    L.call("plom_norm_variance", L.dtype_code(x), L.ptr(x), m, n, ld, L.ptr(mean), L.ptr(var),
+           L.ptr(Y), n, L.stream_ptr())
+    return cv.back(Y)
+
+
+def remove_mean_device(x, ld, divide_variance=False):
+    """Fused mean (+variance) and subtraction on a CUDA tensor: returns
+    (Y, mean, var-or-None), all on the device."""
+    t = L.torch()
+    m, n = x.shape
+    Y = t.empty((m, n), dtype=x.dtype, device="cuda")
+    mean = t.empty(m, dtype=x.dtype, device="cuda")
+    var = t.empty(m, dtype=x.dtype, device="cuda") if divide_variance else None
+    L.call("plom_remove_mean", L.dtype_code(x), L.ptr(x), m, n, ld, L.ptr(mean), L.ptr(var),
+           1 if divide_variance else 0, L.ptr(Y), n, L.stream_ptr())
+    return Y, mean, var
+
+
+# --------------------------------------------------------------------------
+# products: pyLOM/vmmath/maths.py:77-130, src/vector_matrix.c:158-356
+# --------------------------------------------------------------------------
+
+def _operand(A):
+    """-> (Converted, base tensor, ld, transposed?) for a 2-D operand that is
+    row-major or the transpose of a row-major matrix."""
+    t = L.torch()
+    if isinstance(A, t.Tensor):
+        x = A if A.device.type == "cuda" else A.to("cuda")
+        cv = L.Converted(x, "torch", A.device)
+        if x.dim() == 2 and x.shape[0] > 1 and x.shape[1] > 1 and x.stride(0) == 1 \
+                and x.stride(1) >= x.shape[0]:
+            return cv, x.t(), x.stride(1), True
+        xx, ld = L.as_rows(x)
+        return cv, xx, ld, False
+    arr = np.asarray(A)
+    if arr.ndim == 2 and not arr.flags.c_contiguous and arr.flags.f_contiguous and arr.shape[0] > 1:
+        base = L.torch().from_numpy(np.ascontiguousarray(arr.T)).to("cuda")
+        return L.Converted(base, "numpy", None), base, base.shape[1], True
+    cv = L.to_device(arr)
+    xx, ld = L.as_rows(cv.t)
+    return cv, xx, ld, False
+
+
+def _matmul_dev(a, lda, transA, b, ldb, m, n, k, precision=None, out=None, ldc=None):
+    t = L.torch()
+    prec = L.precision_code(precision, a)
+    dt = L.dtype_code(a)
+    C = out if out is not None else t.empty((m, n), dtype=a.dtype, device="cuda")
+    ldc = ldc if ldc is not None else n
+    nbytes = L.load().plom_matmul_workspace(dt, prec, transA, m, n, k)
+    ws = L.workspace(nbytes)
+    L.call("plom_matmul", dt, prec, transA, L.ptr(a), lda, L.ptr(b), ldb, L.ptr(C), ldc, m, n, k,
+           L.ptr(ws), ws.numel(), L.stream_ptr())
+    return C
+
+
+def matmul(A, B, *, precision=None):
+    """C = A @ B (pyLOM/vmmath/maths.py:77).  A may be the transpose of a
+    row-major matrix (the ``A.T`` operands of pyLOM's matmulp calls); that
+    form runs as a split-K reduction over A's long axis."""
+    cva, a, lda, ta = _operand(A)
+    cvb, b, ldb, tb = _operand(B)
+    if tb:
+        b = b.t().contiguous()
+        ldb = b.shape[1]
+    if b.dtype != a.dtype:
+        b = b.to(a.dtype)
+    m = a.shape[1] if ta else a.shape[0]
+    k = a.shape[0] if ta else a.shape[1]
+    if b.shape[0] != k:
+        raise ValueError(f"matmul: shapes {tuple(A.shape)} and {tuple(B.shape)} do not align")
+    n = b.shape[1]
+    C = _matmul_dev(a, lda, 1 if ta else 0, b, ldb, m, n, k, precision)
+    return cva.back(C)
+
+
+def matmulp(A, B, *, precision=None):
+    """Sum over ranks of A_i @ B_i; on one GPU the local product
+    (pyLOM/vmmath/maths.py:93)."""
+    return matmul(A, B, precision=precision)
+
+
+def vecmat(v, A):
+    """C[i,:] = v[i] * A[i,:] (pyLOM/vmmath/maths.py:113)."""
+    t = L.torch()
+    if isinstance(A, t.Tensor):
+        vv = v if isinstance(v, t.Tensor) else t.as_tensor(np.asarray(v), device=A.device)
+        return vv.to(A.dtype).reshape(-1, 1) * A
+    return np.asarray(v).reshape(-1, 1) * np.asarray(A)
+
+
+def transpose(A):
+    """pyLOM/vmmath/maths.py:18."""
+    return A.T
+
+
+# --------------------------------------------------------------------------
+# SVD family: pyLOM/vmmath/svd.py, src/svd.c
+# --------------------------------------------------------------------------
+
+def tsqr_svd_device(x, ld, precision=None):
+    """TSQR-SVD of a CUDA tensor -> (U, S, V) CUDA tensors (V = V^T, n x n)."""
+    t = L.torch()
+    m, n = x.shape
+    if m < n:
+        # wide input: svd of the (tall) transpose, as LAPACK's gesdd would see it
+        # x^T = Ut St Vt  ->  x = Vt^T St Ut^T (plain transposes, also for complex)
+        Ut, St, Vt = tsqr_svd_device(x.transpose(0, 1).contiguous(), m, precision)
+        return Vt.transpose(0, 1).contiguous(), St, Ut.transpose(0, 1).contiguous()
+    dt = L.dtype_code(x)
+    prec = L.precision_code(precision, x)
+    U = t.empty((m, n), dtype=x.dtype, device="cuda")
+    S = t.empty(n, dtype=L.real_dtype(x), device="cuda")
+    V = t.empty((n, n), dtype=x.dtype, device="cuda")
+    ws = L.workspace(L.load().plom_tsqr_svd_workspace(dt, prec, m, n))
+    info = L.new_info()
+    L.call("plom_tsqr_svd", dt, prec, L.ptr(x), m, n, ld, L.ptr(U), n, L.ptr(S), L.ptr(V),
+           L.ptr(ws), ws.numel(), L.ptr(info), L.stream_ptr())
+    L.check_info(info, "tsqr_svd")
+    return U, S, V
+
+
+def tsqr_svd(Ai, *, precision=None):
+    """U, S, V = tsqr_svd(A): A (m x n) = U diag(S) V with U m x n, S n
+    descending, V n x n holding V^T (pyLOM/vmmath/svd.py:228)."""
+    cv = L.to_device(Ai)
+    x, ld = L.as_rows(cv.t)
+    U, S, V = tsqr_svd_device(x, ld, precision)
+    return cv.back(U), cv.back(S), cv.back(V)
+
+
+def svd(A, method="gesdd", *, precision=None):
+    """Thin SVD (pyLOM/vmmath/svd.py:39); computed with the TSQR-SVD."""
+    return tsqr_svd(A, precision=precision)
+
+
+def tsqr(Ai, *, precision=None):
+    """Q, R = tsqr(A): Q m x n orthonormal columns, R n x n upper triangular
+    (pyLOM/vmmath/svd.py:50)."""
+    t = L.torch()
+    cv = L.to_device(Ai)
+    x, ld = L.as_rows(cv.t)
+    m, n = x.shape
+    if x.dtype not in (t.float32, t.float64):
+        raise TypeError("tsqr takes float32 or float64 data")
+    dt = L.dtype_code(x)
+    prec = L.precision_code(precision, x)
+    Q = t.empty((m, n), dtype=x.dtype, device="cuda")
+    R = t.empty((n, n), dtype=x.dtype, device="cuda")
+    ws = L.workspace(L.load().plom_tsqr_workspace(dt, prec, m, n))
+    info = L.new_info()
+    L.call("plom_tsqr", dt, prec, L.ptr(x), m, n, ld, L.ptr(Q), n, L.ptr(R), L.ptr(ws), ws.numel(),
+           L.ptr(info), L.stream_ptr())
+    L.check_info(info, "tsqr")
+    return cv.back(Q), cv.back(R)
+
+
+def qr(A, *, precision=None):
+    """pyLOM/vmmath/svd.py:29."""
+    return tsqr(A, precision=precision)
+
+
+def randomized_svd_device(x, ld, r, q, seed, precision=None):
+    t = L.torch()
+    m, n = x.shape
+    dt = L.dtype_code(x)
+    prec = L.precision_code(precision, x)
+    U = t.empty((m, r), dtype=x.dtype, device="cuda")
+    S = t.empty(r, dtype=x.dtype, device="cuda")
+    V = t.empty((r, n), dtype=x.dtype, device="cuda")
+    ws = L.workspace(L.load().plom_randomized_svd_workspace(dt, prec, m, n, r))
+    info = L.new_info()
+    L.call("plom_randomized_svd", dt, prec, L.ptr(x), m, n, ld, r, q, seed, L.ptr(U), r, L.ptr(S),
+           L.ptr(V), L.ptr(ws), ws.numel(), L.ptr(info), L.stream_ptr())
+    L.check_info(info, "randomized_svd")
+    return U, S, V
+
+
+def randomized_svd(Ai, r, q, seed=-1, *, precision=None):
+    """Randomized SVD with q power iterations (pyLOM/vmmath/svd.py:255).
+    Returns U m x r, S r, V r x n.  The uniform [0,1) test matrix comes from
+    a Philox counter stream keyed by ``seed`` (time-seeded when seed < 0, as
+    in pyLOM)."""
+    seed = int(time.time()) if seed < 0 else int(seed)
+    cv = L.to_device(Ai)
+    x, ld = L.as_rows(cv.t)
+    if x.dtype not in (L.torch().float32, L.torch().float64):
+        raise TypeError("randomized_svd takes float32 or float64 data")
+    U, S, V = randomized_svd_device(x, ld, int(r), int(q), seed, precision)
+    return cv.back(U), cv.back(S), cv.back(V)
+
+
+def randomized_qr(Ai, r, q, seed=-1, *, precision=None):
+    """Q (m x r), B = Q^T A (r x n) of the randomized range finder
+    (pyLOM/vmmath/svd.py:121), from the same device pipeline."""
+    U, S, V = randomized_svd(Ai, r, q, seed, precision=precision)
+    t = L.torch()
+    if isinstance(U, t.Tensor):
+        return U, S.reshape(-1, 1) * V
+    return U, S.reshape(-1, 1) * V
+
+
+# --------------------------------------------------------------------------
+# host-side helpers on small vectors
+# --------------------------------------------------------------------------
+
+def _host(v):
+    t = L.torch()
+    if isinstance(v, t.Tensor):
+        return v.detach().cpu().numpy()
+    return np.asarray(v)
+
+
+def compute_truncation_residual(S, r):
+    """Number of modes for a residual r > 0 or an energy fraction r < 0
+    (pyLOM/vmmath/truncation.py:17; the float64 C version returns ii+1 in the
+    energy branch, truncation.c:69, as the py path does)."""
+    S = _host(S).astype(np.float64)
+    N = 0
+    if r > 0:
+        # suffix norms ||S[ii:]|| / ||S|| computed once
+        tail = np.sqrt(np.cumsum((S * S)[::-1])[::-1])
+        normS = tail[0] if tail.size else 0.0
+        for ii in range(S.shape[0]):
+            if tail[ii] / normS < r:
+                break
+            N += 1
+    else:
+        r = abs(r)
+        normS = np.sum(S)
+        acc = 0.0
+        for ii in range(S.shape[0]):
+            acc += S[ii] / normS
+            N += 1
+            if acc > r:
+                break
+    return N
+
+
+def energy(original, rec):
+    """1 - ||orig - rec||^2 / ||orig||^2 (pyLOM/vmmath/truncation.py:42)."""
+    t = L.torch()
+    if isinstance(original, t.Tensor):
+        return float(1.0 - ((original - rec) ** 2).sum() / (original ** 2).sum())
+    o, r_ = np.asarray(original), np.asarray(rec)
+    return float(1.0 - np.sum((o - r_) ** 2) / np.sum(o ** 2))
+
+
+def RMSE(A, B, relative=True):
+    """pyLOM/vmmath/stats.py:17."""
+    t = L.torch()
+    if isinstance(A, t.Tensor):
+        d = A - B
+        den = (A * A).sum() if relative else float(np.prod(A.shape))
+        return float(t.sqrt((d * d).sum() / den))
+    A, B = np.asarray(A), np.asarray(B)
+    d = A - B
+    den = np.sum(A * A) if relative else np.prod(A.shape)
+    return float(np.sqrt(np.sum(d * d) / den))
+
+
+def hammwin(N):
+    """Hamming window 0.54 - 0.46 cos(2 pi i / (N-1)) (pyLOM/vmmath/fft.py:17)."""
+    return 0.54 - 0.46 * np.cos(2 * np.pi * np.arange(N) / (N - 1))

@@ -1,0 +1,80 @@
+"""The C ABI boundary without a GPU: the library builds/loads, exports every
+symbol include/plom.h declares, answers workspace queries and rejects bad
+arguments with an error status (no kernel is launched)."""
+import ctypes
+import os
+import re
+
+import pytest
+
+from pyloworder_gb300 import _lib as L
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_symbols():
+    names = set()
+    for fn in os.listdir(os.path.join(ROOT, "include")):
+        if fn.endswith(".h"):
+            src = open(os.path.join(ROOT, "include", fn)).read()
+            names |= set(re.findall(r"\b(plom_\w+)\s*\(", src))
+    return sorted(names)
+
+
+def test_exports_every_declared_symbol():
+    lib = L.load()
+    names = declared_symbols()
+    assert len(names) >= 10
+    missing = [n for n in names if not hasattr(lib, n)]
+    assert not missing, missing
+
+
+def test_python_prototypes_match_header():
+    assert set(L.PROTOS) == set(declared_symbols())
+
+
+def test_workspace_queries():
+    lib = L.load()
+    m, n = 8388608, 1024
+    mixed = lib.plom_tsqr_svd_workspace(L.F32, L.PREC_MIXED, m, n)
+    fp64 = lib.plom_tsqr_svd_workspace(L.F32, L.PREC_FP64, m, n)
+    # mixed: one FP32 m x n buffer (Q1 lives in U); FP64: two FP64 buffers
+    assert 4 * m * n <= mixed < 4 * m * n + (1 << 30)
+    assert 16 * m * n <= fp64 < 16 * m * n + (1 << 30)
+    assert lib.plom_randomized_svd_workspace(L.F32, L.PREC_MIXED, m, n, 80) < 8 * m * 80 * 3 + (1 << 30)
+    assert lib.plom_matmul_workspace(L.F64, L.PREC_FP64, 1, 1024, 80, m) > 0
+
+
+@pytest.mark.parametrize("args", [
+    dict(prec=7), dict(m=0), dict(n=0), dict(ldx=3), dict(ws_bytes=16),
+])
+def test_bad_arguments_rejected(args):
+    lib = L.load()
+    p = dict(dtype=L.F64, prec=L.PREC_FP64, m=100, n=8, ldx=8, ws_bytes=1 << 30)
+    p.update(args)
+    dummy = ctypes.c_void_p(16)
+    st = lib.plom_tsqr_svd(p["dtype"], p["prec"], dummy, p["m"], p["n"], p["ldx"], dummy, 8, dummy,
+                           dummy, dummy, p["ws_bytes"], dummy, None)
+    assert st < 0
+    assert lib.plom_last_error_string()
+
+
+def test_matmul_rejects_bad_transA():
+    lib = L.load()
+    d = ctypes.c_void_p(16)
+    assert lib.plom_matmul(L.F32, 1, 5, d, 4, d, 4, d, 4, 4, 4, 4, d, 0, None) == L.PLOM_ERR_ARG if hasattr(L, "PLOM_ERR_ARG") else -1
+
+
+@pytest.mark.parametrize("dtype", [0, 1, 2, 3])
+@pytest.mark.parametrize("prec", [0, 1])
+def test_workspace_dry_runs_launch_nothing(dtype, prec):
+    # A query walks the whole driver with a null arena; any kernel launch in
+    # that walk fails here (no GPU) and the query reports 0.
+    lib = L.load()
+    for m, n in [(16384, 200), (8388608, 1024), (5, 1), (1000, 33), (300, 64)]:
+        assert lib.plom_tsqr_svd_workspace(dtype, prec, m, n) > 0, lib.plom_last_error_string()
+    if dtype in (0, 1):
+        assert lib.plom_tsqr_workspace(dtype, prec, 4000, 50) > 0
+        assert lib.plom_randomized_svd_workspace(dtype, prec, 3000, 120, 16) > 0
+        for tA in (0, 1):
+            assert lib.plom_matmul_workspace(dtype, prec, tA, 100, 20, 30) > 0

@@ -1,0 +1,221 @@
+"""GPU parity of the SVD path (averaging, matmul, tsqr, tsqr_svd,
+randomized_svd, POD) against the oracle and the golden fixtures produced by
+pyLOM itself.
+
+Tolerances: FP64 form 1e-10 relative on sigma (signal modes) and 1e-12
+normwise (|dS|/S_1); mixed form 1e-5 relative on sigma for modes above
+1e-3 S_1 and 1e-4 rad subspace angle.  Modes are compared up to sign/phase.
+"""
+import numpy as np
+import pytest
+
+from oracle import plom_oracle as O
+from tests.helpers import cols_up_to_phase, orthogonality, sigma_normwise, sigma_rel, subspace_angle
+
+pytestmark = pytest.mark.gpu
+
+torch = pytest.importorskip("torch")
+if not torch.cuda.is_available():  # collected on CPU hosts, run on the GPU machine
+    pytest.skip("needs a CUDA GPU", allow_module_level=True)
+
+import pyloworder_gb300 as P  # noqa: E402
+
+
+def test_averaging_golden(golden):
+    g = golden("averaging")
+    m = P.math.temporal_mean(g["X"])
+    np.testing.assert_allclose(m, g["mean"], rtol=1e-14, atol=1e-15)
+    np.testing.assert_allclose(P.math.subtract_mean(g["X"], m), g["Y"], rtol=1e-13, atol=1e-14)
+    v = P.math.temporal_variance(g["X"], m)
+    np.testing.assert_allclose(v, g["var"], rtol=1e-12)
+    np.testing.assert_allclose(P.math.norm_variance(g["X"], m, v), g["Yv"], rtol=1e-11)
+
+
+@pytest.mark.parametrize("m,n", [(1000, 37), (4096, 256), (3, 1), (777, 1000)])
+def test_averaging_f32_shapes(m, n):
+    X = np.random.default_rng(m + n).standard_normal((m, n)).astype(np.float32) + 3.0
+    mean = P.math.temporal_mean(X)
+    ref = X.astype(np.float64).mean(axis=1)
+    np.testing.assert_allclose(mean, ref, rtol=1e-6, atol=1e-6)
+    Y = P.math.subtract_mean(X, mean)
+    np.testing.assert_allclose(Y, X - mean[:, None], rtol=1e-6, atol=1e-6)
+
+
+def test_kat_example_svd(golden):
+    g = golden("kat_example_svd")
+    U, S, V = P.math.tsqr_svd(g["A"])
+    np.testing.assert_allclose(S, g["S"], rtol=1e-13)
+    cols_up_to_phase(U, g["U"], 1e-12)
+    cols_up_to_phase(V.T, g["V"].T, 1e-12)
+
+
+def test_tsqr_svd_f64_golden(golden):
+    g = golden("tsqr_svd_f64")
+    U, S, V = P.math.tsqr_svd(g["A"])
+    assert sigma_rel(S, g["S"]) < 1e-12
+    cols_up_to_phase(U, g["U"], 1e-10)
+    cols_up_to_phase(V.T, g["V"].T, 1e-10)
+    assert orthogonality(U) < 1e-13
+
+
+@pytest.mark.parametrize("precision", ["mixed", "fp64"])
+def test_tsqr_svd_f32_golden(golden, precision):
+    g = golden("tsqr_svd_f32")
+    U, S, V = P.math.tsqr_svd(g["A"], precision=precision)
+    assert U.dtype == np.float32 and S.dtype == np.float32
+    ref = O.tsqr_svd(g["A"].astype(np.float64))
+    assert sigma_rel(S, ref[1]) < 1e-5
+    assert sigma_rel(S, g["S"]) < 2e-5
+    cols_up_to_phase(U, ref[0], 1e-3)
+    assert orthogonality(U) < 1e-5
+
+
+def test_pod_cfg1_small_golden(golden):
+    g = golden("pod_cfg1_small")
+    U, S, V = P.POD.run(g["X"])
+    k = 10
+    assert sigma_rel(S, g["S"], k) < 1e-10
+    assert sigma_normwise(S, g["S"]) < 1e-12
+    cols_up_to_phase(U[:, :k], g["U"][:, :k], 1e-9)
+    Ut, St, Vt = P.POD.truncate(U, S, V, r=1e-6)
+    assert Ut.shape[1] == int(g["N_res"])
+    assert P.POD.truncate(U, S, V, r=-0.99)[0].shape[1] == int(g["N_energy"])
+    Xr = P.POD.reconstruct(Ut, St, Vt)
+    np.testing.assert_allclose(Xr, g["Xr"], atol=1e-11)
+
+
+def test_pod_divvar_golden(golden):
+    g = golden("pod_divvar")
+    U, S, V = P.POD.run(g["X"], remove_mean=True, divide_variance=True)
+    assert sigma_rel(S, g["S"], 10) < 1e-10
+    assert sigma_normwise(S, g["S"]) < 1e-12
+
+
+def test_pod_f32_nomean_golden(golden):
+    g = golden("pod_f32_nomean")
+    U, S, V = P.POD.run(g["X"], remove_mean=False)
+    ref = O.pod_run(g["X"].astype(np.float64), remove_mean=False)
+    assert S.dtype == np.float32
+    assert sigma_rel(S, ref[1], 10) < 1e-5
+    assert subspace_angle(U[:, :10], ref[0][:, :10]) < 1e-4
+
+
+def test_randomized_philox_matches_oracle():
+    rng = np.random.default_rng(5)
+    X = (rng.standard_normal((3000, 12)) @ rng.standard_normal((12, 120))
+         + 1e-3 * rng.standard_normal((3000, 120)))
+    r, q, seed = 16, 3, 1234
+    U, S, V = P.math.randomized_svd(X, r, q, seed=seed)
+    assert U.shape == (3000, r) and S.shape == (r,) and V.shape == (r, 120)
+    omega = O.philox_uniform((120, r), seed, np.float64)
+    Ur, Sr, Vr = O.randomized_svd(X, r, q, omega=omega)
+    assert sigma_rel(S, Sr, 12) < 1e-10
+    cols_up_to_phase(U[:, :12], Ur[:, :12], 1e-8)
+    cols_up_to_phase(V[:12].T, Vr[:12].T, 1e-8)
+
+
+def test_randomized_reference_omega_subspace(golden):
+    # pyLOM draws Omega with numpy's MT19937; ours is Philox.  Both capture the
+    # same dominant subspace: compare sigma and subspaces, not raw vectors.
+    g = golden("pod_randomized")
+    U, S, V = P.POD.run(g["X"], remove_mean=False, randomized=True, r=int(g["r"]), q=int(g["q"]),
+                        seed=int(g["seed"]))
+    # signal modes only: below 1e-2 S_1 the field is noise, whose captured
+    # directions depend on the test matrix itself
+    k = int(np.sum(g["S"] > 1e-2 * g["S"][0]))
+    assert k >= 6
+    assert sigma_rel(S, g["S"], k) < 1e-8
+    assert subspace_angle(U[:, :k], g["U"][:, :k]) < 1e-6
+
+
+@pytest.mark.parametrize("dtype", [np.float64, np.float32])
+def test_matmul_and_matmulp(dtype):
+    rng = np.random.default_rng(2)
+    A = rng.standard_normal((5000, 96)).astype(dtype)
+    B = rng.standard_normal((96, 40)).astype(dtype)
+    Q = rng.standard_normal((5000, 40)).astype(dtype)
+    tol = 1e-12 if dtype == np.float64 else 2e-5
+    ref = A.astype(np.float64) @ B.astype(np.float64)
+    np.testing.assert_allclose(P.math.matmul(A, B), ref, rtol=tol, atol=tol * np.abs(ref).max())
+    ref2 = A.T.astype(np.float64) @ Q.astype(np.float64)
+    got = P.math.matmulp(A.T, Q)
+    assert got.shape == (96, 40)
+    np.testing.assert_allclose(got, ref2, rtol=tol, atol=tol * np.abs(ref2).max())
+
+
+def test_matmul_torch_transposed_view():
+    rng = np.random.default_rng(3)
+    A = torch.tensor(rng.standard_normal((3000, 64)), device="cuda")
+    Q = torch.tensor(rng.standard_normal((3000, 8)), device="cuda")
+    got = P.math.matmul(A.T, Q)
+    assert isinstance(got, torch.Tensor) and got.is_cuda
+    ref = A.T.cpu().numpy() @ Q.cpu().numpy()
+    np.testing.assert_allclose(got.cpu().numpy(), ref, rtol=1e-12, atol=1e-10)
+
+
+@pytest.mark.parametrize("dtype", [np.float64, np.float32])
+def test_tsqr(dtype):
+    rng = np.random.default_rng(4)
+    X = rng.standard_normal((4000, 50)).astype(dtype)
+    Q, R = P.math.tsqr(X)
+    tol = 1e-12 if dtype == np.float64 else 5e-6
+    assert orthogonality(Q) < tol * 10
+    np.testing.assert_allclose(np.tril(R, -1), 0)
+    np.testing.assert_allclose(Q.astype(np.float64) @ R, X, atol=tol * 10 * np.abs(X).max())
+
+
+@pytest.mark.parametrize("m,n,ld", [(1, 1, 1), (5, 1, 1), (64, 64, 64), (1000, 33, 40),
+                                    (2049, 129, 129), (300, 500, 500)])
+def test_tsqr_svd_shapes(m, n, ld):
+    rng = np.random.default_rng(m * 7 + n)
+    base = rng.standard_normal((m, ld))
+    Xt = torch.tensor(base, device="cuda")[:, :n]  # strided view when ld > n
+    U, S, V = P.math.tsqr_svd(Xt)
+    X = base[:, :n]
+    Sr = np.linalg.svd(X, compute_uv=False)
+    k = min(m, n)
+    assert U.shape == (m, k) and S.shape == (k,) and V.shape == (k, n)
+    assert sigma_normwise(S.cpu().numpy(), Sr) < 1e-12
+    Un, Sn, Vn = U.cpu().numpy(), S.cpu().numpy(), V.cpu().numpy()
+    np.testing.assert_allclose((Un * Sn) @ Vn, X, atol=1e-11 * np.abs(X).max())
+
+
+@pytest.mark.parametrize("dtype,precision,tol", [(np.complex128, "fp64", 1e-11),
+                                                 (np.complex64, "mixed", 2e-5)])
+def test_tsqr_svd_complex(dtype, precision, tol):
+    rng = np.random.default_rng(9)
+    X = (rng.standard_normal((2000, 24)) + 1j * rng.standard_normal((2000, 24))).astype(dtype)
+    U, S, V = P.math.tsqr_svd(X, precision=precision)
+    Ur, Sr, Vr = np.linalg.svd(X.astype(np.complex128), full_matrices=False)
+    assert sigma_rel(S, Sr) < tol
+    cols_up_to_phase(U, Ur, tol * 100)
+    np.testing.assert_allclose((U.astype(np.complex128) * S) @ V, X, atol=tol * 10 * np.abs(X).max())
+
+
+def test_pod_cfg1_full_fp64():
+    """cfg1: 128x128 grid x 200 snapshots, FP64, mean removed, truncation at
+    residual 1e-6; sigma within 1e-10 (signal modes) of the FP64 oracle."""
+    from pyloworder_gb300 import datagen
+    X = datagen.pod_field_np(128, 128, 200, 10, seed=1001)
+    U, S, V = P.POD.run(X)
+    Ur, Sr, Vr = O.pod_run(X)
+    assert sigma_rel(S, Sr, 10) < 1e-10
+    assert sigma_normwise(S, Sr) < 1e-12
+    cols_up_to_phase(U[:, :10], Ur[:, :10], 1e-8)
+    Ut, St, Vt = P.POD.truncate(U, S, V, r=1e-6)
+    assert Ut.shape[1] == O.pod_truncate(Ur, Sr, Vr, r=1e-6)[0].shape[1]
+
+
+def test_nonfinite_input_reports_error():
+    X = np.ones((100, 4))
+    X[3, 2] = np.nan
+    with pytest.raises(RuntimeError):
+        P.math.tsqr_svd(X)
+
+
+def test_torch_in_torch_out():
+    X = torch.randn(2000, 16, device="cuda", dtype=torch.float64)
+    U, S, V = P.POD.run(X)
+    assert all(isinstance(t, torch.Tensor) and t.is_cuda for t in (U, S, V))
+    Xc = X - X.mean(dim=1, keepdim=True)
+    np.testing.assert_allclose(((U * S) @ V).cpu().numpy(), Xc.cpu().numpy(), atol=1e-11)
