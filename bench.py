@@ -197,7 +197,7 @@ def run_ours(args):
     del X
     torch.cuda.synchronize()
     st = torch.cuda.current_stream()
-    prof = L.Profiler() if hasattr(L, "Profiler") else None
+    prof = L.Profiler()
 
     def step():
         return P.vmmath.tsqr_svd_device(Y, n, "mixed")

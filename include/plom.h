@@ -57,6 +57,15 @@ extern "C" {
 const char* plom_last_error_string(void);
 int plom_version(void);
 
+/* Per-kernel device timing on the calling host thread, the device-side
+   counterpart of pyLOM's named timing channels (pyLOM/utils/cr.py:199-246
+   cr_start/cr_stop, cr_info).  plom_profile_begin starts recording CUDA
+   events around every kernel launch; plom_profile_end waits for them and
+   writes one line per kernel name: "name launches total_ms flops bytes"
+   (algorithmic flops/bytes of the launches). */
+int plom_profile_begin(void);
+int plom_profile_end(char* buf, size_t cap);
+
 /* ---- averaging --------------------------------------------------------- */
 /* replaces stemporal_mean/dtemporal_mean (pyLOM/vmmath/src/averaging.c:10,29;
    Python pyLOM/vmmath/averaging.py:18).  mean has m entries. */
@@ -118,6 +127,31 @@ int plom_randomized_svd(int dtype, int prec, const void* X, int64_t m, int64_t n
 /* replaces srandom_matrix/drandom_matrix (vector_matrix.c:950,964): out[i] =
    uniform [0,1) for flat index i, Philox4x32-10 with key = seed, counter = i. */
 int plom_fill_uniform(int dtype, void* out, int64_t count, uint64_t seed, void* stream);
+
+/* ---- DMD ------------------------------------------------------------- */
+/* replaces the reduced-operator part of DMD.run (pyLOM/DMD/wrapper.py:84-117:
+   Atilde, eigen -> maths.py:161 / vector_matrix.c:500 zeigen, vandermonde
+   maths.py:203, cholesky maths.py:249, inv maths.py:277, _order_modes
+   wrapper.py:18-45), all FP64 on the device.  Inputs: aux1 = U^T Y2 (r x nt),
+   S (r), VT (r x nt) with nt = n_snapshots - 1.  Outputs (device, FP64):
+   muReal, muImag (r), bJov (r complex, interleaved) in pyLOM's mode order,
+   and Mphi (nt x r complex, interleaved) such that the DMD modes are
+   Phi = Y2 Mphi (one tall product, plom_matmul with the real view). */
+size_t plom_dmd_reduced_workspace(int64_t r, int64_t nt);
+int plom_dmd_reduced(const double* aux1, const double* S, const double* VT, int64_t r, int64_t nt,
+                     double* muReal, double* muImag, double* bJov, double* Mphi, void* ws,
+                     size_t ws_bytes, int* info, void* stream);
+
+/* ---- SPOD ------------------------------------------------------------ */
+/* replaces the Welch/FFT loop of SPOD.run (pyLOM/SPOD/wrapper.py:66-76 with
+   _fft at :18-20, window from pyLOM/vmmath/fft.py:17 hammwin): for every block
+   b (start b*step) and point i, the windowed FFT of Y[i, b*step : b*step+nDFT]
+   is scaled by `scale` (pyLOM: winWeight/nDFT, here also /sqrt(nBlks)), bins
+   1..nf-2 doubled, and bins 0..nf-1 written to Q[f][i][b] (complex,
+   interleaved; Q_f is row-major M x nBlks).  twr/twi: cos/-sin(2 pi j/nDFT). */
+int plom_spod_fft(int dtype, const void* Y, int64_t M, int64_t N, int64_t ldy, int64_t nDFT,
+                  int64_t step, int64_t nBlks, int64_t nf, const void* window, const void* twr,
+                  const void* twi, double scale, void* Q, void* stream);
 
 #ifdef __cplusplus
 }

@@ -1,0 +1,93 @@
+"""pyLOM.SPOD hot path on GB300.
+
+SPOD.run follows pyLOM/SPOD/wrapper.py:24-95: mean removal, Welch blocks
+(nDFT, nolap), window, FFT along time with pyLOM's scaling and one-sided
+doubling, one TSQR-SVD per frequency of the M x nBlks block matrix, P = Re(U)
+laid out as pyLOM lays it out, L = |S|^2, frequencies sorted by L[:, 0].
+
+``window='hamming'`` (default) is the reference's window
+(pyLOM/vmmath/fft.py:17); ``window='hann'`` is the symmetric Hann window.
+"""
+from __future__ import annotations
+
+import math
+
+import numpy as np
+
+from . import _lib as L
+from . import vmmath as M
+
+__all__ = ["run"]
+
+
+def _window(name, n):
+    i = np.arange(n)
+    if name == "hamming":
+        return 0.54 - 0.46 * np.cos(2 * np.pi * i / (n - 1))
+    if name == "hann":
+        return 0.5 - 0.5 * np.cos(2 * np.pi * i / (n - 1))
+    raise ValueError("window must be 'hamming' or 'hann'")
+
+
+def spod_fft_device(Y, ldy, nDFT, nolap, nBlks, nf, win, scale):
+    """Q[f] (M x nBlks complex) for every frequency bin, as one device array."""
+    t = L.torch()
+    Mrows, N = Y.shape
+    rdt = Y.dtype
+    cdt = t.complex128 if rdt == t.float64 else t.complex64
+    Q = t.empty((nf, Mrows, nBlks), dtype=cdt, device="cuda")
+    j = np.arange(nDFT)
+    wd = t.tensor(win, dtype=rdt, device="cuda")
+    twr = t.tensor(np.cos(2 * np.pi * j / nDFT), dtype=rdt, device="cuda")
+    twi = t.tensor(-np.sin(2 * np.pi * j / nDFT), dtype=rdt, device="cuda")
+    L.call("plom_spod_fft", L.dtype_code(Y), L.ptr(Y), Mrows, N, ldy, nDFT, nDFT - nolap, nBlks, nf,
+           L.ptr(wd), L.ptr(twr), L.ptr(twi), float(scale), L.ptr(Q), L.stream_ptr())
+    return Q
+
+
+def run_device(x, ld, t_host, nDFT=0, nolap=0, remove_mean=True, window="hamming", precision=None):
+    t = L.torch()
+    Mrows, N = x.shape
+    dt = float(t_host[1] - t_host[0])
+    if nDFT == 0:
+        nDFT = int(np.power(2, np.floor(np.log2(N / 10))))
+    win = _window(window, nDFT)
+    if nolap == 0:
+        nolap = int(np.floor(nDFT / 2))
+    nBlks = int(np.floor((N - nolap) / (nDFT - nolap)))
+    if nBlks < 1:
+        raise ValueError("SPOD: not enough snapshots for one block")
+    winWeight = 1 / np.mean(win)
+    if remove_mean:
+        Y, _, _ = M.remove_mean_device(x, ld)
+        ldy = Y.shape[1]
+    else:
+        Y, ldy = x, ld
+    f = np.arange(np.ceil(nDFT / 2) + 1) / dt / nDFT
+    nf = f.shape[0]
+    Q = spod_fft_device(Y, ldy, nDFT, nolap, nBlks, nf, win, winWeight / nDFT / math.sqrt(nBlks))
+    Lm = t.empty((nf, nBlks), dtype=x.dtype, device="cuda")
+    P = t.empty((Mrows * nBlks, nf), dtype=x.dtype, device="cuda")
+    P3 = P.view(nBlks, Mrows, nf)  # P[i + M*b, f] = Re U_f[i, b]
+    for fi in range(nf):
+        U, S, _ = M.tsqr_svd_device(Q[fi], nBlks, precision)
+        P3[:, :, fi] = U.real.transpose(0, 1)
+        Lm[fi] = (S * S).to(x.dtype)
+    order = np.argsort(Lm[:, 0].cpu().numpy())[::-1].copy()
+    od = t.as_tensor(order, device="cuda")
+    return Lm.index_select(0, od), P.index_select(1, od), f[order]
+
+
+def run(X, t, nDFT: int = 0, nolap: int = 0, remove_mean: bool = True, *, window="hamming",
+        precision=None):
+    """Spectral POD of X (points x snapshots) sampled at times t.  Returns L
+    (nf x nBlks modal energies), P ((M nBlks) x nf real modes) and f."""
+    cv = L.to_device(X)
+    x, ld = L.as_rows(cv.t)
+    if x.dtype not in (L.torch().float32, L.torch().float64):
+        raise TypeError("SPOD.run takes float32 or float64 data")
+    th = t.detach().cpu().numpy() if hasattr(t, "detach") else np.asarray(t)
+    Lm, P, f = run_device(x, ld, th, nDFT, nolap, remove_mean, window, precision)
+    if cv.kind == "numpy":
+        return Lm.cpu().numpy(), P.cpu().numpy(), f
+    return cv.back(Lm), cv.back(P), L.torch().as_tensor(f, device=cv.device)

@@ -9,6 +9,8 @@ PyTorch tensors; there is no CPU fallback.
 from . import vmmath
 from . import vmmath as math
 from . import POD
+from . import DMD
+from . import SPOD
 
 __version__ = "0.1.0"
 

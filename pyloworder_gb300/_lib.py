@@ -21,7 +21,8 @@ INFO_WORDS = 8
 NUM_MESSAGES = {1: "Cholesky breakdown after all shift escalations",
                 2: "one-sided Jacobi did not converge",
                 3: "non-finite values in the input",
-                4: "eigenvalue iteration did not converge"}
+                4: "eigenvalue iteration did not converge",
+                5: "a bounded device-side wait expired"}
 
 _lock = threading.Lock()
 _lib = None
@@ -35,6 +36,8 @@ c_sz = ctypes.c_size_t
 PROTOS = {
     "plom_last_error_string": (ctypes.c_char_p, []),
     "plom_version": (c_int, []),
+    "plom_profile_begin": (c_int, []),
+    "plom_profile_end": (c_int, [ctypes.c_char_p, c_sz]),
     "plom_temporal_mean": (c_int, [c_int, c_vp, c_i64, c_i64, c_i64, c_vp, c_vp]),
     "plom_subtract_mean": (c_int, [c_int, c_vp, c_i64, c_i64, c_i64, c_vp, c_vp, c_i64, c_vp]),
     "plom_temporal_variance": (c_int, [c_int, c_vp, c_i64, c_i64, c_i64, c_vp, c_vp, c_vp]),
@@ -55,6 +58,11 @@ PROTOS = {
                                     ctypes.c_uint64, c_vp, c_i64, c_vp, c_vp, c_vp, c_sz, c_vp,
                                     c_vp]),
     "plom_fill_uniform": (c_int, [c_int, c_vp, c_i64, ctypes.c_uint64, c_vp]),
+    "plom_spod_fft": (c_int, [c_int, c_vp, c_i64, c_i64, c_i64, c_i64, c_i64, c_i64, c_i64, c_vp, c_vp,
+                              c_vp, ctypes.c_double, c_vp, c_vp]),
+    "plom_dmd_reduced_workspace": (c_sz, [c_i64, c_i64]),
+    "plom_dmd_reduced": (c_int, [c_vp, c_vp, c_vp, c_i64, c_i64, c_vp, c_vp, c_vp, c_vp, c_vp, c_sz,
+                                 c_vp, c_vp]),
 }
 
 
@@ -196,6 +204,24 @@ def check_info(info, what):
     if v[0] != 0:
         raise PlomError(f"{what}: {NUM_MESSAGES.get(v[0], 'numerical failure')} (info={v})")
     return v
+
+
+class Profiler:
+    """Per-kernel CUDA-event timings of libplom launches made on this thread
+    (plom_profile_begin / plom_profile_end)."""
+
+    def start(self):
+        call("plom_profile_begin")
+
+    def stop(self):
+        buf = ctypes.create_string_buffer(1 << 16)
+        call("plom_profile_end", buf, len(buf))
+        out = {}
+        for line in buf.value.decode().splitlines():
+            name, cnt, ms, fl, by = line.split()
+            out[name] = {"name": name, "count": int(cnt), "ms_total": float(ms),
+                         "flops": float(fl), "bytes": float(by)}
+        return out
 
 
 def precision_code(precision, x):

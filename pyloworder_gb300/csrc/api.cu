@@ -1,4 +1,8 @@
 // Library-wide C-ABI entries: version and per-thread error string.
+#include <map>
+#include <string>
+#include <vector>
+
 #include "plom_common.cuh"
 
 namespace plom {
@@ -14,7 +18,61 @@ void set_error(const char* fmt, ...) {
 
 const char* last_error() { return g_err; }
 
+static thread_local std::vector<ProfEntry>* g_prof = nullptr;
+bool prof_on() { return g_prof != nullptr; }
+void prof_push(const ProfEntry& e) {
+  if (g_prof) g_prof->push_back(e);
+}
+
 }  // namespace plom
 
 extern "C" const char* plom_last_error_string(void) { return plom::last_error(); }
 extern "C" int plom_version(void) { return 100; }
+
+extern "C" int plom_profile_begin(void) {
+  if (!plom::g_prof) plom::g_prof = new std::vector<plom::ProfEntry>();
+  plom::g_prof->clear();
+  return PLOM_OK;
+}
+
+extern "C" int plom_profile_end(char* buf, size_t cap) {
+  using namespace plom;
+  if (!g_prof) {
+    if (buf && cap) buf[0] = 0;
+    return PLOM_OK;
+  }
+  struct Agg {
+    int count = 0;
+    double ms = 0, flops = 0, bytes = 0;
+  };
+  std::map<std::string, Agg> agg;
+  int status = PLOM_OK;
+  for (auto& e : *g_prof) {
+    float ms = 0.f;
+    if (cudaEventSynchronize(e.b) != cudaSuccess || cudaEventElapsedTime(&ms, e.a, e.b) != cudaSuccess)
+      status = PLOM_ERR_CUDA;
+    Agg& a = agg[e.name];
+    a.count += 1;
+    a.ms += ms;
+    a.flops += e.flops;
+    a.bytes += e.bytes;
+    cudaEventDestroy(e.a);
+    cudaEventDestroy(e.b);
+  }
+  delete g_prof;
+  g_prof = nullptr;
+  std::string out;
+  char line[256];
+  for (auto& kv : agg) {
+    snprintf(line, sizeof(line), "%s %d %.6f %.6e %.6e\n", kv.first.c_str(), kv.second.count,
+             kv.second.ms, kv.second.flops, kv.second.bytes);
+    out += line;
+  }
+  if (buf && cap) {
+    size_t n = out.size() < cap - 1 ? out.size() : cap - 1;
+    memcpy(buf, out.data(), n);
+    buf[n] = 0;
+  }
+  if (status != PLOM_OK) set_error("plom_profile_end: event timing failed");
+  return status;
+}

@@ -162,6 +162,8 @@ static int launch_rows(const T* X, int64_t m, int64_t n, int64_t ldx, const T* m
   int64_t blocks = cdiv(warps, threads / 32);
   const int64_t cap = (int64_t)num_sms() * 8 * 4;  // persistent-ish grid: 8 blocks/SM x 4 waves
   if (blocks > cap) blocks = cap;
+  ProfScope prof("rows_mean_subtract", st, 0.0,
+                 (double)m * n * sizeof(T) * (ymode == Y_NONE ? 1.0 : 2.0));
   if (vec)
     row_kernel<T, true><<<(unsigned)blocks, threads, 0, st>>>(X, m, n, ldx, mean_in, var_in,
                                                               mean_out, var_out, want_var, ymode,

@@ -250,6 +250,7 @@ int chol_shifted(const double* G, double* R, int n, int batch, double rel0, doub
   const int T = (n + NB - 1) / NB;
   int want = std::max(batch * std::max(1, T * (T + 1) / 2), 1);
   int blocks = coop_blocks((const void*)chol_coop_kernel, 256, 0, want);
+  ProfScope prof("chol_fp64", st, (double)n * n * n / 3.0 * batch, 16.0 * n * n * batch);
   void* args[] = {(void*)&G, (void*)&R, (void*)&Dinv, (void*)&n, (void*)&batch,
                   (void*)&rel0, (void*)&relfail, (void*)&s, (void*)&info};
   PLOM_CHECK_CUDA(cudaLaunchCooperativeKernel((const void*)chol_coop_kernel, dim3(blocks),
@@ -350,6 +351,7 @@ int trtri_upper(const double* R, double* W, int n, int batch, Arena& ws, cudaStr
   while ((int64_t)threads * 4 < n) threads += 32;
   int64_t tasks = (int64_t)n * batch;
   int blocks = (int)std::min<int64_t>(tasks, (int64_t)num_sms() * 2);
+  ProfScope prof("trtri_fp64", st, (double)n * n * n / 3.0 * batch, 16.0 * n * n * batch);
   trtri_col_kernel<<<blocks, threads, 0, st>>>(Rt, W, n, batch);
   PLOM_CHECK_LAUNCH();
   return PLOM_OK;
@@ -561,6 +563,7 @@ int jacobi_svd(const double* A, int n, int batch, int cplx, double* S, double* U
   const int np = n + (n & 1);
   int want = (int)std::max<int64_t>(1, cdiv((int64_t)np / 2 * batch, 8));
   int blocks = coop_blocks((const void*)jacobi_coop_kernel, 256, 0, want);
+  ProfScope prof("jacobi_svd_fp64", st, 0.0, 24.0 * n * n * batch * (cplx ? 2 : 1));
   void* args[] = {(void*)&A, (void*)&n, (void*)&batch, (void*)&cplx, (void*)&js,
                   (void*)&S, (void*)&U, (void*)&VH, (void*)&info};
   PLOM_CHECK_CUDA(cudaLaunchCooperativeKernel((const void*)jacobi_coop_kernel, dim3(blocks),

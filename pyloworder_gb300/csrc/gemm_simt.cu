@@ -93,6 +93,8 @@ int gemm_nn_batched(const TA* A, int64_t lda, int64_t sA, const TB* B, int64_t l
   constexpr int BM = 128, BN = 64, BK = 8;
   dim3 grid((unsigned)cdiv(M, BM), (unsigned)cdiv(N, BN), (unsigned)batch);
   PLOM_REQUIRE(grid.y <= 65535 && batch <= 65535, PLOM_ERR_ARG, "gemm_nn: N or batch too large");
+  ProfScope prof(sizeof(Acc) == 8 ? "gemm_nn_fp64" : "gemm_nn_fp32", st, 2.0 * M * N * K * batch,
+                 (double)batch * ((double)M * K * sizeof(TA) + (double)M * N * sizeof(TC)));
   gemm_nn_kernel<TA, TB, TC, Acc, BM, BN, BK, 8, 4><<<grid, 256, 0, st>>>(A, lda, sA, B, ldb, sB, C,
                                                                           ldc, sC, M, N, K);
   PLOM_CHECK_LAUNCH();
@@ -259,6 +261,9 @@ int gemm_tn_batched(const TA* A, int64_t lda, int64_t sA, const TB* B, int64_t l
   PLOM_CHECK_LAUNCH();
   if (K > 0) {
     dim3 grid((unsigned)p.ntiles, (unsigned)p.chunks, (unsigned)batch);
+    ProfScope prof(sizeof(Acc) == 8 ? "gemm_tn_fp64" : "gemm_tn_fp32", st,
+                   (sym ? 1.0 : 2.0) * M * N * K * batch,
+                   (double)batch * K * ((double)M * sizeof(TA) + (sym ? 0.0 : (double)N * sizeof(TB))));
     gemm_tn_kernel<TA, TB, Acc, BM, BN, BK><<<grid, 256, 0, st>>>(A, lda, sA, B, ldb, sB, part, M,
                                                                   N, K, p.kchunk, p.chunks, tiles);
     PLOM_CHECK_LAUNCH();

@@ -73,15 +73,26 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, volati
                                           int* err) {
   if (mbar_try_wait(bar, parity)) return true;
   const uint64_t t0 = gtimer();
+  uint32_t spins = 0;
   while (true) {
     if (mbar_try_wait(bar, parity)) return true;
     if (*abort_flag) return false;
+    if ((++spins & 1023u) == 0 && err && *(volatile int*)err == PLOM_NUM_TIMEOUT) {
+      *abort_flag = 1;  // another CTA of this launch gave up: stop too
+      return false;
+    }
     if (gtimer() - t0 > WAIT_NS) {
       *abort_flag = 1;
       if (err) atomicMax(err, PLOM_NUM_TIMEOUT);
       return false;
     }
   }
+}
+
+// A CTA that starts after another CTA of the same launch timed out skips its
+// work (the launch's result is already invalid and reported).
+__device__ __forceinline__ bool launch_aborted(const int* err) {
+  return err && *(volatile const int*)err == PLOM_NUM_TIMEOUT;
 }
 
 __device__ __forceinline__ void tmem_alloc(uint32_t* dst, uint32_t ncols) {
@@ -244,6 +255,7 @@ __global__ void __launch_bounds__(160, 1)
   const int64_t m0 = (tile / col_tiles) * BM;
   const int n0 = (int)(tile % col_tiles) * AP_BN;
   const int KB = (K + BK - 1) / BK;
+  if (launch_aborted(err)) return;
 
   if (threadIdx.x == 0) {
     for (int s = 0; s < AP_STAGES; ++s) {
@@ -255,7 +267,7 @@ __global__ void __launch_bounds__(160, 1)
     mbar_fence_init();
   }
   if (warp == 4) {
-    tmem_alloc(&tmem_sh, AP_BN);
+    tmem_alloc(&tmem_sh, 2 * AP_BN);  // main hi*hi + correction hi*lo + lo*hi
     tmem_relinquish();
   }
   fence_before();
@@ -314,9 +326,10 @@ __global__ void __launch_bounds__(160, 1)
 #pragma unroll
       for (int kk = 0; kk < BK / 8; ++kk) {
         const uint64_t adv = (uint64_t)(kk * 32) >> 4;  // 8 tf32 = 32 bytes along K
-        mma_tf32(tmem, dAhi + adv, dBhi + adv, idesc, (kb > 0 || kk > 0) ? 1u : 0u);
-        mma_tf32(tmem, dAhi + adv, dBlo + adv, idesc, 1u);
-        mma_tf32(tmem, dAlo + adv, dBhi + adv, idesc, 1u);
+        const uint32_t acc = (kb > 0 || kk > 0) ? 1u : 0u;
+        mma_tf32(tmem, dAhi + adv, dBhi + adv, idesc, acc);
+        mma_tf32(tmem + AP_BN, dAhi + adv, dBlo + adv, idesc, acc);
+        mma_tf32(tmem + AP_BN, dAlo + adv, dBhi + adv, idesc, 1u);
       }
       mma_commit(&empty_bar[s]);
     }
@@ -325,15 +338,22 @@ __global__ void __launch_bounds__(160, 1)
 
   if (warp < 4) {
     // ---- epilogue: TMEM -> registers -> C
-    if (mbar_wait(&acc_bar, 0, &abort_sh, err)) {
+    const bool ready = mbar_wait(&acc_bar, 0, &abort_sh, err);
+    __syncwarp();
+    if (__all_sync(0xffffffffu, ready)) {
       fence_after();
       const int64_t row = m0 + warp * 32 + lane;
       const bool vec = ((ldc & 3) == 0) && ((reinterpret_cast<uintptr_t>(C) & 15) == 0);
 #pragma unroll 1
       for (int cc = 0; cc < AP_BN / 32; ++cc) {
-        uint32_t r[32];
-        tmem_ld32(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(cc * 32), r);
+        uint32_t r[32], rc[32];
+        const uint32_t ta = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(cc * 32);
+        tmem_ld32(ta, r);
+        tmem_ld32(ta + AP_BN, rc);
         tmem_wait_ld();
+#pragma unroll
+        for (int j = 0; j < 32; ++j)
+          r[j] = __float_as_uint(__uint_as_float(r[j]) + __uint_as_float(rc[j]));
         const int col0 = n0 + cc * 32;
         if (row < m && col0 < ncols) {
           float* dst = C + row * ldc + col0;
@@ -355,8 +375,9 @@ __global__ void __launch_bounds__(160, 1)
   fence_before();
   __syncthreads();
   if (warp == 4) {
+    __syncwarp();
     fence_after();
-    tmem_dealloc(tmem, AP_BN);
+    tmem_dealloc(tmem, 2 * AP_BN);
   }
 }
 
@@ -365,17 +386,25 @@ __global__ void __launch_bounds__(160, 1)
 // ---------------------------------------------------------------------------
 constexpr int GR_BN = 128;
 constexpr int GR_STAGES = 3;
-constexpr int GR_KSUB = 4096;  // rows per FP32 accumulation before the FP64 drain
+// Rows accumulated in TMEM (FP32) before the FP64 drain.  The tensor core's
+// FP32 accumulation truncates on every UMMA, so the bias grows with the number
+// of UMMA per drain; 2048 rows = 256 UMMA per accumulator keeps it near
+// 7e-6 relative on off-diagonal entries, and the diagonal (sums of squares,
+// where the bias does not cancel) is computed separately on the CUDA cores
+// with compensated FP32 sums (Kahan) folded into FP64 at every drain.
+constexpr int GR_KSUB = 2048;
 constexpr uint32_t GR_T_BYTES = BM * ROWB;  // one 128 x 32 fp32 operand tile
 constexpr uint32_t GR_STAGE_BYTES = 4 * GR_T_BYTES;
 constexpr size_t GR_SMEM = (size_t)GR_STAGES * GR_STAGE_BYTES + 1024;
+constexpr uint32_t GR_TMEM_COLS = 512;  // 2 buffers x (main 128 + correction 128)
 
 __global__ void __launch_bounds__(288, 1)
     tc_gram_kernel(const float* __restrict__ A, int64_t lda, int64_t m, int N, int tn,
                    int64_t rows_per_chunk, int chunks, double* __restrict__ part, int a_vec,
                    int* err) {
   extern __shared__ uint8_t smem_raw[];
-  __shared__ uint64_t full_bar[GR_STAGES], empty_bar[GR_STAGES], tfull[2], tempty[2];
+  __shared__ uint64_t full_bar[GR_STAGES], empty_bar[GR_STAGES], tfull[2], tempty[2], dfull[2];
+  __shared__ double diag_sh[2][BM];
   __shared__ uint32_t tmem_sh;
   __shared__ int abort_sh;
   const uint32_t base = (smem_u32(smem_raw) + 1023u) & ~1023u;
@@ -397,6 +426,7 @@ __global__ void __launch_bounds__(288, 1)
   const int KB = (int)((nrows + BK - 1) / BK);
   const int nsub = (int)((nrows + GR_KSUB - 1) / GR_KSUB);
   constexpr int KB_PER_SUB = GR_KSUB / BK;
+  if (launch_aborted(err)) return;
 
   if (threadIdx.x == 0) {
     for (int s = 0; s < GR_STAGES; ++s) {
@@ -406,12 +436,13 @@ __global__ void __launch_bounds__(288, 1)
     for (int b = 0; b < 2; ++b) {
       mbar_init(&tfull[b], 1);
       mbar_init(&tempty[b], 128);
+      mbar_init(&dfull[b], 128);
     }
     abort_sh = 0;
     mbar_fence_init();
   }
   if (warp == 8) {
-    tmem_alloc(&tmem_sh, 2 * GR_BN);
+    tmem_alloc(&tmem_sh, GR_TMEM_COLS);
     tmem_relinquish();
   }
   fence_before();
@@ -422,8 +453,12 @@ __global__ void __launch_bounds__(288, 1)
 
   if (warp >= 4 && warp < 8) {
     // ---- producers: rows r0..r0+31 of A, columns of the I and J blocks,
-    // transposed into K-major tiles (lane = K index) and split hi/lo.
+    // transposed into K-major tiles (lane = K index) and split hi/lo.  On a
+    // diagonal tile they also keep Kahan sums of x^2 for their 32 columns.
     const int w = warp - 4;
+    float dsum[32], dcmp[32];
+#pragma unroll
+    for (int q = 0; q < 32; ++q) dsum[q] = dcmp[q] = 0.f;
     for (int kb = 0; kb < KB; ++kb) {
       const int s = kb % GR_STAGES;
       const uint32_t ph = (uint32_t)(kb / GR_STAGES) & 1u;
@@ -435,12 +470,13 @@ __global__ void __launch_bounds__(288, 1)
       for (int blk = 0; blk < (diag ? 1 : 2); ++blk) {
         const int C0 = blk ? J0 : I0;
         const uint32_t shi = st + (blk ? 2 * GR_T_BYTES : 0), slo = shi + GR_T_BYTES;
-#pragma unroll 2
+#pragma unroll
         for (int j4 = 0; j4 < 8; ++j4) {
           const int mr0 = 32 * w + 4 * j4;
           float4 v = load4(A, lda, row, r_end, (int64_t)C0 + mr0, N, a_vec != 0);
           float4 hi, lo;
           split4(v, hi, lo);
+          const float xv[4] = {v.x, v.y, v.z, v.w};
           const float hv[4] = {hi.x, hi.y, hi.z, hi.w}, lv[4] = {lo.x, lo.y, lo.z, lo.w};
 #pragma unroll
           for (int q = 0; q < 4; ++q) {
@@ -448,14 +484,35 @@ __global__ void __launch_bounds__(288, 1)
             const uint32_t off = mr * ROWB + ((kchunk ^ (mr & 7u)) << 4) + kin;
             st_shared_f32(shi + off, hv[q]);
             st_shared_f32(slo + off, lv[q]);
+            if (diag) {  // Kahan: dsum += x^2
+              const float y = xv[q] * xv[q] - dcmp[4 * j4 + q];
+              const float t = dsum[4 * j4 + q] + y;
+              dcmp[4 * j4 + q] = (t - dsum[4 * j4 + q]) - y;
+              dsum[4 * j4 + q] = t;
+            }
           }
         }
       }
       fence_proxy_async();
       mbar_arrive(&full_bar[s]);
+      if ((kb % KB_PER_SUB) == KB_PER_SUB - 1 || kb == KB - 1) {
+        // end of a sub-chunk: column sums over the 32 lanes in FP64
+        const int b = (kb / KB_PER_SUB) & 1;
+        double mine = 0.0;
+        if (diag) {
+#pragma unroll
+          for (int q = 0; q < 32; ++q) {
+            const double v = warp_sum((double)dsum[q] - (double)dcmp[q]);
+            if (lane == q) mine = v;
+            dsum[q] = dcmp[q] = 0.f;
+          }
+        }
+        diag_sh[b][32 * w + lane] = mine;
+        mbar_arrive(&dfull[b]);
+      }
     }
   } else if (warp == 8 && lane == 0) {
-    // ---- UMMA issuer
+    // ---- UMMA issuer: main += hi*hi, correction += hi*lo + lo*hi
     constexpr uint32_t idesc = idesc_tf32(BM, GR_BN);
     bool ok = true;
     int kb = 0;
@@ -466,7 +523,8 @@ __global__ void __launch_bounds__(288, 1)
         break;
       }
       fence_after();
-      const uint32_t dt = tmem + (uint32_t)(b * GR_BN);
+      const uint32_t dmain = tmem + (uint32_t)(b * 2 * GR_BN);
+      const uint32_t dcorr = dmain + (uint32_t)GR_BN;
       const int kb_end = (kb + KB_PER_SUB < KB) ? kb + KB_PER_SUB : KB;
       for (int kl = 0; kb < kb_end; ++kb, ++kl) {
         const int s = kb % GR_STAGES;
@@ -483,9 +541,10 @@ __global__ void __launch_bounds__(288, 1)
 #pragma unroll
         for (int kk = 0; kk < BK / 8; ++kk) {
           const uint64_t adv = (uint64_t)(kk * 32) >> 4;
-          mma_tf32(dt, dAhi + adv, dBhi + adv, idesc, (kl > 0 || kk > 0) ? 1u : 0u);
-          mma_tf32(dt, dAhi + adv, dBlo + adv, idesc, 1u);
-          mma_tf32(dt, dAlo + adv, dBhi + adv, idesc, 1u);
+          const uint32_t first = (kl > 0 || kk > 0) ? 1u : 0u;
+          mma_tf32(dmain, dAhi + adv, dBhi + adv, idesc, first);
+          mma_tf32(dcorr, dAhi + adv, dBlo + adv, idesc, first);
+          mma_tf32(dcorr, dAlo + adv, dBhi + adv, idesc, 1u);
         }
         mma_commit(&empty_bar[s]);
       }
@@ -496,26 +555,34 @@ __global__ void __launch_bounds__(288, 1)
     const int rloc = warp * 32 + lane;
     for (int sub = 0; sub < nsub; ++sub) {
       const int b = sub & 1;
-      if (!mbar_wait(&tfull[b], ((uint32_t)sub >> 1) & 1u, &abort_sh, err)) break;
+      const uint32_t par = ((uint32_t)sub >> 1) & 1u;
+      bool ready = mbar_wait(&tfull[b], par, &abort_sh, err);
+      ready = ready && mbar_wait(&dfull[b], par, &abort_sh, err);
+      __syncwarp();
+      if (!__all_sync(0xffffffffu, ready)) break;
       fence_after();
+      const double dval = diag_sh[b][rloc];
       double* prow = P + (int64_t)rloc * GR_BN;
 #pragma unroll 1
       for (int cc = 0; cc < GR_BN / 32; ++cc) {
-        uint32_t r[32];
-        tmem_ld32(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(b * GR_BN + cc * 32), r);
+        uint32_t rm[32], rc[32];
+        const uint32_t ta = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(b * 2 * GR_BN + cc * 32);
+        tmem_ld32(ta, rm);
+        tmem_ld32(ta + GR_BN, rc);
         tmem_wait_ld();
         double* d = prow + cc * 32;
-        if (sub == 0) {
 #pragma unroll
-          for (int j = 0; j < 32; j += 2)
-            *reinterpret_cast<double2*>(d + j) =
-                make_double2((double)__uint_as_float(r[j]), (double)__uint_as_float(r[j + 1]));
-        } else {
-#pragma unroll
-          for (int j = 0; j < 32; j += 2) {
+        for (int j = 0; j < 32; j += 2) {
+          double v0 = (double)__uint_as_float(rm[j]) + (double)__uint_as_float(rc[j]);
+          double v1 = (double)__uint_as_float(rm[j + 1]) + (double)__uint_as_float(rc[j + 1]);
+          if (diag && cc * 32 + j == rloc) v0 = dval;
+          if (diag && cc * 32 + j + 1 == rloc) v1 = dval;
+          if (sub == 0) {
+            *reinterpret_cast<double2*>(d + j) = make_double2(v0, v1);
+          } else {
             double2 o = *reinterpret_cast<double2*>(d + j);
-            o.x += (double)__uint_as_float(r[j]);
-            o.y += (double)__uint_as_float(r[j + 1]);
+            o.x += v0;
+            o.y += v1;
             *reinterpret_cast<double2*>(d + j) = o;
           }
         }
@@ -531,8 +598,9 @@ __global__ void __launch_bounds__(288, 1)
   fence_before();
   __syncthreads();
   if (warp == 8) {
+    __syncwarp();
     fence_after();
-    tmem_dealloc(tmem, 2 * GR_BN);
+    tmem_dealloc(tmem, GR_TMEM_COLS);
   }
 }
 
@@ -594,11 +662,13 @@ int tc_gram_tf32x3(const float* A, int64_t lda, int64_t m, int64_t N, double* G,
     attr = true;
   }
   const int a_vec = ((lda & 3) == 0) && ((reinterpret_cast<uintptr_t>(A) & 15) == 0);
+  ProfScope prof_g("tc_gram_tf32x3", st, (double)m * N * N, 4.0 * m * N);
   tc::tc_gram_kernel<<<tiles * chunks_eff, 288, tc::GR_SMEM, st>>>(A, lda, m, (int)N, tn, rpc,
                                                                    chunks_eff, part, a_vec, err);
   PLOM_CHECK_LAUNCH();
   const int64_t total = N * N;
   int blocks = (int)std::min<int64_t>(cdiv(total, 256), (int64_t)num_sms() * 16);
+  ProfScope prof_r("gram_reduce", st, 0.0, 8.0 * (double)tiles * chunks_eff * tc::BM * tc::GR_BN);
   tc::gram_reduce_kernel<<<blocks, 256, 0, st>>>(part, (int)N, tn, chunks_eff, G);
   PLOM_CHECK_LAUNCH();
   return PLOM_OK;
@@ -632,6 +702,7 @@ int tc_apply_tf32x3(const float* A, int64_t lda, int64_t m, int64_t N, const TW*
   const int64_t tiles = cdiv(m, tc::BM) * col_tiles;
   PLOM_REQUIRE(tiles < (1ll << 31), PLOM_ERR_ARG, "tc_apply: too many tiles");
   const int a_vec = ((lda & 3) == 0) && ((reinterpret_cast<uintptr_t>(A) & 15) == 0);
+  ProfScope prof_a("tc_apply_tf32x3", st, 2.0 * m * N * k, 4.0 * ((double)m * N + (double)m * k));
   tc::tc_apply_kernel<<<(unsigned)tiles, 160, tc::AP_SMEM, st>>>(A, lda, m, (int)N, Whi, Wlo,
                                                                  (int)k, col_tiles, C, ldc, a_vec,
                                                                  err);

@@ -96,6 +96,38 @@ __device__ __forceinline__ T warp_max(T v) {
   return v;
 }
 
+// ---------------------------------------------------------------------------
+// per-kernel device timing (host-thread local; off unless plom_profile_begin
+// was called on this thread).  A ProfScope around a launch records CUDA events
+// on the launch stream and the launch's algorithmic flops and bytes.
+// ---------------------------------------------------------------------------
+struct ProfEntry {
+  const char* name;
+  cudaEvent_t a, b;
+  double flops, bytes;
+};
+bool prof_on();
+void prof_push(const ProfEntry& e);
+struct ProfScope {
+  ProfEntry e;
+  cudaStream_t st;
+  bool on;
+  ProfScope(const char* name, cudaStream_t s, double flops, double bytes) : st(s), on(prof_on()) {
+    if (!on) return;
+    e.name = name;
+    e.flops = flops;
+    e.bytes = bytes;
+    cudaEventCreate(&e.a);
+    cudaEventCreate(&e.b);
+    cudaEventRecord(e.a, st);
+  }
+  ~ProfScope() {
+    if (!on) return;
+    cudaEventRecord(e.b, st);
+    prof_push(e);
+  }
+};
+
 // status words written by kernels (device side) and read back by the host.
 // Index 0: numerical failure code (0 = ok), 1: count of Cholesky shift
 // escalations, 2: Jacobi sweeps of the last small SVD, 3: non-finite input seen.

@@ -1,0 +1,175 @@
+// SPOD Fourier stage: Welch blocks of the mean-removed snapshot matrix,
+// windowed and transformed along time, written per frequency as the
+// M x nBlks complex matrices the per-frequency SVDs consume.
+//
+// Reference behaviour (pyLowOrder pyLOM/SPOD/wrapper.py:24-85, _fft at :18):
+//   block b starts at b*(nDFT - nolap); Xf = Y[:, i0:i0+nDFT] * window;
+//   qk = winWeight/nDFT * fft(Xf)[:, :nf]; qk[:, 1:-1] *= 2;
+//   Q_f = qk[:, f] over blocks, divided by sqrt(nBlks) before its SVD.
+// Here `scale` = winWeight / nDFT / sqrt(nBlks) and the output layout is
+// Q[f][i][b] (complex, interleaved re/im): Q_f is row-major M x nBlks.
+//
+// GB300 mapping: a CTA owns R consecutive points; each warp transforms whole
+// windows (radix-2 decimation-in-time FFT in its own shared-memory buffer
+// when nDFT is a power of two, a direct DFT from a twiddle table otherwise);
+// results are staged in shared memory as [row][block][bin] and streamed out
+// per frequency as contiguous R*nBlks runs.  HBM-bound: bytes = read M*N*s +
+// write M*nBlks*nf*2s.
+#include <algorithm>
+#include <cmath>
+
+#include "plom_common.cuh"
+#include "plom_kernels.cuh"
+
+namespace plom {
+
+template <typename T>
+struct c2 {
+  T re, im;
+};
+
+template <typename T>
+__global__ void __launch_bounds__(256) spod_fft_kernel(
+    const T* __restrict__ Y, int64_t M, int64_t N, int64_t ldy, int nDFT, int log2n, int step,
+    int nBlks, int nf, const T* __restrict__ window, const T* __restrict__ twr,
+    const T* __restrict__ twi, T scale, int R, T* __restrict__ Q) {
+  extern __shared__ unsigned char smem_raw[];
+  T* sw = reinterpret_cast<T*>(smem_raw);                    // window  [nDFT]
+  T* sc = sw + nDFT;                                          // cos     [nDFT]
+  T* ss = sc + nDFT;                                          // sin     [nDFT]
+  c2<T>* buf = reinterpret_cast<c2<T>*>(ss + nDFT);           // 8 warps x nDFT
+  c2<T>* stage = buf + 8 * (size_t)nDFT;                      // R x nBlks x nf
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  for (int j = tid; j < nDFT; j += blockDim.x) {
+    sw[j] = window[j];
+    sc[j] = twr[j];
+    ss[j] = twi[j];
+  }
+  __syncthreads();
+  const int64_t i0 = (int64_t)blockIdx.x * R;
+  const int rows = (int)std::min<int64_t>((int64_t)R, M - i0);
+  c2<T>* wb = buf + (size_t)warp * nDFT;
+  const int nwin = rows * nBlks;
+  for (int wdx = warp; wdx < nwin; wdx += 8) {
+    const int r = wdx / nBlks, b = wdx % nBlks;
+    const T* x = Y + (i0 + r) * ldy + (int64_t)b * step;
+    c2<T>* out = stage + ((size_t)r * nBlks + b) * nf;
+    if (log2n >= 0) {
+      // windowed samples into bit-reversed positions
+      for (int j = lane; j < nDFT; j += 32) {
+        const unsigned rj = __brev((unsigned)j) >> (32 - log2n);
+        wb[rj].re = x[j] * sw[j];
+        wb[rj].im = T(0);
+      }
+      __syncwarp();
+      for (int s = 1; s <= log2n; ++s) {
+        const int half = 1 << (s - 1);
+        const int tstride = nDFT >> s;  // twiddle index step
+        for (int bf = lane; bf < nDFT / 2; bf += 32) {
+          const int grp = bf / half, pos = bf % half;
+          const int a = grp * 2 * half + pos, c = a + half;
+          const T wr = sc[pos * tstride], wi = ss[pos * tstride];  // e^{-2 pi i k / n}
+          const c2<T> u = wb[a], v = wb[c];
+          const T tr = v.re * wr - v.im * wi, ti = v.re * wi + v.im * wr;
+          wb[a].re = u.re + tr;
+          wb[a].im = u.im + ti;
+          wb[c].re = u.re - tr;
+          wb[c].im = u.im - ti;
+        }
+        __syncwarp();
+      }
+      for (int k = lane; k < nf; k += 32) {
+        const T f = (k >= 1 && k <= nf - 2) ? T(2) * scale : scale;
+        out[k].re = wb[k].re * f;
+        out[k].im = wb[k].im * f;
+      }
+      __syncwarp();
+    } else {
+      // direct DFT (nDFT not a power of two)
+      for (int j = lane; j < nDFT; j += 32) {
+        wb[j].re = x[j] * sw[j];
+        wb[j].im = T(0);
+      }
+      __syncwarp();
+      for (int k = lane; k < nf; k += 32) {
+        T sr = 0, si = 0;
+        int idx = 0;
+        for (int j = 0; j < nDFT; ++j) {
+          sr += wb[j].re * sc[idx];
+          si += wb[j].re * ss[idx];
+          idx += k;
+          if (idx >= nDFT) idx -= nDFT;
+        }
+        const T f = (k >= 1 && k <= nf - 2) ? T(2) * scale : scale;
+        out[k].re = sr * f;
+        out[k].im = si * f;
+      }
+      __syncwarp();
+    }
+  }
+  __syncthreads();
+  // stream out: Q[f][i0 + r][b]
+  const int per_f = rows * nBlks;
+  c2<T>* Qc = reinterpret_cast<c2<T>*>(Q);
+  for (int64_t e = tid; e < (int64_t)nf * per_f; e += blockDim.x) {
+    const int f = (int)(e / per_f), rb = (int)(e % per_f);
+    const int r = rb / nBlks, b = rb % nBlks;
+    Qc[((int64_t)f * M + i0 + r) * nBlks + b] = stage[((size_t)r * nBlks + b) * nf + f];
+  }
+}
+
+template <typename T>
+static int spod_fft_impl(const T* Y, int64_t M, int64_t N, int64_t ldy, int nDFT, int step,
+                         int nBlks, int nf, const T* window, const T* twr, const T* twi,
+                         double scale, T* Q, cudaStream_t st) {
+  int log2n = -1;
+  if ((nDFT & (nDFT - 1)) == 0) {
+    log2n = 0;
+    while ((1 << log2n) < nDFT) ++log2n;
+  }
+  const size_t fixed = sizeof(T) * 3 * (size_t)nDFT + sizeof(c2<T>) * 8 * (size_t)nDFT;
+  const size_t per_row = sizeof(c2<T>) * (size_t)nBlks * nf;
+  const size_t cap = 200 * 1024;
+  PLOM_REQUIRE(fixed + per_row <= cap, PLOM_ERR_UNSUPPORTED,
+               "spod_fft: nDFT=%d with %d blocks does not fit one CTA", nDFT, nBlks);
+  int R = (int)std::min<size_t>(8, (cap - fixed) / per_row);
+  R = std::max(1, R);
+  const size_t smem = fixed + per_row * R;
+  PLOM_CHECK_CUDA(cudaFuncSetAttribute(spod_fft_kernel<T>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  const int64_t grid = cdiv(M, R);
+  PLOM_REQUIRE(grid < (1ll << 31), PLOM_ERR_ARG, "spod_fft: too many rows");
+  ProfScope prof("spod_fft", st, 5.0 * (double)M * nBlks * nDFT * (log2n > 0 ? log2n : nDFT),
+                 (double)sizeof(T) * ((double)M * N + 2.0 * M * nBlks * nf));
+  spod_fft_kernel<T><<<(unsigned)grid, 256, smem, st>>>(Y, M, N, ldy, nDFT, log2n, step, nBlks,
+                                                        nf, window, twr, twi, (T)scale, R, Q);
+  PLOM_CHECK_LAUNCH();
+  return PLOM_OK;
+}
+
+}  // namespace plom
+
+using namespace plom;
+
+extern "C" int plom_spod_fft(int dtype, const void* Y, int64_t M, int64_t N, int64_t ldy,
+                             int64_t nDFT, int64_t step, int64_t nBlks, int64_t nf,
+                             const void* window, const void* twr, const void* twi, double scale,
+                             void* Q, void* stream) {
+  PLOM_REQUIRE(Y && window && twr && twi && Q, PLOM_ERR_ARG, "spod_fft: null pointer");
+  PLOM_REQUIRE(M >= 1 && nDFT >= 2 && nDFT <= 8192 && step >= 1 && nBlks >= 1 && nf >= 1 &&
+                   nf <= nDFT && ldy >= N,
+               PLOM_ERR_ARG, "spod_fft: bad sizes");
+  PLOM_REQUIRE((nBlks - 1) * step + nDFT <= N, PLOM_ERR_ARG,
+               "spod_fft: blocks run past the last snapshot");
+  cudaStream_t st = (cudaStream_t)stream;
+  if (dtype == PLOM_F32)
+    return spod_fft_impl<float>((const float*)Y, M, N, ldy, (int)nDFT, (int)step, (int)nBlks,
+                                (int)nf, (const float*)window, (const float*)twr,
+                                (const float*)twi, scale, (float*)Q, st);
+  if (dtype == PLOM_F64)
+    return spod_fft_impl<double>((const double*)Y, M, N, ldy, (int)nDFT, (int)step, (int)nBlks,
+                                 (int)nf, (const double*)window, (const double*)twr,
+                                 (const double*)twi, scale, (double*)Q, st);
+  set_error("spod_fft: dtype must be F32 or F64");
+  return PLOM_ERR_UNSUPPORTED;
+}

@@ -514,8 +514,14 @@ static int matmul_impl(int prec, int transA, const T* A, int64_t lda, const T* B
   const bool fp64 = (prec == PLOM_PREC_FP64) || sizeof(T) == 8;
   if (transA == 0) {
     if constexpr (sizeof(T) == 4) {
-      if (!fp64 && tc_apply_supported(m, k, n, lda, ldc))
-        return tc_apply_tf32x3<float>(A, lda, m, k, B, ldb, n, C, ldc, nullptr, ws, st);
+      if (!fp64 && tc_apply_supported(m, k, n, lda, ldc)) {
+        int* flag = ws.take<int>(PLOM_INFO_WORDS);  // launch-wide abort word
+        if (!ws.measuring()) {
+          PLOM_REQUIRE(!ws.overflow(), PLOM_ERR_WORKSPACE, "matmul: workspace too small");
+          PLOM_CHECK_CUDA(cudaMemsetAsync(flag, 0, sizeof(int) * PLOM_INFO_WORDS, st));
+        }
+        return tc_apply_tf32x3<float>(A, lda, m, k, B, ldb, n, C, ldc, flag, ws, st);
+      }
     }
     if (ws.measuring()) return PLOM_OK;
     if (fp64) return gemm_nn<T, T, T, double>(A, lda, B, ldb, C, ldc, m, n, k, st);

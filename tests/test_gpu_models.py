@@ -1,0 +1,164 @@
+"""GPU parity of DMD and SPOD against pyLOM's own outputs (golden fixtures)
+and the oracle.
+
+pyLOM builds its Vandermonde matrices and SPOD Fourier coefficients in
+complex64 even for float64 input (see the oracle's REFERENCE_DTYPES note), so
+comparisons with its fixtures use single-precision tolerances; comparisons
+with the precision-consistent oracle (REFERENCE_DTYPES=False) use FP64 ones.
+DMD modes and amplitudes are compared through invariants of the eigenvector
+normalisation (|b|, b_j Phi_j); SPOD through L and f (Re(U) depends on the
+arbitrary phase of each complex singular vector).
+"""
+import numpy as np
+import pytest
+
+from oracle import plom_oracle as O
+
+pytestmark = pytest.mark.gpu
+torch = pytest.importorskip("torch")
+if not torch.cuda.is_available():
+    pytest.skip("needs a CUDA GPU", allow_module_level=True)
+
+import pyloworder_gb300 as P  # noqa: E402
+
+
+def _faithful(flag):
+    class _Ctx:
+        def __enter__(self):
+            self.old = O.REFERENCE_DTYPES
+            O.REFERENCE_DTYPES = flag
+
+        def __exit__(self, *a):
+            O.REFERENCE_DTYPES = self.old
+    return _Ctx()
+
+
+def _match_modes(mu, mu_ref):
+    """index map j -> k with mu[j] ~ mu_ref[k] (eigenvalue sets may differ in
+    the order of near-ties)."""
+    idx = []
+    for z in mu:
+        idx.append(int(np.argmin(np.abs(mu_ref - z))))
+    assert len(set(idx)) == len(idx)
+    return np.array(idx)
+
+
+@pytest.mark.parametrize("name,remove_mean", [("dmd_small", False), ("dmd_small_mean", True)])
+def test_dmd_golden(golden, name, remove_mean):
+    g = golden(name)
+    muR, muI, Phi, b = P.DMD.run(g["X"], float(g["r"]), remove_mean=remove_mean)
+    mu = muR + 1j * muI
+    mu_ref = g["muReal"] + 1j * g["muImag"]
+    assert mu.shape == mu_ref.shape
+    k = _match_modes(mu, mu_ref)
+    np.testing.assert_allclose(mu, mu_ref[k], rtol=1e-9, atol=1e-11)
+    # pyLOM's complex64 Vandermonde limits its amplitudes to ~1e-7 relative,
+    # amplified by cond(P) when noise modes are kept (residual truncation)
+    tol = 2e-6 if remove_mean is False else 3e-2
+    np.testing.assert_allclose(np.abs(b), np.abs(g["bJov"][k]), rtol=tol)
+    bp = b[None, :] * Phi
+    bp_ref = g["bJov"][k][None, :] * g["Phi"][:, k]
+    np.testing.assert_allclose(bp, bp_ref, atol=tol * np.abs(bp_ref).max())
+    # against the precision-consistent FP64 restatement the match is tight
+    with _faithful(False):
+        oR, oI, oPhi, ob = O.dmd_run(g["X"], float(g["r"]), remove_mean=remove_mean)
+    ko = _match_modes(mu, oR + 1j * oI)
+    np.testing.assert_allclose(np.abs(b), np.abs(ob[ko]), rtol=1e-7)
+    # same order as pyLOM: amplitudes descending, pairs positive-imag first
+    assert np.all(np.diff(np.abs(b)) <= 1e-9 * np.abs(b).max())
+    for j in range(len(muI) - 1):
+        if muI[j] != 0 and abs(muI[j] + muI[j + 1]) < 1e-9 and abs(muR[j] - muR[j + 1]) < 1e-9:
+            assert muI[j] > 0
+
+
+def test_dmd_matches_fp64_oracle(golden):
+    g = golden("dmd_small")
+    muR, muI, Phi, b = P.DMD.run(g["X"], 8, remove_mean=False)
+    with _faithful(False):
+        oR, oI, oPhi, ob = O.dmd_run(g["X"], 8, remove_mean=False)
+    mu, mu_ref = muR + 1j * muI, oR + 1j * oI
+    k = _match_modes(mu, mu_ref)
+    np.testing.assert_allclose(mu, mu_ref[k], rtol=1e-10, atol=1e-12)
+    np.testing.assert_allclose(np.abs(b), np.abs(ob[k]), rtol=1e-8)
+    bp, bp_ref = b[None, :] * Phi, ob[k][None, :] * oPhi[:, k]
+    np.testing.assert_allclose(bp, bp_ref, atol=1e-8 * np.abs(bp_ref).max())
+
+
+def test_dmd_true_eigenvalues_and_helpers(golden):
+    g = golden("dmd_small")
+    muR, muI, Phi, b = P.DMD.run(g["X"], 8, remove_mean=False)
+    lam = np.concatenate([g["lam"], np.conj(g["lam"])])
+    mu = muR + 1j * muI
+    for l in lam:
+        assert np.min(np.abs(mu - l)) < 1e-4
+    d, w = P.DMD.frequency_damping(muR, muI, 0.1)
+    od, ow = O.dmd_frequency_damping(muR, muI, 0.1)
+    np.testing.assert_allclose(d, od, rtol=1e-12)
+    np.testing.assert_allclose(w, ow, rtol=1e-12)
+    tt = np.arange(48.0)
+    Xr = P.DMD.reconstruction_jovanovic(Phi, muR, muI, tt, b)
+    with _faithful(False):
+        Xo = O.dmd_reconstruction_jovanovic(Phi, muR, muI, tt, b)
+    np.testing.assert_allclose(Xr, Xo, atol=1e-9 * np.abs(Xo).max())
+    rel = np.linalg.norm(Xr - g["X"]) / np.linalg.norm(g["X"])
+    assert rel < 1e-3
+
+
+def test_dmd_f32_mixed():
+    from tests.golden.make_golden import dmd_field
+    X, lam = dmd_field(4000, 96, 5, seed=77)
+    muR, muI, Phi, b = P.DMD.run(X.astype(np.float32), 10, remove_mean=False)
+    assert Phi.dtype == np.complex64 and muR.dtype == np.float32
+    with _faithful(False):
+        oR, oI, oPhi, ob = O.dmd_run(X, 10, remove_mean=False)
+    mu, mu_ref = muR + 1j * muI, oR + 1j * oI
+    k = _match_modes(mu, mu_ref)
+    np.testing.assert_allclose(mu, mu_ref[k], atol=1e-5)
+
+
+@pytest.mark.parametrize("tag", ["f64", "f32"])
+def test_spod_golden(golden, tag):
+    g = golden("spod_" + tag)
+    Lm, Pm, f = P.SPOD.run(g["X"], g["t"], nDFT=int(g["nDFT"]), nolap=int(g["nolap"]))
+    assert Lm.shape == g["L"].shape and Pm.shape == g["P"].shape and Lm.dtype == g["L"].dtype
+    np.testing.assert_allclose(f, g["f"], rtol=1e-12)
+    tol = 1e-4 if tag == "f64" else 2e-3  # the reference itself runs in complex64
+    np.testing.assert_allclose(Lm[:, :3], g["L"][:, :3], rtol=tol, atol=tol * 1e-3 * g["L"].max())
+
+
+def test_spod_fp64_matches_oracle(golden):
+    g = golden("spod_f64")
+    Lm, Pm, f = P.SPOD.run(g["X"], g["t"], nDFT=int(g["nDFT"]), nolap=int(g["nolap"]))
+    with _faithful(False):
+        Lo, Po, fo = O.spod_run(g["X"], g["t"], nDFT=int(g["nDFT"]), nolap=int(g["nolap"]))
+    np.testing.assert_allclose(f, fo, rtol=1e-12)
+    np.testing.assert_allclose(Lm, Lo, rtol=1e-9, atol=1e-12 * Lo.max())
+    # |P| of the leading mode per frequency is phase-independent only in norm
+    # over blocks+points of |U|; check the column norms of P are <= sqrt(nBlks)
+    assert np.all(np.linalg.norm(Pm, axis=0) <= np.sqrt(Lm.shape[1]) + 1e-9)
+
+
+def test_spod_defaults_golden(golden):
+    g = golden("spod_defaults")
+    Lm, Pm, f = P.SPOD.run(g["X"], g["t"])
+    assert Lm.shape == g["L"].shape and Pm.shape == g["P"].shape
+    np.testing.assert_allclose(f, g["f"], rtol=1e-12)
+    np.testing.assert_allclose(Lm, g["L"], rtol=1e-4, atol=1e-6 * g["L"].max())
+
+
+@pytest.mark.parametrize("nDFT,nolap", [(64, 32), (50, 10), (10, 2), (256, 128)])
+def test_spod_fft_stage(nDFT, nolap):
+    rng = np.random.default_rng(nDFT)
+    M, N = 37, 700
+    Y = rng.standard_normal((M, N))
+    nBlks = (N - nolap) // (nDFT - nolap)
+    nf = int(np.ceil(nDFT / 2) + 1)
+    win = 0.54 - 0.46 * np.cos(2 * np.pi * np.arange(nDFT) / (nDFT - 1))
+    scale = (1 / win.mean()) / nDFT / np.sqrt(nBlks)
+    Yd = torch.tensor(Y, device="cuda")
+    Q = P.SPOD.spod_fft_device(Yd, N, nDFT, nolap, nBlks, nf, win, scale).cpu().numpy()
+    for b in range(nBlks):
+        i0 = b * (nDFT - nolap)
+        F = np.fft.fft(Y[:, i0:i0 + nDFT] * win, axis=1)[:, :nf] * scale
+        F[:, 1:nf - 1] *= 2
+        np.testing.assert_allclose(Q[:, :, b].T, F, rtol=1e-11, atol=1e-12 * np.abs(F).max())
