@@ -153,6 +153,26 @@ int plom_spod_fft(int dtype, const void* Y, int64_t M, int64_t N, int64_t ldy, i
                   int64_t step, int64_t nBlks, int64_t nf, const void* window, const void* twr,
                   const void* twi, double scale, void* Q, void* stream);
 
+/* ---- allocation-free reduction product ------------------------------- */
+/* No counterpart in the reference.  For callers that cannot allocate device
+   memory -- a host integration whose device memory is owned by another
+   framework's pool, or a latency-critical loop where cudaMalloc/cudaFree
+   (which synchronise the device) are not acceptable -- this computes the same
+   product as plom_matmul(dtype, PLOM_PREC_FP64, transA = 1, ...):
+   C(m x n) = A(k x m)^T B(k x n), FP64 accumulation, F32 or F64 data, with
+   no workspace argument.  Its split-K partial sums (m * n * 8 bytes per
+   chunk, at least one chunk) live in a static device array of
+   PLOM_STATIC_SCRATCH_BYTES that every GPU loading the library holds until
+   the process exits; larger results are rejected with PLOM_ERR_WORKSPACE
+   before anything is launched.  The first call on each device looks up the
+   array's device address (cudaGetSymbolAddress, with that device current):
+   make that first call before any stream capture.  All calls share the
+   array, so calls that overlap on the GPU race; serialise them (one stream,
+   or events).  Allocates nothing and calls no allocating routine. */
+#define PLOM_STATIC_SCRATCH_BYTES (32u << 20)
+int plom_matmulp_static(int dtype, const void* A, int64_t lda, const void* B, int64_t ldb,
+                        void* C, int64_t ldc, int64_t m, int64_t n, int64_t k, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

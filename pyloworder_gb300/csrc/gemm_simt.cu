@@ -284,6 +284,56 @@ int gemm_tn(const TA* A, int64_t lda, const TB* B, int64_t ldb, TC* C, int64_t l
   return gemm_tn_batched<TA, TB, Acc, TC>(A, lda, 0, B, ldb, 0, C, ldc, 0, M, N, K, sym, 1, ws, st);
 }
 
+// The split-K product of gemm_tn (non-symmetric, one matrix) computed in a
+// caller-given scratch region of `cap` bytes instead of an arena: the chunk
+// count is lowered until the FP64 partials and the tile list fit.  Returns
+// PLOM_ERR_WORKSPACE (and launches nothing) when one chunk does not fit.
+template <typename TA, typename TB, typename TC>
+int gemm_tn_in_scratch(const TA* A, int64_t lda, const TB* B, int64_t ldb, TC* C, int64_t ldc,
+                       int64_t M, int64_t N, int64_t K, void* scratch, size_t cap,
+                       cudaStream_t st) {
+  if (M == 0 || N == 0) return PLOM_OK;
+  constexpr int BM = 64, BN = 64, BK = 16;
+  PLOM_REQUIRE(A && B && C && scratch, PLOM_ERR_ARG, "null operand");
+  TnPlan p = tn_plan(M, N, K, false, 1);
+  const size_t tiles_bytes = ((size_t)p.tm * p.tn * sizeof(int2) + 255) / 256 * 256;
+  const size_t per_chunk = (size_t)M * N * sizeof(double);
+  PLOM_REQUIRE(cap > tiles_bytes && (cap - tiles_bytes) / per_chunk >= 1, PLOM_ERR_WORKSPACE,
+               "result %lld x %lld needs %zu bytes of scratch; the static scratch holds %zu",
+               (long long)M, (long long)N, per_chunk + tiles_bytes, cap);
+  int64_t chunks = std::min<int64_t>(p.chunks, (int64_t)((cap - tiles_bytes) / per_chunk));
+  int64_t kchunk = cdiv(std::max<int64_t>(K, 1), chunks);
+  kchunk = cdiv(kchunk, BK) * BK;
+  chunks = std::max<int64_t>(1, cdiv(K, kchunk));
+  int2* tiles = reinterpret_cast<int2*>(scratch);
+  double* part = reinterpret_cast<double*>(static_cast<char*>(scratch) + tiles_bytes);
+  make_tiles_kernel<<<1, 1, 0, st>>>(tiles, (int)p.tm, (int)p.tn, 0);
+  PLOM_CHECK_LAUNCH();
+  if (K > 0) {
+    dim3 grid((unsigned)p.ntiles, (unsigned)chunks, 1u);
+    gemm_tn_kernel<TA, TB, double, BM, BN, BK><<<grid, 256, 0, st>>>(A, lda, 0, B, ldb, 0, part, M,
+                                                                     N, K, kchunk, (int)chunks,
+                                                                     tiles);
+    PLOM_CHECK_LAUNCH();
+  } else {
+    PLOM_CHECK_CUDA(cudaMemsetAsync(part, 0, per_chunk, st));  // empty sum
+    chunks = 1;
+  }
+  int64_t total = M * N;
+  int blocks = (int)std::min<int64_t>(cdiv(total, 256), (int64_t)num_sms() * 16);
+  reduce_partials_kernel<double, TC><<<blocks, 256, 0, st>>>(part, (int)chunks, M, N, 0, BM, BN, C,
+                                                             ldc, 0, 1);
+  PLOM_CHECK_LAUNCH();
+  return PLOM_OK;
+}
+template int gemm_tn_in_scratch<float, float, float>(const float*, int64_t, const float*, int64_t,
+                                                     float*, int64_t, int64_t, int64_t, int64_t,
+                                                     void*, size_t, cudaStream_t);
+template int gemm_tn_in_scratch<double, double, double>(const double*, int64_t, const double*,
+                                                        int64_t, double*, int64_t, int64_t,
+                                                        int64_t, int64_t, void*, size_t,
+                                                        cudaStream_t);
+
 // explicit instantiations used across the library
 #define NN(TA, TB, TC, ACC)                                                                  \
   template int gemm_nn<TA, TB, TC, ACC>(const TA*, int64_t, const TB*, int64_t, TC*, int64_t, \

@@ -25,6 +25,10 @@ int gemm_tn_batched(const TA* A, int64_t lda, int64_t sA, const TB* B, int64_t l
                     TC* C, int64_t ldc, int64_t sC, int64_t M, int64_t N, int64_t K, bool sym,
                     int batch, Arena& ws, cudaStream_t st);
 size_t gemm_tn_workspace(int64_t M, int64_t N, int64_t K, bool sym, size_t acc_bytes);
+template <typename TA, typename TB, typename TC>
+int gemm_tn_in_scratch(const TA* A, int64_t lda, const TB* B, int64_t ldb, TC* C, int64_t ldc,
+                       int64_t M, int64_t N, int64_t K, void* scratch, size_t cap,
+                       cudaStream_t st);
 size_t gemm_tn_workspace_batched(int64_t M, int64_t N, int64_t K, bool sym, size_t acc_bytes,
                                  int batch);
 

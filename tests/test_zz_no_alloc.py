@@ -1,0 +1,69 @@
+"""plom_matmulp_static, the allocation-free variant of the reduction product
+C = A^T B (matmulp(A.T, B)), for callers that cannot allocate device memory
+(another framework owns the device's memory pool, or a loop must not pay the
+device synchronisation of cudaMalloc/cudaFree).  It keeps its split-K
+partials in a static device array instead of a caller workspace.
+
+Checked through the C ABI against the existing entry point plom_matmul
+(transA = 1, FP64 accumulation) on two calls in a row, with the tolerance the
+other product tests use; a result too large for the static array must be
+rejected before anything runs.  This file is collected last on purpose.
+"""
+import ctypes
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+torch = pytest.importorskip("torch")
+if not torch.cuda.is_available():
+    pytest.skip("needs a CUDA GPU", allow_module_level=True)
+
+from pyloworder_gb300 import _lib as L  # noqa: E402
+
+STATIC_BYTES = 32 << 20
+
+
+def _existing(lib, dt, A, B, m, n, k):
+    C = torch.empty((m, n), dtype=A.dtype, device="cuda")
+    ws = L.workspace(lib.plom_matmul_workspace(dt, L.PREC_FP64, 1, m, n, k))
+    st = lib.plom_matmul(dt, L.PREC_FP64, 1, L.ptr(A), m, L.ptr(B), n, L.ptr(C), n, m, n, k,
+                         L.ptr(ws), ws.numel(), L.stream_ptr())
+    assert st == 0, lib.plom_last_error_string()
+    return C
+
+
+def _static(lib, dt, A, B, m, n, k):
+    C = torch.full((m, n), float("nan"), dtype=A.dtype, device="cuda")
+    st = lib.plom_matmulp_static(dt, L.ptr(A), m, L.ptr(B), n, L.ptr(C), n, m, n, k, L.stream_ptr())
+    assert st == 0, lib.plom_last_error_string()
+    return C
+
+
+@pytest.mark.parametrize("dtype,code,rtol", [(torch.float64, L.F64, 1e-12), (torch.float32, L.F32, 2e-5)])
+def test_static_scratch_matches_existing_entry_point(dtype, code, rtol):
+    lib = L.load()
+    g = torch.Generator(device="cuda")
+    g.manual_seed(11)
+    # two calls in a row, different shapes: the second must not see the first's leftovers
+    for (m, n, k) in [(96, 40, 50000), (64, 80, 123457)]:
+        A = torch.randn((k, m), dtype=dtype, device="cuda", generator=g)
+        B = torch.randn((k, n), dtype=dtype, device="cuda", generator=g)
+        ref = _existing(lib, code, A, B, m, n, k)
+        got = _static(lib, code, A, B, m, n, k)
+        torch.cuda.synchronize()
+        scale = float(ref.abs().max())
+        np.testing.assert_allclose(got.cpu().numpy(), ref.cpu().numpy(), rtol=rtol,
+                                   atol=rtol * scale)
+
+
+def test_result_beyond_static_scratch_is_rejected():
+    lib = L.load()
+    m = n = 2048  # 2048 * 2048 * 8 bytes = 32 MiB of partials + tile list > the array
+    A = torch.zeros((4, m), dtype=torch.float64, device="cuda")
+    B = torch.zeros((4, n), dtype=torch.float64, device="cuda")
+    C = torch.zeros((m, n), dtype=torch.float64, device="cuda")
+    st = lib.plom_matmulp_static(L.F64, L.ptr(A), m, L.ptr(B), n, L.ptr(C), n, m, n, 4,
+                                 L.stream_ptr())
+    assert st == -2  # PLOM_ERR_WORKSPACE
+    assert b"static scratch" in lib.plom_last_error_string()
