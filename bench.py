@@ -221,6 +221,7 @@ def run_ours(args):
     ms = ev0.elapsed_time(ev1) / args.steps
     ms = max_over_ranks(ms, world)
     kernels = prof.stop() if prof else {}
+    info_words = L.last_info
     value = algorithmic_bytes(m, n) * world / (ms * 1e-3) / 1e9
 
     # accuracy of the mixed form against the FP64 form on a row sample
@@ -297,7 +298,9 @@ def run_ours(args):
                            "parallelism": "replicas" if world > 1 else "single"},
                 "clocks": clk.summary(), "gpu_launches": sum(k["count"] for k in kernels.values()) if kernels else None,
                 "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "fp64_form": fp64,
-                "accuracy_vs_fp64": acc, "kernels": kernels}
+                "accuracy_vs_fp64": acc, "kernels": kernels,
+                "info": {"cholesky_shift_escalations": info_words[1] if info_words else None,
+                         "jacobi_sweeps": info_words[2] if info_words else None}}
         print(json.dumps(line), flush=True)
     if world > 1:
         import torch.distributed as dist

@@ -201,8 +201,13 @@ def new_info():
     return t.zeros(INFO_WORDS, dtype=t.int32, device="cuda")
 
 
+last_info = None  # info words of the most recent checked call (diagnostics)
+
+
 def check_info(info, what):
+    global last_info
     v = info.cpu().tolist()
+    last_info = v
     if v[0] != 0:
         raise PlomError(f"{what}: {NUM_MESSAGES.get(v[0], 'numerical failure')} (info={v})")
     return v

@@ -380,7 +380,7 @@ __device__ __forceinline__ void rr_pair(int step, int k, int np, int& a, int& b)
   }
 }
 
-__global__ void __launch_bounds__(256) jacobi_coop_kernel(const double* __restrict__ A, int n,
+__global__ void __launch_bounds__(128) jacobi_coop_kernel(const double* __restrict__ A, int n,
                                                           int batch, int cplx, JacState js,
                                                           double* __restrict__ S,
                                                           double* __restrict__ U,
@@ -412,7 +412,9 @@ __global__ void __launch_bounds__(256) jacobi_coop_kernel(const double* __restri
 
   const int np = n + (n & 1);
   const int pairs = np / 2;
-  const double tol = 2.220446049250313e-16 * sqrt((double)n) ;
+  // rotate while |a_p^H a_q| > n eps ||a_p|| ||a_q||: below that the pair is
+  // orthogonal to working precision (one-sided Jacobi stopping rule)
+  const double tol = 2.220446049250313e-16 * (double)n;
   int sweep = 0;
   for (; sweep < JACOBI_MAX_SWEEPS; ++sweep) {
     int myrot = 0;
@@ -561,13 +563,15 @@ int jacobi_svd(const double* A, int n, int batch, int cplx, double* S, double* U
   PLOM_REQUIRE(!ws.overflow(), PLOM_ERR_WORKSPACE, "jacobi: workspace too small");
   PLOM_REQUIRE(A && S && U && VH && info, PLOM_ERR_ARG, "jacobi: null pointer");
   const int np = n + (n & 1);
-  int want = (int)std::max<int64_t>(1, cdiv((int64_t)np / 2 * batch, 8));
-  int blocks = coop_blocks((const void*)jacobi_coop_kernel, 256, 0, want);
+  // one warp per column pair, 4 warps per CTA: spreads the FP64 work over
+  // as many SMs as there are pairs / 4
+  int want = (int)std::max<int64_t>(1, cdiv((int64_t)np / 2 * batch, 4));
+  int blocks = coop_blocks((const void*)jacobi_coop_kernel, 128, 0, want);
   ProfScope prof("jacobi_svd_fp64", st, 0.0, 24.0 * n * n * batch * (cplx ? 2 : 1));
   void* args[] = {(void*)&A, (void*)&n, (void*)&batch, (void*)&cplx, (void*)&js,
                   (void*)&S, (void*)&U, (void*)&VH, (void*)&info};
   PLOM_CHECK_CUDA(cudaLaunchCooperativeKernel((const void*)jacobi_coop_kernel, dim3(blocks),
-                                              dim3(256), args, 0, st));
+                                              dim3(128), args, 0, st));
   return PLOM_OK;
 }
 
