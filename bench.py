@@ -13,6 +13,14 @@ s*m*n (write U), s = 4.
 Usage: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 Multi-GPU: the path runs one replica per GPU ("replicas only"); value is the
 sum over ranks of matrices processed / max-over-ranks time.
+
+Besides the timed step, rank 0 reports (outside the timed region): per-kernel
+CUDA-event timings and the roofline of the dominant kernel, the accuracy of
+the mixed form against the plain FP64 GPU form and that form's throughput on
+a row sample, the end-to-end rate through the public API from pinned host
+memory, the CPU oracle on a row sample, and the POD/DMD/SPOD serving mix
+(jobs/s, p50/p99 latency).  --quick leaves those side legs out; it never
+changes the timed step.
 """
 from __future__ import annotations
 
@@ -43,6 +51,47 @@ def algorithmic_bytes(m, n, s=4):
 
 def algorithmic_flops(m, n):
     return 4.0 * m * n * n
+
+
+def ncu_traffic(kernel):
+    """DRAM bytes per launch of `kernel` for the bench workload, from the
+    committed ncu summary (profiles/dram_traffic.txt: 'kernel bytes_per_launch')."""
+    try:
+        with open(os.path.join(ROOT, "profiles", "dram_traffic.txt")) as f:
+            for line in f:
+                parts = line.split()
+                if len(parts) >= 2 and parts[0] == kernel and not line.startswith("#"):
+                    return float(parts[1])
+    except OSError:
+        pass
+    return None
+
+
+def serving_leg(njobs=48, seed=5, slots=4, budget=150e9):
+    """Serving mix (config 5 distribution, bounded sample): saturation
+    throughput and Poisson-arrival latency, mixed form; FP64 form on the
+    subset of small jobs for the speed ratio."""
+    from pyloworder_gb300 import serving
+    jobs = serving.make_mix(njobs, seed=seed)
+    warm = serving.make_mix(3, seed=seed + 1, m_range=(16384, 65536), n_range=(32, 64))
+    serving.Server(budget, slots).run(warm, realtime=False)
+    _, sat = serving.Server(budget, slots).run(jobs, realtime=False)
+    rate = 0.7 * sat["jobs_per_s"]
+    jobs2 = serving.make_mix(njobs, seed=seed, rate=rate)
+    _, poi = serving.Server(budget, slots).run(jobs2, realtime=True)
+    small = [j for j in serving.make_mix(njobs, seed=seed) if j.m * j.n <= 2**24][:12]
+    for j in small:
+        j.arrival = 0.0
+    _, smx = serving.Server(budget, slots, precision="mixed").run(small, realtime=False)
+    _, s64 = serving.Server(budget, slots, precision="fp64").run(small, realtime=False)
+    return {"workload": f"{njobs} POD/DMD/SPOD jobs, m log-uniform 16384-4194304, n log-uniform "
+                        f"32-1024, FP32, {slots} streams, {budget / 1e9:.0f} GB admission budget",
+            "jobs_per_s": sat["jobs_per_s"], "saturation": sat,
+            "poisson_rate_jobs_per_s": rate, "p50_ms": poi["p50_ms"], "p99_ms": poi["p99_ms"],
+            "poisson": poi,
+            "mixed_vs_fp64_small_jobs": {"jobs": len(small), "mixed_wall_s": smx["wall_s"],
+                                         "fp64_wall_s": s64["wall_s"],
+                                         "speedup": s64["wall_s"] / smx["wall_s"]}}
 
 
 def peaks():
@@ -224,21 +273,25 @@ def run_ours(args):
     info_words = L.last_info
     value = algorithmic_bytes(m, n) * world / (ms * 1e-3) / 1e9
 
-    # accuracy of the mixed form against the FP64 form on a row sample
+    # accuracy of the mixed form against the FP64 form on a row sample: every
+    # 8th point, so the sample spans the whole domain and keeps the 64 modes
+    # distinct (a contiguous block of rows would be a thin strip of the grid)
     acc = {}
     fp64 = {}
     if rank == 0 and not args.quick:
-        ms_rows = min(m, FP64_SAMPLE_ROWS)
-        Ys = Y[:ms_rows]
+        stride = max(1, m // FP64_SAMPLE_ROWS)
+        Ys = Y[::stride]
+        ms_rows = Ys.shape[0]
+        ldys = n * stride
         torch.cuda.synchronize()
-        P.vmmath.tsqr_svd_device(Ys[:65536], n, "fp64")  # warm
+        P.vmmath.tsqr_svd_device(Ys[:65536], ldys, "fp64")  # warm
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record(st)
-        U64, S64, V64 = P.vmmath.tsqr_svd_device(Ys, n, "fp64")
+        U64, S64, V64 = P.vmmath.tsqr_svd_device(Ys, ldys, "fp64")
         e1.record(st)
         torch.cuda.synchronize()
         t64 = e0.elapsed_time(e1)
-        Um, Sm, Vm = P.vmmath.tsqr_svd_device(Ys, n, "mixed")
+        Um, Sm, Vm = P.vmmath.tsqr_svd_device(Ys, ldys, "mixed")
         torch.cuda.synchronize()
         s64 = S64.double().cpu().numpy()
         sm = Sm.double().cpu().numpy()
@@ -246,7 +299,7 @@ def run_ours(args):
         a = Um[:, :k].double()
         b = U64[:, :k].double()
         cosines = torch.linalg.svdvals(a.T @ b).cpu().numpy()
-        acc = {"sample_rows": ms_rows,
+        acc = {"sample_rows": ms_rows, "sample": f"every {stride}th point",
                "sigma_rel_err_retained": float(np.max(np.abs(sm[:k] - s64[:k]) / s64[:k])),
                "subspace_angle_retained": float(np.arccos(min(1.0, cosines.min()))),
                "orth_retained": float(torch.linalg.matrix_norm(
@@ -281,14 +334,22 @@ def run_ours(args):
 
     hbm, bf16, how = peaks()
     cpu = cpu_baseline() if (rank == 0 and not args.quick and world == 1) else None
+    serve = serving_leg() if (rank == 0 and not args.quick) else None
     if rank == 0:
         roof = None
         if kernels:
-            top = max(kernels.values(), key=lambda k: k["ms_total"])
+            tc = [k for k in kernels.values() if k["name"].startswith("tc_")]
+            top = max(tc or kernels.values(), key=lambda k: k["ms_total"])
+            per_launch_ms = top["ms_total"] / top["count"]
             achieved = top["flops"] / (top["ms_total"] * 1e-3) / 1e12
             roof = {"bound": "tensor", "kernel": top["name"], "achieved": achieved, "peak": bf16,
-                    "unit": "TFLOP/s", "frac": achieved / bf16, "traffic": None,
-                    "peak_source": how}
+                    "unit": "TFLOP/s", "frac": achieved / bf16,
+                    "traffic": ncu_traffic(top["name"]), "peak_source": how,
+                    "per_launch_ms": per_launch_ms,
+                    "algorithmic_flops_per_launch": top["flops"] / top["count"],
+                    "note": "achieved counts algorithmic FLOPs; the kernel issues 3 TF32 UMMA "
+                            "per product term (hi*hi + hi*lo + lo*hi)",
+                    "tf32_pipe_tflops": 3 * achieved}
         line = {"metric": "TSQR-SVD GB/s", "value": value, "unit": "GB/s", "n_gpus": world,
                 "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
@@ -298,7 +359,7 @@ def run_ours(args):
                            "parallelism": "replicas" if world > 1 else "single"},
                 "clocks": clk.summary(), "gpu_launches": sum(k["count"] for k in kernels.values()) if kernels else None,
                 "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "fp64_form": fp64,
-                "accuracy_vs_fp64": acc, "kernels": kernels,
+                "accuracy_vs_fp64": acc, "serving": serve, "kernels": kernels,
                 "info": {"cholesky_shift_escalations": info_words[1] if info_words else None,
                          "jacobi_sweeps": info_words[2] if info_words else None}}
         print(json.dumps(line), flush=True)
@@ -308,8 +369,76 @@ def run_ours(args):
     return 0
 
 
+# ---------------------------------------------------------------------------
+# other configurations (not the headline line): randomized SVD (config 2),
+# DMD (config 3), SPOD (config 4)
+# ---------------------------------------------------------------------------
+
+def run_other(args):
+    import torch
+    import pyloworder_gb300 as P
+    from pyloworder_gb300 import _lib as L, datagen
+    L.load()
+    st = torch.cuda.current_stream()
+    out = {"n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "higher_is_better": True,
+           "scaling": "weak", "vs_baseline": None, "data": "synthetic", "dtype": "f32"}
+    if args.workload == "randomized":
+        m, n, r, q = args.m, N_FULL, 80, 2
+        nx, ny = datagen.grid_for_points(m)
+        X = datagen.pod_field_device(nx, ny, n, NMODES, seed=SEED, noise=1e-5, amp_pow=1.5)
+        Y, _, _ = P.vmmath.remove_mean_device(X, n)
+        del X
+        step = lambda: P.vmmath.randomized_svd_device(Y, n, r, q, 7, "mixed")  # noqa: E731
+        nbytes = 4 * m * n * (2 + 2 * q) + 4 * m * r
+        out.update(metric="randomized_svd GB/s", unit="GB/s",
+                   config={"workload": f"randomized_svd {m}x{n} f32, r={r} (64+16), q={q}",
+                           "precision": "mixed"})
+    elif args.workload == "dmd":
+        m, n, r = 2_097_152, 512, 32
+        X, lam = datagen.dmd_field_device(m, n)
+        step = lambda: P.DMD.run_device(X, n, r, remove_mean=False, precision="mixed")  # noqa: E731
+        nbytes = 4 * m * n + 2 * 4 * m * (n - 1) + 8 * m * r
+        out.update(metric="DMD GB/s", unit="GB/s",
+                   config={"workload": f"DMD.run {m}x{n} f32, r={r}", "precision": "mixed"})
+    else:
+        M, N = 1_048_576, 8192
+        X = datagen.spod_field_device(M, N)
+        t = np.arange(N, dtype=np.float64)
+        step = lambda: P.SPOD.run_device(X, N, t, nDFT=256, nolap=128, precision="mixed")  # noqa: E731
+        nbytes = 4 * M * N + 4 * M * 63 * 129
+        out.update(metric="SPOD GB/s", unit="GB/s",
+                   config={"workload": f"SPOD.run {M}x{N} f32, nDFT=256, nolap=128 (63 blocks, "
+                                       "129 frequencies), Hamming window", "precision": "mixed"})
+    for _ in range(args.warmup):
+        res = step()
+    torch.cuda.synchronize()
+    prof = L.Profiler()
+    prof.start()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(0) as clk:
+        e0.record(st)
+        for _ in range(args.steps):
+            res = step()
+        e1.record(st)
+        torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / args.steps
+    kernels = prof.stop()
+    out.update(value=nbytes / (ms * 1e-3) / 1e9, ms_per_step=ms, clocks=clk.summary(),
+               kernels=kernels, gpu_launches=sum(k["count"] for k in kernels.values()))
+    if args.workload == "dmd":
+        mu = (res[0].double() + 1j * res[1].double()).cpu().numpy()
+        true = np.concatenate([lam, np.conj(lam)])
+        out["max_abs_lambda_err"] = float(max(np.min(np.abs(mu - z)) for z in true))
+    if args.workload == "randomized":
+        out["sigma_head"] = res[1][:4].double().cpu().numpy().tolist()
+    print(json.dumps(out), flush=True)
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
+    ap.add_argument("--workload", default="tsqr_svd",
+                    choices=["tsqr_svd", "randomized", "dmd", "spod"])
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
@@ -319,6 +448,8 @@ def main():
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
+    if args.workload != "tsqr_svd":
+        return run_other(args)
     return run_ours(args)
 
 

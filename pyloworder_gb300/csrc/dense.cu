@@ -360,12 +360,13 @@ int trtri_upper(const double* R, double* W, int n, int batch, Arena& ws, cudaStr
 // ---------------------------------------------------------------------------
 // one-sided Jacobi SVD (Hestenes), real or complex, cooperative
 // ---------------------------------------------------------------------------
+template <typename T>
 struct JacState {
-  double* At;   // batch x n x (n*cw): rows = columns of A
-  double* Vt;   // batch x n x (n*cw): rows = columns of V
+  T* At;        // batch x n x (n*cw): rows = columns of A
+  T* Vt;        // batch x n x (n*cw): rows = columns of V
   int* counts;  // [JACOBI_MAX_SWEEPS]
   int* perm;    // batch x n
-  double* nrm;  // batch x n
+  T* nrm;       // batch x n
 };
 
 __device__ __forceinline__ void rr_pair(int step, int k, int np, int& a, int& b) {
@@ -380,8 +381,12 @@ __device__ __forceinline__ void rr_pair(int step, int k, int np, int& a, int& b)
   }
 }
 
+// T = double: the SVD itself.  T = float: a fast pass whose accumulated
+// rotations (js.Vt) precondition the FP64 pass; with S == nullptr the output
+// stage is skipped.
+template <typename T>
 __global__ void __launch_bounds__(128) jacobi_coop_kernel(const double* __restrict__ A, int n,
-                                                          int batch, int cplx, JacState js,
+                                                          int batch, int cplx, JacState<T> js,
                                                           double* __restrict__ S,
                                                           double* __restrict__ U,
                                                           double* __restrict__ VH, int* info) {
@@ -400,12 +405,12 @@ __global__ void __launch_bounds__(128) jacobi_coop_kernel(const double* __restri
     int64_t b = e / ((int64_t)n * n), r = e % ((int64_t)n * n);
     int i = (int)(r / n), j = (int)(r % n);
     const double* src = A + b * mat + (int64_t)i * rl + (int64_t)j * cw;
-    double* dst = js.At + b * mat + (int64_t)j * rl + (int64_t)i * cw;
-    dst[0] = src[0];
-    if (cplx) dst[1] = src[1];
-    double* v = js.Vt + b * mat + (int64_t)i * rl + (int64_t)j * cw;
-    v[0] = (i == j) ? 1.0 : 0.0;
-    if (cplx) v[1] = 0.0;
+    T* dst = js.At + b * mat + (int64_t)j * rl + (int64_t)i * cw;
+    dst[0] = (T)src[0];
+    if (cplx) dst[1] = (T)src[1];
+    T* v = js.Vt + b * mat + (int64_t)i * rl + (int64_t)j * cw;
+    v[0] = (i == j) ? T(1) : T(0);
+    if (cplx) v[1] = T(0);
   }
   if (gtid < JACOBI_MAX_SWEEPS) js.counts[gtid] = 0;
   grid.sync();
@@ -414,7 +419,7 @@ __global__ void __launch_bounds__(128) jacobi_coop_kernel(const double* __restri
   const int pairs = np / 2;
   // rotate while |a_p^H a_q| > n eps ||a_p|| ||a_q||: below that the pair is
   // orthogonal to working precision (one-sided Jacobi stopping rule)
-  const double tol = 2.220446049250313e-16 * (double)n;
+  const T tol = (sizeof(T) == 8 ? T(2.220446049250313e-16) : T(1.1920929e-07)) * (T)n;
   int sweep = 0;
   for (; sweep < JACOBI_MAX_SWEEPS; ++sweep) {
     int myrot = 0;
@@ -429,19 +434,19 @@ __global__ void __launch_bounds__(128) jacobi_coop_kernel(const double* __restri
           p = q;
           q = t;
         }
-        double* ap = js.At + b * mat + (int64_t)p * rl;
-        double* aq = js.At + b * mat + (int64_t)q * rl;
-        double alpha = 0.0, beta = 0.0, gr = 0.0, gi = 0.0;
+        T* ap = js.At + b * mat + (int64_t)p * rl;
+        T* aq = js.At + b * mat + (int64_t)q * rl;
+        T alpha = 0, beta = 0, gr = 0, gi = 0;
         if (!cplx) {
           for (int64_t i = lane; i < n; i += 32) {
-            double x = ap[i], y = aq[i];
+            T x = ap[i], y = aq[i];
             alpha = fma(x, x, alpha);
             beta = fma(y, y, beta);
             gr = fma(x, y, gr);
           }
         } else {
           for (int64_t i = lane; i < n; i += 32) {
-            double xr = ap[2 * i], xi = ap[2 * i + 1], yr = aq[2 * i], yi = aq[2 * i + 1];
+            T xr = ap[2 * i], xi = ap[2 * i + 1], yr = aq[2 * i], yi = aq[2 * i + 1];
             alpha += xr * xr + xi * xi;
             beta += yr * yr + yi * yi;
             gr += xr * yr + xi * yi;  // conj(x) * y
@@ -452,33 +457,33 @@ __global__ void __launch_bounds__(128) jacobi_coop_kernel(const double* __restri
         beta = warp_sum(beta);
         gr = warp_sum(gr);
         if (cplx) gi = warp_sum(gi);
-        const double gabs = cplx ? hypot(gr, gi) : fabs(gr);
-        if (!(alpha > 0.0 && beta > 0.0) || !(gabs > tol * sqrt(alpha) * sqrt(beta))) continue;
+        const T gabs = cplx ? hypot(gr, gi) : fabs(gr);
+        if (!(alpha > T(0) && beta > T(0)) || !(gabs > tol * sqrt(alpha) * sqrt(beta))) continue;
         ++myrot;
-        const double zeta = (beta - alpha) / (2.0 * gabs);
-        const double t = copysign(1.0, zeta) / (fabs(zeta) + sqrt(1.0 + zeta * zeta));
-        const double c = 1.0 / sqrt(1.0 + t * t), s = c * t;
+        const T zeta = (beta - alpha) / (T(2) * gabs);
+        const T t = copysign(T(1), zeta) / (fabs(zeta) + sqrt(T(1) + zeta * zeta));
+        const T c = T(1) / sqrt(T(1) + t * t), s = c * t;
         // phase e^{i phi} = gamma/|gamma| (real: sign of gamma)
-        const double er = cplx ? gr / gabs : copysign(1.0, gr), ei = cplx ? gi / gabs : 0.0;
-        double* vp = js.Vt + b * mat + (int64_t)p * rl;
-        double* vq = js.Vt + b * mat + (int64_t)q * rl;
+        const T er = cplx ? gr / gabs : copysign(T(1), gr), ei = cplx ? gi / gabs : T(0);
+        T* vp = js.Vt + b * mat + (int64_t)p * rl;
+        T* vq = js.Vt + b * mat + (int64_t)q * rl;
         // a' = c a - s e^{-i phi} b ;  b' = s e^{i phi} a + c b
         for (int side = 0; side < 2; ++side) {
-          double* x = side ? vp : ap;
-          double* y = side ? vq : aq;
+          T* x = side ? vp : ap;
+          T* y = side ? vq : aq;
           if (!cplx) {
             for (int64_t i = lane; i < n; i += 32) {
-              double xv = x[i], yv = y[i];
+              T xv = x[i], yv = y[i];
               x[i] = c * xv - s * er * yv;
               y[i] = s * er * xv + c * yv;
             }
           } else {
             for (int64_t i = lane; i < n; i += 32) {
-              double xr = x[2 * i], xi = x[2 * i + 1], yr = y[2 * i], yi = y[2 * i + 1];
+              T xr = x[2 * i], xi = x[2 * i + 1], yr = y[2 * i], yi = y[2 * i + 1];
               // e^{-i phi} y = (er - i ei)(yr + i yi)
-              double zr = er * yr + ei * yi, zi = er * yi - ei * yr;
+              T zr = er * yr + ei * yi, zi = er * yi - ei * yr;
               // e^{i phi} x = (er + i ei)(xr + i xi)
-              double wr = er * xr - ei * xi, wi = er * xi + ei * xr;
+              T wr = er * xr - ei * xi, wi = er * xi + ei * xr;
               x[2 * i] = c * xr - s * zr;
               x[2 * i + 1] = c * xi - s * zi;
               y[2 * i] = s * wr + c * yr;
@@ -493,27 +498,28 @@ __global__ void __launch_bounds__(128) jacobi_coop_kernel(const double* __restri
     grid.sync();
     if (js.counts[sweep] == 0) break;
   }
+  if (S == nullptr) return;  // preconditioning pass: only js.Vt is wanted
   if (gtid == 0) {
     info[ST_SWEEPS] = sweep + 1;
     if (sweep >= JACOBI_MAX_SWEEPS) atomicMax(&info[ST_FAIL], PLOM_NUM_JACOBI);
   }
   // column norms
   for (int64_t task = gwarp; task < (int64_t)batch * n; task += nwarps) {
-    const double* a = js.At + (task / n) * mat + (task % n) * rl;
+    const T* a = js.At + (task / n) * mat + (task % n) * rl;
     double s = 0.0;
-    for (int64_t i = lane; i < rl; i += 32) s = fma(a[i], a[i], s);
+    for (int64_t i = lane; i < rl; i += 32) s = fma((double)a[i], (double)a[i], s);
     s = warp_sum(s);
-    if (lane == 0) js.nrm[task] = sqrt(s);
+    if (lane == 0) js.nrm[task] = (T)sqrt(s);
   }
   grid.sync();
   // descending order: rank of each column (ties broken by index)
   for (int64_t e = gtid; e < (int64_t)batch * n; e += gthreads) {
     const int64_t b = e / n;
     const int j = (int)(e % n);
-    const double sj = js.nrm[e];
+    const T sj = js.nrm[e];
     int rank = 0;
     for (int k = 0; k < n; ++k) {
-      double sk = js.nrm[b * n + k];
+      T sk = js.nrm[b * n + k];
       rank += (sk > sj) || (sk == sj && k < j);
     }
     js.perm[b * n + rank] = j;
@@ -525,54 +531,129 @@ __global__ void __launch_bounds__(128) jacobi_coop_kernel(const double* __restri
     const int64_t r = e % ((int64_t)n * n);
     const int k = (int)(r / n), i = (int)(r % n);
     const int src = js.perm[b * n + k];
-    const double sk = js.nrm[b * n + src];
+    const double sk = (double)js.nrm[b * n + src];
     if (i == 0) S[b * n + k] = sk;
     const double inv = sk > 0.0 ? 1.0 / sk : 0.0;
-    const double* a = js.At + b * mat + (int64_t)src * rl + (int64_t)i * cw;
+    const T* a = js.At + b * mat + (int64_t)src * rl + (int64_t)i * cw;
     double* u = U + b * mat + (int64_t)i * rl + (int64_t)k * cw;
-    u[0] = a[0] * inv;
-    if (cplx) u[1] = a[1] * inv;
-    const double* v = js.Vt + b * mat + (int64_t)src * rl + (int64_t)i * cw;
+    u[0] = (double)a[0] * inv;
+    if (cplx) u[1] = (double)a[1] * inv;
+    const T* v = js.Vt + b * mat + (int64_t)src * rl + (int64_t)i * cw;
     double* vh = VH + b * mat + (int64_t)k * rl + (int64_t)i * cw;
-    vh[0] = v[0];
-    if (cplx) vh[1] = -v[1];
+    vh[0] = (double)v[0];
+    if (cplx) vh[1] = -(double)v[1];
   }
 }
 
-size_t dense_workspace(int n, int batch, int cplx) {
-  Arena a(nullptr, 0);
-  const size_t mat = (size_t)n * n * (cplx ? 2 : 1);
-  a.take<double>(mat * batch);
-  a.take<double>(mat * batch);
-  a.take<int>(JACOBI_MAX_SWEEPS);
-  a.take<int>((size_t)batch * n);
-  a.take<double>((size_t)batch * n);
-  return a.off + 256;
-}
+// FP32 pre-pass + FP64 finish is used for real matrices from this size on
+constexpr int JACOBI_PRECOND_MIN_N = 128;
 
-int jacobi_svd(const double* A, int n, int batch, int cplx, double* S, double* U, double* VH,
-               int* info, Arena& ws, cudaStream_t st) {
-  JacState js;
-  const size_t mat = (size_t)n * n * (cplx ? 2 : 1);
-  js.At = ws.take<double>(mat * batch);
-  js.Vt = ws.take<double>(mat * batch);
-  js.counts = ws.take<int>(JACOBI_MAX_SWEEPS);
-  js.perm = ws.take<int>((size_t)batch * n);
-  js.nrm = ws.take<double>((size_t)batch * n);
-  if (ws.measuring() || n == 0 || batch == 0) return PLOM_OK;
-  PLOM_REQUIRE(!ws.overflow(), PLOM_ERR_WORKSPACE, "jacobi: workspace too small");
-  PLOM_REQUIRE(A && S && U && VH && info, PLOM_ERR_ARG, "jacobi: null pointer");
+template <typename T>
+static int jacobi_launch(const double* A, int n, int batch, int cplx, JacState<T>& js, double* S,
+                         double* U, double* VH, int* info, cudaStream_t st) {
   const int np = n + (n & 1);
   // one warp per column pair, 4 warps per CTA: spreads the FP64 work over
   // as many SMs as there are pairs / 4
   int want = (int)std::max<int64_t>(1, cdiv((int64_t)np / 2 * batch, 4));
-  int blocks = coop_blocks((const void*)jacobi_coop_kernel, 128, 0, want);
-  ProfScope prof("jacobi_svd_fp64", st, 0.0, 24.0 * n * n * batch * (cplx ? 2 : 1));
+  int blocks = coop_blocks((const void*)jacobi_coop_kernel<T>, 128, 0, want);
   void* args[] = {(void*)&A, (void*)&n, (void*)&batch, (void*)&cplx, (void*)&js,
                   (void*)&S, (void*)&U, (void*)&VH, (void*)&info};
-  PLOM_CHECK_CUDA(cudaLaunchCooperativeKernel((const void*)jacobi_coop_kernel, dim3(blocks),
+  ProfScope prof(sizeof(T) == 8 ? "jacobi_svd_fp64" : "jacobi_pass_fp32", st, 0.0,
+                 (double)sizeof(T) * 3.0 * n * n * batch * (cplx ? 2 : 1));
+  PLOM_CHECK_CUDA(cudaLaunchCooperativeKernel((const void*)jacobi_coop_kernel<T>, dim3(blocks),
                                               dim3(128), args, 0, st));
   return PLOM_OK;
+}
+
+template <typename T>
+static void carve_jac(Arena& ws, JacState<T>& js, int n, int batch, int cplx) {
+  const size_t mat = (size_t)n * n * (cplx ? 2 : 1);
+  js.At = ws.take<T>(mat * batch);
+  js.Vt = ws.take<T>(mat * batch);
+  js.counts = ws.take<int>(JACOBI_MAX_SWEEPS);
+  js.perm = ws.take<int>((size_t)batch * n);
+  js.nrm = ws.take<T>((size_t)batch * n);
+}
+
+size_t dense_workspace(int n, int batch, int cplx) {
+  Arena a(nullptr, 0);
+  JacState<double> js;
+  carve_jac(a, js, n, batch, cplx);
+  return a.off + 256;
+}
+
+// Real n x n SVD with an FP32 pre-pass: one-sided Jacobi in FP32 yields V0;
+// V0 is re-orthogonalised in FP64 (one CholeskyQR step), A1 = A V0 has
+// nearly orthogonal columns, and the FP64 Jacobi on A1 converges in a few
+// sweeps; V = V0 V1.
+static int jacobi_svd_precond(const double* A, int n, double* S, double* U, double* VH, int* info,
+                              Arena& ws, cudaStream_t st) {
+  const size_t nn = (size_t)n * n;
+  JacState<float> j32;
+  carve_jac(ws, j32, n, 1, 0);
+  double* V0 = ws.take<double>(nn);
+  double* G = ws.take<double>(nn);
+  double* Rv = ws.take<double>(nn);
+  double* Wv = ws.take<double>(nn);
+  double* V0n = ws.take<double>(nn);
+  double* A1 = ws.take<double>(nn);
+  double* VH1 = ws.take<double>(nn);
+  double* V0nT = ws.take<double>(nn);
+  const size_t mark = ws.off;
+  size_t need = mark;
+  // FP64 pass state (reuses the scratch after the small FP64 products)
+  JacState<double> j64;
+  carve_jac(ws, j64, n, 1, 0);
+  need = std::max(need, ws.off);
+  ws.off = mark;
+  if (ws.measuring()) {
+    gemm_tn<double, double, double, double>(V0, n, V0, n, G, n, n, n, n, true, ws, st);
+    need = std::max(need, ws.off);
+    ws.off = mark;
+    chol_shifted(G, Rv, n, 1, 0.0, 1e-12, info, ws, st);
+    need = std::max(need, ws.off);
+    ws.off = mark;
+    trtri_upper(Rv, Wv, n, 1, ws, st);
+    ws.off = std::max(need, ws.off);
+    return PLOM_OK;
+  }
+  PLOM_REQUIRE(!ws.overflow(), PLOM_ERR_WORKSPACE, "jacobi: workspace too small");
+  PLOM_TRY(jacobi_launch<float>(A, n, 1, 0, j32, nullptr, nullptr, nullptr, info, st));
+  {
+    double* Vt64 = A1;  // temporarily: rows = v_k in FP64
+    PLOM_TRY((convert<float, double>(j32.Vt, Vt64, (int64_t)nn, st)));
+    PLOM_TRY(transpose_f64(Vt64, V0, n, n, 1, st));  // columns = v_k
+  }
+  PLOM_TRY((gemm_tn<double, double, double, double>(V0, n, V0, n, G, n, n, n, n, true, ws, st)));
+  need = std::max(need, ws.off);
+  ws.off = mark;
+  PLOM_TRY(chol_shifted(G, Rv, n, 1, 0.0, 1e-12, info, ws, st));
+  need = std::max(need, ws.off);
+  ws.off = mark;
+  PLOM_TRY(trtri_upper(Rv, Wv, n, 1, ws, st));
+  need = std::max(need, ws.off);
+  ws.off = mark;
+  PLOM_TRY((gemm_nn<double, double, double, double>(V0, n, Wv, n, V0n, n, n, n, n, st)));
+  PLOM_TRY((gemm_nn<double, double, double, double>(A, n, V0n, n, A1, n, n, n, n, st)));
+  carve_jac(ws, j64, n, 1, 0);
+  PLOM_TRY(jacobi_launch<double>(A1, n, 1, 0, j64, S, U, VH1, info, st));
+  // VH = VH1 V0n^T  (row k = (V0n v1_k)^T)
+  PLOM_TRY(transpose_f64(V0n, V0nT, n, n, 1, st));
+  PLOM_TRY((gemm_nn<double, double, double, double>(VH1, n, V0nT, n, VH, n, n, n, n, st)));
+  ws.off = std::max(need, ws.off);
+  return PLOM_OK;
+}
+
+int jacobi_svd(const double* A, int n, int batch, int cplx, double* S, double* U, double* VH,
+               int* info, Arena& ws, cudaStream_t st) {
+  if (!cplx && batch == 1 && n >= JACOBI_PRECOND_MIN_N)
+    return jacobi_svd_precond(A, n, S, U, VH, info, ws, st);
+  JacState<double> js;
+  carve_jac(ws, js, n, batch, cplx);
+  if (ws.measuring() || n == 0 || batch == 0) return PLOM_OK;
+  PLOM_REQUIRE(!ws.overflow(), PLOM_ERR_WORKSPACE, "jacobi: workspace too small");
+  PLOM_REQUIRE(A && S && U && VH && info, PLOM_ERR_ARG, "jacobi: null pointer");
+  return jacobi_launch<double>(A, n, batch, cplx, js, S, U, VH, info, st);
 }
 
 // ---------------------------------------------------------------------------

@@ -441,8 +441,11 @@ __global__ void __launch_bounds__(288, 1)
   const uint32_t base = (smem_u32(smem_raw) + 1023u) & ~1023u;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   // work item -> (upper tile ti <= tj, chunk)
-  const int item = blockIdx.x;
-  const int tile = item / chunks, chunk = item % chunks;
+  // consecutive CTAs take different tiles of the same row chunk, so the CTAs
+  // resident together read the same rows and share them through L2
+  const int ntiles_all = tn * (tn + 1) / 2;
+  const int chunk = (int)(blockIdx.x / ntiles_all), tile = (int)(blockIdx.x % ntiles_all);
+  const int item = tile * chunks + chunk;  // partial slab index (tile-major)
   int ti = 0, rem = tile;
   while (rem >= tn - ti) {
     rem -= tn - ti;
@@ -813,8 +816,11 @@ __global__ void __launch_bounds__(320, 1)
   const uint32_t base = (smem_u32(smem_raw) + 1023u) & ~1023u;
   const uint32_t raw_base = base, op_base = base + GT_RAW_STAGES * GT_RAW_BYTES;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int item = blockIdx.x;
-  const int tile = item / chunks, chunk = item % chunks;
+  // consecutive CTAs take different tiles of the same row chunk, so the CTAs
+  // resident together read the same rows and share them through L2
+  const int ntiles_all = tn * (tn + 1) / 2;
+  const int chunk = (int)(blockIdx.x / ntiles_all), tile = (int)(blockIdx.x % ntiles_all);
+  const int item = tile * chunks + chunk;  // partial slab index (tile-major)
   int ti = 0, rem = tile;
   while (rem >= tn - ti) {
     rem -= tn - ti;

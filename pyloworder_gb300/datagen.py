@@ -65,7 +65,8 @@ def pod_field_device(nx, ny, nt, nmodes, seed, noise=1e-5, amp_pow=1.5, dtype="f
     tdt = getattr(torch, dtype) if isinstance(dtype, str) else dtype
     rng, kx, ky, w, th = _pod_params(nmodes, seed, distinct, kmax)
     m = nx * ny
-    amps = np.array([k ** (-amp_pow) for k in range(1, nmodes + 1)])
+    amps = np.array([2.0 ** (-k) if amp_pow is None else k ** (-amp_pow)
+                     for k in range(1, nmodes + 1)])
     t = np.arange(nt, dtype=np.float64)
     T = torch.tensor(amps[:, None] * np.cos(np.outer(w, t) + th[:, None]), device="cuda",
                      dtype=torch.float64)
@@ -95,3 +96,83 @@ def grid_for_points(m):
     while m % ny:
         ny -= 1
     return m // ny, ny
+
+
+def dmd_field_device(m, n, npairs=16, seed=1003, dt=0.1, noise=1e-5, width=32.0,
+                     dtype="float32", chunk_rows=1 << 20):
+    """Config-3 field: 16 conjugate eigenvalue pairs lambda_j = exp((s_j + i w_j) dt),
+    s_j ~ U[-0.05, 0], w_j ~ U[0.05, 3], spatial modes complex Gaussian fields
+    smoothed along the point index by a Gaussian filter of standard deviation
+    `width` points, plus `noise` white noise.  X = 2 Re(Phi diag(lambda^t)).
+    Returns (X on the device, lambda)."""
+    import torch
+    tdt = getattr(torch, dtype) if isinstance(dtype, str) else dtype
+    rng = np.random.default_rng(seed)
+    sig = rng.uniform(-0.05, 0.0, npairs)
+    om = rng.uniform(0.05, 3.0, npairs)
+    lam = np.exp((sig + 1j * om) * dt)
+    t = np.arange(n)
+    T = lam[:, None] ** t[None, :]                       # npairs x n
+    Tr = torch.tensor(np.concatenate([T.real, -T.imag]), device="cuda", dtype=torch.float64)
+    half = int(4 * width)
+    ker = np.exp(-0.5 * (np.arange(-half, half + 1) / width) ** 2)
+    ker /= np.sqrt(np.sum(ker ** 2))
+    kt = torch.tensor(ker, device="cuda", dtype=torch.float32).reshape(1, 1, -1)
+    g = torch.Generator(device="cuda")
+    g.manual_seed(int(seed))
+    X = torch.empty((m, n), dtype=tdt, device="cuda")
+    for r0 in range(0, m, chunk_rows):
+        r1 = min(m, r0 + chunk_rows)
+        rows = r1 - r0
+        # white complex fields with a halo so chunks join smoothly in distribution
+        w = torch.randn((2 * npairs, 1, rows + 2 * half), device="cuda", dtype=torch.float32,
+                        generator=g)
+        ph = torch.nn.functional.conv1d(w, kt).reshape(2 * npairs, rows).T.to(torch.float64)
+        blk = 2.0 * (ph @ Tr)                            # 2 Re(Phi T)
+        blk += noise * torch.randn(blk.shape, device="cuda", dtype=torch.float64, generator=g)
+        X[r0:r1].copy_(blk)
+        del w, ph, blk
+    return X, lam
+
+
+def spod_field_device(M, N, noscill=8, seed=1004, fs=1.0, bw=0.002, phi=0.9, ncomp=16,
+                      noise_amp=0.1, dtype="float32", chunk_rows=1 << 16):
+    """Config-4 field: `noscill` narrow-band oscillators (centre frequency
+    ~ U[0.01, 0.4] fs, bandwidth 0.002 fs, each a sum of `ncomp` sinusoids with
+    random frequencies inside its band and random phases) with random smooth
+    spatial shapes, plus AR(1) red noise x_t = phi x_{t-1} + e_t (phi = 0.9),
+    realised per row by filtering white noise with 1/(1 - phi e^{-i w}) in the
+    Fourier domain (circular AR(1))."""
+    import torch
+    tdt = getattr(torch, dtype) if isinstance(dtype, str) else dtype
+    rng = np.random.default_rng(seed)
+    t = np.arange(N) / fs
+    S = np.zeros((noscill, N))
+    for j in range(noscill):
+        fc = rng.uniform(0.01, 0.4) * fs
+        fr = fc + rng.uniform(-0.5, 0.5, ncomp) * bw * fs
+        phs = rng.uniform(0, 2 * np.pi, ncomp)
+        S[j] = np.cos(2 * np.pi * fr[:, None] * t[None, :] + phs[:, None]).sum(0) / np.sqrt(ncomp)
+    St = torch.tensor(S, device="cuda", dtype=torch.float32)
+    kx = rng.uniform(0.5, 4.0, noscill)
+    ph0 = rng.uniform(0, 2 * np.pi, noscill)
+    amp = 1.0 / (1 + np.arange(noscill))
+    kxt = torch.tensor(kx, device="cuda", dtype=torch.float32)
+    pht = torch.tensor(ph0, device="cuda", dtype=torch.float32)
+    ampt = torch.tensor(amp, device="cuda", dtype=torch.float32)
+    freqs = torch.fft.rfftfreq(N, device="cuda")
+    H = 1.0 / (1.0 - phi * torch.exp(-2j * np.pi * freqs))
+    g = torch.Generator(device="cuda")
+    g.manual_seed(int(seed))
+    X = torch.empty((M, N), dtype=tdt, device="cuda")
+    for r0 in range(0, M, chunk_rows):
+        r1 = min(M, r0 + chunk_rows)
+        x = torch.arange(r0, r1, device="cuda", dtype=torch.float32) / M * 2 * np.pi
+        shapes = ampt * torch.sin(x[:, None] * kxt[None, :] + pht[None, :])
+        blk = shapes @ St
+        e = torch.randn((r1 - r0, N), device="cuda", dtype=torch.float32, generator=g)
+        red = torch.fft.irfft(torch.fft.rfft(e, dim=1) * H, n=N, dim=1)
+        blk += noise_amp * red
+        X[r0:r1].copy_(blk)
+        del blk, e, red, shapes
+    return X

@@ -110,30 +110,47 @@ def run_job(job, X, precision="mixed"):
 
 
 class Server:
-    """Admission-controlled continuous batching over `slots` CUDA streams."""
+    """Admission-controlled continuous batching over `slots` CUDA streams.
 
-    def __init__(self, hbm_budget_bytes=150e9, slots=4, precision="mixed"):
+    `executor(job, stream_index)` runs one job and returns its result; the
+    default generates the job's data and runs it on the worker's own CUDA
+    stream.  `footprint(job)` gives the bytes a job holds while admitted.
+    """
+
+    def __init__(self, hbm_budget_bytes=150e9, slots=4, precision="mixed", executor=None,
+                 footprint=None):
         self.budget = float(hbm_budget_bytes)
         self.slots = int(slots)
         self.precision = precision
         self.lock = threading.Condition()
         self.in_use = 0.0
+        self.peak_in_use = 0.0
         self.free_slots = self.slots
+        self.executor = executor
+        self.footprint = footprint or (lambda j: footprint_bytes(j, self.precision))
+        self._streams = {}
+
+    def _gpu_execute(self, job, wid):
+        torch = L.torch()
+        stream = self._streams.get(wid)
+        if stream is None:
+            stream = self._streams[wid] = torch.cuda.Stream()
+        with torch.cuda.stream(stream):
+            X = generate(job)
+            res = run_job(job, X, self.precision)
+            del X
+        stream.synchronize()
+        return res
 
     def _worker(self, wid, work_q, done_q, t0):
-        torch = L.torch()
-        stream = torch.cuda.Stream()
+        execute = self.executor or self._gpu_execute
         while True:
             item = work_q.get()
             if item is None:
                 return
             job, nbytes = item
             try:
-                with torch.cuda.stream(stream):
-                    X = generate(job)
-                    job.result = run_job(job, X, self.precision)
-                    del X
-                stream.synchronize()
+                job.result = execute(job, wid)
             except Exception as e:  # a failing job reports its error; the others continue
                 job.error = f"{type(e).__name__}: {e}"
             job.done = time.perf_counter() - t0
@@ -146,10 +163,11 @@ class Server:
     def run(self, jobs, realtime=True):
         """Serve `jobs` (sorted by arrival).  Returns the finished jobs and a
         summary {jobs_per_s, p50_ms, p99_ms, ...}."""
-        torch = L.require_cuda()
-        L.load()
+        if self.executor is None:
+            L.require_cuda()
+            L.load()
         jobs = sorted(jobs, key=lambda j: j.arrival)
-        sizes = [footprint_bytes(j, self.precision) for j in jobs]
+        sizes = [self.footprint(j) for j in jobs]
         work_q: queue.Queue = queue.Queue()
         done_q: queue.Queue = queue.Queue()
         t0 = time.perf_counter()
@@ -172,6 +190,7 @@ class Server:
                     self.lock.wait()
                 self.free_slots -= 1
                 self.in_use += nbytes
+                self.peak_in_use = max(self.peak_in_use, self.in_use)
             if not realtime:
                 job.arrival = time.perf_counter() - t0
             job.admitted = time.perf_counter() - t0
@@ -180,7 +199,8 @@ class Server:
             work_q.put(None)
         for w in workers:
             w.join()
-        torch.cuda.synchronize()
+        if self.executor is None:
+            L.torch().cuda.synchronize()
         finished = []
         while not done_q.empty():
             finished.append(done_q.get())
@@ -192,5 +212,6 @@ class Server:
                    "jobs_per_s": len(ok) / wall if wall > 0 else float("nan"),
                    "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
                    "slots": self.slots, "hbm_budget_gb": self.budget / 1e9,
-                   "precision": self.precision}
+                   "peak_admitted_gb": self.peak_in_use / 1e9, "precision": self.precision,
+                   "errors": [(j.jid, j.kind, j.m, j.n, j.error) for j in finished if j.error][:8]}
         return finished + rejected, summary
