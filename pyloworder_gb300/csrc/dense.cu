@@ -359,14 +359,42 @@ int trtri_upper(const double* R, double* W, int n, int batch, Arena& ws, cudaStr
 
 // ---------------------------------------------------------------------------
 // one-sided Jacobi SVD (Hestenes), real or complex, cooperative
+//
+// The columns of A (rows of At) are rotated in pairs until every pair is
+// orthogonal to the tolerance.  GB300 runs FP64 at a small fraction of its
+// FP32 rate, so the kernels keep the FP64 instructions per row and pair low:
+//  * squared column norms are carried from rotation to rotation
+//    (a'^2 = a^2 - t|g|, b'^2 = b^2 + t|g|), recomputed exactly once per
+//    sweep and after cancellation, so each pair needs one dot product;
+//  * rotations are applied in scaled form (column = d * stored row):
+//    x' = x - t (dq/dp) e^{-i phi} y,  y' = y + t (dp/dq) e^{i phi} x,
+//    d' = c d: two FMAs per row; a scale is folded back into its row when it
+//    falls below 2^-40 (|t| <= 1 bounds the growth of a stored row to
+//    sqrt(2) per rotation);
+//  * the angle t is computed in FP32: every t gives an exactly orthogonal
+//    rotation as long as c = (1 + t^2)^-1/2 is exact for that t, and c comes
+//    from an FP32 estimate refined by two Newton steps in FP64;
+//  * the matrix is first scaled by a power of two so that max |a_ij| < 1.
+// Block ordering (jacobi_block_kernel): the columns are grouped in blocks of
+// 4; one CTA holds a pair of blocks (8 rows of At and of Vt) in shared
+// memory for one round-robin step over the blocks, applies the 16 cross
+// rotations in 4 rounds of 4 disjoint pairs (plus the 6 + 6 rotations inside
+// the two blocks at the first step of a sweep) and writes the rows back: one
+// grid barrier per block step instead of one per column step.  Problems
+// whose 8 rows do not fit in shared memory use jacobi_pair_kernel (one warp
+// per column pair, one grid barrier per column step).
 // ---------------------------------------------------------------------------
-template <typename T>
+constexpr double JAC_FOLD_BELOW = 9.094947017729282e-13;  // 2^-40
+
 struct JacState {
-  T* At;        // batch x n x (n*cw): rows = columns of A
-  T* Vt;        // batch x n x (n*cw): rows = columns of V
-  int* counts;  // [JACOBI_MAX_SWEEPS]
-  int* perm;    // batch x n
-  T* nrm;       // batch x n
+  double* At;     // batch x n x pitch: rows = columns of A (times dsc)
+  double* Vt;     // batch x n x pitch: rows = columns of V (times dsc)
+  double* nrm2;   // batch x n: squared column norms; < 0 = recompute
+  double* dsc;    // batch x n: column scales
+  int* counts;    // [JACOBI_MAX_SWEEPS] rotations per sweep
+  int* perm;      // batch x n
+  unsigned long long* amax;  // [batch] bits of max |a_ij|
+  int64_t pitch;  // doubles per row (n * cw rounded up to even)
 };
 
 __device__ __forceinline__ void rr_pair(int step, int k, int np, int& a, int& b) {
@@ -381,114 +409,536 @@ __device__ __forceinline__ void rr_pair(int step, int k, int np, int& a, int& b)
   }
 }
 
-// T = double: the SVD itself.  T = float: a fast pass whose accumulated
-// rotations (js.Vt) precondition the FP64 pass; with S == nullptr the output
-// stage is skipped.
-template <typename T>
-__global__ void __launch_bounds__(128) jacobi_coop_kernel(const double* __restrict__ A, int n,
-                                                          int batch, int cplx, JacState<T> js,
+// Rotation of a pair with squared norms al, be and |a_p^H a_q| = gabs.
+// False when the pair is orthogonal to the tolerance (gabs^2 <= tol2 al be).
+__device__ __forceinline__ bool jac_angle(double al, double be, double gabs, double tol2,
+                                          double& t, double& c, double& sq) {
+  if (!(al > 0.0 && be > 0.0) || !(gabs * gabs > tol2 * (al * be))) return false;
+  const double diff = be - al;
+  const float gf = (float)gabs;
+  if (gf >= 1e-30f) {
+    const float z = (float)diff / (2.0f * gf);
+    const float az = fabsf(z);
+    t = (double)(az > 1e18f ? 0.5f / z : copysignf(1.0f, z) / (az + sqrtf(fmaf(z, z, 1.0f))));
+  } else {
+    const double z = diff / (2.0 * gabs);
+    const double az = fabs(z);
+    t = az > 1e150 ? 0.5 / z : copysign(1.0, z) / (az + sqrt(fma(z, z, 1.0)));
+  }
+  const double x = fma(t, t, 1.0);
+  double y = (double)rsqrtf((float)x);
+#pragma unroll
+  for (int it = 0; it < 2; ++it) {
+    const double r = fma(-x * y, y, 1.0);
+    y = fma(0.5 * y, r, y);
+  }
+  c = y;
+  sq = x * y;
+  return true;
+}
+
+// x^H y over rows [0, len) of the warp's pair (+ |x|^2, |y|^2 when SQ)
+template <int CW, bool SQ>
+__device__ __forceinline__ void jac_dots(const double* x, const double* y, int64_t len, int lane,
+                                         double& gr, double& gi, double& sa, double& sb) {
+  double g0 = 0, g1 = 0, h0 = 0, a0 = 0, a1 = 0, b0 = 0, b1 = 0;
+  if (CW == 1) {
+    int64_t i = lane;
+    for (; i + 96 < len; i += 128) {
+      const double x0 = x[i], x1 = x[i + 32], x2 = x[i + 64], x3 = x[i + 96];
+      const double y0 = y[i], y1 = y[i + 32], y2 = y[i + 64], y3 = y[i + 96];
+      g0 = fma(x0, y0, g0);
+      g1 = fma(x1, y1, g1);
+      g0 = fma(x2, y2, g0);
+      g1 = fma(x3, y3, g1);
+      if (SQ) {
+        a0 = fma(x0, x0, a0);
+        a1 = fma(x1, x1, a1);
+        a0 = fma(x2, x2, a0);
+        a1 = fma(x3, x3, a1);
+        b0 = fma(y0, y0, b0);
+        b1 = fma(y1, y1, b1);
+        b0 = fma(y2, y2, b0);
+        b1 = fma(y3, y3, b1);
+      }
+    }
+    for (; i < len; i += 32) {
+      const double x0 = x[i], y0 = y[i];
+      g0 = fma(x0, y0, g0);
+      if (SQ) {
+        a0 = fma(x0, x0, a0);
+        b0 = fma(y0, y0, b0);
+      }
+    }
+  } else {
+    for (int64_t i = lane; i < len; i += 32) {
+      const double xr = x[2 * i], xi = x[2 * i + 1], yr = y[2 * i], yi = y[2 * i + 1];
+      g0 = fma(xr, yr, g0);  // conj(x) * y
+      g0 = fma(xi, yi, g0);
+      h0 = fma(xr, yi, h0);
+      h0 = fma(-xi, yr, h0);
+      if (SQ) {
+        a0 = fma(xr, xr, a0);
+        a0 = fma(xi, xi, a0);
+        b0 = fma(yr, yr, b0);
+        b0 = fma(yi, yi, b0);
+      }
+    }
+  }
+  gr = warp_sum(g0 + g1);
+  gi = (CW == 2) ? warp_sum(h0) : 0.0;
+  if (SQ) {
+    sa = warp_sum(a0 + a1);
+    sb = warp_sum(b0 + b1);
+  } else {
+    sa = sb = 0.0;
+  }
+}
+
+// x <- x - w y, y <- y + v x (old x) over rows [0, len); real: w, v real
+template <int CW>
+__device__ __forceinline__ void jac_rotate(double* x, double* y, int64_t len, int lane, double wr,
+                                           double wi, double vr, double vi) {
+  if (CW == 1) {
+    int64_t i = lane;
+    for (; i + 96 < len; i += 128) {
+      double xv[4], yv[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        xv[u] = x[i + 32 * u];
+        yv[u] = y[i + 32 * u];
+      }
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        x[i + 32 * u] = fma(-wr, yv[u], xv[u]);
+        y[i + 32 * u] = fma(vr, xv[u], yv[u]);
+      }
+    }
+    for (; i < len; i += 32) {
+      const double xv = x[i], yv = y[i];
+      x[i] = fma(-wr, yv, xv);
+      y[i] = fma(vr, xv, yv);
+    }
+  } else {
+    for (int64_t i = lane; i < len; i += 32) {
+      const double xr = x[2 * i], xi = x[2 * i + 1], yr = y[2 * i], yi = y[2 * i + 1];
+      x[2 * i] = xr - (wr * yr - wi * yi);
+      x[2 * i + 1] = xi - (wr * yi + wi * yr);
+      y[2 * i] = yr + (vr * xr - vi * xi);
+      y[2 * i + 1] = yi + (vr * xi + vi * xr);
+    }
+  }
+}
+
+// One pair (rows x, y of At; xv, yv of Vt) by one warp.  nrm/d/e point at
+// the pair's norm and scale slots.  Returns 1 when the pair was rotated.
+template <int CW>
+__device__ __forceinline__ int jac_pair(double* x, double* y, double* xv, double* yv, int64_t n,
+                                        double* na_, double* nb_, double* da_, double* db_,
+                                        double* ea_, double* eb_, double tol2, int lane) {
+  double al = *na_, be = *nb_;
+  const double da = *da_, db = *db_, ea = *ea_, eb = *eb_;
+  const bool need = (al < 0.0) || (be < 0.0);
+  double gr, gi, sa, sb;
+  if (need)
+    jac_dots<CW, true>(x, y, n, lane, gr, gi, sa, sb);
+  else
+    jac_dots<CW, false>(x, y, n, lane, gr, gi, sa, sb);
+  if (al < 0.0) al = da * da * sa;
+  if (be < 0.0) be = db * db * sb;
+  const double dd = da * db;
+  gr *= dd;
+  gi *= dd;
+  const double gabs = (CW == 1) ? fabs(gr) : sqrt(fma(gr, gr, gi * gi));
+  double t, c, sq;
+  if (!jac_angle(al, be, gabs, tol2, t, c, sq)) {
+    if (lane == 0 && need) {
+      *na_ = al;
+      *nb_ = be;
+    }
+    return 0;
+  }
+  const double tp = t * (db * ea), tq = t * (da * eb);  // t dq/dp, t dp/dq
+  if (CW == 1) {
+    const double e = copysign(1.0, gr);  // phase of gamma
+    jac_rotate<1>(x, y, n, lane, tp * e, 0.0, tq * e, 0.0);
+    jac_rotate<1>(xv, yv, n, lane, tp * e, 0.0, tq * e, 0.0);
+  } else {
+    const double ig = 1.0 / gabs;
+    const double er = gr * ig, ei = gi * ig;
+    jac_rotate<2>(x, y, n, lane, tp * er, -tp * ei, tq * er, tq * ei);
+    jac_rotate<2>(xv, yv, n, lane, tp * er, -tp * ei, tq * er, tq * ei);
+  }
+  __syncwarp();
+  if (lane == 0) {
+    // carried norms; a large relative drop is recomputed next time
+    const double na = fma(-t, gabs, al), nb = fma(t, gabs, be);
+    *na_ = (na > 0.125 * al) ? na : -1.0;
+    *nb_ = (nb > 0.125 * be) ? nb : -1.0;
+    *da_ = da * c;
+    *db_ = db * c;
+    *ea_ = ea * sq;
+    *eb_ = eb * sq;
+  }
+  return 1;
+}
+
+// Shared prologue: scale by a power of two (max |a_ij| < 1), At = A^T,
+// Vt = I, unit scales, norms flagged for recomputation.
+template <int CW>
+__device__ void jac_init(const double* __restrict__ A, int n, int batch, JacState& js,
+                         cg::grid_group& grid) {
+  const int64_t rl = (int64_t)n * CW;
+  const int64_t P = js.pitch;
+  const int64_t gtid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t gthreads = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t e = gtid; e < batch; e += gthreads) js.amax[e] = 0ull;
+  if (gtid < JACOBI_MAX_SWEEPS) js.counts[gtid] = 0;
+  grid.sync();
+  for (int64_t e = gtid; e < (int64_t)batch * n * rl; e += gthreads) {
+    const double v = fabs(A[e]);
+    if (v > 0.0) atomicMax(&js.amax[e / ((int64_t)n * rl)], (unsigned long long)__double_as_longlong(v));
+  }
+  grid.sync();
+  for (int64_t e = gtid; e < (int64_t)batch * n * n; e += gthreads) {
+    const int64_t b = e / ((int64_t)n * n), r = e % ((int64_t)n * n);
+    const int i = (int)(r / n), j = (int)(r % n);
+    int ex = 0;
+    frexp(__longlong_as_double((long long)js.amax[b]), &ex);
+    const double sc = ldexp(1.0, -ex);
+    const double* src = A + b * n * rl + (int64_t)i * rl + (int64_t)j * CW;
+    double* dst = js.At + b * n * P + (int64_t)j * P + (int64_t)i * CW;
+    dst[0] = src[0] * sc;
+    if (CW == 2) dst[1] = src[1] * sc;
+    double* v = js.Vt + b * n * P + (int64_t)i * P + (int64_t)j * CW;
+    v[0] = (i == j) ? 1.0 : 0.0;
+    if (CW == 2) v[1] = 0.0;
+    if (j == 0) {
+      for (int64_t p = rl; p < P; ++p) {  // row padding stays zero
+        js.At[b * n * P + (int64_t)i * P + p] = 0.0;
+        js.Vt[b * n * P + (int64_t)i * P + p] = 0.0;
+      }
+      js.nrm2[b * n + i] = -1.0;
+      js.dsc[b * n + i] = 1.0;
+    }
+  }
+  grid.sync();
+}
+
+// Shared epilogue: exact norms, descending order, outputs
+//   S = sigma, U[i][k] = a_perm(k)[i] / sigma, VH[k][:] = conj(v_perm(k)).
+template <int CW>
+__device__ void jac_finish(int n, int batch, JacState& js, int sweep, double* __restrict__ S,
+                           double* __restrict__ U, double* __restrict__ VH, int* info,
+                           cg::grid_group& grid) {
+  const int64_t rl = (int64_t)n * CW;
+  const int64_t P = js.pitch;
+  const int lane = threadIdx.x & 31;
+  const int64_t gtid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t gthreads = (int64_t)gridDim.x * blockDim.x;
+  const int64_t gwarp = gtid >> 5, nwarps = gthreads >> 5;
+  if (gtid == 0) {
+    info[ST_SWEEPS] = sweep + 1;
+    if (sweep >= JACOBI_MAX_SWEEPS) atomicMax(&info[ST_FAIL], PLOM_NUM_JACOBI);
+  }
+  for (int64_t task = gwarp; task < (int64_t)batch * n; task += nwarps) {
+    const double* a = js.At + (task / n) * n * P + (task % n) * P;
+    double s = 0.0;
+    for (int64_t i = lane; i < rl; i += 32) s = fma(a[i], a[i], s);
+    s = warp_sum(s);
+    if (lane == 0) js.nrm2[task] = js.dsc[task] * js.dsc[task] * s;
+  }
+  grid.sync();
+  for (int64_t e = gtid; e < (int64_t)batch * n; e += gthreads) {
+    const int64_t b = e / n;
+    const int j = (int)(e % n);
+    const double sj = js.nrm2[e];
+    int rank = 0;
+    for (int k = 0; k < n; ++k) {
+      const double sk = js.nrm2[b * n + k];
+      rank += (sk > sj) || (sk == sj && k < j);
+    }
+    js.perm[b * n + rank] = j;
+  }
+  grid.sync();
+  for (int64_t e = gtid; e < (int64_t)batch * n * n; e += gthreads) {
+    const int64_t b = e / ((int64_t)n * n);
+    const int64_t r = e % ((int64_t)n * n);
+    const int k = (int)(r / n), i = (int)(r % n);
+    const int src = js.perm[b * n + k];
+    const double s2 = js.nrm2[b * n + src];
+    const double sk = sqrt(s2);
+    int ex = 0;
+    frexp(__longlong_as_double((long long)js.amax[b]), &ex);
+    if (i == 0) S[b * n + k] = ldexp(sk, ex);
+    const double d = js.dsc[b * n + src];
+    const double f = sk > 0.0 ? d / sk : 0.0;
+    const double* a = js.At + b * n * P + (int64_t)src * P + (int64_t)i * CW;
+    double* u = U + b * n * rl + (int64_t)i * rl + (int64_t)k * CW;
+    u[0] = a[0] * f;
+    if (CW == 2) u[1] = a[1] * f;
+    const double* v = js.Vt + b * n * P + (int64_t)src * P + (int64_t)i * CW;
+    double* vh = VH + b * n * rl + (int64_t)k * rl + (int64_t)i * CW;
+    vh[0] = v[0] * d;
+    if (CW == 2) vh[1] = -v[1] * d;
+  }
+}
+
+__device__ __forceinline__ void bulk_load(uint32_t dst, const void* src, uint32_t bytes,
+                                          uint32_t bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),
+      "l"(reinterpret_cast<uint64_t>(src)), "r"(bytes), "r"(bar)
+      : "memory");
+}
+
+// rounds of the 6 pairs inside a block of 4: (0,1)(2,3) / (0,2)(1,3) / (0,3)(1,2)
+__device__ __forceinline__ void intra_pair(int round, int which, int& a, int& b) {
+  if (round == 0) {
+    a = which ? 2 : 0;
+    b = which ? 3 : 1;
+  } else if (round == 1) {
+    a = which ? 1 : 0;
+    b = which ? 3 : 2;
+  } else {
+    a = which ? 1 : 0;
+    b = which ? 2 : 3;
+  }
+}
+
+constexpr uint64_t JAC_WAIT_NS = 2000000000ull;
+
+template <int CW>
+__global__ void __launch_bounds__(128) jacobi_block_kernel(const double* __restrict__ A, int n,
+                                                           int batch, JacState js, double tol2,
+                                                           double* __restrict__ S,
+                                                           double* __restrict__ U,
+                                                           double* __restrict__ VH, int* info) {
+  extern __shared__ __align__(16) double jsm[];  // [8][pitch] At rows, [8][pitch] Vt rows
+  __shared__ double snrm[8], sd[8], se[8];
+  __shared__ int scol[8];
+  __shared__ __align__(8) uint64_t bar;
+  __shared__ int abort_sh;
+  cg::grid_group grid = cg::this_grid();
+  const int64_t P = js.pitch;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  double* cA = jsm;
+  double* cV = jsm + 8 * P;
+  const uint32_t bar_s = (uint32_t)__cvta_generic_to_shared(&bar);
+  if (threadIdx.x == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar_s));
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    abort_sh = 0;
+  }
+  jac_init<CW>(A, n, batch, js, grid);  // ends with a grid barrier
+
+  const int nb = (n + 3) / 4;
+  const int nbp = (nb + (nb & 1) < 2) ? 2 : nb + (nb & 1);  // even, >= 2
+  const int bpairs = nbp / 2;
+  const int64_t tasks = (int64_t)bpairs * batch;
+  uint32_t phase = 0;
+  int sweep = 0;
+  for (; sweep < JACOBI_MAX_SWEEPS; ++sweep) {
+    int myrot = 0;
+    for (int step = 0; step < nbp - 1; ++step) {
+      for (int64_t task = blockIdx.x; task < tasks; task += gridDim.x) {
+        const int64_t b = task / bpairs;
+        int bi, bj;
+        rr_pair(step, (int)(task % bpairs), nbp, bi, bj);
+        double* At = js.At + b * n * P;
+        double* Vt = js.Vt + b * n * P;
+        if (threadIdx.x < 8) {
+          const int col = 4 * (threadIdx.x < 4 ? bi : bj) + (threadIdx.x & 3);
+          const bool v = col < n;
+          scol[threadIdx.x] = v ? col : -1;
+          snrm[threadIdx.x] = v ? js.nrm2[b * n + col] : 0.0;
+          const double d = v ? js.dsc[b * n + col] : 1.0;
+          sd[threadIdx.x] = d;
+          se[threadIdx.x] = 1.0 / d;  // exact inverse once per block step (no drift of d e)
+        }
+        __syncthreads();
+        // rows in: bulk copies (pitch is even, so every row is 16-byte aligned)
+        if (threadIdx.x == 0 && !abort_sh) {
+          asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+          uint32_t bytes = 0;
+          for (int s8 = 0; s8 < 8; ++s8)
+            if (scol[s8] >= 0) bytes += 2u * (uint32_t)(P * 8);
+          asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar_s),
+                       "r"(bytes)
+                       : "memory");
+          for (int s8 = 0; s8 < 8; ++s8) {
+            const int col = scol[s8];
+            if (col < 0) continue;
+            bulk_load((uint32_t)__cvta_generic_to_shared(cA + s8 * P), At + (int64_t)col * P,
+                      (uint32_t)(P * 8), bar_s);
+            bulk_load((uint32_t)__cvta_generic_to_shared(cV + s8 * P), Vt + (int64_t)col * P,
+                      (uint32_t)(P * 8), bar_s);
+          }
+        }
+        if (!abort_sh) {
+          // bounded wait for the rows
+          uint32_t ok = 0;
+          uint64_t t0 = 0;
+          asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t0));
+          while (true) {
+            asm volatile(
+                "{\n\t.reg .pred p;\n\t"
+                "mbarrier.try_wait.parity.acquire.cta.shared::cta.b64 p, [%1], %2;\n\t"
+                "selp.u32 %0, 1, 0, p;\n\t}"
+                : "=r"(ok)
+                : "r"(bar_s), "r"(phase)
+                : "memory");
+            if (ok) break;
+            uint64_t t1;
+            asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t1));
+            if (t1 - t0 > JAC_WAIT_NS) {
+              abort_sh = 1;
+              break;
+            }
+          }
+          phase ^= 1u;
+        }
+        __syncthreads();
+        if (abort_sh) {
+          // rows never arrived: report and do no more work (every later task
+          // of this block skips too; the barriers stay uniform)
+          if (threadIdx.x == 0) atomicMax(&info[ST_FAIL], PLOM_NUM_TIMEOUT);
+          __syncthreads();
+          continue;
+        }
+        if (step == 0) {
+          // exact squared norms once per sweep
+          for (int s8 = warp; s8 < 8; s8 += 4) {
+            double acc = 0.0;
+            if (scol[s8] >= 0) {
+              const double* x = cA + s8 * P;
+              for (int64_t i = lane; i < (int64_t)n * CW; i += 32) acc = fma(x[i], x[i], acc);
+              acc = warp_sum(acc);
+            }
+            if (lane == 0) snrm[s8] = sd[s8] * sd[s8] * acc;
+          }
+          __syncthreads();
+          for (int r = 0; r < 3; ++r) {
+            int a, c;
+            intra_pair(r, warp & 1, a, c);
+            const int off = (warp >> 1) * 4;
+            a += off;
+            c += off;
+            if (scol[a] >= 0 && scol[c] >= 0)
+              myrot += jac_pair<CW>(cA + a * P, cA + c * P, cV + a * P, cV + c * P, n, &snrm[a],
+                                    &snrm[c], &sd[a], &sd[c], &se[a], &se[c], tol2, lane);
+            __syncthreads();
+          }
+        }
+        for (int u = 0; u < 4; ++u) {
+          const int a = warp, c = 4 + ((warp + u) & 3);
+          if (scol[a] >= 0 && scol[c] >= 0)
+            myrot += jac_pair<CW>(cA + a * P, cA + c * P, cV + a * P, cV + c * P, n, &snrm[a],
+                                  &snrm[c], &sd[a], &sd[c], &se[a], &se[c], tol2, lane);
+          __syncthreads();
+        }
+        // rows out; a scale below 2^-40 is folded into its rows
+        for (int s8 = 0; s8 < 8; ++s8) {
+          const int col = scol[s8];
+          if (col < 0) continue;
+          double* ga = At + (int64_t)col * P;
+          double* gv = Vt + (int64_t)col * P;
+          const double* sa = cA + s8 * P;
+          const double* sv = cV + s8 * P;
+          const double f = sd[s8];
+          if (f < JAC_FOLD_BELOW) {
+            for (int64_t i = threadIdx.x; i < P; i += 128) {
+              ga[i] = sa[i] * f;
+              gv[i] = sv[i] * f;
+            }
+          } else {
+            for (int64_t i = threadIdx.x; i < P; i += 128) {
+              ga[i] = sa[i];
+              gv[i] = sv[i];
+            }
+          }
+        }
+        if (threadIdx.x < 8 && scol[threadIdx.x] >= 0) {
+          const int col = scol[threadIdx.x];
+          const bool fold = sd[threadIdx.x] < JAC_FOLD_BELOW;
+          js.nrm2[b * n + col] = snrm[threadIdx.x];
+          js.dsc[b * n + col] = fold ? 1.0 : sd[threadIdx.x];
+        }
+        __syncthreads();
+      }
+      grid.sync();
+    }
+    if (lane == 0 && myrot) atomicAdd(&js.counts[sweep], myrot);
+    grid.sync();
+    if (js.counts[sweep] == 0) break;
+  }
+  if (S == nullptr) return;
+  jac_finish<CW>(n, batch, js, sweep, S, U, VH, info, grid);
+}
+
+// one warp per column pair, 4 pairs per 128-thread block, rows in global memory
+template <int CW>
+__global__ void __launch_bounds__(128) jacobi_pair_kernel(const double* __restrict__ A, int n,
+                                                          int batch, JacState js, double tol2,
                                                           double* __restrict__ S,
                                                           double* __restrict__ U,
                                                           double* __restrict__ VH, int* info) {
   cg::grid_group grid = cg::this_grid();
-  const int cw = cplx ? 2 : 1;
-  const int64_t rl = (int64_t)n * cw;  // doubles per row
-  const int64_t mat = (int64_t)n * rl;
+  const int64_t P = js.pitch;
   const int lane = threadIdx.x & 31;
   const int64_t gwarp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
-  const int64_t gtid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  const int64_t gthreads = (int64_t)gridDim.x * blockDim.x;
-
-  // init: At[j][i] = A[i][j] (complex: element-wise, no conjugation), Vt = I
-  for (int64_t e = gtid; e < (int64_t)batch * n * n; e += gthreads) {
-    int64_t b = e / ((int64_t)n * n), r = e % ((int64_t)n * n);
-    int i = (int)(r / n), j = (int)(r % n);
-    const double* src = A + b * mat + (int64_t)i * rl + (int64_t)j * cw;
-    T* dst = js.At + b * mat + (int64_t)j * rl + (int64_t)i * cw;
-    dst[0] = (T)src[0];
-    if (cplx) dst[1] = (T)src[1];
-    T* v = js.Vt + b * mat + (int64_t)i * rl + (int64_t)j * cw;
-    v[0] = (i == j) ? T(1) : T(0);
-    if (cplx) v[1] = T(0);
-  }
-  if (gtid < JACOBI_MAX_SWEEPS) js.counts[gtid] = 0;
-  grid.sync();
-
+  jac_init<CW>(A, n, batch, js, grid);
   const int np = n + (n & 1);
   const int pairs = np / 2;
-  // rotate while |a_p^H a_q| > n eps ||a_p|| ||a_q||: below that the pair is
-  // orthogonal to working precision (one-sided Jacobi stopping rule)
-  const T tol = (sizeof(T) == 8 ? T(2.220446049250313e-16) : T(1.1920929e-07)) * (T)n;
+  const int64_t total = (int64_t)pairs * batch;
   int sweep = 0;
   for (; sweep < JACOBI_MAX_SWEEPS; ++sweep) {
     int myrot = 0;
+    // exact squared norms once per sweep
+    for (int64_t task = gwarp; task < (int64_t)batch * n; task += nwarps) {
+      const double* a = js.At + (task / n) * n * P + (task % n) * P;
+      double s = 0.0;
+      for (int64_t i = lane; i < (int64_t)n * CW; i += 32) s = fma(a[i], a[i], s);
+      s = warp_sum(s);
+      if (lane == 0) js.nrm2[task] = js.dsc[task] * js.dsc[task] * s;
+    }
+    grid.sync();
     for (int step = 0; step < np - 1; ++step) {
-      for (int64_t task = gwarp; task < (int64_t)pairs * batch; task += nwarps) {
+      for (int64_t task = gwarp; task < total; task += nwarps) {
         const int64_t b = task / pairs;
         int p, q;
         rr_pair(step, (int)(task % pairs), np, p, q);
-        if (p >= n || q >= n) continue;
         if (p > q) {
-          int t = p;
+          const int t = p;
           p = q;
           q = t;
         }
-        T* ap = js.At + b * mat + (int64_t)p * rl;
-        T* aq = js.At + b * mat + (int64_t)q * rl;
-        T alpha = 0, beta = 0, gr = 0, gi = 0;
-        if (!cplx) {
-          for (int64_t i = lane; i < n; i += 32) {
-            T x = ap[i], y = aq[i];
-            alpha = fma(x, x, alpha);
-            beta = fma(y, y, beta);
-            gr = fma(x, y, gr);
-          }
-        } else {
-          for (int64_t i = lane; i < n; i += 32) {
-            T xr = ap[2 * i], xi = ap[2 * i + 1], yr = aq[2 * i], yi = aq[2 * i + 1];
-            alpha += xr * xr + xi * xi;
-            beta += yr * yr + yi * yi;
-            gr += xr * yr + xi * yi;  // conj(x) * y
-            gi += xr * yi - xi * yr;
-          }
-        }
-        alpha = warp_sum(alpha);
-        beta = warp_sum(beta);
-        gr = warp_sum(gr);
-        if (cplx) gi = warp_sum(gi);
-        const T gabs = cplx ? hypot(gr, gi) : fabs(gr);
-        if (!(alpha > T(0) && beta > T(0)) || !(gabs > tol * sqrt(alpha) * sqrt(beta))) continue;
-        ++myrot;
-        const T zeta = (beta - alpha) / (T(2) * gabs);
-        const T t = copysign(T(1), zeta) / (fabs(zeta) + sqrt(T(1) + zeta * zeta));
-        const T c = T(1) / sqrt(T(1) + t * t), s = c * t;
-        // phase e^{i phi} = gamma/|gamma| (real: sign of gamma)
-        const T er = cplx ? gr / gabs : copysign(T(1), gr), ei = cplx ? gi / gabs : T(0);
-        T* vp = js.Vt + b * mat + (int64_t)p * rl;
-        T* vq = js.Vt + b * mat + (int64_t)q * rl;
-        // a' = c a - s e^{-i phi} b ;  b' = s e^{i phi} a + c b
-        for (int side = 0; side < 2; ++side) {
-          T* x = side ? vp : ap;
-          T* y = side ? vq : aq;
-          if (!cplx) {
-            for (int64_t i = lane; i < n; i += 32) {
-              T xv = x[i], yv = y[i];
-              x[i] = c * xv - s * er * yv;
-              y[i] = s * er * xv + c * yv;
+        if (q >= n) continue;
+        double* At = js.At + b * n * P;
+        double* Vt = js.Vt + b * n * P;
+        const int64_t ip = b * n + p, iq = b * n + q;
+        double ep = 1.0 / js.dsc[ip], eq = 1.0 / js.dsc[iq];
+        if (jac_pair<CW>(At + (int64_t)p * P, At + (int64_t)q * P, Vt + (int64_t)p * P,
+                         Vt + (int64_t)q * P, n, &js.nrm2[ip], &js.nrm2[iq], &js.dsc[ip],
+                         &js.dsc[iq], &ep, &eq, tol2, lane)) {
+          ++myrot;
+          __syncwarp();
+          const double dp = js.dsc[ip], dq = js.dsc[iq];
+          __syncwarp();
+          // fold a small scale into its rows
+          for (int side = 0; side < 2; ++side) {
+            const double f = side ? dq : dp;
+            if (f >= JAC_FOLD_BELOW) continue;
+            const int col = side ? q : p;
+            double* ga = At + (int64_t)col * P;
+            double* gv = Vt + (int64_t)col * P;
+            for (int64_t i = lane; i < P; i += 32) {
+              ga[i] *= f;
+              gv[i] *= f;
             }
-          } else {
-            for (int64_t i = lane; i < n; i += 32) {
-              T xr = x[2 * i], xi = x[2 * i + 1], yr = y[2 * i], yi = y[2 * i + 1];
-              // e^{-i phi} y = (er - i ei)(yr + i yi)
-              T zr = er * yr + ei * yi, zi = er * yi - ei * yr;
-              // e^{i phi} x = (er + i ei)(xr + i xi)
-              T wr = er * xr - ei * xi, wi = er * xi + ei * xr;
-              x[2 * i] = c * xr - s * zr;
-              x[2 * i + 1] = c * xi - s * zi;
-              y[2 * i] = s * wr + c * yr;
-              y[2 * i + 1] = s * wi + c * yi;
-            }
+            __syncwarp();
+            if (lane == 0) js.dsc[b * n + col] = 1.0;
           }
         }
       }
@@ -498,162 +948,102 @@ __global__ void __launch_bounds__(128) jacobi_coop_kernel(const double* __restri
     grid.sync();
     if (js.counts[sweep] == 0) break;
   }
-  if (S == nullptr) return;  // preconditioning pass: only js.Vt is wanted
-  if (gtid == 0) {
-    info[ST_SWEEPS] = sweep + 1;
-    if (sweep >= JACOBI_MAX_SWEEPS) atomicMax(&info[ST_FAIL], PLOM_NUM_JACOBI);
-  }
-  // column norms
-  for (int64_t task = gwarp; task < (int64_t)batch * n; task += nwarps) {
-    const T* a = js.At + (task / n) * mat + (task % n) * rl;
-    double s = 0.0;
-    for (int64_t i = lane; i < rl; i += 32) s = fma((double)a[i], (double)a[i], s);
-    s = warp_sum(s);
-    if (lane == 0) js.nrm[task] = (T)sqrt(s);
-  }
-  grid.sync();
-  // descending order: rank of each column (ties broken by index)
-  for (int64_t e = gtid; e < (int64_t)batch * n; e += gthreads) {
-    const int64_t b = e / n;
-    const int j = (int)(e % n);
-    const T sj = js.nrm[e];
-    int rank = 0;
-    for (int k = 0; k < n; ++k) {
-      T sk = js.nrm[b * n + k];
-      rank += (sk > sj) || (sk == sj && k < j);
-    }
-    js.perm[b * n + rank] = j;
-  }
-  grid.sync();
-  // outputs: S, U[i][k] = At[perm k][i] / s, VH[k][:] = conj(Vt[perm k][:])
-  for (int64_t e = gtid; e < (int64_t)batch * n * n; e += gthreads) {
-    const int64_t b = e / ((int64_t)n * n);
-    const int64_t r = e % ((int64_t)n * n);
-    const int k = (int)(r / n), i = (int)(r % n);
-    const int src = js.perm[b * n + k];
-    const double sk = (double)js.nrm[b * n + src];
-    if (i == 0) S[b * n + k] = sk;
-    const double inv = sk > 0.0 ? 1.0 / sk : 0.0;
-    const T* a = js.At + b * mat + (int64_t)src * rl + (int64_t)i * cw;
-    double* u = U + b * mat + (int64_t)i * rl + (int64_t)k * cw;
-    u[0] = (double)a[0] * inv;
-    if (cplx) u[1] = (double)a[1] * inv;
-    const T* v = js.Vt + b * mat + (int64_t)src * rl + (int64_t)i * cw;
-    double* vh = VH + b * mat + (int64_t)k * rl + (int64_t)i * cw;
-    vh[0] = (double)v[0];
-    if (cplx) vh[1] = -(double)v[1];
-  }
+  if (S == nullptr) return;
+  jac_finish<CW>(n, batch, js, sweep, S, U, VH, info, grid);
 }
 
-// FP32 pre-pass + FP64 finish is used for real matrices from this size on
-constexpr int JACOBI_PRECOND_MIN_N = 128;
+// real matrices from this size on are solved through their transpose
+constexpr int JACOBI_TRANSPOSED_MIN_N = 64;
+constexpr size_t JAC_BLOCK_SMEM_MAX = 200 * 1024;
 
-template <typename T>
-static int jacobi_launch(const double* A, int n, int batch, int cplx, JacState<T>& js, double* S,
-                         double* U, double* VH, int* info, cudaStream_t st) {
-  const int np = n + (n & 1);
-  // one warp per column pair, 4 warps per CTA: spreads the FP64 work over
-  // as many SMs as there are pairs / 4
-  int want = (int)std::max<int64_t>(1, cdiv((int64_t)np / 2 * batch, 4));
-  int blocks = coop_blocks((const void*)jacobi_coop_kernel<T>, 128, 0, want);
-  void* args[] = {(void*)&A, (void*)&n, (void*)&batch, (void*)&cplx, (void*)&js,
-                  (void*)&S, (void*)&U, (void*)&VH, (void*)&info};
-  ProfScope prof(sizeof(T) == 8 ? "jacobi_svd_fp64" : "jacobi_pass_fp32", st, 0.0,
-                 (double)sizeof(T) * 3.0 * n * n * batch * (cplx ? 2 : 1));
-  PLOM_CHECK_CUDA(cudaLaunchCooperativeKernel((const void*)jacobi_coop_kernel<T>, dim3(blocks),
-                                              dim3(128), args, 0, st));
+static int64_t jac_pitch(int n, int cplx) {
+  const int64_t rl = (int64_t)n * (cplx ? 2 : 1);
+  return rl + (rl & 1);
+}
+
+template <int CW>
+static int jacobi_launch_cw(const double* A, int n, int batch, JacState& js, double tol2,
+                            double* S, double* U, double* VH, int* info, cudaStream_t st) {
+  void* args[] = {(void*)&A,    (void*)&n, (void*)&batch, (void*)&js, (void*)&tol2,
+                  (void*)&S,    (void*)&U, (void*)&VH,    (void*)&info};
+  const size_t smem = (size_t)16 * js.pitch * sizeof(double);
+  ProfScope prof("jacobi_svd_fp64", st, 0.0, 8.0 * 3.0 * n * n * batch * CW);
+  if (smem <= JAC_BLOCK_SMEM_MAX) {
+    const void* k = (const void*)jacobi_block_kernel<CW>;
+    PLOM_CHECK_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    const int nb = (n + 3) / 4;
+    const int nbp = std::max(2, nb + (nb & 1));
+    const int want = (int)std::max<int64_t>(1, (int64_t)nbp / 2 * batch);
+    const int blocks = coop_blocks(k, 128, smem, want);
+    PLOM_CHECK_CUDA(cudaLaunchCooperativeKernel(k, dim3(blocks), dim3(128), args, smem, st));
+  } else {
+    const void* k = (const void*)jacobi_pair_kernel<CW>;
+    const int want = (int)std::max<int64_t>(1, cdiv((int64_t)(n + (n & 1)) / 2 * batch, 4));
+    const int blocks = coop_blocks(k, 128, 0, want);
+    PLOM_CHECK_CUDA(cudaLaunchCooperativeKernel(k, dim3(blocks), dim3(128), args, 0, st));
+  }
   return PLOM_OK;
 }
 
-template <typename T>
-static void carve_jac(Arena& ws, JacState<T>& js, int n, int batch, int cplx) {
-  const size_t mat = (size_t)n * n * (cplx ? 2 : 1);
-  js.At = ws.take<T>(mat * batch);
-  js.Vt = ws.take<T>(mat * batch);
+static int jacobi_launch(const double* A, int n, int batch, int cplx, JacState& js, double tol,
+                         double* S, double* U, double* VH, int* info, cudaStream_t st) {
+  const double tol2 = tol * tol;
+  return cplx ? jacobi_launch_cw<2>(A, n, batch, js, tol2, S, U, VH, info, st)
+              : jacobi_launch_cw<1>(A, n, batch, js, tol2, S, U, VH, info, st);
+}
+
+static void carve_jac(Arena& ws, JacState& js, int n, int batch, int cplx) {
+  js.pitch = jac_pitch(n, cplx);
+  const size_t mat = (size_t)n * js.pitch;
+  js.At = ws.take<double>(mat * batch);
+  js.Vt = ws.take<double>(mat * batch);
+  js.nrm2 = ws.take<double>((size_t)batch * n);
+  js.dsc = ws.take<double>((size_t)batch * n);
   js.counts = ws.take<int>(JACOBI_MAX_SWEEPS);
   js.perm = ws.take<int>((size_t)batch * n);
-  js.nrm = ws.take<T>((size_t)batch * n);
+  js.amax = ws.take<unsigned long long>((size_t)batch);
 }
 
 size_t dense_workspace(int n, int batch, int cplx) {
   Arena a(nullptr, 0);
-  JacState<double> js;
+  if (!cplx && batch == 1 && n >= JACOBI_TRANSPOSED_MIN_N) a.take<double>(3 * (size_t)n * n);
+  JacState js;
   carve_jac(a, js, n, batch, cplx);
   return a.off + 256;
 }
 
-// Real n x n SVD with an FP32 pre-pass: one-sided Jacobi in FP32 yields V0;
-// V0 is re-orthogonalised in FP64 (one CholeskyQR step), A1 = A V0 has
-// nearly orthogonal columns, and the FP64 Jacobi on A1 converges in a few
-// sweeps; V = V0 V1.
-static int jacobi_svd_precond(const double* A, int n, double* S, double* U, double* VH, int* info,
-                              Arena& ws, cudaStream_t st) {
+// Real n x n SVD through the transpose: one-sided Jacobi on A^T (whose
+// columns are the rows of A) needs fewer sweeps than on A for the
+// triangular factors of the TSQR.  A^T = Ut S Vt^T  ->  A = Vt S Ut^T.
+static int jacobi_svd_transposed(const double* A, int n, double tol, double* S, double* U,
+                                 double* VH, int* info, Arena& ws, cudaStream_t st) {
   const size_t nn = (size_t)n * n;
-  JacState<float> j32;
-  carve_jac(ws, j32, n, 1, 0);
-  double* V0 = ws.take<double>(nn);
-  double* G = ws.take<double>(nn);
-  double* Rv = ws.take<double>(nn);
-  double* Wv = ws.take<double>(nn);
-  double* V0n = ws.take<double>(nn);
-  double* A1 = ws.take<double>(nn);
-  double* VH1 = ws.take<double>(nn);
-  double* V0nT = ws.take<double>(nn);
-  const size_t mark = ws.off;
-  size_t need = mark;
-  // FP64 pass state (reuses the scratch after the small FP64 products)
-  JacState<double> j64;
-  carve_jac(ws, j64, n, 1, 0);
-  need = std::max(need, ws.off);
-  ws.off = mark;
-  if (ws.measuring()) {
-    gemm_tn<double, double, double, double>(V0, n, V0, n, G, n, n, n, n, true, ws, st);
-    need = std::max(need, ws.off);
-    ws.off = mark;
-    chol_shifted(G, Rv, n, 1, 0.0, 1e-12, info, ws, st);
-    need = std::max(need, ws.off);
-    ws.off = mark;
-    trtri_upper(Rv, Wv, n, 1, ws, st);
-    ws.off = std::max(need, ws.off);
-    return PLOM_OK;
-  }
+  double* At = ws.take<double>(nn);
+  double* Ut = ws.take<double>(nn);
+  double* VHt = ws.take<double>(nn);
+  JacState js;
+  carve_jac(ws, js, n, 1, 0);
+  if (ws.measuring()) return PLOM_OK;
   PLOM_REQUIRE(!ws.overflow(), PLOM_ERR_WORKSPACE, "jacobi: workspace too small");
-  PLOM_TRY(jacobi_launch<float>(A, n, 1, 0, j32, nullptr, nullptr, nullptr, info, st));
-  {
-    double* Vt64 = A1;  // temporarily: rows = v_k in FP64
-    PLOM_TRY((convert<float, double>(j32.Vt, Vt64, (int64_t)nn, st)));
-    PLOM_TRY(transpose_f64(Vt64, V0, n, n, 1, st));  // columns = v_k
-  }
-  PLOM_TRY((gemm_tn<double, double, double, double>(V0, n, V0, n, G, n, n, n, n, true, ws, st)));
-  need = std::max(need, ws.off);
-  ws.off = mark;
-  PLOM_TRY(chol_shifted(G, Rv, n, 1, 0.0, 1e-12, info, ws, st));
-  need = std::max(need, ws.off);
-  ws.off = mark;
-  PLOM_TRY(trtri_upper(Rv, Wv, n, 1, ws, st));
-  need = std::max(need, ws.off);
-  ws.off = mark;
-  PLOM_TRY((gemm_nn<double, double, double, double>(V0, n, Wv, n, V0n, n, n, n, n, st)));
-  PLOM_TRY((gemm_nn<double, double, double, double>(A, n, V0n, n, A1, n, n, n, n, st)));
-  carve_jac(ws, j64, n, 1, 0);
-  PLOM_TRY(jacobi_launch<double>(A1, n, 1, 0, j64, S, U, VH1, info, st));
-  // VH = VH1 V0n^T  (row k = (V0n v1_k)^T)
-  PLOM_TRY(transpose_f64(V0n, V0nT, n, n, 1, st));
-  PLOM_TRY((gemm_nn<double, double, double, double>(VH1, n, V0nT, n, VH, n, n, n, n, st)));
-  ws.off = std::max(need, ws.off);
+  PLOM_REQUIRE(A && S && U && VH && info, PLOM_ERR_ARG, "jacobi: null pointer");
+  PLOM_TRY(transpose_f64(A, At, n, n, 1, st));
+  PLOM_TRY(jacobi_launch(At, n, 1, 0, js, tol, S, Ut, VHt, info, st));
+  PLOM_TRY(transpose_f64(VHt, U, n, n, 1, st));   // U of A = Vt (columns)
+  PLOM_TRY(transpose_f64(Ut, VH, n, n, 1, st));   // rows of V^T of A = columns of Ut
   return PLOM_OK;
 }
 
-int jacobi_svd(const double* A, int n, int batch, int cplx, double* S, double* U, double* VH,
-               int* info, Arena& ws, cudaStream_t st) {
-  if (!cplx && batch == 1 && n >= JACOBI_PRECOND_MIN_N)
-    return jacobi_svd_precond(A, n, S, U, VH, info, ws, st);
-  JacState<double> js;
+int jacobi_svd(const double* A, int n, int batch, int cplx, double tol, double* S, double* U,
+               double* VH, int* info, Arena& ws, cudaStream_t st) {
+  if (!(tol > 0.0)) tol = 2.220446049250313e-16 * (double)std::max(n, 1);
+  if (!cplx && batch == 1 && n >= JACOBI_TRANSPOSED_MIN_N)
+    return jacobi_svd_transposed(A, n, tol, S, U, VH, info, ws, st);
+  JacState js;
   carve_jac(ws, js, n, batch, cplx);
   if (ws.measuring() || n == 0 || batch == 0) return PLOM_OK;
   PLOM_REQUIRE(!ws.overflow(), PLOM_ERR_WORKSPACE, "jacobi: workspace too small");
   PLOM_REQUIRE(A && S && U && VH && info, PLOM_ERR_ARG, "jacobi: null pointer");
-  return jacobi_launch<double>(A, n, batch, cplx, js, S, U, VH, info, st);
+  return jacobi_launch(A, n, batch, cplx, js, tol, S, U, VH, info, st);
 }
 
 // ---------------------------------------------------------------------------

@@ -1,0 +1,920 @@
+// Tensor-core (tcgen05, sm_103a) tall products of the mixed form on
+// "fp16 pairs".
+//
+// A tall FP32 operand Y (m x N) is packed once into two fp16 planes,
+//     hi = fp16(y s_j),  lo = fp16(y s_j - hi),
+// with a power-of-two scale s_j per column (max |y s_j| in [2^13, 2^14)), so
+// hi + lo carries 22 significant bits of y s_j.  Products run on the f16
+// tensor pipe (kind::f16, FP32 accumulation in TMEM) as hi*hi + hi*lo + lo*hi
+// (the dropped lo*lo term is below 2^-22 |x y|), at twice the rate of TF32
+// and with half the operand bytes.  Both planes are row-major m x ldp
+// (ldp = N rounded up to 64; padding columns are zero), which serves both
+// products without a transpose:
+//
+//  gram_packed  G (N x N, FP64) = Y^T Y over the m rows.  Upper 128 x 128
+//               tiles x row chunks; operands are MN-major 128-byte-swizzled
+//               tiles straight from TMA (the row-major planes are MN-major for
+//               Y^T Y).  Every 4096 rows the FP32 TMEM accumulators (hi*hi and
+//               the correction terms kept apart) are drained into an FP64
+//               partial, and the diagonal of a diagonal tile (sums of squares,
+//               where the FP32 accumulation bias does not cancel) is summed
+//               on the CUDA cores with compensated FP32 sums folded into FP64.
+//               Partials are summed in FP64 in a fixed order.
+//  apply_packed C (m x k) = Y W for a small FP64 W: the row-major planes are
+//               the K-major A operand; W is scaled per column and split into
+//               K-major fp16 hi/lo copies once.  The epilogue writes FP32 C or
+//               the packed planes of C (scale 2^14), ready for the next
+//               product.  Persistent CTAs; two TMEM accumulator buffers so the
+//               epilogue of one tile overlaps the products of the next.
+//
+// Every mbarrier wait is bounded (%globaltimer, 2 s); on expiry the CTA
+// records PLOM_NUM_TIMEOUT in the caller's info word, stops issuing work,
+// frees its TMEM and returns.
+#include <cuda.h>
+#include <cudaTypedefs.h>
+#include <cuda_fp16.h>
+
+#include <algorithm>
+#include <mutex>
+
+#include "plom_common.cuh"
+#include "plom_kernels.cuh"
+#include "plom_tc.cuh"
+
+namespace plom {
+namespace hp {
+
+constexpr uint64_t WAIT_NS = 2000000000ull;
+constexpr int PK_LOG2 = 14;  // packed values: max |y s| in [2^13, 2^14)
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ uint64_t gtimer() {
+  uint64_t t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count));
+}
+__device__ __forceinline__ void mbar_fence_init() {
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+  asm volatile("mbarrier.arrive.release.cta.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar))
+               : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)),
+               "r"(bytes)
+               : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.acquire.cta.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+// Bounded wait.  False (and the CTA abort flag raised) on expiry, or when
+// another role of the CTA or another CTA of the launch already gave up.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, volatile int* abort_flag,
+                                          int* err) {
+  if (mbar_try_wait(bar, parity)) return true;
+  const uint64_t t0 = gtimer();
+  uint32_t spins = 0;
+  while (true) {
+    if (mbar_try_wait(bar, parity)) return true;
+    if (*abort_flag) return false;
+    if ((++spins & 1023u) == 0 && err && *(volatile int*)err == PLOM_NUM_TIMEOUT) {
+      *abort_flag = 1;
+      return false;
+    }
+    if (gtimer() - t0 > WAIT_NS) {
+      *abort_flag = 1;
+      if (err) atomicMax(err, PLOM_NUM_TIMEOUT);
+      return false;
+    }
+  }
+}
+__device__ __forceinline__ bool launch_aborted(const int* err) {
+  return err && *(volatile const int*)err == PLOM_NUM_TIMEOUT;
+}
+__device__ __forceinline__ void tmem_alloc(uint32_t* dst, uint32_t ncols) {
+  asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                   smem_u32(dst)),
+               "r"(ncols)
+               : "memory");
+}
+__device__ __forceinline__ void tmem_relinquish() {
+  asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+}
+__device__ __forceinline__ void tmem_dealloc(uint32_t taddr, uint32_t ncols) {
+  asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(ncols)
+               : "memory");
+}
+__device__ __forceinline__ void fence_before() {
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+}
+__device__ __forceinline__ void fence_after() {
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+}
+__device__ __forceinline__ void mma_f16(uint32_t d_tmem, uint64_t adesc, uint64_t bdesc,
+                                        uint32_t idesc, uint32_t accum) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "setp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(d_tmem),
+      "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accum)
+      : "memory");
+}
+__device__ __forceinline__ void mma_commit(uint64_t* bar) {
+  asm volatile(
+      "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+          smem_u32(bar))
+      : "memory");
+}
+// 32 lanes x 32 consecutive 32-bit columns; thread i of the warp gets lane
+// (32 * (warp % 4) + i) of the addressed quarter.
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&r)[32]) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x32.b32 "
+      "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+      "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+        "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
+        "=r"(r[14]), "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]),
+        "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]),
+        "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+      : "r"(taddr));
+}
+__device__ __forceinline__ void tmem_wait_ld() {
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+}
+// 3-D tiled TMA load (plane z of the packed planes).  x is a multiple of 64
+// fp16 (128 bytes) at every call site.
+__device__ __forceinline__ void tma_load_3d(uint32_t dst, const CUtensorMap* map, int x, int y,
+                                            int z, uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes "
+      "[%0], [%1, {%2, %3, %4}], [%5];" ::"r"(dst),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(z), "r"(smem_u32(bar))
+      : "memory");
+}
+__device__ __forceinline__ void tma_prefetch_map(const CUtensorMap* map) {
+  asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(map)) : "memory");
+}
+
+// Shared-memory matrix descriptor, 128-byte swizzle, sm_100 version 1.
+//  K-major tiles: 8-row core groups 1024 bytes apart (SBO), LBO unused.
+//  MN-major tiles: 64-element swizzle atoms LBO bytes apart along M/N, 8-row
+//  K groups 1024 bytes apart (SBO).
+__device__ __forceinline__ uint64_t desc_sw128(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
+  uint64_t d = 0;
+  d |= (uint64_t)((saddr >> 4) & 0x3FFFu);
+  d |= (uint64_t)((lbo >> 4) & 0x3FFFu) << 16;
+  d |= (uint64_t)((sbo >> 4) & 0x3FFFu) << 32;
+  d |= (uint64_t)1 << 46;
+  d |= (uint64_t)2 << 61;
+  return d;
+}
+// Instruction descriptor: kind::f16, D = F32, A = B = F16; a_mn/b_mn select
+// MN-major operands.
+__host__ __device__ constexpr uint32_t idesc_f16(int M, int N, int a_mn, int b_mn) {
+  return (1u << 4) | ((uint32_t)a_mn << 15) | ((uint32_t)b_mn << 16) |
+         ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+}
+
+__device__ __forceinline__ uint16_t ld_shared_u16(uint32_t addr) {
+  uint16_t v;
+  asm volatile("ld.shared.u16 %0, [%1];" : "=h"(v) : "r"(addr));
+  return v;
+}
+
+// ---------------------------------------------------------------------------
+// packing
+// ---------------------------------------------------------------------------
+// column maxima of |Y| (bits of non-negative floats order like unsigned ints)
+__global__ void colmax_kernel(const float* __restrict__ Y, int64_t ld, int64_t m, int N,
+                              unsigned* __restrict__ cmax) {
+  const int64_t rows = (m + gridDim.x - 1) / gridDim.x;
+  const int64_t r0 = (int64_t)blockIdx.x * rows;
+  const int64_t r1 = (r0 + rows < m) ? r0 + rows : m;
+  for (int c = threadIdx.x; c < N; c += blockDim.x) {
+    float mx = 0.f;
+#pragma unroll 8
+    for (int64_t r = r0; r < r1; ++r) mx = fmaxf(mx, fabsf(Y[r * ld + c]));
+    if (mx > 0.f) atomicMax(&cmax[c], __float_as_uint(mx));
+  }
+}
+
+// s_j = 2^(14 - e_j) with max_j = f 2^e_j, f in [0.5, 1); 1 for zero or
+// padding columns (clamped so that s_j stays a finite float)
+__global__ void colscale_kernel(const unsigned* __restrict__ cmax, int N, int ldp,
+                                float* __restrict__ s) {
+  for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < ldp; j += gridDim.x * blockDim.x) {
+    const float v = (j < N) ? __uint_as_float(cmax[j]) : 0.f;
+    int e = 0;
+    frexpf(v, &e);
+    e = e < -100 ? -100 : e;
+    s[j] = (v > 0.f) ? ldexpf(1.f, PK_LOG2 - e) : 1.f;
+  }
+}
+
+__global__ void fill_scale_kernel(float* __restrict__ s, int ldp, float v) {
+  for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < ldp; j += gridDim.x * blockDim.x)
+    s[j] = v;
+}
+
+__device__ __forceinline__ void split8(const float (&v)[8], uint4& h, uint4& l) {
+  uint32_t hw[4], lw[4];
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    const __half h0 = __float2half_rn(v[2 * q]), h1 = __float2half_rn(v[2 * q + 1]);
+    const __half l0 = __float2half_rn(v[2 * q] - __half2float(h0));
+    const __half l1 = __float2half_rn(v[2 * q + 1] - __half2float(h1));
+    hw[q] = (uint32_t)__half_as_ushort(h0) | ((uint32_t)__half_as_ushort(h1) << 16);
+    lw[q] = (uint32_t)__half_as_ushort(l0) | ((uint32_t)__half_as_ushort(l1) << 16);
+  }
+  h = make_uint4(hw[0], hw[1], hw[2], hw[3]);
+  l = make_uint4(lw[0], lw[1], lw[2], lw[3]);
+}
+
+// hi/lo planes (m x ldp) of Y diag(s); columns N..ldp-1 are zero
+__global__ void pack_kernel(const float* __restrict__ Y, int64_t ld, int64_t m, int N, int ldp,
+                            const float* __restrict__ s, __half* __restrict__ hi,
+                            __half* __restrict__ lo, int vec) {
+  const int groups = ldp / 8;
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < m * groups;
+       e += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t r = e / groups;
+    const int c0 = (int)(e % groups) * 8;
+    const float* src = Y + r * ld + c0;
+    float v[8];
+    if (vec && c0 + 8 <= N) {
+      const float4 a = __ldg(reinterpret_cast<const float4*>(src));
+      const float4 b = __ldg(reinterpret_cast<const float4*>(src + 4));
+      v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w;
+      v[4] = b.x; v[5] = b.y; v[6] = b.z; v[7] = b.w;
+    } else {
+#pragma unroll
+      for (int q = 0; q < 8; ++q) v[q] = (c0 + q < N) ? src[q] : 0.f;
+    }
+#pragma unroll
+    for (int q = 0; q < 8; ++q) v[q] *= s[c0 + q];
+    uint4 h, l;
+    split8(v, h, l);
+    *reinterpret_cast<uint4*>(hi + r * ldp + c0) = h;
+    *reinterpret_cast<uint4*>(lo + r * ldp + c0) = l;
+  }
+}
+
+// W (nin x k, FP64, ldw) -> Bt hi/lo (k rows x ldk, K-major fp16) of
+// diag(1/s_in) W diag(t) with t_j a power of two (max |.| in [2^13, 2^14)),
+// and the epilogue factor f_j = out_scale / t_j.  One block per column j of
+// W; blocks j >= k write f_j = 0 (their Bt rows are never read).
+__global__ void __launch_bounds__(256) split_w16_kernel(const double* __restrict__ W,
+                                                        int64_t ldw, int nin, int k, int ldk,
+                                                        const float* __restrict__ s_in,
+                                                        float out_scale, __half* __restrict__ bhi,
+                                                        __half* __restrict__ blo,
+                                                        float* __restrict__ f) {
+  __shared__ double red[8];
+  const int j = blockIdx.x;
+  if (j >= k) {
+    if (threadIdx.x == 0) f[j] = 0.f;
+    return;
+  }
+  // 1 / s_in is exact (powers of two)
+  double mx = 0.0;
+  for (int i = threadIdx.x; i < nin; i += blockDim.x)
+    mx = fmax(mx, fabs(W[(int64_t)i * ldw + j] * (double)(1.0f / s_in[i])));
+  mx = warp_max(mx);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = mx;
+  __syncthreads();
+  mx = 0.0;
+  for (int w = 0; w < 8; ++w) mx = fmax(mx, red[w]);
+  int e = 0;
+  frexp(mx, &e);
+  e = e < -900 ? -900 : (e > 900 ? 900 : e);
+  const double t = (mx > 0.0) ? ldexp(1.0, PK_LOG2 - e) : 1.0;
+  for (int i = threadIdx.x; i < ldk; i += blockDim.x) {
+    const float x = (i < nin) ? (float)(W[(int64_t)i * ldw + j] * (double)(1.0f / s_in[i]) * t) : 0.f;
+    const __half h = __float2half_rn(x);
+    const __half l = __float2half_rn(x - __half2float(h));
+    bhi[(int64_t)j * ldk + i] = h;
+    blo[(int64_t)j * ldk + i] = l;
+  }
+  if (threadIdx.x == 0) f[j] = (float)((double)out_scale / t);
+}
+
+// ---------------------------------------------------------------------------
+// gram: upper 128 x 128 tiles x row chunks, MN-major operands from TMA
+// ---------------------------------------------------------------------------
+constexpr int G_BK = 64;                       // rows per stage
+constexpr uint32_t G_BOX = 64 * 128;           // 64 rows x 64 fp16 (8 KB)
+constexpr uint32_t G_TILE = 2 * G_BOX;         // 64 rows x 128 columns of one plane
+constexpr uint32_t G_STAGE = 4 * G_TILE;       // A hi, A lo, B hi, B lo
+constexpr int G_STAGES = 3;
+// Rows accumulated in TMEM (FP32) before the FP64 drain: 256 UMMA of K = 16
+// per accumulator.
+constexpr int G_KSUB = 4096;
+constexpr size_t G_SMEM = (size_t)G_STAGES * G_STAGE + 1024;
+constexpr uint32_t G_TMEM = 512;               // 2 buffers x (main 128 + correction 128)
+
+__global__ void __launch_bounds__(320, 1)
+    gram16_kernel(const __grid_constant__ CUtensorMap tmP, int64_t m, int tn,
+                  int64_t rows_per_chunk, int chunks, double* __restrict__ part, int* err) {
+  extern __shared__ uint8_t smem_raw[];
+  __shared__ uint64_t full_bar[G_STAGES], empty_bar[G_STAGES];
+  __shared__ uint64_t tfull[2], tempty[2], dfull[2];
+  __shared__ double diag_sh[2][128];
+  __shared__ uint32_t tmem_sh;
+  __shared__ int abort_sh;
+  const uint32_t base = (smem_u32(smem_raw) + 1023u) & ~1023u;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  // consecutive CTAs take different tiles of the same row chunk, so the CTAs
+  // resident together read the same rows and share them through L2
+  const int ntiles = tn * (tn + 1) / 2;
+  const int chunk = (int)(blockIdx.x / ntiles), tile = (int)(blockIdx.x % ntiles);
+  const int item = tile * chunks + chunk;  // partial slab index (tile-major)
+  int ti = 0, rem = tile;
+  while (rem >= tn - ti) {
+    rem -= tn - ti;
+    ++ti;
+  }
+  const int tj = ti + rem;
+  const bool diag = (ti == tj);
+  const int I0 = ti * 128, J0 = tj * 128;
+  const int64_t r_beg = (int64_t)chunk * rows_per_chunk;
+  const int64_t r_end = (r_beg + rows_per_chunk < m) ? r_beg + rows_per_chunk : m;
+  const int64_t nrows = (r_end > r_beg) ? r_end - r_beg : 0;
+  const int KB = (int)((nrows + G_BK - 1) / G_BK);
+  constexpr int KB_PER_SUB = G_KSUB / G_BK;
+  const int nsub = (KB + KB_PER_SUB - 1) / KB_PER_SUB;
+  if (launch_aborted(err)) return;
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < G_STAGES; ++s) {
+      mbar_init(&full_bar[s], 1);
+      mbar_init(&empty_bar[s], diag ? 1 + 128 : 1);  // MMA commit (+ diagonal warps)
+    }
+    for (int b = 0; b < 2; ++b) {
+      mbar_init(&tfull[b], 1);
+      mbar_init(&tempty[b], 128);
+      mbar_init(&dfull[b], 128);
+    }
+    abort_sh = 0;
+    mbar_fence_init();
+  }
+  if (warp == 8) {
+    tmem_alloc(&tmem_sh, G_TMEM);
+    tmem_relinquish();
+  }
+  if (warp == 9 && lane == 0) tma_prefetch_map(&tmP);
+  fence_before();
+  __syncthreads();
+  fence_after();
+  const uint32_t tmem = tmem_sh;
+  double* P = part + (int64_t)item * 128 * 128;
+
+  if (warp == 9) {
+    // ---- TMA producer: 64 rows x (I block [+ J block]) of both planes
+    if (lane == 0) {
+      const uint32_t bytes = (diag ? 2u : 4u) * G_TILE;
+      for (int kb = 0; kb < KB; ++kb) {
+        const int s = kb % G_STAGES;
+        const uint32_t ph = (uint32_t)(kb / G_STAGES) & 1u;
+        if (!mbar_wait(&empty_bar[s], ph ^ 1u, &abort_sh, err)) break;
+        const uint32_t st = base + s * G_STAGE;
+        const int y = (int)(r_beg + (int64_t)kb * G_BK);
+        mbar_expect_tx(&full_bar[s], bytes);
+#pragma unroll
+        for (int z = 0; z < 2; ++z) {
+          tma_load_3d(st + z * G_TILE, &tmP, I0, y, z, &full_bar[s]);
+          tma_load_3d(st + z * G_TILE + G_BOX, &tmP, I0 + 64, y, z, &full_bar[s]);
+          if (!diag) {
+            tma_load_3d(st + (2 + z) * G_TILE, &tmP, J0, y, z, &full_bar[s]);
+            tma_load_3d(st + (2 + z) * G_TILE + G_BOX, &tmP, J0 + 64, y, z, &full_bar[s]);
+          }
+        }
+      }
+    }
+  } else if (warp >= 4 && warp < 8) {
+    // ---- diagonal tiles: compensated sums of (hi + lo)^2 per column
+    if (diag) {
+      const int c = threadIdx.x - 128;           // column of the I block
+      const uint32_t cb = (uint32_t)(c >> 6) * G_BOX;
+      const uint32_t w = (uint32_t)(c & 63);
+      const uint32_t ch = w >> 3, within = (w & 7u) * 2u;
+      float sum = 0.f, cmp = 0.f;
+      for (int kb = 0; kb < KB; ++kb) {
+        const int s = kb % G_STAGES;
+        const uint32_t ph = (uint32_t)(kb / G_STAGES) & 1u;
+        if (!mbar_wait(&full_bar[s], ph, &abort_sh, err)) break;
+        const uint32_t st = base + s * G_STAGE + cb;
+#pragma unroll 8
+        for (uint32_t k = 0; k < (uint32_t)G_BK; ++k) {
+          const uint32_t off = (k >> 3) * 1024u + (k & 7u) * 128u + (((ch ^ (k & 7u)) << 4) | within);
+          const float v = __half2float(__ushort_as_half(ld_shared_u16(st + off))) +
+                          __half2float(__ushort_as_half(ld_shared_u16(st + G_TILE + off)));
+          const float y = fmaf(v, v, -cmp);
+          const float t = sum + y;
+          cmp = (t - sum) - y;
+          sum = t;
+        }
+        mbar_arrive(&empty_bar[s]);
+        if ((kb % KB_PER_SUB) == KB_PER_SUB - 1 || kb == KB - 1) {
+          const int b = (kb / KB_PER_SUB) & 1;
+          diag_sh[b][c] = (double)sum - (double)cmp;
+          sum = cmp = 0.f;
+          mbar_arrive(&dfull[b]);
+        }
+      }
+    }
+  } else if (warp == 8 && lane == 0) {
+    // ---- UMMA issuer: main += hi*hi, correction += hi*lo + lo*hi
+    constexpr uint32_t idesc = idesc_f16(128, 128, 1, 1);
+    bool ok = true;
+    int kb = 0;
+    for (int sub = 0; sub < nsub && ok; ++sub) {
+      const int b = sub & 1;
+      if (!mbar_wait(&tempty[b], (((uint32_t)sub >> 1) & 1u) ^ 1u, &abort_sh, err)) {
+        ok = false;
+        break;
+      }
+      fence_after();
+      const uint32_t dmain = tmem + (uint32_t)(b * 256);
+      const uint32_t dcorr = dmain + 128u;
+      const int kb_end = (kb + KB_PER_SUB < KB) ? kb + KB_PER_SUB : KB;
+      for (int kl = 0; kb < kb_end; ++kb, ++kl) {
+        const int s = kb % G_STAGES;
+        const uint32_t ph = (uint32_t)(kb / G_STAGES) & 1u;
+        if (!mbar_wait(&full_bar[s], ph, &abort_sh, err)) {
+          ok = false;
+          break;
+        }
+        fence_after();
+        const uint32_t st = base + s * G_STAGE;
+        const uint32_t aH = st, aL = st + G_TILE;
+        const uint32_t bH = diag ? aH : st + 2 * G_TILE, bL = diag ? aL : st + 3 * G_TILE;
+#pragma unroll
+        for (int kk = 0; kk < G_BK / 16; ++kk) {
+          const uint32_t adv = (uint32_t)kk * 2048u;  // 16 rows of 128 bytes
+          const uint64_t dAH = desc_sw128(aH + adv, G_BOX, 1024), dAL = desc_sw128(aL + adv, G_BOX, 1024);
+          const uint64_t dBH = desc_sw128(bH + adv, G_BOX, 1024), dBL = desc_sw128(bL + adv, G_BOX, 1024);
+          const uint32_t first = (kl > 0 || kk > 0) ? 1u : 0u;
+          mma_f16(dmain, dAH, dBH, idesc, first);
+          mma_f16(dcorr, dAH, dBL, idesc, first);
+          mma_f16(dcorr, dAL, dBH, idesc, 1u);
+        }
+        mma_commit(&empty_bar[s]);
+      }
+      if (ok) mma_commit(&tfull[b]);
+    }
+  } else if (warp < 4) {
+    // ---- epilogue: drain each finished sub-chunk into the FP64 partial
+    const int rloc = warp * 32 + lane;
+    for (int sub = 0; sub < nsub; ++sub) {
+      const int b = sub & 1;
+      const uint32_t par = ((uint32_t)sub >> 1) & 1u;
+      bool ready = mbar_wait(&tfull[b], par, &abort_sh, err);
+      if (diag) ready = ready && mbar_wait(&dfull[b], par, &abort_sh, err);
+      __syncwarp();
+      if (!__all_sync(0xffffffffu, ready)) break;
+      fence_after();
+      const double dval = diag ? diag_sh[b][rloc] : 0.0;
+      double* prow = P + (int64_t)rloc * 128;
+#pragma unroll 1
+      for (int cc = 0; cc < 4; ++cc) {
+        uint32_t rm[32], rc[32];
+        const uint32_t ta = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(b * 256 + cc * 32);
+        tmem_ld32(ta, rm);
+        tmem_ld32(ta + 128, rc);
+        tmem_wait_ld();
+        double* d = prow + cc * 32;
+#pragma unroll
+        for (int j = 0; j < 32; j += 2) {
+          double v0 = (double)__uint_as_float(rm[j]) + (double)__uint_as_float(rc[j]);
+          double v1 = (double)__uint_as_float(rm[j + 1]) + (double)__uint_as_float(rc[j + 1]);
+          if (diag && cc * 32 + j == rloc) v0 = dval;
+          if (diag && cc * 32 + j + 1 == rloc) v1 = dval;
+          if (sub == 0) {
+            *reinterpret_cast<double2*>(d + j) = make_double2(v0, v1);
+          } else {
+            double2 o = *reinterpret_cast<double2*>(d + j);
+            o.x += v0;
+            o.y += v1;
+            *reinterpret_cast<double2*>(d + j) = o;
+          }
+        }
+      }
+      fence_before();
+      mbar_arrive(&tempty[b]);
+    }
+    if (nsub == 0) {  // empty chunk: the partial is zero
+      double* prow = P + (int64_t)rloc * 128;
+      for (int j = 0; j < 128; ++j) prow[j] = 0.0;
+    }
+  }
+  fence_before();
+  __syncthreads();
+  if (warp == 8) {
+    __syncwarp();
+    fence_after();
+    tmem_dealloc(tmem, G_TMEM);
+  }
+}
+
+// G[i][j] = sum over chunks of the tile partials (fixed order) / (s_i s_j), mirrored
+__global__ void gram16_reduce_kernel(const double* __restrict__ part, int N, int tn, int chunks,
+                                     const float* __restrict__ s, double* __restrict__ G) {
+  const int64_t total = (int64_t)N * N;
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < total;
+       e += (int64_t)gridDim.x * blockDim.x) {
+    const int i = (int)(e / N), j = (int)(e % N);
+    int a = i, b = j;
+    if (a / 128 > b / 128) {
+      a = j;
+      b = i;
+    }
+    const int ti = a / 128, tj = b / 128;
+    const int tile = ti * tn - ti * (ti - 1) / 2 + (tj - ti);
+    const double* p = part + ((int64_t)tile * chunks) * 128 * 128 + (int64_t)(a - ti * 128) * 128 +
+                      (b - tj * 128);
+    double acc = 0.0;
+    for (int c = 0; c < chunks; ++c) acc += p[(int64_t)c * 128 * 128];
+    G[e] = acc / ((double)s[i] * (double)s[j]);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// apply: C (m x k) = Y W, persistent CTAs over 128 x 128 output tiles
+// ---------------------------------------------------------------------------
+constexpr int A_BK = 64;                       // K per stage (one 128-byte row)
+constexpr uint32_t A_TILE = 128 * 128;         // 128 rows x 64 fp16 (16 KB)
+constexpr uint32_t A_STAGE = 4 * A_TILE;       // A hi, A lo, B hi, B lo
+constexpr int A_STAGES = 3;
+constexpr size_t A_SMEM = (size_t)A_STAGES * A_STAGE + 1024;
+
+struct ApplyOut {
+  float* C;        // FP32 output (m x k, ldc) or nullptr
+  int64_t ldc;
+  __half* ohi;     // packed output planes (m x ldo) or nullptr
+  __half* olo;
+  int ldo;
+};
+
+__global__ void __launch_bounds__(192, 1)
+    apply16_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
+                   int64_t m, int kblocks, int k, int64_t col_tiles, int64_t tiles,
+                   const float* __restrict__ f, ApplyOut out, int* err) {
+  extern __shared__ uint8_t smem_raw[];
+  __shared__ uint64_t full_bar[A_STAGES], empty_bar[A_STAGES], tfull[2], tempty[2];
+  __shared__ uint32_t tmem_sh;
+  __shared__ int abort_sh;
+  const uint32_t base = (smem_u32(smem_raw) + 1023u) & ~1023u;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (launch_aborted(err)) return;
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < A_STAGES; ++s) {
+      mbar_init(&full_bar[s], 1);
+      mbar_init(&empty_bar[s], 1);
+    }
+    for (int b = 0; b < 2; ++b) {
+      mbar_init(&tfull[b], 1);
+      mbar_init(&tempty[b], 128);
+    }
+    abort_sh = 0;
+    mbar_fence_init();
+  }
+  if (warp == 4) {
+    tmem_alloc(&tmem_sh, 512);  // 2 buffers x (main 128 + correction 128)
+    tmem_relinquish();
+  }
+  if (warp == 5 && lane == 0) {
+    tma_prefetch_map(&tmA);
+    tma_prefetch_map(&tmB);
+  }
+  fence_before();
+  __syncthreads();
+  fence_after();
+  const uint32_t tmem = tmem_sh;
+
+  if (warp == 5) {
+    // ---- TMA producer, running ahead across tiles
+    if (lane == 0) {
+      int64_t g = 0;
+      bool ok = true;
+      for (int64_t t = blockIdx.x; t < tiles && ok; t += gridDim.x) {
+        const int rb = (int)(t / col_tiles), cb = (int)(t % col_tiles);
+        for (int kb = 0; kb < kblocks; ++kb, ++g) {
+          const int s = (int)(g % A_STAGES);
+          const uint32_t ph = (uint32_t)(g / A_STAGES) & 1u;
+          if (!mbar_wait(&empty_bar[s], ph ^ 1u, &abort_sh, err)) {
+            ok = false;
+            break;
+          }
+          const uint32_t st = base + s * A_STAGE;
+          mbar_expect_tx(&full_bar[s], A_STAGE);
+          tma_load_3d(st, &tmA, kb * A_BK, rb * 128, 0, &full_bar[s]);
+          tma_load_3d(st + A_TILE, &tmA, kb * A_BK, rb * 128, 1, &full_bar[s]);
+          tma_load_3d(st + 2 * A_TILE, &tmB, kb * A_BK, cb * 128, 0, &full_bar[s]);
+          tma_load_3d(st + 3 * A_TILE, &tmB, kb * A_BK, cb * 128, 1, &full_bar[s]);
+        }
+      }
+    }
+  } else if (warp == 4) {
+    // ---- UMMA issuer
+    if (lane == 0) {
+      constexpr uint32_t idesc = idesc_f16(128, 128, 0, 0);
+      int64_t g = 0;
+      int i = 0;
+      bool ok = true;
+      for (int64_t t = blockIdx.x; t < tiles && ok; t += gridDim.x, ++i) {
+        const int b = i & 1;
+        if (!mbar_wait(&tempty[b], (((uint32_t)i >> 1) & 1u) ^ 1u, &abort_sh, err)) {
+          ok = false;
+          break;
+        }
+        fence_after();
+        const uint32_t dmain = tmem + (uint32_t)(b * 256);
+        const uint32_t dcorr = dmain + 128u;
+        for (int kb = 0; kb < kblocks; ++kb, ++g) {
+          const int s = (int)(g % A_STAGES);
+          const uint32_t ph = (uint32_t)(g / A_STAGES) & 1u;
+          if (!mbar_wait(&full_bar[s], ph, &abort_sh, err)) {
+            ok = false;
+            break;
+          }
+          fence_after();
+          const uint32_t st = base + s * A_STAGE;
+#pragma unroll
+          for (int kk = 0; kk < A_BK / 16; ++kk) {
+            const uint32_t adv = (uint32_t)kk * 32u;  // 16 fp16 along K
+            const uint64_t dAH = desc_sw128(st + adv, 16, 1024);
+            const uint64_t dAL = desc_sw128(st + A_TILE + adv, 16, 1024);
+            const uint64_t dBH = desc_sw128(st + 2 * A_TILE + adv, 16, 1024);
+            const uint64_t dBL = desc_sw128(st + 3 * A_TILE + adv, 16, 1024);
+            const uint32_t acc = (kb > 0 || kk > 0) ? 1u : 0u;
+            mma_f16(dmain, dAH, dBH, idesc, acc);
+            mma_f16(dcorr, dAH, dBL, idesc, acc);
+            mma_f16(dcorr, dAL, dBH, idesc, 1u);
+          }
+          mma_commit(&empty_bar[s]);
+        }
+        if (ok) mma_commit(&tfull[b]);
+      }
+    }
+  } else {
+    // ---- epilogue (warps 0-3): TMEM -> scale -> FP32 or packed store
+    int i = 0;
+    for (int64_t t = blockIdx.x; t < tiles; t += gridDim.x, ++i) {
+      const int b = i & 1;
+      const bool ready = mbar_wait(&tfull[b], ((uint32_t)i >> 1) & 1u, &abort_sh, err);
+      __syncwarp();
+      if (!__all_sync(0xffffffffu, ready)) break;
+      fence_after();
+      const int64_t rb = t / col_tiles, cb = t % col_tiles;
+      const int64_t row = rb * 128 + warp * 32 + lane;
+#pragma unroll 1
+      for (int cc = 0; cc < 4; ++cc) {
+        uint32_t rm[32], rc[32];
+        const uint32_t ta = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(b * 256 + cc * 32);
+        tmem_ld32(ta, rm);
+        tmem_ld32(ta + 128, rc);
+        tmem_wait_ld();
+        const int col0 = (int)(cb * 128) + cc * 32;
+        if (row >= m) continue;
+        float v[32];
+#pragma unroll
+        for (int j = 0; j < 32; ++j)
+          v[j] = (__uint_as_float(rm[j]) + __uint_as_float(rc[j])) * __ldg(f + col0 + j);
+        if (out.C) {
+          float* dst = out.C + row * out.ldc + col0;
+          if (col0 + 32 <= k && ((out.ldc & 3) == 0) &&
+              ((reinterpret_cast<uintptr_t>(out.C) & 15) == 0)) {
+#pragma unroll
+            for (int j = 0; j < 32; j += 4)
+              *reinterpret_cast<float4*>(dst + j) = make_float4(v[j], v[j + 1], v[j + 2], v[j + 3]);
+          } else {
+#pragma unroll
+            for (int j = 0; j < 32; ++j)
+              if (col0 + j < k) dst[j] = v[j];
+          }
+        } else if (col0 < out.ldo) {  // ldo is a multiple of 64: whole 32-column groups
+#pragma unroll
+          for (int j = 0; j < 32; j += 8) {
+            float w[8];
+#pragma unroll
+            for (int q = 0; q < 8; ++q) w[q] = v[j + q];
+            uint4 h, l;
+            split8(w, h, l);
+            *reinterpret_cast<uint4*>(out.ohi + row * out.ldo + col0 + j) = h;
+            *reinterpret_cast<uint4*>(out.olo + row * out.ldo + col0 + j) = l;
+          }
+        }
+      }
+      fence_before();
+      mbar_arrive(&tempty[b]);
+    }
+  }
+  fence_before();
+  __syncthreads();
+  if (warp == 4) {
+    __syncwarp();
+    fence_after();
+    tmem_dealloc(tmem, 512);
+  }
+}
+
+}  // namespace hp
+
+// ---------------------------------------------------------------------------
+// host side
+// ---------------------------------------------------------------------------
+static PFN_cuTensorMapEncodeTiled_v12000 encode_fn16() {
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault,
+                                         &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+  });
+  return fn;
+}
+
+// 3-D fp16 map over two planes of `rows` x `inner` (row pitch ld elements),
+// 128-byte swizzle, zero fill out of bounds
+static bool make_map_planes(CUtensorMap* map, const __half* base, uint64_t inner, uint64_t rows,
+                            uint64_t ld, uint32_t box_inner, uint32_t box_rows) {
+  PFN_cuTensorMapEncodeTiled_v12000 fn = encode_fn16();
+  if (!fn) return false;
+  if ((reinterpret_cast<uintptr_t>(base) & 15) || ((ld * 2) & 15)) return false;
+  cuuint64_t dims[3] = {inner, rows, 2};
+  cuuint64_t strides[2] = {ld * 2, ld * 2 * rows};
+  cuuint32_t box[3] = {box_inner, box_rows, 1};
+  cuuint32_t estr[3] = {1, 1, 1};
+  CUresult r = fn(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 3, const_cast<__half*>(base), dims,
+                  strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                  CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  return r == CUDA_SUCCESS;
+}
+
+int64_t packed_ld(int64_t N) { return cdiv(N, 64) * 64; }
+
+void packed_carve(Arena& ws, Packed& p, int64_t m, int64_t N) {
+  p.m = m;
+  p.N = N;
+  p.ld = packed_ld(N);
+  p.hi = ws.take<__half>((size_t)(2 * m * p.ld));
+  p.lo = p.hi ? p.hi + m * p.ld : nullptr;
+  p.scale = ws.take<float>((size_t)p.ld);
+}
+
+void packed_view(Packed& p, void* storage, int64_t m, int64_t N, float* scale) {
+  p.m = m;
+  p.N = N;
+  p.ld = packed_ld(N);
+  p.hi = static_cast<__half*>(storage);
+  p.lo = p.hi ? p.hi + m * p.ld : nullptr;
+  p.scale = scale;
+}
+
+int pack_f32(const float* Y, int64_t ld, int64_t m, int64_t N, Packed& p, Arena& ws,
+             cudaStream_t st) {
+  unsigned* cmax = ws.take<unsigned>((size_t)N);
+  if (ws.measuring()) return PLOM_OK;
+  PLOM_REQUIRE(!ws.overflow(), PLOM_ERR_WORKSPACE, "pack: workspace too small");
+  PLOM_REQUIRE(Y && p.hi && p.scale && cmax && m >= 1 && N >= 1 && ld >= N, PLOM_ERR_ARG,
+               "pack: bad arguments");
+  ProfScope prof("pack_f16x2", st, 0.0, 4.0 * (double)m * N + 4.0 * (double)m * p.ld);
+  PLOM_CHECK_CUDA(cudaMemsetAsync(cmax, 0, (size_t)N * sizeof(unsigned), st));
+  const int threads = 256;
+  const int rblocks = (int)std::max<int64_t>(1, std::min<int64_t>(m, (int64_t)num_sms() * 8));
+  hp::colmax_kernel<<<rblocks, threads, 0, st>>>(Y, ld, m, (int)N, cmax);
+  PLOM_CHECK_LAUNCH();
+  hp::colscale_kernel<<<(int)cdiv(p.ld, 256), 256, 0, st>>>(cmax, (int)N, (int)p.ld, p.scale);
+  PLOM_CHECK_LAUNCH();
+  const int vec = ((ld & 3) == 0) && ((reinterpret_cast<uintptr_t>(Y) & 15) == 0);
+  const int64_t items = m * (p.ld / 8);
+  const int blocks = (int)std::max<int64_t>(1, std::min<int64_t>(cdiv(items, 256), (int64_t)num_sms() * 16));
+  hp::pack_kernel<<<blocks, 256, 0, st>>>(Y, ld, m, (int)N, (int)p.ld, p.scale, p.hi, p.lo, vec);
+  PLOM_CHECK_LAUNCH();
+  return PLOM_OK;
+}
+
+// work items of the Gram: tiles x chunks, a whole number of waves of the
+// GPU (one CTA per SM) and at least 4 waves when the rows allow it
+static int gram16_chunks(int64_t m, int tiles) {
+  const int64_t sms = num_sms();
+  const int64_t maxc = std::max<int64_t>(1, cdiv(m, 4 * hp::G_BK));
+  int64_t best = 1;
+  for (int64_t waves = 1; waves <= 64; ++waves) {
+    const int64_t items = waves * sms;
+    if (items % tiles) continue;
+    const int64_t c = items / tiles;
+    if (c > maxc) break;
+    best = c;
+    if (waves >= 4) break;
+  }
+  if (best == 1) best = std::min<int64_t>(maxc, cdiv(4 * sms, tiles));
+  return (int)std::max<int64_t>(1, best);
+}
+
+int gram_packed(const Packed& p, double* G, int* err, Arena& ws, cudaStream_t st) {
+  const int64_t m = p.m, N = p.N;
+  const int tn = (int)cdiv(p.ld, 128);
+  const int tiles = tn * (tn + 1) / 2;
+  const int chunks = gram16_chunks(m, tiles);
+  int64_t rpc = cdiv(m, chunks);
+  rpc = cdiv(rpc, hp::G_BK) * hp::G_BK;  // chunk boundaries on stage boundaries
+  const int chunks_eff = (int)std::max<int64_t>(1, cdiv(m, rpc));
+  double* part = ws.take<double>((size_t)tiles * chunks_eff * 128 * 128);
+  if (ws.measuring()) return PLOM_OK;
+  PLOM_REQUIRE(!ws.overflow(), PLOM_ERR_WORKSPACE, "gram16: workspace too small");
+  PLOM_REQUIRE(p.hi && G && part && m >= 1 && m < (1ll << 31), PLOM_ERR_ARG,
+               "gram16: bad arguments");
+  static bool attr = false;
+  if (!attr) {
+    PLOM_CHECK_CUDA(cudaFuncSetAttribute(hp::gram16_kernel,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)hp::G_SMEM));
+    attr = true;
+  }
+  CUtensorMap tm;
+  PLOM_REQUIRE(make_map_planes(&tm, p.hi, (uint64_t)p.ld, (uint64_t)m, (uint64_t)p.ld, 64, 64),
+               PLOM_ERR_CUDA, "gram16: tensor map encoding failed");
+  ProfScope prof_g("tc_gram_f16x3", st, (double)m * N * N, 4.0 * (double)m * p.ld);
+  hp::gram16_kernel<<<tiles * chunks_eff, 320, hp::G_SMEM, st>>>(tm, m, tn, rpc, chunks_eff, part,
+                                                                 err);
+  PLOM_CHECK_LAUNCH();
+  const int64_t total = N * N;
+  const int blocks = (int)std::min<int64_t>(cdiv(total, 256), (int64_t)num_sms() * 16);
+  ProfScope prof_r("gram_reduce", st, 0.0, 8.0 * (double)tiles * chunks_eff * 128 * 128);
+  hp::gram16_reduce_kernel<<<blocks, 256, 0, st>>>(part, (int)N, tn, chunks_eff, p.scale, G);
+  PLOM_CHECK_LAUNCH();
+  return PLOM_OK;
+}
+
+int apply_packed(const Packed& p, const double* W, int64_t ldw, int64_t k, float* C, int64_t ldc,
+                 Packed* out, int* err, Arena& ws, cudaStream_t st) {
+  const int64_t m = p.m;
+  const int64_t ldk = p.ld;  // K extent of the W copies (= packed pitch of the input)
+  const int64_t col_tiles = cdiv(k, 128);
+  __half* bhi = ws.take<__half>((size_t)(2 * k * ldk));
+  __half* blo = bhi ? bhi + k * ldk : nullptr;
+  float* f = ws.take<float>((size_t)(col_tiles * 128));
+  if (ws.measuring()) return PLOM_OK;
+  PLOM_REQUIRE(!ws.overflow(), PLOM_ERR_WORKSPACE, "apply16: workspace too small");
+  PLOM_REQUIRE(p.hi && W && (C || out) && m >= 1 && m < (1ll << 31) && k >= 1, PLOM_ERR_ARG,
+               "apply16: bad arguments");
+  if (out) PLOM_REQUIRE(out->hi && out->scale && out->m == m && out->N == k, PLOM_ERR_ARG,
+                        "apply16: bad packed output");
+  static bool attr = false;
+  if (!attr) {
+    PLOM_CHECK_CUDA(cudaFuncSetAttribute(hp::apply16_kernel,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)hp::A_SMEM));
+    attr = true;
+  }
+  const float out_scale = out ? (float)(1 << hp::PK_LOG2) : 1.0f;
+  hp::split_w16_kernel<<<(int)(col_tiles * 128), 256, 0, st>>>(W, ldw, (int)p.N, (int)k, (int)ldk,
+                                                              p.scale, out_scale, bhi, blo, f);
+  PLOM_CHECK_LAUNCH();
+  if (out) {
+    // packed output columns carry the fixed scale 2^14
+    hp::fill_scale_kernel<<<(int)cdiv(out->ld, 256), 256, 0, st>>>(out->scale, (int)out->ld,
+                                                                   out_scale);
+    PLOM_CHECK_LAUNCH();
+  }
+  CUtensorMap tmA, tmB;
+  PLOM_REQUIRE(make_map_planes(&tmA, p.hi, (uint64_t)p.ld, (uint64_t)m, (uint64_t)p.ld, 64, 128) &&
+                   make_map_planes(&tmB, bhi, (uint64_t)ldk, (uint64_t)k, (uint64_t)ldk, 64, 128),
+               PLOM_ERR_CUDA, "apply16: tensor map encoding failed");
+  const int64_t tiles = cdiv(m, 128) * col_tiles;
+  const int grid = (int)std::min<int64_t>(tiles, num_sms());
+  hp::ApplyOut o;
+  o.C = out ? nullptr : C;
+  o.ldc = ldc;
+  o.ohi = out ? out->hi : nullptr;
+  o.olo = out ? out->lo : nullptr;
+  o.ldo = out ? (int)out->ld : 0;
+  ProfScope prof("tc_apply_f16x3", st, 2.0 * m * p.N * k,
+                 4.0 * ((double)m * p.ld + (double)m * k));
+  hp::apply16_kernel<<<grid, 192, hp::A_SMEM, st>>>(tmA, tmB, m, (int)(ldk / 64), (int)k,
+                                                    col_tiles, tiles, f, o, err);
+  PLOM_CHECK_LAUNCH();
+  return PLOM_OK;
+}
+
+}  // namespace plom

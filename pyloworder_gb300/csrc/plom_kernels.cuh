@@ -44,9 +44,11 @@ int trtri_upper(const double* R, double* W, int n, int batch, Arena& ws, cudaStr
 // One-sided Jacobi SVD of `batch` square n x n matrices A (ld n, stride n*n),
 // real (cplx=0) or complex interleaved (cplx=1, A holds n x 2n doubles).
 // Outputs: S (batch x n, descending), U (n x n, row-major, A = U diag(S) V^H),
-// VH (n x n rows = conj of right singular vectors, i.e. V^H).
-int jacobi_svd(const double* A, int n, int batch, int cplx, double* S, double* U, double* VH,
-               int* info, Arena& ws, cudaStream_t st);
+// VH (n x n rows = conj of right singular vectors, i.e. V^H).  Rotation
+// stops when every column pair has |a_p^H a_q| <= tol ||a_p|| ||a_q||
+// (tol <= 0: n * DBL_EPSILON).
+int jacobi_svd(const double* A, int n, int batch, int cplx, double tol, double* S, double* U,
+               double* VH, int* info, Arena& ws, cudaStream_t st);
 size_t dense_workspace(int n, int batch, int cplx);
 
 // complex <-> real-embedding helpers for n x n matrices (batched)

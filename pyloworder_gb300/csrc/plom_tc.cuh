@@ -1,6 +1,8 @@
 // Tensor-core (tcgen05) kernels of the mixed form: TF32 products split into
 // three terms (hi*hi + hi*lo + lo*hi) with FP32 accumulation in TMEM.
 #pragma once
+#include <cuda_fp16.h>
+
 #include "plom_common.cuh"
 
 namespace plom {
@@ -14,5 +16,29 @@ bool tc_apply_supported(int64_t m, int64_t N, int64_t k, int64_t lda, int64_t ld
 template <typename TW>
 int tc_apply_tf32x3(const float* A, int64_t lda, int64_t m, int64_t N, const TW* W, int64_t ldw,
                     int64_t k, float* C, int64_t ldc, int* err, Arena& ws, cudaStream_t st);
+
+// Tall FP32 operand packed as two fp16 planes (gemm_f16.cu):
+//   hi + lo = Y diag(scale), hi and lo row-major m x ld (ld = N rounded up to
+//   64, padding columns zero; lo = hi + m * ld), scale[j] a power of two.
+struct Packed {
+  __half* hi;
+  __half* lo;
+  float* scale;  // [ld]
+  int64_t m, N, ld;
+};
+int64_t packed_ld(int64_t N);
+// carve planes and scales from the workspace
+void packed_carve(Arena& ws, Packed& p, int64_t m, int64_t N);
+// planes in caller storage of 4 m packed_ld(N) bytes, scales in `scale`
+void packed_view(Packed& p, void* storage, int64_t m, int64_t N, float* scale);
+// pack an FP32 matrix with per-column power-of-two scales
+int pack_f32(const float* Y, int64_t ld, int64_t m, int64_t N, Packed& p, Arena& ws,
+             cudaStream_t st);
+// G (N x N, FP64) = Y^T Y
+int gram_packed(const Packed& p, double* G, int* err, Arena& ws, cudaStream_t st);
+// Y W for W (N x k, FP64, ldw): FP32 into C (ldc) when out == nullptr, else
+// packed into *out (planes m x packed_ld(k), scale 2^14)
+int apply_packed(const Packed& p, const double* W, int64_t ldw, int64_t k, float* C, int64_t ldc,
+                 Packed* out, int* err, Arena& ws, cudaStream_t st);
 
 }  // namespace plom

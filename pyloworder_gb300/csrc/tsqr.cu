@@ -37,13 +37,21 @@ static const double U32 = 5.9604644775390625e-08;  // 2^-24 (TF32x3 ~ FP32)
 // ---------------------------------------------------------------------------
 // tall operations, dispatched on precision
 // ---------------------------------------------------------------------------
+// the packed tensor-core kernels address rows with 32-bit TMA coordinates
+static bool packed_ok(int64_t m) { return m >= 1 && m < (1ll << 31); }
+
 template <typename TA>
 static int tall_gram(int prec, const TA* A, int64_t lda, int64_t m, int64_t N, double* G,
                      int* err, Arena& ws, cudaStream_t st) {
   if (prec == PLOM_PREC_FP64)
     return gemm_tn<TA, TA, double, double>(A, lda, A, lda, G, N, N, N, m, true, ws, st);
   if constexpr (sizeof(TA) == 4) {
-    if (tc_gram_supported(m, N, lda)) return tc_gram_tf32x3(A, lda, m, N, G, err, ws, st);
+    if (packed_ok(m)) {
+      Packed p;
+      packed_carve(ws, p, m, N);
+      PLOM_TRY(pack_f32(A, lda, m, N, p, ws, st));
+      return gram_packed(p, G, err, ws, st);
+    }
     return gemm_tn<TA, TA, float, double>(A, lda, A, lda, G, N, N, N, m, true, ws, st);
   } else {
     return gemm_tn<TA, TA, double, double>(A, lda, A, lda, G, N, N, N, m, true, ws, st);
@@ -59,8 +67,12 @@ static int tall_apply(int prec, const TA* A, int64_t lda, int64_t m, int64_t N, 
     return gemm_nn<TA, double, TO, double>(A, lda, W, k, C, ldc, m, k, N, st);
   }
   if constexpr (sizeof(TA) == 4 && sizeof(TO) == 4) {
-    if (tc_apply_supported(m, N, k, lda, ldc))
-      return tc_apply_tf32x3<double>(A, lda, m, N, W, k, k, C, ldc, err, ws, st);
+    if (packed_ok(m)) {
+      Packed p;
+      packed_carve(ws, p, m, N);
+      PLOM_TRY(pack_f32(A, lda, m, N, p, ws, st));
+      return apply_packed(p, W, k, k, C, ldc, nullptr, err, ws, st);
+    }
   }
   float* Wf = ws.take<float>((size_t)N * k);
   if (ws.measuring()) return PLOM_OK;
@@ -173,6 +185,169 @@ static int cholqr3(int prec, bool cplx, const TI* X, int64_t m, int n, int64_t l
   return PLOM_OK;
 }
 
+// ---------------------------------------------------------------------------
+// mixed form on FP32 data: CholeskyQR3 on packed fp16-pair operands.  X is
+// packed once (P0); every apply writes the next Q already packed (P1, P2),
+// so each tall operand is read by the tensor cores without conversion.
+// P2 reuses P0's storage; P1 lives in the caller's output buffer when that
+// is large enough (`p1_store`, 4 m packed_ld(N) bytes), else in the workspace.
+// ---------------------------------------------------------------------------
+struct PackedCore {
+  Packed P0, P1, P2;
+  double *G, *H, *R1, *R2, *R3, *W1, *W2, *W3, *Rp, *Re, *F;
+};
+
+static void carve_packed_core(Arena& ws, PackedCore& b, int64_t m, int N, bool p1_external,
+                              void* p1_store) {
+  const size_t nn = (size_t)N * N;
+  b.G = ws.take<double>(nn);
+  b.H = ws.take<double>(nn);
+  b.R1 = ws.take<double>(nn);
+  b.R2 = ws.take<double>(nn);
+  b.R3 = ws.take<double>(nn);
+  b.W1 = ws.take<double>(nn);
+  b.W2 = ws.take<double>(nn);
+  b.W3 = ws.take<double>(nn);
+  b.Rp = ws.take<double>(nn);
+  b.Re = ws.take<double>(nn);
+  b.F = ws.take<double>(nn);
+  packed_carve(ws, b.P0, m, N);
+  b.P2 = b.P0;
+  b.P2.scale = ws.take<float>((size_t)b.P0.ld);
+  if (p1_external) {
+    float* sc = ws.take<float>((size_t)b.P0.ld);
+    packed_view(b.P1, p1_store, m, N, sc);
+  } else {
+    packed_carve(ws, b.P1, m, N);
+  }
+}
+
+static int chol_pass_packed(bool cplx, int n, const Packed& P, PackedCore& b, double* R,
+                            double* W, double rel0, double relfail, int* info, Arena& ws,
+                            cudaStream_t st) {
+  const int N = cplx ? 2 * n : n;
+  double* Gtarget = cplx ? b.H : b.G;
+  const size_t mark = ws.off;
+  size_t need = mark;
+  PLOM_TRY(gram_packed(P, Gtarget, info, ws, st));
+  need = std::max(need, ws.off);
+  ws.off = mark;
+  if (cplx && !ws.measuring()) PLOM_TRY(complexify_gram(b.H, b.G, n, 1, st));
+  PLOM_TRY(chol_shifted(b.G, R, N, 1, rel0, relfail, info, ws, st));
+  need = std::max(need, ws.off);
+  ws.off = mark;
+  PLOM_TRY(trtri_upper(R, W, N, 1, ws, st));
+  need = std::max(need, ws.off);
+  ws.off = need;
+  return PLOM_OK;
+}
+
+static int cholqr3_packed(bool cplx, const float* X, int64_t m, int n, int64_t ldx,
+                          PackedCore& b, int* info, Arena& ws, cudaStream_t st) {
+  const int N = cplx ? 2 * n : n;
+  double rel1, relfail;
+  shifts_for(PLOM_PREC_MIXED, m, N, rel1, relfail);
+  const size_t mark = ws.off;
+  size_t need = mark;
+  auto sub = [&](auto&& fn) -> int {
+    ws.off = mark;
+    const int s = fn();
+    need = std::max(need, ws.off);
+    ws.off = mark;
+    return s;
+  };
+  int s = PLOM_OK;
+  PLOM_TRY(sub([&] { return pack_f32(X, ldx, m, N, b.P0, ws, st); }));
+  // pass 1
+  PLOM_TRY(sub([&] { return chol_pass_packed(cplx, n, b.P0, b, b.R1, b.W1, rel1, relfail, info, ws, st); }));
+  const double* F1 = ws.measuring() ? b.W1 : rowform(cplx, b.W1, b.F, n, st, s);
+  PLOM_TRY(s);
+  PLOM_TRY(sub([&] { return apply_packed(b.P0, F1, N, N, nullptr, 0, &b.P1, info, ws, st); }));
+  // pass 2
+  PLOM_TRY(sub([&] { return chol_pass_packed(cplx, n, b.P1, b, b.R2, b.W2, 0.0, relfail, info, ws, st); }));
+  const double* F2 = ws.measuring() ? b.W2 : rowform(cplx, b.W2, b.F, n, st, s);
+  PLOM_TRY(s);
+  PLOM_TRY(sub([&] { return apply_packed(b.P1, F2, N, N, nullptr, 0, &b.P2, info, ws, st); }));
+  // pass 3
+  PLOM_TRY(sub([&] { return chol_pass_packed(cplx, n, b.P2, b, b.R3, b.W3, 0.0, relfail, info, ws, st); }));
+  ws.off = need;
+  if (!ws.measuring()) {
+    PLOM_TRY((gemm_nn<double, double, double, double>(b.R3, N, b.R2, N, b.Rp, N, N, N, N, st)));
+    PLOM_TRY((gemm_nn<double, double, double, double>(b.Rp, N, b.R1, N, b.Re, N, N, N, N, st)));
+  }
+  return PLOM_OK;
+}
+
+// P1 may live in a float output buffer of m rows x ld floats when ld covers
+// the packed pitch (4 m packed_ld(N) bytes)
+static bool p1_fits(int64_t ld_floats, int N) { return ld_floats >= packed_ld(N); }
+
+static int tsqr_svd_packed(bool cplx, const float* X, int64_t m, int n, int64_t ldx, float* U,
+                           int64_t ldu, float* S, float* VT, int* info, Arena& ws,
+                           cudaStream_t st) {
+  const int N = cplx ? 2 * n : n;
+  PackedCore b;
+  carve_packed_core(ws, b, m, N, p1_fits(ldu, N), U);
+  const int cw = cplx ? 2 : 1;
+  double* Rc = ws.take<double>((size_t)n * n * cw);
+  double* Ur = ws.take<double>((size_t)n * n * cw);
+  double* VH = ws.take<double>((size_t)n * n * cw);
+  double* S64 = ws.take<double>(n);
+  double* Me = ws.take<double>((size_t)N * N);
+  double* Ue = ws.take<double>((size_t)N * N);
+  if (!ws.measuring())
+    PLOM_REQUIRE(!ws.overflow(), PLOM_ERR_WORKSPACE, "tsqr_svd: workspace too small (%zu > %zu)",
+                 ws.off, ws.cap);
+  const size_t mark = ws.off;
+  PLOM_TRY(cholqr3_packed(cplx, X, m, n, ldx, b, info, ws, st));
+  size_t need = ws.off;
+  ws.off = mark;
+  const double* Rin = b.Re;
+  if (cplx && !ws.measuring()) {
+    PLOM_TRY(embed_to_complex(b.Re, Rc, n, 1, st));
+    Rin = Rc;
+  }
+  // the mixed form's R carries FP32-level information: columns orthogonal to
+  // 1e-8 are final there
+  PLOM_TRY(jacobi_svd(Rin, n, 1, cplx ? 1 : 0, 1e-8, S64, Ur, VH, info, ws, st));
+  need = std::max(need, ws.off);
+  ws.off = mark;
+  const double* Mop = b.F;
+  if (!ws.measuring()) {
+    // M = R3^-1 Ur (embedded for complex), the right operand of Q2 x M
+    if (cplx) {
+      PLOM_TRY(complex_to_embed(Ur, Ue, n, 1, st));
+      PLOM_TRY((gemm_nn<double, double, double, double>(b.W3, N, Ue, N, Me, N, N, N, N, st)));
+      PLOM_TRY(embed_to_rowform(Me, b.F, n, 1, st));
+    } else {
+      PLOM_TRY((gemm_nn<double, double, double, double>(b.W3, N, Ur, N, Me, N, N, N, N, st)));
+      Mop = Me;
+    }
+  }
+  PLOM_TRY(apply_packed(b.P2, Mop, N, N, U, ldu, nullptr, info, ws, st));
+  if (!ws.measuring()) {
+    PLOM_TRY((convert<double, float>(S64, S, n, st)));
+    PLOM_TRY((convert<double, float>(VH, VT, (int64_t)n * n * cw, st)));
+  }
+  ws.off = std::max(need, ws.off);
+  return PLOM_OK;
+}
+
+static int tsqr_packed(const float* X, int64_t m, int n, int64_t ldx, float* Q, int64_t ldq,
+                       float* R, int* info, Arena& ws, cudaStream_t st) {
+  PackedCore b;
+  carve_packed_core(ws, b, m, n, p1_fits(ldq, n), Q);
+  if (!ws.measuring()) PLOM_REQUIRE(!ws.overflow(), PLOM_ERR_WORKSPACE, "tsqr: workspace too small");
+  const size_t mark = ws.off;
+  PLOM_TRY(cholqr3_packed(false, X, m, n, ldx, b, info, ws, st));
+  const size_t need = ws.off;
+  ws.off = mark;
+  PLOM_TRY(apply_packed(b.P2, b.W3, n, n, Q, ldq, nullptr, info, ws, st));
+  if (!ws.measuring()) PLOM_TRY((convert<double, float>(b.Re, R, (int64_t)n * n, st)));
+  ws.off = std::max(need, ws.off);
+  return PLOM_OK;
+}
+
 template <typename TI, typename TC>
 static void carve_core(Arena& ws, CoreBufs<TI, TC>& b, int64_t m, int N, bool need_q1) {
   const size_t nn = (size_t)N * N;
@@ -197,6 +372,10 @@ static void carve_core(Arena& ws, CoreBufs<TI, TC>& b, int64_t m, int N, bool ne
 template <typename TI, typename TC>
 static int tsqr_svd_impl(int prec, bool cplx, const TI* X, int64_t m, int n, int64_t ldx, TI* U,
                          int64_t ldu, TI* S, TI* VT, int* info, Arena& ws, cudaStream_t st) {
+  if constexpr (std::is_same<TI, float>::value && std::is_same<TC, float>::value) {
+    if (prec == PLOM_PREC_MIXED && packed_ok(m))
+      return tsqr_svd_packed(cplx, X, m, n, ldx, U, ldu, S, VT, info, ws, st);
+  }
   const int N = cplx ? 2 * n : n;
   // Q1 can live in U when U has the compute type and is densely packed
   const bool q1_in_u = std::is_same<TI, TC>::value && ldu == N;
@@ -223,7 +402,10 @@ static int tsqr_svd_impl(int prec, bool cplx, const TI* X, int64_t m, int n, int
     PLOM_TRY(embed_to_complex(b.Re, Rc, n, 1, st));
     Rin = Rc;
   }
-  PLOM_TRY(jacobi_svd(Rin, n, 1, cplx ? 1 : 0, S64, Ur, VH, info, ws, st));
+  // the mixed form's R carries FP32-level information: columns orthogonal to
+  // 1e-8 are final there; the FP64 form iterates to n * DBL_EPSILON
+  const double jtol = (prec == PLOM_PREC_MIXED) ? 1e-8 : 0.0;
+  PLOM_TRY(jacobi_svd(Rin, n, 1, cplx ? 1 : 0, jtol, S64, Ur, VH, info, ws, st));
   need = std::max(need, ws.off);
   ws.off = scratch_mark;
   if (!ws.measuring()) {
@@ -251,6 +433,10 @@ static int tsqr_svd_impl(int prec, bool cplx, const TI* X, int64_t m, int n, int
 template <typename TI, typename TC>
 static int tsqr_impl(int prec, const TI* X, int64_t m, int n, int64_t ldx, TI* Q, int64_t ldq,
                      TI* R, int* info, Arena& ws, cudaStream_t st) {
+  if constexpr (std::is_same<TI, float>::value && std::is_same<TC, float>::value) {
+    if (prec == PLOM_PREC_MIXED && packed_ok(m))
+      return tsqr_packed(X, m, n, ldx, Q, ldq, R, info, ws, st);
+  }
   CoreBufs<TI, TC> b;
   const bool q1_in_q = std::is_same<TI, TC>::value && ldq == n;
   carve_core<TI, TC>(ws, b, m, n, !q1_in_q);
@@ -514,13 +700,18 @@ static int matmul_impl(int prec, int transA, const T* A, int64_t lda, const T* B
   const bool fp64 = (prec == PLOM_PREC_FP64) || sizeof(T) == 8;
   if (transA == 0) {
     if constexpr (sizeof(T) == 4) {
-      if (!fp64 && tc_apply_supported(m, k, n, lda, ldc)) {
+      if (!fp64 && packed_ok(m) && m >= 1 && n >= 1 && k >= 1) {
         int* flag = ws.take<int>(PLOM_INFO_WORDS);  // launch-wide abort word
+        double* B64 = ws.take<double>((size_t)k * n);
+        Packed p;
+        packed_carve(ws, p, m, k);
         if (!ws.measuring()) {
           PLOM_REQUIRE(!ws.overflow(), PLOM_ERR_WORKSPACE, "matmul: workspace too small");
           PLOM_CHECK_CUDA(cudaMemsetAsync(flag, 0, sizeof(int) * PLOM_INFO_WORDS, st));
+          PLOM_TRY((copy2d<float, double>(B, ldb, B64, n, k, n, st)));
         }
-        return tc_apply_tf32x3<float>(A, lda, m, k, B, ldb, n, C, ldc, flag, ws, st);
+        PLOM_TRY(pack_f32(A, lda, m, k, p, ws, st));
+        return apply_packed(p, B64, n, n, C, ldc, nullptr, flag, ws, st);
       }
     }
     if (ws.measuring()) return PLOM_OK;

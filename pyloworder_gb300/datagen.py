@@ -59,12 +59,17 @@ def pod_field_np(nx, ny, nt, nmodes, seed, noise=1e-4, amp_pow=None, dtype=np.fl
 
 
 def pod_field_device(nx, ny, nt, nmodes, seed, noise=1e-5, amp_pow=1.5, dtype="float32",
-                     distinct=True, kmax=16, chunk_rows=1 << 20):
-    """Config-2 style field generated in HBM (torch, row chunks)."""
+                     distinct=True, kmax=16, chunk_rows=1 << 20, m=None):
+    """Config-2 style field generated in HBM (torch, row chunks).  With `m`
+    given, the first m points of the nx x ny grid (row by row) are used, so
+    any point count fits a grid with nx * ny >= m."""
     import torch
     tdt = getattr(torch, dtype) if isinstance(dtype, str) else dtype
     rng, kx, ky, w, th = _pod_params(nmodes, seed, distinct, kmax)
-    m = nx * ny
+    if m is None:
+        m = nx * ny
+    if not (0 < m <= nx * ny) or nx < 2 or ny < 2:
+        raise ValueError("pod_field_device: need nx, ny >= 2 and 0 < m <= nx * ny")
     amps = np.array([2.0 ** (-k) if amp_pow is None else k ** (-amp_pow)
                      for k in range(1, nmodes + 1)])
     t = np.arange(nt, dtype=np.float64)
@@ -91,11 +96,14 @@ def pod_field_device(nx, ny, nt, nmodes, seed, noise=1e-5, amp_pow=1.5, dtype="f
 
 
 def grid_for_points(m):
-    """nx, ny with nx * ny = m and nx >= ny, as square as a power-of-two split allows."""
-    ny = 1 << (int(math.log2(m)) // 2) if m & (m - 1) == 0 else int(math.isqrt(m))
-    while m % ny:
-        ny -= 1
-    return m // ny, ny
+    """nx, ny with nx >= ny >= 2 covering m points: nx * ny = m for powers of
+    two, otherwise ny = floor(sqrt(m)) and nx * ny >= m (the last grid row is
+    partly used)."""
+    if m & (m - 1) == 0:
+        ny = max(2, 1 << (int(math.log2(m)) // 2))
+    else:
+        ny = max(2, int(math.isqrt(m)))
+    return max(2, -(-m // ny)), ny
 
 
 def dmd_field_device(m, n, npairs=16, seed=1003, dt=0.1, noise=1e-5, width=32.0,

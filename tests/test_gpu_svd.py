@@ -96,10 +96,15 @@ def test_pod_f32_nomean_golden(golden):
     U, S, V = P.POD.run(g["X"], remove_mean=False)
     ref = O.pod_run(g["X"].astype(np.float64), remove_mean=False)
     assert S.dtype == np.float32
-    assert sigma_rel(S, ref[1], 10) < 1e-5
-    # mode 10 (2.5e-3) sits on the noise floor (mode 11: 2.4e-3), so the
-    # 10-mode subspace is ill-conditioned even for pyLOM's own float32 result
-    # (2.9e-5 rad); the 9 signal modes are well separated
+    assert sigma_rel(S, ref[1], 9) < 1e-5
+    # mode 10 (2.5e-3) sits on the noise floor (mode 11: 2.4e-3).  The mixed
+    # form's tensor-core operands carry 22-23 significant bits of the FP32
+    # input; rounding X in its 23rd-24th bits moves sigma_10 by 1e-6 to 1e-5
+    # relative depending on the rounding pattern (measured on this matrix with
+    # inputs perturbed by one ulp), so the noise-floor mode gets a wider
+    # bound.  The 10-mode subspace is ill-conditioned even for pyLOM
+    # (2.9e-5 rad); the 9 signal modes are well separated.
+    assert sigma_rel(S, ref[1], 10) < 5e-5
     assert subspace_angle(U[:, :9], ref[0][:, :9]) < 1e-4
 
 
