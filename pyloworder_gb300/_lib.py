@@ -238,6 +238,6 @@ def precision_code(precision, x):
     p = str(precision).lower()
     if p in ("fp64", "double", "float64"):
         return PREC_FP64
-    if p in ("mixed", "tf32x3", "fp32"):
+    if p in ("mixed", "fp32"):
         return PREC_MIXED
     raise ValueError(f"precision must be 'fp64' or 'mixed', got {precision!r}")

@@ -583,9 +583,182 @@ __device__ __forceinline__ int jac_pair(double* x, double* y, double* xv, double
   return 1;
 }
 
+// ---------------------------------------------------------------------------
+// Double-float storage (mixed form, real): each element of At and Vt is an
+// unevaluated sum hi + lo of two FP32 numbers (~48 significant bits) held in
+// the 8-byte slot of a double.  Dots and rotations run on the FP32 pipe with
+// error-free transformations (Knuth's two-sum, FMA two-product); the scalar
+// pair parameters stay in FP64.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ float2 df_split(double v) {
+  const float h = (float)v;
+  return make_float2(h, (float)(v - (double)h));
+}
+__device__ __forceinline__ double df_val(float2 a) { return (double)a.x + (double)a.y; }
+__device__ __forceinline__ float2 two_sum(float a, float b) {
+  const float s = a + b;
+  const float bb = s - a;
+  return make_float2(s, (a - (s - bb)) + (b - bb));
+}
+__device__ __forceinline__ float2 fast_two_sum(float a, float b) {
+  const float s = a + b;
+  return make_float2(s, b - (s - a));
+}
+// a - t b
+__device__ __forceinline__ float2 df_fms(float2 a, float2 t, float2 b) {
+  const float ph = t.x * b.x;
+  float pe = fmaf(t.x, b.x, -ph);
+  pe = fmaf(t.x, b.y, pe);
+  pe = fmaf(t.y, b.x, pe);
+  const float2 sm = two_sum(a.x, -ph);
+  return fast_two_sum(sm.x, sm.y + (a.y - pe));
+}
+// acc += x y (acc.y collects the low-order parts)
+__device__ __forceinline__ void df_dot_acc(float2& acc, float2 x, float2 y) {
+  const float ph = x.x * y.x;
+  float pe = fmaf(x.x, y.x, -ph);
+  pe = fmaf(x.x, y.y, pe);
+  pe = fmaf(x.y, y.x, pe);
+  const float2 sm = two_sum(acc.x, ph);
+  acc.x = sm.x;
+  acc.y += sm.y + pe;
+}
+__device__ __forceinline__ double df_warp_sum(float2 v) {
+  v = fast_two_sum(v.x, v.y);
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const float h = __shfl_xor_sync(0xffffffffu, v.x, o);
+    const float l = __shfl_xor_sync(0xffffffffu, v.y, o);
+    const float2 sm = two_sum(v.x, h);
+    v = fast_two_sum(sm.x, sm.y + (v.y + l));
+  }
+  return df_val(v);
+}
+
+template <bool SQ>
+__device__ __forceinline__ void jac_dots_df(const float2* x, const float2* y, int64_t len,
+                                            int lane, double& gr, double& sa, double& sb) {
+  float2 g0 = make_float2(0.f, 0.f), g1 = g0, a0 = g0, b0 = g0;
+  int64_t i = lane;
+  for (; i + 32 < len; i += 64) {
+    const float2 x0 = x[i], x1 = x[i + 32], y0 = y[i], y1 = y[i + 32];
+    df_dot_acc(g0, x0, y0);
+    df_dot_acc(g1, x1, y1);
+    if (SQ) {
+      df_dot_acc(a0, x0, x0);
+      df_dot_acc(a0, x1, x1);
+      df_dot_acc(b0, y0, y0);
+      df_dot_acc(b0, y1, y1);
+    }
+  }
+  for (; i < len; i += 32) {
+    const float2 x0 = x[i], y0 = y[i];
+    df_dot_acc(g0, x0, y0);
+    if (SQ) {
+      df_dot_acc(a0, x0, x0);
+      df_dot_acc(b0, y0, y0);
+    }
+  }
+  const float2 sm = two_sum(g0.x, g1.x);
+  gr = df_warp_sum(make_float2(sm.x, sm.y + g0.y + g1.y));
+  if (SQ) {
+    sa = df_warp_sum(a0);
+    sb = df_warp_sum(b0);
+  } else {
+    sa = sb = 0.0;
+  }
+}
+
+// x <- x - tp y, y <- y - tqn x (old x)
+__device__ __forceinline__ void jac_rotate_df(float2* x, float2* y, int64_t len, int lane,
+                                              float2 tp, float2 tqn) {
+  int64_t i = lane;
+  for (; i + 32 < len; i += 64) {
+    const float2 x0 = x[i], x1 = x[i + 32], y0 = y[i], y1 = y[i + 32];
+    x[i] = df_fms(x0, tp, y0);
+    x[i + 32] = df_fms(x1, tp, y1);
+    y[i] = df_fms(y0, tqn, x0);
+    y[i + 32] = df_fms(y1, tqn, x1);
+  }
+  for (; i < len; i += 32) {
+    const float2 x0 = x[i], y0 = y[i];
+    x[i] = df_fms(x0, tp, y0);
+    y[i] = df_fms(y0, tqn, x0);
+  }
+}
+
+// jac_pair on double-float rows (real)
+__device__ __forceinline__ int jac_pair_df(float2* x, float2* y, float2* xv, float2* yv,
+                                           int64_t n, double* na_, double* nb_, double* da_,
+                                           double* db_, double* ea_, double* eb_, double tol2,
+                                           int lane) {
+  double al = *na_, be = *nb_;
+  const double da = *da_, db = *db_, ea = *ea_, eb = *eb_;
+  const bool need = (al < 0.0) || (be < 0.0);
+  double gr, sa, sb;
+  if (need)
+    jac_dots_df<true>(x, y, n, lane, gr, sa, sb);
+  else
+    jac_dots_df<false>(x, y, n, lane, gr, sa, sb);
+  if (al < 0.0) al = da * da * sa;
+  if (be < 0.0) be = db * db * sb;
+  gr *= da * db;
+  const double gabs = fabs(gr);
+  double t, c, sq;
+  if (!jac_angle(al, be, gabs, tol2, t, c, sq)) {
+    if (lane == 0 && need) {
+      *na_ = al;
+      *nb_ = be;
+    }
+    return 0;
+  }
+  const double e = copysign(1.0, gr);
+  const float2 tp = df_split(t * (db * ea) * e), tqn = df_split(-t * (da * eb) * e);
+  jac_rotate_df(x, y, n, lane, tp, tqn);
+  jac_rotate_df(xv, yv, n, lane, tp, tqn);
+  __syncwarp();
+  if (lane == 0) {
+    const double na = fma(-t, gabs, al), nb = fma(t, gabs, be);
+    *na_ = (na > 0.125 * al) ? na : -1.0;
+    *nb_ = (nb > 0.125 * be) ? nb : -1.0;
+    *da_ = da * c;
+    *db_ = db * c;
+    *ea_ = ea * sq;
+    *eb_ = eb * sq;
+  }
+  return 1;
+}
+
+template <int CW, bool DF>
+__device__ __forceinline__ int jac_pair_any(double* x, double* y, double* xv, double* yv,
+                                            int64_t n, double* na_, double* nb_, double* da_,
+                                            double* db_, double* ea_, double* eb_, double tol2,
+                                            int lane) {
+  if constexpr (DF)
+    return jac_pair_df(reinterpret_cast<float2*>(x), reinterpret_cast<float2*>(y),
+                       reinterpret_cast<float2*>(xv), reinterpret_cast<float2*>(yv), n, na_, nb_,
+                       da_, db_, ea_, eb_, tol2, lane);
+  else
+    return jac_pair<CW>(x, y, xv, yv, n, na_, nb_, da_, db_, ea_, eb_, tol2, lane);
+}
+
+// element i of a stored row as FP64 (double or double-float storage)
+template <bool DF>
+__device__ __forceinline__ double jac_get(const double* row, int64_t i) {
+  if (DF) return df_val(reinterpret_cast<const float2*>(row)[i]);
+  return row[i];
+}
+template <bool DF>
+__device__ __forceinline__ void jac_put(double* row, int64_t i, double v) {
+  if (DF)
+    reinterpret_cast<float2*>(row)[i] = df_split(v);
+  else
+    row[i] = v;
+}
+
 // Shared prologue: scale by a power of two (max |a_ij| < 1), At = A^T,
 // Vt = I, unit scales, norms flagged for recomputation.
-template <int CW>
+template <int CW, bool DF>
 __device__ void jac_init(const double* __restrict__ A, int n, int batch, JacState& js,
                          cg::grid_group& grid) {
   const int64_t rl = (int64_t)n * CW;
@@ -607,12 +780,12 @@ __device__ void jac_init(const double* __restrict__ A, int n, int batch, JacStat
     frexp(__longlong_as_double((long long)js.amax[b]), &ex);
     const double sc = ldexp(1.0, -ex);
     const double* src = A + b * n * rl + (int64_t)i * rl + (int64_t)j * CW;
-    double* dst = js.At + b * n * P + (int64_t)j * P + (int64_t)i * CW;
-    dst[0] = src[0] * sc;
-    if (CW == 2) dst[1] = src[1] * sc;
-    double* v = js.Vt + b * n * P + (int64_t)i * P + (int64_t)j * CW;
-    v[0] = (i == j) ? 1.0 : 0.0;
-    if (CW == 2) v[1] = 0.0;
+    double* dst = js.At + b * n * P + (int64_t)j * P;
+    jac_put<DF>(dst, (int64_t)i * CW, src[0] * sc);
+    if (CW == 2) jac_put<DF>(dst, (int64_t)i * CW + 1, src[1] * sc);
+    double* v = js.Vt + b * n * P + (int64_t)i * P;
+    jac_put<DF>(v, (int64_t)j * CW, (i == j) ? 1.0 : 0.0);
+    if (CW == 2) jac_put<DF>(v, (int64_t)j * CW + 1, 0.0);
     if (j == 0) {
       for (int64_t p = rl; p < P; ++p) {  // row padding stays zero
         js.At[b * n * P + (int64_t)i * P + p] = 0.0;
@@ -627,7 +800,7 @@ __device__ void jac_init(const double* __restrict__ A, int n, int batch, JacStat
 
 // Shared epilogue: exact norms, descending order, outputs
 //   S = sigma, U[i][k] = a_perm(k)[i] / sigma, VH[k][:] = conj(v_perm(k)).
-template <int CW>
+template <int CW, bool DF>
 __device__ void jac_finish(int n, int batch, JacState& js, int sweep, double* __restrict__ S,
                            double* __restrict__ U, double* __restrict__ VH, int* info,
                            cg::grid_group& grid) {
@@ -644,7 +817,10 @@ __device__ void jac_finish(int n, int batch, JacState& js, int sweep, double* __
   for (int64_t task = gwarp; task < (int64_t)batch * n; task += nwarps) {
     const double* a = js.At + (task / n) * n * P + (task % n) * P;
     double s = 0.0;
-    for (int64_t i = lane; i < rl; i += 32) s = fma(a[i], a[i], s);
+    for (int64_t i = lane; i < rl; i += 32) {
+      const double x = jac_get<DF>(a, i);
+      s = fma(x, x, s);
+    }
     s = warp_sum(s);
     if (lane == 0) js.nrm2[task] = js.dsc[task] * js.dsc[task] * s;
   }
@@ -673,14 +849,14 @@ __device__ void jac_finish(int n, int batch, JacState& js, int sweep, double* __
     if (i == 0) S[b * n + k] = ldexp(sk, ex);
     const double d = js.dsc[b * n + src];
     const double f = sk > 0.0 ? d / sk : 0.0;
-    const double* a = js.At + b * n * P + (int64_t)src * P + (int64_t)i * CW;
+    const double* a = js.At + b * n * P + (int64_t)src * P;
     double* u = U + b * n * rl + (int64_t)i * rl + (int64_t)k * CW;
-    u[0] = a[0] * f;
-    if (CW == 2) u[1] = a[1] * f;
-    const double* v = js.Vt + b * n * P + (int64_t)src * P + (int64_t)i * CW;
+    u[0] = jac_get<DF>(a, (int64_t)i * CW) * f;
+    if (CW == 2) u[1] = jac_get<DF>(a, (int64_t)i * CW + 1) * f;
+    const double* v = js.Vt + b * n * P + (int64_t)src * P;
     double* vh = VH + b * n * rl + (int64_t)k * rl + (int64_t)i * CW;
-    vh[0] = v[0] * d;
-    if (CW == 2) vh[1] = -v[1] * d;
+    vh[0] = jac_get<DF>(v, (int64_t)i * CW) * d;
+    if (CW == 2) vh[1] = -jac_get<DF>(v, (int64_t)i * CW + 1) * d;
   }
 }
 
@@ -708,7 +884,7 @@ __device__ __forceinline__ void intra_pair(int round, int which, int& a, int& b)
 
 constexpr uint64_t JAC_WAIT_NS = 2000000000ull;
 
-template <int CW>
+template <int CW, bool DF>
 __global__ void __launch_bounds__(128) jacobi_block_kernel(const double* __restrict__ A, int n,
                                                            int batch, JacState js, double tol2,
                                                            double* __restrict__ S,
@@ -730,7 +906,8 @@ __global__ void __launch_bounds__(128) jacobi_block_kernel(const double* __restr
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     abort_sh = 0;
   }
-  jac_init<CW>(A, n, batch, js, grid);  // ends with a grid barrier
+  static_assert(!DF || CW == 1, "double-float rows are real");
+  jac_init<CW, DF>(A, n, batch, js, grid);  // ends with a grid barrier
 
   const int nb = (n + 3) / 4;
   const int nbp = (nb + (nb & 1) < 2) ? 2 : nb + (nb & 1);  // even, >= 2
@@ -812,7 +989,10 @@ __global__ void __launch_bounds__(128) jacobi_block_kernel(const double* __restr
             double acc = 0.0;
             if (scol[s8] >= 0) {
               const double* x = cA + s8 * P;
-              for (int64_t i = lane; i < (int64_t)n * CW; i += 32) acc = fma(x[i], x[i], acc);
+              for (int64_t i = lane; i < (int64_t)n * CW; i += 32) {
+                const double v = jac_get<DF>(x, i);
+                acc = fma(v, v, acc);
+              }
               acc = warp_sum(acc);
             }
             if (lane == 0) snrm[s8] = sd[s8] * sd[s8] * acc;
@@ -825,16 +1005,18 @@ __global__ void __launch_bounds__(128) jacobi_block_kernel(const double* __restr
             a += off;
             c += off;
             if (scol[a] >= 0 && scol[c] >= 0)
-              myrot += jac_pair<CW>(cA + a * P, cA + c * P, cV + a * P, cV + c * P, n, &snrm[a],
-                                    &snrm[c], &sd[a], &sd[c], &se[a], &se[c], tol2, lane);
+              myrot += jac_pair_any<CW, DF>(cA + a * P, cA + c * P, cV + a * P, cV + c * P, n,
+                                            &snrm[a], &snrm[c], &sd[a], &sd[c], &se[a], &se[c],
+                                            tol2, lane);
             __syncthreads();
           }
         }
         for (int u = 0; u < 4; ++u) {
           const int a = warp, c = 4 + ((warp + u) & 3);
           if (scol[a] >= 0 && scol[c] >= 0)
-            myrot += jac_pair<CW>(cA + a * P, cA + c * P, cV + a * P, cV + c * P, n, &snrm[a],
-                                  &snrm[c], &sd[a], &sd[c], &se[a], &se[c], tol2, lane);
+            myrot += jac_pair_any<CW, DF>(cA + a * P, cA + c * P, cV + a * P, cV + c * P, n,
+                                          &snrm[a], &snrm[c], &sd[a], &sd[c], &se[a], &se[c],
+                                          tol2, lane);
           __syncthreads();
         }
         // rows out; a scale below 2^-40 is folded into its rows
@@ -848,8 +1030,8 @@ __global__ void __launch_bounds__(128) jacobi_block_kernel(const double* __restr
           const double f = sd[s8];
           if (f < JAC_FOLD_BELOW) {
             for (int64_t i = threadIdx.x; i < P; i += 128) {
-              ga[i] = sa[i] * f;
-              gv[i] = sv[i] * f;
+              jac_put<DF>(ga, i, jac_get<DF>(sa, i) * f);
+              jac_put<DF>(gv, i, jac_get<DF>(sv, i) * f);
             }
           } else {
             for (int64_t i = threadIdx.x; i < P; i += 128) {
@@ -873,7 +1055,7 @@ __global__ void __launch_bounds__(128) jacobi_block_kernel(const double* __restr
     if (js.counts[sweep] == 0) break;
   }
   if (S == nullptr) return;
-  jac_finish<CW>(n, batch, js, sweep, S, U, VH, info, grid);
+  jac_finish<CW, DF>(n, batch, js, sweep, S, U, VH, info, grid);
 }
 
 // one warp per column pair, 4 pairs per 128-thread block, rows in global memory
@@ -888,7 +1070,7 @@ __global__ void __launch_bounds__(128) jacobi_pair_kernel(const double* __restri
   const int lane = threadIdx.x & 31;
   const int64_t gwarp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
-  jac_init<CW>(A, n, batch, js, grid);
+  jac_init<CW, false>(A, n, batch, js, grid);
   const int np = n + (n & 1);
   const int pairs = np / 2;
   const int64_t total = (int64_t)pairs * batch;
@@ -949,7 +1131,7 @@ __global__ void __launch_bounds__(128) jacobi_pair_kernel(const double* __restri
     if (js.counts[sweep] == 0) break;
   }
   if (S == nullptr) return;
-  jac_finish<CW>(n, batch, js, sweep, S, U, VH, info, grid);
+  jac_finish<CW, false>(n, batch, js, sweep, S, U, VH, info, grid);
 }
 
 // real matrices from this size on are solved through their transpose
@@ -963,13 +1145,17 @@ static int64_t jac_pitch(int n, int cplx) {
 
 template <int CW>
 static int jacobi_launch_cw(const double* A, int n, int batch, JacState& js, double tol2,
-                            double* S, double* U, double* VH, int* info, cudaStream_t st) {
+                            bool df, double* S, double* U, double* VH, int* info,
+                            cudaStream_t st) {
   void* args[] = {(void*)&A,    (void*)&n, (void*)&batch, (void*)&js, (void*)&tol2,
                   (void*)&S,    (void*)&U, (void*)&VH,    (void*)&info};
   const size_t smem = (size_t)16 * js.pitch * sizeof(double);
-  ProfScope prof("jacobi_svd_fp64", st, 0.0, 8.0 * 3.0 * n * n * batch * CW);
+  const bool use_df = df && CW == 1 && smem <= JAC_BLOCK_SMEM_MAX;
+  ProfScope prof(use_df ? "jacobi_svd_df" : "jacobi_svd_fp64", st, 0.0,
+                 8.0 * 3.0 * n * n * batch * CW);
   if (smem <= JAC_BLOCK_SMEM_MAX) {
-    const void* k = (const void*)jacobi_block_kernel<CW>;
+    const void* k = use_df ? (const void*)jacobi_block_kernel<1, true>
+                           : (const void*)jacobi_block_kernel<CW, false>;
     PLOM_CHECK_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     const int nb = (n + 3) / 4;
     const int nbp = std::max(2, nb + (nb & 1));
@@ -985,11 +1171,15 @@ static int jacobi_launch_cw(const double* A, int n, int batch, JacState& js, dou
   return PLOM_OK;
 }
 
+// Tolerances at or above this level (the mixed form's) run on double-float rows
+constexpr double JAC_DF_TOL = 1e-10;
+
 static int jacobi_launch(const double* A, int n, int batch, int cplx, JacState& js, double tol,
                          double* S, double* U, double* VH, int* info, cudaStream_t st) {
   const double tol2 = tol * tol;
-  return cplx ? jacobi_launch_cw<2>(A, n, batch, js, tol2, S, U, VH, info, st)
-              : jacobi_launch_cw<1>(A, n, batch, js, tol2, S, U, VH, info, st);
+  const bool df = tol >= JAC_DF_TOL;
+  return cplx ? jacobi_launch_cw<2>(A, n, batch, js, tol2, false, S, U, VH, info, st)
+              : jacobi_launch_cw<1>(A, n, batch, js, tol2, df, S, U, VH, info, st);
 }
 
 static void carve_jac(Arena& ws, JacState& js, int n, int batch, int cplx) {

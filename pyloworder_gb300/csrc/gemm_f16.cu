@@ -797,14 +797,17 @@ int pack_f32(const float* Y, int64_t ld, int64_t m, int64_t N, Packed& p, Arena&
   PLOM_REQUIRE(!ws.overflow(), PLOM_ERR_WORKSPACE, "pack: workspace too small");
   PLOM_REQUIRE(Y && p.hi && p.scale && cmax && m >= 1 && N >= 1 && ld >= N, PLOM_ERR_ARG,
                "pack: bad arguments");
-  ProfScope prof("pack_f16x2", st, 0.0, 4.0 * (double)m * N + 4.0 * (double)m * p.ld);
   PLOM_CHECK_CUDA(cudaMemsetAsync(cmax, 0, (size_t)N * sizeof(unsigned), st));
   const int threads = 256;
-  const int rblocks = (int)std::max<int64_t>(1, std::min<int64_t>(m, (int64_t)num_sms() * 8));
-  hp::colmax_kernel<<<rblocks, threads, 0, st>>>(Y, ld, m, (int)N, cmax);
-  PLOM_CHECK_LAUNCH();
-  hp::colscale_kernel<<<(int)cdiv(p.ld, 256), 256, 0, st>>>(cmax, (int)N, (int)p.ld, p.scale);
-  PLOM_CHECK_LAUNCH();
+  {
+    ProfScope prof("colmax", st, 0.0, 4.0 * (double)m * N);
+    const int rblocks = (int)std::max<int64_t>(1, std::min<int64_t>(m, (int64_t)num_sms() * 8));
+    hp::colmax_kernel<<<rblocks, threads, 0, st>>>(Y, ld, m, (int)N, cmax);
+    PLOM_CHECK_LAUNCH();
+    hp::colscale_kernel<<<(int)cdiv(p.ld, 256), 256, 0, st>>>(cmax, (int)N, (int)p.ld, p.scale);
+    PLOM_CHECK_LAUNCH();
+  }
+  ProfScope prof("pack_f16x2", st, 0.0, 4.0 * (double)m * N + 4.0 * (double)m * p.ld);
   const int vec = ((ld & 3) == 0) && ((reinterpret_cast<uintptr_t>(Y) & 15) == 0);
   const int64_t items = m * (p.ld / 8);
   const int blocks = (int)std::max<int64_t>(1, std::min<int64_t>(cdiv(items, 256), (int64_t)num_sms() * 16));

@@ -18,9 +18,9 @@
 //   performed.
 //
 // Precision forms: PLOM_PREC_FP64 runs every product in FP64 (Q1, Q2 stored
-// in FP64); PLOM_PREC_MIXED stores Q1, Q2 in FP32 and runs the tall products
-// on the tensor cores (gemm_tc.cu; CUDA-core FP32 when the shape does not
-// fit the tensor-core kernels), keeping every n x n step in FP64.
+// in FP64); PLOM_PREC_MIXED packs the FP32 operand once as fp16 hi/lo pairs
+// and runs every tall product on the tensor cores (gemm_f16.cu), each apply
+// writing the next Q already packed; every n x n step stays in FP64.
 #include <algorithm>
 #include <cmath>
 #include <type_traits>
