@@ -95,12 +95,16 @@ def serving_leg(njobs=48, seed=5, slots=4, budget=150e9):
 
 
 def peaks():
+    """(HBM GB/s, dense bf16 TFLOP/s, source).  The tensor-core kernels are
+    timed inside a seconds-long step, so the sustained bf16 figure applies."""
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
             d = json.load(f)
-        return d.get("hbm_gbs", 6800.0), d.get("bf16_tflops", 1900.0), "measured"
+        return (d.get("hbm_gbs", 6800.0),
+                d.get("bf16_tflops_sustained", d.get("bf16_tflops", 1700.0)),
+                "measured (sustained bf16)")
     except Exception:
-        return 6800.0, 1900.0, "fallback"
+        return 6800.0, 1700.0, "fallback"
 
 
 class ClockSampler:

@@ -687,6 +687,24 @@ __device__ __forceinline__ void jac_rotate_df(float2* x, float2* y, int64_t len,
   }
 }
 
+// x <- x - tp y, y <- y - tqn x over rows [h0, h1) of the warp
+__device__ __forceinline__ void jac_rotate_df_range(float2* x, float2* y, int64_t h0, int64_t h1,
+                                                    int lane, float2 tp, float2 tqn) {
+  int64_t i = h0 + lane;
+  for (; i + 32 < h1; i += 64) {
+    const float2 x0 = x[i], x1 = x[i + 32], y0 = y[i], y1 = y[i + 32];
+    x[i] = df_fms(x0, tp, y0);
+    x[i + 32] = df_fms(x1, tp, y1);
+    y[i] = df_fms(y0, tqn, x0);
+    y[i + 32] = df_fms(y1, tqn, x1);
+  }
+  for (; i < h1; i += 32) {
+    const float2 x0 = x[i], y0 = y[i];
+    x[i] = df_fms(x0, tp, y0);
+    y[i] = df_fms(y0, tqn, x0);
+  }
+}
+
 // jac_pair on double-float rows (real)
 __device__ __forceinline__ int jac_pair_df(float2* x, float2* y, float2* xv, float2* yv,
                                            int64_t n, double* na_, double* nb_, double* da_,
@@ -1058,6 +1076,345 @@ __global__ void __launch_bounds__(128) jacobi_block_kernel(const double* __restr
   jac_finish<CW, DF>(n, batch, js, sweep, S, U, VH, info, grid);
 }
 
+// ---------------------------------------------------------------------------
+// Double-float block kernel with 16 warps per CTA (mixed form, real): the 4
+// pairs of a round get 4 warps each (a quarter of the rows per warp), and the
+// pair parameters are computed once per pair, by one lane, in double-float
+// FP32 arithmetic (no FP64 instructions inside the sweep loop):
+//   t from zeta in FP32 (any t is exact for the rotation it defines),
+//   c = (1 + t^2)^-1/2 from an FP32 estimate and one Newton step in
+//   double-float, scales d, 1/d, carried norms and t dq/dp in double-float.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ float2 df_mul(float2 a, float2 b) {
+  const float p = a.x * b.x;
+  float e = fmaf(a.x, b.x, -p);
+  e = fmaf(a.x, b.y, e);
+  e = fmaf(a.y, b.x, e);
+  return fast_two_sum(p, e);
+}
+__device__ __forceinline__ float2 df_add2(float2 a, float2 b) {
+  const float2 s = two_sum(a.x, b.x);
+  return fast_two_sum(s.x, s.y + (a.y + b.y));
+}
+__device__ __forceinline__ float2 df_mulf(float2 a, float t) {
+  const float p = a.x * t;
+  const float e = fmaf(a.x, t, -p);
+  return fast_two_sum(p, fmaf(a.y, t, e));
+}
+// 1 / d in double-float
+__device__ __forceinline__ float2 df_recip(float2 d) {
+  const float h = 1.0f / d.x;
+  const float r = fmaf(-d.x, h, 1.0f) - d.y * h;
+  return fast_two_sum(h, r * h);
+}
+
+struct DfPair {
+  float2 tp, tqn;  // x -= tp y ; y -= tqn x
+  int rot;
+};
+
+// Pair parameters (one lane).  al/be: squared norms (x < 0: recompute from
+// sa/sb), g: a_p^T a_q of the stored rows, d/e: scales and their inverses.
+__device__ __forceinline__ DfPair df_params(float2& al, float2& be, float2 sa, float2 sb, float2 g,
+                                            float2& dp, float2& dq, float2& ep, float2& eq,
+                                            float tol) {
+  DfPair out;
+  out.rot = 0;
+  out.tp = out.tqn = make_float2(0.f, 0.f);
+  if (al.x < 0.f) al = df_mul(df_mul(dp, dp), sa);
+  if (be.x < 0.f) be = df_mul(df_mul(dq, dq), sb);
+  g = df_mul(df_mul(dp, dq), g);
+  const float sg = (g.x < 0.f) ? -1.f : 1.f;
+  const float2 ga = make_float2(fabsf(g.x), sg * g.y);
+  if (!(al.x > 0.f && be.x > 0.f) || !(ga.x > tol * sqrtf(al.x) * sqrtf(be.x))) return out;
+  // zeta = (be - al) / (2 |g|) with the difference in double-float
+  const float2 s = two_sum(be.x, -al.x);
+  const float diff = s.x + (s.y + (be.y - al.y));
+  const float z = diff / (2.0f * ga.x);
+  const float az = fabsf(z);
+  const float t = az > 1e18f ? 0.5f / z : copysignf(1.0f, z) / (az + sqrtf(fmaf(z, z, 1.0f)));
+  // x = 1 + t^2 (double-float), c = x^-1/2, sq = x^1/2
+  const float p = t * t;
+  float2 x = fast_two_sum(1.0f, p);
+  x.y += fmaf(t, t, -p);
+  const float y0 = rsqrtf(x.x);
+  const float q = y0 * y0, qe = fmaf(y0, y0, -q);
+  const float r = fmaf(-x.x, q, 1.0f) - fmaf(x.x, qe, x.y * q);
+  const float2 c = fast_two_sum(y0, 0.5f * y0 * r);
+  const float2 sq = df_mul(x, c);
+  out.tp = df_mulf(df_mul(dq, ep), t * sg);
+  out.tqn = df_mulf(df_mul(dp, eq), -t * sg);
+  // carried norms: al - t|g|, be + t|g|; a large relative drop is recomputed
+  const float2 tg = df_mulf(ga, t);
+  const float2 na = df_add2(al, make_float2(-tg.x, -tg.y));
+  const float2 nb = df_add2(be, tg);
+  al = (na.x > 0.125f * al.x) ? na : make_float2(-1.f, 0.f);
+  be = (nb.x > 0.125f * be.x) ? nb : make_float2(-1.f, 0.f);
+  dp = df_mul(dp, c);
+  dq = df_mul(dq, c);
+  ep = df_mul(ep, sq);
+  eq = df_mul(eq, sq);
+  out.rot = 1;
+  return out;
+}
+
+// dots of rows [h0, h1) of the warp; SQ adds |x|^2 and |y|^2
+template <bool SQ>
+__device__ __forceinline__ void df16_dots(const float2* x, const float2* y, int64_t h0, int64_t h1,
+                                          int lane, float2& g, float2& a2, float2& b2) {
+  float2 g0 = make_float2(0.f, 0.f), g1 = g0, aa = g0, bb = g0;
+  int64_t i = h0 + lane;
+  for (; i + 32 < h1; i += 64) {
+    const float2 x0 = x[i], x1 = x[i + 32], y0 = y[i], y1 = y[i + 32];
+    df_dot_acc(g0, x0, y0);
+    df_dot_acc(g1, x1, y1);
+    if (SQ) {
+      df_dot_acc(aa, x0, x0);
+      df_dot_acc(aa, x1, x1);
+      df_dot_acc(bb, y0, y0);
+      df_dot_acc(bb, y1, y1);
+    }
+  }
+  for (; i < h1; i += 32) {
+    const float2 x0 = x[i], y0 = y[i];
+    df_dot_acc(g0, x0, y0);
+    if (SQ) {
+      df_dot_acc(aa, x0, x0);
+      df_dot_acc(bb, y0, y0);
+    }
+  }
+  g = df_add2(g0, g1);
+  a2 = aa;
+  b2 = bb;
+}
+
+__device__ __forceinline__ float2 df_warp_sum2(float2 v) {
+  v = fast_two_sum(v.x, v.y);
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const float h = __shfl_xor_sync(0xffffffffu, v.x, o);
+    const float l = __shfl_xor_sync(0xffffffffu, v.y, o);
+    const float2 sm = two_sum(v.x, h);
+    v = fast_two_sum(sm.x, sm.y + (v.y + l));
+  }
+  return v;
+}
+
+__global__ void __launch_bounds__(512, 1)
+    jacobi_block_df16_kernel(const double* __restrict__ A, int n, int batch, JacState js,
+                             float tol, double* __restrict__ S, double* __restrict__ U,
+                             double* __restrict__ VH, int* info) {
+  extern __shared__ __align__(16) double jsm[];  // [8][pitch] At rows, [8][pitch] Vt rows
+  __shared__ float2 snrm[8], sd[8], se[8];
+  __shared__ float2 red[4][4][3];                 // [pair][quarter][g a2 b2]
+  __shared__ DfPair prm[4];
+  __shared__ int scol[8];
+  __shared__ __align__(8) uint64_t bar;
+  __shared__ int abort_sh;
+  cg::grid_group grid = cg::this_grid();
+  const int64_t P = js.pitch;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int pk = warp >> 2, qtr = warp & 3;       // pair slot, row quarter
+  const int64_t h0 = (int64_t)n * qtr / 4, h1 = (int64_t)n * (qtr + 1) / 4;
+  float2* cA = reinterpret_cast<float2*>(jsm);
+  float2* cV = reinterpret_cast<float2*>(jsm + 8 * P);
+  const uint32_t bar_s = (uint32_t)__cvta_generic_to_shared(&bar);
+  if (threadIdx.x == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar_s));
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    abort_sh = 0;
+  }
+  jac_init<1, true>(A, n, batch, js, grid);  // ends with a grid barrier
+
+  const int nb = (n + 3) / 4;
+  const int nbp = (nb + (nb & 1) < 2) ? 2 : nb + (nb & 1);  // even, >= 2
+  const int bpairs = nbp / 2;
+  const int64_t tasks = (int64_t)bpairs * batch;
+  uint32_t phase = 0;
+  int sweep = 0;
+  for (; sweep < JACOBI_MAX_SWEEPS; ++sweep) {
+    int myrot = 0;
+    for (int step = 0; step < nbp - 1; ++step) {
+      for (int64_t task = blockIdx.x; task < tasks; task += gridDim.x) {
+        const int64_t b = task / bpairs;
+        int bi, bj;
+        rr_pair(step, (int)(task % bpairs), nbp, bi, bj);
+        double* At = js.At + b * n * P;
+        double* Vt = js.Vt + b * n * P;
+        if (threadIdx.x < 8) {
+          const int col = 4 * (threadIdx.x < 4 ? bi : bj) + (threadIdx.x & 3);
+          const bool v = col < n;
+          scol[threadIdx.x] = v ? col : -1;
+          const double nr = v ? js.nrm2[b * n + col] : 0.0;
+          snrm[threadIdx.x] = nr < 0.0 ? make_float2(-1.f, 0.f) : df_split(nr);
+          const float2 d = df_split(v ? js.dsc[b * n + col] : 1.0);
+          sd[threadIdx.x] = d;
+          se[threadIdx.x] = df_recip(d);  // exact inverse once per block step
+        }
+        __syncthreads();
+        if (threadIdx.x == 0 && !abort_sh) {
+          asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+          uint32_t bytes = 0;
+          for (int s8 = 0; s8 < 8; ++s8)
+            if (scol[s8] >= 0) bytes += 2u * (uint32_t)(P * 8);
+          asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar_s),
+                       "r"(bytes)
+                       : "memory");
+          for (int s8 = 0; s8 < 8; ++s8) {
+            const int col = scol[s8];
+            if (col < 0) continue;
+            bulk_load((uint32_t)__cvta_generic_to_shared(cA + s8 * P), At + (int64_t)col * P,
+                      (uint32_t)(P * 8), bar_s);
+            bulk_load((uint32_t)__cvta_generic_to_shared(cV + s8 * P), Vt + (int64_t)col * P,
+                      (uint32_t)(P * 8), bar_s);
+          }
+        }
+        if (!abort_sh) {
+          uint32_t ok = 0;
+          uint64_t t0 = 0;
+          asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t0));
+          while (true) {
+            asm volatile(
+                "{\n\t.reg .pred p;\n\t"
+                "mbarrier.try_wait.parity.acquire.cta.shared::cta.b64 p, [%1], %2;\n\t"
+                "selp.u32 %0, 1, 0, p;\n\t}"
+                : "=r"(ok)
+                : "r"(bar_s), "r"(phase)
+                : "memory");
+            if (ok) break;
+            uint64_t t1;
+            asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t1));
+            if (t1 - t0 > JAC_WAIT_NS) {
+              abort_sh = 1;
+              break;
+            }
+          }
+          phase ^= 1u;
+        }
+        __syncthreads();
+        if (abort_sh) {
+          if (threadIdx.x == 0) atomicMax(&info[ST_FAIL], PLOM_NUM_TIMEOUT);
+          __syncthreads();
+          continue;
+        }
+        if (step == 0) {
+          // exact squared norms once per sweep: 2 warps per row
+          const int s8 = warp >> 1, half = warp & 1;
+          float2 acc = make_float2(0.f, 0.f);
+          if (scol[s8] >= 0) {
+            const float2* x = cA + s8 * P;
+            for (int64_t i = (int64_t)n * half / 2 + lane; i < (int64_t)n * (half + 1) / 2; i += 32)
+              df_dot_acc(acc, x[i], x[i]);
+          }
+          acc = df_warp_sum2(acc);
+          if (lane == 0) red[s8 >> 1][(s8 & 1) * 2 + half][0] = acc;
+          __syncthreads();
+          if (threadIdx.x < 8) {
+            const int r8 = threadIdx.x;
+            const float2 sum = df_add2(red[r8 >> 1][(r8 & 1) * 2][0], red[r8 >> 1][(r8 & 1) * 2 + 1][0]);
+            snrm[r8] = df_mul(df_mul(sd[r8], sd[r8]), sum);
+          }
+          __syncthreads();
+        }
+        const int nrounds = (step == 0) ? 7 : 4;
+        for (int rd = 0; rd < nrounds; ++rd) {
+          // pair of this warp's slot pk in round rd
+          int a, c;
+          if (step == 0 && rd < 3) {
+            intra_pair(rd, pk & 1, a, c);
+            const int off = (pk >> 1) * 4;
+            a += off;
+            c += off;
+          } else {
+            const int u = (step == 0) ? rd - 3 : rd;
+            a = pk;
+            c = 4 + ((pk + u) & 3);
+          }
+          const bool live = scol[a] >= 0 && scol[c] >= 0;
+          const bool need = live && (snrm[a].x < 0.f || snrm[c].x < 0.f);
+          if (live) {
+            float2 g, a2, b2;
+            if (need)
+              df16_dots<true>(cA + a * P, cA + c * P, h0, h1, lane, g, a2, b2);
+            else
+              df16_dots<false>(cA + a * P, cA + c * P, h0, h1, lane, g, a2, b2);
+            g = df_warp_sum2(g);
+            if (need) {
+              a2 = df_warp_sum2(a2);
+              b2 = df_warp_sum2(b2);
+            }
+            if (lane == 0) {
+              red[pk][qtr][0] = g;
+              red[pk][qtr][1] = a2;
+              red[pk][qtr][2] = b2;
+            }
+          }
+          __syncthreads();
+          if (qtr == pk && lane == 0) {
+            // one lane per pair, on four different warps (SM sub-partitions)
+            DfPair pr;
+            pr.rot = 0;
+            if (live) {
+              float2 g = red[pk][0][0], a2 = red[pk][0][1], b2 = red[pk][0][2];
+#pragma unroll
+              for (int w = 1; w < 4; ++w) {
+                g = df_add2(g, red[pk][w][0]);
+                a2 = df_add2(a2, red[pk][w][1]);
+                b2 = df_add2(b2, red[pk][w][2]);
+              }
+              pr = df_params(snrm[a], snrm[c], a2, b2, g, sd[a], sd[c], se[a], se[c], tol);
+            }
+            prm[pk] = pr;
+            myrot += pr.rot;
+          }
+          __syncthreads();
+          const DfPair pr = prm[pk];
+          if (pr.rot) {
+            jac_rotate_df_range(cA + a * P, cA + c * P, h0, h1, lane, pr.tp, pr.tqn);
+            jac_rotate_df_range(cV + a * P, cV + c * P, h0, h1, lane, pr.tp, pr.tqn);
+          }
+          __syncthreads();
+        }
+        // rows out; a scale below 2^-40 is folded into its rows
+        for (int s8 = 0; s8 < 8; ++s8) {
+          const int col = scol[s8];
+          if (col < 0) continue;
+          double* ga = At + (int64_t)col * P;
+          double* gv = Vt + (int64_t)col * P;
+          const double* sa = jsm + s8 * P;
+          const double* sv = jsm + (8 + s8) * P;
+          const double f = df_val(sd[s8]);
+          if (f < JAC_FOLD_BELOW) {
+            for (int64_t i = threadIdx.x; i < P; i += 512) {
+              jac_put<true>(ga, i, jac_get<true>(sa, i) * f);
+              jac_put<true>(gv, i, jac_get<true>(sv, i) * f);
+            }
+          } else {
+            for (int64_t i = threadIdx.x; i < P; i += 512) {
+              ga[i] = sa[i];
+              gv[i] = sv[i];
+            }
+          }
+        }
+        if (threadIdx.x < 8 && scol[threadIdx.x] >= 0) {
+          const int col = scol[threadIdx.x];
+          const double f = df_val(sd[threadIdx.x]);
+          const bool fold = f < JAC_FOLD_BELOW;
+          js.nrm2[b * n + col] = snrm[threadIdx.x].x < 0.f ? -1.0 : df_val(snrm[threadIdx.x]);
+          js.dsc[b * n + col] = fold ? 1.0 : f;
+        }
+        __syncthreads();
+      }
+      grid.sync();
+    }
+    if (lane == 0 && myrot) atomicAdd(&js.counts[sweep], myrot);
+    grid.sync();
+    if (js.counts[sweep] == 0) break;
+  }
+  if (S == nullptr) return;
+  jac_finish<1, true>(n, batch, js, sweep, S, U, VH, info, grid);
+}
+
 // one warp per column pair, 4 pairs per 128-thread block, rows in global memory
 template <int CW>
 __global__ void __launch_bounds__(128) jacobi_pair_kernel(const double* __restrict__ A, int n,
@@ -1153,9 +1510,21 @@ static int jacobi_launch_cw(const double* A, int n, int batch, JacState& js, dou
   const bool use_df = df && CW == 1 && smem <= JAC_BLOCK_SMEM_MAX;
   ProfScope prof(use_df ? "jacobi_svd_df" : "jacobi_svd_fp64", st, 0.0,
                  8.0 * 3.0 * n * n * batch * CW);
+  if (use_df) {
+    const void* k = (const void*)jacobi_block_df16_kernel;
+    PLOM_CHECK_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    const int nb = (n + 3) / 4;
+    const int nbp = std::max(2, nb + (nb & 1));
+    const int want = (int)std::max<int64_t>(1, (int64_t)nbp / 2 * batch);
+    const int blocks = coop_blocks(k, 512, smem, want);
+    float tolf = (float)sqrt(tol2);
+    void* args16[] = {(void*)&A,    (void*)&n, (void*)&batch, (void*)&js, (void*)&tolf,
+                      (void*)&S,    (void*)&U, (void*)&VH,    (void*)&info};
+    PLOM_CHECK_CUDA(cudaLaunchCooperativeKernel(k, dim3(blocks), dim3(512), args16, smem, st));
+    return PLOM_OK;
+  }
   if (smem <= JAC_BLOCK_SMEM_MAX) {
-    const void* k = use_df ? (const void*)jacobi_block_kernel<1, true>
-                           : (const void*)jacobi_block_kernel<CW, false>;
+    const void* k = (const void*)jacobi_block_kernel<CW, false>;
     PLOM_CHECK_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     const int nb = (n + 3) / 4;
     const int nbp = std::max(2, nb + (nb & 1));

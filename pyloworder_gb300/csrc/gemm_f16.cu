@@ -199,17 +199,40 @@ __device__ __forceinline__ uint16_t ld_shared_u16(uint32_t addr) {
 // ---------------------------------------------------------------------------
 // packing
 // ---------------------------------------------------------------------------
-// column maxima of |Y| (bits of non-negative floats order like unsigned ints)
-__global__ void colmax_kernel(const float* __restrict__ Y, int64_t ld, int64_t m, int N,
-                              unsigned* __restrict__ cmax) {
+// column maxima of |Y| (bits of non-negative floats order like unsigned ints);
+// each block takes a contiguous range of rows, threads take 4-column groups
+// (16-byte loads when rows are aligned)
+__global__ void __launch_bounds__(256) colmax_kernel(const float* __restrict__ Y, int64_t ld,
+                                                     int64_t m, int N, int vec,
+                                                     unsigned* __restrict__ cmax) {
   const int64_t rows = (m + gridDim.x - 1) / gridDim.x;
   const int64_t r0 = (int64_t)blockIdx.x * rows;
   const int64_t r1 = (r0 + rows < m) ? r0 + rows : m;
-  for (int c = threadIdx.x; c < N; c += blockDim.x) {
-    float mx = 0.f;
+  if (vec) {
+    for (int c = threadIdx.x * 4; c < N; c += blockDim.x * 4) {
+      float4 mx = make_float4(0.f, 0.f, 0.f, 0.f);
+      const float* p = Y + r0 * ld + c;
 #pragma unroll 8
-    for (int64_t r = r0; r < r1; ++r) mx = fmaxf(mx, fabsf(Y[r * ld + c]));
-    if (mx > 0.f) atomicMax(&cmax[c], __float_as_uint(mx));
+      for (int64_t r = r0; r < r1; ++r, p += ld) {
+        const float4 v = __ldg(reinterpret_cast<const float4*>(p));
+        mx.x = fmaxf(mx.x, fabsf(v.x));
+        mx.y = fmaxf(mx.y, fabsf(v.y));
+        mx.z = fmaxf(mx.z, fabsf(v.z));
+        mx.w = fmaxf(mx.w, fabsf(v.w));
+      }
+      if (mx.x > 0.f) atomicMax(&cmax[c], __float_as_uint(mx.x));
+      if (mx.y > 0.f) atomicMax(&cmax[c + 1], __float_as_uint(mx.y));
+      if (mx.z > 0.f) atomicMax(&cmax[c + 2], __float_as_uint(mx.z));
+      if (mx.w > 0.f) atomicMax(&cmax[c + 3], __float_as_uint(mx.w));
+    }
+  } else {
+    for (int c = threadIdx.x; c < N; c += blockDim.x) {
+      float mx = 0.f;
+      const float* p = Y + r0 * ld + c;
+#pragma unroll 8
+      for (int64_t r = r0; r < r1; ++r, p += ld) mx = fmaxf(mx, fabsf(__ldg(p)));
+      if (mx > 0.f) atomicMax(&cmax[c], __float_as_uint(mx));
+    }
   }
 }
 
@@ -245,32 +268,43 @@ __device__ __forceinline__ void split8(const float (&v)[8], uint4& h, uint4& l) 
   l = make_uint4(lw[0], lw[1], lw[2], lw[3]);
 }
 
-// hi/lo planes (m x ldp) of Y diag(s); columns N..ldp-1 are zero
-__global__ void pack_kernel(const float* __restrict__ Y, int64_t ld, int64_t m, int N, int ldp,
-                            const float* __restrict__ s, __half* __restrict__ hi,
-                            __half* __restrict__ lo, int vec) {
+// hi/lo planes (m x ldp) of Y diag(s); columns N..ldp-1 are zero.  Blocks
+// take tiles of `rt` rows; threads take 8-column groups of a tile.
+__global__ void __launch_bounds__(256) pack_kernel(const float* __restrict__ Y, int64_t ld,
+                                                   int64_t m, int N, int ldp, int rt,
+                                                   const float* __restrict__ s,
+                                                   __half* __restrict__ hi,
+                                                   __half* __restrict__ lo, int vec) {
   const int groups = ldp / 8;
-  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < m * groups;
-       e += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t r = e / groups;
-    const int c0 = (int)(e % groups) * 8;
-    const float* src = Y + r * ld + c0;
-    float v[8];
-    if (vec && c0 + 8 <= N) {
-      const float4 a = __ldg(reinterpret_cast<const float4*>(src));
-      const float4 b = __ldg(reinterpret_cast<const float4*>(src + 4));
-      v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w;
-      v[4] = b.x; v[5] = b.y; v[6] = b.z; v[7] = b.w;
-    } else {
+  for (int64_t tile = blockIdx.x; tile * rt < m; tile += gridDim.x) {
+    const int64_t r0 = tile * rt;
+    const int nr = (int)((m - r0 < rt) ? m - r0 : rt);
+    const int items = nr * groups;
+#pragma unroll 2
+    for (int idx = threadIdx.x; idx < items; idx += blockDim.x) {
+      const int rr = idx / groups;
+      const int c0 = (idx - rr * groups) * 8;
+      const int64_t r = r0 + rr;
+      const float* src = Y + r * ld + c0;
+      float v[8];
+      if (vec && c0 + 8 <= N) {
+        const float4 a = __ldg(reinterpret_cast<const float4*>(src));
+        const float4 b = __ldg(reinterpret_cast<const float4*>(src + 4));
+        v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w;
+        v[4] = b.x; v[5] = b.y; v[6] = b.z; v[7] = b.w;
+      } else {
 #pragma unroll
-      for (int q = 0; q < 8; ++q) v[q] = (c0 + q < N) ? src[q] : 0.f;
+        for (int q = 0; q < 8; ++q) v[q] = (c0 + q < N) ? src[q] : 0.f;
+      }
+      const float4 s0 = __ldg(reinterpret_cast<const float4*>(s + c0));
+      const float4 s1 = __ldg(reinterpret_cast<const float4*>(s + c0 + 4));
+      v[0] *= s0.x; v[1] *= s0.y; v[2] *= s0.z; v[3] *= s0.w;
+      v[4] *= s1.x; v[5] *= s1.y; v[6] *= s1.z; v[7] *= s1.w;
+      uint4 h, l;
+      split8(v, h, l);
+      *reinterpret_cast<uint4*>(hi + r * ldp + c0) = h;
+      *reinterpret_cast<uint4*>(lo + r * ldp + c0) = l;
     }
-#pragma unroll
-    for (int q = 0; q < 8; ++q) v[q] *= s[c0 + q];
-    uint4 h, l;
-    split8(v, h, l);
-    *reinterpret_cast<uint4*>(hi + r * ldp + c0) = h;
-    *reinterpret_cast<uint4*>(lo + r * ldp + c0) = l;
   }
 }
 
@@ -802,16 +836,20 @@ int pack_f32(const float* Y, int64_t ld, int64_t m, int64_t N, Packed& p, Arena&
   {
     ProfScope prof("colmax", st, 0.0, 4.0 * (double)m * N);
     const int rblocks = (int)std::max<int64_t>(1, std::min<int64_t>(m, (int64_t)num_sms() * 8));
-    hp::colmax_kernel<<<rblocks, threads, 0, st>>>(Y, ld, m, (int)N, cmax);
+    const int cvec = ((ld & 3) == 0) && ((N & 3) == 0) && ((reinterpret_cast<uintptr_t>(Y) & 15) == 0);
+    hp::colmax_kernel<<<rblocks, threads, 0, st>>>(Y, ld, m, (int)N, cvec, cmax);
     PLOM_CHECK_LAUNCH();
     hp::colscale_kernel<<<(int)cdiv(p.ld, 256), 256, 0, st>>>(cmax, (int)N, (int)p.ld, p.scale);
     PLOM_CHECK_LAUNCH();
   }
   ProfScope prof("pack_f16x2", st, 0.0, 4.0 * (double)m * N + 4.0 * (double)m * p.ld);
   const int vec = ((ld & 3) == 0) && ((reinterpret_cast<uintptr_t>(Y) & 15) == 0);
-  const int64_t items = m * (p.ld / 8);
-  const int blocks = (int)std::max<int64_t>(1, std::min<int64_t>(cdiv(items, 256), (int64_t)num_sms() * 16));
-  hp::pack_kernel<<<blocks, 256, 0, st>>>(Y, ld, m, (int)N, (int)p.ld, p.scale, p.hi, p.lo, vec);
+  const int groups = (int)(p.ld / 8);
+  const int rt = std::max(1, 2048 / groups);  // rows per tile: >= 2048 groups when rows are short
+  const int64_t tiles = cdiv(m, rt);
+  const int blocks = (int)std::max<int64_t>(1, std::min<int64_t>(tiles, (int64_t)num_sms() * 8));
+  hp::pack_kernel<<<blocks, 256, 0, st>>>(Y, ld, m, (int)N, (int)p.ld, rt, p.scale, p.hi, p.lo,
+                                          vec);
   PLOM_CHECK_LAUNCH();
   return PLOM_OK;
 }
