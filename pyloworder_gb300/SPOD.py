@@ -19,6 +19,8 @@ from . import vmmath as M
 
 __all__ = ["run"]
 
+SVD_STREAMS = 8  # concurrent per-frequency SVDs
+
 
 def _window(name, n):
     i = np.arange(n)
@@ -69,10 +71,25 @@ def run_device(x, ld, t_host, nDFT=0, nolap=0, remove_mean=True, window="hamming
     Lm = t.empty((nf, nBlks), dtype=x.dtype, device="cuda")
     P = t.empty((Mrows * nBlks, nf), dtype=x.dtype, device="cuda")
     P3 = P.view(nBlks, Mrows, nf)  # P[i + M*b, f] = Re U_f[i, b]
+    # the per-frequency SVDs are independent: round-robin over a few streams so
+    # that their small n x n stages (Cholesky, Jacobi) overlap
+    main = t.cuda.current_stream()
+    ready = t.cuda.Event()
+    ready.record(main)
+    streams = [t.cuda.Stream() for _ in range(min(SVD_STREAMS, nf))]
+    infos = []
+    for s in streams:
+        s.wait_event(ready)
     for fi in range(nf):
-        U, S, _ = M.tsqr_svd_device(Q[fi], nBlks, precision)
-        P3[:, :, fi] = U.real.transpose(0, 1)
-        Lm[fi] = (S * S).to(x.dtype)
+        with t.cuda.stream(streams[fi % len(streams)]):
+            U, S, _ = M.tsqr_svd_device(Q[fi], nBlks, precision, info_out=infos)
+            P3[:, :, fi] = U.real.transpose(0, 1)
+            Lm[fi] = (S * S).to(x.dtype)
+            del U, S
+    for s in streams:
+        main.wait_stream(s)
+    for info in infos:
+        L.check_info(info, "SPOD tsqr_svd")
     order = np.argsort(Lm[:, 0].cpu().numpy())[::-1].copy()
     od = t.as_tensor(order, device="cuda")
     return Lm.index_select(0, od), P.index_select(1, od), f[order]

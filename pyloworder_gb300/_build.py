@@ -21,6 +21,12 @@ NVCC_FLAGS = [
 ]
 
 
+def _extra_flags():
+    """Additional nvcc flags from PLOM_NVCC_FLAGS (whitespace separated), e.g.
+    -D overrides of kernel tile constants when tuning."""
+    return os.environ.get("PLOM_NVCC_FLAGS", "").split()
+
+
 def _nvcc():
     for cand in (os.environ.get("NVCC"), "/usr/local/cuda/bin/nvcc", "nvcc"):
         if cand and (os.path.sep not in cand or os.path.exists(cand)):
@@ -52,7 +58,7 @@ def build(force: bool = False, verbose: bool = False, jobs: int | None = None) -
 
     def compile_one(src):
         obj = os.path.join(BUILD, os.path.basename(src)[:-3] + ".o")
-        cmd = [nvcc, *NVCC_FLAGS, "-I", INCLUDE, "-c", src, "-o", obj]
+        cmd = [nvcc, *NVCC_FLAGS, *_extra_flags(), "-I", INCLUDE, "-c", src, "-o", obj]
         if verbose:
             print(" ".join(cmd), flush=True)
         r = subprocess.run(cmd, capture_output=True, text=True)

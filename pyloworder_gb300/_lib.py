@@ -118,27 +118,41 @@ def require_cuda():
 
 
 class Converted:
-    """Input array moved to the device, plus how to hand results back."""
+    """Input array moved to the device, plus how to hand results back.
 
-    def __init__(self, tensor, kind, device):
+    Results for a host torch tensor in page-locked memory come back in
+    page-locked memory too (torch's pinned-memory cache: repeated calls of
+    the same size reuse the same blocks, and device-to-host copies run at the
+    DMA rate instead of the first-touch rate of fresh pageable pages)."""
+
+    def __init__(self, tensor, kind, device, pinned=False):
         self.t = tensor
         self.kind = kind      # 'numpy' | 'torch'
         self.device = device  # original torch device for kind == 'torch'
+        self.pinned = pinned
 
     def back(self, x):
         if self.kind == "numpy":
             return x.cpu().numpy()
-        return x.to(self.device) if x.device != self.device else x
+        if x.device == self.device:
+            return x
+        if self.device.type == "cpu" and self.pinned:
+            out = torch().empty(x.shape, dtype=x.dtype, pin_memory=True)
+            out.copy_(x)
+            return out
+        return x.to(self.device)
 
 
 def to_device(A, dtype=None):
     """numpy array / torch tensor -> CUDA torch tensor (no copy when already
     a CUDA tensor of the right dtype with unit inner stride)."""
     t = require_cuda()
+    pinned = False
     if isinstance(A, t.Tensor):
         kind, dev = "torch", A.device
         x = A
         if x.device.type != "cuda":
+            pinned = bool(x.is_pinned())
             x = x.to("cuda")
     else:
         kind, dev = "numpy", None
@@ -146,7 +160,7 @@ def to_device(A, dtype=None):
         x = t.from_numpy(np.ascontiguousarray(arr)).to("cuda")
     if dtype is not None and x.dtype != dtype:
         x = x.to(dtype)
-    return Converted(x, kind, dev)
+    return Converted(x, kind, dev, pinned)
 
 
 def dtype_code(x):

@@ -3,7 +3,10 @@
 // row-major, each row a time series).
 //
 // GB300 mapping: one warp per row, 16-byte vector loads/stores when the row
-// start and length allow it, FP64 accumulation for both f32 and f64 data.
+// start and length allow it.  f64 data accumulate in FP64; f32 data in FP32
+// with compensated (Kahan) per-lane sums folded into FP64 across the warp (no
+// per-element FP64 instruction: GB300's FP64 rate is 1/64 of FP32), and the
+// mean is subtracted in FP32 as the reference's float32 path does.
 // All modes are HBM-bound: algorithmic bytes = read m*n*s (+ write m*n*s when
 // Y is produced).  A row is re-read from L1/L2 for the second and third
 // sweeps (variance, write-out), never from HBM for rows up to ~64 KB.
@@ -51,6 +54,109 @@ __device__ __forceinline__ void vstore<float>(float* p, const double* v) {
 template <>
 __device__ __forceinline__ void vstore<double>(double* p, const double* v) {
   *reinterpret_cast<double2*>(p) = make_double2(v[0], v[1]);
+}
+
+__device__ __forceinline__ void kahan_add(float& s, float& c, float v) {
+  const float y = v - c;
+  const float t = s + y;
+  c = (t - s) - y;
+  s = t;
+}
+
+// f32 rows: FP32 compensated sums (see the file comment)
+template <bool VEC>
+__global__ void __launch_bounds__(256) row_kernel_f32(const float* __restrict__ X, int64_t m,
+                                                      int64_t n, int64_t ldx,
+                                                      const float* __restrict__ mean_in,
+                                                      const float* __restrict__ var_in,
+                                                      float* __restrict__ mean_out,
+                                                      float* __restrict__ var_out, int want_var,
+                                                      int ymode, float* __restrict__ Y,
+                                                      int64_t ldy) {
+  const int lane = threadIdx.x & 31;
+  const int64_t warps_total = (int64_t)gridDim.x * (blockDim.x >> 5);
+  for (int64_t row = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); row < m;
+       row += warps_total) {
+    const float* x = X + row * ldx;
+    float muf;
+    if (mean_in) {
+      muf = mean_in[row];
+    } else {
+      float s = 0.f, c = 0.f;
+      if (VEC) {
+        const int64_t nv = n / 4;
+        int64_t j = lane;
+        for (; j + 96 < nv; j += 128) {  // 4 vectors in flight per lane
+          const float4 a = __ldg(reinterpret_cast<const float4*>(x + j * 4));
+          const float4 b = __ldg(reinterpret_cast<const float4*>(x + (j + 32) * 4));
+          const float4 d = __ldg(reinterpret_cast<const float4*>(x + (j + 64) * 4));
+          const float4 e = __ldg(reinterpret_cast<const float4*>(x + (j + 96) * 4));
+          kahan_add(s, c, (a.x + a.y) + (a.z + a.w));
+          kahan_add(s, c, (b.x + b.y) + (b.z + b.w));
+          kahan_add(s, c, (d.x + d.y) + (d.z + d.w));
+          kahan_add(s, c, (e.x + e.y) + (e.z + e.w));
+        }
+        for (; j < nv; j += 32) {
+          const float4 a = __ldg(reinterpret_cast<const float4*>(x + j * 4));
+          kahan_add(s, c, (a.x + a.y) + (a.z + a.w));
+        }
+      } else {
+        for (int64_t j = lane; j < n; j += 32) kahan_add(s, c, x[j]);
+      }
+      const double tot = warp_sum((double)s - (double)c);
+      const double mu = tot / (double)n;
+      muf = (float)mu;
+      if (lane == 0 && mean_out) mean_out[row] = muf;
+    }
+    float var = 1.f;
+    if (want_var) {
+      float s2 = 0.f, c2 = 0.f;
+      if (VEC) {
+        const int64_t nv = n / 4;
+        for (int64_t j = lane; j < nv; j += 32) {
+          const float4 a = __ldg(reinterpret_cast<const float4*>(x + j * 4));
+          const float d0 = a.x - muf, d1 = a.y - muf, d2 = a.z - muf, d3 = a.w - muf;
+          kahan_add(s2, c2, fmaf(d0, d0, d1 * d1) + fmaf(d2, d2, d3 * d3));
+        }
+      } else {
+        for (int64_t j = lane; j < n; j += 32) {
+          const float d = x[j] - muf;
+          kahan_add(s2, c2, d * d);
+        }
+      }
+      const double tot = warp_sum((double)s2 - (double)c2);
+      var = (float)(tot / (double)n);
+      if (lane == 0 && var_out) var_out[row] = var;
+    } else if (var_in) {
+      var = var_in[row];
+    }
+    if (ymode != Y_NONE) {
+      const float inv = (ymode == Y_NORM) ? 1.f / var : 1.f;
+      float* y = Y + row * ldy;
+      if (VEC) {
+        const int64_t nv = n / 4;
+        for (int64_t j = lane; j < nv; j += 32) {
+          float4 a = __ldg(reinterpret_cast<const float4*>(x + j * 4));
+          a.x -= muf;
+          a.y -= muf;
+          a.z -= muf;
+          a.w -= muf;
+          if (ymode == Y_NORM) {
+            a.x *= inv;
+            a.y *= inv;
+            a.z *= inv;
+            a.w *= inv;
+          }
+          *reinterpret_cast<float4*>(y + j * 4) = a;
+        }
+      } else {
+        for (int64_t j = lane; j < n; j += 32) {
+          const float d = x[j] - muf;
+          y[j] = (ymode == Y_NORM) ? d * inv : d;
+        }
+      }
+    }
+  }
 }
 
 // One warp per row.  VEC: use 16-byte vectors (caller checked alignment).
@@ -164,14 +270,25 @@ static int launch_rows(const T* X, int64_t m, int64_t n, int64_t ldx, const T* m
   if (blocks > cap) blocks = cap;
   ProfScope prof("rows_mean_subtract", st, 0.0,
                  (double)m * n * sizeof(T) * (ymode == Y_NONE ? 1.0 : 2.0));
-  if (vec)
-    row_kernel<T, true><<<(unsigned)blocks, threads, 0, st>>>(X, m, n, ldx, mean_in, var_in,
-                                                              mean_out, var_out, want_var, ymode,
-                                                              Y, ldy);
-  else
-    row_kernel<T, false><<<(unsigned)blocks, threads, 0, st>>>(X, m, n, ldx, mean_in, var_in,
-                                                               mean_out, var_out, want_var, ymode,
-                                                               Y, ldy);
+  if constexpr (sizeof(T) == 4) {
+    if (vec)
+      row_kernel_f32<true><<<(unsigned)blocks, threads, 0, st>>>(X, m, n, ldx, mean_in, var_in,
+                                                                 mean_out, var_out, want_var,
+                                                                 ymode, Y, ldy);
+    else
+      row_kernel_f32<false><<<(unsigned)blocks, threads, 0, st>>>(X, m, n, ldx, mean_in, var_in,
+                                                                  mean_out, var_out, want_var,
+                                                                  ymode, Y, ldy);
+  } else {
+    if (vec)
+      row_kernel<T, true><<<(unsigned)blocks, threads, 0, st>>>(X, m, n, ldx, mean_in, var_in,
+                                                                mean_out, var_out, want_var,
+                                                                ymode, Y, ldy);
+    else
+      row_kernel<T, false><<<(unsigned)blocks, threads, 0, st>>>(X, m, n, ldx, mean_in, var_in,
+                                                                 mean_out, var_out, want_var,
+                                                                 ymode, Y, ldy);
+  }
   PLOM_CHECK_LAUNCH();
   return PLOM_OK;
 }

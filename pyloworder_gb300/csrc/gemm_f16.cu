@@ -350,20 +350,32 @@ __global__ void __launch_bounds__(256) split_w16_kernel(const double* __restrict
 // ---------------------------------------------------------------------------
 // gram: upper 128 x 128 tiles x row chunks, MN-major operands from TMA
 // ---------------------------------------------------------------------------
-constexpr int G_BK = 64;                       // rows per stage
-constexpr uint32_t G_BOX = 64 * 128;           // 64 rows x 64 fp16 (8 KB)
-constexpr uint32_t G_TILE = 2 * G_BOX;         // 64 rows x 128 columns of one plane
+#ifndef PLOM_GRAM_BK
+#define PLOM_GRAM_BK 64
+#endif
+#ifndef PLOM_GRAM_KSUB
+#define PLOM_GRAM_KSUB 4096
+#endif
+constexpr int G_BK = PLOM_GRAM_BK;             // rows per stage (a multiple of 16)
+constexpr uint32_t G_BOX = G_BK * 128;         // G_BK rows x 64 fp16
+constexpr uint32_t G_TILE = 2 * G_BOX;         // G_BK rows x 128 columns of one plane
 constexpr uint32_t G_STAGE = 4 * G_TILE;       // A hi, A lo, B hi, B lo
-constexpr int G_STAGES = 3;
-// Rows accumulated in TMEM (FP32) before the FP64 drain: 256 UMMA of K = 16
-// per accumulator.
-constexpr int G_KSUB = 4096;
+constexpr int G_STAGES = (3 * 64) / G_BK;      // 192 KiB of stages
+static_assert(G_BK % 16 == 0 && G_BK >= 16 && G_BK <= 64, "stage rows");
+// Rows accumulated in TMEM (FP32) before the FP64 drain (4,096 rows: 256 UMMA
+// of K = 16 per accumulator).
+constexpr int G_KSUB = PLOM_GRAM_KSUB;
+static_assert(G_KSUB % G_BK == 0, "drain on stage boundaries");
 constexpr size_t G_SMEM = (size_t)G_STAGES * G_STAGE + 1024;
 constexpr uint32_t G_TMEM = 512;               // 2 buffers x (main 128 + correction 128)
 
+// SYM: upper tiles of A^T A (tmB unused) with the exact diagonal on diagonal
+// tiles; otherwise every tile of A^T B (tna x tnb tiles, B from tmB).
+template <bool SYM>
 __global__ void __launch_bounds__(320, 1)
-    gram16_kernel(const __grid_constant__ CUtensorMap tmP, int64_t m, int tn,
-                  int64_t rows_per_chunk, int chunks, double* __restrict__ part, int* err) {
+    gram16_kernel(const __grid_constant__ CUtensorMap tmP, const __grid_constant__ CUtensorMap tmB,
+                  int64_t m, int tn, int tnb, int64_t rows_per_chunk, int chunks,
+                  double* __restrict__ part, int* err) {
   extern __shared__ uint8_t smem_raw[];
   __shared__ uint64_t full_bar[G_STAGES], empty_bar[G_STAGES];
   __shared__ uint64_t tfull[2], tempty[2], dfull[2];
@@ -374,16 +386,22 @@ __global__ void __launch_bounds__(320, 1)
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   // consecutive CTAs take different tiles of the same row chunk, so the CTAs
   // resident together read the same rows and share them through L2
-  const int ntiles = tn * (tn + 1) / 2;
+  const int ntiles = SYM ? tn * (tn + 1) / 2 : tn * tnb;
   const int chunk = (int)(blockIdx.x / ntiles), tile = (int)(blockIdx.x % ntiles);
   const int item = tile * chunks + chunk;  // partial slab index (tile-major)
-  int ti = 0, rem = tile;
-  while (rem >= tn - ti) {
-    rem -= tn - ti;
-    ++ti;
+  int ti = 0, tj = 0;
+  if (SYM) {
+    int rem = tile;
+    while (rem >= tn - ti) {
+      rem -= tn - ti;
+      ++ti;
+    }
+    tj = ti + rem;
+  } else {
+    ti = tile / tnb;
+    tj = tile % tnb;
   }
-  const int tj = ti + rem;
-  const bool diag = (ti == tj);
+  const bool diag = SYM && (ti == tj);
   const int I0 = ti * 128, J0 = tj * 128;
   const int64_t r_beg = (int64_t)chunk * rows_per_chunk;
   const int64_t r_end = (r_beg + rows_per_chunk < m) ? r_beg + rows_per_chunk : m;
@@ -410,7 +428,10 @@ __global__ void __launch_bounds__(320, 1)
     tmem_alloc(&tmem_sh, G_TMEM);
     tmem_relinquish();
   }
-  if (warp == 9 && lane == 0) tma_prefetch_map(&tmP);
+  if (warp == 9 && lane == 0) {
+    tma_prefetch_map(&tmP);
+    if (!SYM) tma_prefetch_map(&tmB);
+  }
   fence_before();
   __syncthreads();
   fence_after();
@@ -433,8 +454,9 @@ __global__ void __launch_bounds__(320, 1)
           tma_load_3d(st + z * G_TILE, &tmP, I0, y, z, &full_bar[s]);
           tma_load_3d(st + z * G_TILE + G_BOX, &tmP, I0 + 64, y, z, &full_bar[s]);
           if (!diag) {
-            tma_load_3d(st + (2 + z) * G_TILE, &tmP, J0, y, z, &full_bar[s]);
-            tma_load_3d(st + (2 + z) * G_TILE + G_BOX, &tmP, J0 + 64, y, z, &full_bar[s]);
+            const CUtensorMap* mb = SYM ? &tmP : &tmB;
+            tma_load_3d(st + (2 + z) * G_TILE, mb, J0, y, z, &full_bar[s]);
+            tma_load_3d(st + (2 + z) * G_TILE + G_BOX, mb, J0 + 64, y, z, &full_bar[s]);
           }
         }
       }
@@ -562,6 +584,25 @@ __global__ void __launch_bounds__(320, 1)
     __syncwarp();
     fence_after();
     tmem_dealloc(tmem, G_TMEM);
+  }
+}
+
+// C[i][j] (Na x Nb, ldc) = sum over chunks of the tile partials / (sA_i sB_j)
+__global__ void tn16_reduce_kernel(const double* __restrict__ part, int Na, int Nb, int tnb,
+                                   int chunks, const float* __restrict__ sa,
+                                   const float* __restrict__ sb, double* __restrict__ C,
+                                   int64_t ldc) {
+  const int64_t total = (int64_t)Na * Nb;
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < total;
+       e += (int64_t)gridDim.x * blockDim.x) {
+    const int i = (int)(e / Nb), j = (int)(e % Nb);
+    const int ti = i / 128, tj = j / 128;
+    const int tile = ti * tnb + tj;
+    const double* p = part + ((int64_t)tile * chunks) * 128 * 128 + (int64_t)(i - ti * 128) * 128 +
+                      (j - tj * 128);
+    double acc = 0.0;
+    for (int c = 0; c < chunks; ++c) acc += p[(int64_t)c * 128 * 128];
+    C[(int64_t)i * ldc + j] = acc / ((double)sa[i] * (double)sb[j]);
   }
 }
 
@@ -854,22 +895,18 @@ int pack_f32(const float* Y, int64_t ld, int64_t m, int64_t N, Packed& p, Arena&
   return PLOM_OK;
 }
 
-// work items of the Gram: tiles x chunks, a whole number of waves of the
-// GPU (one CTA per SM) and at least 4 waves when the rows allow it
+// work items of the Gram: tiles x chunks, the fewest whole waves of the GPU
+// (one CTA per SM) that the tile count divides, with chunks of at least four
+// stages; fewer chunks keep the partial slabs (and their reduction) small
 static int gram16_chunks(int64_t m, int tiles) {
   const int64_t sms = num_sms();
   const int64_t maxc = std::max<int64_t>(1, cdiv(m, 4 * hp::G_BK));
-  int64_t best = 1;
   for (int64_t waves = 1; waves <= 64; ++waves) {
     const int64_t items = waves * sms;
     if (items % tiles) continue;
-    const int64_t c = items / tiles;
-    if (c > maxc) break;
-    best = c;
-    if (waves >= 4) break;
+    return (int)std::max<int64_t>(1, std::min(maxc, items / tiles));
   }
-  if (best == 1) best = std::min<int64_t>(maxc, cdiv(4 * sms, tiles));
-  return (int)std::max<int64_t>(1, best);
+  return (int)std::max<int64_t>(1, std::min<int64_t>(maxc, cdiv(2 * sms, tiles)));
 }
 
 int gram_packed(const Packed& p, double* G, int* err, Arena& ws, cudaStream_t st) {
@@ -887,22 +924,66 @@ int gram_packed(const Packed& p, double* G, int* err, Arena& ws, cudaStream_t st
                "gram16: bad arguments");
   static bool attr = false;
   if (!attr) {
-    PLOM_CHECK_CUDA(cudaFuncSetAttribute(hp::gram16_kernel,
+    PLOM_CHECK_CUDA(cudaFuncSetAttribute(hp::gram16_kernel<true>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)hp::G_SMEM));
+    PLOM_CHECK_CUDA(cudaFuncSetAttribute(hp::gram16_kernel<false>,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)hp::G_SMEM));
     attr = true;
   }
   CUtensorMap tm;
-  PLOM_REQUIRE(make_map_planes(&tm, p.hi, (uint64_t)p.ld, (uint64_t)m, (uint64_t)p.ld, 64, 64),
+  PLOM_REQUIRE(make_map_planes(&tm, p.hi, (uint64_t)p.ld, (uint64_t)m, (uint64_t)p.ld, 64, hp::G_BK),
                PLOM_ERR_CUDA, "gram16: tensor map encoding failed");
   ProfScope prof_g("tc_gram_f16x3", st, (double)m * N * N, 4.0 * (double)m * p.ld);
-  hp::gram16_kernel<<<tiles * chunks_eff, 320, hp::G_SMEM, st>>>(tm, m, tn, rpc, chunks_eff, part,
-                                                                 err);
+  hp::gram16_kernel<true><<<tiles * chunks_eff, 320, hp::G_SMEM, st>>>(tm, tm, m, tn, tn, rpc,
+                                                                       chunks_eff, part, err);
   PLOM_CHECK_LAUNCH();
   const int64_t total = N * N;
   const int blocks = (int)std::min<int64_t>(cdiv(total, 256), (int64_t)num_sms() * 16);
   ProfScope prof_r("gram_reduce", st, 0.0, 8.0 * (double)tiles * chunks_eff * 128 * 128);
   hp::gram16_reduce_kernel<<<blocks, 256, 0, st>>>(part, (int)N, tn, chunks_eff, p.scale, G);
+  PLOM_CHECK_LAUNCH();
+  return PLOM_OK;
+}
+
+int tn_packed(const Packed& a, const Packed& b, double* C, int64_t ldc, int* err, Arena& ws,
+              cudaStream_t st) {
+  const int64_t m = a.m;
+  const int tna = (int)cdiv(a.ld, 128), tnb = (int)cdiv(b.ld, 128);
+  const int tiles = tna * tnb;
+  const int chunks = gram16_chunks(m, tiles);
+  int64_t rpc = cdiv(m, chunks);
+  rpc = cdiv(rpc, hp::G_BK) * hp::G_BK;
+  const int chunks_eff = (int)std::max<int64_t>(1, cdiv(m, rpc));
+  double* part = ws.take<double>((size_t)tiles * chunks_eff * 128 * 128);
+  if (ws.measuring()) return PLOM_OK;
+  PLOM_REQUIRE(!ws.overflow(), PLOM_ERR_WORKSPACE, "tn16: workspace too small");
+  PLOM_REQUIRE(a.hi && b.hi && C && part && m >= 1 && m < (1ll << 31) && b.m == m &&
+                   ldc >= b.N,
+               PLOM_ERR_ARG, "tn16: bad arguments");
+  static bool attr = false;
+  if (!attr) {
+    PLOM_CHECK_CUDA(cudaFuncSetAttribute(hp::gram16_kernel<false>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)hp::G_SMEM));
+    attr = true;
+  }
+  CUtensorMap ta, tb;
+  PLOM_REQUIRE(make_map_planes(&ta, a.hi, (uint64_t)a.ld, (uint64_t)m, (uint64_t)a.ld, 64, hp::G_BK) &&
+                   make_map_planes(&tb, b.hi, (uint64_t)b.ld, (uint64_t)m, (uint64_t)b.ld, 64, hp::G_BK),
+               PLOM_ERR_CUDA, "tn16: tensor map encoding failed");
+  {
+    ProfScope prof("tc_tn_f16x3", st, 2.0 * (double)m * a.N * b.N,
+                   4.0 * (double)m * (a.ld + b.ld));
+    hp::gram16_kernel<false><<<tiles * chunks_eff, 320, hp::G_SMEM, st>>>(ta, tb, m, tna, tnb, rpc,
+                                                                          chunks_eff, part, err);
+    PLOM_CHECK_LAUNCH();
+  }
+  const int64_t total = a.N * b.N;
+  const int blocks = (int)std::max<int64_t>(1, std::min<int64_t>(cdiv(total, 256), (int64_t)num_sms() * 16));
+  hp::tn16_reduce_kernel<<<blocks, 256, 0, st>>>(part, (int)a.N, (int)b.N, tnb, chunks_eff, a.scale,
+                                                 b.scale, C, ldc);
   PLOM_CHECK_LAUNCH();
   return PLOM_OK;
 }

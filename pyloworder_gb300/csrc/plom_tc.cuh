@@ -27,6 +27,9 @@ int pack_f32(const float* Y, int64_t ld, int64_t m, int64_t N, Packed& p, Arena&
              cudaStream_t st);
 // G (N x N, FP64) = Y^T Y
 int gram_packed(const Packed& p, double* G, int* err, Arena& ws, cudaStream_t st);
+// C (A.N x B.N, FP64, ldc) = A^T B for two packed operands with the same rows
+int tn_packed(const Packed& a, const Packed& b, double* C, int64_t ldc, int* err, Arena& ws,
+              cudaStream_t st);
 // Y W for W (N x k, FP64, ldw): FP32 into C (ldc) when out == nullptr, else
 // packed into *out (planes m x packed_ld(k), scale 2^14)
 int apply_packed(const Packed& p, const double* W, int64_t ldw, int64_t k, float* C, int64_t ldc,

@@ -118,6 +118,142 @@ __global__ void __launch_bounds__(256) spod_fft_kernel(
   }
 }
 
+// ---------------------------------------------------------------------------
+// Fast path: FP32 data, nDFT = 32 E with E a power of two (1..32).  One warp
+// transforms one window in registers: lane l holds samples l + 32 e; an
+// E-point DIF FFT over its registers, twiddles w_N^(l k1), then a 32-point
+// DIF FFT across the lanes with shuffles.  Lane l, register r ends with bin
+// k1 + E k2, k1 = bitrev_E(r), k2 = bitrev_32(l).  A CTA owns one point (all
+// its Welch blocks); its bins are staged in shared memory as [block][bin]
+// and written per frequency as contiguous runs of nBlks values.
+// ---------------------------------------------------------------------------
+template <int E>
+__device__ __forceinline__ void warp_fft(float (&re)[E], float (&im)[E], int lane, int N,
+                                         const float* __restrict__ tc,
+                                         const float* __restrict__ ts) {
+  // E-point DIF over the registers (twiddle w_{2h}^j = w_N^{j N / 2h})
+#pragma unroll
+  for (int h = E / 2; h >= 1; h >>= 1) {
+#pragma unroll
+    for (int blk = 0; blk < E; blk += 2 * h) {
+#pragma unroll
+      for (int j = 0; j < h; ++j) {
+        const float ur = re[blk + j], ui = im[blk + j];
+        const float vr = re[blk + j + h], vi = im[blk + j + h];
+        re[blk + j] = ur + vr;
+        im[blk + j] = ui + vi;
+        const float dr = ur - vr, di = ui - vi;
+        const int ti = j * (N / (2 * h));
+        const float wr = tc[ti], wi = ts[ti];
+        re[blk + j + h] = dr * wr - di * wi;
+        im[blk + j + h] = dr * wi + di * wr;
+      }
+    }
+  }
+  // twiddles w_N^(l k1), k1 = bitrev_E(r)
+#pragma unroll
+  for (int r = 1; r < E; ++r) {
+    const int k1 = (int)(__brev((unsigned)r) >> (32 - __ffs(E) + 1));
+    const int ti = (lane * k1) & (N - 1);
+    const float wr = tc[ti], wi = ts[ti];
+    const float xr = re[r], xi = im[r];
+    re[r] = xr * wr - xi * wi;
+    im[r] = xr * wi + xi * wr;
+  }
+  // 32-point DIF across the lanes
+#pragma unroll
+  for (int d = 16; d >= 1; d >>= 1) {
+    const bool upper = (lane & d) != 0;
+    const int ti = (lane & (d - 1)) * (N / (2 * d));
+    const float wr = tc[ti], wi = ts[ti];
+#pragma unroll
+    for (int r = 0; r < E; ++r) {
+      const float pr = __shfl_xor_sync(0xffffffffu, re[r], d);
+      const float pi = __shfl_xor_sync(0xffffffffu, im[r], d);
+      if (!upper) {
+        re[r] += pr;
+        im[r] += pi;
+      } else {
+        const float dr = pr - re[r], di = pi - im[r];
+        re[r] = dr * wr - di * wi;
+        im[r] = dr * wi + di * wr;
+      }
+    }
+  }
+}
+
+template <int E>
+__global__ void __launch_bounds__(256) spod_fft32_kernel(
+    const float* __restrict__ Y, int64_t M, int64_t ldy, int step, int nBlks, int nf,
+    const float* __restrict__ window, const float* __restrict__ twr,
+    const float* __restrict__ twi, float scale, float* __restrict__ Q) {
+  constexpr int N = 32 * E;
+  extern __shared__ unsigned char smem_raw[];
+  float* sw = reinterpret_cast<float*>(smem_raw);  // window [N]
+  float* sc = sw + N;                              // cos    [N]
+  float* ss = sc + N;                              // -sin   [N]
+  c2<float>* stage = reinterpret_cast<c2<float>*>(ss + N);  // [nBlks][nf]
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  for (int j = tid; j < N; j += blockDim.x) {
+    sw[j] = window[j];
+    sc[j] = twr[j];
+    ss[j] = twi[j];
+  }
+  __syncthreads();
+  constexpr int LOGE = (E == 1) ? 0 : (E == 2) ? 1 : (E == 4) ? 2 : (E == 8) ? 3 : (E == 16) ? 4 : 5;
+  for (int64_t row = blockIdx.x; row < M; row += gridDim.x) {
+    const float* x = Y + row * ldy;
+    for (int b = warp; b < nBlks; b += 8) {
+      const float* xb = x + (int64_t)b * step;
+      float re[E], im[E];
+#pragma unroll
+      for (int e = 0; e < E; ++e) {
+        const int j = lane + 32 * e;
+        re[e] = __ldg(xb + j) * sw[j];
+        im[e] = 0.f;
+      }
+      warp_fft<E>(re, im, lane, N, sc, ss);
+      const int k2 = (int)(__brev((unsigned)lane) >> 27);
+      c2<float>* out = stage + (size_t)b * nf;
+#pragma unroll
+      for (int r = 0; r < E; ++r) {
+        const int k1 = LOGE ? (int)(__brev((unsigned)r) >> (32 - LOGE)) : 0;
+        const int f = k1 + E * k2;
+        if (f < nf) {
+          const float g = (f >= 1 && f <= nf - 2) ? 2.f * scale : scale;
+          out[f].re = re[r] * g;
+          out[f].im = im[r] * g;
+        }
+      }
+    }
+    __syncthreads();
+    // Q[f][row][b]: one contiguous run of nBlks values per frequency
+    c2<float>* Qc = reinterpret_cast<c2<float>*>(Q);
+    for (int e = tid; e < nf * nBlks; e += blockDim.x) {
+      const int f = e / nBlks, b = e - f * nBlks;
+      Qc[((int64_t)f * M + row) * nBlks + b] = stage[(size_t)b * nf + f];
+    }
+    __syncthreads();
+  }
+}
+
+template <int E>
+static int spod_fft32_launch(const float* Y, int64_t M, int64_t ldy, int step, int nBlks, int nf,
+                             const float* window, const float* twr, const float* twi, double scale,
+                             float* Q, cudaStream_t st) {
+  const size_t smem = sizeof(float) * 3 * 32 * E + sizeof(c2<float>) * (size_t)nBlks * nf;
+  PLOM_CHECK_CUDA(cudaFuncSetAttribute(spod_fft32_kernel<E>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  int per_sm = 0;
+  PLOM_CHECK_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, spod_fft32_kernel<E>,
+                                                                256, smem));
+  const int64_t grid = std::min<int64_t>(M, (int64_t)std::max(1, per_sm) * num_sms() * 8);
+  spod_fft32_kernel<E><<<(unsigned)grid, 256, smem, st>>>(Y, M, ldy, step, nBlks, nf, window, twr,
+                                                          twi, (float)scale, Q);
+  PLOM_CHECK_LAUNCH();
+  return PLOM_OK;
+}
+
 template <typename T>
 static int spod_fft_impl(const T* Y, int64_t M, int64_t N, int64_t ldy, int nDFT, int step,
                          int nBlks, int nf, const T* window, const T* twr, const T* twi,
@@ -126,6 +262,21 @@ static int spod_fft_impl(const T* Y, int64_t M, int64_t N, int64_t ldy, int nDFT
   if ((nDFT & (nDFT - 1)) == 0) {
     log2n = 0;
     while ((1 << log2n) < nDFT) ++log2n;
+  }
+  if constexpr (sizeof(T) == 4) {
+    const size_t stage = sizeof(c2<float>) * (size_t)nBlks * nf + sizeof(float) * 3 * nDFT;
+    if (log2n >= 5 && log2n <= 10 && stage <= 200 * 1024) {
+      ProfScope prof("spod_fft", st, 5.0 * (double)M * nBlks * nDFT * log2n,
+                     (double)sizeof(T) * ((double)M * N + 2.0 * M * nBlks * nf));
+      switch (log2n) {
+        case 5: return spod_fft32_launch<1>(Y, M, ldy, step, nBlks, nf, window, twr, twi, scale, Q, st);
+        case 6: return spod_fft32_launch<2>(Y, M, ldy, step, nBlks, nf, window, twr, twi, scale, Q, st);
+        case 7: return spod_fft32_launch<4>(Y, M, ldy, step, nBlks, nf, window, twr, twi, scale, Q, st);
+        case 8: return spod_fft32_launch<8>(Y, M, ldy, step, nBlks, nf, window, twr, twi, scale, Q, st);
+        case 9: return spod_fft32_launch<16>(Y, M, ldy, step, nBlks, nf, window, twr, twi, scale, Q, st);
+        default: return spod_fft32_launch<32>(Y, M, ldy, step, nBlks, nf, window, twr, twi, scale, Q, st);
+      }
+    }
   }
   const size_t fixed = sizeof(T) * 3 * (size_t)nDFT + sizeof(c2<T>) * 8 * (size_t)nDFT;
   const size_t per_row = sizeof(c2<T>) * (size_t)nBlks * nf;

@@ -453,10 +453,76 @@ static int tsqr_impl(int prec, const TI* X, int64_t m, int n, int64_t ldx, TI* Q
 // ---------------------------------------------------------------------------
 // randomized SVD (pyLOM/vmmath/svd.py:121-144, 255-273; svd.c:1267-1519)
 // ---------------------------------------------------------------------------
+// Mixed form on FP32 data: A is packed once; the passes over it (A Omega,
+// A^T Q, A Q2, Q^T A) run on the tensor cores from the packed planes.
+static int rsvd_packed(const float* A, int64_t m, int64_t n, int64_t lda, int r, int q,
+                       uint64_t seed, float* U, int64_t ldu, float* S, float* VT, int* info,
+                       Arena& ws, cudaStream_t st) {
+  Packed Ap, Qp;
+  packed_carve(ws, Ap, m, n);
+  packed_carve(ws, Qp, m, r);
+  float* omega = ws.take<float>((size_t)n * r);
+  double* om64 = ws.take<double>((size_t)n * r);
+  float* Y = ws.take<float>((size_t)m * r);
+  float* Qm = ws.take<float>((size_t)m * r);
+  float* Rq = ws.take<float>((size_t)r * r);
+  double* Q2 = ws.take<double>((size_t)n * r);  // A^T Q (n x r); the last one is B^T
+  double* Ub = ws.take<double>((size_t)n * r);
+  double* Sb = ws.take<double>(r);
+  double* VbH = ws.take<double>((size_t)r * r);
+  double* Ur = ws.take<double>((size_t)r * r);
+  double* Vo = ws.take<double>((size_t)r * n);
+  const size_t mark = ws.off;
+  size_t need = mark;
+  auto sub = [&](auto&& fn) -> int {
+    ws.off = mark;
+    const int s = fn();
+    need = std::max(need, ws.off);
+    ws.off = mark;
+    return s;
+  };
+  const bool meas = ws.measuring();
+  if (!meas) {
+    PLOM_REQUIRE(!ws.overflow(), PLOM_ERR_WORKSPACE, "randomized_svd: workspace too small");
+    PLOM_TRY(fill_uniform_dispatch(PLOM_F32, omega, n * r, seed, st));
+    PLOM_TRY((convert<float, double>(omega, om64, n * r, st)));
+  }
+  PLOM_TRY(sub([&] { return pack_f32(A, lda, m, n, Ap, ws, st); }));
+  // Y = A Omega
+  PLOM_TRY(sub([&] { return apply_packed(Ap, om64, r, r, Y, r, nullptr, info, ws, st); }));
+  for (int j = 0; j <= q; ++j) {
+    PLOM_TRY(sub([&] { return tsqr_packed(Y, m, r, r, Qm, r, Rq, info, ws, st); }));
+    PLOM_TRY(sub([&] { return pack_f32(Qm, r, m, r, Qp, ws, st); }));
+    // Q2 = A^T Q (n x r); after the last iteration this is B^T = (Q^T A)^T
+    PLOM_TRY(sub([&] { return tn_packed(Ap, Qp, Q2, r, info, ws, st); }));
+    if (j == q) break;
+    PLOM_TRY(sub([&] { return apply_packed(Ap, Q2, r, r, Y, r, nullptr, info, ws, st); }));
+  }
+  // svd(B) through the tall n x r matrix B^T: B^T = Ub Sb VbH -> B = Vb Sb Ub^T
+  PLOM_TRY(sub([&]() {
+    return tsqr_svd_impl<double, double>(PLOM_PREC_FP64, false, Q2, n, r, r, Ub, r, Sb, VbH, info,
+                                         ws, st);
+  }));
+  if (!meas) {
+    PLOM_TRY(transpose_f64(VbH, Ur, r, r, 1, st));  // Ur = Vb = VbH^T (real)
+    PLOM_TRY(transpose_f64(Ub, Vo, n, r, 1, st));   // V (r x n) = Ub^T
+    PLOM_TRY((convert<double, float>(Sb, S, r, st)));
+    PLOM_TRY((convert<double, float>(Vo, VT, (int64_t)r * n, st)));
+  }
+  // U = Q Ur
+  PLOM_TRY(sub([&] { return tall_apply<float, float>(PLOM_PREC_MIXED, Qm, r, m, r, Ur, r, U, ldu, info, ws, st); }));
+  ws.off = need;
+  return PLOM_OK;
+}
+
 template <typename TI, typename TC>
 static int rsvd_impl(int prec, const TI* A, int64_t m, int64_t n, int64_t lda, int r, int q,
                      uint64_t seed, TI* U, int64_t ldu, TI* S, TI* VT, int* info, Arena& ws,
                      cudaStream_t st) {
+  if constexpr (std::is_same<TI, float>::value && std::is_same<TC, float>::value) {
+    if (prec == PLOM_PREC_MIXED && packed_ok(m))
+      return rsvd_packed(A, m, n, lda, r, q, seed, U, ldu, S, VT, info, ws, st);
+  }
   TI* omega = ws.take<TI>((size_t)n * r);
   TC* omc = ws.take<TC>((size_t)n * r);
   TC* Y = ws.take<TC>((size_t)m * r);

@@ -182,14 +182,17 @@ def transpose(A):
 # SVD family: pyLOM/vmmath/svd.py, src/svd.c
 # --------------------------------------------------------------------------
 
-def tsqr_svd_device(x, ld, precision=None):
-    """TSQR-SVD of a CUDA tensor -> (U, S, V) CUDA tensors (V = V^T, n x n)."""
+def tsqr_svd_device(x, ld, precision=None, info_out=None):
+    """TSQR-SVD of a CUDA tensor -> (U, S, V) CUDA tensors (V = V^T, n x n).
+    With `info_out` (a list) the status words are appended to it unchecked
+    instead of being read back at once, so that calls on several streams can
+    overlap; the caller checks them with L.check_info afterwards."""
     t = L.torch()
     m, n = x.shape
     if m < n:
         # wide input: svd of the (tall) transpose, as LAPACK's gesdd would see it
         # x^T = Ut St Vt  ->  x = Vt^T St Ut^T (plain transposes, also for complex)
-        Ut, St, Vt = tsqr_svd_device(x.transpose(0, 1).contiguous(), m, precision)
+        Ut, St, Vt = tsqr_svd_device(x.transpose(0, 1).contiguous(), m, precision, info_out)
         return Vt.transpose(0, 1).contiguous(), St, Ut.transpose(0, 1).contiguous()
     dt = L.dtype_code(x)
     prec = L.precision_code(precision, x)
@@ -200,7 +203,10 @@ def tsqr_svd_device(x, ld, precision=None):
     info = L.new_info()
     L.call("plom_tsqr_svd", dt, prec, L.ptr(x), m, n, ld, L.ptr(U), n, L.ptr(S), L.ptr(V),
            L.ptr(ws), ws.numel(), L.ptr(info), L.stream_ptr())
-    L.check_info(info, "tsqr_svd")
+    if info_out is None:
+        L.check_info(info, "tsqr_svd")
+    else:
+        info_out.append(info)
     return U, S, V
 
 

@@ -41,7 +41,11 @@ def test_workspace_queries():
     # mixed: one FP32 m x n buffer (Q1 lives in U); FP64: two FP64 buffers
     assert 4 * m * n <= mixed < 4 * m * n + (1 << 30)
     assert 16 * m * n <= fp64 < 16 * m * n + (1 << 30)
-    assert lib.plom_randomized_svd_workspace(L.F32, L.PREC_MIXED, m, n, 80) < 8 * m * 80 * 3 + (1 << 30)
+    # mixed randomized: A packed once (4 m n bytes), Q packed (pitch 128), Y and
+    # Q in FP32, and the packed CholeskyQR of the m x r sketch (two pitch-128
+    # operands)
+    rs = lib.plom_randomized_svd_workspace(L.F32, L.PREC_MIXED, m, n, 80)
+    assert 4 * m * n <= rs < 4 * m * n + 4 * m * 128 * 3 + 8 * m * 80 + (1 << 30)
     assert lib.plom_matmul_workspace(L.F64, L.PREC_FP64, 1, 1024, 80, m) > 0
 
 

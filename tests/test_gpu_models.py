@@ -162,3 +162,24 @@ def test_spod_fft_stage(nDFT, nolap):
         F = np.fft.fft(Y[:, i0:i0 + nDFT] * win, axis=1)[:, :nf] * scale
         F[:, 1:nf - 1] *= 2
         np.testing.assert_allclose(Q[:, :, b].T, F, rtol=1e-11, atol=1e-12 * np.abs(F).max())
+
+
+@pytest.mark.parametrize("nDFT,nolap", [(32, 16), (64, 32), (256, 128), (1024, 512), (128, 0)])
+def test_spod_fft_stage_f32_register_fft(nDFT, nolap):
+    """FP32 power-of-two windows take the warp-register FFT; compare with numpy."""
+    rng = np.random.default_rng(nDFT + 7)
+    M, N = 29, 3000
+    Y = rng.standard_normal((M, N)).astype(np.float32)
+    step = nDFT - nolap if nolap else nDFT
+    nBlks = (N - nolap) // step
+    nf = nDFT // 2 + 1
+    win = 0.54 - 0.46 * np.cos(2 * np.pi * np.arange(nDFT) / (nDFT - 1))
+    scale = (1 / win.mean()) / nDFT / np.sqrt(nBlks)
+    Yd = torch.tensor(Y, device="cuda")
+    Q = P.SPOD.spod_fft_device(Yd, N, nDFT, nDFT - step, nBlks, nf, win, scale).cpu().numpy()
+    assert Q.dtype == np.complex64
+    for b in range(nBlks):
+        i0 = b * step
+        F = np.fft.fft(Y[:, i0:i0 + nDFT].astype(np.float64) * win, axis=1)[:, :nf] * scale
+        F[:, 1:nf - 1] *= 2
+        np.testing.assert_allclose(Q[:, :, b].T, F, rtol=0, atol=2e-6 * np.abs(F).max())

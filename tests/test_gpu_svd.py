@@ -122,6 +122,22 @@ def test_randomized_philox_matches_oracle():
     cols_up_to_phase(V[:12].T, Vr[:12].T, 1e-8)
 
 
+def test_randomized_f32_mixed_tensor_core():
+    """FP32 data take the packed tensor-core passes (A Omega, A^T Q, A Q2)."""
+    rng = np.random.default_rng(15)
+    X = (rng.standard_normal((20000, 12)) * np.logspace(0, -1.5, 12)) @ rng.standard_normal((12, 300))
+    X = (X + 1e-4 * rng.standard_normal(X.shape)).astype(np.float32)
+    r, q, seed = 24, 2, 99
+    U, S, V = P.math.randomized_svd(X, r, q, seed=seed)
+    assert U.dtype == np.float32 and U.shape == (20000, r) and V.shape == (r, 300)
+    omega = O.philox_uniform((300, r), seed, np.float32).astype(np.float64)
+    Ur, Sr, Vr = O.randomized_svd(X.astype(np.float64), r, q, omega=omega)
+    assert sigma_rel(S, Sr, 12) < 1e-5
+    assert subspace_angle(U[:, :12], Ur[:, :12]) < 1e-4
+    assert subspace_angle(V[:12].T, Vr[:12].T) < 1e-4
+    assert orthogonality(U) < 1e-5
+
+
 def test_randomized_reference_omega_subspace(golden):
     # pyLOM draws Omega with numpy's MT19937; ours is Philox.  Both capture the
     # same dominant subspace: compare sigma and subspaces, not raw vectors.
