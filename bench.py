@@ -277,6 +277,43 @@ def run_ours(args):
     info_words = L.last_info
     value = algorithmic_bytes(m, n) * world / (ms * 1e-3) / 1e9
 
+    # end to end through the public API with pinned host buffers
+    # (first, on a clean allocator: the timed loop's outputs released)
+    e2e = None
+    del U, S, V
+    if rank == 0 and not args.quick:
+        Yh = torch.empty((m, n), dtype=torch.float32, pin_memory=True)
+        Yh.copy_(Y)
+        torch.cuda.empty_cache()
+        steps = max(1, min(args.steps, 3))
+        # one untimed full-size call: page-locks the result blocks, which the
+        # pinned-memory cache then hands back to every later call
+        Uh, Sh, Vh = P.math.tsqr_svd(Yh)
+        del Uh, Sh, Vh
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(steps):
+            Uh, Sh, Vh = P.math.tsqr_svd(Yh)
+            del Uh, Sh, Vh
+        torch.cuda.synchronize()
+        te = (time.perf_counter() - t0) / steps
+        # the two copies alone (pinned host memory, same sizes)
+        t0 = time.perf_counter()
+        Xd = Yh.to("cuda")
+        torch.cuda.synchronize()
+        h2d_ms = (time.perf_counter() - t0) * 1e3
+        Uh = torch.empty((m, n), dtype=torch.float32, pin_memory=True)
+        t0 = time.perf_counter()
+        Uh.copy_(Xd)
+        torch.cuda.synchronize()
+        d2h_ms = (time.perf_counter() - t0) * 1e3
+        del Xd, Uh
+        e2e = {"value": algorithmic_bytes(m, n) / te / 1e9, "unit": "GB/s",
+               "h2d_bytes_per_step": int(4 * m * n),
+               "d2h_bytes_per_step": int(4 * m * n + 4 * n + 4 * n * n),
+               "ms_per_step": te * 1e3, "h2d_input_ms": h2d_ms, "d2h_u_ms": d2h_ms}
+        del Yh
+
     # accuracy of the mixed form against the FP64 form on a row sample: every
     # 8th point, so the sample spans the whole domain and keeps the 64 modes
     # distinct (a contiguous block of rows would be a thin strip of the grid)
@@ -316,33 +353,7 @@ def run_ours(args):
         fp64 = {"value": algorithmic_bytes(ms_rows, n) / (t64 * 1e-3) / 1e9, "unit": "GB/s",
                 "ms": t64, "rows": ms_rows,
                 "note": "plain FP64 GPU form on a row sample (throughput is linear in rows)"}
-        del U64, S64, V64, Um, Sm, Vm
-
-    # end to end through the public API with pinned host buffers
-    e2e = None
-    if rank == 0 and not args.quick:
-        del U, S, V
-        Yh = torch.empty((m, n), dtype=torch.float32, pin_memory=True)
-        Yh.copy_(Y)
-        del Y
-        torch.cuda.empty_cache()
-        steps = max(1, min(args.steps, 3))
-        # one untimed full-size call: page-locks the result blocks, which the
-        # pinned-memory cache then hands back to every later call
-        Uh, Sh, Vh = P.math.tsqr_svd(Yh)
-        del Uh, Sh, Vh
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        for _ in range(steps):
-            Uh, Sh, Vh = P.math.tsqr_svd(Yh)
-            del Uh, Sh, Vh
-        torch.cuda.synchronize()
-        te = (time.perf_counter() - t0) / steps
-        e2e = {"value": algorithmic_bytes(m, n) / te / 1e9, "unit": "GB/s",
-               "h2d_bytes_per_step": int(4 * m * n),
-               "d2h_bytes_per_step": int(4 * m * n + 4 * n + 4 * n * n),
-               "ms_per_step": te * 1e3}
-        del Yh
+        del U64, S64, V64, Um, Sm, Vm, Ys
 
     hbm, bf16, how = peaks()
     cpu = cpu_baseline() if (rank == 0 and not args.quick and world == 1) else None
@@ -369,7 +380,7 @@ def run_ours(args):
                 "config": {"workload": f"tsqr_svd {m}x{n} f32 (POD config 2, mean removed)",
                            "precision": "mixed", "l2": "inputs larger than L2 (32 GiB)",
                            "parallelism": "replicas" if world > 1 else "single"},
-                "clocks": clk.summary(), "gpu_launches": sum(k["count"] for k in kernels.values()) if kernels else None,
+                "clocks": clk.summary(), "gpu_launches": sum(k["launches"] for k in kernels.values()) if kernels else None,
                 "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "fp64_form": fp64,
                 "accuracy_vs_fp64": acc, "serving": serve, "kernels": kernels,
                 "info": {"cholesky_shift_escalations": info_words[1] if info_words else None,
@@ -436,7 +447,7 @@ def run_other(args):
     ms = e0.elapsed_time(e1) / args.steps
     kernels = prof.stop()
     out.update(value=nbytes / (ms * 1e-3) / 1e9, ms_per_step=ms, clocks=clk.summary(),
-               kernels=kernels, gpu_launches=sum(k["count"] for k in kernels.values()))
+               kernels=kernels, gpu_launches=sum(k["launches"] for k in kernels.values()))
     if args.workload == "dmd":
         mu = (res[0].double() + 1j * res[1].double()).cpu().numpy()
         true = np.concatenate([lam, np.conj(lam)])

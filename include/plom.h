@@ -61,8 +61,9 @@ int plom_version(void);
    counterpart of pyLOM's named timing channels (pyLOM/utils/cr.py:199-246
    cr_start/cr_stop, cr_info).  plom_profile_begin starts recording CUDA
    events around every kernel launch; plom_profile_end waits for them and
-   writes one line per kernel name: "name launches total_ms flops bytes"
-   (algorithmic flops/bytes of the launches). */
+   writes one line per timed region name: "name regions total_ms flops bytes
+   launches" (algorithmic flops/bytes of the regions; a region is one kernel
+   launch, or a routine's few launches timed together). */
 int plom_profile_begin(void);
 int plom_profile_end(char* buf, size_t cap);
 
@@ -116,6 +117,16 @@ int plom_tsqr_svd(int dtype, int prec, const void* X, int64_t m, int64_t n, int6
                   int64_t ldu, void* S, void* VT, void* ws, size_t ws_bytes, int* info,
                   void* stream);
 
+/* a batch of tsqr_svd problems of one shape (problem p at X + p xstride,
+   U + p ustride, S + p n, VT + p n n; strides in elements of dtype): the
+   per-frequency SVDs of SPOD (pyLOM/SPOD/wrapper.py:75-85 calls tsqr_svd once
+   per frequency).  The mixed form on F32/C64 data runs every stage as one
+   launch over the batch; the other forms run the problems one by one. */
+size_t plom_tsqr_svd_batched_workspace(int dtype, int prec, int64_t batch, int64_t m, int64_t n);
+int plom_tsqr_svd_batched(int dtype, int prec, const void* X, int64_t batch, int64_t m, int64_t n,
+                          int64_t ldx, int64_t xstride, void* U, int64_t ldu, int64_t ustride,
+                          void* S, void* VT, void* ws, size_t ws_bytes, int* info, void* stream);
+
 /* replaces srandomized_svd/drandomized_svd (svd.c:1198,1453; svd.py:255):
    U m x r, S r, VT r x n.  The test matrix Omega (n x r) is uniform [0,1)
    from a Philox4x32-10 counter stream keyed by seed (see plom_fill_uniform). */
@@ -152,6 +163,14 @@ int plom_dmd_reduced(const double* aux1, const double* S, const double* VT, int6
 int plom_spod_fft(int dtype, const void* Y, int64_t M, int64_t N, int64_t ldy, int64_t nDFT,
                   int64_t step, int64_t nBlks, int64_t nf, const void* window, const void* twr,
                   const void* twi, double scale, void* Q, void* stream);
+
+/* replaces the mode layout of SPOD.run (pyLOM/SPOD/wrapper.py:84,
+   P[:, ifreq] = real(U).reshape(M*nBlks, order='F')) for the G frequencies
+   f0 .. f0+G-1 of one batched SVD: P[(b*M + i)*nf + f0 + g] = Re U_g[i][b].
+   U: G problems of M x nBlks complex values (interleaved, dtype = the real
+   type), ustride complex elements apart; P: (M*nBlks) x nf, row-major. */
+int plom_spod_modes(int dtype, const void* U, int64_t G, int64_t M, int64_t nBlks,
+                    int64_t ustride, void* P, int64_t nf, int64_t f0, void* stream);
 
 /* ---- allocation-free reduction product ------------------------------- */
 /* No counterpart in the reference.  For callers that cannot allocate device

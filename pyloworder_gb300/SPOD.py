@@ -19,7 +19,7 @@ from . import vmmath as M
 
 __all__ = ["run"]
 
-SVD_STREAMS = 8  # concurrent per-frequency SVDs
+SVD_BATCH_MAX = 64  # frequencies per batched SVD
 
 
 def _window(name, n):
@@ -47,6 +47,21 @@ def spod_fft_device(Y, ldy, nDFT, nolap, nBlks, nf, win, scale):
     return Q
 
 
+def _svd_batch(Q, nBlks, precision):
+    """Frequencies per batched SVD: half of the free device memory (the
+    driver's free memory plus what torch's caching allocator holds unused)
+    over the per-frequency footprint (workspace + U), at most SVD_BATCH_MAX."""
+    t = L.torch()
+    nf, Mrows = Q.shape[0], Q.shape[1]
+    dt = L.dtype_code(Q)
+    prec = L.precision_code(precision, Q)
+    per = (L.load().plom_tsqr_svd_batched_workspace(dt, prec, 2, Mrows, nBlks)
+           - L.load().plom_tsqr_svd_batched_workspace(dt, prec, 1, Mrows, nBlks))
+    per = max(per, 1) + Q[0].numel() * Q.element_size()
+    free = t.cuda.mem_get_info()[0] + t.cuda.memory_reserved() - t.cuda.memory_allocated()
+    return int(max(1, min(nf, SVD_BATCH_MAX, (free // 2) // per)))
+
+
 def run_device(x, ld, t_host, nDFT=0, nolap=0, remove_mean=True, window="hamming", precision=None):
     t = L.torch()
     Mrows, N = x.shape
@@ -68,28 +83,22 @@ def run_device(x, ld, t_host, nDFT=0, nolap=0, remove_mean=True, window="hamming
     f = np.arange(np.ceil(nDFT / 2) + 1) / dt / nDFT
     nf = f.shape[0]
     Q = spod_fft_device(Y, ldy, nDFT, nolap, nBlks, nf, win, winWeight / nDFT / math.sqrt(nBlks))
+    del Y  # the Fourier coefficients are all the SVDs need
     Lm = t.empty((nf, nBlks), dtype=x.dtype, device="cuda")
     P = t.empty((Mrows * nBlks, nf), dtype=x.dtype, device="cuda")
-    P3 = P.view(nBlks, Mrows, nf)  # P[i + M*b, f] = Re U_f[i, b]
-    # the per-frequency SVDs are independent: round-robin over a few streams so
-    # that their small n x n stages (Cholesky, Jacobi) overlap
-    main = t.cuda.current_stream()
-    ready = t.cuda.Event()
-    ready.record(main)
-    streams = [t.cuda.Stream() for _ in range(min(SVD_STREAMS, nf))]
-    infos = []
-    for s in streams:
-        s.wait_event(ready)
-    for fi in range(nf):
-        with t.cuda.stream(streams[fi % len(streams)]):
-            U, S, _ = M.tsqr_svd_device(Q[fi], nBlks, precision, info_out=infos)
-            P3[:, :, fi] = U.real.transpose(0, 1)
-            Lm[fi] = (S * S).to(x.dtype)
-            del U, S
-    for s in streams:
-        main.wait_stream(s)
-    for info in infos:
-        L.check_info(info, "SPOD tsqr_svd")
+    # P[i + M*b, f] = Re U_f[i, b]
+    # the per-frequency SVDs run as batches of frequencies (one launch per
+    # stage for the whole batch), as many per batch as device memory allows
+    group = _svd_batch(Q, nBlks, precision)
+    # the mode-layout kernel stages group x nBlks real parts per point
+    group = max(1, min(group, (48 * 1024) // (x.element_size() * (nBlks | 1))))
+    for f0 in range(0, nf, group):
+        f1 = min(nf, f0 + group)
+        U, S, _ = M.tsqr_svd_batched_device(Q[f0:f1], precision)
+        L.call("plom_spod_modes", L.dtype_code(P), L.ptr(U), f1 - f0, Mrows, nBlks,
+               U.stride(0) if f1 - f0 > 1 else Mrows * nBlks, L.ptr(P), nf, f0, L.stream_ptr())
+        Lm[f0:f1] = (S * S).to(x.dtype)
+        del U, S
     order = np.argsort(Lm[:, 0].cpu().numpy())[::-1].copy()
     od = t.as_tensor(order, device="cuda")
     return Lm.index_select(0, od), P.index_select(1, od), f[order]

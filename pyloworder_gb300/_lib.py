@@ -53,6 +53,10 @@ PROTOS = {
     "plom_tsqr_svd_workspace": (c_sz, [c_int, c_int, c_i64, c_i64]),
     "plom_tsqr_svd": (c_int, [c_int, c_int, c_vp, c_i64, c_i64, c_i64, c_vp, c_i64, c_vp, c_vp, c_vp,
                               c_sz, c_vp, c_vp]),
+    "plom_spod_modes": (c_int, [c_int, c_vp, c_i64, c_i64, c_i64, c_i64, c_vp, c_i64, c_i64, c_vp]),
+    "plom_tsqr_svd_batched_workspace": (c_sz, [c_int, c_int, c_i64, c_i64, c_i64]),
+    "plom_tsqr_svd_batched": (c_int, [c_int, c_int, c_vp, c_i64, c_i64, c_i64, c_i64, c_i64, c_vp,
+                                      c_i64, c_i64, c_vp, c_vp, c_vp, c_sz, c_vp, c_vp]),
     "plom_randomized_svd_workspace": (c_sz, [c_int, c_int, c_i64, c_i64, c_i64]),
     "plom_randomized_svd": (c_int, [c_int, c_int, c_vp, c_i64, c_i64, c_i64, c_i64, c_int,
                                     ctypes.c_uint64, c_vp, c_i64, c_vp, c_vp, c_vp, c_sz, c_vp,
@@ -239,9 +243,9 @@ class Profiler:
         call("plom_profile_end", buf, len(buf))
         out = {}
         for line in buf.value.decode().splitlines():
-            name, cnt, ms, fl, by = line.split()
+            name, cnt, ms, fl, by, nl = line.split()
             out[name] = {"name": name, "count": int(cnt), "ms_total": float(ms),
-                         "flops": float(fl), "bytes": float(by)}
+                         "flops": float(fl), "bytes": float(by), "launches": int(nl)}
         return out
 
 

@@ -42,7 +42,7 @@ extern "C" int plom_profile_end(char* buf, size_t cap) {
     return PLOM_OK;
   }
   struct Agg {
-    int count = 0;
+    int count = 0, launches = 0;
     double ms = 0, flops = 0, bytes = 0;
   };
   std::map<std::string, Agg> agg;
@@ -53,6 +53,7 @@ extern "C" int plom_profile_end(char* buf, size_t cap) {
       status = PLOM_ERR_CUDA;
     Agg& a = agg[e.name];
     a.count += 1;
+    a.launches += e.launches;
     a.ms += ms;
     a.flops += e.flops;
     a.bytes += e.bytes;
@@ -64,8 +65,8 @@ extern "C" int plom_profile_end(char* buf, size_t cap) {
   std::string out;
   char line[256];
   for (auto& kv : agg) {
-    snprintf(line, sizeof(line), "%s %d %.6f %.6e %.6e\n", kv.first.c_str(), kv.second.count,
-             kv.second.ms, kv.second.flops, kv.second.bytes);
+    snprintf(line, sizeof(line), "%s %d %.6f %.6e %.6e %d\n", kv.first.c_str(), kv.second.count,
+             kv.second.ms, kv.second.flops, kv.second.bytes, kv.second.launches);
     out += line;
   }
   if (buf && cap) {

@@ -48,6 +48,7 @@ __global__ void __launch_bounds__(256) chol_coop_kernel(const double* __restrict
   cg::grid_group grid = cg::this_grid();
   __shared__ double S[NB][NB + 1];
   __shared__ double P[NB][NB + 1];
+  __shared__ double rpiv;
   __shared__ int sflag;
   const int tid = threadIdx.x;
   const int T = (n + NB - 1) / NB;
@@ -87,13 +88,17 @@ __global__ void __launch_bounds__(256) chol_coop_kernel(const double* __restrict
     grid.sync();
     for (int k = 0; k < T; ++k) {
       const int k0 = k * NB, nbk = min(NB, n - k0);
-      // (1) diagonal block: factor + invert, one CTA per problem
+      // (1) diagonal block, one CTA per problem: the factor and Z = R_kk^-T
+      // row by row in the same steps (forward substitution of R^T Z = I):
+      //   piv = sqrt(S_jj), R_j. = S_j. / piv, Z_j. = P_j. / piv,
+      //   S_ac -= R_ja R_jc (j < a <= c),  P_a. -= R_ja Z_j. (a > j),  P = I at start
       for (int b = blockIdx.x; b < batch; b += gridDim.x) {
         if (stt.status[b] != 0) continue;
         double* Rb = R + b * nn;
         for (int e = tid; e < NB * NB; e += blockDim.x) {
           int i = e / NB, j = e % NB;
           S[i][j] = (i < nbk && j < nbk) ? Rb[(int64_t)(k0 + i) * n + k0 + j] : 0.0;
+          P[i][j] = (i == j) ? 1.0 : 0.0;
         }
         __syncthreads();
         for (int j = 0; j < nbk; ++j) {
@@ -101,17 +106,29 @@ __global__ void __launch_bounds__(256) chol_coop_kernel(const double* __restrict
             double d = S[j][j];
             bool ok = (d > 0.0) && isfinite(d);
             sflag = ok ? 1 : 0;
-            S[j][j] = ok ? sqrt(d) : 1.0;
+            const double piv = ok ? sqrt(d) : 1.0;
+            S[j][j] = piv;
+            rpiv = 1.0 / piv;
           }
           __syncthreads();
           if (!sflag) break;
-          const double piv = S[j][j];
-          for (int i = j + 1 + tid; i < nbk; i += blockDim.x) S[j][i] /= piv;
+          const double rp = rpiv;
+          for (int i = tid; i < nbk; i += blockDim.x) {
+            if (i > j) S[j][i] *= rp;
+            else P[j][i] *= rp;
+          }
           __syncthreads();
           const int w = nbk - j - 1;
-          for (int e = tid; e < w * w; e += blockDim.x) {
-            int a = j + 1 + e / w, c = j + 1 + e % w;
-            if (a <= c) S[a][c] -= S[j][a] * S[j][c];
+          const int ns = w * w, np = w * (j + 1);
+          for (int e = tid; e < ns + np; e += blockDim.x) {
+            if (e < ns) {
+              const int a = j + 1 + e / w, c = j + 1 + e % w;
+              if (a <= c) S[a][c] -= S[j][a] * S[j][c];
+            } else {
+              const int e2 = e - ns;
+              const int a = j + 1 + e2 / (j + 1), q = e2 % (j + 1);
+              P[a][q] -= S[j][a] * P[j][q];
+            }
           }
           __syncthreads();
         }
@@ -125,20 +142,11 @@ __global__ void __launch_bounds__(256) chol_coop_kernel(const double* __restrict
           int i = e / nbk, j = e % nbk;
           Rb[(int64_t)(k0 + i) * n + k0 + j] = (i <= j) ? S[i][j] : 0.0;
         }
-        // inverse of the upper triangular block: thread c -> column c
+        // R_kk^-1 = Z^T
         double* Db = Dinv + (int64_t)b * NB * NB;
-        if (tid < nbk) {
-          const int c = tid;
-          double x[NB];
-#pragma unroll
-          for (int i = 0; i < NB; ++i) x[i] = 0.0;
-          x[c] = 1.0 / S[c][c];
-          for (int i = c - 1; i >= 0; --i) {
-            double acc = 0.0;
-            for (int t = i + 1; t <= c; ++t) acc += S[i][t] * x[t];
-            x[i] = -acc / S[i][i];
-          }
-          for (int i = 0; i < NB; ++i) Db[i * NB + c] = (i <= c) ? x[i] : 0.0;
+        for (int e = tid; e < NB * NB; e += blockDim.x) {
+          int i = e / NB, c = e % NB;
+          Db[e] = (i <= c && c < nbk) ? P[c][i] : 0.0;
         }
         __syncthreads();
       }
@@ -259,56 +267,39 @@ int chol_shifted(const double* G, double* R, int n, int batch, double rel0, doub
 }
 
 // ---------------------------------------------------------------------------
-// triangular inverse: W = R^{-1}, R upper (batch).  One CTA per column
-// (column-oriented back substitution on R^T rows, one barrier per step).
+// triangular inverse: W = R^{-1}, R upper (batch), by recursive halving:
+//   [A B; 0 C]^{-1} = [A^{-1}, -A^{-1} (B C^{-1}); 0, C^{-1}]
+// The 32 x 32 diagonal blocks are inverted first (one warp each, back
+// substitution per column); each level s = 32, 64, ... then joins the pairs
+// of s x s inverses along the diagonal with two batched products that skip
+// the triangular zero bands (n^3/6 FMAs in all, spread over every SM).
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(1024) trtri_col_kernel(const double* __restrict__ Rt,
-                                                         double* __restrict__ W, int n,
-                                                         int batch) {
-  __shared__ double wk[2];
-  const int tid = threadIdx.x;
+__global__ void __launch_bounds__(32) trtri_leaf_kernel(const double* __restrict__ R,
+                                                        double* __restrict__ W, int n) {
+  __shared__ double S[32][33];
+  __shared__ double X[32][33];
+  __shared__ double dinv[32];
   const int64_t nn = (int64_t)n * n;
-  constexpr int PER = 4;  // rows per thread: n <= 4 * blockDim
-  for (int64_t task = blockIdx.x; task < (int64_t)n * batch; task += gridDim.x) {
-    const int64_t b = task / n;
-    const int j = (int)(task % n);
-    const double* Rb = Rt + b * nn;  // Rb[k*n + i] = R[i][k]
-    double w[PER];
-#pragma unroll
-    for (int p = 0; p < PER; ++p) {
-      int i = tid + p * blockDim.x;
-      w[p] = (i == j) ? 1.0 : 0.0;
-    }
-    for (int k = j; k >= 0; --k) {
-      const int owner = k % blockDim.x, slot = k / blockDim.x;
-      if (tid == owner) {
-        double v = 0.0;
-#pragma unroll
-        for (int p = 0; p < PER; ++p)
-          if (p == slot) v = w[p] / Rb[(int64_t)k * n + k];
-#pragma unroll
-        for (int p = 0; p < PER; ++p)
-          if (p == slot) w[p] = v;
-        wk[k & 1] = v;
-      }
-      __syncthreads();
-      const double x = wk[k & 1];
-      const double* col = Rb + (int64_t)k * n;
-#pragma unroll
-      for (int p = 0; p < PER; ++p) {
-        int i = tid + p * blockDim.x;
-        if (i < k) w[p] -= col[i] * x;
-      }
-    }
-    __syncthreads();
-    double* Wb = W + b * nn;
-#pragma unroll
-    for (int p = 0; p < PER; ++p) {
-      int i = tid + p * blockDim.x;
-      if (i < n) Wb[(int64_t)i * n + j] = (i <= j) ? w[p] : 0.0;
-    }
-    __syncthreads();
+  const double* Rb = R + (int64_t)blockIdx.y * nn;
+  double* Wb = W + (int64_t)blockIdx.y * nn;
+  const int j0 = blockIdx.x * 32, nb = min(32, n - j0);
+  const int c = threadIdx.x;
+  for (int i = 0; i < 32; ++i) {
+    S[i][c] = (i < nb && c < nb) ? Rb[(int64_t)(j0 + i) * n + j0 + c] : (i == c ? 1.0 : 0.0);
+    X[i][c] = 0.0;
   }
+  __syncwarp();
+  dinv[c] = 1.0 / S[c][c];
+  __syncwarp();
+  X[c][c] = dinv[c];
+  for (int i = c - 1; i >= 0; --i) {
+    double acc = 0.0;
+    for (int t = i + 1; t <= c; ++t) acc = fma(S[i][t], X[t][c], acc);
+    X[i][c] = -acc * dinv[i];
+  }
+  __syncwarp();
+  if (c < nb)
+    for (int i = 0; i < nb; ++i) Wb[(int64_t)(j0 + i) * n + j0 + c] = X[i][c];
 }
 
 __global__ void transpose_f64_kernel(const double* __restrict__ in, double* __restrict__ out,
@@ -341,19 +332,38 @@ int transpose_f64(const double* in, double* out, int64_t rows, int64_t cols, int
 }
 
 int trtri_upper(const double* R, double* W, int n, int batch, Arena& ws, cudaStream_t st) {
-  double* Rt = ws.take<double>((size_t)n * n * batch);
+  double* T = ws.take<double>((size_t)n * n * batch);  // B C^{-1} blocks
   if (ws.measuring() || n == 0 || batch == 0) return PLOM_OK;
   PLOM_REQUIRE(!ws.overflow(), PLOM_ERR_WORKSPACE, "trtri: workspace too small");
   PLOM_REQUIRE(R && W, PLOM_ERR_ARG, "trtri: null pointer");
-  PLOM_REQUIRE(n <= 4096, PLOM_ERR_UNSUPPORTED, "trtri: n > 4096");
-  PLOM_TRY(transpose_f64(R, Rt, n, n, batch, st));
-  int threads = std::min(1024, std::max(32, (int)cdiv(n, 4 * 32) * 32));
-  while ((int64_t)threads * 4 < n) threads += 32;
-  int64_t tasks = (int64_t)n * batch;
-  int blocks = (int)std::min<int64_t>(tasks, (int64_t)num_sms() * 2);
-  ProfScope prof("trtri_fp64", st, (double)n * n * n / 3.0 * batch, 16.0 * n * n * batch);
-  trtri_col_kernel<<<blocks, threads, 0, st>>>(Rt, W, n, batch);
+  PLOM_REQUIRE(batch <= 65535, PLOM_ERR_ARG, "trtri: batch too large");
+  const int64_t nn = (int64_t)n * n;
+  int launches = 1;
+  for (int s = 32; s < n; s *= 2) launches += 2 * ((n / (2 * s) > 0) + (2 * (n / (2 * s)) * s + s < n));
+  ProfScope prof("trtri_fp64", st, (double)n * n * n / 3.0 * batch, 16.0 * n * n * batch, launches);
+  PLOM_CHECK_CUDA(cudaMemsetAsync(W, 0, sizeof(double) * nn * batch, st));
+  trtri_leaf_kernel<<<dim3((unsigned)cdiv(n, 32), (unsigned)batch), 32, 0, st>>>(R, W, n);
   PLOM_CHECK_LAUNCH();
+  for (int s = 32; s < n; s *= 2) {
+    // sub-block t: rows [2ts, 2ts + s) hold A^{-1}, columns [2ts + s, 2ts + 2s) C^{-1}
+    const int64_t step = 2 * (int64_t)s * (n + 1);
+    const int nfull = n / (2 * s);
+    const int tail_c0 = 2 * nfull * s + s;  // a last, narrower sub-block
+    for (int part = 0; part < 2; ++part) {
+      const int nsub = part == 0 ? nfull : (tail_c0 < n ? 1 : 0);
+      if (nsub == 0) continue;
+      const int64_t off = part == 0 ? 0 : (int64_t)nfull * step;
+      const int cols = part == 0 ? s : n - tail_c0;
+      const int64_t ab = off + s;                  // row r0, column c0 = r0 + s
+      const int64_t cc = off + (int64_t)s * n + s; // C^{-1} at (c0, c0)
+      // T = B C^{-1}
+      PLOM_TRY(gemm_sq(R + ab, n, nn, step, W + cc, n, nn, step, T + ab, n, nn, step, s, cols,
+                       cols, batch, nsub, 1.0, 2, st, nullptr));
+      // W12 = -A^{-1} T
+      PLOM_TRY(gemm_sq(W + off, n, nn, step, T + ab, n, nn, step, W + ab, n, nn, step, s, cols, s,
+                       batch, nsub, -1.0, 1, st, nullptr));
+    }
+  }
   return PLOM_OK;
 }
 

@@ -203,8 +203,11 @@ __device__ __forceinline__ uint16_t ld_shared_u16(uint32_t addr) {
 // each block takes a contiguous range of rows, threads take 4-column groups
 // (16-byte loads when rows are aligned)
 __global__ void __launch_bounds__(256) colmax_kernel(const float* __restrict__ Y, int64_t ld,
-                                                     int64_t m, int N, int vec,
+                                                     int64_t m, int N, int vec, int64_t bstride,
                                                      unsigned* __restrict__ cmax) {
+  // problem blockIdx.y of a batch (matrices bstride elements apart)
+  Y += (int64_t)blockIdx.y * bstride;
+  cmax += (int64_t)blockIdx.y * N;
   const int64_t rows = (m + gridDim.x - 1) / gridDim.x;
   const int64_t r0 = (int64_t)blockIdx.x * rows;
   const int64_t r1 = (r0 + rows < m) ? r0 + rows : m;
@@ -238,19 +241,23 @@ __global__ void __launch_bounds__(256) colmax_kernel(const float* __restrict__ Y
 
 // s_j = 2^(14 - e_j) with max_j = f 2^e_j, f in [0.5, 1); 1 for zero or
 // padding columns (clamped so that s_j stays a finite float)
-__global__ void colscale_kernel(const unsigned* __restrict__ cmax, int N, int ldp,
+__global__ void colscale_kernel(const unsigned* __restrict__ cmax, int N, int ldp, int batch,
                                 float* __restrict__ s) {
-  for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < ldp; j += gridDim.x * blockDim.x) {
-    const float v = (j < N) ? __uint_as_float(cmax[j]) : 0.f;
-    int e = 0;
-    frexpf(v, &e);
-    e = e < -100 ? -100 : e;
-    s[j] = (v > 0.f) ? ldexpf(1.f, PK_LOG2 - e) : 1.f;
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < (int64_t)batch * ldp;
+       e += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t pb = e / ldp;
+    const int j = (int)(e - pb * ldp);
+    const float v = (j < N) ? __uint_as_float(cmax[pb * N + j]) : 0.f;
+    int ex = 0;
+    frexpf(v, &ex);
+    ex = ex < -100 ? -100 : ex;
+    s[e] = (v > 0.f) ? ldexpf(1.f, PK_LOG2 - ex) : 1.f;
   }
 }
 
-__global__ void fill_scale_kernel(float* __restrict__ s, int ldp, float v) {
-  for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < ldp; j += gridDim.x * blockDim.x)
+__global__ void fill_scale_kernel(float* __restrict__ s, int64_t count, float v) {
+  for (int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; j < count;
+       j += (int64_t)gridDim.x * blockDim.x)
     s[j] = v;
 }
 
@@ -268,26 +275,35 @@ __device__ __forceinline__ void split8(const float (&v)[8], uint4& h, uint4& l) 
   l = make_uint4(lw[0], lw[1], lw[2], lw[3]);
 }
 
-// hi/lo planes (m x ldp) of Y diag(s); columns N..ldp-1 are zero.  Blocks
-// take tiles of `rt` rows; threads take 8-column groups of a tile.
+// hi/lo planes (mp x ldp per problem) of Y diag(s); columns N..ldp-1 and
+// rows m..mp-1 are zero.  Blocks take tiles of `rt` rows of one problem;
+// threads take 8-column groups of a tile.
 __global__ void __launch_bounds__(256) pack_kernel(const float* __restrict__ Y, int64_t ld,
                                                    int64_t m, int N, int ldp, int rt,
                                                    const float* __restrict__ s,
                                                    __half* __restrict__ hi,
-                                                   __half* __restrict__ lo, int vec) {
+                                                   __half* __restrict__ lo, int vec,
+                                                   int64_t bstride, int64_t mp, int batch) {
   const int groups = ldp / 8;
-  for (int64_t tile = blockIdx.x; tile * rt < m; tile += gridDim.x) {
-    const int64_t r0 = tile * rt;
-    const int nr = (int)((m - r0 < rt) ? m - r0 : rt);
+  const int64_t tpp = (mp + rt - 1) / rt;  // tiles per problem
+  for (int64_t tile = blockIdx.x; tile < tpp * batch; tile += gridDim.x) {
+    const int64_t pb = tile / tpp;
+    const int64_t r0 = (tile - pb * tpp) * rt;
+    const int nr = (int)((mp - r0 < rt) ? mp - r0 : rt);
     const int items = nr * groups;
+    const float* Yp = Y + pb * bstride;
+    const float* sp = s + pb * ldp;
 #pragma unroll 2
     for (int idx = threadIdx.x; idx < items; idx += blockDim.x) {
       const int rr = idx / groups;
       const int c0 = (idx - rr * groups) * 8;
       const int64_t r = r0 + rr;
-      const float* src = Y + r * ld + c0;
+      const float* src = Yp + r * ld + c0;
       float v[8];
-      if (vec && c0 + 8 <= N) {
+      if (r >= m) {
+#pragma unroll
+        for (int q = 0; q < 8; ++q) v[q] = 0.f;
+      } else if (vec && c0 + 8 <= N) {
         const float4 a = __ldg(reinterpret_cast<const float4*>(src));
         const float4 b = __ldg(reinterpret_cast<const float4*>(src + 4));
         v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w;
@@ -296,14 +312,15 @@ __global__ void __launch_bounds__(256) pack_kernel(const float* __restrict__ Y, 
 #pragma unroll
         for (int q = 0; q < 8; ++q) v[q] = (c0 + q < N) ? src[q] : 0.f;
       }
-      const float4 s0 = __ldg(reinterpret_cast<const float4*>(s + c0));
-      const float4 s1 = __ldg(reinterpret_cast<const float4*>(s + c0 + 4));
+      const float4 s0 = __ldg(reinterpret_cast<const float4*>(sp + c0));
+      const float4 s1 = __ldg(reinterpret_cast<const float4*>(sp + c0 + 4));
       v[0] *= s0.x; v[1] *= s0.y; v[2] *= s0.z; v[3] *= s0.w;
       v[4] *= s1.x; v[5] *= s1.y; v[6] *= s1.z; v[7] *= s1.w;
       uint4 h, l;
       split8(v, h, l);
-      *reinterpret_cast<uint4*>(hi + r * ldp + c0) = h;
-      *reinterpret_cast<uint4*>(lo + r * ldp + c0) = l;
+      const int64_t ro = pb * mp + r;
+      *reinterpret_cast<uint4*>(hi + ro * ldp + c0) = h;
+      *reinterpret_cast<uint4*>(lo + ro * ldp + c0) = l;
     }
   }
 }
@@ -317,8 +334,18 @@ __global__ void __launch_bounds__(256) split_w16_kernel(const double* __restrict
                                                         const float* __restrict__ s_in,
                                                         float out_scale, __half* __restrict__ bhi,
                                                         __half* __restrict__ blo,
-                                                        float* __restrict__ f) {
+                                                        float* __restrict__ f, int64_t wstride,
+                                                        int fstride) {
   __shared__ double red[8];
+  // problem blockIdx.y of a batch: W_p, its input scales, its rows of Bt, its factors
+  {
+    const int64_t pb = blockIdx.y;
+    W += pb * wstride;
+    s_in += pb * ldk;
+    bhi += pb * k * (int64_t)ldk;
+    blo += pb * k * (int64_t)ldk;
+    f += pb * fstride;
+  }
   const int j = blockIdx.x;
   if (j >= k) {
     if (threadIdx.x == 0) f[j] = 0.f;
@@ -375,7 +402,7 @@ template <bool SYM>
 __global__ void __launch_bounds__(320, 1)
     gram16_kernel(const __grid_constant__ CUtensorMap tmP, const __grid_constant__ CUtensorMap tmB,
                   int64_t m, int tn, int tnb, int64_t rows_per_chunk, int chunks,
-                  double* __restrict__ part, int* err) {
+                  double* __restrict__ part, int* err, int64_t mp) {
   extern __shared__ uint8_t smem_raw[];
   __shared__ uint64_t full_bar[G_STAGES], empty_bar[G_STAGES];
   __shared__ uint64_t tfull[2], tempty[2], dfull[2];
@@ -386,9 +413,14 @@ __global__ void __launch_bounds__(320, 1)
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   // consecutive CTAs take different tiles of the same row chunk, so the CTAs
   // resident together read the same rows and share them through L2
+  // work item -> (problem of the batch, row chunk, tile); the problems' rows
+  // are mp apart in the planes
   const int ntiles = SYM ? tn * (tn + 1) / 2 : tn * tnb;
-  const int chunk = (int)(blockIdx.x / ntiles), tile = (int)(blockIdx.x % ntiles);
-  const int item = tile * chunks + chunk;  // partial slab index (tile-major)
+  const int per_problem = ntiles * chunks;
+  const int pb = (int)(blockIdx.x / per_problem);
+  const int rem_item = (int)(blockIdx.x % per_problem);
+  const int chunk = rem_item / ntiles, tile = rem_item % ntiles;
+  const int item = (pb * ntiles + tile) * chunks + chunk;  // partial slab index (tile-major)
   int ti = 0, tj = 0;
   if (SYM) {
     int rem = tile;
@@ -447,7 +479,7 @@ __global__ void __launch_bounds__(320, 1)
         const uint32_t ph = (uint32_t)(kb / G_STAGES) & 1u;
         if (!mbar_wait(&empty_bar[s], ph ^ 1u, &abort_sh, err)) break;
         const uint32_t st = base + s * G_STAGE;
-        const int y = (int)(r_beg + (int64_t)kb * G_BK);
+        const int y = (int)((int64_t)pb * mp + r_beg + (int64_t)kb * G_BK);
         mbar_expect_tx(&full_bar[s], bytes);
 #pragma unroll
         for (int z = 0; z < 2; ++z) {
@@ -608,11 +640,15 @@ __global__ void tn16_reduce_kernel(const double* __restrict__ part, int Na, int 
 
 // G[i][j] = sum over chunks of the tile partials (fixed order) / (s_i s_j), mirrored
 __global__ void gram16_reduce_kernel(const double* __restrict__ part, int N, int tn, int chunks,
-                                     const float* __restrict__ s, double* __restrict__ G) {
-  const int64_t total = (int64_t)N * N;
+                                     const float* __restrict__ s, double* __restrict__ G,
+                                     int batch, int ld) {
+  const int64_t total = (int64_t)N * N * batch;
+  const int ntiles = tn * (tn + 1) / 2;
   for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < total;
        e += (int64_t)gridDim.x * blockDim.x) {
-    const int i = (int)(e / N), j = (int)(e % N);
+    const int64_t pb = e / ((int64_t)N * N);
+    const int64_t r = e - pb * N * N;
+    const int i = (int)(r / N), j = (int)(r % N);
     int a = i, b = j;
     if (a / 128 > b / 128) {
       a = j;
@@ -620,11 +656,12 @@ __global__ void gram16_reduce_kernel(const double* __restrict__ part, int N, int
     }
     const int ti = a / 128, tj = b / 128;
     const int tile = ti * tn - ti * (ti - 1) / 2 + (tj - ti);
-    const double* p = part + ((int64_t)tile * chunks) * 128 * 128 + (int64_t)(a - ti * 128) * 128 +
-                      (b - tj * 128);
+    const double* p = part + ((pb * ntiles + tile) * chunks) * 128 * 128 +
+                      (int64_t)(a - ti * 128) * 128 + (b - tj * 128);
     double acc = 0.0;
     for (int c = 0; c < chunks; ++c) acc += p[(int64_t)c * 128 * 128];
-    G[e] = acc / ((double)s[i] * (double)s[j]);
+    const float* sp = s + pb * ld;
+    G[e] = acc / ((double)sp[i] * (double)sp[j]);
   }
 }
 
@@ -635,11 +672,13 @@ constexpr int A_BK = 64;                       // K per stage (one 128-byte row)
 constexpr uint32_t A_TILE = 128 * 128;         // 128 rows x 64 fp16 (16 KB)
 constexpr uint32_t A_STAGE = 4 * A_TILE;       // A hi, A lo, B hi, B lo
 constexpr int A_STAGES = 3;
-constexpr size_t A_SMEM = (size_t)A_STAGES * A_STAGE + 1024;
+constexpr uint32_t A_STG = 4 * 4096;           // epilogue staging: 32 rows x 128 bytes per warp
+constexpr size_t A_SMEM = (size_t)A_STAGES * A_STAGE + A_STG + 1024;
 
 struct ApplyOut {
   float* C;        // FP32 output (m x k, ldc) or nullptr
   int64_t ldc;
+  int64_t cstride; // elements between the problems' C (batch)
   __half* ohi;     // packed output planes (m x ldo) or nullptr
   __half* olo;
   int ldo;
@@ -648,13 +687,27 @@ struct ApplyOut {
 __global__ void __launch_bounds__(192, 1)
     apply16_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
                    int64_t m, int kblocks, int k, int64_t col_tiles, int64_t tiles,
-                   const float* __restrict__ f, ApplyOut out, int* err) {
+                   const float* __restrict__ f, ApplyOut out, int* err, int64_t mp,
+                   int64_t row_tiles, int fstride, int upper) {
+  // tile t -> (problem pb, row block rb, column block cb); a problem's rows are
+  // mp apart in the packed planes (input and packed output alike).  CTA x takes
+  // tile r G + x in even rounds r and r G + (G - 1 - x) in odd ones, so with
+  // an upper-triangular W (upper != 0: column block cb needs only the first
+  // (cb + 1) 128 rows of W, the K blocks below 2 (cb + 1)) the long and short
+  // column blocks alternate on every CTA.
   extern __shared__ uint8_t smem_raw[];
   __shared__ uint64_t full_bar[A_STAGES], empty_bar[A_STAGES], tfull[2], tempty[2];
   __shared__ uint32_t tmem_sh;
   __shared__ int abort_sh;
   const uint32_t base = (smem_u32(smem_raw) + 1023u) & ~1023u;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int64_t G = gridDim.x;
+  auto apply_tile = [&](int64_t r) -> int64_t {
+    return r * G + ((r & 1) ? G - 1 - blockIdx.x : (int64_t)blockIdx.x);
+  };
+  auto apply_kend = [&](int cb) -> int {
+    return upper ? min(kblocks, (cb + 1) * (128 / A_BK)) : kblocks;
+  };
   if (launch_aborted(err)) return;
 
   if (threadIdx.x == 0) {
@@ -687,9 +740,15 @@ __global__ void __launch_bounds__(192, 1)
     if (lane == 0) {
       int64_t g = 0;
       bool ok = true;
-      for (int64_t t = blockIdx.x; t < tiles && ok; t += gridDim.x) {
-        const int rb = (int)(t / col_tiles), cb = (int)(t % col_tiles);
-        for (int kb = 0; kb < kblocks; ++kb, ++g) {
+      for (int64_t r = 0; r * gridDim.x < tiles && ok; ++r) {
+        const int64_t t = apply_tile(r);
+        if (t >= tiles) continue;
+        const int64_t pb = t / (row_tiles * col_tiles);
+        const int64_t rt = t - pb * row_tiles * col_tiles;
+        const int rb = (int)(rt / col_tiles), cb = (int)(rt % col_tiles);
+        const int ya = (int)(pb * mp + (int64_t)rb * 128), yb = (int)(pb * k + (int64_t)cb * 128);
+        const int kend = apply_kend(cb);
+        for (int kb = 0; kb < kend; ++kb, ++g) {
           const int s = (int)(g % A_STAGES);
           const uint32_t ph = (uint32_t)(g / A_STAGES) & 1u;
           if (!mbar_wait(&empty_bar[s], ph ^ 1u, &abort_sh, err)) {
@@ -698,10 +757,10 @@ __global__ void __launch_bounds__(192, 1)
           }
           const uint32_t st = base + s * A_STAGE;
           mbar_expect_tx(&full_bar[s], A_STAGE);
-          tma_load_3d(st, &tmA, kb * A_BK, rb * 128, 0, &full_bar[s]);
-          tma_load_3d(st + A_TILE, &tmA, kb * A_BK, rb * 128, 1, &full_bar[s]);
-          tma_load_3d(st + 2 * A_TILE, &tmB, kb * A_BK, cb * 128, 0, &full_bar[s]);
-          tma_load_3d(st + 3 * A_TILE, &tmB, kb * A_BK, cb * 128, 1, &full_bar[s]);
+          tma_load_3d(st, &tmA, kb * A_BK, ya, 0, &full_bar[s]);
+          tma_load_3d(st + A_TILE, &tmA, kb * A_BK, ya, 1, &full_bar[s]);
+          tma_load_3d(st + 2 * A_TILE, &tmB, kb * A_BK, yb, 0, &full_bar[s]);
+          tma_load_3d(st + 3 * A_TILE, &tmB, kb * A_BK, yb, 1, &full_bar[s]);
         }
       }
     }
@@ -712,7 +771,9 @@ __global__ void __launch_bounds__(192, 1)
       int64_t g = 0;
       int i = 0;
       bool ok = true;
-      for (int64_t t = blockIdx.x; t < tiles && ok; t += gridDim.x, ++i) {
+      for (int64_t r = 0; r * gridDim.x < tiles && ok; ++r) {
+        const int64_t t = apply_tile(r);
+        if (t >= tiles) continue;
         const int b = i & 1;
         if (!mbar_wait(&tempty[b], (((uint32_t)i >> 1) & 1u) ^ 1u, &abort_sh, err)) {
           ok = false;
@@ -721,7 +782,8 @@ __global__ void __launch_bounds__(192, 1)
         fence_after();
         const uint32_t dmain = tmem + (uint32_t)(b * 256);
         const uint32_t dcorr = dmain + 128u;
-        for (int kb = 0; kb < kblocks; ++kb, ++g) {
+        const int kend = apply_kend((int)(t % col_tiles));
+        for (int kb = 0; kb < kend; ++kb, ++g) {
           const int s = (int)(g % A_STAGES);
           const uint32_t ph = (uint32_t)(g / A_STAGES) & 1u;
           if (!mbar_wait(&full_bar[s], ph, &abort_sh, err)) {
@@ -745,19 +807,29 @@ __global__ void __launch_bounds__(192, 1)
           mma_commit(&empty_bar[s]);
         }
         if (ok) mma_commit(&tfull[b]);
+        ++i;
       }
     }
   } else {
     // ---- epilogue (warps 0-3): TMEM -> scale -> FP32 or packed store
+    uint4* stg = reinterpret_cast<uint4*>(smem_raw + (base - smem_u32(smem_raw)) +
+                                          A_STAGES * A_STAGE + warp * 4096);
     int i = 0;
-    for (int64_t t = blockIdx.x; t < tiles; t += gridDim.x, ++i) {
+    for (int64_t r = 0; r * gridDim.x < tiles; ++r) {
+      const int64_t t = apply_tile(r);
+      if (t >= tiles) continue;
       const int b = i & 1;
       const bool ready = mbar_wait(&tfull[b], ((uint32_t)i >> 1) & 1u, &abort_sh, err);
       __syncwarp();
       if (!__all_sync(0xffffffffu, ready)) break;
       fence_after();
-      const int64_t rb = t / col_tiles, cb = t % col_tiles;
-      const int64_t row = rb * 128 + warp * 32 + lane;
+      const int64_t pb = t / (row_tiles * col_tiles);
+      const int64_t rt = t - pb * row_tiles * col_tiles;
+      const int64_t rb = rt / col_tiles, cb = rt % col_tiles;
+      const int64_t row0 = rb * 128 + warp * 32;  // first row of this warp (within the problem)
+      const float* fp = f + pb * fstride;
+      const bool c_vec = out.C && ((out.ldc & 3) == 0) && ((out.cstride & 3) == 0) &&
+                         ((reinterpret_cast<uintptr_t>(out.C) & 15) == 0);
 #pragma unroll 1
       for (int cc = 0; cc < 4; ++cc) {
         uint32_t rm[32], rc[32];
@@ -766,38 +838,67 @@ __global__ void __launch_bounds__(192, 1)
         tmem_ld32(ta + 128, rc);
         tmem_wait_ld();
         const int col0 = (int)(cb * 128) + cc * 32;
-        if (row >= m) continue;
         float v[32];
 #pragma unroll
         for (int j = 0; j < 32; ++j)
-          v[j] = (__uint_as_float(rm[j]) + __uint_as_float(rc[j])) * __ldg(f + col0 + j);
-        if (out.C) {
-          float* dst = out.C + row * out.ldc + col0;
-          if (col0 + 32 <= k && ((out.ldc & 3) == 0) &&
-              ((reinterpret_cast<uintptr_t>(out.C) & 15) == 0)) {
+          v[j] = (__uint_as_float(rm[j]) + __uint_as_float(rc[j])) * __ldg(fp + col0 + j);
+        // 32-column groups go through the warp's staging rows (row r: 8
+        // chunks of 16 bytes, chunk q in slot q ^ (r & 7)) and leave as 128
+        // contiguous bytes per row (fewer at the last columns); FP32 rows < m
+        // and columns < k, packed rows < mp (padding rows get the zeros their
+        // zero input rows produce)
+        const bool staged = out.C ? (col0 < k) : (col0 < out.ldo);
+        if (staged) {
+          __syncwarp();
+          if (out.C) {
 #pragma unroll
-            for (int j = 0; j < 32; j += 4)
-              *reinterpret_cast<float4*>(dst + j) = make_float4(v[j], v[j + 1], v[j + 2], v[j + 3]);
+            for (int q = 0; q < 8; ++q)
+              stg[lane * 8 + (q ^ (lane & 7))] =
+                  make_uint4(__float_as_uint(v[4 * q]), __float_as_uint(v[4 * q + 1]),
+                             __float_as_uint(v[4 * q + 2]), __float_as_uint(v[4 * q + 3]));
           } else {
 #pragma unroll
-            for (int j = 0; j < 32; ++j)
-              if (col0 + j < k) dst[j] = v[j];
+            for (int g = 0; g < 4; ++g) {
+              float w[8];
+#pragma unroll
+              for (int q = 0; q < 8; ++q) w[q] = v[8 * g + q];
+              uint4 h, l;
+              split8(w, h, l);
+              stg[lane * 8 + (g ^ (lane & 7))] = h;
+              stg[lane * 8 + ((4 + g) ^ (lane & 7))] = l;
+            }
           }
-        } else if (col0 < out.ldo) {  // ldo is a multiple of 64: whole 32-column groups
+          __syncwarp();
+          const int q = lane & 7;
 #pragma unroll
-          for (int j = 0; j < 32; j += 8) {
-            float w[8];
+          for (int s8 = 0; s8 < 8; ++s8) {
+            const int rr = 4 * s8 + (lane >> 3);
+            const uint4 val = stg[rr * 8 + (q ^ (rr & 7))];
+            const int64_t r = row0 + rr;
+            if (out.C) {
+              const int c = col0 + 4 * q;
+              if (r < m && c < k) {
+                float* dst = out.C + pb * out.cstride + r * out.ldc + c;
+                if (c_vec && c + 4 <= k) {
+                  *reinterpret_cast<uint4*>(dst) = val;
+                } else {
+                  const float w4[4] = {__uint_as_float(val.x), __uint_as_float(val.y),
+                                       __uint_as_float(val.z), __uint_as_float(val.w)};
 #pragma unroll
-            for (int q = 0; q < 8; ++q) w[q] = v[j + q];
-            uint4 h, l;
-            split8(w, h, l);
-            *reinterpret_cast<uint4*>(out.ohi + row * out.ldo + col0 + j) = h;
-            *reinterpret_cast<uint4*>(out.olo + row * out.ldo + col0 + j) = l;
+                  for (int e = 0; e < 4; ++e)
+                    if (c + e < k) dst[e] = w4[e];
+                }
+              }
+            } else if (r < mp) {
+              __half* plane = q < 4 ? out.ohi : out.olo;
+              *reinterpret_cast<uint4*>(plane + (pb * mp + r) * out.ldo + col0 + 8 * (q & 3)) = val;
+            }
           }
         }
       }
       fence_before();
       mbar_arrive(&tempty[b]);
+      ++i;
     }
   }
   fence_before();
@@ -847,50 +948,64 @@ static bool make_map_planes(CUtensorMap* map, const __half* base, uint64_t inner
 
 int64_t packed_ld(int64_t N) { return cdiv(N, 64) * 64; }
 
-void packed_carve(Arena& ws, Packed& p, int64_t m, int64_t N) {
+// rows per problem in the planes: m for one problem; for a batch, m rounded
+// up to 128 so that no stage or output tile of one problem reaches the next
+int64_t packed_rows(int64_t m, int64_t batch) { return batch > 1 ? cdiv(m, 128) * 128 : m; }
+
+void packed_carve(Arena& ws, Packed& p, int64_t m, int64_t N, int64_t batch) {
   p.m = m;
   p.N = N;
   p.ld = packed_ld(N);
-  p.hi = ws.take<__half>((size_t)(2 * m * p.ld));
-  p.lo = p.hi ? p.hi + m * p.ld : nullptr;
-  p.scale = ws.take<float>((size_t)p.ld);
+  p.batch = batch;
+  p.mp = packed_rows(m, batch);
+  p.hi = ws.take<__half>((size_t)(2 * batch * p.mp * p.ld));
+  p.lo = p.hi ? p.hi + batch * p.mp * p.ld : nullptr;
+  p.scale = ws.take<float>((size_t)(batch * p.ld));
 }
 
-void packed_view(Packed& p, void* storage, int64_t m, int64_t N, float* scale) {
+void packed_view(Packed& p, void* storage, int64_t m, int64_t N, float* scale, int64_t batch) {
   p.m = m;
   p.N = N;
   p.ld = packed_ld(N);
+  p.batch = batch;
+  p.mp = packed_rows(m, batch);
   p.hi = static_cast<__half*>(storage);
-  p.lo = p.hi ? p.hi + m * p.ld : nullptr;
+  p.lo = p.hi ? p.hi + batch * p.mp * p.ld : nullptr;
   p.scale = scale;
 }
 
 int pack_f32(const float* Y, int64_t ld, int64_t m, int64_t N, Packed& p, Arena& ws,
-             cudaStream_t st) {
-  unsigned* cmax = ws.take<unsigned>((size_t)N);
+             cudaStream_t st, int64_t bstride) {
+  const int64_t batch = p.batch;
+  unsigned* cmax = ws.take<unsigned>((size_t)(N * batch));
   if (ws.measuring()) return PLOM_OK;
   PLOM_REQUIRE(!ws.overflow(), PLOM_ERR_WORKSPACE, "pack: workspace too small");
   PLOM_REQUIRE(Y && p.hi && p.scale && cmax && m >= 1 && N >= 1 && ld >= N, PLOM_ERR_ARG,
                "pack: bad arguments");
-  PLOM_CHECK_CUDA(cudaMemsetAsync(cmax, 0, (size_t)N * sizeof(unsigned), st));
+  PLOM_REQUIRE(batch == 1 || bstride >= m * ld, PLOM_ERR_ARG, "pack: batch stride < m * ld");
+  PLOM_CHECK_CUDA(cudaMemsetAsync(cmax, 0, (size_t)(N * batch) * sizeof(unsigned), st));
   const int threads = 256;
   {
     ProfScope prof("colmax", st, 0.0, 4.0 * (double)m * N);
-    const int rblocks = (int)std::max<int64_t>(1, std::min<int64_t>(m, (int64_t)num_sms() * 8));
-    const int cvec = ((ld & 3) == 0) && ((N & 3) == 0) && ((reinterpret_cast<uintptr_t>(Y) & 15) == 0);
-    hp::colmax_kernel<<<rblocks, threads, 0, st>>>(Y, ld, m, (int)N, cvec, cmax);
+    const int rblocks = (int)std::max<int64_t>(
+        1, std::min<int64_t>(m, cdiv((int64_t)num_sms() * 8, batch)));
+    const int cvec = ((ld & 3) == 0) && ((N & 3) == 0) && ((bstride & 3) == 0) &&
+                     ((reinterpret_cast<uintptr_t>(Y) & 15) == 0);
+    hp::colmax_kernel<<<dim3(rblocks, (unsigned)batch), threads, 0, st>>>(Y, ld, m, (int)N, cvec,
+                                                                         bstride, cmax);
     PLOM_CHECK_LAUNCH();
-    hp::colscale_kernel<<<(int)cdiv(p.ld, 256), 256, 0, st>>>(cmax, (int)N, (int)p.ld, p.scale);
+    hp::colscale_kernel<<<(int)std::min<int64_t>(cdiv(p.ld * batch, 256), 4096), 256, 0, st>>>(
+        cmax, (int)N, (int)p.ld, (int)batch, p.scale);
     PLOM_CHECK_LAUNCH();
   }
-  ProfScope prof("pack_f16x2", st, 0.0, 4.0 * (double)m * N + 4.0 * (double)m * p.ld);
+  ProfScope prof("pack_f16x2", st, 0.0, 4.0 * (double)m * N * batch + 4.0 * (double)p.mp * p.ld * batch);
   const int vec = ((ld & 3) == 0) && ((reinterpret_cast<uintptr_t>(Y) & 15) == 0);
   const int groups = (int)(p.ld / 8);
   const int rt = std::max(1, 2048 / groups);  // rows per tile: >= 2048 groups when rows are short
-  const int64_t tiles = cdiv(m, rt);
+  const int64_t tiles = cdiv(p.mp, rt) * batch;
   const int blocks = (int)std::max<int64_t>(1, std::min<int64_t>(tiles, (int64_t)num_sms() * 8));
   hp::pack_kernel<<<blocks, 256, 0, st>>>(Y, ld, m, (int)N, (int)p.ld, rt, p.scale, p.hi, p.lo,
-                                          vec);
+                                          vec && ((bstride & 3) == 0), bstride, p.mp, (int)batch);
   PLOM_CHECK_LAUNCH();
   return PLOM_OK;
 }
@@ -910,18 +1025,19 @@ static int gram16_chunks(int64_t m, int tiles) {
 }
 
 int gram_packed(const Packed& p, double* G, int* err, Arena& ws, cudaStream_t st) {
-  const int64_t m = p.m, N = p.N;
+  const int64_t m = p.m, N = p.N, batch = p.batch;
   const int tn = (int)cdiv(p.ld, 128);
   const int tiles = tn * (tn + 1) / 2;
-  const int chunks = gram16_chunks(m, tiles);
+  const int chunks = gram16_chunks(m, (int)std::min<int64_t>(tiles * batch, 1 << 20));
   int64_t rpc = cdiv(m, chunks);
   rpc = cdiv(rpc, hp::G_BK) * hp::G_BK;  // chunk boundaries on stage boundaries
   const int chunks_eff = (int)std::max<int64_t>(1, cdiv(m, rpc));
-  double* part = ws.take<double>((size_t)tiles * chunks_eff * 128 * 128);
+  double* part = ws.take<double>((size_t)(batch * tiles * chunks_eff) * 128 * 128);
   if (ws.measuring()) return PLOM_OK;
   PLOM_REQUIRE(!ws.overflow(), PLOM_ERR_WORKSPACE, "gram16: workspace too small");
-  PLOM_REQUIRE(p.hi && G && part && m >= 1 && m < (1ll << 31), PLOM_ERR_ARG,
-               "gram16: bad arguments");
+  PLOM_REQUIRE(p.hi && G && part && m >= 1 && batch * p.mp < (1ll << 31) &&
+                   batch * tiles * chunks_eff < (1ll << 31),
+               PLOM_ERR_ARG, "gram16: bad arguments");
   static bool attr = false;
   if (!attr) {
     PLOM_CHECK_CUDA(cudaFuncSetAttribute(hp::gram16_kernel<true>,
@@ -933,16 +1049,18 @@ int gram_packed(const Packed& p, double* G, int* err, Arena& ws, cudaStream_t st
     attr = true;
   }
   CUtensorMap tm;
-  PLOM_REQUIRE(make_map_planes(&tm, p.hi, (uint64_t)p.ld, (uint64_t)m, (uint64_t)p.ld, 64, hp::G_BK),
+  PLOM_REQUIRE(make_map_planes(&tm, p.hi, (uint64_t)p.ld, (uint64_t)(batch * p.mp),
+                               (uint64_t)p.ld, 64, hp::G_BK),
                PLOM_ERR_CUDA, "gram16: tensor map encoding failed");
-  ProfScope prof_g("tc_gram_f16x3", st, (double)m * N * N, 4.0 * (double)m * p.ld);
-  hp::gram16_kernel<true><<<tiles * chunks_eff, 320, hp::G_SMEM, st>>>(tm, tm, m, tn, tn, rpc,
-                                                                       chunks_eff, part, err);
+  ProfScope prof_g("tc_gram_f16x3", st, (double)m * N * N * batch, 4.0 * (double)m * p.ld * batch);
+  hp::gram16_kernel<true><<<(unsigned)(batch * tiles * chunks_eff), 320, hp::G_SMEM, st>>>(
+      tm, tm, m, tn, tn, rpc, chunks_eff, part, err, p.mp);
   PLOM_CHECK_LAUNCH();
-  const int64_t total = N * N;
+  const int64_t total = N * N * batch;
   const int blocks = (int)std::min<int64_t>(cdiv(total, 256), (int64_t)num_sms() * 16);
-  ProfScope prof_r("gram_reduce", st, 0.0, 8.0 * (double)tiles * chunks_eff * 128 * 128);
-  hp::gram16_reduce_kernel<<<blocks, 256, 0, st>>>(part, (int)N, tn, chunks_eff, p.scale, G);
+  ProfScope prof_r("gram_reduce", st, 0.0, 8.0 * (double)batch * tiles * chunks_eff * 128 * 128);
+  hp::gram16_reduce_kernel<<<blocks, 256, 0, st>>>(part, (int)N, tn, chunks_eff, p.scale, G,
+                                                   (int)batch, (int)p.ld);
   PLOM_CHECK_LAUNCH();
   return PLOM_OK;
 }
@@ -960,7 +1078,7 @@ int tn_packed(const Packed& a, const Packed& b, double* C, int64_t ldc, int* err
   if (ws.measuring()) return PLOM_OK;
   PLOM_REQUIRE(!ws.overflow(), PLOM_ERR_WORKSPACE, "tn16: workspace too small");
   PLOM_REQUIRE(a.hi && b.hi && C && part && m >= 1 && m < (1ll << 31) && b.m == m &&
-                   ldc >= b.N,
+                   ldc >= b.N && a.batch == 1 && b.batch == 1,
                PLOM_ERR_ARG, "tn16: bad arguments");
   static bool attr = false;
   if (!attr) {
@@ -976,8 +1094,8 @@ int tn_packed(const Packed& a, const Packed& b, double* C, int64_t ldc, int* err
   {
     ProfScope prof("tc_tn_f16x3", st, 2.0 * (double)m * a.N * b.N,
                    4.0 * (double)m * (a.ld + b.ld));
-    hp::gram16_kernel<false><<<tiles * chunks_eff, 320, hp::G_SMEM, st>>>(ta, tb, m, tna, tnb, rpc,
-                                                                          chunks_eff, part, err);
+    hp::gram16_kernel<false><<<tiles * chunks_eff, 320, hp::G_SMEM, st>>>(
+        ta, tb, m, tna, tnb, rpc, chunks_eff, part, err, m);
     PLOM_CHECK_LAUNCH();
   }
   const int64_t total = a.N * b.N;
@@ -989,19 +1107,25 @@ int tn_packed(const Packed& a, const Packed& b, double* C, int64_t ldc, int* err
 }
 
 int apply_packed(const Packed& p, const double* W, int64_t ldw, int64_t k, float* C, int64_t ldc,
-                 Packed* out, int* err, Arena& ws, cudaStream_t st) {
-  const int64_t m = p.m;
+                 Packed* out, int* err, Arena& ws, cudaStream_t st, int64_t wstride,
+                 int64_t cstride, bool upper) {
+  const int64_t m = p.m, batch = p.batch;
   const int64_t ldk = p.ld;  // K extent of the W copies (= packed pitch of the input)
   const int64_t col_tiles = cdiv(k, 128);
-  __half* bhi = ws.take<__half>((size_t)(2 * k * ldk));
-  __half* blo = bhi ? bhi + k * ldk : nullptr;
-  float* f = ws.take<float>((size_t)(col_tiles * 128));
+  const int fstride = (int)(col_tiles * 128);
+  __half* bhi = ws.take<__half>((size_t)(2 * batch * k * ldk));
+  __half* blo = bhi ? bhi + batch * k * ldk : nullptr;
+  float* f = ws.take<float>((size_t)(batch * fstride));
   if (ws.measuring()) return PLOM_OK;
   PLOM_REQUIRE(!ws.overflow(), PLOM_ERR_WORKSPACE, "apply16: workspace too small");
-  PLOM_REQUIRE(p.hi && W && (C || out) && m >= 1 && m < (1ll << 31) && k >= 1, PLOM_ERR_ARG,
-               "apply16: bad arguments");
-  if (out) PLOM_REQUIRE(out->hi && out->scale && out->m == m && out->N == k, PLOM_ERR_ARG,
-                        "apply16: bad packed output");
+  PLOM_REQUIRE(p.hi && W && (C || out) && m >= 1 && batch * p.mp < (1ll << 31) && k >= 1 &&
+                   batch * k < (1ll << 31),
+               PLOM_ERR_ARG, "apply16: bad arguments");
+  PLOM_REQUIRE(batch == 1 || (wstride >= p.N * ldw && (out || cstride >= m * ldc)), PLOM_ERR_ARG,
+               "apply16: batch strides too small");
+  if (out) PLOM_REQUIRE(out->hi && out->scale && out->m == m && out->N == k && out->batch == batch &&
+                            out->mp == p.mp,
+                        PLOM_ERR_ARG, "apply16: bad packed output");
   static bool attr = false;
   if (!attr) {
     PLOM_CHECK_CUDA(cudaFuncSetAttribute(hp::apply16_kernel,
@@ -1010,31 +1134,39 @@ int apply_packed(const Packed& p, const double* W, int64_t ldw, int64_t k, float
     attr = true;
   }
   const float out_scale = out ? (float)(1 << hp::PK_LOG2) : 1.0f;
-  hp::split_w16_kernel<<<(int)(col_tiles * 128), 256, 0, st>>>(W, ldw, (int)p.N, (int)k, (int)ldk,
-                                                              p.scale, out_scale, bhi, blo, f);
+  hp::split_w16_kernel<<<dim3((unsigned)fstride, (unsigned)batch), 256, 0, st>>>(
+      W, ldw, (int)p.N, (int)k, (int)ldk, p.scale, out_scale, bhi, blo, f, wstride, fstride);
   PLOM_CHECK_LAUNCH();
   if (out) {
     // packed output columns carry the fixed scale 2^14
-    hp::fill_scale_kernel<<<(int)cdiv(out->ld, 256), 256, 0, st>>>(out->scale, (int)out->ld,
-                                                                   out_scale);
+    hp::fill_scale_kernel<<<(int)std::min<int64_t>(cdiv(out->ld * batch, 256), 4096), 256, 0, st>>>(
+        out->scale, out->ld * batch, out_scale);
     PLOM_CHECK_LAUNCH();
   }
   CUtensorMap tmA, tmB;
-  PLOM_REQUIRE(make_map_planes(&tmA, p.hi, (uint64_t)p.ld, (uint64_t)m, (uint64_t)p.ld, 64, 128) &&
-                   make_map_planes(&tmB, bhi, (uint64_t)ldk, (uint64_t)k, (uint64_t)ldk, 64, 128),
+  PLOM_REQUIRE(make_map_planes(&tmA, p.hi, (uint64_t)p.ld, (uint64_t)(batch * p.mp),
+                               (uint64_t)p.ld, 64, 128) &&
+                   make_map_planes(&tmB, bhi, (uint64_t)ldk, (uint64_t)(batch * k), (uint64_t)ldk,
+                                   64, 128),
                PLOM_ERR_CUDA, "apply16: tensor map encoding failed");
-  const int64_t tiles = cdiv(m, 128) * col_tiles;
+  const int64_t row_tiles = cdiv(p.mp, 128);
+  const int64_t tiles = batch * row_tiles * col_tiles;
   const int grid = (int)std::min<int64_t>(tiles, num_sms());
   hp::ApplyOut o;
   o.C = out ? nullptr : C;
   o.ldc = ldc;
+  o.cstride = cstride;
   o.ohi = out ? out->hi : nullptr;
   o.olo = out ? out->lo : nullptr;
   o.ldo = out ? (int)out->ld : 0;
-  ProfScope prof("tc_apply_f16x3", st, 2.0 * m * p.N * k,
-                 4.0 * ((double)m * p.ld + (double)m * k));
+  // an upper-triangular W (k = N) needs m N (N + 1) flops: row i of W meets
+  // columns j >= i only
+  const bool tri = upper && k == p.N;
+  const double flops = tri ? (double)m * p.N * (p.N + 1) * batch : 2.0 * m * p.N * k * batch;
+  ProfScope prof("tc_apply_f16x3", st, flops, 4.0 * ((double)m * p.ld + (double)m * k) * batch);
   hp::apply16_kernel<<<grid, 192, hp::A_SMEM, st>>>(tmA, tmB, m, (int)(ldk / 64), (int)k,
-                                                    col_tiles, tiles, f, o, err);
+                                                    col_tiles, tiles, f, o, err, p.mp, row_tiles,
+                                                    fstride, tri ? 1 : 0);
   PLOM_CHECK_LAUNCH();
   return PLOM_OK;
 }

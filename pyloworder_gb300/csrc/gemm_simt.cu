@@ -17,6 +17,7 @@
 #include "plom_kernels.cuh"
 
 #include <algorithm>
+#include <memory>
 
 namespace plom {
 
@@ -29,7 +30,7 @@ __global__ void __launch_bounds__(256) gemm_nn_kernel(const TA* __restrict__ A, 
                                                       int64_t sA, const TB* __restrict__ B,
                                                       int64_t ldb, int64_t sB, TC* __restrict__ C,
                                                       int64_t ldc, int64_t sC, int64_t M,
-                                                      int64_t N, int64_t K) {
+                                                      int64_t N, int64_t K, int b_upper) {
   static_assert(BM == 16 * TM && BN == 16 * TN, "tile/thread mismatch");
   A += (int64_t)blockIdx.z * sA;
   B += (int64_t)blockIdx.z * sB;
@@ -45,17 +46,19 @@ __global__ void __launch_bounds__(256) gemm_nn_kernel(const TA* __restrict__ A, 
 #pragma unroll
     for (int j = 0; j < TN; ++j) acc[i][j] = Acc(0);
 
-  for (int64_t k0 = 0; k0 < K; k0 += BK) {
+  // B upper triangular (B[k][j] = 0 for k > j): this column block needs k < n0 + BN
+  const int64_t kend = b_upper ? min(K, n0 + BN) : K;
+  for (int64_t k0 = 0; k0 < kend; k0 += BK) {
     // A tile: BM rows x BK cols
     for (int e = threadIdx.x; e < BM * BK; e += 256) {
       int r = e / BK, c = e % BK;
       int64_t gr = m0 + r, gc = k0 + c;
-      As[c][r] = (gr < M && gc < K) ? (Acc)A[gr * lda + gc] : Acc(0);
+      As[c][r] = (gr < M && gc < kend) ? (Acc)A[gr * lda + gc] : Acc(0);
     }
     for (int e = threadIdx.x; e < BK * BN; e += 256) {
       int r = e / BN, c = e % BN;
       int64_t gr = k0 + r, gc = n0 + c;
-      Bs[r][c] = (gr < K && gc < N) ? (Acc)B[gr * ldb + gc] : Acc(0);
+      Bs[r][c] = (gr < kend && gc < N) ? (Acc)B[gr * ldb + gc] : Acc(0);
     }
     __syncthreads();
 #pragma unroll
@@ -87,24 +90,101 @@ __global__ void __launch_bounds__(256) gemm_nn_kernel(const TA* __restrict__ A, 
 template <typename TA, typename TB, typename TC, typename Acc>
 int gemm_nn_batched(const TA* A, int64_t lda, int64_t sA, const TB* B, int64_t ldb, int64_t sB,
                     TC* C, int64_t ldc, int64_t sC, int64_t M, int64_t N, int64_t K, int batch,
-                    cudaStream_t st) {
+                    cudaStream_t st, bool b_upper) {
   if (M == 0 || N == 0 || batch == 0) return PLOM_OK;
   PLOM_REQUIRE(A && B && C, PLOM_ERR_ARG, "gemm_nn: null operand");
   constexpr int BM = 128, BN = 64, BK = 8;
   dim3 grid((unsigned)cdiv(M, BM), (unsigned)cdiv(N, BN), (unsigned)batch);
   PLOM_REQUIRE(grid.y <= 65535 && batch <= 65535, PLOM_ERR_ARG, "gemm_nn: N or batch too large");
-  ProfScope prof(sizeof(Acc) == 8 ? "gemm_nn_fp64" : "gemm_nn_fp32", st, 2.0 * M * N * K * batch,
+  const double fl = b_upper && N == K ? (double)M * N * (N + 1) : 2.0 * M * N * K;
+  ProfScope prof(sizeof(Acc) == 8 ? "gemm_nn_fp64" : "gemm_nn_fp32", st, fl * batch,
                  (double)batch * ((double)M * K * sizeof(TA) + (double)M * N * sizeof(TC)));
-  gemm_nn_kernel<TA, TB, TC, Acc, BM, BN, BK, 8, 4><<<grid, 256, 0, st>>>(A, lda, sA, B, ldb, sB, C,
-                                                                          ldc, sC, M, N, K);
+  gemm_nn_kernel<TA, TB, TC, Acc, BM, BN, BK, 8, 4><<<grid, 256, 0, st>>>(
+      A, lda, sA, B, ldb, sB, C, ldc, sC, M, N, K, b_upper ? 1 : 0);
   PLOM_CHECK_LAUNCH();
   return PLOM_OK;
 }
 
 template <typename TA, typename TB, typename TC, typename Acc>
 int gemm_nn(const TA* A, int64_t lda, const TB* B, int64_t ldb, TC* C, int64_t ldc, int64_t M,
-            int64_t N, int64_t K, cudaStream_t st) {
-  return gemm_nn_batched<TA, TB, TC, Acc>(A, lda, 0, B, ldb, 0, C, ldc, 0, M, N, K, 1, st);
+            int64_t N, int64_t K, cudaStream_t st, bool b_upper) {
+  return gemm_nn_batched<TA, TB, TC, Acc>(A, lda, 0, B, ldb, 0, C, ldc, 0, M, N, K, 1, st, b_upper);
+}
+
+// ----------------------------------------------------------------------------
+// Small FP64 products of the n x n stage: C = alpha A B on 32 x 32 tiles.  A
+// tile's K range is clipped to the band where triangular operands are
+// non-zero (tri bit 0: A upper, A[i][k] = 0 for k < i; bit 1: B upper,
+// B[k][j] = 0 for k > j), so a triangular x triangular product costs n^3/6
+// FMAs and triangular x dense n^3/2.  FP64 throughput per SM bounds these
+// products on GB300, so the tiles are small enough (1,024 for n = 1,024) that
+// the longest tile is a small share of the whole.  grid.z enumerates
+// (problem b, sub-block t): operands sit at b*s + t*tstride.
+// ----------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) gemm_sq_kernel(const double* __restrict__ A, int64_t lda,
+                                                      int64_t sA, int64_t tA,
+                                                      const double* __restrict__ B, int64_t ldb,
+                                                      int64_t sB, int64_t tB, double* __restrict__ C,
+                                                      int64_t ldc, int64_t sC, int64_t tC, int M,
+                                                      int N, int K, int nsub, double alpha, int tri) {
+  const int64_t b = blockIdx.z / nsub, t = blockIdx.z % nsub;
+  A += b * sA + t * tA;
+  B += b * sB + t * tB;
+  C += b * sC + t * tC;
+  __shared__ double As[32][33];  // [k][row]
+  __shared__ double Bs[32][33];  // [k][col]
+  const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+  const int m0 = blockIdx.x * 32, n0 = blockIdx.y * 32;
+  const int kbeg = (tri & 1) ? m0 : 0;
+  const int kend = (tri & 2) ? min(K, n0 + 32) : K;
+  double c00 = 0.0, c01 = 0.0, c10 = 0.0, c11 = 0.0;
+  for (int k0 = kbeg; k0 < kend; k0 += 32) {
+    for (int e = threadIdx.x; e < 32 * 32; e += 256) {
+      const int r = e >> 5, c = e & 31;
+      const int ga = m0 + r, gk = k0 + c;
+      As[c][r] = (ga < M && gk < kend) ? A[(int64_t)ga * lda + gk] : 0.0;
+      const int gb = k0 + r, gn = n0 + c;
+      Bs[r][c] = (gb < kend && gn < N) ? B[(int64_t)gb * ldb + gn] : 0.0;
+    }
+    __syncthreads();
+#pragma unroll 8
+    for (int kk = 0; kk < 32; ++kk) {
+      const double a0 = As[kk][ty], a1 = As[kk][ty + 16];
+      const double b0 = Bs[kk][tx], b1 = Bs[kk][tx + 16];
+      c00 = fma(a0, b0, c00);
+      c01 = fma(a0, b1, c01);
+      c10 = fma(a1, b0, c10);
+      c11 = fma(a1, b1, c11);
+    }
+    __syncthreads();
+  }
+  const int r0 = m0 + ty, r1 = r0 + 16, q0 = n0 + tx, q1 = q0 + 16;
+  if (r0 < M && q0 < N) C[(int64_t)r0 * ldc + q0] = alpha * c00;
+  if (r0 < M && q1 < N) C[(int64_t)r0 * ldc + q1] = alpha * c01;
+  if (r1 < M && q0 < N) C[(int64_t)r1 * ldc + q0] = alpha * c10;
+  if (r1 < M && q1 < N) C[(int64_t)r1 * ldc + q1] = alpha * c11;
+}
+
+int gemm_sq(const double* A, int64_t lda, int64_t sA, int64_t tA, const double* B, int64_t ldb,
+            int64_t sB, int64_t tB, double* C, int64_t ldc, int64_t sC, int64_t tC, int M, int N,
+            int K, int batch, int nsub, double alpha, int tri, cudaStream_t st, const char* tag) {
+  if (M <= 0 || N <= 0 || batch <= 0 || nsub <= 0) return PLOM_OK;
+  PLOM_REQUIRE(A && B && C, PLOM_ERR_ARG, "gemm_sq: null operand");
+  PLOM_REQUIRE((int64_t)batch * nsub <= 65535, PLOM_ERR_ARG, "gemm_sq: batch too large");
+  const dim3 grid((unsigned)cdiv(M, 32), (unsigned)cdiv(N, 32), (unsigned)(batch * nsub));
+  // FMAs of the band the kernel visits, counted as flops (2 per FMA)
+  double fl = 2.0 * M * N * K;
+  if ((tri & 3) == 3) fl = 2.0 * M * (double)N * K / 6.0;
+  else if (tri & 3) fl = 2.0 * M * (double)N * K / 2.0;
+  // tag == nullptr: timed by the caller's region
+  std::unique_ptr<ProfScope> prof;
+  if (tag)
+    prof.reset(new ProfScope(tag, st, fl * batch * nsub,
+                             8.0 * batch * nsub * ((double)M * K + (double)K * N + (double)M * N)));
+  gemm_sq_kernel<<<grid, 256, 0, st>>>(A, lda, sA, tA, B, ldb, sB, tB, C, ldc, sC, tC, M, N, K,
+                                       nsub, alpha, tri);
+  PLOM_CHECK_LAUNCH();
+  return PLOM_OK;
 }
 
 // ----------------------------------------------------------------------------
@@ -337,10 +417,10 @@ template int gemm_tn_in_scratch<double, double, double>(const double*, int64_t, 
 // explicit instantiations used across the library
 #define NN(TA, TB, TC, ACC)                                                                  \
   template int gemm_nn<TA, TB, TC, ACC>(const TA*, int64_t, const TB*, int64_t, TC*, int64_t, \
-                                        int64_t, int64_t, int64_t, cudaStream_t);             \
+                                        int64_t, int64_t, int64_t, cudaStream_t, bool);       \
   template int gemm_nn_batched<TA, TB, TC, ACC>(const TA*, int64_t, int64_t, const TB*, int64_t, \
                                                 int64_t, TC*, int64_t, int64_t, int64_t, int64_t, \
-                                                int64_t, int, cudaStream_t);
+                                                int64_t, int, cudaStream_t, bool);
 NN(float, float, float, float)
 NN(float, double, double, double)
 NN(float, double, float, double)

@@ -105,6 +105,7 @@ struct ProfEntry {
   const char* name;
   cudaEvent_t a, b;
   double flops, bytes;
+  int launches = 1;  // kernel launches inside the scope
 };
 bool prof_on();
 void prof_push(const ProfEntry& e);
@@ -112,11 +113,13 @@ struct ProfScope {
   ProfEntry e;
   cudaStream_t st;
   bool on;
-  ProfScope(const char* name, cudaStream_t s, double flops, double bytes) : st(s), on(prof_on()) {
+  ProfScope(const char* name, cudaStream_t s, double flops, double bytes, int launches = 1)
+      : st(s), on(prof_on()) {
     if (!on) return;
     e.name = name;
     e.flops = flops;
     e.bytes = bytes;
+    e.launches = launches;
     cudaEventCreate(&e.a);
     cudaEventCreate(&e.b);
     cudaEventRecord(e.a, st);

@@ -12,11 +12,12 @@ int rows_dispatch(int dtype, const void* X, int64_t m, int64_t n, int64_t ldx, c
 // ---- gemm_simt.cu ----
 template <typename TA, typename TB, typename TC, typename Acc>
 int gemm_nn(const TA* A, int64_t lda, const TB* B, int64_t ldb, TC* C, int64_t ldc, int64_t M,
-            int64_t N, int64_t K, cudaStream_t st);
+            int64_t N, int64_t K, cudaStream_t st, bool b_upper = false);
+// b_upper: B is upper triangular (B[k][j] = 0 for k > j), its zero band is skipped
 template <typename TA, typename TB, typename TC, typename Acc>
 int gemm_nn_batched(const TA* A, int64_t lda, int64_t sA, const TB* B, int64_t ldb, int64_t sB,
                     TC* C, int64_t ldc, int64_t sC, int64_t M, int64_t N, int64_t K, int batch,
-                    cudaStream_t st);
+                    cudaStream_t st, bool b_upper = false);
 template <typename TA, typename TB, typename Acc, typename TC>
 int gemm_tn(const TA* A, int64_t lda, const TB* B, int64_t ldb, TC* C, int64_t ldc, int64_t M,
             int64_t N, int64_t K, bool sym, Arena& ws, cudaStream_t st);
@@ -25,6 +26,19 @@ int gemm_tn_batched(const TA* A, int64_t lda, int64_t sA, const TB* B, int64_t l
                     TC* C, int64_t ldc, int64_t sC, int64_t M, int64_t N, int64_t K, bool sym,
                     int batch, Arena& ws, cudaStream_t st);
 size_t gemm_tn_workspace(int64_t M, int64_t N, int64_t K, bool sym, size_t acc_bytes);
+// C = alpha A B for small FP64 operands (n x n stage), 32 x 32 tiles; tri bit
+// 0: A upper triangular, bit 1: B upper triangular (the zero bands are
+// skipped).  Operands of problem b, sub-block t sit at b * s + t * tstride.
+int gemm_sq(const double* A, int64_t lda, int64_t sA, int64_t tA, const double* B, int64_t ldb,
+            int64_t sB, int64_t tB, double* C, int64_t ldc, int64_t sC, int64_t tC, int M, int N,
+            int K, int batch, int nsub, double alpha, int tri, cudaStream_t st,
+            const char* tag = "gemm_sq_fp64");
+// square n x n products, batch of problems n*n apart
+inline int gemm_sq_nn(const double* A, const double* B, double* C, int n, int batch, int tri,
+                      cudaStream_t st) {
+  const int64_t nn = (int64_t)n * n;
+  return gemm_sq(A, n, nn, 0, B, n, nn, 0, C, n, nn, 0, n, n, n, batch, 1, 1.0, tri, st);
+}
 template <typename TA, typename TB, typename TC>
 int gemm_tn_in_scratch(const TA* A, int64_t lda, const TB* B, int64_t ldb, TC* C, int64_t ldc,
                        int64_t M, int64_t N, int64_t K, void* scratch, size_t cap,

@@ -9,30 +9,39 @@
 namespace plom {
 
 // Tall FP32 operand packed as two fp16 planes (gemm_f16.cu):
-//   hi + lo = Y diag(scale), hi and lo row-major m x ld (ld = N rounded up to
-//   64, padding columns zero; lo = hi + m * ld), scale[j] a power of two.
+//   hi + lo = Y diag(scale), hi and lo row-major (batch x mp) x ld (ld = N
+//   rounded up to 64, padding columns zero; lo right after hi), scale[p][j]
+//   a power of two per problem and column.  A batch holds `batch` problems
+//   of m rows each, mp rows apart (mp = m for one problem, else m rounded up
+//   to 128 with zero padding rows).
 struct Packed {
   __half* hi;
   __half* lo;
-  float* scale;  // [ld]
+  float* scale;  // [batch][ld]
   int64_t m, N, ld;
+  int64_t batch = 1, mp = 0;
 };
 int64_t packed_ld(int64_t N);
+int64_t packed_rows(int64_t m, int64_t batch);
 // carve planes and scales from the workspace
-void packed_carve(Arena& ws, Packed& p, int64_t m, int64_t N);
-// planes in caller storage of 4 m packed_ld(N) bytes, scales in `scale`
-void packed_view(Packed& p, void* storage, int64_t m, int64_t N, float* scale);
-// pack an FP32 matrix with per-column power-of-two scales
+void packed_carve(Arena& ws, Packed& p, int64_t m, int64_t N, int64_t batch = 1);
+// planes in caller storage of 4 batch packed_rows(m) packed_ld(N) bytes, scales in `scale`
+void packed_view(Packed& p, void* storage, int64_t m, int64_t N, float* scale, int64_t batch = 1);
+// pack an FP32 matrix (a batch: matrices bstride elements apart) with
+// per-column power-of-two scales
 int pack_f32(const float* Y, int64_t ld, int64_t m, int64_t N, Packed& p, Arena& ws,
-             cudaStream_t st);
-// G (N x N, FP64) = Y^T Y
+             cudaStream_t st, int64_t bstride = 0);
+// G (N x N, FP64; a batch: batch x N x N) = Y^T Y
 int gram_packed(const Packed& p, double* G, int* err, Arena& ws, cudaStream_t st);
 // C (A.N x B.N, FP64, ldc) = A^T B for two packed operands with the same rows
 int tn_packed(const Packed& a, const Packed& b, double* C, int64_t ldc, int* err, Arena& ws,
               cudaStream_t st);
-// Y W for W (N x k, FP64, ldw): FP32 into C (ldc) when out == nullptr, else
-// packed into *out (planes m x packed_ld(k), scale 2^14)
+// Y W for W (N x k, FP64, ldw; a batch: W_p wstride apart): FP32 into C
+// (ldc; C_p cstride apart) when out == nullptr, else packed into *out
+// (planes like the input, scale 2^14).  upper: W (k = N) is upper triangular,
+// and the zero blocks below its diagonal are skipped
 int apply_packed(const Packed& p, const double* W, int64_t ldw, int64_t k, float* C, int64_t ldc,
-                 Packed* out, int* err, Arena& ws, cudaStream_t st);
+                 Packed* out, int* err, Arena& ws, cudaStream_t st, int64_t wstride = 0,
+                 int64_t cstride = 0, bool upper = false);
 
 }  // namespace plom

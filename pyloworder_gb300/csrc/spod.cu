@@ -298,6 +298,53 @@ static int spod_fft_impl(const T* Y, int64_t M, int64_t N, int64_t ldy, int nDFT
   return PLOM_OK;
 }
 
+// P[(b M + i) nf + f0 + g] = Re U_g[i][b] for the G frequencies f0 .. f0+G-1
+// of one batched SVD (U_g: M x nBlks complex, interleaved, ustride complex
+// elements apart): pyLOM's column layout of the modes, real(U) flattened in
+// Fortran order into column ifreq of P (SPOD/wrapper.py:84).  A block stages
+// one point's G x nBlks real parts and writes them back frequency-fastest, so
+// both the reads (along b) and the writes (along f) are contiguous.
+template <typename T>
+__global__ void __launch_bounds__(256) spod_modes_kernel(const T* __restrict__ U, int64_t M,
+                                                         int nBlks, int G, int64_t ustride,
+                                                         T* __restrict__ P, int64_t nf, int64_t f0,
+                                                         int pitch) {
+  extern __shared__ __align__(16) unsigned char modes_sm[];
+  T* tile = reinterpret_cast<T*>(modes_sm);  // [G][pitch]
+  const int tot = G * nBlks;
+  for (int64_t i = blockIdx.x; i < M; i += gridDim.x) {
+    for (int e = threadIdx.x; e < tot; e += blockDim.x) {
+      const int g = e / nBlks, b = e - g * nBlks;
+      tile[g * pitch + b] = U[2 * ((int64_t)g * ustride + i * nBlks + b)];
+    }
+    __syncthreads();
+    for (int e = threadIdx.x; e < tot; e += blockDim.x) {
+      const int b = e / G, g = e - b * G;
+      P[((int64_t)b * M + i) * nf + f0 + g] = tile[g * pitch + b];
+    }
+    __syncthreads();
+  }
+}
+
+template <typename T>
+static int spod_modes_impl(const T* U, int64_t G, int64_t M, int64_t nBlks, int64_t ustride, T* P,
+                           int64_t nf, int64_t f0, cudaStream_t st) {
+  const int pitch = (int)(nBlks | 1);  // odd pitch: the frequency-fastest reads spread over banks
+  const size_t smem = sizeof(T) * (size_t)G * pitch;
+  PLOM_REQUIRE(smem <= 200 * 1024, PLOM_ERR_UNSUPPORTED,
+               "spod_modes: %lld frequencies x %lld blocks do not fit in shared memory",
+               (long long)G, (long long)nBlks);
+  if (smem > 48 * 1024)
+    PLOM_CHECK_CUDA(cudaFuncSetAttribute(spod_modes_kernel<T>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  const int64_t grid = std::min<int64_t>(M, (int64_t)num_sms() * 8);
+  ProfScope prof("spod_modes", st, 0.0, (double)sizeof(T) * 3.0 * G * M * nBlks);
+  spod_modes_kernel<T><<<(unsigned)grid, 256, smem, st>>>(U, M, (int)nBlks, (int)G, ustride, P, nf,
+                                                          f0, pitch);
+  PLOM_CHECK_LAUNCH();
+  return PLOM_OK;
+}
+
 }  // namespace plom
 
 using namespace plom;
@@ -322,5 +369,19 @@ extern "C" int plom_spod_fft(int dtype, const void* Y, int64_t M, int64_t N, int
                                  (int)nf, (const double*)window, (const double*)twr,
                                  (const double*)twi, scale, (double*)Q, st);
   set_error("spod_fft: dtype must be F32 or F64");
+  return PLOM_ERR_UNSUPPORTED;
+}
+
+extern "C" int plom_spod_modes(int dtype, const void* U, int64_t G, int64_t M, int64_t nBlks,
+                               int64_t ustride, void* P, int64_t nf, int64_t f0, void* stream) {
+  PLOM_REQUIRE(U && P, PLOM_ERR_ARG, "spod_modes: null pointer");
+  PLOM_REQUIRE(G >= 1 && M >= 1 && nBlks >= 1 && ustride >= M * nBlks && f0 >= 0 && f0 + G <= nf,
+               PLOM_ERR_ARG, "spod_modes: bad sizes");
+  cudaStream_t st = (cudaStream_t)stream;
+  if (dtype == PLOM_F32)
+    return spod_modes_impl<float>((const float*)U, G, M, nBlks, ustride, (float*)P, nf, f0, st);
+  if (dtype == PLOM_F64)
+    return spod_modes_impl<double>((const double*)U, G, M, nBlks, ustride, (double*)P, nf, f0, st);
+  set_error("spod_modes: dtype must be F32 or F64 (the real type of U)");
   return PLOM_ERR_UNSUPPORTED;
 }

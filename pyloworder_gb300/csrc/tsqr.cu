@@ -61,24 +61,25 @@ static int tall_gram(int prec, const TA* A, int64_t lda, int64_t m, int64_t N, d
 // C(m x k) = A(m x N) W(N x k), W in FP64 (converted for the mixed form)
 template <typename TA, typename TO>
 static int tall_apply(int prec, const TA* A, int64_t lda, int64_t m, int64_t N, const double* W,
-                      int64_t k, TO* C, int64_t ldc, int* err, Arena& ws, cudaStream_t st) {
+                      int64_t k, TO* C, int64_t ldc, int* err, Arena& ws, cudaStream_t st,
+                      bool upper = false) {
   if (prec == PLOM_PREC_FP64 || sizeof(TA) == 8) {
     if (ws.measuring()) return PLOM_OK;  // workspace query: launch nothing
-    return gemm_nn<TA, double, TO, double>(A, lda, W, k, C, ldc, m, k, N, st);
+    return gemm_nn<TA, double, TO, double>(A, lda, W, k, C, ldc, m, k, N, st, upper);
   }
   if constexpr (sizeof(TA) == 4 && sizeof(TO) == 4) {
     if (packed_ok(m)) {
       Packed p;
       packed_carve(ws, p, m, N);
       PLOM_TRY(pack_f32(A, lda, m, N, p, ws, st));
-      return apply_packed(p, W, k, k, C, ldc, nullptr, err, ws, st);
+      return apply_packed(p, W, k, k, C, ldc, nullptr, err, ws, st, 0, 0, upper);
     }
   }
   float* Wf = ws.take<float>((size_t)N * k);
   if (ws.measuring()) return PLOM_OK;
   PLOM_REQUIRE(!ws.overflow(), PLOM_ERR_WORKSPACE, "tall_apply: workspace too small");
   PLOM_TRY((convert<double, float>(W, Wf, N * k, st)));
-  return gemm_nn<TA, float, TO, float>(A, lda, Wf, k, C, ldc, m, k, N, st);
+  return gemm_nn<TA, float, TO, float>(A, lda, Wf, k, C, ldc, m, k, N, st, upper);
 }
 
 // Shifts are passed to the Cholesky relative to trace(G)/N; the absolute
@@ -159,7 +160,7 @@ static int cholqr3(int prec, bool cplx, const TI* X, int64_t m, int n, int64_t l
   ws.off = mark;
   TC* Q1 = q1_store ? q1_store : b.Q1;
   int64_t ld1 = q1_store ? ldq1 : N;
-  PLOM_TRY((tall_apply<TI, TC>(prec, X, ldx, m, N, F1, N, Q1, ld1, info, ws, st)));
+  PLOM_TRY((tall_apply<TI, TC>(prec, X, ldx, m, N, F1, N, Q1, ld1, info, ws, st, true)));
   need = std::max(need, ws.off);
   ws.off = mark;
   // pass 2
@@ -169,7 +170,7 @@ static int cholqr3(int prec, bool cplx, const TI* X, int64_t m, int n, int64_t l
   ws.off = mark;
   const double* F2 = ws.measuring() ? b.W2 : rowform(cplx, b.W2, b.F, n, st, s);
   if (!ws.measuring()) PLOM_TRY(s);
-  PLOM_TRY((tall_apply<TC, TC>(prec, Q1, ld1, m, N, F2, N, b.Q2, N, info, ws, st)));
+  PLOM_TRY((tall_apply<TC, TC>(prec, Q1, ld1, m, N, F2, N, b.Q2, N, info, ws, st, true)));
   need = std::max(need, ws.off);
   ws.off = mark;
   // pass 3
@@ -179,8 +180,8 @@ static int cholqr3(int prec, bool cplx, const TI* X, int64_t m, int n, int64_t l
   ws.off = need;
   // Re = R3 R2 R1
   if (!ws.measuring()) {
-    PLOM_TRY((gemm_nn<double, double, double, double>(b.R3, N, b.R2, N, b.Rp, N, N, N, N, st)));
-    PLOM_TRY((gemm_nn<double, double, double, double>(b.Rp, N, b.R1, N, b.Re, N, N, N, N, st)));
+    PLOM_TRY((gemm_sq_nn(b.R3, b.R2, b.Rp, N, 1, 3, st)));
+    PLOM_TRY((gemm_sq_nn(b.Rp, b.R1, b.Re, N, 1, 3, st)));
   }
   return PLOM_OK;
 }
@@ -262,18 +263,18 @@ static int cholqr3_packed(bool cplx, const float* X, int64_t m, int n, int64_t l
   PLOM_TRY(sub([&] { return chol_pass_packed(cplx, n, b.P0, b, b.R1, b.W1, rel1, relfail, info, ws, st); }));
   const double* F1 = ws.measuring() ? b.W1 : rowform(cplx, b.W1, b.F, n, st, s);
   PLOM_TRY(s);
-  PLOM_TRY(sub([&] { return apply_packed(b.P0, F1, N, N, nullptr, 0, &b.P1, info, ws, st); }));
+  PLOM_TRY(sub([&] { return apply_packed(b.P0, F1, N, N, nullptr, 0, &b.P1, info, ws, st, 0, 0, true); }));
   // pass 2
   PLOM_TRY(sub([&] { return chol_pass_packed(cplx, n, b.P1, b, b.R2, b.W2, 0.0, relfail, info, ws, st); }));
   const double* F2 = ws.measuring() ? b.W2 : rowform(cplx, b.W2, b.F, n, st, s);
   PLOM_TRY(s);
-  PLOM_TRY(sub([&] { return apply_packed(b.P1, F2, N, N, nullptr, 0, &b.P2, info, ws, st); }));
+  PLOM_TRY(sub([&] { return apply_packed(b.P1, F2, N, N, nullptr, 0, &b.P2, info, ws, st, 0, 0, true); }));
   // pass 3
   PLOM_TRY(sub([&] { return chol_pass_packed(cplx, n, b.P2, b, b.R3, b.W3, 0.0, relfail, info, ws, st); }));
   ws.off = need;
   if (!ws.measuring()) {
-    PLOM_TRY((gemm_nn<double, double, double, double>(b.R3, N, b.R2, N, b.Rp, N, N, N, N, st)));
-    PLOM_TRY((gemm_nn<double, double, double, double>(b.Rp, N, b.R1, N, b.Re, N, N, N, N, st)));
+    PLOM_TRY((gemm_sq_nn(b.R3, b.R2, b.Rp, N, 1, 3, st)));
+    PLOM_TRY((gemm_sq_nn(b.Rp, b.R1, b.Re, N, 1, 3, st)));
   }
   return PLOM_OK;
 }
@@ -317,10 +318,10 @@ static int tsqr_svd_packed(bool cplx, const float* X, int64_t m, int n, int64_t 
     // M = R3^-1 Ur (embedded for complex), the right operand of Q2 x M
     if (cplx) {
       PLOM_TRY(complex_to_embed(Ur, Ue, n, 1, st));
-      PLOM_TRY((gemm_nn<double, double, double, double>(b.W3, N, Ue, N, Me, N, N, N, N, st)));
+      PLOM_TRY((gemm_sq_nn(b.W3, Ue, Me, N, 1, 1, st)));
       PLOM_TRY(embed_to_rowform(Me, b.F, n, 1, st));
     } else {
-      PLOM_TRY((gemm_nn<double, double, double, double>(b.W3, N, Ur, N, Me, N, N, N, N, st)));
+      PLOM_TRY((gemm_sq_nn(b.W3, Ur, Me, N, 1, 1, st)));
       Mop = Me;
     }
   }
@@ -333,6 +334,110 @@ static int tsqr_svd_packed(bool cplx, const float* X, int64_t m, int n, int64_t 
   return PLOM_OK;
 }
 
+// ---------------------------------------------------------------------------
+// Batched mixed-form TSQR-SVD: `batch` FP32 problems of the same shape (real,
+// or complex as interleaved real views), e.g. SPOD's per-frequency matrices.
+// Every stage is one launch over the whole batch: packed Grams and applies
+// with a problem index on the work items, batched Cholesky / inverse /
+// Jacobi, batched small GEMMs.
+// ---------------------------------------------------------------------------
+static int tsqr_svd_batched_packed(bool cplx, const float* X, int64_t batch, int64_t m, int n,
+                                   int64_t ldx, int64_t xstride, float* U, int64_t ldu,
+                                   int64_t ustride, float* S, float* VT, int* info, Arena& ws,
+                                   cudaStream_t st) {
+  const int N = cplx ? 2 * n : n;
+  const int cw = cplx ? 2 : 1;
+  const int bi = (int)batch;
+  const int64_t NN = (int64_t)N * N;
+  const size_t nnb = (size_t)(NN * batch);
+  double* G = ws.take<double>(nnb);
+  double* H = ws.take<double>(nnb);
+  double* R1 = ws.take<double>(nnb);
+  double* R2 = ws.take<double>(nnb);
+  double* R3 = ws.take<double>(nnb);
+  double* W1 = ws.take<double>(nnb);
+  double* W2 = ws.take<double>(nnb);
+  double* W3 = ws.take<double>(nnb);
+  double* Rp = ws.take<double>(nnb);
+  double* Re = ws.take<double>(nnb);
+  double* F = ws.take<double>(nnb);
+  double* Me = ws.take<double>(nnb);
+  double* Ue = ws.take<double>(nnb);
+  const size_t cnb = (size_t)n * n * cw * batch;
+  double* Rc = ws.take<double>(cnb);
+  double* Ur = ws.take<double>(cnb);
+  double* VH = ws.take<double>(cnb);
+  double* S64 = ws.take<double>((size_t)n * batch);
+  Packed P0, P1, P2;
+  packed_carve(ws, P0, m, N, batch);
+  packed_carve(ws, P1, m, N, batch);
+  P2 = P0;
+  P2.scale = ws.take<float>((size_t)(P0.ld * batch));
+  if (!ws.measuring())
+    PLOM_REQUIRE(!ws.overflow(), PLOM_ERR_WORKSPACE, "tsqr_svd_batched: workspace too small");
+  const size_t mark = ws.off;
+  size_t need = mark;
+  auto sub = [&](auto&& fn) -> int {
+    ws.off = mark;
+    const int s = fn();
+    need = std::max(need, ws.off);
+    ws.off = mark;
+    return s;
+  };
+  const bool meas = ws.measuring();
+  double rel1, relfail;
+  shifts_for(PLOM_PREC_MIXED, m, N, rel1, relfail);
+  auto pass = [&](const Packed& P, double* R, double* W, double rel0) -> int {
+    PLOM_TRY(sub([&] { return gram_packed(P, cplx ? H : G, info, ws, st); }));
+    if (cplx && !meas) PLOM_TRY(complexify_gram(H, G, n, bi, st));
+    PLOM_TRY(sub([&] { return chol_shifted(G, R, N, bi, rel0, relfail, info, ws, st); }));
+    return sub([&] { return trtri_upper(R, W, N, bi, ws, st); });
+  };
+  auto rowform_b = [&](const double* W) -> const double* {
+    if (!cplx || meas) return W;
+    return embed_to_rowform(W, F, n, bi, st) == PLOM_OK ? F : nullptr;
+  };
+  PLOM_TRY(sub([&] { return pack_f32(X, ldx, m, N, P0, ws, st, xstride); }));
+  PLOM_TRY(pass(P0, R1, W1, rel1));
+  const double* F1 = rowform_b(W1);
+  PLOM_REQUIRE(meas || F1, PLOM_ERR_CUDA, "tsqr_svd_batched: embedding failed");
+  PLOM_TRY(sub([&] { return apply_packed(P0, F1, N, N, nullptr, 0, &P1, info, ws, st, NN, 0, true); }));
+  PLOM_TRY(pass(P1, R2, W2, 0.0));
+  const double* F2 = rowform_b(W2);
+  PLOM_REQUIRE(meas || F2, PLOM_ERR_CUDA, "tsqr_svd_batched: embedding failed");
+  PLOM_TRY(sub([&] { return apply_packed(P1, F2, N, N, nullptr, 0, &P2, info, ws, st, NN, 0, true); }));
+  PLOM_TRY(pass(P2, R3, W3, 0.0));
+  const double* Rin = Re;
+  if (!meas) {
+    PLOM_TRY((gemm_sq_nn(R3, R2, Rp, N, bi, 3, st)));
+    PLOM_TRY((gemm_sq_nn(Rp, R1, Re, N, bi, 3, st)));
+    if (cplx) {
+      PLOM_TRY(embed_to_complex(Re, Rc, n, bi, st));
+      Rin = Rc;
+    }
+  }
+  PLOM_TRY(sub([&] { return jacobi_svd(Rin, n, bi, cplx ? 1 : 0, 1e-8, S64, Ur, VH, info, ws, st); }));
+  const double* Mop = F;
+  if (!meas) {
+    // M = R3^-1 Ur (embedded for complex), the right operand of Q2 x M
+    if (cplx) {
+      PLOM_TRY(complex_to_embed(Ur, Ue, n, bi, st));
+      PLOM_TRY((gemm_sq_nn(W3, Ue, Me, N, bi, 1, st)));
+      PLOM_TRY(embed_to_rowform(Me, F, n, bi, st));
+    } else {
+      PLOM_TRY((gemm_sq_nn(W3, Ur, Me, N, bi, 1, st)));
+      Mop = Me;
+    }
+  }
+  PLOM_TRY(sub([&] { return apply_packed(P2, Mop, N, N, U, ldu, nullptr, info, ws, st, NN, ustride); }));
+  if (!meas) {
+    PLOM_TRY((convert<double, float>(S64, S, (int64_t)n * batch, st)));
+    PLOM_TRY((convert<double, float>(VH, VT, (int64_t)n * n * cw * batch, st)));
+  }
+  ws.off = need;
+  return PLOM_OK;
+}
+
 static int tsqr_packed(const float* X, int64_t m, int n, int64_t ldx, float* Q, int64_t ldq,
                        float* R, int* info, Arena& ws, cudaStream_t st) {
   PackedCore b;
@@ -342,7 +447,7 @@ static int tsqr_packed(const float* X, int64_t m, int n, int64_t ldx, float* Q, 
   PLOM_TRY(cholqr3_packed(false, X, m, n, ldx, b, info, ws, st));
   const size_t need = ws.off;
   ws.off = mark;
-  PLOM_TRY(apply_packed(b.P2, b.W3, n, n, Q, ldq, nullptr, info, ws, st));
+  PLOM_TRY(apply_packed(b.P2, b.W3, n, n, Q, ldq, nullptr, info, ws, st, 0, 0, true));
   if (!ws.measuring()) PLOM_TRY((convert<double, float>(b.Re, R, (int64_t)n * n, st)));
   ws.off = std::max(need, ws.off);
   return PLOM_OK;
@@ -413,11 +518,11 @@ static int tsqr_svd_impl(int prec, bool cplx, const TI* X, int64_t m, int n, int
     const double* Mop;
     if (cplx) {
       PLOM_TRY(complex_to_embed(Ur, Ue, n, 1, st));
-      PLOM_TRY((gemm_nn<double, double, double, double>(b.W3, N, Ue, N, Me, N, N, N, N, st)));
+      PLOM_TRY((gemm_sq_nn(b.W3, Ue, Me, N, 1, 1, st)));
       PLOM_TRY(embed_to_rowform(Me, b.F, n, 1, st));
       Mop = b.F;
     } else {
-      PLOM_TRY((gemm_nn<double, double, double, double>(b.W3, N, Ur, N, Me, N, N, N, N, st)));
+      PLOM_TRY((gemm_sq_nn(b.W3, Ur, Me, N, 1, 1, st)));
       Mop = Me;
     }
     PLOM_TRY((tall_apply<TC, TI>(prec, b.Q2, N, m, N, Mop, N, U, ldu, info, ws, st)));
@@ -444,7 +549,7 @@ static int tsqr_impl(int prec, const TI* X, int64_t m, int n, int64_t ldx, TI* Q
   PLOM_TRY((cholqr3<TI, TC>(prec, false, X, m, n, ldx, q1_in_q ? (TC*)(void*)Q : nullptr, n, b,
                             info, ws, st)));
   size_t need = ws.off;
-  PLOM_TRY((tall_apply<TC, TI>(prec, b.Q2, n, m, n, b.W3, n, Q, ldq, info, ws, st)));
+  PLOM_TRY((tall_apply<TC, TI>(prec, b.Q2, n, m, n, b.W3, n, Q, ldq, info, ws, st, true)));
   if (!ws.measuring()) PLOM_TRY((convert<double, TI>(b.Re, R, (int64_t)n * n, st)));
   ws.off = std::max(need, ws.off);
   return PLOM_OK;
@@ -663,11 +768,75 @@ extern "C" int plom_tsqr_svd(int dtype, int prec, const void* X, int64_t m, int6
   PLOM_REQUIRE(ldx >= n && ldu >= n, PLOM_ERR_ARG, "tsqr_svd: leading dimension < n");
   PLOM_REQUIRE(X && U && S && VT && info && ws, PLOM_ERR_ARG, "tsqr_svd: null pointer");
   size_t need = plom_tsqr_svd_workspace(dtype, prec, m, n);
+  PLOM_REQUIRE(need > 0, PLOM_ERR_ARG, "tsqr_svd: workspace query failed");
   PLOM_REQUIRE(ws_bytes >= need, PLOM_ERR_WORKSPACE, "tsqr_svd: workspace %zu < required %zu",
                ws_bytes, need);
   Arena a(ws, ws_bytes);
   PLOM_CHECK_CUDA(cudaMemsetAsync(info, 0, sizeof(int) * PLOM_INFO_WORDS, (cudaStream_t)stream));
   return tsqr_svd_dispatch(dtype, prec, X, m, n, ldx, U, ldu, S, VT, info, a, (cudaStream_t)stream);
+}
+
+// batch of problems: the mixed form on FP32 / complex64 data runs batched;
+// every other form runs the single-problem driver per problem, reusing one
+// workspace.  Strides in elements of the data type.
+static int tsqr_svd_batched_dispatch(int dtype, int prec, const void* X, int64_t batch, int64_t m,
+                                     int64_t n, int64_t ldx, int64_t xstride, void* U, int64_t ldu,
+                                     int64_t ustride, void* S, void* VT, int* info, Arena& ws,
+                                     cudaStream_t st) {
+  const bool mixed32 = prec == PLOM_PREC_MIXED && (dtype == PLOM_F32 || dtype == PLOM_C64) &&
+                       m >= n && packed_ok(cdiv(m, 128) * 128 * batch);
+  if (mixed32) {
+    const int c = dtype == PLOM_C64 ? 2 : 1;
+    return tsqr_svd_batched_packed(c == 2, (const float*)X, batch, m, (int)n, c * ldx, c * xstride,
+                                   (float*)U, c * ldu, c * ustride, (float*)S, (float*)VT, info, ws,
+                                   st);
+  }
+  const size_t es = (dtype == PLOM_F32) ? 4 : (dtype == PLOM_F64 || dtype == PLOM_C64) ? 8 : 16;
+  const size_t rs = (dtype == PLOM_F32 || dtype == PLOM_C64) ? 4 : 8;
+  const size_t mark = ws.off;
+  size_t need = mark;
+  for (int64_t p = 0; p < (ws.measuring() ? 1 : batch); ++p) {
+    ws.off = mark;
+    const char* xp = X ? (const char*)X + (size_t)p * xstride * es : nullptr;
+    char* up = U ? (char*)U + (size_t)p * ustride * es : nullptr;
+    char* sp = S ? (char*)S + (size_t)p * n * rs : nullptr;
+    char* vp = VT ? (char*)VT + (size_t)p * n * n * es : nullptr;
+    PLOM_TRY(tsqr_svd_dispatch(dtype, prec, xp, m, n, ldx, up, ldu, sp, vp, info, ws, st));
+    need = std::max(need, ws.off);
+  }
+  ws.off = need;
+  return PLOM_OK;
+}
+
+extern "C" size_t plom_tsqr_svd_batched_workspace(int dtype, int prec, int64_t batch, int64_t m,
+                                                  int64_t n) {
+  size_t bytes = 0;
+  int dummy[PLOM_INFO_WORDS];
+  run_measured(&bytes, [&](Arena& a) {
+    return tsqr_svd_batched_dispatch(dtype, prec, nullptr, batch, m, n, n, m * n, nullptr, n,
+                                     m * n, nullptr, nullptr, dummy, a, 0);
+  });
+  return bytes;
+}
+
+extern "C" int plom_tsqr_svd_batched(int dtype, int prec, const void* X, int64_t batch, int64_t m,
+                                     int64_t n, int64_t ldx, int64_t xstride, void* U, int64_t ldu,
+                                     int64_t ustride, void* S, void* VT, void* ws, size_t ws_bytes,
+                                     int* info, void* stream) {
+  PLOM_REQUIRE(prec_ok(prec), PLOM_ERR_ARG, "bad precision %d", prec);
+  PLOM_REQUIRE(batch >= 1 && m >= 1 && n >= 1 && n <= 4096 && m >= n, PLOM_ERR_ARG,
+               "tsqr_svd_batched: need batch >= 1 and 1 <= n <= min(m, 4096)");
+  PLOM_REQUIRE(ldx >= n && ldu >= n && xstride >= m * ldx && ustride >= m * ldu, PLOM_ERR_ARG,
+               "tsqr_svd_batched: leading dimension or stride too small");
+  PLOM_REQUIRE(X && U && S && VT && info && ws, PLOM_ERR_ARG, "tsqr_svd_batched: null pointer");
+  size_t need = plom_tsqr_svd_batched_workspace(dtype, prec, batch, m, n);
+  PLOM_REQUIRE(need > 0, PLOM_ERR_ARG, "tsqr_svd_batched: workspace query failed");
+  PLOM_REQUIRE(ws_bytes >= need, PLOM_ERR_WORKSPACE, "tsqr_svd_batched: workspace %zu < %zu",
+               ws_bytes, need);
+  Arena a(ws, ws_bytes);
+  PLOM_CHECK_CUDA(cudaMemsetAsync(info, 0, sizeof(int) * PLOM_INFO_WORDS, (cudaStream_t)stream));
+  return tsqr_svd_batched_dispatch(dtype, prec, X, batch, m, n, ldx, xstride, U, ldu, ustride, S,
+                                   VT, info, a, (cudaStream_t)stream);
 }
 
 static int tsqr_dispatch(int dtype, int prec, const void* X, int64_t m, int64_t n, int64_t ldx,
@@ -703,6 +872,7 @@ extern "C" int plom_tsqr(int dtype, int prec, const void* X, int64_t m, int64_t 
   PLOM_REQUIRE(ldx >= n && ldq >= n, PLOM_ERR_ARG, "tsqr: leading dimension < n");
   PLOM_REQUIRE(X && Q && R && info && ws, PLOM_ERR_ARG, "tsqr: null pointer");
   size_t need = plom_tsqr_workspace(dtype, prec, m, n);
+  PLOM_REQUIRE(need > 0, PLOM_ERR_ARG, "tsqr: workspace query failed");
   PLOM_REQUIRE(ws_bytes >= need, PLOM_ERR_WORKSPACE, "tsqr: workspace %zu < required %zu",
                ws_bytes, need);
   Arena a(ws, ws_bytes);
@@ -748,6 +918,7 @@ extern "C" int plom_randomized_svd(int dtype, int prec, const void* X, int64_t m
   PLOM_REQUIRE(ldx >= n && ldu >= r, PLOM_ERR_ARG, "randomized_svd: leading dimension too small");
   PLOM_REQUIRE(X && U && S && VT && info && ws, PLOM_ERR_ARG, "randomized_svd: null pointer");
   size_t need = plom_randomized_svd_workspace(dtype, prec, m, n, r);
+  PLOM_REQUIRE(need > 0, PLOM_ERR_ARG, "randomized_svd: workspace query failed");
   PLOM_REQUIRE(ws_bytes >= need, PLOM_ERR_WORKSPACE, "randomized_svd: workspace %zu < %zu",
                ws_bytes, need);
   Arena a(ws, ws_bytes);
@@ -820,6 +991,7 @@ extern "C" int plom_matmul(int dtype, int prec, int transA, const void* A, int64
                "matmul: leading dimension too small");
   PLOM_REQUIRE((A && B && C) || m * n == 0, PLOM_ERR_ARG, "matmul: null pointer");
   size_t need = plom_matmul_workspace(dtype, prec, transA, m, n, k);
+  PLOM_REQUIRE(need > 0, PLOM_ERR_ARG, "matmul: workspace query failed");
   PLOM_REQUIRE(ws_bytes >= need, PLOM_ERR_WORKSPACE, "matmul: workspace %zu < %zu", ws_bytes,
                need);
   Arena a(ws, ws_bytes);

@@ -210,6 +210,32 @@ def tsqr_svd_device(x, ld, precision=None, info_out=None):
     return U, S, V
 
 
+def tsqr_svd_batched_device(x3, precision=None, info_out=None):
+    """TSQR-SVD of each matrix of a (batch, m, n) CUDA tensor (m >= n, unit
+    inner stride, equal strides between matrices) -> U (batch, m, n), S
+    (batch, n), V (batch, n, n) holding V^T.  The mixed form on float32 /
+    complex64 data runs every stage as one launch over the batch."""
+    t = L.torch()
+    b, m, n = x3.shape
+    if x3.stride(2) != 1 or (b > 1 and x3.stride(0) < m * x3.stride(1)):
+        x3 = x3.contiguous()
+    dt = L.dtype_code(x3)
+    prec = L.precision_code(precision, x3)
+    U = t.empty((b, m, n), dtype=x3.dtype, device="cuda")
+    S = t.empty((b, n), dtype=L.real_dtype(x3), device="cuda")
+    V = t.empty((b, n, n), dtype=x3.dtype, device="cuda")
+    ws = L.workspace(L.load().plom_tsqr_svd_batched_workspace(dt, prec, b, m, n))
+    info = L.new_info()
+    L.call("plom_tsqr_svd_batched", dt, prec, L.ptr(x3), b, m, n, x3.stride(1),
+           x3.stride(0) if b > 1 else m * x3.stride(1), L.ptr(U), n, m * n, L.ptr(S), L.ptr(V),
+           L.ptr(ws), ws.numel(), L.ptr(info), L.stream_ptr())
+    if info_out is None:
+        L.check_info(info, "tsqr_svd_batched")
+    else:
+        info_out.append(info)
+    return U, S, V
+
+
 def tsqr_svd(Ai, *, precision=None):
     """U, S, V = tsqr_svd(A): A (m x n) = U diag(S) V with U m x n, S n
     descending, V n x n holding V^T (pyLOM/vmmath/svd.py:228)."""

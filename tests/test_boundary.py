@@ -77,6 +77,9 @@ def test_workspace_dry_runs_launch_nothing(dtype, prec):
     lib = L.load()
     for m, n in [(16384, 200), (8388608, 1024), (5, 1), (1000, 33), (300, 64)]:
         assert lib.plom_tsqr_svd_workspace(dtype, prec, m, n) > 0, lib.plom_last_error_string()
+    for b, m, n in [(1, 2500, 24), (5, 2500, 24), (129, 65536, 63), (3, 5, 1)]:
+        assert lib.plom_tsqr_svd_batched_workspace(dtype, prec, b, m, n) > 0, \
+            lib.plom_last_error_string()
     if dtype in (0, 1):
         assert lib.plom_tsqr_workspace(dtype, prec, 4000, 50) > 0
         assert lib.plom_randomized_svd_workspace(dtype, prec, 3000, 120, 16) > 0

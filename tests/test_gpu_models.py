@@ -146,6 +146,24 @@ def test_spod_defaults_golden(golden):
     np.testing.assert_allclose(Lm, g["L"], rtol=1e-4, atol=1e-6 * g["L"].max())
 
 
+@pytest.mark.parametrize("dt", [torch.complex64, torch.complex128])
+@pytest.mark.parametrize("G,M,nBlks,nf,f0", [(5, 1000, 63, 9, 3), (1, 77, 8, 4, 0), (16, 300, 64, 16, 0)])
+def test_spod_mode_layout(dt, G, M, nBlks, nf, f0):
+    """P[(b M + i) nf + f0 + g] = Re U_g[i][b] (pyLOM's Fortran-order columns)."""
+    from pyloworder_gb300 import _lib as L
+    g = torch.Generator(device="cuda")
+    g.manual_seed(G * 1000 + M)
+    U = torch.randn((G, M, nBlks), dtype=dt, device="cuda", generator=g)
+    rdt = torch.float32 if dt == torch.complex64 else torch.float64
+    Pm = torch.full((M * nBlks, nf), -7.0, dtype=rdt, device="cuda")
+    L.call("plom_spod_modes", L.dtype_code(Pm), L.ptr(U), G, M, nBlks,
+           M * nBlks, L.ptr(Pm), nf, f0, L.stream_ptr())
+    ref = torch.full((M * nBlks, nf), -7.0, dtype=rdt, device="cuda")
+    for k in range(G):
+        ref[:, f0 + k] = U[k].real.T.reshape(-1)
+    assert torch.equal(Pm, ref)
+
+
 @pytest.mark.parametrize("nDFT,nolap", [(64, 32), (50, 10), (10, 2), (256, 128)])
 def test_spod_fft_stage(nDFT, nolap):
     rng = np.random.default_rng(nDFT)

@@ -243,3 +243,29 @@ def test_torch_in_torch_out():
     assert all(isinstance(t, torch.Tensor) and t.is_cuda for t in (U, S, V))
     Xc = X - X.mean(dim=1, keepdim=True)
     np.testing.assert_allclose(((U * S) @ V).cpu().numpy(), Xc.cpu().numpy(), atol=1e-11)
+
+
+@pytest.mark.parametrize("cplx", [False, True])
+@pytest.mark.parametrize("precision", ["mixed", "fp64"])
+def test_tsqr_svd_batched(cplx, precision):
+    """Batched API: every problem of the batch against numpy's SVD."""
+    rng = np.random.default_rng(21 + cplx)
+    b, m, n = 5, 2500, 24
+    spread = np.logspace(0, -2, n)
+    A = rng.standard_normal((b, m, n)) * spread
+    if cplx:
+        A = A + 1j * rng.standard_normal((b, m, n)) * spread
+    dt = (np.complex64 if cplx else np.float32) if precision == "mixed" else (
+        np.complex128 if cplx else np.float64)
+    A = A.astype(dt)
+    x = torch.tensor(A, device="cuda")
+    U, S, V = P.vmmath.tsqr_svd_batched_device(x, precision)
+    U, S, V = U.cpu().numpy(), S.cpu().numpy(), V.cpu().numpy()
+    tol = 1e-5 if precision == "mixed" else 1e-12
+    for p in range(b):
+        A64 = A[p].astype(np.complex128 if cplx else np.float64)
+        Sr = np.linalg.svd(A64, compute_uv=False)
+        assert sigma_rel(S[p], Sr) < tol
+        assert orthogonality(U[p].astype(A64.dtype)) < tol * 10
+        rec = (U[p].astype(A64.dtype) * S[p]) @ V[p].astype(A64.dtype)
+        assert np.linalg.norm(rec - A64) / np.linalg.norm(A64) < tol * 10
