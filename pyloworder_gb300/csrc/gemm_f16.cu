@@ -383,6 +383,12 @@ __global__ void __launch_bounds__(256) split_w16_kernel(const double* __restrict
 #ifndef PLOM_GRAM_KSUB
 #define PLOM_GRAM_KSUB 4096
 #endif
+// row chunks of the Gram: the fewest whole waves of CTAs that split evenly
+// into tiles, times this factor (shorter chunks keep the tiles that share a
+// row panel closer together in time, so more of the panel re-reads hit L2)
+#ifndef PLOM_GRAM_WAVE_MULT
+#define PLOM_GRAM_WAVE_MULT 8
+#endif
 constexpr int G_BK = PLOM_GRAM_BK;             // rows per stage (a multiple of 16)
 constexpr uint32_t G_BOX = G_BK * 128;         // G_BK rows x 64 fp16
 constexpr uint32_t G_TILE = 2 * G_BOX;         // G_BK rows x 128 columns of one plane
@@ -688,13 +694,16 @@ __global__ void __launch_bounds__(192, 1)
     apply16_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
                    int64_t m, int kblocks, int k, int64_t col_tiles, int64_t tiles,
                    const float* __restrict__ f, ApplyOut out, int* err, int64_t mp,
-                   int64_t row_tiles, int fstride, int upper) {
+                   int64_t row_tiles, int fstride, int upper, int by_rows) {
   // tile t -> (problem pb, row block rb, column block cb); a problem's rows are
-  // mp apart in the packed planes (input and packed output alike).  CTA x takes
-  // tile r G + x in even rounds r and r G + (G - 1 - x) in odd ones, so with
-  // an upper-triangular W (upper != 0: column block cb needs only the first
-  // (cb + 1) 128 rows of W, the K blocks below 2 (cb + 1)) the long and short
-  // column blocks alternate on every CTA.
+  // mp apart in the packed planes (input and packed output alike).  With an
+  // upper-triangular W (upper != 0) column block cb needs only the first
+  // (cb + 1) 128 rows of W: the K blocks below 2 (cb + 1).
+  // by_rows: CTA x takes whole row blocks (every column tile of row blocks x,
+  // x + G, ...), so the column tiles that re-read a row block's input follow
+  // each other on one SM (L2 hits) and every CTA gets the same work per row
+  // block.  Otherwise it takes single tiles, tile r G + x in even rounds r and
+  // r G + (G - 1 - x) in odd ones.
   extern __shared__ uint8_t smem_raw[];
   __shared__ uint64_t full_bar[A_STAGES], empty_bar[A_STAGES], tfull[2], tempty[2];
   __shared__ uint32_t tmem_sh;
@@ -702,8 +711,16 @@ __global__ void __launch_bounds__(192, 1)
   const uint32_t base = (smem_u32(smem_raw) + 1023u) & ~1023u;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int64_t G = gridDim.x;
-  auto apply_tile = [&](int64_t r) -> int64_t {
-    return r * G + ((r & 1) ? G - 1 - blockIdx.x : (int64_t)blockIdx.x);
+  const int64_t units = tiles / col_tiles;  // row blocks over the batch
+  // tiles of this CTA (by rows), or rounds of G tiles (a round's tile past the
+  // end is skipped)
+  const int64_t my_tiles =
+      by_rows ? (blockIdx.x < units ? ((units - 1 - blockIdx.x) / G + 1) * col_tiles : 0)
+              : (tiles + G - 1) / G;
+  // it-th tile of this CTA (it < my_tiles)
+  auto apply_tile = [&](int64_t it) -> int64_t {
+    if (by_rows) return (blockIdx.x + (it / col_tiles) * G) * col_tiles + it % col_tiles;
+    return it * G + ((it & 1) ? G - 1 - blockIdx.x : (int64_t)blockIdx.x);
   };
   auto apply_kend = [&](int cb) -> int {
     return upper ? min(kblocks, (cb + 1) * (128 / A_BK)) : kblocks;
@@ -740,8 +757,8 @@ __global__ void __launch_bounds__(192, 1)
     if (lane == 0) {
       int64_t g = 0;
       bool ok = true;
-      for (int64_t r = 0; r * gridDim.x < tiles && ok; ++r) {
-        const int64_t t = apply_tile(r);
+      for (int64_t it = 0; it < my_tiles && ok; ++it) {
+        const int64_t t = apply_tile(it);
         if (t >= tiles) continue;
         const int64_t pb = t / (row_tiles * col_tiles);
         const int64_t rt = t - pb * row_tiles * col_tiles;
@@ -771,8 +788,8 @@ __global__ void __launch_bounds__(192, 1)
       int64_t g = 0;
       int i = 0;
       bool ok = true;
-      for (int64_t r = 0; r * gridDim.x < tiles && ok; ++r) {
-        const int64_t t = apply_tile(r);
+      for (int64_t it = 0; it < my_tiles && ok; ++it) {
+        const int64_t t = apply_tile(it);
         if (t >= tiles) continue;
         const int b = i & 1;
         if (!mbar_wait(&tempty[b], (((uint32_t)i >> 1) & 1u) ^ 1u, &abort_sh, err)) {
@@ -815,8 +832,8 @@ __global__ void __launch_bounds__(192, 1)
     uint4* stg = reinterpret_cast<uint4*>(smem_raw + (base - smem_u32(smem_raw)) +
                                           A_STAGES * A_STAGE + warp * 4096);
     int i = 0;
-    for (int64_t r = 0; r * gridDim.x < tiles; ++r) {
-      const int64_t t = apply_tile(r);
+    for (int64_t it = 0; it < my_tiles; ++it) {
+      const int64_t t = apply_tile(it);
       if (t >= tiles) continue;
       const int b = i & 1;
       const bool ready = mbar_wait(&tfull[b], ((uint32_t)i >> 1) & 1u, &abort_sh, err);
@@ -907,6 +924,91 @@ __global__ void __launch_bounds__(192, 1)
     __syncwarp();
     fence_after();
     tmem_dealloc(tmem, 512);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// renormalisation of long-factor columns of U = Q2 M (see renorm_long_columns)
+// ---------------------------------------------------------------------------
+constexpr int RN_MAX = 8;  // columns per problem
+
+// one block per problem: list the columns j with ||M e_(cw j)||^2 > thr2
+__global__ void __launch_bounds__(256) rn_flag_kernel(const double* __restrict__ M, int N, int n,
+                                                      int cw, int64_t mstride, double thr2,
+                                                      int* __restrict__ list, int* __restrict__ count,
+                                                      double* __restrict__ sums) {
+  const int b = blockIdx.x;
+  const double* Mb = M + (int64_t)b * mstride;
+  if (threadIdx.x == 0) count[b] = 0;
+  if (threadIdx.x < RN_MAX) sums[b * RN_MAX + threadIdx.x] = 0.0;
+  __syncthreads();
+  for (int j = threadIdx.x; j < n; j += blockDim.x) {
+    double s = 0.0;
+    for (int i = 0; i < N; ++i) {
+      const double v = Mb[(int64_t)i * N + (int64_t)cw * j];
+      s = fma(v, v, s);
+    }
+    if (s > thr2) {
+      const int k = atomicAdd(&count[b], 1);
+      if (k < RN_MAX) list[b * RN_MAX + k] = j;
+    }
+  }
+}
+
+// sums of squares of the listed columns (FP32 per thread over a few hundred
+// rows, FP64 across threads)
+__global__ void __launch_bounds__(256) rn_sumsq_kernel(const float* __restrict__ U, int64_t m,
+                                                       int64_t ldu, int cw, int64_t ustride,
+                                                       const int* __restrict__ list,
+                                                       const int* __restrict__ count,
+                                                       double* __restrict__ sums) {
+  const int b = blockIdx.y;
+  const int d = min(count[b], RN_MAX);
+  if (d == 0) return;
+  const float* Ub = U + (int64_t)b * ustride;
+  __shared__ double red[RN_MAX][8];
+  for (int c = 0; c < d; ++c) {
+    const int64_t col = (int64_t)cw * list[b * RN_MAX + c];
+    float acc = 0.f;
+    for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < m;
+         r += (int64_t)gridDim.x * blockDim.x) {
+      const float x = Ub[r * ldu + col];
+      acc = fmaf(x, x, acc);
+      if (cw == 2) {
+        const float y = Ub[r * ldu + col + 1];
+        acc = fmaf(y, y, acc);
+      }
+    }
+    double v = (double)acc;
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if ((threadIdx.x & 31) == 0) red[c][threadIdx.x >> 5] = v;
+  }
+  __syncthreads();
+  if (threadIdx.x < d) {
+    double t = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += red[threadIdx.x][w];
+    atomicAdd(&sums[b * RN_MAX + threadIdx.x], t);
+  }
+}
+
+__global__ void __launch_bounds__(256) rn_scale_kernel(float* __restrict__ U, int64_t m,
+                                                       int64_t ldu, int cw, int64_t ustride,
+                                                       const int* __restrict__ list,
+                                                       const int* __restrict__ count,
+                                                       const double* __restrict__ sums) {
+  const int b = blockIdx.y;
+  const int d = min(count[b], RN_MAX);
+  float* Ub = U + (int64_t)b * ustride;
+  for (int c = 0; c < d; ++c) {
+    const double s2 = sums[b * RN_MAX + c];
+    if (!(s2 > 0.0)) continue;
+    const float f = (float)(1.0 / sqrt(s2));
+    const int64_t col = (int64_t)cw * list[b * RN_MAX + c];
+    for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < m;
+         r += (int64_t)gridDim.x * blockDim.x) {
+      Ub[r * ldu + col] *= f;
+      if (cw == 2) Ub[r * ldu + col + 1] *= f;
+    }
   }
 }
 
@@ -1017,7 +1119,7 @@ static int gram16_chunks(int64_t m, int tiles) {
   const int64_t sms = num_sms();
   const int64_t maxc = std::max<int64_t>(1, cdiv(m, 4 * hp::G_BK));
   for (int64_t waves = 1; waves <= 64; ++waves) {
-    const int64_t items = waves * sms;
+    const int64_t items = waves * sms * PLOM_GRAM_WAVE_MULT;
     if (items % tiles) continue;
     return (int)std::max<int64_t>(1, std::min(maxc, items / tiles));
   }
@@ -1151,7 +1253,12 @@ int apply_packed(const Packed& p, const double* W, int64_t ldw, int64_t k, float
                PLOM_ERR_CUDA, "apply16: tensor map encoding failed");
   const int64_t row_tiles = cdiv(p.mp, 128);
   const int64_t tiles = batch * row_tiles * col_tiles;
-  const int grid = (int)std::min<int64_t>(tiles, num_sms());
+  // whole row blocks per CTA pay for the triangular case (column tiles of very
+  // different lengths); the dense case keeps concurrent tiles of one row
+  // block on different SMs (fewer DRAM re-reads)
+  const bool tri_pre = upper && k == p.N;
+  const int by_rows = (tri_pre && batch * row_tiles >= 2 * num_sms()) ? 1 : 0;
+  const int grid = (int)std::min<int64_t>(by_rows ? batch * row_tiles : tiles, num_sms());
   hp::ApplyOut o;
   o.C = out ? nullptr : C;
   o.ldc = ldc;
@@ -1161,12 +1268,44 @@ int apply_packed(const Packed& p, const double* W, int64_t ldw, int64_t k, float
   o.ldo = out ? (int)out->ld : 0;
   // an upper-triangular W (k = N) needs m N (N + 1) flops: row i of W meets
   // columns j >= i only
-  const bool tri = upper && k == p.N;
+  const bool tri = tri_pre;
   const double flops = tri ? (double)m * p.N * (p.N + 1) * batch : 2.0 * m * p.N * k * batch;
   ProfScope prof("tc_apply_f16x3", st, flops, 4.0 * ((double)m * p.ld + (double)m * k) * batch);
   hp::apply16_kernel<<<grid, 192, hp::A_SMEM, st>>>(tmA, tmB, m, (int)(ldk / 64), (int)k,
                                                     col_tiles, tiles, f, o, err, p.mp, row_tiles,
-                                                    fstride, tri ? 1 : 0);
+                                                    fstride, tri ? 1 : 0, by_rows);
+  PLOM_CHECK_LAUNCH();
+  return PLOM_OK;
+}
+
+}  // namespace plom
+
+namespace plom {
+
+// U = Q2 M in the mixed form: a column of M much longer than 1 means R3^-1
+// is large in a direction that Q2 barely spans -- X is numerically
+// rank-deficient below the 22-bit operand precision (e.g. the null vector of
+// mean-removed snapshots) -- and the FP32 product loses that column's unit
+// norm (its orthogonality to the other columns stays at the operand level).
+// Such columns (up to 8 per problem, ||M e_j|| > 4) are renormalised in the
+// tall space: two strided passes over one column each.
+int renorm_long_columns(const double* M, int N, int n, int cw, float* U, int64_t m, int64_t ldu,
+                        int batch, int64_t mstride, int64_t ustride, Arena& ws, cudaStream_t st) {
+  int* list = ws.take<int>((size_t)batch * hp::RN_MAX);
+  int* count = ws.take<int>((size_t)batch);
+  double* sums = ws.take<double>((size_t)batch * hp::RN_MAX);
+  if (ws.measuring()) return PLOM_OK;
+  PLOM_REQUIRE(!ws.overflow(), PLOM_ERR_WORKSPACE, "renorm: workspace too small");
+  PLOM_REQUIRE(M && U && batch >= 1 && batch <= 65535, PLOM_ERR_ARG, "renorm: bad arguments");
+  ProfScope prof("renorm_cols", st, 0.0, 8.0 * (double)m * batch, 3);
+  hp::rn_flag_kernel<<<batch, 256, 0, st>>>(M, N, n, cw, mstride, 16.0, list, count, sums);
+  PLOM_CHECK_LAUNCH();
+  const unsigned gx = (unsigned)std::max<int64_t>(1, std::min<int64_t>(cdiv(m, 256), (int64_t)num_sms() * 4));
+  hp::rn_sumsq_kernel<<<dim3(gx, (unsigned)batch), 256, 0, st>>>(U, m, ldu, cw, ustride, list, count,
+                                                                sums);
+  PLOM_CHECK_LAUNCH();
+  hp::rn_scale_kernel<<<dim3(gx, (unsigned)batch), 256, 0, st>>>(U, m, ldu, cw, ustride, list, count,
+                                                                sums);
   PLOM_CHECK_LAUNCH();
   return PLOM_OK;
 }

@@ -44,4 +44,10 @@ int apply_packed(const Packed& p, const double* W, int64_t ldw, int64_t k, float
                  Packed* out, int* err, Arena& ws, cudaStream_t st, int64_t wstride = 0,
                  int64_t cstride = 0, bool upper = false);
 
+// U = Q2 M (m x cw*n FP32, ldu; a batch: U_p ustride, M_p mstride apart):
+// renormalise the columns whose M column (N x N, real or embedded complex)
+// is longer than 4
+int renorm_long_columns(const double* M, int N, int n, int cw, float* U, int64_t m, int64_t ldu,
+                        int batch, int64_t mstride, int64_t ustride, Arena& ws, cudaStream_t st);
+
 }  // namespace plom

@@ -84,6 +84,9 @@ static int tall_apply(int prec, const TA* A, int64_t lda, int64_t m, int64_t N, 
 
 // Shifts are passed to the Cholesky relative to trace(G)/N; the absolute
 // shift is s = c u trace(G) (trace(G) = ||X||_F^2 >= ||X||_2^2).
+#ifndef PLOM_MIXED_SHIFT
+#define PLOM_MIXED_SHIFT 16
+#endif
 static void shifts_for(int prec, int64_t m, int64_t N, double& rel1, double& relfail) {
   const double u = (prec == PLOM_PREC_FP64) ? U64 : U32;
   const double n = (double)N;
@@ -91,7 +94,7 @@ static void shifts_for(int prec, int64_t m, int64_t N, double& rel1, double& rel
   // escalated on breakdown (the bound grows with m far past what the FP64
   // partial-Gram summation needs).
   const double c1 = (prec == PLOM_PREC_FP64) ? std::max(11.0 * ((double)m * n + n * (n + 1.0)), 4.0)
-                                             : 16.0;
+                                             : (double)PLOM_MIXED_SHIFT;
   rel1 = c1 * u * n;
   relfail = 16.0 * u * n;
 }
@@ -326,6 +329,7 @@ static int tsqr_svd_packed(bool cplx, const float* X, int64_t m, int n, int64_t 
     }
   }
   PLOM_TRY(apply_packed(b.P2, Mop, N, N, U, ldu, nullptr, info, ws, st));
+  PLOM_TRY(renorm_long_columns(Me, N, n, cw, U, m, ldu, 1, 0, 0, ws, st));
   if (!ws.measuring()) {
     PLOM_TRY((convert<double, float>(S64, S, n, st)));
     PLOM_TRY((convert<double, float>(VH, VT, (int64_t)n * n * cw, st)));
@@ -429,7 +433,10 @@ static int tsqr_svd_batched_packed(bool cplx, const float* X, int64_t batch, int
       Mop = Me;
     }
   }
-  PLOM_TRY(sub([&] { return apply_packed(P2, Mop, N, N, U, ldu, nullptr, info, ws, st, NN, ustride); }));
+  PLOM_TRY(sub([&] {
+    PLOM_TRY(apply_packed(P2, Mop, N, N, U, ldu, nullptr, info, ws, st, NN, ustride));
+    return renorm_long_columns(Me, N, n, cw, U, m, ldu, bi, NN, ustride, ws, st);
+  }));
   if (!meas) {
     PLOM_TRY((convert<double, float>(S64, S, (int64_t)n * batch, st)));
     PLOM_TRY((convert<double, float>(VH, VT, (int64_t)n * n * cw * batch, st)));

@@ -108,6 +108,24 @@ def test_pod_f32_nomean_golden(golden):
     assert subspace_angle(U[:, :9], ref[0][:, :9]) < 1e-4
 
 
+def test_mixed_mean_removed_u_orthonormal():
+    """Mean-removed snapshots have an exact null vector (X 1 = 0), far below
+    the mixed form's 22-bit operand precision; every column of U, including
+    the null one, must still come out orthonormal."""
+    from pyloworder_gb300 import datagen
+    m, n = 262144, 256
+    nx, ny = datagen.grid_for_points(m)
+    X = datagen.pod_field_device(nx, ny, n, 32, seed=77, noise=1e-5, amp_pow=1.5, m=m)
+    Y, _, _ = P.vmmath.remove_mean_device(X, n)
+    U, S, V = P.vmmath.tsqr_svd_device(Y, n, "mixed")
+    Ud = U.double()
+    D = Ud.T @ Ud - torch.eye(n, dtype=torch.float64, device="cuda")
+    assert float(S[-1] / S[0]) < 1e-6          # the null direction is there
+    assert float(D.abs().max()) < 1e-4
+    Vd = V.double()
+    assert float((Vd @ Vd.T - torch.eye(n, dtype=torch.float64, device="cuda")).abs().max()) < 1e-6
+
+
 def test_randomized_philox_matches_oracle():
     rng = np.random.default_rng(5)
     X = (rng.standard_normal((3000, 12)) @ rng.standard_normal((12, 120))
