@@ -122,6 +122,16 @@ int plom_tsqr_svd(int dtype, int prec, const void* X, int64_t m, int64_t n, int6
    per-frequency SVDs of SPOD (pyLOM/SPOD/wrapper.py:75-85 calls tsqr_svd once
    per frequency).  The mixed form on F32/C64 data runs every stage as one
    launch over the batch; the other forms run the problems one by one. */
+/* plom_tsqr_svd with X, U, S, VT in HOST memory (page-locked memory lets
+   the copies overlap the GPU work; pageable memory works too).  The same
+   pyLOM interface (svd.py:228); the call streams X to the device in row
+   chunks on an internal copy stream, overlapping the first pass, and copies
+   U, S, VT back on `stream`.  m >= n. */
+size_t plom_tsqr_svd_host_workspace(int dtype, int prec, int64_t m, int64_t n);
+int plom_tsqr_svd_host(int dtype, int prec, const void* X, int64_t m, int64_t n, int64_t ldx,
+                       void* U, int64_t ldu, void* S, void* VT, void* ws, size_t ws_bytes,
+                       int* info, void* stream);
+
 size_t plom_tsqr_svd_batched_workspace(int dtype, int prec, int64_t batch, int64_t m, int64_t n);
 int plom_tsqr_svd_batched(int dtype, int prec, const void* X, int64_t batch, int64_t m, int64_t n,
                           int64_t ldx, int64_t xstride, void* U, int64_t ldu, int64_t ustride,

@@ -54,6 +54,9 @@ PROTOS = {
     "plom_tsqr_svd": (c_int, [c_int, c_int, c_vp, c_i64, c_i64, c_i64, c_vp, c_i64, c_vp, c_vp, c_vp,
                               c_sz, c_vp, c_vp]),
     "plom_spod_modes": (c_int, [c_int, c_vp, c_i64, c_i64, c_i64, c_i64, c_vp, c_i64, c_i64, c_vp]),
+    "plom_tsqr_svd_host_workspace": (c_sz, [c_int, c_int, c_i64, c_i64]),
+    "plom_tsqr_svd_host": (c_int, [c_int, c_int, c_vp, c_i64, c_i64, c_i64, c_vp, c_i64, c_vp, c_vp,
+                                   c_vp, c_sz, c_vp, c_vp]),
     "plom_tsqr_svd_batched_workspace": (c_sz, [c_int, c_int, c_i64, c_i64, c_i64]),
     "plom_tsqr_svd_batched": (c_int, [c_int, c_int, c_vp, c_i64, c_i64, c_i64, c_i64, c_i64, c_vp,
                                       c_i64, c_i64, c_vp, c_vp, c_vp, c_sz, c_vp, c_vp]),

@@ -387,7 +387,7 @@ __global__ void __launch_bounds__(256) split_w16_kernel(const double* __restrict
 // into tiles, times this factor (shorter chunks keep the tiles that share a
 // row panel closer together in time, so more of the panel re-reads hit L2)
 #ifndef PLOM_GRAM_WAVE_MULT
-#define PLOM_GRAM_WAVE_MULT 8
+#define PLOM_GRAM_WAVE_MULT 4
 #endif
 constexpr int G_BK = PLOM_GRAM_BK;             // rows per stage (a multiple of 16)
 constexpr uint32_t G_BOX = G_BK * 128;         // G_BK rows x 64 fp16
@@ -647,7 +647,7 @@ __global__ void tn16_reduce_kernel(const double* __restrict__ part, int Na, int 
 // G[i][j] = sum over chunks of the tile partials (fixed order) / (s_i s_j), mirrored
 __global__ void gram16_reduce_kernel(const double* __restrict__ part, int N, int tn, int chunks,
                                      const float* __restrict__ s, double* __restrict__ G,
-                                     int batch, int ld) {
+                                     int batch, int ld, int accumulate) {
   const int64_t total = (int64_t)N * N * batch;
   const int ntiles = tn * (tn + 1) / 2;
   for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < total;
@@ -667,7 +667,8 @@ __global__ void gram16_reduce_kernel(const double* __restrict__ part, int N, int
     double acc = 0.0;
     for (int c = 0; c < chunks; ++c) acc += p[(int64_t)c * 128 * 128];
     const float* sp = s + pb * ld;
-    G[e] = acc / ((double)sp[i] * (double)sp[j]);
+    const double v = acc / ((double)sp[i] * (double)sp[j]);
+    G[e] = accumulate ? G[e] + v : v;
   }
 }
 
@@ -1033,13 +1034,17 @@ static PFN_cuTensorMapEncodeTiled_v12000 encode_fn16() {
 
 // 3-D fp16 map over two planes of `rows` x `inner` (row pitch ld elements),
 // 128-byte swizzle, zero fill out of bounds
+// planes as a 3-D tensor {inner, rows, 2}; pstride: elements from the hi to the
+// lo plane (0: rows * ld, planes back to back)
 static bool make_map_planes(CUtensorMap* map, const __half* base, uint64_t inner, uint64_t rows,
-                            uint64_t ld, uint32_t box_inner, uint32_t box_rows) {
+                            uint64_t ld, uint32_t box_inner, uint32_t box_rows,
+                            uint64_t pstride = 0) {
   PFN_cuTensorMapEncodeTiled_v12000 fn = encode_fn16();
   if (!fn) return false;
-  if ((reinterpret_cast<uintptr_t>(base) & 15) || ((ld * 2) & 15)) return false;
+  if (pstride == 0) pstride = ld * rows;
+  if ((reinterpret_cast<uintptr_t>(base) & 15) || ((ld * 2) & 15) || ((pstride * 2) & 15)) return false;
   cuuint64_t dims[3] = {inner, rows, 2};
-  cuuint64_t strides[2] = {ld * 2, ld * 2 * rows};
+  cuuint64_t strides[2] = {ld * 2, pstride * 2};
   cuuint32_t box[3] = {box_inner, box_rows, 1};
   cuuint32_t estr[3] = {1, 1, 1};
   CUresult r = fn(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 3, const_cast<__half*>(base), dims,
@@ -1063,6 +1068,18 @@ void packed_carve(Arena& ws, Packed& p, int64_t m, int64_t N, int64_t batch) {
   p.hi = ws.take<__half>((size_t)(2 * batch * p.mp * p.ld));
   p.lo = p.hi ? p.hi + batch * p.mp * p.ld : nullptr;
   p.scale = ws.take<float>((size_t)(batch * p.ld));
+}
+
+Packed packed_rows_view(const Packed& p, int64_t r0, int64_t rows, int64_t mp, float* scale) {
+  Packed v = p;
+  v.pstride = p.pstride ? p.pstride : p.batch * p.mp * p.ld;
+  v.hi = p.hi ? p.hi + r0 * p.ld : nullptr;
+  v.lo = p.lo ? p.lo + r0 * p.ld : nullptr;
+  v.scale = scale;
+  v.m = rows;
+  v.mp = mp;
+  v.batch = 1;
+  return v;
 }
 
 void packed_view(Packed& p, void* storage, int64_t m, int64_t N, float* scale, int64_t batch) {
@@ -1126,7 +1143,8 @@ static int gram16_chunks(int64_t m, int tiles) {
   return (int)std::max<int64_t>(1, std::min<int64_t>(maxc, cdiv(2 * sms, tiles)));
 }
 
-int gram_packed(const Packed& p, double* G, int* err, Arena& ws, cudaStream_t st) {
+int gram_packed(const Packed& p, double* G, int* err, Arena& ws, cudaStream_t st,
+                bool accumulate) {
   const int64_t m = p.m, N = p.N, batch = p.batch;
   const int tn = (int)cdiv(p.ld, 128);
   const int tiles = tn * (tn + 1) / 2;
@@ -1152,7 +1170,7 @@ int gram_packed(const Packed& p, double* G, int* err, Arena& ws, cudaStream_t st
   }
   CUtensorMap tm;
   PLOM_REQUIRE(make_map_planes(&tm, p.hi, (uint64_t)p.ld, (uint64_t)(batch * p.mp),
-                               (uint64_t)p.ld, 64, hp::G_BK),
+                               (uint64_t)p.ld, 64, hp::G_BK, (uint64_t)p.pstride),
                PLOM_ERR_CUDA, "gram16: tensor map encoding failed");
   ProfScope prof_g("tc_gram_f16x3", st, (double)m * N * N * batch, 4.0 * (double)m * p.ld * batch);
   hp::gram16_kernel<true><<<(unsigned)(batch * tiles * chunks_eff), 320, hp::G_SMEM, st>>>(
@@ -1162,7 +1180,7 @@ int gram_packed(const Packed& p, double* G, int* err, Arena& ws, cudaStream_t st
   const int blocks = (int)std::min<int64_t>(cdiv(total, 256), (int64_t)num_sms() * 16);
   ProfScope prof_r("gram_reduce", st, 0.0, 8.0 * (double)batch * tiles * chunks_eff * 128 * 128);
   hp::gram16_reduce_kernel<<<blocks, 256, 0, st>>>(part, (int)N, tn, chunks_eff, p.scale, G,
-                                                   (int)batch, (int)p.ld);
+                                                   (int)batch, (int)p.ld, accumulate ? 1 : 0);
   PLOM_CHECK_LAUNCH();
   return PLOM_OK;
 }
@@ -1190,8 +1208,10 @@ int tn_packed(const Packed& a, const Packed& b, double* C, int64_t ldc, int* err
     attr = true;
   }
   CUtensorMap ta, tb;
-  PLOM_REQUIRE(make_map_planes(&ta, a.hi, (uint64_t)a.ld, (uint64_t)m, (uint64_t)a.ld, 64, hp::G_BK) &&
-                   make_map_planes(&tb, b.hi, (uint64_t)b.ld, (uint64_t)m, (uint64_t)b.ld, 64, hp::G_BK),
+  PLOM_REQUIRE(make_map_planes(&ta, a.hi, (uint64_t)a.ld, (uint64_t)m, (uint64_t)a.ld, 64, hp::G_BK,
+                               (uint64_t)a.pstride) &&
+                   make_map_planes(&tb, b.hi, (uint64_t)b.ld, (uint64_t)m, (uint64_t)b.ld, 64, hp::G_BK,
+                                   (uint64_t)b.pstride),
                PLOM_ERR_CUDA, "tn16: tensor map encoding failed");
   {
     ProfScope prof("tc_tn_f16x3", st, 2.0 * (double)m * a.N * b.N,
@@ -1223,8 +1243,8 @@ int apply_packed(const Packed& p, const double* W, int64_t ldw, int64_t k, float
   PLOM_REQUIRE(p.hi && W && (C || out) && m >= 1 && batch * p.mp < (1ll << 31) && k >= 1 &&
                    batch * k < (1ll << 31),
                PLOM_ERR_ARG, "apply16: bad arguments");
-  PLOM_REQUIRE(batch == 1 || (wstride >= p.N * ldw && (out || cstride >= m * ldc)), PLOM_ERR_ARG,
-               "apply16: batch strides too small");
+  PLOM_REQUIRE(batch == 1 || ((wstride == 0 || wstride >= p.N * ldw) && (out || cstride >= m * ldc)),
+               PLOM_ERR_ARG, "apply16: batch strides too small");
   if (out) PLOM_REQUIRE(out->hi && out->scale && out->m == m && out->N == k && out->batch == batch &&
                             out->mp == p.mp,
                         PLOM_ERR_ARG, "apply16: bad packed output");
@@ -1247,7 +1267,7 @@ int apply_packed(const Packed& p, const double* W, int64_t ldw, int64_t k, float
   }
   CUtensorMap tmA, tmB;
   PLOM_REQUIRE(make_map_planes(&tmA, p.hi, (uint64_t)p.ld, (uint64_t)(batch * p.mp),
-                               (uint64_t)p.ld, 64, 128) &&
+                               (uint64_t)p.ld, 64, 128, (uint64_t)p.pstride) &&
                    make_map_planes(&tmB, bhi, (uint64_t)ldk, (uint64_t)(batch * k), (uint64_t)ldk,
                                    64, 128),
                PLOM_ERR_CUDA, "apply16: tensor map encoding failed");

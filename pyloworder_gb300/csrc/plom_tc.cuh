@@ -20,7 +20,11 @@ struct Packed {
   float* scale;  // [batch][ld]
   int64_t m, N, ld;
   int64_t batch = 1, mp = 0;
+  int64_t pstride = 0;  // elements from hi to lo; 0: batch mp ld (planes back to back)
 };
+// a row range [r0, r0 + rows) of one packed problem as a problem of its own
+// (planes and plane stride of the parent; scales as given)
+Packed packed_rows_view(const Packed& p, int64_t r0, int64_t rows, int64_t mp, float* scale);
 int64_t packed_ld(int64_t N);
 int64_t packed_rows(int64_t m, int64_t batch);
 // carve planes and scales from the workspace
@@ -32,7 +36,8 @@ void packed_view(Packed& p, void* storage, int64_t m, int64_t N, float* scale, i
 int pack_f32(const float* Y, int64_t ld, int64_t m, int64_t N, Packed& p, Arena& ws,
              cudaStream_t st, int64_t bstride = 0);
 // G (N x N, FP64; a batch: batch x N x N) = Y^T Y
-int gram_packed(const Packed& p, double* G, int* err, Arena& ws, cudaStream_t st);
+int gram_packed(const Packed& p, double* G, int* err, Arena& ws, cudaStream_t st,
+                bool accumulate = false);
 // C (A.N x B.N, FP64, ldc) = A^T B for two packed operands with the same rows
 int tn_packed(const Packed& a, const Packed& b, double* C, int64_t ldc, int* err, Arena& ws,
               cudaStream_t st);

@@ -23,6 +23,8 @@
 // writing the next Q already packed; every n x n step stays in FP64.
 #include <algorithm>
 #include <cmath>
+#include <map>
+#include <mutex>
 #include <type_traits>
 
 #include "plom_common.cuh"
@@ -246,6 +248,35 @@ static int chol_pass_packed(bool cplx, int n, const Packed& P, PackedCore& b, do
   return PLOM_OK;
 }
 
+// passes 2 and 3 from Q1 (packed in b.P1; R1 in b.R1) and Re = R3 R2 R1
+static int cholqr3_packed_passes23(bool cplx, int n, PackedCore& b, double relfail, int* info,
+                                   Arena& ws, cudaStream_t st) {
+  const int N = cplx ? 2 * n : n;
+  const size_t mark = ws.off;
+  size_t need = mark;
+  auto sub = [&](auto&& fn) -> int {
+    ws.off = mark;
+    const int s = fn();
+    need = std::max(need, ws.off);
+    ws.off = mark;
+    return s;
+  };
+  int s = PLOM_OK;
+  // pass 2
+  PLOM_TRY(sub([&] { return chol_pass_packed(cplx, n, b.P1, b, b.R2, b.W2, 0.0, relfail, info, ws, st); }));
+  const double* F2 = ws.measuring() ? b.W2 : rowform(cplx, b.W2, b.F, n, st, s);
+  PLOM_TRY(s);
+  PLOM_TRY(sub([&] { return apply_packed(b.P1, F2, N, N, nullptr, 0, &b.P2, info, ws, st, 0, 0, true); }));
+  // pass 3
+  PLOM_TRY(sub([&] { return chol_pass_packed(cplx, n, b.P2, b, b.R3, b.W3, 0.0, relfail, info, ws, st); }));
+  ws.off = need;
+  if (!ws.measuring()) {
+    PLOM_TRY((gemm_sq_nn(b.R3, b.R2, b.Rp, N, 1, 3, st)));
+    PLOM_TRY((gemm_sq_nn(b.Rp, b.R1, b.Re, N, 1, 3, st)));
+  }
+  return PLOM_OK;
+}
+
 static int cholqr3_packed(bool cplx, const float* X, int64_t m, int n, int64_t ldx,
                           PackedCore& b, int* info, Arena& ws, cudaStream_t st) {
   const int N = cplx ? 2 * n : n;
@@ -267,18 +298,8 @@ static int cholqr3_packed(bool cplx, const float* X, int64_t m, int n, int64_t l
   const double* F1 = ws.measuring() ? b.W1 : rowform(cplx, b.W1, b.F, n, st, s);
   PLOM_TRY(s);
   PLOM_TRY(sub([&] { return apply_packed(b.P0, F1, N, N, nullptr, 0, &b.P1, info, ws, st, 0, 0, true); }));
-  // pass 2
-  PLOM_TRY(sub([&] { return chol_pass_packed(cplx, n, b.P1, b, b.R2, b.W2, 0.0, relfail, info, ws, st); }));
-  const double* F2 = ws.measuring() ? b.W2 : rowform(cplx, b.W2, b.F, n, st, s);
-  PLOM_TRY(s);
-  PLOM_TRY(sub([&] { return apply_packed(b.P1, F2, N, N, nullptr, 0, &b.P2, info, ws, st, 0, 0, true); }));
-  // pass 3
-  PLOM_TRY(sub([&] { return chol_pass_packed(cplx, n, b.P2, b, b.R3, b.W3, 0.0, relfail, info, ws, st); }));
+  PLOM_TRY(sub([&] { return cholqr3_packed_passes23(cplx, n, b, relfail, info, ws, st); }));
   ws.off = need;
-  if (!ws.measuring()) {
-    PLOM_TRY((gemm_sq_nn(b.R3, b.R2, b.Rp, N, 1, 3, st)));
-    PLOM_TRY((gemm_sq_nn(b.Rp, b.R1, b.Re, N, 1, 3, st)));
-  }
   return PLOM_OK;
 }
 
@@ -286,12 +307,11 @@ static int cholqr3_packed(bool cplx, const float* X, int64_t m, int n, int64_t l
 // the packed pitch (4 m packed_ld(N) bytes)
 static bool p1_fits(int64_t ld_floats, int N) { return ld_floats >= packed_ld(N); }
 
-static int tsqr_svd_packed(bool cplx, const float* X, int64_t m, int n, int64_t ldx, float* U,
-                           int64_t ldu, float* S, float* VT, int* info, Arena& ws,
-                           cudaStream_t st) {
+// svd(Re) = Ur S V^T and U = Q2 (R3^-1 Ur) into U (m x n, ldu), S, VT, after
+// the CholeskyQR3 passes (b.P2, b.W3, b.Re)
+static int svd_tail_packed(bool cplx, int n, PackedCore& b, int64_t m, float* U, int64_t ldu,
+                           float* S, float* VT, int* info, Arena& ws, cudaStream_t st) {
   const int N = cplx ? 2 * n : n;
-  PackedCore b;
-  carve_packed_core(ws, b, m, N, p1_fits(ldu, N), U);
   const int cw = cplx ? 2 : 1;
   double* Rc = ws.take<double>((size_t)n * n * cw);
   double* Ur = ws.take<double>((size_t)n * n * cw);
@@ -303,9 +323,7 @@ static int tsqr_svd_packed(bool cplx, const float* X, int64_t m, int n, int64_t 
     PLOM_REQUIRE(!ws.overflow(), PLOM_ERR_WORKSPACE, "tsqr_svd: workspace too small (%zu > %zu)",
                  ws.off, ws.cap);
   const size_t mark = ws.off;
-  PLOM_TRY(cholqr3_packed(cplx, X, m, n, ldx, b, info, ws, st));
-  size_t need = ws.off;
-  ws.off = mark;
+  size_t need = mark;
   const double* Rin = b.Re;
   if (cplx && !ws.measuring()) {
     PLOM_TRY(embed_to_complex(b.Re, Rc, n, 1, st));
@@ -334,6 +352,24 @@ static int tsqr_svd_packed(bool cplx, const float* X, int64_t m, int n, int64_t 
     PLOM_TRY((convert<double, float>(S64, S, n, st)));
     PLOM_TRY((convert<double, float>(VH, VT, (int64_t)n * n * cw, st)));
   }
+  ws.off = std::max(need, ws.off);
+  return PLOM_OK;
+}
+
+static int tsqr_svd_packed(bool cplx, const float* X, int64_t m, int n, int64_t ldx, float* U,
+                           int64_t ldu, float* S, float* VT, int* info, Arena& ws,
+                           cudaStream_t st) {
+  const int N = cplx ? 2 * n : n;
+  PackedCore b;
+  carve_packed_core(ws, b, m, N, p1_fits(ldu, N), U);
+  if (!ws.measuring())
+    PLOM_REQUIRE(!ws.overflow(), PLOM_ERR_WORKSPACE, "tsqr_svd: workspace too small (%zu > %zu)",
+                 ws.off, ws.cap);
+  const size_t mark = ws.off;
+  PLOM_TRY(cholqr3_packed(cplx, X, m, n, ldx, b, info, ws, st));
+  const size_t need = ws.off;
+  ws.off = mark;
+  PLOM_TRY(svd_tail_packed(cplx, n, b, m, U, ldu, S, VT, info, ws, st));
   ws.off = std::max(need, ws.off);
   return PLOM_OK;
 }
@@ -844,6 +880,208 @@ extern "C" int plom_tsqr_svd_batched(int dtype, int prec, const void* X, int64_t
   PLOM_CHECK_CUDA(cudaMemsetAsync(info, 0, sizeof(int) * PLOM_INFO_WORDS, (cudaStream_t)stream));
   return tsqr_svd_batched_dispatch(dtype, prec, X, batch, m, n, ldx, xstride, U, ldu, ustride, S,
                                    VT, info, a, (cudaStream_t)stream);
+}
+
+// ---------------------------------------------------------------------------
+// Host-buffer entry: X, U, S, VT in host memory (page-locked memory lets the
+// copies overlap the GPU work).  The mixed form on real FP32 data streams X
+// in row chunks: the copy engine moves chunk c + 1 while the GPU packs chunk
+// c with its own power-of-two column scales and adds its Gram into G1; the
+// pass-1 product then runs over the chunks as a batch (one W = R1^-1, the
+// chunks' own input scales, one packed Q1 of all rows), and the remaining
+// passes, the small SVD and U = Q2 (R3^-1 Ur) are the device pipeline.  The
+// last chunk is padded with zero rows (they stay zero through every pass).
+// Other forms copy X in whole, run the device driver and copy back.
+// ---------------------------------------------------------------------------
+constexpr int HOST_CHUNKS = 16;
+
+struct HostPlan {
+  int64_t mc;  // rows per chunk (a multiple of 128)
+  int C;       // chunks
+  int64_t M;   // C * mc >= m
+};
+
+static HostPlan host_plan(int64_t m) {
+  HostPlan h;
+  const int64_t want = std::min<int64_t>(HOST_CHUNKS, std::max<int64_t>(1, m / 65536));
+  h.mc = cdiv(cdiv(m, want), 128) * 128;
+  h.C = (int)cdiv(m, h.mc);
+  h.M = h.mc * h.C;
+  return h;
+}
+
+// one non-blocking copy stream per device, created on first use
+static cudaStream_t host_copy_stream() {
+  static std::mutex mu;
+  static std::map<int, cudaStream_t> streams;
+  int dev = 0;
+  cudaGetDevice(&dev);
+  std::lock_guard<std::mutex> lock(mu);
+  auto it = streams.find(dev);
+  if (it != streams.end()) return it->second;
+  cudaStream_t s = nullptr;
+  if (cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking) != cudaSuccess) return nullptr;
+  streams[dev] = s;
+  return s;
+}
+
+struct HostEvents {
+  cudaEvent_t start = nullptr, copied[2] = {nullptr, nullptr}, freed[2] = {nullptr, nullptr};
+  bool ok = false;
+  HostEvents() {
+    ok = cudaEventCreateWithFlags(&start, cudaEventDisableTiming) == cudaSuccess;
+    for (int i = 0; i < 2; ++i) {
+      ok = ok && cudaEventCreateWithFlags(&copied[i], cudaEventDisableTiming) == cudaSuccess;
+      ok = ok && cudaEventCreateWithFlags(&freed[i], cudaEventDisableTiming) == cudaSuccess;
+    }
+  }
+  ~HostEvents() {  // released once their pending work completes
+    if (start) cudaEventDestroy(start);
+    for (int i = 0; i < 2; ++i) {
+      if (copied[i]) cudaEventDestroy(copied[i]);
+      if (freed[i]) cudaEventDestroy(freed[i]);
+    }
+  }
+};
+
+static int tsqr_svd_host_mixed(const float* Xh, int64_t m, int n, int64_t ldx, float* Uh,
+                               int64_t ldu, float* Sh, float* VTh, int* info, Arena& ws,
+                               cudaStream_t st) {
+  const int N = n;
+  const HostPlan pl = host_plan(m);
+  const int64_t ldp = packed_ld(N);
+  const int64_t M = pl.M;
+  const bool meas = ws.measuring();
+  float* Ud = ws.take<float>((size_t)M * std::max<int64_t>(n, ldp));  // U, and Q1's planes before it
+  float* stage = ws.take<float>((size_t)2 * pl.mc * n);
+  float* Sd = ws.take<float>((size_t)n);
+  float* VTd = ws.take<float>((size_t)n * n);
+  float* xscale = ws.take<float>((size_t)pl.C * ldp);
+  float* qscale = ws.take<float>((size_t)pl.C * ldp);
+  PackedCore b;
+  carve_packed_core(ws, b, M, N, true, Ud);
+  b.P1.scale = qscale;
+  if (!meas) {
+    PLOM_REQUIRE(!ws.overflow(), PLOM_ERR_WORKSPACE, "tsqr_svd_host: workspace too small");
+    PLOM_REQUIRE(Xh && Uh && Sh && VTh, PLOM_ERR_ARG, "tsqr_svd_host: null host pointer");
+  }
+  const size_t mark = ws.off;
+  size_t need = mark;
+  auto sub = [&](auto&& fn) -> int {
+    ws.off = mark;
+    const int s = fn();
+    need = std::max(need, ws.off);
+    ws.off = mark;
+    return s;
+  };
+  double rel1, relfail;
+  shifts_for(PLOM_PREC_MIXED, M, N, rel1, relfail);
+  HostEvents ev;
+  cudaStream_t cs = nullptr;
+  if (!meas) {
+    cs = host_copy_stream();
+    PLOM_REQUIRE(cs && ev.ok, PLOM_ERR_CUDA, "tsqr_svd_host: copy stream or events unavailable");
+    PLOM_CHECK_CUDA(cudaEventRecord(ev.start, st));  // the staging buffers are free from here
+    PLOM_CHECK_CUDA(cudaStreamWaitEvent(cs, ev.start, 0));
+  }
+  // pass 1, chunk by chunk: copy, pack with the chunk's scales, add its Gram
+  for (int c = 0; c < pl.C; ++c) {
+    const int slot = c & 1;
+    const int64_t r0 = (int64_t)c * pl.mc;
+    const int64_t rows = std::min<int64_t>(pl.mc, m - r0);
+    float* sb = stage ? stage + (int64_t)slot * pl.mc * n : nullptr;
+    if (!meas) {
+      if (c >= 2) PLOM_CHECK_CUDA(cudaStreamWaitEvent(cs, ev.freed[slot], 0));
+      PLOM_CHECK_CUDA(cudaMemcpy2DAsync(sb, sizeof(float) * n, Xh + r0 * ldx, sizeof(float) * ldx,
+                                        sizeof(float) * n, rows, cudaMemcpyHostToDevice, cs));
+      PLOM_CHECK_CUDA(cudaEventRecord(ev.copied[slot], cs));
+      PLOM_CHECK_CUDA(cudaStreamWaitEvent(st, ev.copied[slot], 0));
+    }
+    Packed v = packed_rows_view(b.P0, r0, rows, pl.mc, xscale ? xscale + (int64_t)c * ldp : nullptr);
+    PLOM_TRY(sub([&] { return pack_f32(sb, n, rows, N, v, ws, st); }));
+    if (!meas) PLOM_CHECK_CUDA(cudaEventRecord(ev.freed[slot], st));
+    PLOM_TRY(sub([&] { return gram_packed(v, b.G, info, ws, st, c > 0); }));
+  }
+  PLOM_TRY(sub([&] { return chol_shifted(b.G, b.R1, N, 1, rel1, relfail, info, ws, st); }));
+  PLOM_TRY(sub([&] { return trtri_upper(b.R1, b.W1, N, 1, ws, st); }));
+  // Q1 = X R1^-1 with the chunks as a batch: one W, each chunk's input scales
+  Packed P0b = b.P0, P1b = b.P1;
+  P0b.batch = P1b.batch = pl.C;
+  P0b.m = P1b.m = pl.mc;
+  P0b.mp = P1b.mp = pl.mc;
+  P0b.scale = xscale;
+  P1b.scale = qscale;
+  PLOM_TRY(sub([&] { return apply_packed(P0b, b.W1, N, N, nullptr, 0, &P1b, info, ws, st, 0, 0, true); }));
+  PLOM_TRY(sub([&] { return cholqr3_packed_passes23(false, n, b, relfail, info, ws, st); }));
+  PLOM_TRY(sub([&] { return svd_tail_packed(false, n, b, M, Ud, n, Sd, VTd, info, ws, st); }));
+  ws.off = need;
+  if (!meas) {
+    PLOM_CHECK_CUDA(cudaMemcpy2DAsync(Uh, sizeof(float) * ldu, Ud, sizeof(float) * n,
+                                      sizeof(float) * n, m, cudaMemcpyDeviceToHost, st));
+    PLOM_CHECK_CUDA(cudaMemcpyAsync(Sh, Sd, sizeof(float) * n, cudaMemcpyDeviceToHost, st));
+    PLOM_CHECK_CUDA(cudaMemcpyAsync(VTh, VTd, sizeof(float) * n * n, cudaMemcpyDeviceToHost, st));
+  }
+  return PLOM_OK;
+}
+
+static size_t dtype_bytes(int dtype) {
+  return dtype == PLOM_F32 ? 4 : (dtype == PLOM_F64 || dtype == PLOM_C64) ? 8 : 16;
+}
+static size_t real_bytes(int dtype) { return (dtype == PLOM_F32 || dtype == PLOM_C64) ? 4 : 8; }
+
+static int tsqr_svd_host_dispatch(int dtype, int prec, const void* X, int64_t m, int64_t n,
+                                  int64_t ldx, void* U, int64_t ldu, void* S, void* VT, int* info,
+                                  Arena& ws, cudaStream_t st) {
+  if (prec == PLOM_PREC_MIXED && dtype == PLOM_F32 && packed_ok(host_plan(m).M))
+    return tsqr_svd_host_mixed((const float*)X, m, (int)n, ldx, (float*)U, ldu, (float*)S,
+                               (float*)VT, info, ws, st);
+  // whole copies around the device driver
+  const size_t es = dtype_bytes(dtype), rs = real_bytes(dtype);
+  char* Xd = ws.take<char>((size_t)m * n * es);
+  char* Ud = ws.take<char>((size_t)m * n * es);
+  char* Sd = ws.take<char>((size_t)n * rs);
+  char* VTd = ws.take<char>((size_t)n * n * es);
+  if (!ws.measuring()) {
+    PLOM_REQUIRE(!ws.overflow(), PLOM_ERR_WORKSPACE, "tsqr_svd_host: workspace too small");
+    PLOM_REQUIRE(X && U && S && VT, PLOM_ERR_ARG, "tsqr_svd_host: null host pointer");
+    PLOM_CHECK_CUDA(cudaMemcpy2DAsync(Xd, es * n, X, es * ldx, es * n, m, cudaMemcpyHostToDevice, st));
+  }
+  PLOM_TRY(tsqr_svd_dispatch(dtype, prec, Xd, m, n, n, Ud, n, Sd, VTd, info, ws, st));
+  if (!ws.measuring()) {
+    PLOM_CHECK_CUDA(cudaMemcpy2DAsync(U, es * ldu, Ud, es * n, es * n, m, cudaMemcpyDeviceToHost, st));
+    PLOM_CHECK_CUDA(cudaMemcpyAsync(S, Sd, rs * n, cudaMemcpyDeviceToHost, st));
+    PLOM_CHECK_CUDA(cudaMemcpyAsync(VT, VTd, es * n * n, cudaMemcpyDeviceToHost, st));
+  }
+  return PLOM_OK;
+}
+
+extern "C" size_t plom_tsqr_svd_host_workspace(int dtype, int prec, int64_t m, int64_t n) {
+  size_t bytes = 0;
+  int dummy[PLOM_INFO_WORDS];
+  run_measured(&bytes, [&](Arena& a) {
+    return tsqr_svd_host_dispatch(dtype, prec, nullptr, m, n, n, nullptr, n, nullptr, nullptr,
+                                  dummy, a, 0);
+  });
+  return bytes;
+}
+
+extern "C" int plom_tsqr_svd_host(int dtype, int prec, const void* X, int64_t m, int64_t n,
+                                  int64_t ldx, void* U, int64_t ldu, void* S, void* VT, void* ws,
+                                  size_t ws_bytes, int* info, void* stream) {
+  PLOM_REQUIRE(prec_ok(prec), PLOM_ERR_ARG, "bad precision %d", prec);
+  PLOM_REQUIRE(m >= 1 && n >= 1 && n <= 4096 && m >= n, PLOM_ERR_ARG,
+               "tsqr_svd_host: need 1 <= n <= min(m, 4096) (m=%lld n=%lld)", (long long)m,
+               (long long)n);
+  PLOM_REQUIRE(ldx >= n && ldu >= n, PLOM_ERR_ARG, "tsqr_svd_host: leading dimension < n");
+  PLOM_REQUIRE(X && U && S && VT && info && ws, PLOM_ERR_ARG, "tsqr_svd_host: null pointer");
+  size_t need = plom_tsqr_svd_host_workspace(dtype, prec, m, n);
+  PLOM_REQUIRE(need > 0, PLOM_ERR_ARG, "tsqr_svd_host: workspace query failed");
+  PLOM_REQUIRE(ws_bytes >= need, PLOM_ERR_WORKSPACE, "tsqr_svd_host: workspace %zu < required %zu",
+               ws_bytes, need);
+  Arena a(ws, ws_bytes);
+  PLOM_CHECK_CUDA(cudaMemsetAsync(info, 0, sizeof(int) * PLOM_INFO_WORDS, (cudaStream_t)stream));
+  return tsqr_svd_host_dispatch(dtype, prec, X, m, n, ldx, U, ldu, S, VT, info, a,
+                                (cudaStream_t)stream);
 }
 
 static int tsqr_dispatch(int dtype, int prec, const void* X, int64_t m, int64_t n, int64_t ldx,

@@ -236,9 +236,62 @@ def tsqr_svd_batched_device(x3, precision=None, info_out=None):
     return U, S, V
 
 
+def _host_rows(Ai):
+    """A host matrix (numpy array or CPU torch tensor) as a row-major CPU
+    tensor with unit inner stride, or None when Ai lives on the device or is
+    not a 2-D m >= n matrix of a supported type."""
+    t = L.torch()
+    if isinstance(Ai, t.Tensor):
+        if Ai.device.type != "cpu":
+            return None
+        x = Ai
+    else:
+        arr = np.asarray(Ai)
+        if arr.dtype not in (np.float32, np.float64, np.complex64, np.complex128):
+            return None
+        x = t.from_numpy(np.ascontiguousarray(arr))
+    if x.dim() != 2 or x.shape[0] < x.shape[1] or x.shape[1] < 1:
+        return None
+    if x.dtype not in (t.float32, t.float64, t.complex64, t.complex128):
+        return None
+    if L.rows_ld(x) is None:
+        x = x.contiguous()
+    return x
+
+
+def tsqr_svd_host(x, precision=None):
+    """TSQR-SVD of a host matrix in one library call (plom_tsqr_svd_host):
+    X streams to the device in row chunks while the first pass runs, and U,
+    S, V come back to host memory -- page-locked when X is."""
+    t = L.torch()
+    m, n = x.shape
+    ld = L.rows_ld(x)
+    dt = L.dtype_code(x)
+    prec = L.precision_code(precision, x)
+    pin = bool(x.is_pinned())
+    U = t.empty((m, n), dtype=x.dtype, pin_memory=pin)
+    S = t.empty(n, dtype=L.real_dtype(x), pin_memory=pin)
+    V = t.empty((n, n), dtype=x.dtype, pin_memory=pin)
+    ws = L.workspace(L.load().plom_tsqr_svd_host_workspace(dt, prec, m, n))
+    info = L.new_info()
+    L.call("plom_tsqr_svd_host", dt, prec, L.ptr(x), m, n, ld, L.ptr(U), n, L.ptr(S), L.ptr(V),
+           L.ptr(ws), ws.numel(), L.ptr(info), L.stream_ptr())
+    L.check_info(info, "tsqr_svd")
+    return U, S, V
+
+
 def tsqr_svd(Ai, *, precision=None):
     """U, S, V = tsqr_svd(A): A (m x n) = U diag(S) V with U m x n, S n
-    descending, V n x n holding V^T (pyLOM/vmmath/svd.py:228)."""
+    descending, V n x n holding V^T (pyLOM/vmmath/svd.py:228).  A host
+    matrix goes through the host-buffer entry (copies overlapped with the
+    first pass); a device tensor through the device entry."""
+    L.require_cuda()
+    x = _host_rows(Ai)
+    if x is not None:
+        U, S, V = tsqr_svd_host(x, precision)
+        if isinstance(Ai, L.torch().Tensor):
+            return U, S, V
+        return U.numpy(), S.numpy(), V.numpy()
     cv = L.to_device(Ai)
     x, ld = L.as_rows(cv.t)
     U, S, V = tsqr_svd_device(x, ld, precision)

@@ -39,7 +39,7 @@ def test_workspace_queries():
     mixed = lib.plom_tsqr_svd_workspace(L.F32, L.PREC_MIXED, m, n)
     fp64 = lib.plom_tsqr_svd_workspace(L.F32, L.PREC_FP64, m, n)
     # mixed: one FP32 m x n buffer (Q1 lives in U) plus the Gram's FP64 tile
-    # partials (36 tiles x 304 row chunks x 128 KiB); FP64: two FP64 buffers
+    # partials (36 tiles x 152 row chunks x 128 KiB); FP64: two FP64 buffers
     assert 4 * m * n <= mixed < 4 * m * n + (2 << 30)
     assert 16 * m * n <= fp64 < 16 * m * n + (1 << 30)
     # mixed randomized: A packed once (4 m n bytes), Q packed (pitch 128), Y and
@@ -78,6 +78,8 @@ def test_workspace_dry_runs_launch_nothing(dtype, prec):
     lib = L.load()
     for m, n in [(16384, 200), (8388608, 1024), (5, 1), (1000, 33), (300, 64)]:
         assert lib.plom_tsqr_svd_workspace(dtype, prec, m, n) > 0, lib.plom_last_error_string()
+    for m, n in [(8388608, 1024), (100000, 50), (5, 1), (1000, 33)]:
+        assert lib.plom_tsqr_svd_host_workspace(dtype, prec, m, n) > 0, lib.plom_last_error_string()
     for b, m, n in [(1, 2500, 24), (5, 2500, 24), (129, 65536, 63), (3, 5, 1)]:
         assert lib.plom_tsqr_svd_batched_workspace(dtype, prec, b, m, n) > 0, \
             lib.plom_last_error_string()

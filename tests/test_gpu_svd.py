@@ -126,6 +126,42 @@ def test_mixed_mean_removed_u_orthonormal():
     assert float((Vd @ Vd.T - torch.eye(n, dtype=torch.float64, device="cuda")).abs().max()) < 1e-6
 
 
+@pytest.mark.parametrize("dtype,precision", [(np.float32, "mixed"), (np.float64, "fp64"),
+                                             (np.complex64, "mixed")])
+def test_tsqr_svd_host_entry(dtype, precision):
+    """Host inputs go through plom_tsqr_svd_host: FP32 mixed streams X in 4
+    row chunks of 75,008 rows (the last one ragged, padded with zero rows),
+    each packed with its own column scales."""
+    rng = np.random.default_rng(3)
+    m, n, k = 300001, 40, 8
+    X = (rng.standard_normal((m, k)) @ rng.standard_normal((k, n))) * np.logspace(0, -3, n)
+    X += 1e-4 * rng.standard_normal((m, n))
+    cplx = np.issubdtype(dtype, np.complexfloating)
+    if cplx:
+        X = X + 1j * ((rng.standard_normal((m, k)) @ rng.standard_normal((k, n))) * np.logspace(0, -3, n))
+    X = X.astype(dtype)
+    Xt = torch.from_numpy(X).pin_memory()
+    Uh, Sh, Vh = P.math.tsqr_svd(Xt, precision=precision)
+    assert Uh.device.type == "cpu" and Uh.is_pinned() and Uh.dtype == Xt.dtype
+    ref = O.tsqr_svd(X.astype(np.complex128 if cplx else np.float64))
+    U, S, V = Uh.numpy(), Sh.numpy(), Vh.numpy()
+    if precision == "mixed":
+        assert sigma_rel(S, ref[1], k) < 1e-5
+        assert subspace_angle(U[:, :k], ref[0][:, :k]) < 1e-4
+        assert orthogonality(U) < 1e-5
+    else:
+        assert sigma_rel(S, ref[1], k) < 1e-10
+        assert sigma_normwise(S, ref[1]) < 1e-12
+        cols_up_to_phase(U[:, :k], ref[0][:, :k], 1e-8)
+        assert orthogonality(U) < 1e-12
+    A = (U * S) @ V
+    assert np.abs(A - X).max() <= (1e-4 if precision == "mixed" else 1e-11) * np.abs(X).max()
+    # numpy in, numpy out, the same call path
+    Un, Sn, Vn = P.math.tsqr_svd(X, precision=precision)
+    assert isinstance(Un, np.ndarray) and Un.dtype == X.dtype
+    np.testing.assert_array_equal(Sn, S)
+
+
 def test_randomized_philox_matches_oracle():
     rng = np.random.default_rng(5)
     X = (rng.standard_normal((3000, 12)) @ rng.standard_normal((12, 120))
