@@ -307,8 +307,8 @@ static int cholqr3_packed(bool cplx, const float* X, int64_t m, int n, int64_t l
 // the packed pitch (4 m packed_ld(N) bytes)
 static bool p1_fits(int64_t ld_floats, int N) { return ld_floats >= packed_ld(N); }
 
-// svd(Re) = Ur S V^T and U = Q2 (R3^-1 Ur) into U (m x n, ldu), S, VT, after
-// the CholeskyQR3 passes (b.P2, b.W3, b.Re)
+// svd(Re) = Ur S V^T and U = Q2 (R3^-1 Ur) into the first m rows of U (ldu),
+// S, VT, after the CholeskyQR3 passes (b.P2, b.W3, b.Re)
 static int svd_tail_packed(bool cplx, int n, PackedCore& b, int64_t m, float* U, int64_t ldu,
                            float* S, float* VT, int* info, Arena& ws, cudaStream_t st) {
   const int N = cplx ? 2 * n : n;
@@ -346,7 +346,9 @@ static int svd_tail_packed(bool cplx, int n, PackedCore& b, int64_t m, float* U,
       Mop = Me;
     }
   }
-  PLOM_TRY(apply_packed(b.P2, Mop, N, N, U, ldu, nullptr, info, ws, st));
+  Packed P2 = b.P2;
+  P2.m = m;  // output rows (the planes may carry zero padding rows past m)
+  PLOM_TRY(apply_packed(P2, Mop, N, N, U, ldu, nullptr, info, ws, st));
   PLOM_TRY(renorm_long_columns(Me, N, n, cw, U, m, ldu, 1, 0, 0, ws, st));
   if (!ws.measuring()) {
     PLOM_TRY((convert<double, float>(S64, S, n, st)));
@@ -1013,11 +1015,24 @@ static int tsqr_svd_host_mixed(const float* Xh, int64_t m, int n, int64_t ldx, f
   P1b.scale = qscale;
   PLOM_TRY(sub([&] { return apply_packed(P0b, b.W1, N, N, nullptr, 0, &P1b, info, ws, st, 0, 0, true); }));
   PLOM_TRY(sub([&] { return cholqr3_packed_passes23(false, n, b, relfail, info, ws, st); }));
-  PLOM_TRY(sub([&] { return svd_tail_packed(false, n, b, M, Ud, n, Sd, VTd, info, ws, st); }));
+  // U straight into page-locked host memory when the caller's U is mapped
+  // (the final product's stores cross the host link while it computes);
+  // otherwise into the device buffer and copied back
+  float* Umapped = nullptr;
+  if (!meas) {
+    void* dp = nullptr;
+    if (cudaHostGetDevicePointer(&dp, Uh, 0) == cudaSuccess) Umapped = static_cast<float*>(dp);
+    else cudaGetLastError();  // pageable U: clear the error and copy
+  }
+  PLOM_TRY(sub([&] {
+    return svd_tail_packed(false, n, b, m, Umapped ? Umapped : Ud, Umapped ? ldu : n, Sd, VTd, info,
+                           ws, st);
+  }));
   ws.off = need;
   if (!meas) {
-    PLOM_CHECK_CUDA(cudaMemcpy2DAsync(Uh, sizeof(float) * ldu, Ud, sizeof(float) * n,
-                                      sizeof(float) * n, m, cudaMemcpyDeviceToHost, st));
+    if (!Umapped)
+      PLOM_CHECK_CUDA(cudaMemcpy2DAsync(Uh, sizeof(float) * ldu, Ud, sizeof(float) * n,
+                                        sizeof(float) * n, m, cudaMemcpyDeviceToHost, st));
     PLOM_CHECK_CUDA(cudaMemcpyAsync(Sh, Sd, sizeof(float) * n, cudaMemcpyDeviceToHost, st));
     PLOM_CHECK_CUDA(cudaMemcpyAsync(VTh, VTd, sizeof(float) * n * n, cudaMemcpyDeviceToHost, st));
   }
