@@ -1393,8 +1393,10 @@ __global__ void __launch_bounds__(512, 1)
           double* gv = Vt + (int64_t)col * P;
           const double* sa = jsm + s8 * P;
           const double* sv = jsm + (8 + s8) * P;
-          const double f = df_val(sd[s8]);
-          if (f < JAC_FOLD_BELOW) {
+          // the fold test on the FP32 head of the scale: no FP64 instruction
+          // per thread and row on the common path (GB300 runs FP64 at 1/64)
+          if (sd[s8].x < (float)JAC_FOLD_BELOW) {
+            const double f = df_val(sd[s8]);
             for (int64_t i = threadIdx.x; i < P; i += 512) {
               jac_put<true>(ga, i, jac_get<true>(sa, i) * f);
               jac_put<true>(gv, i, jac_get<true>(sv, i) * f);
@@ -1408,10 +1410,9 @@ __global__ void __launch_bounds__(512, 1)
         }
         if (threadIdx.x < 8 && scol[threadIdx.x] >= 0) {
           const int col = scol[threadIdx.x];
-          const double f = df_val(sd[threadIdx.x]);
-          const bool fold = f < JAC_FOLD_BELOW;
+          const bool fold = sd[threadIdx.x].x < (float)JAC_FOLD_BELOW;
           js.nrm2[b * n + col] = snrm[threadIdx.x].x < 0.f ? -1.0 : df_val(snrm[threadIdx.x]);
-          js.dsc[b * n + col] = fold ? 1.0 : f;
+          js.dsc[b * n + col] = fold ? 1.0 : df_val(sd[threadIdx.x]);
         }
         __syncthreads();
       }
