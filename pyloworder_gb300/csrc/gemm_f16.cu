@@ -402,8 +402,36 @@ static_assert(G_KSUB % G_BK == 0, "drain on stage boundaries");
 constexpr size_t G_SMEM = (size_t)G_STAGES * G_STAGE + 1024;
 constexpr uint32_t G_TMEM = 512;               // 2 buffers x (main 128 + correction 128)
 
+// Double-float (unevaluated sum of two FP32 numbers, ~48 bits) for the Gram's
+// partial sums: GB300 runs FP64 at 1/64 of its FP32 rate, and the drains of
+// the TMEM accumulators and the reduction of the partials would otherwise be
+// FP64-bound.  TwoSum / Fast2Sum (Knuth, Dekker) and the accurate
+// double-word addition of Joldes, Muller and Popescu (ACM TOMS 44, 2017,
+// Algorithm 6; relative error below 3 u^2).
+__device__ __forceinline__ float2 dw_two_sum(float a, float b) {
+  const float s = a + b;
+  const float bb = s - a;
+  return make_float2(s, (a - (s - bb)) + (b - bb));
+}
+__device__ __forceinline__ float2 dw_fast_two_sum(float a, float b) {
+  const float s = a + b;
+  return make_float2(s, b - (s - a));
+}
+__device__ __forceinline__ float2 dw_add(float2 x, float2 y) {
+  const float2 s = dw_two_sum(x.x, y.x);
+  const float2 t = dw_two_sum(x.y, y.y);
+  const float2 v = dw_fast_two_sum(s.x, s.y + t.x);
+  return dw_fast_two_sum(v.x, t.y + v.y);
+}
+__device__ __forceinline__ float2 dw_from_double(double d) {
+  const float h = __double2float_rn(d);
+  return make_float2(h, __double2float_rn(d - (double)h));
+}
+__device__ __forceinline__ double dw_value(float2 v) { return (double)v.x + (double)v.y; }
+
 // SYM: upper tiles of A^T A (tmB unused) with the exact diagonal on diagonal
-// tiles; otherwise every tile of A^T B (tna x tnb tiles, B from tmB).
+// tiles; otherwise every tile of A^T B (tna x tnb tiles, B from tmB).  The
+// partial of a work item is 128 x 128 double-float values (8 bytes each).
 template <bool SYM>
 __global__ void __launch_bounds__(320, 1)
     gram16_kernel(const __grid_constant__ CUtensorMap tmP, const __grid_constant__ CUtensorMap tmB,
@@ -474,7 +502,7 @@ __global__ void __launch_bounds__(320, 1)
   __syncthreads();
   fence_after();
   const uint32_t tmem = tmem_sh;
-  double* P = part + (int64_t)item * 128 * 128;
+  float2* P = reinterpret_cast<float2*>(part) + (int64_t)item * 128 * 128;
 
   if (warp == 9) {
     // ---- TMA producer: 64 rows x (I block [+ J block]) of both planes
@@ -572,7 +600,7 @@ __global__ void __launch_bounds__(320, 1)
       if (ok) mma_commit(&tfull[b]);
     }
   } else if (warp < 4) {
-    // ---- epilogue: drain each finished sub-chunk into the FP64 partial
+    // ---- epilogue: drain each finished sub-chunk into the double-float partial
     const int rloc = warp * 32 + lane;
     for (int sub = 0; sub < nsub; ++sub) {
       const int b = sub & 1;
@@ -582,8 +610,8 @@ __global__ void __launch_bounds__(320, 1)
       __syncwarp();
       if (!__all_sync(0xffffffffu, ready)) break;
       fence_after();
-      const double dval = diag ? diag_sh[b][rloc] : 0.0;
-      double* prow = P + (int64_t)rloc * 128;
+      const float2 dval = diag ? dw_from_double(diag_sh[b][rloc]) : make_float2(0.f, 0.f);
+      float2* prow = P + (int64_t)rloc * 128;
 #pragma unroll 1
       for (int cc = 0; cc < 4; ++cc) {
         uint32_t rm[32], rc[32];
@@ -591,20 +619,22 @@ __global__ void __launch_bounds__(320, 1)
         tmem_ld32(ta, rm);
         tmem_ld32(ta + 128, rc);
         tmem_wait_ld();
-        double* d = prow + cc * 32;
+        float2* d = prow + cc * 32;
 #pragma unroll
         for (int j = 0; j < 32; j += 2) {
-          double v0 = (double)__uint_as_float(rm[j]) + (double)__uint_as_float(rc[j]);
-          double v1 = (double)__uint_as_float(rm[j + 1]) + (double)__uint_as_float(rc[j + 1]);
+          // main + correction exactly, as a double-float pair
+          float2 v0 = dw_two_sum(__uint_as_float(rm[j]), __uint_as_float(rc[j]));
+          float2 v1 = dw_two_sum(__uint_as_float(rm[j + 1]), __uint_as_float(rc[j + 1]));
           if (diag && cc * 32 + j == rloc) v0 = dval;
           if (diag && cc * 32 + j + 1 == rloc) v1 = dval;
+          float4* q = reinterpret_cast<float4*>(d + j);
           if (sub == 0) {
-            *reinterpret_cast<double2*>(d + j) = make_double2(v0, v1);
+            *q = make_float4(v0.x, v0.y, v1.x, v1.y);
           } else {
-            double2 o = *reinterpret_cast<double2*>(d + j);
-            o.x += v0;
-            o.y += v1;
-            *reinterpret_cast<double2*>(d + j) = o;
+            const float4 o = *q;
+            const float2 a0 = dw_add(make_float2(o.x, o.y), v0);
+            const float2 a1 = dw_add(make_float2(o.z, o.w), v1);
+            *q = make_float4(a0.x, a0.y, a1.x, a1.y);
           }
         }
       }
@@ -612,8 +642,8 @@ __global__ void __launch_bounds__(320, 1)
       mbar_arrive(&tempty[b]);
     }
     if (nsub == 0) {  // empty chunk: the partial is zero
-      double* prow = P + (int64_t)rloc * 128;
-      for (int j = 0; j < 128; ++j) prow[j] = 0.0;
+      float2* prow = P + (int64_t)rloc * 128;
+      for (int j = 0; j < 128; ++j) prow[j] = make_float2(0.f, 0.f);
     }
   }
   fence_before();
@@ -636,11 +666,11 @@ __global__ void tn16_reduce_kernel(const double* __restrict__ part, int Na, int 
     const int i = (int)(e / Nb), j = (int)(e % Nb);
     const int ti = i / 128, tj = j / 128;
     const int tile = ti * tnb + tj;
-    const double* p = part + ((int64_t)tile * chunks) * 128 * 128 + (int64_t)(i - ti * 128) * 128 +
-                      (j - tj * 128);
-    double acc = 0.0;
-    for (int c = 0; c < chunks; ++c) acc += p[(int64_t)c * 128 * 128];
-    C[(int64_t)i * ldc + j] = acc / ((double)sa[i] * (double)sb[j]);
+    const float2* p = reinterpret_cast<const float2*>(part) + ((int64_t)tile * chunks) * 128 * 128 +
+                      (int64_t)(i - ti * 128) * 128 + (j - tj * 128);
+    float2 acc = make_float2(0.f, 0.f);
+    for (int c = 0; c < chunks; ++c) acc = dw_add(acc, p[(int64_t)c * 128 * 128]);
+    C[(int64_t)i * ldc + j] = dw_value(acc) / ((double)sa[i] * (double)sb[j]);
   }
 }
 
@@ -662,12 +692,13 @@ __global__ void gram16_reduce_kernel(const double* __restrict__ part, int N, int
     }
     const int ti = a / 128, tj = b / 128;
     const int tile = ti * tn - ti * (ti - 1) / 2 + (tj - ti);
-    const double* p = part + ((pb * ntiles + tile) * chunks) * 128 * 128 +
-                      (int64_t)(a - ti * 128) * 128 + (b - tj * 128);
-    double acc = 0.0;
-    for (int c = 0; c < chunks; ++c) acc += p[(int64_t)c * 128 * 128];
+    const float2* p = reinterpret_cast<const float2*>(part) +
+                      ((pb * ntiles + tile) * chunks) * 128 * 128 + (int64_t)(a - ti * 128) * 128 +
+                      (b - tj * 128);
+    float2 acc = make_float2(0.f, 0.f);
+    for (int c = 0; c < chunks; ++c) acc = dw_add(acc, p[(int64_t)c * 128 * 128]);
     const float* sp = s + pb * ld;
-    const double v = acc / ((double)sp[i] * (double)sp[j]);
+    const double v = dw_value(acc) / ((double)sp[i] * (double)sp[j]);
     G[e] = accumulate ? G[e] + v : v;
   }
 }
@@ -933,23 +964,28 @@ __global__ void __launch_bounds__(192, 1)
 // ---------------------------------------------------------------------------
 constexpr int RN_MAX = 8;  // columns per problem
 
-// one block per problem: list the columns j with ||M e_(cw j)||^2 > thr2
+// list the columns j with ||M e_(cw j)||^2 > thr2: blocks of 32 columns x 8
+// row groups per problem (count and sums zeroed beforehand)
 __global__ void __launch_bounds__(256) rn_flag_kernel(const double* __restrict__ M, int N, int n,
                                                       int cw, int64_t mstride, double thr2,
-                                                      int* __restrict__ list, int* __restrict__ count,
-                                                      double* __restrict__ sums) {
-  const int b = blockIdx.x;
+                                                      int* __restrict__ list, int* __restrict__ count) {
+  const int b = blockIdx.y;
   const double* Mb = M + (int64_t)b * mstride;
-  if (threadIdx.x == 0) count[b] = 0;
-  if (threadIdx.x < RN_MAX) sums[b * RN_MAX + threadIdx.x] = 0.0;
-  __syncthreads();
-  for (int j = threadIdx.x; j < n; j += blockDim.x) {
-    double s = 0.0;
-    for (int i = 0; i < N; ++i) {
+  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+  const int j = blockIdx.x * 32 + tx;
+  __shared__ double part[8][33];
+  double s = 0.0;
+  if (j < n)
+    for (int i = ty; i < N; i += 8) {
       const double v = Mb[(int64_t)i * N + (int64_t)cw * j];
       s = fma(v, v, s);
     }
-    if (s > thr2) {
+  part[ty][tx] = s;
+  __syncthreads();
+  if (ty == 0 && j < n) {
+    double t = 0.0;
+    for (int r = 0; r < 8; ++r) t += part[r][tx];
+    if (t > thr2) {
       const int k = atomicAdd(&count[b], 1);
       if (k < RN_MAX) list[b * RN_MAX + k] = j;
     }
@@ -1318,7 +1354,10 @@ int renorm_long_columns(const double* M, int N, int n, int cw, float* U, int64_t
   PLOM_REQUIRE(!ws.overflow(), PLOM_ERR_WORKSPACE, "renorm: workspace too small");
   PLOM_REQUIRE(M && U && batch >= 1 && batch <= 65535, PLOM_ERR_ARG, "renorm: bad arguments");
   ProfScope prof("renorm_cols", st, 0.0, 8.0 * (double)m * batch, 3);
-  hp::rn_flag_kernel<<<batch, 256, 0, st>>>(M, N, n, cw, mstride, 16.0, list, count, sums);
+  PLOM_CHECK_CUDA(cudaMemsetAsync(count, 0, sizeof(int) * batch, st));
+  PLOM_CHECK_CUDA(cudaMemsetAsync(sums, 0, sizeof(double) * batch * hp::RN_MAX, st));
+  hp::rn_flag_kernel<<<dim3((unsigned)cdiv(n, 32), (unsigned)batch), 256, 0, st>>>(
+      M, N, n, cw, mstride, 16.0, list, count);
   PLOM_CHECK_LAUNCH();
   const unsigned gx = (unsigned)std::max<int64_t>(1, std::min<int64_t>(cdiv(m, 256), (int64_t)num_sms() * 4));
   hp::rn_sumsq_kernel<<<dim3(gx, (unsigned)batch), 256, 0, st>>>(U, m, ldu, cw, ustride, list, count,
