@@ -428,6 +428,28 @@ def run_other(args):
         out.update(metric="randomized_svd GB/s", unit="GB/s",
                    config={"workload": f"randomized_svd {m}x{n} f32, r={r} (64+16), q={q}",
                            "precision": "mixed"})
+    elif args.workload == "streaming":
+        # the POD field of the headline workload arriving in 8 batches of 128
+        # snapshots: init_qr_streaming on the first, update_qr_streaming on
+        # the others (range r = 80, q = 2)
+        m, n, r, q, nb = args.m, N_FULL, 80, 2, 8
+        nx, ny = datagen.grid_for_points(m)
+        X = datagen.pod_field_device(nx, ny, n, NMODES, seed=SEED, noise=1e-5, amp_pow=1.5, m=m)
+        Y, _, _ = P.vmmath.remove_mean_device(X, n)
+        del X
+        w = n // nb
+        batches = [Y[:, i * w:(i + 1) * w] for i in range(nb)]
+
+        def step():
+            Q, B, Yo = P.math.init_qr_streaming(batches[0], r, q, seed=7)
+            for bt in batches[1:]:
+                Q, B, Yo = P.math.update_qr_streaming(bt, Q, B, Yo, r, q)
+            return Q, B, Yo
+        # per batch: A Omega, q x (A^T Q, A O2), Q^T A and, in an update, Q2^T A
+        nbytes = 4 * m * w * (2 + 2 * q + 1) * nb + 4 * m * r * (2 * nb)
+        out.update(metric="streaming QR GB/s", unit="GB/s",
+                   config={"workload": f"init/update_qr_streaming {m}x{n} f32 in {nb} batches of {w} "
+                                       f"snapshots, r={r}, q={q}", "precision": "mixed"})
     elif args.workload == "dmd":
         m, n, r = 2_097_152, 512, 32
         X, lam = datagen.dmd_field_device(m, n)
@@ -473,7 +495,7 @@ def run_other(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--workload", default="tsqr_svd",
-                    choices=["tsqr_svd", "randomized", "dmd", "spod"])
+                    choices=["tsqr_svd", "randomized", "dmd", "spod", "streaming"])
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)

@@ -212,6 +212,48 @@ def randomized_svd(Ai, r, q, seed=-1, omega=None):
     return matmul(Q, Ur), S, V
 
 
+def init_qr_streaming(Ai, r, q, seed=None, omega=None):
+    """Streaming randomized range finder, first batch.
+    pyLOM/vmmath/svd.py:175-193: Omega = rand(n, r) after seed(seed),
+    Y = A Omega, q times (Q = tsqr(Y); Y = A (A^T Q)), Q = tsqr(Y), B = Q^T A.
+    Returns (Q m x r, B r x n, Y m x r)."""
+    n = Ai.shape[1]
+    if omega is None:
+        np.random.seed(seed=seed)
+        omega = np.random.rand(n, r).astype(Ai.dtype)
+    Y = matmul(Ai, omega)
+    for _ in range(q):
+        Q, _ = tsqr(Y)
+        Q2 = matmulp(Ai.T, Q)
+        Y = matmul(Ai, Q2)
+    Q, _ = tsqr(Y)
+    B = matmulp(Q.T, Ai)
+    return Q, B, Y
+
+
+def update_qr_streaming(Ai, Q1, B1, Yo, r, q, omega=None):
+    """Streaming randomized range finder, next batch of snapshots.
+    pyLOM/vmmath/svd.py:196-225: Omega = rand(n_new, r) (numpy's global
+    stream, continuing), Yn = A Omega and q power steps on the new batch,
+    Yo += Yn, Q2 = tsqr(Yo), B2 = [(Q2^T Q1) B1, Q2^T A].  Returns
+    (Q2 m x r, B2 r x (n_old + n_new), Yo); the reference adds into the
+    caller's Yo in place, this restatement returns a new array."""
+    n = Ai.shape[1]
+    if omega is None:
+        omega = np.random.rand(n, r).astype(Ai.dtype)
+    Yn = matmul(Ai, omega)
+    for _ in range(q):
+        Qp, _ = tsqr(Yn)
+        O2 = matmulp(Ai.T, Qp)
+        Yn = matmul(Ai, O2)
+    Yo = Yo + Yn
+    Q2, _ = tsqr(Yo)
+    Q2Q1 = matmulp(Q2.T, Q1)
+    B2o = matmul(Q2Q1, B1)
+    B2n = matmulp(Q2.T, Ai)
+    return Q2, np.hstack((B2o, B2n)), Yo
+
+
 # ---------------------------------------------------------------------------
 # truncation  (pyLOM/vmmath/truncation.py)
 # ---------------------------------------------------------------------------
@@ -270,6 +312,14 @@ def pod_run(X, remove_mean=True, divide_variance=False, randomized=False, r=1, q
     if randomized:
         return randomized_svd(Y, r, q, seed=seed, omega=omega)
     return tsqr_svd(Y)
+
+
+def pca_run(X, divide_variance=True, randomized=False, r=1, q=3, seed=-1):
+    """pyLOM/PCA/wrapper.py:17-38: components U and scores (diag(S) V)^T of the
+    POD of the mean-removed (variance-normalised) data."""
+    U, S, V = pod_run(X, remove_mean=True, divide_variance=divide_variance, randomized=randomized,
+                      r=r, q=q, seed=seed)
+    return U, vecmat(S, V).T
 
 
 def pod_truncate(U, S, V, r=1e-8):

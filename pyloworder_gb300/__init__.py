@@ -11,6 +11,7 @@ from . import vmmath as math
 from . import POD
 from . import DMD
 from . import SPOD
+from . import PCA
 
 __version__ = "0.1.0"
 

@@ -1215,6 +1215,26 @@ static int matmul_impl(int prec, int transA, const T* A, int64_t lda, const T* B
     if (fp64) return gemm_nn<T, T, T, double>(A, lda, B, ldb, C, ldc, m, n, k, st);
     return gemm_nn<T, T, T, float>(A, lda, B, ldb, C, ldc, m, n, k, st);
   }
+  if constexpr (sizeof(T) == 4) {
+    // mixed form: both tall operands packed, the reduction over their k rows
+    // on the tensor cores (A^T B, double-float partials), FP32 result
+    if (!fp64 && packed_ok(k) && m >= 1 && n >= 1 && k >= 1) {
+      int* flag = ws.take<int>(PLOM_INFO_WORDS);
+      double* C64 = ws.take<double>((size_t)m * n);
+      Packed pa, pb;
+      packed_carve(ws, pa, k, m);
+      packed_carve(ws, pb, k, n);
+      if (!ws.measuring()) {
+        PLOM_REQUIRE(!ws.overflow(), PLOM_ERR_WORKSPACE, "matmul: workspace too small");
+        PLOM_CHECK_CUDA(cudaMemsetAsync(flag, 0, sizeof(int) * PLOM_INFO_WORDS, st));
+      }
+      PLOM_TRY(pack_f32(A, lda, k, m, pa, ws, st));
+      PLOM_TRY(pack_f32(B, ldb, k, n, pb, ws, st));
+      PLOM_TRY(tn_packed(pa, pb, C64, n, flag, ws, st));
+      if (ws.measuring()) return PLOM_OK;
+      return copy2d<double, float>(C64, n, C, ldc, m, n, st);
+    }
+  }
   if (fp64) return gemm_tn<T, T, double, T>(A, lda, B, ldb, C, ldc, m, n, k, false, ws, st);
   return gemm_tn<T, T, float, T>(A, lda, B, ldb, C, ldc, m, n, k, false, ws, st);
 }

@@ -22,7 +22,8 @@ from . import _lib as L
 __all__ = [
     "temporal_mean", "subtract_mean", "temporal_variance", "norm_variance",
     "matmul", "matmulp", "vecmat", "transpose", "tsqr", "tsqr_svd", "randomized_svd",
-    "randomized_qr", "compute_truncation_residual", "energy", "hammwin", "RMSE",
+    "randomized_qr", "init_qr_streaming", "update_qr_streaming", "compute_truncation_residual",
+    "energy", "hammwin", "RMSE",
 ]
 
 
@@ -367,6 +368,129 @@ def randomized_qr(Ai, r, q, seed=-1, *, precision=None):
     if isinstance(U, t.Tensor):
         return U, S.reshape(-1, 1) * V
     return U, S.reshape(-1, 1) * V
+
+
+# --------------------------------------------------------------------------
+# streaming range finder: pyLOM/vmmath/svd.py:175-225
+# --------------------------------------------------------------------------
+
+# Philox key of the last init_qr_streaming and the number of draws made from
+# it (pyLOM's update_qr_streaming keeps drawing from numpy's global stream
+# after the seeded init; here every update draws from the next key)
+_QR_STREAM = {"seed": 0, "draws": 0}
+
+
+def _uniform_device(rows, cols, seed, dtype):
+    """rows x cols uniform [0, 1) from the Philox4x32-10 stream keyed by seed."""
+    t = L.torch()
+    out = t.empty((rows, cols), dtype=dtype, device="cuda")
+    L.call("plom_fill_uniform", L.dtype_code(out), L.ptr(out), out.numel(), int(seed) & (2**64 - 1),
+           L.stream_ptr())
+    return out
+
+
+def _householder_signs(Q):
+    """Signs s with Q diag(s) and diag(s) R the factors Householder QR (LAPACK
+    geqrf, m > n) returns for the matrix whose CholeskyQR factors (R with a
+    positive diagonal) are Q, R: s_k is minus the sign of the k-th pivot of
+    the LU of Q's top n x n block shifted by diag(s) -- the sign rule of
+    Householder reconstruction (Ballard, Demmel, Grigori, Jacquelin, Knight,
+    Nguyen, J. Parallel Distrib. Comput. 85, 2015), which is Householder's
+    own choice of the reflection that avoids cancellation.  Every pivot is
+    at least 1 in magnitude.  n x n work, on the host (n is the range size)."""
+    n = Q.shape[1]
+    Q1 = Q[:n, :n].double().cpu().numpy().copy()
+    s = np.empty(n)
+    for k in range(n):
+        s[k] = -1.0 if Q1[k, k] >= 0 else 1.0
+        Q1[k, k] -= s[k]
+        Q1[k + 1:, k] /= Q1[k, k]
+        Q1[k + 1:, k + 1:] -= np.outer(Q1[k + 1:, k], Q1[k, k + 1:])
+    return s
+
+
+def _tsqr_householder(Y, precision):
+    """tsqr of a tall device matrix with Householder QR's column signs, so
+    that sums of such factors across calls (the streaming update's Yo += Yn)
+    follow the reference."""
+    t = L.torch()
+    Q, R = tsqr(Y, precision=precision)
+    s = t.as_tensor(_householder_signs(Q), dtype=Q.dtype, device="cuda")
+    return Q * s, R * s[:, None]
+
+
+def _device_like(A, dtype):
+    t = L.torch()
+    if isinstance(A, t.Tensor):
+        return A.to(device="cuda", dtype=dtype)
+    return t.as_tensor(np.asarray(A), dtype=dtype, device="cuda")
+
+
+def init_qr_streaming(Ai, r, q, seed=None, *, omega=None, precision=None):
+    """First batch of the streaming randomized range finder
+    (pyLOM/vmmath/svd.py:175-193): Omega uniform [0, 1) (n x r; the Philox
+    stream keyed by ``seed``, time-seeded when None, or the given ``omega``),
+    Y = A Omega, q times (Q = tsqr(Y); Y = A (A^T Q)), Q = tsqr(Y),
+    B = Q^T A.  Returns Q (m x r), B (r x n), Y (m x r) of the input's kind."""
+    t = L.torch()
+    cv = L.to_device(Ai)
+    x, _ = L.as_rows(cv.t)
+    if x.dtype not in (t.float32, t.float64):
+        raise TypeError("init_qr_streaming takes float32 or float64 data")
+    n = x.shape[1]
+    r, q = int(r), int(q)
+    if omega is None:
+        seed = int(time.time()) if seed is None else int(seed)
+        _QR_STREAM.update(seed=seed, draws=1)
+        om = _uniform_device(n, r, seed, x.dtype)
+    else:
+        om = _device_like(omega, x.dtype)
+    Y = matmul(x, om, precision=precision)
+    for _ in range(q):
+        Q, _ = _tsqr_householder(Y, precision)
+        Y = matmul(x, matmul(x.T, Q, precision=precision), precision=precision)
+    Q, _ = _tsqr_householder(Y, precision)
+    B = matmul(Q.T, x, precision=precision)
+    return cv.back(Q), cv.back(B), cv.back(Y)
+
+
+def update_qr_streaming(Ai, Q1, B1, Yo, r, q, *, omega=None, seed=None, precision=None):
+    """Next batch of snapshots (pyLOM/vmmath/svd.py:196-225): Yn = A Omega
+    with q power steps on the batch, Yo += Yn (in place, as the reference
+    does), Q2 = tsqr(Yo), B2 = [(Q2^T Q1) B1, Q2^T A].  Omega: ``omega`` if
+    given, else the Philox stream keyed by ``seed``, else the next key after
+    the last init_qr_streaming.  Returns Q2, B2 and Yo."""
+    t = L.torch()
+    cv = L.to_device(Ai)
+    x, _ = L.as_rows(cv.t)
+    if x.dtype not in (t.float32, t.float64):
+        raise TypeError("update_qr_streaming takes float32 or float64 data")
+    n = x.shape[1]
+    r, q = int(r), int(q)
+    if omega is None:
+        if seed is None:
+            seed = _QR_STREAM["seed"] * 1000003 + _QR_STREAM["draws"]
+            _QR_STREAM["draws"] += 1
+        om = _uniform_device(n, r, seed, x.dtype)
+    else:
+        om = _device_like(omega, x.dtype)
+    q1 = _device_like(Q1, x.dtype)
+    b1 = _device_like(B1, x.dtype)
+    Yn = matmul(x, om, precision=precision)
+    for _ in range(q):
+        Qp, _ = _tsqr_householder(Yn, precision)
+        Yn = matmul(x, matmul(x.T, Qp, precision=precision), precision=precision)
+    yo = _device_like(Yo, x.dtype) + Yn
+    Q2, _ = _tsqr_householder(yo, precision)
+    B2o = matmul(matmul(Q2.T, q1, precision=precision), b1, precision=precision)
+    B2n = matmul(Q2.T, x, precision=precision)
+    B2 = t.cat([B2o, B2n], dim=1)
+    # Yo += Yn in the caller's array
+    if isinstance(Yo, t.Tensor):
+        Yo.copy_(yo.to(device=Yo.device, dtype=Yo.dtype))
+    else:
+        np.copyto(Yo, yo.cpu().numpy().astype(np.asarray(Yo).dtype, copy=False))
+    return cv.back(Q2), cv.back(B2), Yo
 
 
 # --------------------------------------------------------------------------

@@ -183,6 +183,11 @@ def main(refroot):
     U3, S3, V3 = pyLOM.POD.run(Xf, remove_mean=False)
     np.savez_compressed(os.path.join(HERE, "pod_f32_nomean.npz"), X=Xf, U=U3, S=S3, V=V3)
 
+    # PCA: components and scores, variance normalised (the default) and not
+    Uc, Sc = pyLOM.PCA.run(X)
+    Uc2, Sc2 = pyLOM.PCA.run(X, divide_variance=False)
+    np.savez_compressed(os.path.join(HERE, "pca.npz"), X=X, U=Uc, scores=Sc, U_nv=Uc2, scores_nv=Sc2)
+
     # truncation residual cases
     Ss = np.sort(np.abs(rng.standard_normal(50)))[::-1] ** 3
     rs = np.array([1e-1, 1e-2, 1e-4, 1e-8, -0.5, -0.9, -0.99, -1.0])
@@ -193,6 +198,19 @@ def main(refroot):
     X = pod_field(16, 16, 48, 10, seed=1002)
     U, S, V = pyLOM.POD.run(X, remove_mean=False, randomized=True, r=12, q=3, seed=25)
     np.savez_compressed(os.path.join(HERE, "pod_randomized.npz"), X=X, U=U, S=S, V=V, r=12, q=3, seed=25)
+
+    # streaming range finder: two batches of snapshots; the Omegas the
+    # reference draws (seed 7, then numpy's global stream) are stored too
+    Xs1 = pod_field(16, 16, 40, 10, seed=1006)
+    Xs2 = pod_field(16, 16, 24, 10, seed=1007)
+    Q1, B1, Y1 = pyLOM.math.init_qr_streaming(Xs1, 8, 2, seed=7)
+    Y1 = Y1.copy()
+    Q2, B2, Y2 = pyLOM.math.update_qr_streaming(Xs2, Q1, B1, Y1.copy(), 8, 2)
+    np.random.seed(seed=7)
+    om1 = np.random.rand(Xs1.shape[1], 8).astype(Xs1.dtype)
+    om2 = np.random.rand(Xs2.shape[1], 8).astype(Xs2.dtype)
+    np.savez_compressed(os.path.join(HERE, "qr_streaming.npz"), X1=Xs1, X2=Xs2, Q1=Q1, B1=B1, Y1=Y1,
+                        Q2=Q2, B2=B2, Y2=Y2, om1=om1, om2=om2, r=8, q=2, seed=7)
 
     # DMD
     Xd, lam = dmd_field(500, 48, 4, seed=1003)

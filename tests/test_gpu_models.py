@@ -146,6 +146,18 @@ def test_spod_defaults_golden(golden):
     np.testing.assert_allclose(Lm, g["L"], rtol=1e-4, atol=1e-6 * g["L"].max())
 
 
+@pytest.mark.parametrize("divide_variance,ukey,skey", [(True, "U", "scores"),
+                                                        (False, "U_nv", "scores_nv")])
+def test_pca_golden(golden, divide_variance, ukey, skey):
+    """PCA.run: components and scores of the reference (10 signal modes)."""
+    from tests.helpers import cols_up_to_phase
+    g = golden("pca")
+    U, sc = P.PCA.run(g["X"], divide_variance=divide_variance)
+    assert U.shape == g[ukey].shape and sc.shape == g[skey].shape
+    cols_up_to_phase(U[:, :10], g[ukey][:, :10], 1e-8)
+    cols_up_to_phase(sc[:, :10], g[skey][:, :10], 1e-8)
+
+
 @pytest.mark.parametrize("dt", [torch.complex64, torch.complex128])
 @pytest.mark.parametrize("G,M,nBlks,nf,f0", [(5, 1000, 63, 9, 3), (1, 77, 8, 4, 0), (16, 300, 64, 16, 0)])
 def test_spod_mode_layout(dt, G, M, nBlks, nf, f0):

@@ -162,6 +162,53 @@ def test_tsqr_svd_host_entry(dtype, precision):
     np.testing.assert_array_equal(Sn, S)
 
 
+def test_qr_streaming_matches_reference(golden):
+    """init/update_qr_streaming with the reference's own Omegas reproduce its
+    Q, B and Y (FP64 data, FP64 form); tsqr's factors carry Householder QR's
+    column signs, so the update's Yo + Yn sums the same columns."""
+    g = golden("qr_streaming")
+    r, q = int(g["r"]), int(g["q"])
+    Q1, B1, Y1 = P.math.init_qr_streaming(g["X1"], r, q, omega=g["om1"])
+    assert isinstance(Q1, np.ndarray) and Q1.shape == g["Q1"].shape and B1.shape == g["B1"].shape
+    np.testing.assert_allclose(Q1, g["Q1"], rtol=0, atol=1e-10)
+    np.testing.assert_allclose(B1, g["B1"], rtol=0, atol=1e-10 * np.abs(g["B1"]).max())
+    np.testing.assert_allclose(Y1, g["Y1"], rtol=0, atol=1e-10 * np.abs(g["Y1"]).max())
+    Yo = Y1.copy()
+    Q2, B2, Y2 = P.math.update_qr_streaming(g["X2"], Q1, B1, Yo, r, q, omega=g["om2"])
+    assert Y2 is Yo  # Yo += Yn in the caller's array, as the reference does
+    np.testing.assert_allclose(Q2, g["Q2"], rtol=0, atol=1e-10)
+    np.testing.assert_allclose(B2, g["B2"], rtol=0, atol=1e-10 * np.abs(g["B2"]).max())
+    np.testing.assert_allclose(Y2, g["Y2"], rtol=0, atol=1e-10 * np.abs(g["Y2"]).max())
+
+
+def test_qr_streaming_f32_mixed_and_philox():
+    """FP32 batches (mixed form) against the FP64 oracle with the same Omegas,
+    and the Philox draws: a seeded init and its updates are deterministic."""
+    from pyloworder_gb300 import datagen
+    X1 = datagen.pod_field_np(64, 64, 40, 8, seed=31, noise=1e-6).astype(np.float32)
+    X2 = datagen.pod_field_np(64, 64, 30, 8, seed=32, noise=1e-6).astype(np.float32)
+    r, q = 8, 2
+    om1 = O.philox_uniform((40, r), 5, np.float32)
+    om2 = O.philox_uniform((30, r), 6, np.float32)
+    Q1, B1, Y1 = P.math.init_qr_streaming(X1, r, q, omega=om1)
+    Q2, B2, Y2 = P.math.update_qr_streaming(X2, Q1, B1, Y1.copy(), r, q, omega=om2)
+    q1, b1, y1 = O.init_qr_streaming(X1.astype(np.float64), r, q, omega=om1.astype(np.float64))
+    q2, b2, y2 = O.update_qr_streaming(X2.astype(np.float64), q1, b1, y1.copy(), r, q,
+                                       omega=om2.astype(np.float64))
+    # the leading modes of the streamed basis (U = Q2 Ur over svd(B2))
+    Ur, S, _ = np.linalg.svd(B2.astype(np.float64), full_matrices=False)
+    ur, s, _ = np.linalg.svd(b2, full_matrices=False)
+    assert sigma_rel(S, s, 6) < 1e-4
+    assert subspace_angle(Q2 @ Ur[:, :6], q2 @ ur[:, :6]) < 1e-4
+    assert orthogonality(Q2) < 1e-5
+    # Philox: same seed, same results
+    a = P.math.init_qr_streaming(X1, r, q, seed=99)
+    ua = P.math.update_qr_streaming(X2, a[0], a[1], a[2].copy(), r, q)
+    b = P.math.init_qr_streaming(X1, r, q, seed=99)
+    ub = P.math.update_qr_streaming(X2, b[0], b[1], b[2].copy(), r, q)
+    np.testing.assert_array_equal(ua[1], ub[1])
+
+
 def test_randomized_philox_matches_oracle():
     rng = np.random.default_rng(5)
     X = (rng.standard_normal((3000, 12)) @ rng.standard_normal((12, 120))

@@ -82,6 +82,34 @@ def test_randomized_numpy_omega(golden):
     _cols_match_up_to_sign(U, g["U"], 1e-8)
 
 
+def test_pca(golden):
+    g = golden("pca")
+    U, sc = O.pca_run(g["X"])
+    _cols_match_up_to_sign(U[:, :10], g["U"][:, :10], 1e-8)
+    _cols_match_up_to_sign(sc[:, :10], g["scores"][:, :10], 1e-8)
+    U2, sc2 = O.pca_run(g["X"], divide_variance=False)
+    _cols_match_up_to_sign(U2[:, :10], g["U_nv"][:, :10], 1e-8)
+    _cols_match_up_to_sign(sc2[:, :10], g["scores_nv"][:, :10], 1e-8)
+
+
+def test_qr_streaming(golden):
+    """init/update_qr_streaming with the reference's own Omegas."""
+    g = golden("qr_streaming")
+    r, q = int(g["r"]), int(g["q"])
+    Q1, B1, Y1 = O.init_qr_streaming(g["X1"], r, q, omega=g["om1"])
+    np.testing.assert_allclose(Q1, g["Q1"], rtol=0, atol=1e-12)
+    np.testing.assert_allclose(B1, g["B1"], rtol=0, atol=1e-10 * np.abs(g["B1"]).max())
+    np.testing.assert_allclose(Y1, g["Y1"], rtol=0, atol=1e-10 * np.abs(g["Y1"]).max())
+    Q2, B2, Y2 = O.update_qr_streaming(g["X2"], Q1, B1, Y1, r, q, omega=g["om2"])
+    assert B2.shape == (r, g["X1"].shape[1] + g["X2"].shape[1])
+    np.testing.assert_allclose(Q2, g["Q2"], rtol=0, atol=1e-12)
+    np.testing.assert_allclose(B2, g["B2"], rtol=0, atol=1e-10 * np.abs(g["B2"]).max())
+    np.testing.assert_allclose(Y2, g["Y2"], rtol=0, atol=1e-10 * np.abs(g["Y2"]).max())
+    # the seeded draw is the reference's: seed(7), then the global stream
+    Qs, Bs, Ys = O.init_qr_streaming(g["X1"], r, q, seed=int(g["seed"]))
+    np.testing.assert_allclose(Qs, g["Q1"], rtol=0, atol=1e-12)
+
+
 @pytest.mark.parametrize("name", ["dmd_small", "dmd_small_mean"])
 def test_dmd(golden, name):
     g = golden(name)
