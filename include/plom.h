@@ -182,6 +182,28 @@ int plom_spod_fft(int dtype, const void* Y, int64_t M, int64_t N, int64_t ldy, i
 int plom_spod_modes(int dtype, const void* U, int64_t G, int64_t M, int64_t nBlks,
                     int64_t ustride, void* P, int64_t nf, int64_t f0, void* stream);
 
+/* ---- packed tall operands (mixed form) --------------------------------- */
+/* No counterpart in the reference.  A caller that multiplies the same FP32
+   matrix X (m x N, ldx) several times -- the streaming range finder uses one
+   batch of snapshots in every product of a batch -- packs it once into a
+   device buffer of plom_packed_bytes(m, N) bytes (two fp16 planes with
+   per-column power-of-two scales, the mixed form's operand) and passes the
+   buffer to the products:
+     plom_packed_apply: C (m x k FP32, ldc) = X W, W N x k FP64 (ldw);
+     plom_packed_tn:    C (Na x Nb FP64, ldc) = Xa^T Xb, both packed with
+                        the same m rows.
+   Buffers and workspaces are device memory; info as everywhere. */
+size_t plom_packed_bytes(int64_t m, int64_t N);
+int plom_pack(const void* X, int64_t m, int64_t N, int64_t ldx, void* packed, size_t bytes,
+              void* stream);
+size_t plom_packed_apply_workspace(int64_t m, int64_t N, int64_t k);
+int plom_packed_apply(const void* packed, int64_t m, int64_t N, const double* W, int64_t ldw,
+                      int64_t k, void* C, int64_t ldc, void* ws, size_t ws_bytes, int* info,
+                      void* stream);
+size_t plom_packed_tn_workspace(int64_t m, int64_t Na, int64_t Nb);
+int plom_packed_tn(const void* pa, int64_t Na, const void* pb, int64_t Nb, int64_t m, double* C,
+                   int64_t ldc, void* ws, size_t ws_bytes, int* info, void* stream);
+
 /* ---- allocation-free reduction product ------------------------------- */
 /* No counterpart in the reference.  For callers that cannot allocate device
    memory -- a host integration whose device memory is owned by another

@@ -209,14 +209,23 @@ __global__ void __launch_bounds__(256) colmax_kernel(const float* __restrict__ Y
   Y += (int64_t)blockIdx.y * bstride;
   cmax += (int64_t)blockIdx.y * N;
   const int64_t rows = (m + gridDim.x - 1) / gridDim.x;
-  const int64_t r0 = (int64_t)blockIdx.x * rows;
-  const int64_t r1 = (r0 + rows < m) ? r0 + rows : m;
+  const int64_t r0b = (int64_t)blockIdx.x * rows;
+  const int64_t r1 = (r0b + rows < m) ? r0b + rows : m;
+  // narrow matrices: the block's threads split into (row lane, column group)
+  // so that all of them read; rows r0b + tr, r0b + tr + TR, ...
+  const int groups = vec ? N / 4 : N;
+  const int TR = groups >= (int)blockDim.x ? 1 : (int)blockDim.x / groups;
+  const int tr = (int)threadIdx.x / (groups >= (int)blockDim.x ? (int)blockDim.x : groups);
+  const int tc = (int)threadIdx.x - tr * (groups >= (int)blockDim.x ? (int)blockDim.x : groups);
+  if (tr >= TR) return;
+  const int cstep = groups >= (int)blockDim.x ? (int)blockDim.x : groups;
+  const int64_t r0 = r0b + tr;
   if (vec) {
-    for (int c = threadIdx.x * 4; c < N; c += blockDim.x * 4) {
+    for (int c = tc * 4; c < N; c += cstep * 4) {
       float4 mx = make_float4(0.f, 0.f, 0.f, 0.f);
       const float* p = Y + r0 * ld + c;
 #pragma unroll 8
-      for (int64_t r = r0; r < r1; ++r, p += ld) {
+      for (int64_t r = r0; r < r1; r += TR, p += TR * ld) {
         const float4 v = __ldg(reinterpret_cast<const float4*>(p));
         mx.x = fmaxf(mx.x, fabsf(v.x));
         mx.y = fmaxf(mx.y, fabsf(v.y));
@@ -229,11 +238,11 @@ __global__ void __launch_bounds__(256) colmax_kernel(const float* __restrict__ Y
       if (mx.w > 0.f) atomicMax(&cmax[c + 3], __float_as_uint(mx.w));
     }
   } else {
-    for (int c = threadIdx.x; c < N; c += blockDim.x) {
+    for (int c = tc; c < N; c += cstep) {
       float mx = 0.f;
       const float* p = Y + r0 * ld + c;
 #pragma unroll 8
-      for (int64_t r = r0; r < r1; ++r, p += ld) mx = fmaxf(mx, fabsf(__ldg(p)));
+      for (int64_t r = r0; r < r1; r += TR, p += TR * ld) mx = fmaxf(mx, fabsf(__ldg(p)));
       if (mx > 0.f) atomicMax(&cmax[c], __float_as_uint(mx));
     }
   }
@@ -534,27 +543,37 @@ __global__ void __launch_bounds__(320, 1)
       const uint32_t cb = (uint32_t)(c >> 6) * G_BOX;
       const uint32_t w = (uint32_t)(c & 63);
       const uint32_t ch = w >> 3, within = (w & 7u) * 2u;
-      float sum = 0.f, cmp = 0.f;
+      // two independent compensated chains (even and odd rows) halve the
+      // dependent latency per stage, so the diagonal keeps pace with the MMA
+      float sum0 = 0.f, cmp0 = 0.f, sum1 = 0.f, cmp1 = 0.f;
       for (int kb = 0; kb < KB; ++kb) {
         const int s = kb % G_STAGES;
         const uint32_t ph = (uint32_t)(kb / G_STAGES) & 1u;
         if (!mbar_wait(&full_bar[s], ph, &abort_sh, err)) break;
         const uint32_t st = base + s * G_STAGE + cb;
-#pragma unroll 8
-        for (uint32_t k = 0; k < (uint32_t)G_BK; ++k) {
-          const uint32_t off = (k >> 3) * 1024u + (k & 7u) * 128u + (((ch ^ (k & 7u)) << 4) | within);
-          const float v = __half2float(__ushort_as_half(ld_shared_u16(st + off))) +
-                          __half2float(__ushort_as_half(ld_shared_u16(st + G_TILE + off)));
-          const float y = fmaf(v, v, -cmp);
-          const float t = sum + y;
-          cmp = (t - sum) - y;
-          sum = t;
+#pragma unroll 4
+        for (uint32_t k = 0; k < (uint32_t)G_BK; k += 2) {
+          const uint32_t off0 = (k >> 3) * 1024u + (k & 7u) * 128u + (((ch ^ (k & 7u)) << 4) | within);
+          const uint32_t k1 = k + 1;
+          const uint32_t off1 = (k1 >> 3) * 1024u + (k1 & 7u) * 128u + (((ch ^ (k1 & 7u)) << 4) | within);
+          const float v0 = __half2float(__ushort_as_half(ld_shared_u16(st + off0))) +
+                           __half2float(__ushort_as_half(ld_shared_u16(st + G_TILE + off0)));
+          const float v1 = __half2float(__ushort_as_half(ld_shared_u16(st + off1))) +
+                           __half2float(__ushort_as_half(ld_shared_u16(st + G_TILE + off1)));
+          const float y0 = fmaf(v0, v0, -cmp0);
+          const float y1 = fmaf(v1, v1, -cmp1);
+          const float t0 = sum0 + y0;
+          const float t1 = sum1 + y1;
+          cmp0 = (t0 - sum0) - y0;
+          cmp1 = (t1 - sum1) - y1;
+          sum0 = t0;
+          sum1 = t1;
         }
         mbar_arrive(&empty_bar[s]);
         if ((kb % KB_PER_SUB) == KB_PER_SUB - 1 || kb == KB - 1) {
           const int b = (kb / KB_PER_SUB) & 1;
-          diag_sh[b][c] = (double)sum - (double)cmp;
-          sum = cmp = 0.f;
+          diag_sh[b][c] = ((double)sum0 - (double)cmp0) + ((double)sum1 - (double)cmp1);
+          sum0 = cmp0 = sum1 = cmp1 = 0.f;
           mbar_arrive(&dfull[b]);
         }
       }
@@ -1370,3 +1389,99 @@ int renorm_long_columns(const double* M, int N, int n, int cw, float* U, int64_t
 }
 
 }  // namespace plom
+
+// ---------------------------------------------------------------------------
+// C ABI: packed tall operands kept by the caller.  A buffer holds the two
+// fp16 planes (m x ld each), the ld column scales and the column-maxima
+// scratch of the packing; products read it as often as the caller needs (the
+// streaming range finder packs a batch of snapshots once for all its
+// products).
+// ---------------------------------------------------------------------------
+using namespace plom;
+
+namespace {
+struct PackedBuf {
+  Packed p;
+  char* scratch;
+  size_t scratch_bytes;
+};
+size_t packed_buf_layout(int64_t m, int64_t N, void* base, PackedBuf* out) {
+  Arena a(base, ~size_t(0) >> 1);
+  Packed p;
+  packed_carve(a, p, m, N);
+  const size_t scr0 = (a.off + 255) / 256 * 256;
+  a.off = scr0 + sizeof(unsigned) * (size_t)N + 256;
+  if (out) {
+    out->p = p;
+    out->scratch = base ? static_cast<char*>(base) + scr0 : nullptr;
+    out->scratch_bytes = sizeof(unsigned) * (size_t)N + 256;
+  }
+  return a.off;
+}
+}  // namespace
+
+extern "C" size_t plom_packed_bytes(int64_t m, int64_t N) {
+  if (m < 1 || N < 1) return 0;
+  return packed_buf_layout(m, N, nullptr, nullptr);
+}
+
+extern "C" int plom_pack(const void* X, int64_t m, int64_t N, int64_t ldx, void* packed,
+                         size_t bytes, void* stream) {
+  PLOM_REQUIRE(X && packed && m >= 1 && N >= 1 && ldx >= N, PLOM_ERR_ARG, "pack: bad arguments");
+  PLOM_REQUIRE(m < (1ll << 31), PLOM_ERR_UNSUPPORTED, "pack: m >= 2^31");
+  PLOM_REQUIRE(bytes >= plom_packed_bytes(m, N), PLOM_ERR_WORKSPACE, "pack: buffer too small");
+  PackedBuf b;
+  packed_buf_layout(m, N, packed, &b);
+  Arena scr(b.scratch, b.scratch_bytes);
+  return pack_f32(static_cast<const float*>(X), ldx, m, N, b.p, scr, (cudaStream_t)stream);
+}
+
+extern "C" size_t plom_packed_apply_workspace(int64_t m, int64_t N, int64_t k) {
+  if (m < 1 || N < 1 || k < 1) return 0;
+  Packed p;
+  Arena a(nullptr, 0);
+  packed_carve(a, p, m, N);  // only to size the product's own workspace below
+  Arena w(nullptr, 0);
+  apply_packed(p, nullptr, k, k, nullptr, k, nullptr, nullptr, w, 0);
+  return w.off + 1024;
+}
+
+extern "C" int plom_packed_apply(const void* packed, int64_t m, int64_t N, const double* W,
+                                 int64_t ldw, int64_t k, void* C, int64_t ldc, void* ws,
+                                 size_t ws_bytes, int* info, void* stream) {
+  PLOM_REQUIRE(packed && W && C && ws && info && m >= 1 && N >= 1 && k >= 1 && ldw >= k &&
+                   ldc >= k,
+               PLOM_ERR_ARG, "packed_apply: bad arguments");
+  PLOM_REQUIRE(ws_bytes >= plom_packed_apply_workspace(m, N, k), PLOM_ERR_WORKSPACE,
+               "packed_apply: workspace too small");
+  PackedBuf b;
+  packed_buf_layout(m, N, const_cast<void*>(packed), &b);
+  Arena a(ws, ws_bytes);
+  return apply_packed(b.p, W, ldw, k, static_cast<float*>(C), ldc, nullptr, info, a,
+                      (cudaStream_t)stream);
+}
+
+extern "C" size_t plom_packed_tn_workspace(int64_t m, int64_t Na, int64_t Nb) {
+  if (m < 1 || Na < 1 || Nb < 1) return 0;
+  Packed pa, pb;
+  Arena a(nullptr, 0);
+  packed_carve(a, pa, m, Na);
+  packed_carve(a, pb, m, Nb);
+  Arena w(nullptr, 0);
+  tn_packed(pa, pb, nullptr, Nb, nullptr, w, 0);
+  return w.off + 1024;
+}
+
+extern "C" int plom_packed_tn(const void* pa, int64_t Na, const void* pb, int64_t Nb, int64_t m,
+                              double* C, int64_t ldc, void* ws, size_t ws_bytes, int* info,
+                              void* stream) {
+  PLOM_REQUIRE(pa && pb && C && ws && info && m >= 1 && Na >= 1 && Nb >= 1 && ldc >= Nb,
+               PLOM_ERR_ARG, "packed_tn: bad arguments");
+  PLOM_REQUIRE(ws_bytes >= plom_packed_tn_workspace(m, Na, Nb), PLOM_ERR_WORKSPACE,
+               "packed_tn: workspace too small");
+  PackedBuf a, b;
+  packed_buf_layout(m, Na, const_cast<void*>(pa), &a);
+  packed_buf_layout(m, Nb, const_cast<void*>(pb), &b);
+  Arena w(ws, ws_bytes);
+  return tn_packed(a.p, b.p, C, ldc, info, w, (cudaStream_t)stream);
+}

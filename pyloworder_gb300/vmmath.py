@@ -419,6 +419,57 @@ def _tsqr_householder(Y, precision):
     return Q * s, R * s[:, None]
 
 
+def _pack_dev(x):
+    """Packed copy (plom_pack) of a float32 CUDA matrix with unit inner
+    stride: the mixed form's tall operand, reusable across products."""
+    m, N = x.shape
+    ld = L.rows_ld(x)
+    if ld is None:
+        x = x.contiguous()
+        ld = N
+    buf = L.workspace(L.load().plom_packed_bytes(m, N))
+    L.call("plom_pack", L.ptr(x), m, N, ld, L.ptr(buf), buf.numel(), L.stream_ptr())
+    return buf, m, N
+
+
+def _packed_apply(pk, W, infos):
+    """X W (m x k float32) for a packed X and an FP64 W (N x k)."""
+    t = L.torch()
+    buf, m, N = pk
+    W = W.to(t.float64).contiguous()
+    k = W.shape[1]
+    C = t.empty((m, k), dtype=t.float32, device="cuda")
+    ws = L.workspace(L.load().plom_packed_apply_workspace(m, N, k))
+    info = L.new_info()
+    L.call("plom_packed_apply", L.ptr(buf), m, N, L.ptr(W), k, k, L.ptr(C), k, L.ptr(ws), ws.numel(),
+           L.ptr(info), L.stream_ptr())
+    infos.append(info)
+    return C
+
+
+def _packed_tn(pa, pb, infos):
+    """Xa^T Xb (Na x Nb, FP64) for two packed matrices with the same rows."""
+    t = L.torch()
+    ba, m, Na = pa
+    bb, _, Nb = pb
+    C = t.empty((Na, Nb), dtype=t.float64, device="cuda")
+    ws = L.workspace(L.load().plom_packed_tn_workspace(m, Na, Nb))
+    info = L.new_info()
+    L.call("plom_packed_tn", L.ptr(ba), Na, L.ptr(bb), Nb, m, L.ptr(C), Nb, L.ptr(ws), ws.numel(),
+           L.ptr(info), L.stream_ptr())
+    infos.append(info)
+    return C
+
+
+def _range_packed(xp, om, q, precision, infos):
+    """Y = A Omega and q power steps Y = A (A^T tsqr(Y)) on a packed batch."""
+    Y = _packed_apply(xp, om, infos)
+    for _ in range(q):
+        Q, _ = _tsqr_householder(Y, precision)
+        Y = _packed_apply(xp, _packed_tn(xp, _pack_dev(Q), infos), infos)
+    return Y
+
+
 def _device_like(A, dtype):
     t = L.torch()
     if isinstance(A, t.Tensor):
@@ -445,6 +496,16 @@ def init_qr_streaming(Ai, r, q, seed=None, *, omega=None, precision=None):
         om = _uniform_device(n, r, seed, x.dtype)
     else:
         om = _device_like(omega, x.dtype)
+    if x.dtype == t.float32 and L.precision_code(precision, x) == L.PREC_MIXED:
+        # mixed form: the batch is packed once and read by every product
+        infos = []
+        xp = _pack_dev(x)
+        Y = _range_packed(xp, om, q, precision, infos)
+        Q, _ = _tsqr_householder(Y, precision)
+        B = _packed_tn(xp, _pack_dev(Q), infos).T.to(t.float32)
+        for info in infos:
+            L.check_info(info, "init_qr_streaming")
+        return cv.back(Q), cv.back(B.contiguous()), cv.back(Y)
     Y = matmul(x, om, precision=precision)
     for _ in range(q):
         Q, _ = _tsqr_householder(Y, precision)
@@ -476,14 +537,27 @@ def update_qr_streaming(Ai, Q1, B1, Yo, r, q, *, omega=None, seed=None, precisio
         om = _device_like(omega, x.dtype)
     q1 = _device_like(Q1, x.dtype)
     b1 = _device_like(B1, x.dtype)
-    Yn = matmul(x, om, precision=precision)
-    for _ in range(q):
-        Qp, _ = _tsqr_householder(Yn, precision)
-        Yn = matmul(x, matmul(x.T, Qp, precision=precision), precision=precision)
-    yo = _device_like(Yo, x.dtype) + Yn
-    Q2, _ = _tsqr_householder(yo, precision)
-    B2o = matmul(matmul(Q2.T, q1, precision=precision), b1, precision=precision)
-    B2n = matmul(Q2.T, x, precision=precision)
+    if x.dtype == t.float32 and L.precision_code(precision, x) == L.PREC_MIXED:
+        # mixed form: the batch is packed once and read by every product
+        infos = []
+        xp = _pack_dev(x)
+        yo = _device_like(Yo, x.dtype) + _range_packed(xp, om, q, precision, infos)
+        Q2, _ = _tsqr_householder(yo, precision)
+        q2p = _pack_dev(Q2)
+        Q2Q1 = _packed_tn(q2p, _pack_dev(q1), infos)
+        B2o = matmul(Q2Q1, b1.to(t.float64), precision="fp64").to(t.float32)
+        B2n = _packed_tn(xp, q2p, infos).T.to(t.float32)
+        for info in infos:
+            L.check_info(info, "update_qr_streaming")
+    else:
+        Yn = matmul(x, om, precision=precision)
+        for _ in range(q):
+            Qp, _ = _tsqr_householder(Yn, precision)
+            Yn = matmul(x, matmul(x.T, Qp, precision=precision), precision=precision)
+        yo = _device_like(Yo, x.dtype) + Yn
+        Q2, _ = _tsqr_householder(yo, precision)
+        B2o = matmul(matmul(Q2.T, q1, precision=precision), b1, precision=precision)
+        B2n = matmul(Q2.T, x, precision=precision)
     B2 = t.cat([B2o, B2n], dim=1)
     # Yo += Yn in the caller's array
     if isinstance(Yo, t.Tensor):

@@ -187,7 +187,11 @@ def test_qr_streaming_f32_mixed_and_philox():
     from pyloworder_gb300 import datagen
     X1 = datagen.pod_field_np(64, 64, 40, 8, seed=31, noise=1e-6).astype(np.float32)
     X2 = datagen.pod_field_np(64, 64, 30, 8, seed=32, noise=1e-6).astype(np.float32)
-    r, q = 8, 2
+    # one power step: Y = (A A^T) A Omega spans sigma^3 (3e5 down to 60 for
+    # the six leading modes here), all above the 22-bit operand level of the
+    # mixed form's tsqr; with q = 2 the spread sigma^5 puts the sixth mode at
+    # the operand noise (an FP32 QR would lose it too)
+    r, q = 8, 1
     om1 = O.philox_uniform((40, r), 5, np.float32)
     om2 = O.philox_uniform((30, r), 6, np.float32)
     Q1, B1, Y1 = P.math.init_qr_streaming(X1, r, q, omega=om1)
