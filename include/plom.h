@@ -158,6 +158,21 @@ int plom_fill_uniform(int dtype, void* out, int64_t count, uint64_t seed, void* 
    muReal, muImag (r), bJov (r complex, interleaved) in pyLOM's mode order,
    and Mphi (nt x r complex, interleaved) such that the DMD modes are
    Phi = Y2 Mphi (one tall product, plom_matmul with the real view). */
+/* the inputs of plom_dmd_reduced for FP32 snapshots, from span(U_r) alone
+   (replaces the U^T Y2 product of DMD/wrapper.py:78-84 and the use of the
+   FP32 S and V there): U (m x r, ld ldu) = the retained left singular vectors
+   of Y1 = Y[:, :-1], Y (m x n, ld ldy).  C = U^T U and B = U^T Y are formed
+   with exact products and double-float sums; R^T R = C gives the coordinates
+   Bt = R^-T B of Y in an orthonormal basis of span(U); the FP64 SVD
+   Bt[:, :n-1] = Vb S V'^T gives S (r), VT = V'^T (r x (n-1)) and
+   aux1 = Vb^T Bt[:, 1:] (r x (n-1)), all FP64 on the device.  In exact
+   arithmetic these equal S_r, V_r^T and U_r^T Y2; the reduced operator then
+   depends only on the subspace, not on the accuracy of U's norms, S or V.
+   Needs n >= 2 and 1 <= r <= min(n - 1, 1024). */
+size_t plom_dmd_project_workspace(int64_t m, int64_t n, int64_t r);
+int plom_dmd_project(const float* U, int64_t ldu, const float* Y, int64_t ldy, int64_t m,
+                     int64_t n, int64_t r, double* aux1, double* S, double* VT, void* ws,
+                     size_t ws_bytes, int* info, void* stream);
 size_t plom_dmd_reduced_workspace(int64_t r, int64_t nt);
 int plom_dmd_reduced(const double* aux1, const double* S, const double* VT, int64_t r, int64_t nt,
                      double* muReal, double* muImag, double* bJov, double* Mphi, void* ws,

@@ -31,12 +31,26 @@ def run_device(x, ld, r, remove_mean=True, precision=None):
     U = U[:, :N]
     S = S[:N]
     VT = VT[:N, :]
-    # aux1 = U^T Y2 (N x nt), reduction over the m points
     Y2 = Y[:, 1:]
-    aux1 = M._matmul_dev(U, U.stride(0), 1, Y2, ldy, N, nt, m, precision)
-    aux1 = aux1.to(t.float64).contiguous()
-    S64 = S.to(t.float64).contiguous()
-    VT64 = VT.to(t.float64).contiguous()
+    if Y.dtype == t.float32:
+        # FP32 factors: aux1, S and V^T recomputed from span(U_r) with exact
+        # products (plom_dmd_project), so the eigenvalues do not inherit the
+        # mutual inconsistency of the FP32 / mixed-form U, S and V
+        aux1 = t.empty((N, nt), dtype=t.float64, device="cuda")
+        S64 = t.empty(N, dtype=t.float64, device="cuda")
+        VT64 = t.empty((N, nt), dtype=t.float64, device="cuda")
+        ws = L.workspace(L.load().plom_dmd_project_workspace(m, n, N))
+        info = L.new_info()
+        L.call("plom_dmd_project", L.ptr(U), U.stride(0), L.ptr(Y), ldy, m, n, N, L.ptr(aux1),
+               L.ptr(S64), L.ptr(VT64), L.ptr(ws), ws.numel(), L.ptr(info), L.stream_ptr())
+        L.check_info(info, "DMD projection")
+        del ws
+    else:
+        # aux1 = U^T Y2 (N x nt), reduction over the m points
+        aux1 = M._matmul_dev(U, U.stride(0), 1, Y2, ldy, N, nt, m, precision)
+        aux1 = aux1.to(t.float64).contiguous()
+        S64 = S.to(t.float64).contiguous()
+        VT64 = VT.to(t.float64).contiguous()
     muR = t.empty(N, dtype=t.float64, device="cuda")
     muI = t.empty(N, dtype=t.float64, device="cuda")
     b = t.empty(2 * N, dtype=t.float64, device="cuda")

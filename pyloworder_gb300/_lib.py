@@ -76,6 +76,9 @@ PROTOS = {
                               c_vp, ctypes.c_double, c_vp, c_vp]),
     "plom_matmulp_static": (c_int, [c_int, c_vp, c_i64, c_vp, c_i64, c_vp, c_i64, c_i64, c_i64, c_i64,
                                     c_vp]),
+    "plom_dmd_project_workspace": (c_sz, [c_i64, c_i64, c_i64]),
+    "plom_dmd_project": (c_int, [c_vp, c_i64, c_vp, c_i64, c_i64, c_i64, c_i64, c_vp, c_vp, c_vp,
+                                 c_vp, c_sz, c_vp, c_vp]),
     "plom_dmd_reduced_workspace": (c_sz, [c_i64, c_i64]),
     "plom_dmd_reduced": (c_int, [c_vp, c_vp, c_vp, c_i64, c_i64, c_vp, c_vp, c_vp, c_vp, c_vp, c_sz,
                                  c_vp, c_vp]),

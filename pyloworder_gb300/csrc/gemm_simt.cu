@@ -414,6 +414,160 @@ template int gemm_tn_in_scratch<double, double, double>(const double*, int64_t, 
                                                         int64_t, int64_t, void*, size_t,
                                                         cudaStream_t);
 
+// ----------------------------------------------------------------------------
+// TN with blocked double-float sums:
+//   C(M x N, FP64) = A(K x M)^T B(K x N), A and B FP32, K = points.
+// Each thread sums 32 rows of products with FP32 FMAs (round-to-nearest, so
+// the block errors are unbiased, at most ~32 u of the block's |terms|) and
+// folds the block sum into a double-float accumulator with TwoSum; the
+// accumulator carries ~44 bits across the whole row chunk.  The relative
+// error of a chunk sum is then ~u / sqrt(blocks) instead of the ~u K drift
+// (and, on the tensor cores, the ~1e-5 truncation bias) of one long FP32
+// accumulation, at ~1.2 FP32 instructions per product (GB300 runs FP64 at
+// 1/64 of its FP32 rate).  Row-chunk partials are summed in FP64 in a fixed
+// order.  Used where a reduction over the points must be FP64-accurate (DMD's
+// projection onto span(U_r)).
+// 128 threads as 8 x 16, 4 x 8 outputs each (rows ty*4.., columns tx*4.. and
+// 64 + tx*4..), operands from shared memory as 16-byte vectors, the next
+// 32-row tile prefetched into registers while the current one is summed.
+// ----------------------------------------------------------------------------
+constexpr int DF_BM = 32, DF_BN = 128, DF_BK = 32, DF_THREADS = 128;
+
+__global__ void __launch_bounds__(DF_THREADS) gemm_tn_df_kernel(const float* __restrict__ A,
+                                                                int64_t lda,
+                                                                const float* __restrict__ B,
+                                                                int64_t ldb,
+                                                                double* __restrict__ part,
+                                                                int64_t M, int64_t N, int64_t K,
+                                                                int64_t kchunk, int64_t tm) {
+  constexpr int TM = 4, TN = 8;
+  constexpr int LA = DF_BK * DF_BM / DF_THREADS, LB = DF_BK * DF_BN / DF_THREADS;
+  static_assert(DF_BM == 8 * TM && DF_BN == 16 * TN, "tile / thread layout");
+  __shared__ __align__(16) float As[DF_BK][DF_BM];
+  __shared__ __align__(16) float Bs[DF_BK][DF_BN];
+  const int64_t i0 = (int64_t)(blockIdx.x % tm) * DF_BM, j0 = (int64_t)(blockIdx.x / tm) * DF_BN;
+  const int64_t kbeg = (int64_t)blockIdx.y * kchunk;
+  const int64_t kend = min(K, kbeg + kchunk);
+  const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+  float hi[TM][TN], lo[TM][TN];
+#pragma unroll
+  for (int i = 0; i < TM; ++i)
+#pragma unroll
+    for (int j = 0; j < TN; ++j) hi[i][j] = lo[i][j] = 0.f;
+  float ra[LA], rb[LB];
+  auto load = [&](int64_t k0) {
+#pragma unroll
+    for (int q = 0; q < LA; ++q) {
+      const int e = threadIdx.x + q * DF_THREADS;
+      const int64_t gk = k0 + e / DF_BM, gi = i0 + e % DF_BM;
+      ra[q] = (gk < kend && gi < M) ? A[gk * lda + gi] : 0.f;
+    }
+#pragma unroll
+    for (int q = 0; q < LB; ++q) {
+      const int e = threadIdx.x + q * DF_THREADS;
+      const int64_t gk = k0 + e / DF_BN, gj = j0 + e % DF_BN;
+      rb[q] = (gk < kend && gj < N) ? B[gk * ldb + gj] : 0.f;
+    }
+  };
+  if (kbeg < kend) load(kbeg);
+  for (int64_t k0 = kbeg; k0 < kend; k0 += DF_BK) {
+#pragma unroll
+    for (int q = 0; q < LA; ++q) {
+      const int e = threadIdx.x + q * DF_THREADS;
+      As[e / DF_BM][e % DF_BM] = ra[q];
+    }
+#pragma unroll
+    for (int q = 0; q < LB; ++q) {
+      const int e = threadIdx.x + q * DF_THREADS;
+      Bs[e / DF_BN][e % DF_BN] = rb[q];
+    }
+    __syncthreads();
+    if (k0 + DF_BK < kend) load(k0 + DF_BK);
+    float s[TM][TN];
+#pragma unroll
+    for (int i = 0; i < TM; ++i)
+#pragma unroll
+      for (int j = 0; j < TN; ++j) s[i][j] = 0.f;
+#pragma unroll 8
+    for (int kk = 0; kk < DF_BK; ++kk) {
+      const float4 av = *reinterpret_cast<const float4*>(&As[kk][ty * TM]);
+      const float4 b0 = *reinterpret_cast<const float4*>(&Bs[kk][tx * 4]);
+      const float4 b1 = *reinterpret_cast<const float4*>(&Bs[kk][64 + tx * 4]);
+      const float a[TM] = {av.x, av.y, av.z, av.w};
+      const float b[TN] = {b0.x, b0.y, b0.z, b0.w, b1.x, b1.y, b1.z, b1.w};
+#pragma unroll
+      for (int i = 0; i < TM; ++i)
+#pragma unroll
+        for (int j = 0; j < TN; ++j) s[i][j] = fmaf(a[i], b[j], s[i][j]);
+    }
+    // fold the block sums: (hi, lo) += s with TwoSum
+#pragma unroll
+    for (int i = 0; i < TM; ++i)
+#pragma unroll
+      for (int j = 0; j < TN; ++j) {
+        const float t = hi[i][j] + s[i][j];
+        const float bb = t - hi[i][j];
+        lo[i][j] += (hi[i][j] - (t - bb)) + (s[i][j] - bb);
+        hi[i][j] = t;
+      }
+    __syncthreads();
+  }
+  double* P = part + (int64_t)blockIdx.y * M * N;
+#pragma unroll
+  for (int i = 0; i < TM; ++i) {
+    const int64_t gi = i0 + ty * TM + i;
+    if (gi >= M) continue;
+#pragma unroll
+    for (int j = 0; j < TN; ++j) {
+      const int64_t gj = j0 + (j < 4 ? tx * 4 + j : 64 + tx * 4 + (j - 4));
+      if (gj < N) P[gi * N + gj] = (double)hi[i][j] + (double)lo[i][j];
+    }
+  }
+}
+
+struct DfPlan {
+  int64_t tm, tn, kchunk;
+  int chunks;
+};
+static DfPlan df_plan(int64_t M, int64_t N, int64_t K) {
+  DfPlan p;
+  p.tm = cdiv(M, DF_BM);
+  p.tn = cdiv(N, DF_BN);
+  int c = tn_chunks(p.tm * p.tn, K, DF_BK, 1);
+  int64_t kc = cdiv(std::max<int64_t>(K, 1), c);
+  kc = cdiv(kc, DF_BK) * DF_BK;
+  p.kchunk = kc;
+  p.chunks = (int)std::max<int64_t>(1, cdiv(K, kc));
+  return p;
+}
+
+int gemm_tn_df(const float* A, int64_t lda, const float* B, int64_t ldb, double* C, int64_t ldc,
+               int64_t M, int64_t N, int64_t K, Arena& ws, cudaStream_t st) {
+  if (M == 0 || N == 0) return PLOM_OK;
+  const DfPlan p = df_plan(M, N, K);
+  double* part = ws.take<double>((size_t)p.chunks * M * N);
+  if (ws.measuring()) return PLOM_OK;
+  PLOM_REQUIRE(!ws.overflow(), PLOM_ERR_WORKSPACE, "gemm_tn_df: workspace too small");
+  PLOM_REQUIRE(A && B && C && part, PLOM_ERR_ARG, "gemm_tn_df: null operand");
+  PLOM_REQUIRE(p.tm * p.tn <= INT32_MAX && p.chunks <= 65535, PLOM_ERR_ARG,
+               "gemm_tn_df: result too large");
+  ProfScope prof("gemm_tn_df", st, 2.0 * M * N * K, (double)K * (M + N) * sizeof(float),
+                 K > 0 ? 2 : 1);
+  if (K > 0) {
+    dim3 grid((unsigned)(p.tm * p.tn), (unsigned)p.chunks, 1u);
+    gemm_tn_df_kernel<<<grid, DF_THREADS, 0, st>>>(A, lda, B, ldb, part, M, N, K, p.kchunk, p.tm);
+    PLOM_CHECK_LAUNCH();
+  } else {
+    PLOM_CHECK_CUDA(cudaMemsetAsync(part, 0, sizeof(double) * M * N, st));
+  }
+  const int64_t total = M * N;
+  const int blocks = (int)std::min<int64_t>(cdiv(total, 256), (int64_t)num_sms() * 16);
+  reduce_partials_kernel<double, double><<<blocks, 256, 0, st>>>(part, K > 0 ? p.chunks : 1, M, N,
+                                                                 0, DF_BM, DF_BN, C, ldc, 0, 1);
+  PLOM_CHECK_LAUNCH();
+  return PLOM_OK;
+}
+
 // explicit instantiations used across the library
 #define NN(TA, TB, TC, ACC)                                                                  \
   template int gemm_nn<TA, TB, TC, ACC>(const TA*, int64_t, const TB*, int64_t, TC*, int64_t, \

@@ -45,6 +45,10 @@ int gemm_tn_in_scratch(const TA* A, int64_t lda, const TB* B, int64_t ldb, TC* C
                        cudaStream_t st);
 size_t gemm_tn_workspace_batched(int64_t M, int64_t N, int64_t K, bool sym, size_t acc_bytes,
                                  int batch);
+// C (M x N, FP64, ld ldc) = A^T B for FP32 A (K x M), B (K x N): exact products,
+// compensated double-float sums over row chunks, FP64 chunk reduction.
+int gemm_tn_df(const float* A, int64_t lda, const float* B, int64_t ldb, double* C, int64_t ldc,
+               int64_t M, int64_t N, int64_t K, Arena& ws, cudaStream_t st);
 
 // ---- dense.cu (FP64 small dense, batched, cooperative) ----
 // Upper Cholesky R^T R = G + s I of `batch` n x n matrices (stride n*n, ld n).

@@ -1261,6 +1261,96 @@ extern "C" size_t plom_matmul_workspace(int dtype, int prec, int transA, int64_t
   return bytes;
 }
 
+// ---------------------------------------------------------------------------
+// DMD's reduced operator on span(U_r) (pyLOM/DMD/wrapper.py:78-84 computes
+// U_r^T Y2 V_r S_r^-1 from the truncated SVD of Y1 = Y[:, :-1]).  With FP32
+// factors (and the mixed form's ~1e-5 tensor-core accumulation error in U, S,
+// V) that formula takes the factors' mutual inconsistency into the
+// eigenvalues.  Here every quantity is recomputed from span(U_r) alone:
+//   C = U_r^T U_r and B = U_r^T Y      (exact products, double-float sums),
+//   R^T R = C,  Bt = R^-T B            (coordinates of Y in an orthonormal
+//                                       basis Ut = U_r R^-1 of span(U_r)),
+//   Bt[:, :nt] = Vb S' V'^T            (FP64 SVD, through its transpose),
+//   aux1 = Vb^T Bt[:, 1:],  S',  V'^T  (for the reduced stage).
+// In exact arithmetic Ut Vb = U_r, S' = S_r, V' = V_r and aux1 = U_r^T Y2.
+// ---------------------------------------------------------------------------
+static int dmd_project_impl(const float* U, int64_t ldu, const float* Y, int64_t ldy, int64_t m,
+                            int n, int r, double* aux1, double* S, double* VT, int* info,
+                            Arena& ws, cudaStream_t st) {
+  const int nt = n - 1;
+  double* C = ws.take<double>((size_t)r * r);
+  double* B = ws.take<double>((size_t)r * n);
+  double* R = ws.take<double>((size_t)r * r);
+  double* W = ws.take<double>((size_t)r * r);
+  double* Wt = ws.take<double>((size_t)r * r);
+  double* Bt = ws.take<double>((size_t)r * n);
+  double* BtT = ws.take<double>((size_t)n * r);
+  double* Ub = ws.take<double>((size_t)nt * r);
+  double* VbH = ws.take<double>((size_t)r * r);
+  const size_t mark = ws.off;
+  size_t need = mark;
+  auto sub = [&](auto&& fn) -> int {
+    ws.off = mark;
+    const int s = fn();
+    need = std::max(need, ws.off);
+    ws.off = mark;
+    return s;
+  };
+  const bool meas = ws.measuring();
+  if (!meas) PLOM_REQUIRE(!ws.overflow(), PLOM_ERR_WORKSPACE, "dmd_project: workspace too small");
+  PLOM_TRY(sub([&] { return gemm_tn_df(U, ldu, U, ldu, C, r, r, r, m, ws, st); }));
+  PLOM_TRY(sub([&] { return gemm_tn_df(U, ldu, Y, ldy, B, n, r, n, m, ws, st); }));
+  const double u = 2.220446049250313e-16;
+  PLOM_TRY(sub([&] { return chol_shifted(C, R, r, 1, 0.0, 16.0 * u * r, info, ws, st); }));
+  PLOM_TRY(sub([&] { return trtri_upper(R, W, r, 1, ws, st); }));
+  if (!meas) {
+    PLOM_TRY(transpose_f64(W, Wt, r, r, 1, st));
+    PLOM_TRY((gemm_nn<double, double, double, double>(Wt, r, B, n, Bt, n, r, n, r, st)));
+    PLOM_TRY(transpose_f64(Bt, BtT, r, n, 1, st));  // rows 0..nt-1: Bt[:, :nt]^T
+  }
+  // Bt[:, :nt]^T (nt x r) = Ub S' VbH  ->  Bt[:, :nt] = Vb S' Ub^T
+  PLOM_TRY(sub([&] {
+    return tsqr_svd_impl<double, double>(PLOM_PREC_FP64, false, BtT, nt, r, r, Ub, r, S, VbH,
+                                         info, ws, st);
+  }));
+  if (!meas) {
+    // aux1 = Vb^T Bt[:, 1:] = VbH Bt[:, 1:];  V'^T = Ub^T
+    PLOM_TRY((gemm_nn<double, double, double, double>(VbH, r, Bt + 1, n, aux1, nt, r, nt, r, st)));
+    PLOM_TRY(transpose_f64(Ub, VT, nt, r, 1, st));
+  }
+  ws.off = need;
+  return PLOM_OK;
+}
+
+extern "C" size_t plom_dmd_project_workspace(int64_t m, int64_t n, int64_t r) {
+  if (m < 1 || n < 2 || r < 1 || r > n - 1 || r > 1024 || n > INT32_MAX) return 0;
+  size_t bytes = 0;
+  int dummy[PLOM_INFO_WORDS];
+  run_measured(&bytes, [&](Arena& a) {
+    return dmd_project_impl(nullptr, r, nullptr, n, m, (int)n, (int)r, nullptr, nullptr, nullptr,
+                            dummy, a, nullptr);
+  });
+  return bytes;
+}
+
+extern "C" int plom_dmd_project(const float* U, int64_t ldu, const float* Y, int64_t ldy,
+                                int64_t m, int64_t n, int64_t r, double* aux1, double* S,
+                                double* VT, void* ws, size_t ws_bytes, int* info, void* stream) {
+  PLOM_REQUIRE(m >= 1 && n >= 2 && r >= 1 && r <= n - 1 && r <= 1024 && n <= INT32_MAX,
+               PLOM_ERR_ARG, "dmd_project: need m >= 1, n >= 2 and 1 <= r <= min(n - 1, 1024)");
+  PLOM_REQUIRE(ldu >= r && ldy >= n, PLOM_ERR_ARG, "dmd_project: leading dimension too small");
+  PLOM_REQUIRE(U && Y && aux1 && S && VT && ws && info, PLOM_ERR_ARG,
+               "dmd_project: null pointer");
+  const size_t need = plom_dmd_project_workspace(m, n, r);
+  PLOM_REQUIRE(need > 0, PLOM_ERR_ARG, "dmd_project: workspace query failed");
+  PLOM_REQUIRE(ws_bytes >= need, PLOM_ERR_WORKSPACE, "dmd_project: workspace %zu < %zu", ws_bytes,
+               need);
+  cudaStream_t st = (cudaStream_t)stream;
+  PLOM_CHECK_CUDA(cudaMemsetAsync(info, 0, sizeof(int) * PLOM_INFO_WORDS, st));
+  Arena a(ws, ws_bytes);
+  return dmd_project_impl(U, ldu, Y, ldy, m, (int)n, (int)r, aux1, S, VT, info, a, st);
+}
+
 extern "C" int plom_matmul(int dtype, int prec, int transA, const void* A, int64_t lda,
                            const void* B, int64_t ldb, void* C, int64_t ldc, int64_t m, int64_t n,
                            int64_t k, void* ws, size_t ws_bytes, void* stream) {
