@@ -195,6 +195,13 @@ __device__ __forceinline__ uint16_t ld_shared_u16(uint32_t addr) {
   asm volatile("ld.shared.u16 %0, [%1];" : "=h"(v) : "r"(addr));
   return v;
 }
+__device__ __forceinline__ float2 ld_shared_h2f(uint32_t addr) {
+  uint32_t v;
+  asm volatile("ld.shared.b32 %0, [%1];" : "=r"(v) : "r"(addr));
+  __half2 h;
+  memcpy(&h, &v, sizeof(h));
+  return __half22float2(h);
+}
 
 // ---------------------------------------------------------------------------
 // packing
@@ -449,7 +456,7 @@ __global__ void __launch_bounds__(320, 1)
   extern __shared__ uint8_t smem_raw[];
   __shared__ uint64_t full_bar[G_STAGES], empty_bar[G_STAGES];
   __shared__ uint64_t tfull[2], tempty[2], dfull[2];
-  __shared__ double diag_sh[2][128];
+  __shared__ double diag_sh[2][2][128];  // [buffer][row half][column]
   __shared__ uint32_t tmem_sh;
   __shared__ int abort_sh;
   const uint32_t base = (smem_u32(smem_raw) + 1023u) & ~1023u;
@@ -537,43 +544,53 @@ __global__ void __launch_bounds__(320, 1)
       }
     }
   } else if (warp >= 4 && warp < 8) {
-    // ---- diagonal tiles: compensated sums of (hi + lo)^2 per column
+    // ---- diagonal tiles: compensated sums of (hi + lo)^2 per column.  A
+    // thread takes two adjacent columns (one 32-bit shared load per plane and
+    // row) over one half of each stage's rows, even and odd rows in separate
+    // chains: four independent compensated chains per thread, so the
+    // diagonal keeps pace with the MMA
     if (diag) {
-      const int c = threadIdx.x - 128;           // column of the I block
+      const int t = threadIdx.x - 128;
+      const int c = 2 * (t & 63);                // first of the two columns
+      const int h = t >> 6;                      // row half of each stage
       const uint32_t cb = (uint32_t)(c >> 6) * G_BOX;
       const uint32_t w = (uint32_t)(c & 63);
       const uint32_t ch = w >> 3, within = (w & 7u) * 2u;
-      // two independent compensated chains (even and odd rows) halve the
-      // dependent latency per stage, so the diagonal keeps pace with the MMA
-      float sum0 = 0.f, cmp0 = 0.f, sum1 = 0.f, cmp1 = 0.f;
+      const uint32_t k0 = (uint32_t)h * (G_BK / 2), k1 = k0 + G_BK / 2;
+      // chains: [column][row parity]
+      float sm[2][2] = {{0.f, 0.f}, {0.f, 0.f}}, cp[2][2] = {{0.f, 0.f}, {0.f, 0.f}};
       for (int kb = 0; kb < KB; ++kb) {
         const int s = kb % G_STAGES;
         const uint32_t ph = (uint32_t)(kb / G_STAGES) & 1u;
         if (!mbar_wait(&full_bar[s], ph, &abort_sh, err)) break;
         const uint32_t st = base + s * G_STAGE + cb;
 #pragma unroll 4
-        for (uint32_t k = 0; k < (uint32_t)G_BK; k += 2) {
-          const uint32_t off0 = (k >> 3) * 1024u + (k & 7u) * 128u + (((ch ^ (k & 7u)) << 4) | within);
-          const uint32_t k1 = k + 1;
-          const uint32_t off1 = (k1 >> 3) * 1024u + (k1 & 7u) * 128u + (((ch ^ (k1 & 7u)) << 4) | within);
-          const float v0 = __half2float(__ushort_as_half(ld_shared_u16(st + off0))) +
-                           __half2float(__ushort_as_half(ld_shared_u16(st + G_TILE + off0)));
-          const float v1 = __half2float(__ushort_as_half(ld_shared_u16(st + off1))) +
-                           __half2float(__ushort_as_half(ld_shared_u16(st + G_TILE + off1)));
-          const float y0 = fmaf(v0, v0, -cmp0);
-          const float y1 = fmaf(v1, v1, -cmp1);
-          const float t0 = sum0 + y0;
-          const float t1 = sum1 + y1;
-          cmp0 = (t0 - sum0) - y0;
-          cmp1 = (t1 - sum1) - y1;
-          sum0 = t0;
-          sum1 = t1;
+        for (uint32_t k = k0; k < k1; k += 2) {
+#pragma unroll
+          for (uint32_t u = 0; u < 2; ++u) {
+            const uint32_t kk = k + u;
+            const uint32_t off = (kk >> 3) * 1024u + (kk & 7u) * 128u + (((ch ^ (kk & 7u)) << 4) | within);
+            const float2 hv = ld_shared_h2f(st + off);
+            const float2 lv = ld_shared_h2f(st + G_TILE + off);
+            const float v[2] = {hv.x + lv.x, hv.y + lv.y};  // exact: 22 bits
+#pragma unroll
+            for (int q = 0; q < 2; ++q) {
+              const float y = fmaf(v[q], v[q], -cp[q][u]);
+              const float tt = sm[q][u] + y;
+              cp[q][u] = (tt - sm[q][u]) - y;
+              sm[q][u] = tt;
+            }
+          }
         }
         mbar_arrive(&empty_bar[s]);
         if ((kb % KB_PER_SUB) == KB_PER_SUB - 1 || kb == KB - 1) {
           const int b = (kb / KB_PER_SUB) & 1;
-          diag_sh[b][c] = ((double)sum0 - (double)cmp0) + ((double)sum1 - (double)cmp1);
-          sum0 = cmp0 = sum1 = cmp1 = 0.f;
+#pragma unroll
+          for (int q = 0; q < 2; ++q) {
+            diag_sh[b][h][c + q] = ((double)sm[q][0] - (double)cp[q][0]) +
+                                   ((double)sm[q][1] - (double)cp[q][1]);
+            sm[q][0] = sm[q][1] = cp[q][0] = cp[q][1] = 0.f;
+          }
           mbar_arrive(&dfull[b]);
         }
       }
@@ -629,7 +646,8 @@ __global__ void __launch_bounds__(320, 1)
       __syncwarp();
       if (!__all_sync(0xffffffffu, ready)) break;
       fence_after();
-      const float2 dval = diag ? dw_from_double(diag_sh[b][rloc]) : make_float2(0.f, 0.f);
+      const float2 dval =
+          diag ? dw_from_double(diag_sh[b][0][rloc] + diag_sh[b][1][rloc]) : make_float2(0.f, 0.f);
       float2* prow = P + (int64_t)rloc * 128;
 #pragma unroll 1
       for (int cc = 0; cc < 4; ++cc) {
