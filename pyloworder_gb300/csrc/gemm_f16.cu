@@ -747,7 +747,13 @@ constexpr int A_BK = 64;                       // K per stage (one 128-byte row)
 constexpr uint32_t A_TILE = 128 * 128;         // 128 rows x 64 fp16 (16 KB)
 constexpr uint32_t A_STAGE = 4 * A_TILE;       // A hi, A lo, B hi, B lo
 constexpr int A_STAGES = 3;
-constexpr uint32_t A_STG = 4 * 4096;           // epilogue staging: 32 rows x 128 bytes per warp
+// Warps: 0-7 epilogue (warp w drains TMEM lanes 32 (w % 4).. for the column
+// half w / 4 of the tile), 8 UMMA issuer (and TMEM owner), 9 TMA producer.
+// Eight epilogue warps keep short-K tiles (narrow problems, the first column
+// blocks of a triangular W) from being paced by the TMEM drain and stores.
+constexpr int A_EPI_WARPS = 8;
+constexpr int A_THREADS = 32 * (A_EPI_WARPS + 2);
+constexpr uint32_t A_STG = A_EPI_WARPS * 4096; // epilogue staging: 32 rows x 128 bytes per warp
 constexpr size_t A_SMEM = (size_t)A_STAGES * A_STAGE + A_STG + 1024;
 
 struct ApplyOut {
@@ -759,7 +765,7 @@ struct ApplyOut {
   int ldo;
 };
 
-__global__ void __launch_bounds__(192, 1)
+__global__ void __launch_bounds__(A_THREADS, 1)
     apply16_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
                    int64_t m, int kblocks, int k, int64_t col_tiles, int64_t tiles,
                    const float* __restrict__ f, ApplyOut out, int* err, int64_t mp,
@@ -803,16 +809,16 @@ __global__ void __launch_bounds__(192, 1)
     }
     for (int b = 0; b < 2; ++b) {
       mbar_init(&tfull[b], 1);
-      mbar_init(&tempty[b], 128);
+      mbar_init(&tempty[b], 32 * A_EPI_WARPS);
     }
     abort_sh = 0;
     mbar_fence_init();
   }
-  if (warp == 4) {
+  if (warp == A_EPI_WARPS) {
     tmem_alloc(&tmem_sh, 512);  // 2 buffers x (main 128 + correction 128)
     tmem_relinquish();
   }
-  if (warp == 5 && lane == 0) {
+  if (warp == A_EPI_WARPS + 1 && lane == 0) {
     tma_prefetch_map(&tmA);
     tma_prefetch_map(&tmB);
   }
@@ -821,7 +827,7 @@ __global__ void __launch_bounds__(192, 1)
   fence_after();
   const uint32_t tmem = tmem_sh;
 
-  if (warp == 5) {
+  if (warp == A_EPI_WARPS + 1) {
     // ---- TMA producer, running ahead across tiles
     if (lane == 0) {
       int64_t g = 0;
@@ -850,7 +856,7 @@ __global__ void __launch_bounds__(192, 1)
         }
       }
     }
-  } else if (warp == 4) {
+  } else if (warp == A_EPI_WARPS) {
     // ---- UMMA issuer
     if (lane == 0) {
       constexpr uint32_t idesc = idesc_f16(128, 128, 0, 0);
@@ -897,9 +903,10 @@ __global__ void __launch_bounds__(192, 1)
       }
     }
   } else {
-    // ---- epilogue (warps 0-3): TMEM -> scale -> FP32 or packed store
+    // ---- epilogue (warps 0-7): TMEM -> scale -> FP32 or packed store
     uint4* stg = reinterpret_cast<uint4*>(smem_raw + (base - smem_u32(smem_raw)) +
                                           A_STAGES * A_STAGE + warp * 4096);
+    const int quarter = warp & 3, half = warp >> 2;  // TMEM lane quarter, column half
     int i = 0;
     for (int64_t it = 0; it < my_tiles; ++it) {
       const int64_t t = apply_tile(it);
@@ -912,14 +919,14 @@ __global__ void __launch_bounds__(192, 1)
       const int64_t pb = t / (row_tiles * col_tiles);
       const int64_t rt = t - pb * row_tiles * col_tiles;
       const int64_t rb = rt / col_tiles, cb = rt % col_tiles;
-      const int64_t row0 = rb * 128 + warp * 32;  // first row of this warp (within the problem)
+      const int64_t row0 = rb * 128 + quarter * 32;  // first row of this warp (within the problem)
       const float* fp = f + pb * fstride;
       const bool c_vec = out.C && ((out.ldc & 3) == 0) && ((out.cstride & 3) == 0) &&
                          ((reinterpret_cast<uintptr_t>(out.C) & 15) == 0);
 #pragma unroll 1
-      for (int cc = 0; cc < 4; ++cc) {
+      for (int cc = 2 * half; cc < 2 * half + 2; ++cc) {
         uint32_t rm[32], rc[32];
-        const uint32_t ta = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(b * 256 + cc * 32);
+        const uint32_t ta = tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(b * 256 + cc * 32);
         tmem_ld32(ta, rm);
         tmem_ld32(ta + 128, rc);
         tmem_wait_ld();
@@ -989,7 +996,7 @@ __global__ void __launch_bounds__(192, 1)
   }
   fence_before();
   __syncthreads();
-  if (warp == 4) {
+  if (warp == A_EPI_WARPS) {
     __syncwarp();
     fence_after();
     tmem_dealloc(tmem, 512);
@@ -1364,7 +1371,7 @@ int apply_packed(const Packed& p, const double* W, int64_t ldw, int64_t k, float
   const bool tri = tri_pre;
   const double flops = tri ? (double)m * p.N * (p.N + 1) * batch : 2.0 * m * p.N * k * batch;
   ProfScope prof("tc_apply_f16x3", st, flops, 4.0 * ((double)m * p.ld + (double)m * k) * batch);
-  hp::apply16_kernel<<<grid, 192, hp::A_SMEM, st>>>(tmA, tmB, m, (int)(ldk / 64), (int)k,
+  hp::apply16_kernel<<<grid, hp::A_THREADS, hp::A_SMEM, st>>>(tmA, tmB, m, (int)(ldk / 64), (int)k,
                                                     col_tiles, tiles, f, o, err, p.mp, row_tiles,
                                                     fstride, tri ? 1 : 0, by_rows);
   PLOM_CHECK_LAUNCH();

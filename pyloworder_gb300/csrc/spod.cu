@@ -213,25 +213,34 @@ __global__ void __launch_bounds__(256) spod_fft32_kernel(
         im[e] = 0.f;
       }
       warp_fft<E>(re, im, lane, N, sc, ss);
+      // bins f < nf = 16 E + 1: the even lanes hold f < 16 E (k2 = bitrev5(lane)
+      // < 16), lane 1 holds f = 16 E in register 0.  Staged at
+      // r * 16 + lane / 2 (and 16 E): one contiguous 128-byte row per register
+      // across the warp, no bank conflicts (f-indexed stores would hit two
+      // banks from all 32 lanes)
       const int k2 = (int)(__brev((unsigned)lane) >> 27);
-      c2<float>* out = stage + (size_t)b * nf;
+      float2* out = reinterpret_cast<float2*>(stage) + (size_t)b * nf;
 #pragma unroll
       for (int r = 0; r < E; ++r) {
         const int k1 = LOGE ? (int)(__brev((unsigned)r) >> (32 - LOGE)) : 0;
         const int f = k1 + E * k2;
-        if (f < nf) {
+        if ((lane & 1) == 0 || (lane == 1 && r == 0)) {
           const float g = (f >= 1 && f <= nf - 2) ? 2.f * scale : scale;
-          out[f].re = re[r] * g;
-          out[f].im = im[r] * g;
+          out[(lane & 1) ? 16 * E : r * 16 + (lane >> 1)] = make_float2(re[r] * g, im[r] * g);
         }
       }
     }
     __syncthreads();
-    // Q[f][row][b]: one contiguous run of nBlks values per frequency
+    // Q[f][row][b]: one contiguous run of nBlks values per frequency; the
+    // stage row stride nf is odd, so a warp reading consecutive blocks of one
+    // frequency spreads over all banks
     c2<float>* Qc = reinterpret_cast<c2<float>*>(Q);
     for (int e = tid; e < nf * nBlks; e += blockDim.x) {
       const int f = e / nBlks, b = e - f * nBlks;
-      Qc[((int64_t)f * M + row) * nBlks + b] = stage[(size_t)b * nf + f];
+      const int k1 = f % E, k2 = f / E;
+      const int r = LOGE ? (int)(__brev((unsigned)k1) >> (32 - LOGE)) : 0;
+      const int slot = (k2 == 16) ? 16 * E : r * 16 + (int)(__brev((unsigned)k2) >> 28);
+      Qc[((int64_t)f * M + row) * nBlks + b] = stage[(size_t)b * nf + slot];
     }
     __syncthreads();
   }
@@ -265,7 +274,8 @@ static int spod_fft_impl(const T* Y, int64_t M, int64_t N, int64_t ldy, int nDFT
   }
   if constexpr (sizeof(T) == 4) {
     const size_t stage = sizeof(c2<float>) * (size_t)nBlks * nf + sizeof(float) * 3 * nDFT;
-    if (log2n >= 5 && log2n <= 10 && stage <= 200 * 1024) {
+    // the register FFT stages the one-sided spectrum (nf = nDFT / 2 + 1)
+    if (log2n >= 5 && log2n <= 10 && nf == nDFT / 2 + 1 && stage <= 200 * 1024) {
       ProfScope prof("spod_fft", st, 5.0 * (double)M * nBlks * nDFT * log2n,
                      (double)sizeof(T) * ((double)M * N + 2.0 * M * nBlks * nf));
       switch (log2n) {
