@@ -123,9 +123,12 @@ __global__ void __launch_bounds__(256) spod_fft_kernel(
 // transforms one window in registers: lane l holds samples l + 32 e; an
 // E-point DIF FFT over its registers, twiddles w_N^(l k1), then a 32-point
 // DIF FFT across the lanes with shuffles.  Lane l, register r ends with bin
-// k1 + E k2, k1 = bitrev_E(r), k2 = bitrev_32(l).  A CTA owns one point (all
-// its Welch blocks); its bins are staged in shared memory as [block][bin]
-// and written per frequency as contiguous runs of nBlks values.
+// k1 + E k2, k1 = bitrev_E(r), k2 = bitrev_32(l).  Two real windows share one
+// complex transform (z = x_a + i x_b; X_a[f] = (Z[f] + conj Z[N-f]) / 2,
+// X_b[f] = (Z[f] - conj Z[N-f]) / 2i), which halves the FFT work.  A CTA owns
+// one point (all its Welch blocks); the pair spectra are staged in shared
+// memory in the register layout (one contiguous row per register across the
+// warp) and written per frequency as contiguous runs of nBlks values.
 // ---------------------------------------------------------------------------
 template <int E>
 __device__ __forceinline__ void warp_fft(float (&re)[E], float (&im)[E], int lane, int N,
@@ -192,7 +195,11 @@ __global__ void __launch_bounds__(256) spod_fft32_kernel(
   float* sw = reinterpret_cast<float*>(smem_raw);  // window [N]
   float* sc = sw + N;                              // cos    [N]
   float* ss = sc + N;                              // -sin   [N]
-  c2<float>* stage = reinterpret_cast<c2<float>*>(ss + N);  // [nBlks][nf]
+  // spectra of window pairs: [pair][N + 1] complex, bin f of a pair at slot
+  // r(f) 32 + lane(f) (the register layout of warp_fft)
+  float2* zs = reinterpret_cast<float2*>(ss + N);
+  constexpr int ZP = N + 1;  // odd pitch: consecutive pairs start 2 banks apart
+  const int npairs = (nBlks + 1) / 2;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   for (int j = tid; j < N; j += blockDim.x) {
     sw[j] = window[j];
@@ -201,46 +208,48 @@ __global__ void __launch_bounds__(256) spod_fft32_kernel(
   }
   __syncthreads();
   constexpr int LOGE = (E == 1) ? 0 : (E == 2) ? 1 : (E == 4) ? 2 : (E == 8) ? 3 : (E == 16) ? 4 : 5;
+  auto slot = [&](int f) -> int {  // f in [0, N)
+    const int k1 = f % E, k2 = f / E;
+    const int r = LOGE ? (int)(__brev((unsigned)k1) >> (32 - LOGE)) : 0;
+    return r * 32 + (int)(__brev((unsigned)k2) >> 27);
+  };
   for (int64_t row = blockIdx.x; row < M; row += gridDim.x) {
     const float* x = Y + row * ldy;
-    for (int b = warp; b < nBlks; b += 8) {
-      const float* xb = x + (int64_t)b * step;
+    // two real windows per complex FFT: z = x_a + i x_b
+    for (int p = warp; p < npairs; p += 8) {
+      const float* xa = x + (int64_t)(2 * p) * step;
+      const bool has_b = 2 * p + 1 < nBlks;
+      const float* xb = xa + step;
       float re[E], im[E];
 #pragma unroll
       for (int e = 0; e < E; ++e) {
         const int j = lane + 32 * e;
-        re[e] = __ldg(xb + j) * sw[j];
-        im[e] = 0.f;
+        re[e] = __ldg(xa + j) * sw[j];
+        im[e] = has_b ? __ldg(xb + j) * sw[j] : 0.f;
       }
       warp_fft<E>(re, im, lane, N, sc, ss);
-      // bins f < nf = 16 E + 1: the even lanes hold f < 16 E (k2 = bitrev5(lane)
-      // < 16), lane 1 holds f = 16 E in register 0.  Staged at
-      // r * 16 + lane / 2 (and 16 E): one contiguous 128-byte row per register
-      // across the warp, no bank conflicts (f-indexed stores would hit two
-      // banks from all 32 lanes)
-      const int k2 = (int)(__brev((unsigned)lane) >> 27);
-      float2* out = reinterpret_cast<float2*>(stage) + (size_t)b * nf;
+      float2* z = zs + (size_t)p * ZP;
 #pragma unroll
-      for (int r = 0; r < E; ++r) {
-        const int k1 = LOGE ? (int)(__brev((unsigned)r) >> (32 - LOGE)) : 0;
-        const int f = k1 + E * k2;
-        if ((lane & 1) == 0 || (lane == 1 && r == 0)) {
-          const float g = (f >= 1 && f <= nf - 2) ? 2.f * scale : scale;
-          out[(lane & 1) ? 16 * E : r * 16 + (lane >> 1)] = make_float2(re[r] * g, im[r] * g);
-        }
-      }
+      for (int r = 0; r < E; ++r) z[r * 32 + lane] = make_float2(re[r], im[r]);
     }
     __syncthreads();
-    // Q[f][row][b]: one contiguous run of nBlks values per frequency; the
-    // stage row stride nf is odd, so a warp reading consecutive blocks of one
-    // frequency spreads over all banks
+    // Q[f][row][b]: one contiguous run of nBlks values per frequency.
+    // X_a[f] = (Z[f] + conj Z[N-f]) / 2,  X_b[f] = (Z[f] - conj Z[N-f]) / (2i)
     c2<float>* Qc = reinterpret_cast<c2<float>*>(Q);
     for (int e = tid; e < nf * nBlks; e += blockDim.x) {
       const int f = e / nBlks, b = e - f * nBlks;
-      const int k1 = f % E, k2 = f / E;
-      const int r = LOGE ? (int)(__brev((unsigned)k1) >> (32 - LOGE)) : 0;
-      const int slot = (k2 == 16) ? 16 * E : r * 16 + (int)(__brev((unsigned)k2) >> 28);
-      Qc[((int64_t)f * M + row) * nBlks + b] = stage[(size_t)b * nf + slot];
+      const float2* z = zs + (size_t)(b >> 1) * ZP;
+      const float2 zk = z[slot(f)], zn = z[slot((N - f) & (N - 1))];
+      const float g = 0.5f * ((f >= 1 && f <= nf - 2) ? 2.f * scale : scale);
+      c2<float> v;
+      if ((b & 1) == 0) {
+        v.re = (zk.x + zn.x) * g;
+        v.im = (zk.y - zn.y) * g;
+      } else {
+        v.re = (zk.y + zn.y) * g;
+        v.im = (zn.x - zk.x) * g;
+      }
+      Qc[((int64_t)f * M + row) * nBlks + b] = v;
     }
     __syncthreads();
   }
@@ -250,7 +259,8 @@ template <int E>
 static int spod_fft32_launch(const float* Y, int64_t M, int64_t ldy, int step, int nBlks, int nf,
                              const float* window, const float* twr, const float* twi, double scale,
                              float* Q, cudaStream_t st) {
-  const size_t smem = sizeof(float) * 3 * 32 * E + sizeof(c2<float>) * (size_t)nBlks * nf;
+  const size_t smem =
+      sizeof(float) * 3 * 32 * E + sizeof(float2) * (size_t)((nBlks + 1) / 2) * (32 * E + 1);
   PLOM_CHECK_CUDA(cudaFuncSetAttribute(spod_fft32_kernel<E>,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   int per_sm = 0;
@@ -273,7 +283,8 @@ static int spod_fft_impl(const T* Y, int64_t M, int64_t N, int64_t ldy, int nDFT
     while ((1 << log2n) < nDFT) ++log2n;
   }
   if constexpr (sizeof(T) == 4) {
-    const size_t stage = sizeof(c2<float>) * (size_t)nBlks * nf + sizeof(float) * 3 * nDFT;
+    const size_t stage =
+        sizeof(float2) * (size_t)((nBlks + 1) / 2) * (nDFT + 1) + sizeof(float) * 3 * nDFT;
     // the register FFT stages the one-sided spectrum (nf = nDFT / 2 + 1)
     if (log2n >= 5 && log2n <= 10 && nf == nDFT / 2 + 1 && stage <= 200 * 1024) {
       ProfScope prof("spod_fft", st, 5.0 * (double)M * nBlks * nDFT * log2n,
