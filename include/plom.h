@@ -196,6 +196,16 @@ int plom_spod_fft(int dtype, const void* Y, int64_t M, int64_t N, int64_t ldy, i
    type), ustride complex elements apart; P: (M*nBlks) x nf, row-major. */
 int plom_spod_modes(int dtype, const void* U, int64_t G, int64_t M, int64_t nBlks,
                     int64_t ustride, void* P, int64_t nf, int64_t f0, void* stream);
+/* the final column order of P (SPOD/wrapper.py:86-95 sorts the frequencies
+   by their leading energy): P[row][c] = T_k[row][g] for f = order[c] =
+   k G + g, where the frequency groups' modes were written densely, group k
+   as a rows x G_k block T_k = T + k gstride (G_k = min(G, nf - k G);
+   plom_spod_modes with nf = G_k, f0 = 0).  rows = M nBlks; order is a device
+   array of nf ints.  Every P row is written whole and contiguous.  SPOD.run
+   puts T_k in the part of the Fourier coefficients its batch has consumed
+   (gstride = 2 G rows). */
+int plom_spod_assemble(int dtype, const void* T, int64_t rows, int64_t nf, int64_t G,
+                       int64_t gstride, const int* order, void* P, void* stream);
 
 /* ---- packed tall operands (mixed form) --------------------------------- */
 /* No counterpart in the reference.  A caller that multiplies the same FP32

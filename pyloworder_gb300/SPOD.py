@@ -85,23 +85,33 @@ def run_device(x, ld, t_host, nDFT=0, nolap=0, remove_mean=True, window="hamming
     Q = spod_fft_device(Y, ldy, nDFT, nolap, nBlks, nf, win, winWeight / nDFT / math.sqrt(nBlks))
     del Y  # the Fourier coefficients are all the SVDs need
     Lm = t.empty((nf, nBlks), dtype=x.dtype, device="cuda")
-    P = t.empty((Mrows * nBlks, nf), dtype=x.dtype, device="cuda")
+    rows = Mrows * nBlks
+    P = t.empty((rows, nf), dtype=x.dtype, device="cuda")
     # P[i + M*b, f] = Re U_f[i, b]
     # the per-frequency SVDs run as batches of frequencies (one launch per
     # stage for the whole batch), as many per batch as device memory allows
     group = _svd_batch(Q, nBlks, precision)
     # the mode-layout kernel stages group x nBlks real parts per point
     group = max(1, min(group, (48 * 1024) // (x.element_size() * (nBlks | 1))))
+    # a batch's modes are written densely (rows x G_k, G_k frequencies per
+    # row) into the Fourier coefficients the batch has just consumed; one
+    # gather then writes P whole rows at a time in the final column order
+    Qr = t.view_as_real(Q).reshape(-1)
     for f0 in range(0, nf, group):
         f1 = min(nf, f0 + group)
         U, S, _ = M.tsqr_svd_batched_device(Q[f0:f1], precision)
         L.call("plom_spod_modes", L.dtype_code(P), L.ptr(U), f1 - f0, Mrows, nBlks,
-               U.stride(0) if f1 - f0 > 1 else Mrows * nBlks, L.ptr(P), nf, f0, L.stream_ptr())
+               U.stride(0) if f1 - f0 > 1 else Mrows * nBlks, L.ptr(Qr[2 * f0 * rows:]), f1 - f0, 0,
+               L.stream_ptr())
         Lm[f0:f1] = (S * S).to(x.dtype)
         del U, S
     order = np.argsort(Lm[:, 0].cpu().numpy())[::-1].copy()
     od = t.as_tensor(order, device="cuda")
-    return Lm.index_select(0, od), P.index_select(1, od), f[order]
+    od32 = t.as_tensor(order.astype(np.int32), device="cuda")
+    L.call("plom_spod_assemble", L.dtype_code(P), L.ptr(Qr), rows, nf, group, 2 * group * rows,
+           L.ptr(od32), L.ptr(P), L.stream_ptr())
+    del Qr, Q
+    return Lm.index_select(0, od), P, f[order]
 
 
 def run(X, t, nDFT: int = 0, nolap: int = 0, remove_mean: bool = True, *, window="hamming",

@@ -54,6 +54,7 @@ PROTOS = {
     "plom_tsqr_svd": (c_int, [c_int, c_int, c_vp, c_i64, c_i64, c_i64, c_vp, c_i64, c_vp, c_vp, c_vp,
                               c_sz, c_vp, c_vp]),
     "plom_spod_modes": (c_int, [c_int, c_vp, c_i64, c_i64, c_i64, c_i64, c_vp, c_i64, c_i64, c_vp]),
+    "plom_spod_assemble": (c_int, [c_int, c_vp, c_i64, c_i64, c_i64, c_i64, c_vp, c_vp, c_vp]),
     "plom_packed_bytes": (c_sz, [c_i64, c_i64]),
     "plom_pack": (c_int, [c_vp, c_i64, c_i64, c_i64, c_vp, c_sz, c_vp]),
     "plom_packed_apply_workspace": (c_sz, [c_i64, c_i64, c_i64]),

@@ -366,9 +366,115 @@ static int spod_modes_impl(const T* U, int64_t G, int64_t M, int64_t nBlks, int6
   return PLOM_OK;
 }
 
+// P[row][c] = T_k[row][g] for frequency f = order[c] = k G + g: the groups'
+// modes, written group-major and dense (T_k: rows x G_k, G_k = min(G, nf - k
+// G), T_k at T + k gstride), gathered into P's final column order.  A block
+// stages RB whole rows: it reads each group's RB x G_k block (contiguous) and
+// writes RB x nf contiguous values.
+// Both phases move 16-byte vectors (the group blocks and the P rows of a
+// block of RB rows are contiguous and 16-byte aligned when RB G_k and RB nf
+// are multiples of 16 bytes / sizeof(T); the tail block falls back to
+// scalars), several per thread in flight.
+template <typename T>
+__global__ void __launch_bounds__(256) spod_assemble_kernel(const T* __restrict__ Tg, int64_t rows,
+                                                            int nf, int G, int64_t gstride,
+                                                            const int* __restrict__ order,
+                                                            T* __restrict__ P, int RB) {
+  constexpr int V = 16 / sizeof(T);  // elements per 16-byte vector
+  using Vec = uint4;
+  extern __shared__ __align__(16) unsigned char asm_sm[];
+  int* ord = reinterpret_cast<int*>(asm_sm);
+  T* tile = reinterpret_cast<T*>(asm_sm + sizeof(int) * (((size_t)nf + 3) & ~(size_t)3));
+  const int pitch = nf | 1;  // [RB][pitch], frequency order
+  for (int c = threadIdx.x; c < nf; c += blockDim.x) ord[c] = order[c];
+  const int ngroups = (nf + G - 1) / G;
+  for (int64_t r0 = (int64_t)blockIdx.x * RB; r0 < rows; r0 += (int64_t)gridDim.x * RB) {
+    const int nr = (int)min((int64_t)RB, rows - r0);
+    __syncthreads();
+    for (int k = 0; k < ngroups; ++k) {
+      const int Gk = min(G, nf - k * G);
+      const T* src = Tg + (int64_t)k * gstride + r0 * Gk;
+      const int cnt = nr * Gk;
+      const bool vec = (cnt % V) == 0 && (reinterpret_cast<uintptr_t>(src) & 15) == 0;
+      if (vec) {
+#pragma unroll 4
+        for (int e4 = threadIdx.x; e4 < cnt / V; e4 += blockDim.x) {
+          const Vec w = __ldg(reinterpret_cast<const Vec*>(src) + e4);
+          const T* wv = reinterpret_cast<const T*>(&w);
+#pragma unroll
+          for (int q = 0; q < V; ++q) {
+            const int e = e4 * V + q, r = e / Gk, g = e - r * Gk;
+            tile[r * pitch + k * G + g] = wv[q];
+          }
+        }
+      } else {
+        for (int e = threadIdx.x; e < cnt; e += blockDim.x) {
+          const int r = e / Gk, g = e - r * Gk;
+          tile[r * pitch + k * G + g] = src[e];
+        }
+      }
+    }
+    __syncthreads();
+    T* dst = P + r0 * nf;
+    const int cnt = nr * nf;
+    if ((cnt % V) == 0 && (reinterpret_cast<uintptr_t>(dst) & 15) == 0) {
+#pragma unroll 4
+      for (int e4 = threadIdx.x; e4 < cnt / V; e4 += blockDim.x) {
+        Vec w;
+        T* wv = reinterpret_cast<T*>(&w);
+#pragma unroll
+        for (int q = 0; q < V; ++q) {
+          const int e = e4 * V + q, r = e / nf, c = e - r * nf;
+          wv[q] = tile[r * pitch + ord[c]];
+        }
+        reinterpret_cast<Vec*>(dst)[e4] = w;
+      }
+    } else {
+      for (int e = threadIdx.x; e < cnt; e += blockDim.x) {
+        const int r = e / nf, c = e - r * nf;
+        dst[e] = tile[r * pitch + ord[c]];
+      }
+    }
+  }
+}
+
+template <typename T>
+static int spod_assemble_impl(const T* Tg, int64_t rows, int nf, int G, int64_t gstride,
+                              const int* order, T* P, cudaStream_t st) {
+  const int RB = 64;
+  const size_t smem = sizeof(int) * (((size_t)nf + 3) & ~(size_t)3) + sizeof(T) * RB * (nf | 1);
+  PLOM_REQUIRE(smem <= 200 * 1024, PLOM_ERR_UNSUPPORTED, "spod_assemble: %d frequencies too many",
+               nf);
+  if (smem > 48 * 1024)
+    PLOM_CHECK_CUDA(cudaFuncSetAttribute(spod_assemble_kernel<T>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  const int64_t grid = std::min<int64_t>((rows + RB - 1) / RB, (int64_t)num_sms() * 8);
+  ProfScope prof("spod_assemble", st, 0.0, 2.0 * sizeof(T) * rows * nf);
+  spod_assemble_kernel<T><<<(unsigned)grid, 256, smem, st>>>(Tg, rows, nf, G, gstride, order, P,
+                                                             RB);
+  PLOM_CHECK_LAUNCH();
+  return PLOM_OK;
+}
+
 }  // namespace plom
 
 using namespace plom;
+
+extern "C" int plom_spod_assemble(int dtype, const void* Tg, int64_t rows, int64_t nf, int64_t G,
+                                  int64_t gstride, const int* order, void* P, void* stream) {
+  PLOM_REQUIRE(Tg && order && P, PLOM_ERR_ARG, "spod_assemble: null pointer");
+  PLOM_REQUIRE(rows >= 1 && nf >= 1 && nf <= 8192 && G >= 1 && G <= nf && gstride >= G * rows,
+               PLOM_ERR_ARG, "spod_assemble: bad sizes");
+  cudaStream_t st = (cudaStream_t)stream;
+  if (dtype == PLOM_F32)
+    return spod_assemble_impl<float>((const float*)Tg, rows, (int)nf, (int)G, gstride, order,
+                                     (float*)P, st);
+  if (dtype == PLOM_F64)
+    return spod_assemble_impl<double>((const double*)Tg, rows, (int)nf, (int)G, gstride, order,
+                                      (double*)P, st);
+  set_error("spod_assemble: dtype must be F32 or F64");
+  return PLOM_ERR_UNSUPPORTED;
+}
 
 extern "C" int plom_spod_fft(int dtype, const void* Y, int64_t M, int64_t N, int64_t ldy,
                              int64_t nDFT, int64_t step, int64_t nBlks, int64_t nf,

@@ -210,6 +210,28 @@ def test_pca_golden(golden, divide_variance, ukey, skey):
     cols_up_to_phase(sc[:, :10], g[skey][:, :10], 1e-8)
 
 
+@pytest.mark.parametrize("dt", [torch.float32, torch.float64])
+@pytest.mark.parametrize("rows,nf,G", [(1000, 17, 5), (77, 129, 36), (130, 4, 4), (64, 1, 1)])
+def test_spod_assemble(dt, rows, nf, G):
+    """plom_spod_assemble gathers the dense per-group mode blocks into P's
+    final (energy-sorted) column order."""
+    from pyloworder_gb300 import _lib as L
+    rng = np.random.default_rng(rows + nf)
+    P_nat = rng.standard_normal((rows, nf))
+    gstride = 2 * G * rows  # the group blocks sit 2 G rows apart (SPOD.run's layout)
+    Tg = np.full(gstride * ((nf + G - 1) // G), np.nan)
+    for k, f0 in enumerate(range(0, nf, G)):
+        blk = P_nat[:, f0:min(nf, f0 + G)].ravel()
+        Tg[k * gstride:k * gstride + blk.size] = blk
+    order = rng.permutation(nf).astype(np.int32)
+    Td = torch.as_tensor(Tg, dtype=dt, device="cuda")
+    od = torch.as_tensor(order, device="cuda")
+    P = torch.empty((rows, nf), dtype=dt, device="cuda")
+    L.call("plom_spod_assemble", L.dtype_code(P), L.ptr(Td), rows, nf, G, gstride, L.ptr(od),
+           L.ptr(P), L.stream_ptr())
+    np.testing.assert_array_equal(P.cpu().numpy(), P_nat[:, order].astype(P.cpu().numpy().dtype))
+
+
 @pytest.mark.parametrize("dt", [torch.complex64, torch.complex128])
 @pytest.mark.parametrize("G,M,nBlks,nf,f0", [(5, 1000, 63, 9, 3), (1, 77, 8, 4, 0), (16, 300, 64, 16, 0)])
 def test_spod_mode_layout(dt, G, M, nBlks, nf, f0):
