@@ -105,6 +105,15 @@ __global__ void __launch_bounds__(256) chol_coop_kernel(const double* __restrict
           if (tid == 0) {
             double d = S[j][j];
             bool ok = (d > 0.0) && isfinite(d);
+            if (!ok && rel0 == 0.0 && isfinite(d)) {
+              // unshifted factorization (a CholeskyQR pass after the first):
+              // a non-positive pivot is a null direction of G, e.g. an exact
+              // zero column of the tall matrix.  Floor this pivot alone (its
+              // row's remaining entries are at the rounding level of G);
+              // a shift of the whole diagonal would bias every other column
+              d = relfail * stt.trace[b] / n;
+              ok = d > 0.0;
+            }
             sflag = ok ? 1 : 0;
             const double piv = ok ? sqrt(d) : 1.0;
             S[j][j] = piv;

@@ -105,6 +105,137 @@ int fill_uniform_dispatch(int dtype, void* out, int64_t count, uint64_t seed, cu
   return PLOM_OK;
 }
 
+// ---------------------------------------------------------------------------
+// Orthonormal completion of U's null columns (real, one problem).  An exact
+// zero column of the tall matrix leaves an exact zero column in every
+// CholeskyQR factor Q, so U = Q M gets a zero column for that singular value
+// (sigma ~ 0), where LAPACK returns a unit vector orthogonal to the other
+// columns.  Candidates are the columns with sigma <= 1e-6 sigma_1 (at most
+// NC_MAX, smallest first); those whose norm is below 1/2 are replaced one at
+// a time by u = e_i - U (U^T e_i), normalised, with a different row i for
+// each (U^T e_i is row i of U, with the columns still to be completed left
+// out).  Without such columns the cost is one strided pass over the candidate
+// columns.
+// ---------------------------------------------------------------------------
+constexpr int NC_MAX = 8;
+
+__global__ void nc_candidates_kernel(const double* __restrict__ S, int n, int* __restrict__ list,
+                                     int* __restrict__ count) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  int c = 0;
+  const double thr = 1e-6 * S[0];
+  for (int j = n - 1; j >= 0 && c < NC_MAX; --j) {
+    if (!(S[j] <= thr)) break;
+    list[c++] = j;
+  }
+  *count = c;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) nc_norms_kernel(const T* __restrict__ U, int64_t m,
+                                                       int64_t ldu, const int* __restrict__ list,
+                                                       const int* __restrict__ count,
+                                                       double* __restrict__ sums) {
+  const int q = blockIdx.y;
+  if (q >= *count) return;
+  const int c = list[q];
+  double s = 0.0;
+  for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < m;
+       r += (int64_t)gridDim.x * blockDim.x) {
+    const double v = (double)U[r * ldu + c];
+    s = fma(v, v, s);
+  }
+  s = warp_sum(s);
+  if ((threadIdx.x & 31) == 0) atomicAdd(&sums[q], s);
+}
+
+__device__ __forceinline__ int64_t nc_row(int q, int64_t m) {
+  return (int64_t)(((uint64_t)(q + 1) * 2654435761ull) % (uint64_t)m);
+}
+
+// u = e_i - U w, w = row i of U without the columns still to be completed
+// (this one included); written into column list[q], its squared norm summed
+template <typename T>
+__global__ void __launch_bounds__(256) nc_project_kernel(T* __restrict__ U, int64_t m, int n,
+                                                         int64_t ldu, const int* __restrict__ list,
+                                                         const int* __restrict__ count,
+                                                         const double* __restrict__ sums, int q,
+                                                         double* __restrict__ nrm2) {
+  if (q >= *count || !(sums[q] < 0.25)) return;
+  extern __shared__ double ncw[];
+  const int64_t i = nc_row(q, m);
+  const int c = list[q];
+  for (int j = threadIdx.x; j < n; j += blockDim.x) ncw[j] = (double)U[i * ldu + j];
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int p = q; p < *count; ++p)
+      if (sums[p] < 0.25) ncw[list[p]] = 0.0;
+  }
+  __syncthreads();
+  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+  double part = 0.0;
+  for (int64_t r = (int64_t)blockIdx.x * 8 + wib; r < m; r += (int64_t)gridDim.x * 8) {
+    const T* row = U + r * ldu;
+    double acc = 0.0;
+    for (int j = lane; j < n; j += 32) acc = fma((double)row[j], ncw[j], acc);
+    acc = warp_sum(acc);
+    const double u = (r == i ? 1.0 : 0.0) - acc;
+    if (lane == 0) {
+      U[r * ldu + c] = (T)u;
+      part = fma(u, u, part);
+    }
+  }
+  __syncwarp();
+  if (lane == 0) atomicAdd(&nrm2[q], part);
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) nc_scale_kernel(T* __restrict__ U, int64_t m, int64_t ldu,
+                                                       const int* __restrict__ list,
+                                                       const int* __restrict__ count,
+                                                       const double* __restrict__ sums, int q,
+                                                       const double* __restrict__ nrm2) {
+  if (q >= *count || !(sums[q] < 0.25) || !(nrm2[q] > 0.0)) return;
+  const int c = list[q];
+  const double f = 1.0 / sqrt(nrm2[q]);
+  for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < m;
+       r += (int64_t)gridDim.x * blockDim.x)
+    U[r * ldu + c] = (T)((double)U[r * ldu + c] * f);
+}
+
+template <typename T>
+int complete_null_columns(const double* S, int n, T* U, int64_t m, int64_t ldu, Arena& ws,
+                          cudaStream_t st) {
+  int* list = ws.take<int>(NC_MAX);
+  int* count = ws.take<int>(1);
+  double* sums = ws.take<double>(NC_MAX);
+  double* nrm2 = ws.take<double>(NC_MAX);
+  if (ws.measuring() || n < 1 || m < 1) return PLOM_OK;
+  PLOM_REQUIRE(!ws.overflow(), PLOM_ERR_WORKSPACE, "null-column completion: workspace too small");
+  PLOM_REQUIRE(S && U && n <= 8192, PLOM_ERR_ARG, "null-column completion: bad arguments");
+  ProfScope prof("null_cols", st, 0.0, (double)sizeof(T) * m, 2 + 2 * NC_MAX);
+  PLOM_CHECK_CUDA(cudaMemsetAsync(sums, 0, sizeof(double) * NC_MAX, st));
+  PLOM_CHECK_CUDA(cudaMemsetAsync(nrm2, 0, sizeof(double) * NC_MAX, st));
+  nc_candidates_kernel<<<1, 32, 0, st>>>(S, n, list, count);
+  PLOM_CHECK_LAUNCH();
+  const unsigned gx = (unsigned)std::max<int64_t>(1, std::min<int64_t>(cdiv(m, 256), (int64_t)num_sms() * 4));
+  nc_norms_kernel<T><<<dim3(gx, NC_MAX), 256, 0, st>>>(U, m, ldu, list, count, sums);
+  PLOM_CHECK_LAUNCH();
+  const unsigned gp = (unsigned)std::max<int64_t>(1, std::min<int64_t>(cdiv(m, 8), (int64_t)num_sms() * 8));
+  for (int q = 0; q < NC_MAX; ++q) {
+    nc_project_kernel<T><<<gp, 256, sizeof(double) * n, st>>>(U, m, n, ldu, list, count, sums, q,
+                                                              nrm2);
+    PLOM_CHECK_LAUNCH();
+    nc_scale_kernel<T><<<gx, 256, 0, st>>>(U, m, ldu, list, count, sums, q, nrm2);
+    PLOM_CHECK_LAUNCH();
+  }
+  return PLOM_OK;
+}
+template int complete_null_columns<float>(const double*, int, float*, int64_t, int64_t, Arena&,
+                                          cudaStream_t);
+template int complete_null_columns<double>(const double*, int, double*, int64_t, int64_t, Arena&,
+                                           cudaStream_t);
+
 }  // namespace plom
 
 extern "C" int plom_fill_uniform(int dtype, void* out, int64_t count, uint64_t seed,

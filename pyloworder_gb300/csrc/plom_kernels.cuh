@@ -53,7 +53,9 @@ int gemm_tn_df(const float* A, int64_t lda, const float* B, int64_t ldb, double*
 // ---- dense.cu (FP64 small dense, batched, cooperative) ----
 // Upper Cholesky R^T R = G + s I of `batch` n x n matrices (stride n*n, ld n).
 // s starts at shift_rel0 * trace(G)/n; on a non-positive pivot the whole
-// factorization restarts with s = max(s*100, shift_rel_fail*trace/n).
+// factorization restarts with s = max(s*100, shift_rel_fail*trace/n).  With
+// shift_rel0 = 0 a non-positive pivot is instead floored alone at
+// shift_rel_fail*trace/n (a null direction of a positive semidefinite G).
 // info[ST_FAIL] = PLOM_NUM_CHOLESKY when all attempts fail.
 int chol_shifted(const double* G, double* R, int n, int batch, double shift_rel0,
                  double shift_rel_fail, int* info, Arena& ws, cudaStream_t st);
@@ -90,5 +92,12 @@ int copy2d(const TI* in, int64_t ldi, TO* out, int64_t ldo, int64_t rows, int64_
 int fill_uniform_dispatch(int dtype, void* out, int64_t count, uint64_t seed, cudaStream_t st);
 int transpose_f64(const double* in, double* out, int64_t rows, int64_t cols, int batch,
                   cudaStream_t st);
+// Orthonormal completion of the columns of U (m x n real, ld ldu) whose
+// singular value is <= 1e-6 sigma_1 and whose norm is below 1/2 (the zero
+// columns an exact zero column of the input leaves); S: n FP64 values,
+// descending.
+template <typename T>
+int complete_null_columns(const double* S, int n, T* U, int64_t m, int64_t ldu, Arena& ws,
+                          cudaStream_t st);
 
 }  // namespace plom

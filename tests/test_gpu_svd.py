@@ -126,6 +126,50 @@ def test_mixed_mean_removed_u_orthonormal():
     assert float((Vd @ Vd.T - torch.eye(n, dtype=torch.float64, device="cuda")).abs().max()) < 1e-6
 
 
+@pytest.mark.parametrize("precision", ["mixed", "fp64"])
+@pytest.mark.parametrize("case", ["zero_col", "zero_cols3", "dup_cols", "rank3", "tiny_m", "n1",
+                                  "wide_ragged"])
+def test_degenerate_inputs(case, precision):
+    """Inputs with exact null directions (zero columns, 20 duplicated columns,
+    rank 3 of 64), few rows, one column, ragged sizes: finite outputs, sigma
+    normwise, X = U S V, and every column of U orthonormal (LAPACK's U is,
+    null directions included: an exact zero column's U column is completed
+    to a unit vector orthogonal to the others)."""
+    rng = np.random.default_rng(5)
+    if case == "zero_col":
+        X = rng.standard_normal((20000, 40))
+        X[:, 7] = 0.0
+    elif case == "zero_cols3":
+        X = rng.standard_normal((20000, 40))
+        X[:, [3, 17, 39]] = 0.0
+    elif case == "dup_cols":
+        X = rng.standard_normal((20000, 40))
+        X[:, 20:] = X[:, :20]
+    elif case == "rank3":
+        X = rng.standard_normal((30000, 3)) @ rng.standard_normal((3, 64))
+    elif case == "tiny_m":
+        X = rng.standard_normal((70, 50))
+    elif case == "n1":
+        X = rng.standard_normal((5000, 1))
+    else:
+        X = rng.standard_normal((4097 * 3 + 5, 131))
+    mixed = precision == "mixed"
+    X = X.astype(np.float32 if mixed else np.float64)
+    U, S, V = P.math.tsqr_svd(X, precision=precision)
+    k = min(X.shape)
+    assert U.shape == (X.shape[0], k) and S.shape == (k,) and V.shape == (k, X.shape[1])
+    assert np.all(np.isfinite(U)) and np.all(np.isfinite(S)) and np.all(np.isfinite(V))
+    Sr = np.linalg.svd(X.astype(np.float64), compute_uv=False)
+    assert np.abs(S - Sr[:k]).max() <= (1e-5 if mixed else 1e-12) * Sr[0]
+    A = (U.astype(np.float64) * S) @ V
+    assert np.abs(A - X).max() <= (1e-4 if mixed else 1e-11) * np.abs(X).max()
+    Ud = U.astype(np.float64)
+    # FP64: 1e-11 (rank 3 of 64 leaves 61 renormalised null columns at ~1e-12)
+    assert np.abs(Ud.T @ Ud - np.eye(k)).max() < (1e-4 if mixed else 1e-11)
+    Vd = V.astype(np.float64)
+    assert np.abs(Vd @ Vd.T - np.eye(k)).max() < (1e-5 if mixed else 1e-12)
+
+
 @pytest.mark.parametrize("dtype,precision", [(np.float32, "mixed"), (np.float64, "fp64"),
                                              (np.complex64, "mixed")])
 def test_tsqr_svd_host_entry(dtype, precision):
