@@ -766,12 +766,89 @@ __device__ __forceinline__ int jac_pair_df(float2* x, float2* y, float2* xv, flo
   return 1;
 }
 
+// jac_pair on double-float rows (complex: element i is slots 2i (re) and
+// 2i + 1 (im)).  Dots x^H y and the rotation x' = x - w y, y' = y + v x with
+// w = t dq/dp e^{-i phi}, v = t dp/dq e^{i phi} on the FP32 pipe; the pair's
+// scalars in FP64 as in jac_pair.
+__device__ __forceinline__ int jac_pair_df_c(float2* x, float2* y, float2* xv, float2* yv,
+                                             int64_t n, double* na_, double* nb_, double* da_,
+                                             double* db_, double* ea_, double* eb_, double tol2,
+                                             int lane) {
+  double al = *na_, be = *nb_;
+  const double da = *da_, db = *db_, ea = *ea_, eb = *eb_;
+  const bool need = (al < 0.0) || (be < 0.0);
+  float2 g = make_float2(0.f, 0.f), h = g, a2 = g, b2 = g;
+  for (int64_t i = lane; i < n; i += 32) {
+    const float2 xr = x[2 * i], xi = x[2 * i + 1], yr = y[2 * i], yi = y[2 * i + 1];
+    df_dot_acc(g, xr, yr);  // conj(x) y
+    df_dot_acc(g, xi, yi);
+    df_dot_acc(h, xr, yi);
+    df_dot_acc(h, make_float2(-xi.x, -xi.y), yr);
+    if (need) {
+      df_dot_acc(a2, xr, xr);
+      df_dot_acc(a2, xi, xi);
+      df_dot_acc(b2, yr, yr);
+      df_dot_acc(b2, yi, yi);
+    }
+  }
+  double gr = df_warp_sum(g), gi = df_warp_sum(h);
+  if (need) {
+    const double sa = df_warp_sum(a2), sb = df_warp_sum(b2);
+    if (al < 0.0) al = da * da * sa;
+    if (be < 0.0) be = db * db * sb;
+  }
+  const double dd = da * db;
+  gr *= dd;
+  gi *= dd;
+  const double gabs = sqrt(fma(gr, gr, gi * gi));
+  double t, c, sq;
+  if (!jac_angle(al, be, gabs, tol2, t, c, sq)) {
+    if (lane == 0 && need) {
+      *na_ = al;
+      *nb_ = be;
+    }
+    return 0;
+  }
+  const double tp = t * (db * ea), tq = t * (da * eb);
+  const double ig = 1.0 / gabs;
+  const double er = gr * ig, ei = gi * ig;
+  // w = tp (er - i ei), v = tq (er + i ei)
+  const float2 wr = df_split(tp * er), wi = df_split(-tp * ei), nwi = df_split(tp * ei);
+  const float2 nvr = df_split(-tq * er), vi = df_split(tq * ei), nvi = df_split(-tq * ei);
+  auto rot = [&](float2* p, float2* q) {
+    for (int64_t i = lane; i < n; i += 32) {
+      const float2 pr = p[2 * i], pi = p[2 * i + 1], qr = q[2 * i], qi = q[2 * i + 1];
+      p[2 * i] = df_fms(df_fms(pr, wr, qr), nwi, qi);       // pr - wr qr + wi qi
+      p[2 * i + 1] = df_fms(df_fms(pi, wr, qi), wi, qr);    // pi - wr qi - wi qr
+      q[2 * i] = df_fms(df_fms(qr, nvr, pr), vi, pi);       // qr + vr pr - vi pi
+      q[2 * i + 1] = df_fms(df_fms(qi, nvr, pi), nvi, pr);  // qi + vr pi + vi pr
+    }
+  };
+  rot(x, y);
+  rot(xv, yv);
+  __syncwarp();
+  if (lane == 0) {
+    const double na = fma(-t, gabs, al), nb = fma(t, gabs, be);
+    *na_ = (na > 0.125 * al) ? na : -1.0;
+    *nb_ = (nb > 0.125 * be) ? nb : -1.0;
+    *da_ = da * c;
+    *db_ = db * c;
+    *ea_ = ea * sq;
+    *eb_ = eb * sq;
+  }
+  return 1;
+}
+
 template <int CW, bool DF>
 __device__ __forceinline__ int jac_pair_any(double* x, double* y, double* xv, double* yv,
                                             int64_t n, double* na_, double* nb_, double* da_,
                                             double* db_, double* ea_, double* eb_, double tol2,
                                             int lane) {
-  if constexpr (DF)
+  if constexpr (DF && CW == 2)
+    return jac_pair_df_c(reinterpret_cast<float2*>(x), reinterpret_cast<float2*>(y),
+                         reinterpret_cast<float2*>(xv), reinterpret_cast<float2*>(yv), n, na_,
+                         nb_, da_, db_, ea_, eb_, tol2, lane);
+  else if constexpr (DF)
     return jac_pair_df(reinterpret_cast<float2*>(x), reinterpret_cast<float2*>(y),
                        reinterpret_cast<float2*>(xv), reinterpret_cast<float2*>(yv), n, na_, nb_,
                        da_, db_, ea_, eb_, tol2, lane);
@@ -943,7 +1020,6 @@ __global__ void __launch_bounds__(128) jacobi_block_kernel(const double* __restr
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     abort_sh = 0;
   }
-  static_assert(!DF || CW == 1, "double-float rows are real");
   jac_init<CW, DF>(A, n, batch, js, grid);  // ends with a grid barrier
 
   const int nb = (n + 3) / 4;
@@ -1528,8 +1604,10 @@ static int jacobi_launch_cw(const double* A, int n, int batch, JacState& js, dou
                   (void*)&S,    (void*)&U, (void*)&VH,    (void*)&info};
   const size_t smem = (size_t)16 * js.pitch * sizeof(double);
   const bool use_df = df && CW == 1 && smem <= JAC_BLOCK_SMEM_MAX;
-  ProfScope prof(use_df ? "jacobi_svd_df" : "jacobi_svd_fp64", st, 0.0,
-                 8.0 * 3.0 * n * n * batch * CW);
+  const bool block_df = df && CW == 2;  // complex: the generic block kernel on double-float rows
+  ProfScope prof(use_df || (block_df && smem <= JAC_BLOCK_SMEM_MAX) ? "jacobi_svd_df"
+                                                                    : "jacobi_svd_fp64",
+                 st, 0.0, 8.0 * 3.0 * n * n * batch * CW);
   if (use_df) {
     const void* k = (const void*)jacobi_block_df16_kernel;
     PLOM_CHECK_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
@@ -1544,7 +1622,8 @@ static int jacobi_launch_cw(const double* A, int n, int batch, JacState& js, dou
     return PLOM_OK;
   }
   if (smem <= JAC_BLOCK_SMEM_MAX) {
-    const void* k = (const void*)jacobi_block_kernel<CW, false>;
+    const void* k = block_df ? (const void*)jacobi_block_kernel<CW, true>
+                             : (const void*)jacobi_block_kernel<CW, false>;
     PLOM_CHECK_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     const int nb = (n + 3) / 4;
     const int nbp = std::max(2, nb + (nb & 1));
@@ -1567,7 +1646,7 @@ static int jacobi_launch(const double* A, int n, int batch, int cplx, JacState& 
                          double* S, double* U, double* VH, int* info, cudaStream_t st) {
   const double tol2 = tol * tol;
   const bool df = tol >= JAC_DF_TOL;
-  return cplx ? jacobi_launch_cw<2>(A, n, batch, js, tol2, false, S, U, VH, info, st)
+  return cplx ? jacobi_launch_cw<2>(A, n, batch, js, tol2, df, S, U, VH, info, st)
               : jacobi_launch_cw<1>(A, n, batch, js, tol2, df, S, U, VH, info, st);
 }
 
