@@ -184,10 +184,13 @@ int plom_dmd_reduced(const double* aux1, const double* S, const double* VT, int6
    b (start b*step) and point i, the windowed FFT of Y[i, b*step : b*step+nDFT]
    is scaled by `scale` (pyLOM: winWeight/nDFT, here also /sqrt(nBlks)), bins
    1..nf-2 doubled, and bins 0..nf-1 written to Q[f][i][b] (complex,
-   interleaved; Q_f is row-major M x nBlks).  twr/twi: cos/-sin(2 pi j/nDFT). */
-int plom_spod_fft(int dtype, const void* Y, int64_t M, int64_t N, int64_t ldy, int64_t nDFT,
-                  int64_t step, int64_t nBlks, int64_t nf, const void* window, const void* twr,
-                  const void* twi, double scale, void* Q, void* stream);
+   interleaved; Q_f is row-major M x nBlks).  twr/twi: cos/-sin(2 pi j/nDFT).
+   mean (M values, or NULL): subtracted from each point's samples as they are
+   loaded (SPOD.run's temporal-mean removal, wrapper.py:58-61, without a
+   centred copy of Y). */
+int plom_spod_fft(int dtype, const void* Y, int64_t M, int64_t N, int64_t ldy, const void* mean,
+                  int64_t nDFT, int64_t step, int64_t nBlks, int64_t nf, const void* window,
+                  const void* twr, const void* twi, double scale, void* Q, void* stream);
 
 /* replaces the mode layout of SPOD.run (pyLOM/SPOD/wrapper.py:84,
    P[:, ifreq] = real(U).reshape(M*nBlks, order='F')) for the G frequencies

@@ -31,8 +31,10 @@ def _window(name, n):
     raise ValueError("window must be 'hamming' or 'hann'")
 
 
-def spod_fft_device(Y, ldy, nDFT, nolap, nBlks, nf, win, scale):
-    """Q[f] (M x nBlks complex) for every frequency bin, as one device array."""
+def spod_fft_device(Y, ldy, nDFT, nolap, nBlks, nf, win, scale, mean=None):
+    """Q[f] (M x nBlks complex) for every frequency bin, as one device array;
+    `mean` (M values on the device) is subtracted from each point's samples
+    as they are loaded."""
     t = L.torch()
     Mrows, N = Y.shape
     rdt = Y.dtype
@@ -42,8 +44,9 @@ def spod_fft_device(Y, ldy, nDFT, nolap, nBlks, nf, win, scale):
     wd = t.tensor(win, dtype=rdt, device="cuda")
     twr = t.tensor(np.cos(2 * np.pi * j / nDFT), dtype=rdt, device="cuda")
     twi = t.tensor(-np.sin(2 * np.pi * j / nDFT), dtype=rdt, device="cuda")
-    L.call("plom_spod_fft", L.dtype_code(Y), L.ptr(Y), Mrows, N, ldy, nDFT, nDFT - nolap, nBlks, nf,
-           L.ptr(wd), L.ptr(twr), L.ptr(twi), float(scale), L.ptr(Q), L.stream_ptr())
+    L.call("plom_spod_fft", L.dtype_code(Y), L.ptr(Y), Mrows, N, ldy, L.ptr(mean), nDFT,
+           nDFT - nolap, nBlks, nf, L.ptr(wd), L.ptr(twr), L.ptr(twi), float(scale), L.ptr(Q),
+           L.stream_ptr())
     return Q
 
 
@@ -75,15 +78,14 @@ def run_device(x, ld, t_host, nDFT=0, nolap=0, remove_mean=True, window="hamming
     if nBlks < 1:
         raise ValueError("SPOD: not enough snapshots for one block")
     winWeight = 1 / np.mean(win)
-    if remove_mean:
-        Y, _, _ = M.remove_mean_device(x, ld)
-        ldy = Y.shape[1]
-    else:
-        Y, ldy = x, ld
+    # the temporal mean is removed as the FFT stage loads the samples (no
+    # centred copy of the snapshots)
+    mean = M.temporal_mean_device(x, ld) if remove_mean else None
     f = np.arange(np.ceil(nDFT / 2) + 1) / dt / nDFT
     nf = f.shape[0]
-    Q = spod_fft_device(Y, ldy, nDFT, nolap, nBlks, nf, win, winWeight / nDFT / math.sqrt(nBlks))
-    del Y  # the Fourier coefficients are all the SVDs need
+    Q = spod_fft_device(x, ld, nDFT, nolap, nBlks, nf, win, winWeight / nDFT / math.sqrt(nBlks),
+                        mean=mean)
+    del mean
     Lm = t.empty((nf, nBlks), dtype=x.dtype, device="cuda")
     rows = Mrows * nBlks
     P = t.empty((rows, nf), dtype=x.dtype, device="cuda")

@@ -73,8 +73,8 @@ PROTOS = {
                                     ctypes.c_uint64, c_vp, c_i64, c_vp, c_vp, c_vp, c_sz, c_vp,
                                     c_vp]),
     "plom_fill_uniform": (c_int, [c_int, c_vp, c_i64, ctypes.c_uint64, c_vp]),
-    "plom_spod_fft": (c_int, [c_int, c_vp, c_i64, c_i64, c_i64, c_i64, c_i64, c_i64, c_i64, c_vp, c_vp,
-                              c_vp, ctypes.c_double, c_vp, c_vp]),
+    "plom_spod_fft": (c_int, [c_int, c_vp, c_i64, c_i64, c_i64, c_vp, c_i64, c_i64, c_i64, c_i64,
+                              c_vp, c_vp, c_vp, ctypes.c_double, c_vp, c_vp]),
     "plom_matmulp_static": (c_int, [c_int, c_vp, c_i64, c_vp, c_i64, c_vp, c_i64, c_i64, c_i64, c_i64,
                                     c_vp]),
     "plom_dmd_project_workspace": (c_sz, [c_i64, c_i64, c_i64]),

@@ -30,9 +30,9 @@ struct c2 {
 
 template <typename T>
 __global__ void __launch_bounds__(256) spod_fft_kernel(
-    const T* __restrict__ Y, int64_t M, int64_t N, int64_t ldy, int nDFT, int log2n, int step,
-    int nBlks, int nf, const T* __restrict__ window, const T* __restrict__ twr,
-    const T* __restrict__ twi, T scale, int R, T* __restrict__ Q) {
+    const T* __restrict__ Y, int64_t M, int64_t N, int64_t ldy, const T* __restrict__ mean,
+    int nDFT, int log2n, int step, int nBlks, int nf, const T* __restrict__ window,
+    const T* __restrict__ twr, const T* __restrict__ twi, T scale, int R, T* __restrict__ Q) {
   extern __shared__ unsigned char smem_raw[];
   T* sw = reinterpret_cast<T*>(smem_raw);                    // window  [nDFT]
   T* sc = sw + nDFT;                                          // cos     [nDFT]
@@ -53,12 +53,13 @@ __global__ void __launch_bounds__(256) spod_fft_kernel(
   for (int wdx = warp; wdx < nwin; wdx += 8) {
     const int r = wdx / nBlks, b = wdx % nBlks;
     const T* x = Y + (i0 + r) * ldy + (int64_t)b * step;
+    const T mu = mean ? mean[i0 + r] : T(0);  // temporal mean removed on load
     c2<T>* out = stage + ((size_t)r * nBlks + b) * nf;
     if (log2n >= 0) {
       // windowed samples into bit-reversed positions
       for (int j = lane; j < nDFT; j += 32) {
         const unsigned rj = __brev((unsigned)j) >> (32 - log2n);
-        wb[rj].re = x[j] * sw[j];
+        wb[rj].re = (x[j] - mu) * sw[j];
         wb[rj].im = T(0);
       }
       __syncwarp();
@@ -87,7 +88,7 @@ __global__ void __launch_bounds__(256) spod_fft_kernel(
     } else {
       // direct DFT (nDFT not a power of two)
       for (int j = lane; j < nDFT; j += 32) {
-        wb[j].re = x[j] * sw[j];
+        wb[j].re = (x[j] - mu) * sw[j];
         wb[j].im = T(0);
       }
       __syncwarp();
@@ -187,8 +188,8 @@ __device__ __forceinline__ void warp_fft(float (&re)[E], float (&im)[E], int lan
 
 template <int E>
 __global__ void __launch_bounds__(256) spod_fft32_kernel(
-    const float* __restrict__ Y, int64_t M, int64_t ldy, int step, int nBlks, int nf,
-    const float* __restrict__ window, const float* __restrict__ twr,
+    const float* __restrict__ Y, int64_t M, int64_t ldy, const float* __restrict__ mean, int step,
+    int nBlks, int nf, const float* __restrict__ window, const float* __restrict__ twr,
     const float* __restrict__ twi, float scale, float* __restrict__ Q) {
   constexpr int N = 32 * E;
   extern __shared__ unsigned char smem_raw[];
@@ -215,6 +216,7 @@ __global__ void __launch_bounds__(256) spod_fft32_kernel(
   };
   for (int64_t row = blockIdx.x; row < M; row += gridDim.x) {
     const float* x = Y + row * ldy;
+    const float mu = mean ? mean[row] : 0.f;  // temporal mean removed on load
     // two real windows per complex FFT: z = x_a + i x_b
     for (int p = warp; p < npairs; p += 8) {
       const float* xa = x + (int64_t)(2 * p) * step;
@@ -224,8 +226,8 @@ __global__ void __launch_bounds__(256) spod_fft32_kernel(
 #pragma unroll
       for (int e = 0; e < E; ++e) {
         const int j = lane + 32 * e;
-        re[e] = __ldg(xa + j) * sw[j];
-        im[e] = has_b ? __ldg(xb + j) * sw[j] : 0.f;
+        re[e] = (__ldg(xa + j) - mu) * sw[j];
+        im[e] = has_b ? (__ldg(xb + j) - mu) * sw[j] : 0.f;
       }
       warp_fft<E>(re, im, lane, N, sc, ss);
       float2* z = zs + (size_t)p * ZP;
@@ -256,7 +258,8 @@ __global__ void __launch_bounds__(256) spod_fft32_kernel(
 }
 
 template <int E>
-static int spod_fft32_launch(const float* Y, int64_t M, int64_t ldy, int step, int nBlks, int nf,
+static int spod_fft32_launch(const float* Y, int64_t M, int64_t ldy, const float* mean, int step,
+                             int nBlks, int nf,
                              const float* window, const float* twr, const float* twi, double scale,
                              float* Q, cudaStream_t st) {
   const size_t smem =
@@ -267,14 +270,16 @@ static int spod_fft32_launch(const float* Y, int64_t M, int64_t ldy, int step, i
   PLOM_CHECK_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, spod_fft32_kernel<E>,
                                                                 256, smem));
   const int64_t grid = std::min<int64_t>(M, (int64_t)std::max(1, per_sm) * num_sms() * 8);
-  spod_fft32_kernel<E><<<(unsigned)grid, 256, smem, st>>>(Y, M, ldy, step, nBlks, nf, window, twr,
+  spod_fft32_kernel<E><<<(unsigned)grid, 256, smem, st>>>(Y, M, ldy, mean, step, nBlks, nf, window,
+                                                          twr,
                                                           twi, (float)scale, Q);
   PLOM_CHECK_LAUNCH();
   return PLOM_OK;
 }
 
 template <typename T>
-static int spod_fft_impl(const T* Y, int64_t M, int64_t N, int64_t ldy, int nDFT, int step,
+static int spod_fft_impl(const T* Y, int64_t M, int64_t N, int64_t ldy, const T* mean, int nDFT,
+                         int step,
                          int nBlks, int nf, const T* window, const T* twr, const T* twi,
                          double scale, T* Q, cudaStream_t st) {
   int log2n = -1;
@@ -290,12 +295,12 @@ static int spod_fft_impl(const T* Y, int64_t M, int64_t N, int64_t ldy, int nDFT
       ProfScope prof("spod_fft", st, 5.0 * (double)M * nBlks * nDFT * log2n,
                      (double)sizeof(T) * ((double)M * N + 2.0 * M * nBlks * nf));
       switch (log2n) {
-        case 5: return spod_fft32_launch<1>(Y, M, ldy, step, nBlks, nf, window, twr, twi, scale, Q, st);
-        case 6: return spod_fft32_launch<2>(Y, M, ldy, step, nBlks, nf, window, twr, twi, scale, Q, st);
-        case 7: return spod_fft32_launch<4>(Y, M, ldy, step, nBlks, nf, window, twr, twi, scale, Q, st);
-        case 8: return spod_fft32_launch<8>(Y, M, ldy, step, nBlks, nf, window, twr, twi, scale, Q, st);
-        case 9: return spod_fft32_launch<16>(Y, M, ldy, step, nBlks, nf, window, twr, twi, scale, Q, st);
-        default: return spod_fft32_launch<32>(Y, M, ldy, step, nBlks, nf, window, twr, twi, scale, Q, st);
+        case 5: return spod_fft32_launch<1>(Y, M, ldy, mean, step, nBlks, nf, window, twr, twi, scale, Q, st);
+        case 6: return spod_fft32_launch<2>(Y, M, ldy, mean, step, nBlks, nf, window, twr, twi, scale, Q, st);
+        case 7: return spod_fft32_launch<4>(Y, M, ldy, mean, step, nBlks, nf, window, twr, twi, scale, Q, st);
+        case 8: return spod_fft32_launch<8>(Y, M, ldy, mean, step, nBlks, nf, window, twr, twi, scale, Q, st);
+        case 9: return spod_fft32_launch<16>(Y, M, ldy, mean, step, nBlks, nf, window, twr, twi, scale, Q, st);
+        default: return spod_fft32_launch<32>(Y, M, ldy, mean, step, nBlks, nf, window, twr, twi, scale, Q, st);
       }
     }
   }
@@ -313,7 +318,7 @@ static int spod_fft_impl(const T* Y, int64_t M, int64_t N, int64_t ldy, int nDFT
   PLOM_REQUIRE(grid < (1ll << 31), PLOM_ERR_ARG, "spod_fft: too many rows");
   ProfScope prof("spod_fft", st, 5.0 * (double)M * nBlks * nDFT * (log2n > 0 ? log2n : nDFT),
                  (double)sizeof(T) * ((double)M * N + 2.0 * M * nBlks * nf));
-  spod_fft_kernel<T><<<(unsigned)grid, 256, smem, st>>>(Y, M, N, ldy, nDFT, log2n, step, nBlks,
+  spod_fft_kernel<T><<<(unsigned)grid, 256, smem, st>>>(Y, M, N, ldy, mean, nDFT, log2n, step, nBlks,
                                                         nf, window, twr, twi, (T)scale, R, Q);
   PLOM_CHECK_LAUNCH();
   return PLOM_OK;
@@ -477,7 +482,7 @@ extern "C" int plom_spod_assemble(int dtype, const void* Tg, int64_t rows, int64
 }
 
 extern "C" int plom_spod_fft(int dtype, const void* Y, int64_t M, int64_t N, int64_t ldy,
-                             int64_t nDFT, int64_t step, int64_t nBlks, int64_t nf,
+                             const void* mean, int64_t nDFT, int64_t step, int64_t nBlks, int64_t nf,
                              const void* window, const void* twr, const void* twi, double scale,
                              void* Q, void* stream) {
   PLOM_REQUIRE(Y && window && twr && twi && Q, PLOM_ERR_ARG, "spod_fft: null pointer");
@@ -488,11 +493,13 @@ extern "C" int plom_spod_fft(int dtype, const void* Y, int64_t M, int64_t N, int
                "spod_fft: blocks run past the last snapshot");
   cudaStream_t st = (cudaStream_t)stream;
   if (dtype == PLOM_F32)
-    return spod_fft_impl<float>((const float*)Y, M, N, ldy, (int)nDFT, (int)step, (int)nBlks,
+    return spod_fft_impl<float>((const float*)Y, M, N, ldy, (const float*)mean, (int)nDFT,
+                                (int)step, (int)nBlks,
                                 (int)nf, (const float*)window, (const float*)twr,
                                 (const float*)twi, scale, (float*)Q, st);
   if (dtype == PLOM_F64)
-    return spod_fft_impl<double>((const double*)Y, M, N, ldy, (int)nDFT, (int)step, (int)nBlks,
+    return spod_fft_impl<double>((const double*)Y, M, N, ldy, (const double*)mean, (int)nDFT,
+                                 (int)step, (int)nBlks,
                                  (int)nf, (const double*)window, (const double*)twr,
                                  (const double*)twi, scale, (double*)Q, st);
   set_error("spod_fft: dtype must be F32 or F64");

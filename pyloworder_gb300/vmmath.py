@@ -88,6 +88,15 @@ def norm_variance(X, X_mean, X_var):
     return cv.back(Y)
 
 
+def temporal_mean_device(x, ld):
+    """Mean over snapshots of each point of a CUDA tensor (rows ld apart)."""
+    t = L.torch()
+    m, n = x.shape
+    out = t.empty(m, dtype=x.dtype, device="cuda")
+    L.call("plom_temporal_mean", L.dtype_code(x), L.ptr(x), m, n, ld, L.ptr(out), L.stream_ptr())
+    return out
+
+
 def remove_mean_device(x, ld, divide_variance=False):
     """Fused mean (+variance) and subtraction on a CUDA tensor: returns
     (Y, mean, var-or-None), all on the device."""

@@ -251,39 +251,51 @@ def test_spod_mode_layout(dt, G, M, nBlks, nf, f0):
 
 
 @pytest.mark.parametrize("nDFT,nolap", [(64, 32), (50, 10), (10, 2), (256, 128)])
-def test_spod_fft_stage(nDFT, nolap):
+@pytest.mark.parametrize("with_mean", [False, True])
+def test_spod_fft_stage(nDFT, nolap, with_mean):
+    """FP64 FFT stage (radix-2 in shared memory or direct DFT) against numpy;
+    with_mean: the per-point mean is subtracted as the samples are loaded."""
     rng = np.random.default_rng(nDFT)
     M, N = 37, 700
-    Y = rng.standard_normal((M, N))
+    Y = rng.standard_normal((M, N)) + 3.0
     nBlks = (N - nolap) // (nDFT - nolap)
     nf = int(np.ceil(nDFT / 2) + 1)
     win = 0.54 - 0.46 * np.cos(2 * np.pi * np.arange(nDFT) / (nDFT - 1))
     scale = (1 / win.mean()) / nDFT / np.sqrt(nBlks)
     Yd = torch.tensor(Y, device="cuda")
-    Q = P.SPOD.spod_fft_device(Yd, N, nDFT, nolap, nBlks, nf, win, scale).cpu().numpy()
+    mu = Y.mean(axis=1) if with_mean else np.zeros(M)
+    md = torch.tensor(mu, device="cuda") if with_mean else None
+    Q = P.SPOD.spod_fft_device(Yd, N, nDFT, nolap, nBlks, nf, win, scale, mean=md).cpu().numpy()
     for b in range(nBlks):
         i0 = b * (nDFT - nolap)
-        F = np.fft.fft(Y[:, i0:i0 + nDFT] * win, axis=1)[:, :nf] * scale
+        F = np.fft.fft((Y[:, i0:i0 + nDFT] - mu[:, None]) * win, axis=1)[:, :nf] * scale
         F[:, 1:nf - 1] *= 2
         np.testing.assert_allclose(Q[:, :, b].T, F, rtol=1e-11, atol=1e-12 * np.abs(F).max())
 
 
 @pytest.mark.parametrize("nDFT,nolap", [(32, 16), (64, 32), (256, 128), (1024, 512), (128, 0)])
-def test_spod_fft_stage_f32_register_fft(nDFT, nolap):
-    """FP32 power-of-two windows take the warp-register FFT; compare with numpy."""
+@pytest.mark.parametrize("with_mean", [False, True])
+def test_spod_fft_stage_f32_register_fft(nDFT, nolap, with_mean):
+    """FP32 power-of-two windows take the warp-register FFT (two windows per
+    complex transform); compare with numpy, optionally with the per-point
+    mean subtracted on load."""
     rng = np.random.default_rng(nDFT + 7)
     M, N = 29, 3000
-    Y = rng.standard_normal((M, N)).astype(np.float32)
+    Y = (rng.standard_normal((M, N)) + 2.0).astype(np.float32)
     step = nDFT - nolap if nolap else nDFT
     nBlks = (N - nolap) // step
     nf = nDFT // 2 + 1
     win = 0.54 - 0.46 * np.cos(2 * np.pi * np.arange(nDFT) / (nDFT - 1))
     scale = (1 / win.mean()) / nDFT / np.sqrt(nBlks)
     Yd = torch.tensor(Y, device="cuda")
-    Q = P.SPOD.spod_fft_device(Yd, N, nDFT, nDFT - step, nBlks, nf, win, scale).cpu().numpy()
+    mu = Y.astype(np.float64).mean(axis=1).astype(np.float32) if with_mean else np.zeros(M, np.float32)
+    md = torch.tensor(mu, device="cuda") if with_mean else None
+    Q = P.SPOD.spod_fft_device(Yd, N, nDFT, nDFT - step, nBlks, nf, win, scale,
+                               mean=md).cpu().numpy()
     assert Q.dtype == np.complex64
     for b in range(nBlks):
         i0 = b * step
-        F = np.fft.fft(Y[:, i0:i0 + nDFT].astype(np.float64) * win, axis=1)[:, :nf] * scale
+        Yc = (Y[:, i0:i0 + nDFT] - mu[:, None]).astype(np.float64)
+        F = np.fft.fft(Yc * win, axis=1)[:, :nf] * scale
         F[:, 1:nf - 1] *= 2
         np.testing.assert_allclose(Q[:, :, b].T, F, rtol=0, atol=2e-6 * np.abs(F).max())
