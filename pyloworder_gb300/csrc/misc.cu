@@ -114,8 +114,9 @@ int fill_uniform_dispatch(int dtype, void* out, int64_t count, uint64_t seed, cu
 // NC_MAX, smallest first); those whose norm is below 1/2 are replaced one at
 // a time by u = e_i - U (U^T e_i), normalised, with a different row i for
 // each (U^T e_i is row i of U, with the columns still to be completed left
-// out).  Without such columns the cost is one strided pass over the candidate
-// columns.
+// out).  The candidates' norms come from the factors, not from U (which may
+// be mapped host memory): U = F M with F the tall factor of Gram G, so
+// ||U e_c||^2 = m_c^T G m_c.  Without null columns U is not touched.
 // ---------------------------------------------------------------------------
 constexpr int NC_MAX = 8;
 
@@ -131,22 +132,24 @@ __global__ void nc_candidates_kernel(const double* __restrict__ S, int n, int* _
   *count = c;
 }
 
-template <typename T>
-__global__ void __launch_bounds__(256) nc_norms_kernel(const T* __restrict__ U, int64_t m,
-                                                       int64_t ldu, const int* __restrict__ list,
+// sums[q] += m_c^T G m_c over the 32 rows k of this block (c = list[q])
+__global__ void __launch_bounds__(256) nc_norms_kernel(const double* __restrict__ G,
+                                                       const double* __restrict__ Mf, int N,
+                                                       const int* __restrict__ list,
                                                        const int* __restrict__ count,
                                                        double* __restrict__ sums) {
   const int q = blockIdx.y;
   if (q >= *count) return;
   const int c = list[q];
-  double s = 0.0;
-  for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < m;
-       r += (int64_t)gridDim.x * blockDim.x) {
-    const double v = (double)U[r * ldu + c];
-    s = fma(v, v, s);
+  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+  double part = 0.0;
+  for (int k = blockIdx.x * 32 + wib; k < min(N, (int)blockIdx.x * 32 + 32); k += 8) {
+    double acc = 0.0;
+    for (int l = lane; l < N; l += 32) acc = fma(G[(int64_t)k * N + l], Mf[(int64_t)l * N + c], acc);
+    acc = warp_sum(acc);
+    part = fma(Mf[(int64_t)k * N + c], acc, part);
   }
-  s = warp_sum(s);
-  if ((threadIdx.x & 31) == 0) atomicAdd(&sums[q], s);
+  if (lane == 0) atomicAdd(&sums[q], part);
 }
 
 __device__ __forceinline__ int64_t nc_row(int q, int64_t m) {
@@ -204,22 +207,24 @@ __global__ void __launch_bounds__(256) nc_scale_kernel(T* __restrict__ U, int64_
 }
 
 template <typename T>
-int complete_null_columns(const double* S, int n, T* U, int64_t m, int64_t ldu, Arena& ws,
-                          cudaStream_t st) {
+int complete_null_columns(const double* S, int n, T* U, int64_t m, int64_t ldu, const double* G,
+                          const double* Mf, Arena& ws, cudaStream_t st) {
   int* list = ws.take<int>(NC_MAX);
   int* count = ws.take<int>(1);
   double* sums = ws.take<double>(NC_MAX);
   double* nrm2 = ws.take<double>(NC_MAX);
   if (ws.measuring() || n < 1 || m < 1) return PLOM_OK;
   PLOM_REQUIRE(!ws.overflow(), PLOM_ERR_WORKSPACE, "null-column completion: workspace too small");
-  PLOM_REQUIRE(S && U && n <= 8192, PLOM_ERR_ARG, "null-column completion: bad arguments");
+  PLOM_REQUIRE(S && U && G && Mf && n <= 8192, PLOM_ERR_ARG,
+               "null-column completion: bad arguments");
   ProfScope prof("null_cols", st, 0.0, (double)sizeof(T) * m, 2 + 2 * NC_MAX);
   PLOM_CHECK_CUDA(cudaMemsetAsync(sums, 0, sizeof(double) * NC_MAX, st));
   PLOM_CHECK_CUDA(cudaMemsetAsync(nrm2, 0, sizeof(double) * NC_MAX, st));
   nc_candidates_kernel<<<1, 32, 0, st>>>(S, n, list, count);
   PLOM_CHECK_LAUNCH();
   const unsigned gx = (unsigned)std::max<int64_t>(1, std::min<int64_t>(cdiv(m, 256), (int64_t)num_sms() * 4));
-  nc_norms_kernel<T><<<dim3(gx, NC_MAX), 256, 0, st>>>(U, m, ldu, list, count, sums);
+  nc_norms_kernel<<<dim3((unsigned)cdiv(n, 32), NC_MAX), 256, 0, st>>>(G, Mf, n, list, count,
+                                                                      sums);
   PLOM_CHECK_LAUNCH();
   const unsigned gp = (unsigned)std::max<int64_t>(1, std::min<int64_t>(cdiv(m, 8), (int64_t)num_sms() * 8));
   for (int q = 0; q < NC_MAX; ++q) {
@@ -231,10 +236,10 @@ int complete_null_columns(const double* S, int n, T* U, int64_t m, int64_t ldu, 
   }
   return PLOM_OK;
 }
-template int complete_null_columns<float>(const double*, int, float*, int64_t, int64_t, Arena&,
-                                          cudaStream_t);
-template int complete_null_columns<double>(const double*, int, double*, int64_t, int64_t, Arena&,
-                                           cudaStream_t);
+template int complete_null_columns<float>(const double*, int, float*, int64_t, int64_t,
+                                          const double*, const double*, Arena&, cudaStream_t);
+template int complete_null_columns<double>(const double*, int, double*, int64_t, int64_t,
+                                           const double*, const double*, Arena&, cudaStream_t);
 
 }  // namespace plom
 

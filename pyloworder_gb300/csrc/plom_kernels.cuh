@@ -95,9 +95,10 @@ int transpose_f64(const double* in, double* out, int64_t rows, int64_t cols, int
 // Orthonormal completion of the columns of U (m x n real, ld ldu) whose
 // singular value is <= 1e-6 sigma_1 and whose norm is below 1/2 (the zero
 // columns an exact zero column of the input leaves); S: n FP64 values,
-// descending.
+// descending; U = F Mf with Mf (n x n, FP64) and G = F^T F (n x n, FP64),
+// from which the candidates' norms are computed.
 template <typename T>
-int complete_null_columns(const double* S, int n, T* U, int64_t m, int64_t ldu, Arena& ws,
-                          cudaStream_t st);
+int complete_null_columns(const double* S, int n, T* U, int64_t m, int64_t ldu, const double* G,
+                          const double* Mf, Arena& ws, cudaStream_t st);
 
 }  // namespace plom

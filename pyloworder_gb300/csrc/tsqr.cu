@@ -350,7 +350,7 @@ static int svd_tail_packed(bool cplx, int n, PackedCore& b, int64_t m, float* U,
   P2.m = m;  // output rows (the planes may carry zero padding rows past m)
   PLOM_TRY(apply_packed(P2, Mop, N, N, U, ldu, nullptr, info, ws, st));
   PLOM_TRY(renorm_long_columns(Me, N, n, cw, U, m, ldu, 1, 0, 0, ws, st));
-  if (!cplx) PLOM_TRY(complete_null_columns<float>(S64, n, U, m, ldu, ws, st));
+  if (!cplx) PLOM_TRY(complete_null_columns<float>(S64, n, U, m, ldu, b.G, Me, ws, st));
   if (!ws.measuring()) {
     PLOM_TRY((convert<double, float>(S64, S, n, st)));
     PLOM_TRY((convert<double, float>(VH, VT, (int64_t)n * n * cw, st)));
@@ -577,7 +577,7 @@ static int tsqr_svd_impl(int prec, bool cplx, const TI* X, int64_t m, int n, int
   } else {
     PLOM_TRY((tall_apply<TC, TI>(prec, b.Q2, N, m, N, b.F, N, U, ldu, info, ws, st)));
   }
-  if (!cplx) PLOM_TRY(complete_null_columns<TI>(S64, n, U, m, ldu, ws, st));
+  if (!cplx) PLOM_TRY(complete_null_columns<TI>(S64, n, U, m, ldu, b.G, Me, ws, st));
   ws.off = std::max(need, ws.off);
   return PLOM_OK;
 }
