@@ -48,6 +48,13 @@ def test_workspace_queries():
     rs = lib.plom_randomized_svd_workspace(L.F32, L.PREC_MIXED, m, n, 80)
     assert 4 * m * n <= rs < 4 * m * n + 4 * m * 128 * 3 + 8 * m * 80 + (1 << 30)
     assert lib.plom_matmul_workspace(L.F64, L.PREC_FP64, 1, 1024, 80, m) > 0
+    # DMD projection on the 2,097,152 x 512 workload (r = 32): the point
+    # reductions' chunk partials and the small FP64 factors, well under 1 GiB;
+    # invalid shapes (r >= n, r > 1024) report 0
+    dp = lib.plom_dmd_project_workspace(2097152, 512, 32)
+    assert 0 < dp < (1 << 30)
+    assert lib.plom_dmd_project_workspace(1000, 10, 10) == 0
+    assert lib.plom_dmd_project_workspace(100000, 2000, 1025) == 0
 
 
 @pytest.mark.parametrize("args", [
