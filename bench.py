@@ -3,8 +3,8 @@
 
 Workload (one "step"): the TSQR-SVD of the large POD snapshot matrix,
 8,388,608 points x 1,024 snapshots, FP32 (32 GiB), temporal mean removed
-before the timed region, mixed precision form (TF32x3 tensor-core tall
-products, FP64 n x n stage).  The matrix is far larger than L2 (129 MB), so no
+before the timed region, mixed precision form (fp16-pair tensor-core tall
+products, FP64 n x n factors, double-float Jacobi SVD of R).  The matrix is far larger than L2 (129 MB), so no
 flush is needed between steps.
 
 metric "TSQR-SVD GB/s" = algorithmic bytes / time, bytes = s*m*n (read X) +

@@ -51,8 +51,9 @@ extern "C" {
 
 /* precision forms */
 #define PLOM_PREC_FP64 0  /* every product and reduction in FP64 (plain FP64 GPU form) */
-#define PLOM_PREC_MIXED 1 /* tall-skinny products on tensor cores (TF32 split into three
-                             terms, FP32 accumulate), small n x n factorizations in FP64 */
+#define PLOM_PREC_MIXED 1 /* tall-skinny products on tensor cores (FP32 operands packed as
+                             fp16 hi/lo pairs with per-column power-of-two scales, three f16
+                             products, FP32 accumulate), small n x n factorizations in FP64 */
 
 const char* plom_last_error_string(void);
 int plom_version(void);

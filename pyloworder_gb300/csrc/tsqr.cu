@@ -34,7 +34,7 @@
 namespace plom {
 
 static const double U64 = 1.1102230246251565e-16;  // 2^-53
-static const double U32 = 5.9604644775390625e-08;  // 2^-24 (TF32x3 ~ FP32)
+static const double U32 = 5.9604644775390625e-08;  // 2^-24 (the fp16-pair products are FP32-accurate)
 
 // ---------------------------------------------------------------------------
 // tall operations, dispatched on precision

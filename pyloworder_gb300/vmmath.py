@@ -7,9 +7,11 @@ out).  One extra keyword-only argument, ``precision``:
 
 * ``'fp64'``  -- every product and reduction in FP64 on the GPU (default for
   float64 / complex128 input);
-* ``'mixed'`` -- tall-skinny products on the tensor cores (TF32 split into
-  three terms, FP32 accumulation), n x n factorizations in FP64 (default for
-  float32 / complex64 input, whose reference path runs in single precision).
+* ``'mixed'`` -- tall-skinny products on the tensor cores (each FP32 operand
+  packed as an fp16 hi/lo pair with a power-of-two column scale, three f16
+  products per tile, FP32 accumulation drained to FP64 or double-float
+  partials), n x n factorizations in FP64 (default for float32 / complex64
+  input, whose reference path runs in single precision).
 """
 from __future__ import annotations
 

@@ -1,9 +1,10 @@
-"""Tensor-core (tcgen05 TF32x3) kernels of the mixed form against FP64
+"""Tensor-core (tcgen05, fp16-pair) kernels of the mixed form against FP64
 products: the tall apply (through math.matmul on float32) and the Gram
 (through math.tsqr on float32, whose R^T R must reproduce X^T X).
 
 Tolerance: 3e-6 relative to the product magnitude (|A||W| per entry), the
-TF32 three-term split being FP32-accurate to ~2^-22."""
+fp16 hi/lo operand pairs (22 significant bits, three products) being
+FP32-accurate to ~2^-22."""
 import numpy as np
 import pytest
 
