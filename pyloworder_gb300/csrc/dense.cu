@@ -414,6 +414,7 @@ struct JacState {
   int* perm;      // batch x n
   unsigned long long* amax;  // [batch] bits of max |a_ij|
   int64_t pitch;  // doubles per row (n * cw rounded up to even)
+  const double* V0;  // real, batch 1: starting rotation product (n x n row-major); null = I
 };
 
 __device__ __forceinline__ void rr_pair(int step, int k, int np, int& a, int& b) {
@@ -898,7 +899,9 @@ __device__ void jac_init(const double* __restrict__ A, int n, int batch, JacStat
     jac_put<DF>(dst, (int64_t)i * CW, src[0] * sc);
     if (CW == 2) jac_put<DF>(dst, (int64_t)i * CW + 1, src[1] * sc);
     double* v = js.Vt + b * n * P + (int64_t)i * P;
-    jac_put<DF>(v, (int64_t)j * CW, (i == j) ? 1.0 : 0.0);
+    // row i of Vt = column i of the starting rotation product
+    const double v0 = (CW == 1 && js.V0) ? js.V0[(int64_t)j * n + i] : ((i == j) ? 1.0 : 0.0);
+    jac_put<DF>(v, (int64_t)j * CW, v0);
     if (CW == 2) jac_put<DF>(v, (int64_t)j * CW + 1, 0.0);
     if (j == 0) {
       for (int64_t p = rl; p < P; ++p) {  // row padding stays zero
@@ -1511,6 +1514,299 @@ __global__ void __launch_bounds__(512, 1)
   jac_finish<1, true>(n, batch, js, sweep, S, U, VH, info, grid);
 }
 
+// ---------------------------------------------------------------------------
+// FP32 pre-sweeps of large real Jacobi problems at the mixed form's tolerance.
+// The block schedule of jacobi_block_df16_kernel (4-column blocks, one CTA
+// per block pair, 8 rows of At and Vt in shared memory, one grid barrier per
+// block step) on FP32 rows with explicit (c, s) rotations: a dot costs one
+// FMA per row instead of a double-float accumulation, a rotation four FMAs.
+// The sweeps stop when every pair is orthogonal to `tol` (at FP32 level, far
+// above the final tolerance) or after max_sweeps.  Output: the rotation
+// product J32 (n x n row-major FP32, J32 = the accumulated V); the host
+// re-orthonormalises it and hands B J32 to the double-float kernel.
+// ---------------------------------------------------------------------------
+constexpr int JAC_PRE32_MIN_N = 512;       // real, batch 1, n from here on
+constexpr float JAC_PRE32_TOL = 2e-6f;     // pair orthogonality of the FP32 phase
+constexpr int JAC_PRE32_MAX_SWEEPS = 30;
+
+struct Jac32State {
+  float* At;      // n x pitch: rows = columns of B (scaled by a power of two)
+  float* Vt;      // n x pitch: rows = columns of the rotation product
+  float* nrm2;    // n squared column norms; < 0 = recompute
+  int* counts;    // [JACOBI_MAX_SWEEPS] rotations per sweep
+  unsigned long long* amax;  // bits of max |b_ij|
+  int64_t pitch;  // floats per row: n rounded up to 4 (16-byte bulk copies)
+};
+
+// (c, s) of the rotation of a pair with squared norms al, be and dot g;
+// c = 0 when the pair is orthogonal to tol.  Carried norms al - t g, be + t g
+// (a drop below 1/8 is flagged for recomputation from the rows).
+__device__ __forceinline__ float2 f32_params(float& al, float& be, float g, float tol) {
+  if (!(al > 0.f && be > 0.f) || !(fabsf(g) > tol * sqrtf(al) * sqrtf(be)))
+    return make_float2(0.f, 0.f);
+  const float z = (be - al) / (2.0f * g);
+  const float az = fabsf(z);
+  const float t = az > 1e18f ? 0.5f / z : copysignf(1.0f, z) / (az + sqrtf(fmaf(z, z, 1.0f)));
+  const float c = 1.0f / sqrtf(fmaf(t, t, 1.0f));
+  const float tg = t * g;
+  const float na = al - tg, nb = be + tg;
+  al = (na > 0.125f * al) ? na : -1.f;
+  be = (nb > 0.125f * be) ? nb : -1.f;
+  return make_float2(c, c * t);
+}
+
+// dots over rows [h0, h1) of the warp (+ squared norms when sq)
+__device__ __forceinline__ void f32_dots(const float* x, const float* y, int64_t h0, int64_t h1,
+                                         int lane, bool sq, float& g, float& a2, float& b2) {
+  float g0 = 0.f, g1 = 0.f, aa = 0.f, bb = 0.f;
+  int64_t i = h0 + lane;
+  for (; i + 32 < h1; i += 64) {
+    const float x0 = x[i], x1 = x[i + 32], y0 = y[i], y1 = y[i + 32];
+    g0 = fmaf(x0, y0, g0);
+    g1 = fmaf(x1, y1, g1);
+    if (sq) {
+      aa = fmaf(x0, x0, fmaf(x1, x1, aa));
+      bb = fmaf(y0, y0, fmaf(y1, y1, bb));
+    }
+  }
+  for (; i < h1; i += 32) {
+    const float x0 = x[i], y0 = y[i];
+    g0 = fmaf(x0, y0, g0);
+    if (sq) {
+      aa = fmaf(x0, x0, aa);
+      bb = fmaf(y0, y0, bb);
+    }
+  }
+  g = warp_sum(g0 + g1);
+  a2 = sq ? warp_sum(aa) : 0.f;
+  b2 = sq ? warp_sum(bb) : 0.f;
+}
+
+// x' = c x - s y, y' = s x + c y over rows [h0, h1)
+__device__ __forceinline__ void f32_rotate(float* x, float* y, int64_t h0, int64_t h1, int lane,
+                                           float c, float s) {
+  for (int64_t i = h0 + lane; i < h1; i += 32) {
+    const float a = x[i], b = y[i];
+    x[i] = fmaf(c, a, -s * b);
+    y[i] = fmaf(s, a, c * b);
+  }
+}
+
+__global__ void __launch_bounds__(512, 1)
+    jacobi_block_f32_kernel(const double* __restrict__ B, int n, Jac32State js, float tol,
+                            int max_sweeps, float* __restrict__ J, int* info) {
+  extern __shared__ __align__(16) float jsm32[];  // [8][pitch] At rows, [8][pitch] Vt rows
+  __shared__ float snrm[8];
+  __shared__ float red[4][4][3];  // [pair][quarter][g a2 b2]
+  __shared__ float2 prm[4];       // (c, s) per pair; c = 0: no rotation
+  __shared__ int scol[8];
+  __shared__ __align__(8) uint64_t bar;
+  __shared__ int abort_sh;
+  cg::grid_group grid = cg::this_grid();
+  const int64_t P = js.pitch;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int pk = warp >> 2, qtr = warp & 3;  // pair slot, row quarter
+  const int64_t h0 = (int64_t)n * qtr / 4, h1 = (int64_t)n * (qtr + 1) / 4;
+  float* cA = jsm32;
+  float* cV = jsm32 + 8 * P;
+  const uint32_t bar_s = (uint32_t)__cvta_generic_to_shared(&bar);
+  if (threadIdx.x == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar_s));
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    abort_sh = 0;
+  }
+  // prologue: power-of-two scale (max |b_ij| < 1), At = B^T in FP32, Vt = I
+  const int64_t gtid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t gthreads = (int64_t)gridDim.x * blockDim.x;
+  if (gtid == 0) js.amax[0] = 0ull;
+  if (gtid < JACOBI_MAX_SWEEPS) js.counts[gtid] = 0;
+  grid.sync();
+  {
+    unsigned long long mx = 0ull;  // non-negative doubles order as their bits
+    for (int64_t e = gtid; e < (int64_t)n * n; e += gthreads) {
+      const unsigned long long v = (unsigned long long)__double_as_longlong(fabs(B[e]));
+      mx = v > mx ? v : mx;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      const unsigned long long w = __shfl_xor_sync(0xffffffffu, mx, o);
+      mx = w > mx ? w : mx;
+    }
+    if (lane == 0 && mx) atomicMax(js.amax, mx);
+  }
+  grid.sync();
+  {
+    int ex = 0;
+    frexp(__longlong_as_double((long long)js.amax[0]), &ex);
+    const double sc = ldexp(1.0, -ex);
+    for (int64_t e = gtid; e < (int64_t)n * P; e += gthreads) {
+      const int64_t i = e / P, j = e % P;  // row i of At / Vt, entry j
+      js.At[e] = (j < n) ? (float)(B[j * n + i] * sc) : 0.f;
+      js.Vt[e] = (j == i) ? 1.f : 0.f;
+    }
+    for (int64_t e = gtid; e < n; e += gthreads) js.nrm2[e] = -1.f;
+  }
+  grid.sync();
+
+  const int nb = (n + 3) / 4;
+  const int nbp = (nb + (nb & 1) < 2) ? 2 : nb + (nb & 1);  // even, >= 2
+  const int bpairs = nbp / 2;
+  uint32_t phase = 0;
+  int sweep = 0;
+  for (; sweep < max_sweeps; ++sweep) {
+    int myrot = 0;
+    for (int step = 0; step < nbp - 1; ++step) {
+      for (int task = blockIdx.x; task < bpairs; task += gridDim.x) {
+        int bi, bj;
+        rr_pair(step, task, nbp, bi, bj);
+        // the row loads go out first (their columns follow from the schedule
+        // alone); the carried norms are read while they are in flight
+        if (threadIdx.x == 0 && !abort_sh) {
+          asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+          uint32_t bytes = 0;
+          for (int s8 = 0; s8 < 8; ++s8)
+            if (4 * (s8 < 4 ? bi : bj) + (s8 & 3) < n) bytes += 2u * (uint32_t)(P * 4);
+          asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar_s),
+                       "r"(bytes)
+                       : "memory");
+          for (int s8 = 0; s8 < 8; ++s8) {
+            const int col = 4 * (s8 < 4 ? bi : bj) + (s8 & 3);
+            if (col >= n) continue;
+            bulk_load((uint32_t)__cvta_generic_to_shared(cA + s8 * P), js.At + (int64_t)col * P,
+                      (uint32_t)(P * 4), bar_s);
+            bulk_load((uint32_t)__cvta_generic_to_shared(cV + s8 * P), js.Vt + (int64_t)col * P,
+                      (uint32_t)(P * 4), bar_s);
+          }
+        }
+        if (threadIdx.x < 8) {
+          const int col = 4 * (threadIdx.x < 4 ? bi : bj) + (threadIdx.x & 3);
+          const bool v = col < n;
+          scol[threadIdx.x] = v ? col : -1;
+          snrm[threadIdx.x] = v ? js.nrm2[col] : 0.f;
+        }
+        if (!abort_sh) {
+          uint32_t ok = 0;
+          uint64_t t0 = 0;
+          asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t0));
+          while (true) {
+            asm volatile(
+                "{\n\t.reg .pred p;\n\t"
+                "mbarrier.try_wait.parity.acquire.cta.shared::cta.b64 p, [%1], %2;\n\t"
+                "selp.u32 %0, 1, 0, p;\n\t}"
+                : "=r"(ok)
+                : "r"(bar_s), "r"(phase)
+                : "memory");
+            if (ok) break;
+            uint64_t t1;
+            asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t1));
+            if (t1 - t0 > JAC_WAIT_NS) {
+              abort_sh = 1;
+              break;
+            }
+          }
+          phase ^= 1u;
+        }
+        __syncthreads();
+        if (abort_sh) {
+          if (threadIdx.x == 0) atomicMax(&info[ST_FAIL], PLOM_NUM_TIMEOUT);
+          __syncthreads();
+          continue;
+        }
+        if (step == 0) {
+          // exact squared norms once per sweep: 2 warps per row
+          const int s8 = warp >> 1, half = warp & 1;
+          float acc = 0.f;
+          if (scol[s8] >= 0) {
+            const float* x = cA + s8 * P;
+            for (int64_t i = (int64_t)n * half / 2 + lane; i < (int64_t)n * (half + 1) / 2; i += 32)
+              acc = fmaf(x[i], x[i], acc);
+          }
+          acc = warp_sum(acc);
+          if (lane == 0) red[s8 >> 1][(s8 & 1) * 2 + half][0] = acc;
+          __syncthreads();
+          if (threadIdx.x < 8) {
+            const int r8 = threadIdx.x;
+            snrm[r8] = red[r8 >> 1][(r8 & 1) * 2][0] + red[r8 >> 1][(r8 & 1) * 2 + 1][0];
+          }
+          __syncthreads();
+        }
+        const int nrounds = (step == 0) ? 7 : 4;
+        for (int rd = 0; rd < nrounds; ++rd) {
+          int a, c;
+          if (step == 0 && rd < 3) {
+            intra_pair(rd, pk & 1, a, c);
+            const int off = (pk >> 1) * 4;
+            a += off;
+            c += off;
+          } else {
+            const int u = (step == 0) ? rd - 3 : rd;
+            a = pk;
+            c = 4 + ((pk + u) & 3);
+          }
+          const bool live = scol[a] >= 0 && scol[c] >= 0;
+          const bool need = live && (snrm[a] < 0.f || snrm[c] < 0.f);
+          if (live) {
+            float g, a2, b2;
+            f32_dots(cA + a * P, cA + c * P, h0, h1, lane, need, g, a2, b2);
+            if (lane == 0) {
+              red[pk][qtr][0] = g;
+              red[pk][qtr][1] = a2;
+              red[pk][qtr][2] = b2;
+            }
+          }
+          __syncthreads();
+          if (qtr == pk && lane == 0) {
+            float2 cs = make_float2(0.f, 0.f);
+            if (live) {
+              const float g = (red[pk][0][0] + red[pk][1][0]) + (red[pk][2][0] + red[pk][3][0]);
+              float al = snrm[a], be = snrm[c];
+              if (al < 0.f) al = (red[pk][0][1] + red[pk][1][1]) + (red[pk][2][1] + red[pk][3][1]);
+              if (be < 0.f) be = (red[pk][0][2] + red[pk][1][2]) + (red[pk][2][2] + red[pk][3][2]);
+              cs = f32_params(al, be, g, tol);
+              snrm[a] = al;
+              snrm[c] = be;
+            }
+            prm[pk] = cs;
+            myrot += cs.x > 0.f ? 1 : 0;
+          }
+          __syncthreads();
+          const float2 cs = prm[pk];
+          if (cs.x > 0.f) {
+            f32_rotate(cA + a * P, cA + c * P, h0, h1, lane, cs.x, cs.y);
+            f32_rotate(cV + a * P, cV + c * P, h0, h1, lane, cs.x, cs.y);
+          }
+          __syncthreads();
+        }
+        // rows out (16-byte vectors: the pitch is a multiple of 4 floats)
+        for (int s8 = 0; s8 < 8; ++s8) {
+          const int col = scol[s8];
+          if (col < 0) continue;
+          float4* ga = reinterpret_cast<float4*>(js.At + (int64_t)col * P);
+          float4* gv = reinterpret_cast<float4*>(js.Vt + (int64_t)col * P);
+          const float4* sa = reinterpret_cast<const float4*>(cA + s8 * P);
+          const float4* sv = reinterpret_cast<const float4*>(cV + s8 * P);
+          for (int64_t i = threadIdx.x; i < P / 4; i += 512) {
+            ga[i] = sa[i];
+            gv[i] = sv[i];
+          }
+        }
+        if (threadIdx.x < 8 && scol[threadIdx.x] >= 0) js.nrm2[scol[threadIdx.x]] = snrm[threadIdx.x];
+        __syncthreads();
+      }
+      grid.sync();
+    }
+    if (lane == 0 && myrot) atomicAdd(&js.counts[sweep], myrot);
+    grid.sync();
+    if (js.counts[sweep] == 0) break;
+  }
+  if (gtid == 0) info[ST_SWEEPS32] = sweep < max_sweeps ? sweep + 1 : sweep;
+  // J32 (row-major): column k = row k of Vt
+  for (int64_t e = gtid; e < (int64_t)n * n; e += gthreads) {
+    const int64_t k = e / n, i = e % n;
+    J[i * n + k] = js.Vt[k * P + i];
+  }
+}
+
 // one warp per column pair, 4 pairs per 128-thread block, rows in global memory
 template <int CW>
 __global__ void __launch_bounds__(128) jacobi_pair_kernel(const double* __restrict__ A, int n,
@@ -1660,14 +1956,129 @@ static void carve_jac(Arena& ws, JacState& js, int n, int batch, int cplx) {
   js.counts = ws.take<int>(JACOBI_MAX_SWEEPS);
   js.perm = ws.take<int>((size_t)batch * n);
   js.amax = ws.take<unsigned long long>((size_t)batch);
+  js.V0 = nullptr;
+}
+
+// ---- FP32 pre-sweeps, host side -------------------------------------------
+// After the FP32 sweeps, J32 (FP32) is orthonormal to ~1e-5.  One
+// Newton-Schulz step of its polar factor, Jo = J32 (3 I - J32^T J32) / 2 =
+// J32 + J32 (I - G) / 2, brings that to ~1e-10 (G from exact FP32 products
+// with double-float sums; the correction term is ~1e-5 and needs FP32 only).
+// B' = B Jo is formed at double-float accuracy as one sum over 3n rows,
+// [Bh; Bh; Bl]^T [Joh; Jol; Joh] (hi/lo FP32 splits, B scaled by the power
+// of two of the FP32 phase), and the double-float kernel starts from
+// V = Jo, so its accumulated rotations are the V of B itself.
+__global__ void pre32_residual_kernel(const double* __restrict__ G, float* __restrict__ E, int n) {
+  const int64_t nn = (int64_t)n * n;
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < nn;
+       e += (int64_t)gridDim.x * blockDim.x)
+    E[e] = (float)(((e / n == e % n) ? 1.0 : 0.0) - G[e]);
+}
+
+__global__ void pre32_operands_kernel(const float* __restrict__ J32, const float* __restrict__ C,
+                                      const double* __restrict__ A,
+                                      const unsigned long long* __restrict__ amax,
+                                      double* __restrict__ Jo, float* __restrict__ Jcat,
+                                      float* __restrict__ Rcat, int n) {
+  const int64_t nn = (int64_t)n * n;
+  int ex = 0;
+  frexp(__longlong_as_double((long long)*amax), &ex);
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < nn;
+       e += (int64_t)gridDim.x * blockDim.x) {
+    const double jo = (double)J32[e] + 0.5 * (double)C[e];
+    Jo[e] = jo;
+    const float jh = (float)jo;
+    const float jl = (float)(jo - (double)jh);
+    Jcat[e] = jh;
+    Jcat[nn + e] = jl;
+    Jcat[2 * nn + e] = jh;
+    const double a = ldexp(A[e], -ex);
+    const float ah = (float)a;
+    const float al = (float)(a - (double)ah);
+    Rcat[e] = ah;
+    Rcat[nn + e] = ah;
+    Rcat[2 * nn + e] = al;
+  }
+}
+
+__global__ void pre32_unscale_kernel(double* __restrict__ S, int n,
+                                     const unsigned long long* __restrict__ amax) {
+  int ex = 0;
+  frexp(__longlong_as_double((long long)*amax), &ex);
+  for (int i = threadIdx.x; i < n; i += blockDim.x) S[i] = ldexp(S[i], ex);
+}
+
+static bool use_pre32(int n, double tol) {
+  const int64_t pitch = ((int64_t)n + 3) / 4 * 4;
+  return n >= JAC_PRE32_MIN_N && tol >= JAC_DF_TOL &&
+         (size_t)16 * pitch * sizeof(float) <= JAC_BLOCK_SMEM_MAX;
+}
+
+// SVD of B = A^T (At holds B, A is B^T) through the FP32 pre-sweeps:
+// B = Ut diag(S) VHt, VHt = (Jo V')^T.
+static int jacobi_pre32(const double* A, const double* At, int n, double tol, double* S,
+                        double* Ut, double* VHt, int* info, Arena& ws, cudaStream_t st) {
+  const size_t nn = (size_t)n * n;
+  Jac32State j32;
+  j32.pitch = ((int64_t)n + 3) / 4 * 4;
+  j32.At = ws.take<float>((size_t)n * j32.pitch);
+  j32.Vt = ws.take<float>((size_t)n * j32.pitch);
+  j32.nrm2 = ws.take<float>(n);
+  j32.counts = ws.take<int>(JACOBI_MAX_SWEEPS);
+  j32.amax = ws.take<unsigned long long>(1);
+  float* J32 = ws.take<float>(nn);
+  float* E = ws.take<float>(nn);
+  float* C = ws.take<float>(nn);
+  double* G = ws.take<double>(nn);
+  double* Jo = ws.take<double>(nn);
+  float* Jcat = ws.take<float>(3 * nn);
+  float* Rcat = ws.take<float>(3 * nn);
+  double* Bp = ws.take<double>(nn);
+  JacState js;
+  carve_jac(ws, js, n, 1, 0);
+  if (ws.measuring()) {  // the partials of the two double-float products
+    PLOM_TRY(gemm_tn_df(nullptr, n, nullptr, n, nullptr, n, n, n, n, ws, st));
+    return gemm_tn_df(nullptr, n, nullptr, n, nullptr, n, n, n, 3 * (int64_t)n, ws, st);
+  }
+  PLOM_REQUIRE(!ws.overflow(), PLOM_ERR_WORKSPACE, "jacobi: workspace too small");
+  {
+    const void* k = (const void*)jacobi_block_f32_kernel;
+    const size_t smem = (size_t)16 * j32.pitch * sizeof(float);
+    PLOM_CHECK_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    const int nb = (n + 3) / 4;
+    const int nbp = std::max(2, nb + (nb & 1));
+    const int blocks = coop_blocks(k, 512, smem, nbp / 2);
+    float tolf = JAC_PRE32_TOL;
+    int maxs = JAC_PRE32_MAX_SWEEPS;
+    const double* Bin = At;
+    void* args[] = {(void*)&Bin,  (void*)&n,   (void*)&j32, (void*)&tolf,
+                    (void*)&maxs, (void*)&J32, (void*)&info};
+    ProfScope prof("jacobi_svd_f32", st, 0.0, 4.0 * 3.0 * n * n);
+    PLOM_CHECK_CUDA(cudaLaunchCooperativeKernel(k, dim3(blocks), dim3(512), args, smem, st));
+  }
+  const int eg = (int)std::max<int64_t>(1, std::min<int64_t>(cdiv((int64_t)nn, 256),
+                                                             (int64_t)num_sms() * 16));
+  PLOM_TRY(gemm_tn_df(J32, n, J32, n, G, n, n, n, n, ws, st));  // G = J32^T J32
+  pre32_residual_kernel<<<eg, 256, 0, st>>>(G, E, n);
+  PLOM_CHECK_LAUNCH();
+  PLOM_TRY((gemm_nn<float, float, float, float>(J32, n, E, n, C, n, n, n, n, st)));
+  pre32_operands_kernel<<<eg, 256, 0, st>>>(J32, C, A, j32.amax, Jo, Jcat, Rcat, n);
+  PLOM_CHECK_LAUNCH();
+  PLOM_TRY(gemm_tn_df(Rcat, n, Jcat, n, Bp, n, n, n, 3 * (int64_t)n, ws, st));  // B Jo, scaled
+  js.V0 = Jo;
+  PLOM_TRY(jacobi_launch(Bp, n, 1, 0, js, tol, S, Ut, VHt, info, st));
+  pre32_unscale_kernel<<<1, 256, 0, st>>>(S, n, j32.amax);
+  PLOM_CHECK_LAUNCH();
+  return PLOM_OK;
 }
 
 size_t dense_workspace(int n, int batch, int cplx) {
-  Arena a(nullptr, 0);
-  if (!cplx && batch == 1 && n >= JACOBI_TRANSPOSED_MIN_N) a.take<double>(3 * (size_t)n * n);
-  JacState js;
-  carve_jac(a, js, n, batch, cplx);
-  return a.off + 256;
+  // the larger of the two forms' needs (the mixed form's tolerance may take
+  // the FP32 pre-sweeps)
+  Arena a(nullptr, 0), b(nullptr, 0);
+  jacobi_svd(nullptr, n, batch, cplx, 1e-8, nullptr, nullptr, nullptr, nullptr, a, nullptr);
+  jacobi_svd(nullptr, n, batch, cplx, 0.0, nullptr, nullptr, nullptr, nullptr, b, nullptr);
+  return std::max(a.off, b.off) + 256;
 }
 
 // Real n x n SVD through the transpose: one-sided Jacobi on A^T (whose
@@ -1679,13 +2090,18 @@ static int jacobi_svd_transposed(const double* A, int n, double tol, double* S, 
   double* At = ws.take<double>(nn);
   double* Ut = ws.take<double>(nn);
   double* VHt = ws.take<double>(nn);
+  const bool pre32 = use_pre32(n, tol);
   JacState js;
-  carve_jac(ws, js, n, 1, 0);
-  if (ws.measuring()) return PLOM_OK;
+  if (!pre32) carve_jac(ws, js, n, 1, 0);
+  if (ws.measuring())
+    return pre32 ? jacobi_pre32(A, At, n, tol, S, Ut, VHt, info, ws, st) : PLOM_OK;
   PLOM_REQUIRE(!ws.overflow(), PLOM_ERR_WORKSPACE, "jacobi: workspace too small");
   PLOM_REQUIRE(A && S && U && VH && info, PLOM_ERR_ARG, "jacobi: null pointer");
   PLOM_TRY(transpose_f64(A, At, n, n, 1, st));
-  PLOM_TRY(jacobi_launch(At, n, 1, 0, js, tol, S, Ut, VHt, info, st));
+  if (pre32)
+    PLOM_TRY(jacobi_pre32(A, At, n, tol, S, Ut, VHt, info, ws, st));
+  else
+    PLOM_TRY(jacobi_launch(At, n, 1, 0, js, tol, S, Ut, VHt, info, st));
   PLOM_TRY(transpose_f64(VHt, U, n, n, 1, st));   // U of A = Vt (columns)
   PLOM_TRY(transpose_f64(Ut, VH, n, n, 1, st));   // rows of V^T of A = columns of Ut
   return PLOM_OK;

@@ -126,6 +126,32 @@ def test_mixed_mean_removed_u_orthonormal():
     assert float((Vd @ Vd.T - torch.eye(n, dtype=torch.float64, device="cuda")).abs().max()) < 1e-6
 
 
+def test_mixed_large_n_fp32_presweeps():
+    """n >= 512 in the mixed form: the SVD of R starts with FP32 Jacobi sweeps,
+    re-orthonormalises their rotation product and finishes with double-float
+    sweeps from it.  The result must match the plain FP64 form within the
+    mixed-form tolerances, with orthonormal U and V."""
+    from pyloworder_gb300 import _lib as L
+    from pyloworder_gb300 import datagen
+    m, n, k = 32768, 1024, 64
+    nx, ny = datagen.grid_for_points(m)
+    X = datagen.pod_field_device(nx, ny, n, k, seed=91, noise=1e-5, amp_pow=1.5, m=m)
+    Y, _, _ = P.vmmath.remove_mean_device(X, n)
+    U, S, V = P.vmmath.tsqr_svd_device(Y, n, "mixed")
+    info = list(L.last_info)
+    print(f"FP32 sweeps {info[4]}, double-float sweeps {info[2]}")
+    assert info[4] > 0  # the FP32 phase ran
+    Ur, Sr, _ = P.vmmath.tsqr_svd_device(Y.double(), n, "fp64")
+    S64, Sr64 = S.double().cpu().numpy(), Sr.cpu().numpy()
+    assert sigma_rel(S64, Sr64, k) < 1e-5
+    assert sigma_normwise(S64, Sr64) < 1e-5
+    assert subspace_angle(U[:, :k].double().cpu().numpy(), Ur[:, :k].cpu().numpy()) < 1e-4
+    eye = torch.eye(n, dtype=torch.float64, device="cuda")
+    Ud, Vd = U.double(), V.double()
+    assert float((Ud.T @ Ud - eye).abs().max()) < 1e-4
+    assert float((Vd @ Vd.T - eye).abs().max()) < 1e-6
+
+
 @pytest.mark.parametrize("precision", ["mixed", "fp64"])
 @pytest.mark.parametrize("case", ["zero_col", "zero_cols3", "dup_cols", "rank3", "tiny_m", "n1",
                                   "wide_ragged"])
