@@ -1555,26 +1555,32 @@ __device__ __forceinline__ float2 f32_params(float& al, float& be, float g, floa
   return make_float2(c, c * t);
 }
 
-// dots over rows [h0, h1) of the warp (+ squared norms when sq)
-__device__ __forceinline__ void f32_dots(const float* x, const float* y, int64_t h0, int64_t h1,
+// dots over rows [h0, h1) of the warp (+ squared norms when sq); two rows per
+// lane and access when both bounds are even (8-byte shared loads, 32-bit
+// indices: the loop is issue-bound)
+__device__ __forceinline__ void f32_dots(const float* x, const float* y, int h0, int h1,
                                          int lane, bool sq, float& g, float& a2, float& b2) {
   float g0 = 0.f, g1 = 0.f, aa = 0.f, bb = 0.f;
-  int64_t i = h0 + lane;
-  for (; i + 32 < h1; i += 64) {
-    const float x0 = x[i], x1 = x[i + 32], y0 = y[i], y1 = y[i + 32];
-    g0 = fmaf(x0, y0, g0);
-    g1 = fmaf(x1, y1, g1);
-    if (sq) {
-      aa = fmaf(x0, x0, fmaf(x1, x1, aa));
-      bb = fmaf(y0, y0, fmaf(y1, y1, bb));
+  if (((h0 | h1) & 1) == 0) {
+    const float2* x2 = reinterpret_cast<const float2*>(x);
+    const float2* y2 = reinterpret_cast<const float2*>(y);
+    for (int i = (h0 >> 1) + lane; i < (h1 >> 1); i += 32) {
+      const float2 xv = x2[i], yv = y2[i];
+      g0 = fmaf(xv.x, yv.x, g0);
+      g1 = fmaf(xv.y, yv.y, g1);
+      if (sq) {
+        aa = fmaf(xv.x, xv.x, fmaf(xv.y, xv.y, aa));
+        bb = fmaf(yv.x, yv.x, fmaf(yv.y, yv.y, bb));
+      }
     }
-  }
-  for (; i < h1; i += 32) {
-    const float x0 = x[i], y0 = y[i];
-    g0 = fmaf(x0, y0, g0);
-    if (sq) {
-      aa = fmaf(x0, x0, aa);
-      bb = fmaf(y0, y0, bb);
+  } else {
+    for (int i = h0 + lane; i < h1; i += 32) {
+      const float x0 = x[i], y0 = y[i];
+      g0 = fmaf(x0, y0, g0);
+      if (sq) {
+        aa = fmaf(x0, x0, aa);
+        bb = fmaf(y0, y0, bb);
+      }
     }
   }
   g = warp_sum(g0 + g1);
@@ -1583,12 +1589,22 @@ __device__ __forceinline__ void f32_dots(const float* x, const float* y, int64_t
 }
 
 // x' = c x - s y, y' = s x + c y over rows [h0, h1)
-__device__ __forceinline__ void f32_rotate(float* x, float* y, int64_t h0, int64_t h1, int lane,
-                                           float c, float s) {
-  for (int64_t i = h0 + lane; i < h1; i += 32) {
-    const float a = x[i], b = y[i];
-    x[i] = fmaf(c, a, -s * b);
-    y[i] = fmaf(s, a, c * b);
+__device__ __forceinline__ void f32_rotate(float* x, float* y, int h0, int h1, int lane, float c,
+                                           float s) {
+  if (((h0 | h1) & 1) == 0) {
+    float2* x2 = reinterpret_cast<float2*>(x);
+    float2* y2 = reinterpret_cast<float2*>(y);
+    for (int i = (h0 >> 1) + lane; i < (h1 >> 1); i += 32) {
+      const float2 a = x2[i], b = y2[i];
+      x2[i] = make_float2(fmaf(c, a.x, -s * b.x), fmaf(c, a.y, -s * b.y));
+      y2[i] = make_float2(fmaf(s, a.x, c * b.x), fmaf(s, a.y, c * b.y));
+    }
+  } else {
+    for (int i = h0 + lane; i < h1; i += 32) {
+      const float a = x[i], b = y[i];
+      x[i] = fmaf(c, a, -s * b);
+      y[i] = fmaf(s, a, c * b);
+    }
   }
 }
 
@@ -1598,7 +1614,6 @@ __global__ void __launch_bounds__(512, 1)
   extern __shared__ __align__(16) float jsm32[];  // [8][pitch] At rows, [8][pitch] Vt rows
   __shared__ float snrm[8];
   __shared__ float red[4][4][3];  // [pair][quarter][g a2 b2]
-  __shared__ float2 prm[4];       // (c, s) per pair; c = 0: no rotation
   __shared__ int scol[8];
   __shared__ __align__(8) uint64_t bar;
   __shared__ int abort_sh;
@@ -1606,7 +1621,7 @@ __global__ void __launch_bounds__(512, 1)
   const int64_t P = js.pitch;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int pk = warp >> 2, qtr = warp & 3;  // pair slot, row quarter
-  const int64_t h0 = (int64_t)n * qtr / 4, h1 = (int64_t)n * (qtr + 1) / 4;
+  const int h0 = n * qtr / 4, h1 = n * (qtr + 1) / 4;
   float* cA = jsm32;
   float* cV = jsm32 + 8 * P;
   const uint32_t bar_s = (uint32_t)__cvta_generic_to_shared(&bar);
@@ -1718,7 +1733,7 @@ __global__ void __launch_bounds__(512, 1)
           float acc = 0.f;
           if (scol[s8] >= 0) {
             const float* x = cA + s8 * P;
-            for (int64_t i = (int64_t)n * half / 2 + lane; i < (int64_t)n * (half + 1) / 2; i += 32)
+            for (int i = n * half / 2 + lane; i < n * (half + 1) / 2; i += 32)
               acc = fmaf(x[i], x[i], acc);
           }
           acc = warp_sum(acc);
@@ -1744,7 +1759,8 @@ __global__ void __launch_bounds__(512, 1)
             c = 4 + ((pk + u) & 3);
           }
           const bool live = scol[a] >= 0 && scol[c] >= 0;
-          const bool need = live && (snrm[a] < 0.f || snrm[c] < 0.f);
+          float al = snrm[a], be = snrm[c];  // read before the owner updates them
+          const bool need = live && (al < 0.f || be < 0.f);
           if (live) {
             float g, a2, b2;
             f32_dots(cA + a * P, cA + c * P, h0, h1, lane, need, g, a2, b2);
@@ -1755,22 +1771,20 @@ __global__ void __launch_bounds__(512, 1)
             }
           }
           __syncthreads();
-          if (qtr == pk && lane == 0) {
-            float2 cs = make_float2(0.f, 0.f);
-            if (live) {
-              const float g = (red[pk][0][0] + red[pk][1][0]) + (red[pk][2][0] + red[pk][3][0]);
-              float al = snrm[a], be = snrm[c];
-              if (al < 0.f) al = (red[pk][0][1] + red[pk][1][1]) + (red[pk][2][1] + red[pk][3][1]);
-              if (be < 0.f) be = (red[pk][0][2] + red[pk][1][2]) + (red[pk][2][2] + red[pk][3][2]);
-              cs = f32_params(al, be, g, tol);
+          // every lane of the pair's four warps derives the same (c, s) from
+          // the same sums in the same order; the first warp stores the norms
+          float2 cs = make_float2(0.f, 0.f);
+          if (live) {
+            const float g = (red[pk][0][0] + red[pk][1][0]) + (red[pk][2][0] + red[pk][3][0]);
+            if (al < 0.f) al = (red[pk][0][1] + red[pk][1][1]) + (red[pk][2][1] + red[pk][3][1]);
+            if (be < 0.f) be = (red[pk][0][2] + red[pk][1][2]) + (red[pk][2][2] + red[pk][3][2]);
+            cs = f32_params(al, be, g, tol);
+            if (qtr == 0 && lane == 0) {
               snrm[a] = al;
               snrm[c] = be;
+              myrot += cs.x > 0.f ? 1 : 0;
             }
-            prm[pk] = cs;
-            myrot += cs.x > 0.f ? 1 : 0;
           }
-          __syncthreads();
-          const float2 cs = prm[pk];
           if (cs.x > 0.f) {
             f32_rotate(cA + a * P, cA + c * P, h0, h1, lane, cs.x, cs.y);
             f32_rotate(cV + a * P, cV + c * P, h0, h1, lane, cs.x, cs.y);

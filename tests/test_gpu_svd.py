@@ -126,14 +126,16 @@ def test_mixed_mean_removed_u_orthonormal():
     assert float((Vd @ Vd.T - torch.eye(n, dtype=torch.float64, device="cuda")).abs().max()) < 1e-6
 
 
-def test_mixed_large_n_fp32_presweeps():
+@pytest.mark.parametrize("n", [1024, 517])
+def test_mixed_large_n_fp32_presweeps(n):
     """n >= 512 in the mixed form: the SVD of R starts with FP32 Jacobi sweeps,
     re-orthonormalises their rotation product and finishes with double-float
     sweeps from it.  The result must match the plain FP64 form within the
-    mixed-form tolerances, with orthonormal U and V."""
+    mixed-form tolerances, with orthonormal U and V (n = 517: odd row
+    quarters take the one-row-per-lane loops)."""
     from pyloworder_gb300 import _lib as L
     from pyloworder_gb300 import datagen
-    m, n, k = 32768, 1024, 64
+    m, k = 32768, 64
     nx, ny = datagen.grid_for_points(m)
     X = datagen.pod_field_device(nx, ny, n, k, seed=91, noise=1e-5, amp_pow=1.5, m=m)
     Y, _, _ = P.vmmath.remove_mean_device(X, n)
