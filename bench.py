@@ -396,7 +396,8 @@ def run_ours(args):
                 "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "fp64_form": fp64,
                 "accuracy_vs_fp64": acc, "serving": serve, "kernels": kernels,
                 "info": {"cholesky_shift_escalations": info_words[1] if info_words else None,
-                         "jacobi_sweeps": info_words[2] if info_words else None}}
+                         "jacobi_sweeps": info_words[2] if info_words else None,
+                         "jacobi_fp32_sweeps": info_words[4] if info_words else None}}
         print(json.dumps(line), flush=True)
     if world > 1:
         import torch.distributed as dist
