@@ -14,7 +14,7 @@
  *     device array `info` (PLOM_INFO_WORDS int32 words), info[0] = PLOM_NUM_*.
  *     Diagnostics in the same array: info[1] Cholesky shift escalations,
  *     info[2] Jacobi sweeps (FP64 or double-float rows), info[4] FP32
- *     Jacobi pre-sweeps (mixed form, real, n >= 512; 0 otherwise).
+ *     Jacobi pre-sweeps (mixed form, real, 512 <= n <= 1600; 0 otherwise).
  *
  * Each declaration names the pyLOM interface it replaces (paths inside the
  * pyLowOrder project): the C symbols pyLOM binds through Cython in

@@ -2022,10 +2022,11 @@ __global__ void pre32_unscale_kernel(double* __restrict__ S, int n,
   for (int i = threadIdx.x; i < n; i += blockDim.x) S[i] = ldexp(S[i], ex);
 }
 
+// Only where the double-float finish runs in shared memory (the df16 block
+// kernel): larger n keeps the double-float-only path.
 static bool use_pre32(int n, double tol) {
-  const int64_t pitch = ((int64_t)n + 3) / 4 * 4;
   return n >= JAC_PRE32_MIN_N && tol >= JAC_DF_TOL &&
-         (size_t)16 * pitch * sizeof(float) <= JAC_BLOCK_SMEM_MAX;
+         (size_t)16 * jac_pitch(n, 0) * sizeof(double) <= JAC_BLOCK_SMEM_MAX;
 }
 
 // SVD of B = A^T (At holds B, A is B^T) through the FP32 pre-sweeps:

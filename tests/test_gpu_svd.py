@@ -128,7 +128,7 @@ def test_mixed_mean_removed_u_orthonormal():
 
 @pytest.mark.parametrize("n", [1024, 517])
 def test_mixed_large_n_fp32_presweeps(n):
-    """n >= 512 in the mixed form: the SVD of R starts with FP32 Jacobi sweeps,
+    """512 <= n <= 1600 in the mixed form: the SVD of R starts with FP32 Jacobi sweeps,
     re-orthonormalises their rotation product and finishes with double-float
     sweeps from it.  The result must match the plain FP64 form within the
     mixed-form tolerances, with orthonormal U and V (n = 517: odd row
