@@ -1523,9 +1523,10 @@ __global__ void __launch_bounds__(512, 1)
 // The sweeps stop when every pair is orthogonal to `tol` (at FP32 level, far
 // above the final tolerance) or after max_sweeps.  Output: the rotation
 // product J32 (n x n row-major FP32, J32 = the accumulated V); the host
-// re-orthonormalises it and hands B J32 to the double-float kernel.
+// re-orthonormalises it to Jo and hands B Jo to the double-float kernel,
+// whose accumulated rotations start from Jo (jacobi_pre32).
 // ---------------------------------------------------------------------------
-constexpr int JAC_PRE32_MIN_N = 512;       // real, batch 1, n from here on
+constexpr int JAC_PRE32_MIN_N = 512;       // real, batch 1, n from here on (see use_pre32)
 constexpr float JAC_PRE32_TOL = 2e-6f;     // pair orthogonality of the FP32 phase
 constexpr int JAC_PRE32_MAX_SWEEPS = 30;
 
