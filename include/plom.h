@@ -106,7 +106,10 @@ int plom_matmul(int dtype, int prec, int transA, const void* A, int64_t lda, con
 /* ---- SVD family -------------------------------------------------------- */
 /* replaces stsqr/dtsqr (pyLOM/vmmath/src/svd.c:416,565; svd.py:50):
    Q (m x n, ldq) with orthonormal columns and upper-triangular R (n x n) with
-   X = Q R.  dtype F32 or F64 (R has the same type). */
+   X = Q R, m >= n.  The factors carry the column signs of Householder QR
+   (LAPACK geqrf + orgqr, which the reference's qr and one-rank tsqr return):
+   R_kk = -sign(pivot_k) |R_kk| as Householder's reflections choose it, not
+   CholeskyQR's positive diagonal.  dtype F32 or F64 (R has the same type). */
 size_t plom_tsqr_workspace(int dtype, int prec, int64_t m, int64_t n);
 int plom_tsqr(int dtype, int prec, const void* X, int64_t m, int64_t n, int64_t ldx, void* Q,
               int64_t ldq, void* R, void* ws, size_t ws_bytes, int* info, void* stream);
@@ -148,6 +151,18 @@ size_t plom_randomized_svd_workspace(int dtype, int prec, int64_t m, int64_t n, 
 int plom_randomized_svd(int dtype, int prec, const void* X, int64_t m, int64_t n, int64_t ldx,
                         int64_t r, int q, uint64_t seed, void* U, int64_t ldu, void* S, void* VT,
                         void* ws, size_t ws_bytes, int* info, void* stream);
+
+/* replaces srandomized_qr/drandomized_qr (svd.c:1012,1267; svd.py:121,
+   randomized_qr2 at svd.py:147 computes the same factors): the randomized
+   range finder Y = X Omega, q times (Q = tsqr(Y), Y = X (X^T Q)), Q =
+   tsqr(Y) with Householder QR's column signs, B = Q^T X.  Outputs Q (m x r,
+   ldq) and B (r x n, dense), both of dtype.  omega: the n x r test matrix
+   (dtype, dense) when not NULL, else uniform [0,1) from Philox4x32-10 keyed by
+   seed (see plom_fill_uniform). */
+size_t plom_randomized_qr_workspace(int dtype, int prec, int64_t m, int64_t n, int64_t r);
+int plom_randomized_qr(int dtype, int prec, const void* X, int64_t m, int64_t n, int64_t ldx,
+                       int64_t r, int q, uint64_t seed, const void* omega, void* Q, int64_t ldq,
+                       void* B, void* ws, size_t ws_bytes, int* info, void* stream);
 
 /* replaces srandom_matrix/drandom_matrix (vector_matrix.c:950,964): out[i] =
    uniform [0,1) for flat index i, Philox4x32-10 with key = seed, counter = i. */

@@ -141,6 +141,30 @@ def tsqr(Ai):
     return matmul(Q1, QW), R
 
 
+def householder_signs(Q):
+    """Column signs s with Q diag(s), diag(s) R the Householder QR factors of
+    the matrix whose CholeskyQR factors (R with a positive diagonal) are Q, R:
+    s_k = minus the sign of the k-th pivot of the LU of Q's top n x n block
+    shifted by diag(s) as it is built (Ballard, Demmel, Grigori, Jacquelin,
+    Knight, Nguyen, J. Parallel Distrib. Comput. 85, 2015).  The sign rule the
+    CUDA tsqr applies on the device; checked here against numpy/LAPACK's
+    factors (the reference's qr, pyLOM/vmmath/svd.py:29-36).  For a square
+    matrix LAPACK's last reflector is the identity (dlarfg of a 1-vector), so
+    the last R entry keeps the pivot's own sign."""
+    m, n = Q.shape
+    A = np.array(Q[:n, :n], dtype=np.float64)
+    s = np.empty(n)
+    for k in range(n):
+        if m == n and k == n - 1:
+            s[k] = 1.0 if A[k, k] >= 0 else -1.0
+            break
+        s[k] = -1.0 if A[k, k] >= 0 else 1.0
+        A[k, k] -= s[k]
+        A[k + 1:, k] /= A[k, k]
+        A[k + 1:, k + 1:] -= np.outer(A[k + 1:, k], A[k, k + 1:])
+    return s
+
+
 def tsqr_svd(Ai):
     """TSQR -> svd(R) -> U = Q @ Ur (Sayadi & Schmid 2016, Alg. 2).
     pyLOM/vmmath/svd.py:228-252.  Returns (U m x n, S n, V n x n) with V = V^T."""
@@ -417,8 +441,12 @@ def hannwin(N):
     return 0.5 - 0.5 * np.cos(2 * np.pi * np.arange(N) / (N - 1))
 
 
-def spod_run(X, t, nDFT=0, nolap=0, remove_mean=True, window="hamming"):
-    """Welch SPOD.  pyLOM/SPOD/wrapper.py:24-95 (``_fft`` at :18-20)."""
+def spod_run(X, t, nDFT=0, nolap=0, remove_mean=True, window="hamming", return_U=False):
+    """Welch SPOD.  pyLOM/SPOD/wrapper.py:24-95 (``_fft`` at :18-20).
+    With ``return_U`` the per-frequency complex left singular vectors
+    (M x nBlks each, in the returned frequency order) come back as a fourth
+    value: P = Re(U) depends on the arbitrary phase of each column, U up to
+    that phase does not."""
     M, N = X.shape
     dt = t[1] - t[0]
     cdtype = _cplx(X.dtype)
@@ -442,12 +470,17 @@ def spod_run(X, t, nDFT=0, nolap=0, remove_mean=True, window="hamming"):
         Q[:, iblk] = qk.reshape((M * nf), order="F")
     L = np.zeros((nf, nBlks), X.dtype)
     P = np.zeros((M * nBlks, nf), X.dtype)
+    Us = []
     for ifreq in range(nf):
         qf = Q[ifreq * M:(ifreq + 1) * M, :].copy() / np.sqrt(nBlks)
         U, S, V = tsqr_svd(qf)
         P[:, ifreq] = np.real(U.reshape((M * nBlks), order="F"))
         L[ifreq, :] = np.abs(S * S)
+        if return_U:
+            Us.append(U)
     order = np.argsort(L[:, 0])[::-1]
+    if return_U:
+        return L[order, :], P[:, order], f[order], [Us[i] for i in order]
     return L[order, :], P[:, order], f[order]
 
 

@@ -72,6 +72,10 @@ PROTOS = {
     "plom_randomized_svd": (c_int, [c_int, c_int, c_vp, c_i64, c_i64, c_i64, c_i64, c_int,
                                     ctypes.c_uint64, c_vp, c_i64, c_vp, c_vp, c_vp, c_sz, c_vp,
                                     c_vp]),
+    "plom_randomized_qr_workspace": (c_sz, [c_int, c_int, c_i64, c_i64, c_i64]),
+    "plom_randomized_qr": (c_int, [c_int, c_int, c_vp, c_i64, c_i64, c_i64, c_i64, c_int,
+                                   ctypes.c_uint64, c_vp, c_vp, c_i64, c_vp, c_vp, c_sz, c_vp,
+                                   c_vp]),
     "plom_fill_uniform": (c_int, [c_int, c_vp, c_i64, ctypes.c_uint64, c_vp]),
     "plom_spod_fft": (c_int, [c_int, c_vp, c_i64, c_i64, c_i64, c_vp, c_i64, c_i64, c_i64, c_i64,
                               c_vp, c_vp, c_vp, ctypes.c_double, c_vp, c_vp]),

@@ -1004,15 +1004,21 @@ __global__ void __launch_bounds__(A_THREADS, 1)
 }
 
 // ---------------------------------------------------------------------------
-// renormalisation of long-factor columns of U = Q2 M (see renorm_long_columns)
+// renormalisation of long-factor columns of U = Q2 M (see renorm_long_columns).
+// Deterministic: the columns are chosen by an ordered scan (the RN_MAX longest
+// factor columns above the threshold, ties to the lower index, listed in index
+// order) and every sum is taken in a fixed order (per-block partials, summed
+// in block order by the consumer), so repeated calls on the same input give
+// bitwise-identical U.
 // ---------------------------------------------------------------------------
-constexpr int RN_MAX = 8;  // columns per problem
+constexpr int RN_MAX = 32;      // columns per problem
+constexpr int RN_THREADS = 256;
 
-// list the columns j with ||M e_(cw j)||^2 > thr2: blocks of 32 columns x 8
-// row groups per problem (count and sums zeroed beforehand)
-__global__ void __launch_bounds__(256) rn_flag_kernel(const double* __restrict__ M, int N, int n,
-                                                      int cw, int64_t mstride, double thr2,
-                                                      int* __restrict__ list, int* __restrict__ count) {
+// nrm2[b n + j] = ||M e_(cw j)||^2: blocks of 32 columns x 8 row groups per
+// problem, the row groups summed in a fixed order
+__global__ void __launch_bounds__(256) rn_norms_kernel(const double* __restrict__ M, int N, int n,
+                                                       int cw, int64_t mstride,
+                                                       double* __restrict__ nrm2) {
   const int b = blockIdx.y;
   const double* Mb = M + (int64_t)b * mstride;
   const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
@@ -1029,25 +1035,89 @@ __global__ void __launch_bounds__(256) rn_flag_kernel(const double* __restrict__
   if (ty == 0 && j < n) {
     double t = 0.0;
     for (int r = 0; r < 8; ++r) t += part[r][tx];
-    if (t > thr2) {
-      const int k = atomicAdd(&count[b], 1);
-      if (k < RN_MAX) list[b * RN_MAX + k] = j;
-    }
+    nrm2[(int64_t)b * n + j] = t;
   }
 }
 
-// sums of squares of the listed columns (FP32 per thread over a few hundred
-// rows, FP64 across threads)
-__global__ void __launch_bounds__(256) rn_sumsq_kernel(const float* __restrict__ U, int64_t m,
-                                                       int64_t ldu, int cw, int64_t ustride,
-                                                       const int* __restrict__ list,
-                                                       const int* __restrict__ count,
-                                                       double* __restrict__ sums) {
+// one warp per problem: the columns with nrm2 > thr2, at most RN_MAX of them
+// (the longest, ties to the lower index), listed in increasing column order
+__global__ void __launch_bounds__(32) rn_select_kernel(const double* __restrict__ nrm2, int n,
+                                                       double thr2, int* __restrict__ list,
+                                                       int* __restrict__ count) {
+  const int b = blockIdx.x;
+  const int lane = threadIdx.x;
+  const double* v = nrm2 + (int64_t)b * n;
+  int total = 0;
+  for (int j0 = 0; j0 < n; j0 += 32) {
+    const int j = j0 + lane;
+    total += __popc(__ballot_sync(0xffffffffu, j < n && v[j] > thr2));
+  }
+  int* out = list + b * RN_MAX;
+  if (total <= RN_MAX) {
+    int c = 0;
+    for (int j0 = 0; j0 < n; j0 += 32) {
+      const int j = j0 + lane;
+      const bool f = j < n && v[j] > thr2;
+      const unsigned bal = __ballot_sync(0xffffffffu, f);
+      if (f) out[c + __popc(bal & ((1u << lane) - 1u))] = j;
+      c += __popc(bal);
+    }
+    if (lane == 0) count[b] = total;
+    return;
+  }
+  // more candidates than slots: RN_MAX rounds of a warp arg-max over the
+  // columns not yet taken (value above the previous pick's, or equal with a
+  // larger index), then the picks are sorted by index
+  double pv = INFINITY;
+  int pj = -1;
+  __shared__ int picks[RN_MAX];
+  for (int r = 0; r < RN_MAX; ++r) {
+    double bv = -1.0;
+    int bj = n;
+    for (int j = lane; j < n; j += 32) {
+      const double x = v[j];
+      const bool avail = x > thr2 && (x < pv || (x == pv && j > pj));
+      if (avail && (x > bv || (x == bv && j < bj))) {
+        bv = x;
+        bj = j;
+      }
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+      const double ov = __shfl_xor_sync(0xffffffffu, bv, o);
+      const int oj = __shfl_xor_sync(0xffffffffu, bj, o);
+      if (ov > bv || (ov == bv && oj < bj)) {
+        bv = ov;
+        bj = oj;
+      }
+    }
+    pv = bv;
+    pj = bj;
+    if (lane == 0) picks[r] = bj;
+  }
+  __syncwarp();
+  if (lane < RN_MAX) {
+    const int mine = picks[lane];
+    int rank = 0;
+    for (int r = 0; r < RN_MAX; ++r) rank += picks[r] < mine;
+    out[rank] = mine;
+  }
+  if (lane == 0) count[b] = RN_MAX;
+}
+
+// per-block partial sums of squares of the listed columns (FP32 per thread
+// over a few hundred rows, FP64 across the block in a fixed order):
+// part[((b RN_MAX) + c) gx + blockIdx.x]
+__global__ void __launch_bounds__(RN_THREADS) rn_sumsq_kernel(const float* __restrict__ U,
+                                                              int64_t m, int64_t ldu, int cw,
+                                                              int64_t ustride,
+                                                              const int* __restrict__ list,
+                                                              const int* __restrict__ count,
+                                                              double* __restrict__ part) {
   const int b = blockIdx.y;
   const int d = min(count[b], RN_MAX);
   if (d == 0) return;
   const float* Ub = U + (int64_t)b * ustride;
-  __shared__ double red[RN_MAX][8];
+  __shared__ double red[RN_THREADS / 32];
   for (int c = 0; c < d; ++c) {
     const int64_t col = (int64_t)cw * list[b * RN_MAX + c];
     float acc = 0.f;
@@ -1060,28 +1130,40 @@ __global__ void __launch_bounds__(256) rn_sumsq_kernel(const float* __restrict__
         acc = fmaf(y, y, acc);
       }
     }
-    double v = (double)acc;
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-    if ((threadIdx.x & 31) == 0) red[c][threadIdx.x >> 5] = v;
-  }
-  __syncthreads();
-  if (threadIdx.x < d) {
-    double t = 0.0;
-    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += red[threadIdx.x][w];
-    atomicAdd(&sums[b * RN_MAX + threadIdx.x], t);
+    double s = warp_sum((double)acc);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double t = 0.0;
+      for (int w = 0; w < RN_THREADS / 32; ++w) t += red[w];
+      part[((int64_t)b * RN_MAX + c) * gridDim.x + blockIdx.x] = t;
+    }
+    __syncthreads();
   }
 }
 
-__global__ void __launch_bounds__(256) rn_scale_kernel(float* __restrict__ U, int64_t m,
-                                                       int64_t ldu, int cw, int64_t ustride,
-                                                       const int* __restrict__ list,
-                                                       const int* __restrict__ count,
-                                                       const double* __restrict__ sums) {
+// every block sums the partials of each listed column in block order (the
+// same fixed order in every block), then scales its rows of that column
+__global__ void __launch_bounds__(RN_THREADS) rn_scale_kernel(float* __restrict__ U, int64_t m,
+                                                              int64_t ldu, int cw, int64_t ustride,
+                                                              const int* __restrict__ list,
+                                                              const int* __restrict__ count,
+                                                              const double* __restrict__ part) {
   const int b = blockIdx.y;
   const int d = min(count[b], RN_MAX);
+  if (d == 0) return;
   float* Ub = U + (int64_t)b * ustride;
+  __shared__ double red[RN_THREADS / 32];
   for (int c = 0; c < d; ++c) {
-    const double s2 = sums[b * RN_MAX + c];
+    const double* pc = part + ((int64_t)b * RN_MAX + c) * gridDim.x;
+    double t = 0.0;
+    for (int k = threadIdx.x; k < (int)gridDim.x; k += blockDim.x) t += pc[k];
+    t = warp_sum(t);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = t;
+    __syncthreads();
+    double s2 = 0.0;
+    for (int w = 0; w < RN_THREADS / 32; ++w) s2 += red[w];
+    __syncthreads();
     if (!(s2 > 0.0)) continue;
     const float f = (float)(1.0 / sqrt(s2));
     const int64_t col = (int64_t)cw * list[b * RN_MAX + c];
@@ -1387,28 +1469,31 @@ namespace plom {
 // rank-deficient below the 22-bit operand precision (e.g. the null vector of
 // mean-removed snapshots) -- and the FP32 product loses that column's unit
 // norm (its orthogonality to the other columns stays at the operand level).
-// Such columns (up to 8 per problem, ||M e_j|| > 4) are renormalised in the
-// tall space: two strided passes over one column each.
+// Such columns (||M e_j|| > 4; the RN_MAX = 32 longest per problem) are
+// renormalised in the tall space: two strided passes over each column.  The
+// choice of columns and every sum are deterministic (see the kernels).
 int renorm_long_columns(const double* M, int N, int n, int cw, float* U, int64_t m, int64_t ldu,
                         int batch, int64_t mstride, int64_t ustride, Arena& ws, cudaStream_t st) {
+  const unsigned gx = (unsigned)std::max<int64_t>(
+      1, std::min<int64_t>(cdiv(m, hp::RN_THREADS), (int64_t)num_sms() * 4));
   int* list = ws.take<int>((size_t)batch * hp::RN_MAX);
   int* count = ws.take<int>((size_t)batch);
-  double* sums = ws.take<double>((size_t)batch * hp::RN_MAX);
+  double* nrm2 = ws.take<double>((size_t)batch * n);
+  double* part = ws.take<double>((size_t)batch * hp::RN_MAX * gx);
   if (ws.measuring()) return PLOM_OK;
   PLOM_REQUIRE(!ws.overflow(), PLOM_ERR_WORKSPACE, "renorm: workspace too small");
   PLOM_REQUIRE(M && U && batch >= 1 && batch <= 65535, PLOM_ERR_ARG, "renorm: bad arguments");
-  ProfScope prof("renorm_cols", st, 0.0, 8.0 * (double)m * batch, 3);
-  PLOM_CHECK_CUDA(cudaMemsetAsync(count, 0, sizeof(int) * batch, st));
-  PLOM_CHECK_CUDA(cudaMemsetAsync(sums, 0, sizeof(double) * batch * hp::RN_MAX, st));
-  hp::rn_flag_kernel<<<dim3((unsigned)cdiv(n, 32), (unsigned)batch), 256, 0, st>>>(
-      M, N, n, cw, mstride, 16.0, list, count);
+  ProfScope prof("renorm_cols", st, 0.0, 8.0 * (double)m * batch, 4);
+  hp::rn_norms_kernel<<<dim3((unsigned)cdiv(n, 32), (unsigned)batch), 256, 0, st>>>(M, N, n, cw,
+                                                                                   mstride, nrm2);
   PLOM_CHECK_LAUNCH();
-  const unsigned gx = (unsigned)std::max<int64_t>(1, std::min<int64_t>(cdiv(m, 256), (int64_t)num_sms() * 4));
-  hp::rn_sumsq_kernel<<<dim3(gx, (unsigned)batch), 256, 0, st>>>(U, m, ldu, cw, ustride, list, count,
-                                                                sums);
+  hp::rn_select_kernel<<<(unsigned)batch, 32, 0, st>>>(nrm2, n, 16.0, list, count);
   PLOM_CHECK_LAUNCH();
-  hp::rn_scale_kernel<<<dim3(gx, (unsigned)batch), 256, 0, st>>>(U, m, ldu, cw, ustride, list, count,
-                                                                sums);
+  hp::rn_sumsq_kernel<<<dim3(gx, (unsigned)batch), hp::RN_THREADS, 0, st>>>(U, m, ldu, cw, ustride,
+                                                                           list, count, part);
+  PLOM_CHECK_LAUNCH();
+  hp::rn_scale_kernel<<<dim3(gx, (unsigned)batch), hp::RN_THREADS, 0, st>>>(U, m, ldu, cw, ustride,
+                                                                           list, count, part);
   PLOM_CHECK_LAUNCH();
   return PLOM_OK;
 }

@@ -132,24 +132,43 @@ __global__ void nc_candidates_kernel(const double* __restrict__ S, int n, int* _
   *count = c;
 }
 
-// sums[q] += m_c^T G m_c over the 32 rows k of this block (c = list[q])
+// part[q gn + blockIdx.x] = sum over the 32 rows k of this block of
+// m_c[k] (G m_c)[k] (c = list[q]); the 8 warps' shares summed in a fixed order
 __global__ void __launch_bounds__(256) nc_norms_kernel(const double* __restrict__ G,
                                                        const double* __restrict__ Mf, int N,
                                                        const int* __restrict__ list,
                                                        const int* __restrict__ count,
-                                                       double* __restrict__ sums) {
+                                                       double* __restrict__ part) {
   const int q = blockIdx.y;
   if (q >= *count) return;
   const int c = list[q];
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
-  double part = 0.0;
+  __shared__ double red[8];
+  double mine = 0.0;
   for (int k = blockIdx.x * 32 + wib; k < min(N, (int)blockIdx.x * 32 + 32); k += 8) {
     double acc = 0.0;
     for (int l = lane; l < N; l += 32) acc = fma(G[(int64_t)k * N + l], Mf[(int64_t)l * N + c], acc);
     acc = warp_sum(acc);
-    part = fma(Mf[(int64_t)k * N + c], acc, part);
+    mine = fma(Mf[(int64_t)k * N + c], acc, mine);
   }
-  if (lane == 0) atomicAdd(&sums[q], part);
+  if (lane == 0) red[wib] = mine;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int w = 0; w < 8; ++w) t += red[w];
+    part[(int64_t)q * gridDim.x + blockIdx.x] = t;
+  }
+}
+
+// out[q] = sum of the g partials of candidate q, in a fixed order (one warp
+// per candidate)
+__global__ void __launch_bounds__(32 * NC_MAX) nc_sum_kernel(const double* __restrict__ part,
+                                                             int g, double* __restrict__ out) {
+  const int q = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  double t = 0.0;
+  for (int k = lane; k < g; k += 32) t += part[(int64_t)q * g + k];
+  t = warp_sum(t);
+  if (lane == 0) out[q] = t;
 }
 
 __device__ __forceinline__ int64_t nc_row(int q, int64_t m) {
@@ -157,15 +176,17 @@ __device__ __forceinline__ int64_t nc_row(int q, int64_t m) {
 }
 
 // u = e_i - U w, w = row i of U without the columns still to be completed
-// (this one included); written into column list[q], its squared norm summed
+// (this one included); written into column list[q], the block's share of its
+// squared norm into part[blockIdx.x] (warps summed in a fixed order)
 template <typename T>
 __global__ void __launch_bounds__(256) nc_project_kernel(T* __restrict__ U, int64_t m, int n,
                                                          int64_t ldu, const int* __restrict__ list,
                                                          const int* __restrict__ count,
                                                          const double* __restrict__ sums, int q,
-                                                         double* __restrict__ nrm2) {
+                                                         double* __restrict__ part) {
   if (q >= *count || !(sums[q] < 0.25)) return;
   extern __shared__ double ncw[];
+  __shared__ double red[8];
   const int64_t i = nc_row(q, m);
   const int c = list[q];
   for (int j = threadIdx.x; j < n; j += blockDim.x) ncw[j] = (double)U[i * ldu + j];
@@ -176,7 +197,7 @@ __global__ void __launch_bounds__(256) nc_project_kernel(T* __restrict__ U, int6
   }
   __syncthreads();
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
-  double part = 0.0;
+  double mine = 0.0;
   for (int64_t r = (int64_t)blockIdx.x * 8 + wib; r < m; r += (int64_t)gridDim.x * 8) {
     const T* row = U + r * ldu;
     double acc = 0.0;
@@ -185,22 +206,38 @@ __global__ void __launch_bounds__(256) nc_project_kernel(T* __restrict__ U, int6
     const double u = (r == i ? 1.0 : 0.0) - acc;
     if (lane == 0) {
       U[r * ldu + c] = (T)u;
-      part = fma(u, u, part);
+      mine = fma(u, u, mine);
     }
   }
-  __syncwarp();
-  if (lane == 0) atomicAdd(&nrm2[q], part);
+  if (lane == 0) red[wib] = mine;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int w = 0; w < 8; ++w) t += red[w];
+    part[blockIdx.x] = t;
+  }
 }
 
+// every block sums the gp partials of the projection in a fixed order, then
+// scales its rows of the completed column to unit norm
 template <typename T>
 __global__ void __launch_bounds__(256) nc_scale_kernel(T* __restrict__ U, int64_t m, int64_t ldu,
                                                        const int* __restrict__ list,
                                                        const int* __restrict__ count,
                                                        const double* __restrict__ sums, int q,
-                                                       const double* __restrict__ nrm2) {
-  if (q >= *count || !(sums[q] < 0.25) || !(nrm2[q] > 0.0)) return;
+                                                       const double* __restrict__ part, int gp) {
+  if (q >= *count || !(sums[q] < 0.25)) return;
+  __shared__ double red[8];
+  double t = 0.0;
+  for (int k = threadIdx.x; k < gp; k += blockDim.x) t += part[k];
+  t = warp_sum(t);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = t;
+  __syncthreads();
+  double nrm2 = 0.0;
+  for (int w = 0; w < 8; ++w) nrm2 += red[w];
+  if (!(nrm2 > 0.0)) return;
   const int c = list[q];
-  const double f = 1.0 / sqrt(nrm2[q]);
+  const double f = 1.0 / sqrt(nrm2);
   for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < m;
        r += (int64_t)gridDim.x * blockDim.x)
     U[r * ldu + c] = (T)((double)U[r * ldu + c] * f);
@@ -209,29 +246,30 @@ __global__ void __launch_bounds__(256) nc_scale_kernel(T* __restrict__ U, int64_
 template <typename T>
 int complete_null_columns(const double* S, int n, T* U, int64_t m, int64_t ldu, const double* G,
                           const double* Mf, Arena& ws, cudaStream_t st) {
+  const unsigned gn = (unsigned)std::max<int64_t>(1, cdiv(n, 32));
+  const unsigned gp = (unsigned)std::max<int64_t>(1, std::min<int64_t>(cdiv(m, 8), (int64_t)num_sms() * 8));
   int* list = ws.take<int>(NC_MAX);
   int* count = ws.take<int>(1);
   double* sums = ws.take<double>(NC_MAX);
-  double* nrm2 = ws.take<double>(NC_MAX);
+  double* npart = ws.take<double>((size_t)NC_MAX * gn);
+  double* ppart = ws.take<double>(gp);
   if (ws.measuring() || n < 1 || m < 1) return PLOM_OK;
   PLOM_REQUIRE(!ws.overflow(), PLOM_ERR_WORKSPACE, "null-column completion: workspace too small");
   PLOM_REQUIRE(S && U && G && Mf && n <= 8192, PLOM_ERR_ARG,
                "null-column completion: bad arguments");
-  ProfScope prof("null_cols", st, 0.0, (double)sizeof(T) * m, 2 + 2 * NC_MAX);
-  PLOM_CHECK_CUDA(cudaMemsetAsync(sums, 0, sizeof(double) * NC_MAX, st));
-  PLOM_CHECK_CUDA(cudaMemsetAsync(nrm2, 0, sizeof(double) * NC_MAX, st));
+  ProfScope prof("null_cols", st, 0.0, (double)sizeof(T) * m, 3 + 2 * NC_MAX);
   nc_candidates_kernel<<<1, 32, 0, st>>>(S, n, list, count);
   PLOM_CHECK_LAUNCH();
   const unsigned gx = (unsigned)std::max<int64_t>(1, std::min<int64_t>(cdiv(m, 256), (int64_t)num_sms() * 4));
-  nc_norms_kernel<<<dim3((unsigned)cdiv(n, 32), NC_MAX), 256, 0, st>>>(G, Mf, n, list, count,
-                                                                      sums);
+  nc_norms_kernel<<<dim3(gn, NC_MAX), 256, 0, st>>>(G, Mf, n, list, count, npart);
   PLOM_CHECK_LAUNCH();
-  const unsigned gp = (unsigned)std::max<int64_t>(1, std::min<int64_t>(cdiv(m, 8), (int64_t)num_sms() * 8));
+  nc_sum_kernel<<<1, 32 * NC_MAX, 0, st>>>(npart, (int)gn, sums);
+  PLOM_CHECK_LAUNCH();
   for (int q = 0; q < NC_MAX; ++q) {
     nc_project_kernel<T><<<gp, 256, sizeof(double) * n, st>>>(U, m, n, ldu, list, count, sums, q,
-                                                              nrm2);
+                                                              ppart);
     PLOM_CHECK_LAUNCH();
-    nc_scale_kernel<T><<<gx, 256, 0, st>>>(U, m, ldu, list, count, sums, q, nrm2);
+    nc_scale_kernel<T><<<gx, 256, 0, st>>>(U, m, ldu, list, count, sums, q, ppart, (int)gp);
     PLOM_CHECK_LAUNCH();
   }
   return PLOM_OK;
@@ -240,6 +278,148 @@ template int complete_null_columns<float>(const double*, int, float*, int64_t, i
                                           const double*, const double*, Arena&, cudaStream_t);
 template int complete_null_columns<double>(const double*, int, double*, int64_t, int64_t,
                                            const double*, const double*, Arena&, cudaStream_t);
+
+// ---------------------------------------------------------------------------
+// Householder QR's column signs for CholeskyQR factors.  CholeskyQR gives R a
+// positive diagonal; LAPACK's geqrf (the reference's qr, numpy.linalg.qr)
+// chooses each reflection to avoid cancellation, so its factors are
+// Q diag(s), diag(s) R for signs s that depend on the data.  s_k is minus the
+// sign of the k-th pivot of the LU factorization of Q's top n x n block
+// shifted by diag(s) as it is built (the sign rule of Householder
+// reconstruction: Ballard, Demmel, Grigori, Jacquelin, Knight, Nguyen,
+// J. Parallel Distrib. Comput. 85 (2015)); every shifted pivot is at least 1
+// in magnitude, so the elimination needs no pivoting and FP32 arithmetic
+// decides the signs.  For a square matrix LAPACK's last reflector is the
+// identity (dlarfg of a 1-vector), so the last sign is the pivot's own.
+// Right-looking, panels of HH_BW columns: one CTA eliminates a panel, a grid
+// updates the trailing block with it.
+// ---------------------------------------------------------------------------
+constexpr int HH_BW = 32;
+
+template <typename T>
+__global__ void hh_load_kernel(const T* __restrict__ Q, int64_t ldq, int n, float* __restrict__ A) {
+  const int64_t total = (int64_t)n * n;
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < total;
+       e += (int64_t)gridDim.x * blockDim.x)
+    A[e] = (float)Q[(e / n) * ldq + e % n];
+}
+
+// columns k0 .. k0+kb-1, rows k0 .. n-1 of A (n x n, ld n): pivot signs into
+// s, multipliers stored below the diagonal
+__global__ void __launch_bounds__(1024) hh_panel_kernel(float* __restrict__ A, int n, int k0,
+                                                        int kb, int square,
+                                                        double* __restrict__ s) {
+  for (int k = k0; k < k0 + kb; ++k) {
+    if (threadIdx.x == 0) {
+      const float p = A[(int64_t)k * n + k];
+      const bool last_sq = square && k == n - 1;
+      const float sk = (p >= 0.f) != last_sq ? -1.f : 1.f;
+      A[(int64_t)k * n + k] = p - sk;
+      s[k] = (double)sk;
+    }
+    __syncthreads();
+    const float piv = A[(int64_t)k * n + k];
+    for (int i = k + 1 + threadIdx.x; i < n; i += blockDim.x) {
+      float* Ai = A + (int64_t)i * n;
+      const float l = Ai[k] / piv;
+      Ai[k] = l;
+      for (int j = k + 1; j < k0 + kb; ++j) Ai[j] = fmaf(-l, A[(int64_t)k * n + j], Ai[j]);
+    }
+    __syncthreads();
+  }
+}
+
+// trailing update after panel k0 (kb columns): for a tile of 32 columns J and
+// 64 rows I past the panel, U12 = L11^-1 A[k0:k0+kb, J] (unit lower L11) and
+// A[I, J] -= L21[I, :] U12.  U12 is not written back: later panels never read
+// rows above them.
+__global__ void __launch_bounds__(256) hh_update_kernel(float* __restrict__ A, int n, int k0,
+                                                        int kb) {
+  __shared__ float L11[HH_BW][HH_BW + 1];
+  __shared__ float U12[HH_BW][33];
+  __shared__ float L21[64][HH_BW + 1];
+  const int c0 = k0 + kb + blockIdx.x * 32;
+  const int r0 = k0 + kb + blockIdx.y * 64;
+  const int tid = threadIdx.x;
+  for (int e = tid; e < HH_BW * HH_BW; e += blockDim.x) {
+    const int t = e / HH_BW, u = e % HH_BW;
+    L11[t][u] = (t < kb && u < kb) ? A[(int64_t)(k0 + t) * n + k0 + u] : 0.f;
+  }
+  for (int e = tid; e < HH_BW * 32; e += blockDim.x) {
+    const int t = e / 32, j = e % 32;
+    U12[t][j] = (t < kb && c0 + j < n) ? A[(int64_t)(k0 + t) * n + c0 + j] : 0.f;
+  }
+  for (int e = tid; e < 64 * HH_BW; e += blockDim.x) {
+    const int i = e / HH_BW, t = e % HH_BW;
+    L21[i][t] = (t < kb && r0 + i < n) ? A[(int64_t)(r0 + i) * n + k0 + t] : 0.f;
+  }
+  __syncthreads();
+  if (tid < 32) {
+    for (int t = 1; t < kb; ++t) {
+      float v = U12[t][tid];
+      for (int u = 0; u < t; ++u) v = fmaf(-L11[t][u], U12[u][tid], v);
+      U12[t][tid] = v;
+    }
+  }
+  __syncthreads();
+  const int j = tid & 31;
+  if (c0 + j >= n) return;
+  for (int i = tid >> 5; i < 64; i += 8) {
+    if (r0 + i >= n) break;
+    float acc = 0.f;
+    for (int t = 0; t < kb; ++t) acc = fmaf(L21[i][t], U12[t][j], acc);
+    float* a = A + (int64_t)(r0 + i) * n + c0 + j;
+    *a -= acc;
+  }
+}
+
+// W (n x n, ld n) <- W diag(s), R (n x n, ld n) <- diag(s) R
+__global__ void sign_fold_kernel(double* __restrict__ W, double* __restrict__ R,
+                                 const double* __restrict__ s, int n) {
+  const int64_t total = (int64_t)n * n;
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < total;
+       e += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i = e / n, j = e % n;
+    if (W) W[e] *= s[j];
+    if (R) R[e] *= s[i];
+  }
+}
+
+template <typename T>
+int householder_signs(const T* Qtop, int64_t ldq, int n, bool square, double* s, Arena& ws,
+                      cudaStream_t st) {
+  float* A = ws.take<float>((size_t)n * n);
+  if (ws.measuring()) return PLOM_OK;
+  PLOM_REQUIRE(!ws.overflow(), PLOM_ERR_WORKSPACE, "householder signs: workspace too small");
+  PLOM_REQUIRE(Qtop && s && n >= 1 && ldq >= n, PLOM_ERR_ARG, "householder signs: bad arguments");
+  ProfScope prof("hh_signs", st, 2.0 * n * (double)n * n / 3.0, 8.0 * n * (double)n,
+                 1 + 2 * (int)cdiv(n, HH_BW));
+  hh_load_kernel<T><<<grid1d((int64_t)n * n), 256, 0, st>>>(Qtop, ldq, n, A);
+  PLOM_CHECK_LAUNCH();
+  for (int k0 = 0; k0 < n; k0 += HH_BW) {
+    const int kb = std::min(HH_BW, n - k0);
+    hh_panel_kernel<<<1, 1024, 0, st>>>(A, n, k0, kb, square ? 1 : 0, s);
+    PLOM_CHECK_LAUNCH();
+    const int rest = n - k0 - kb;
+    if (rest > 0) {
+      hh_update_kernel<<<dim3((unsigned)cdiv(rest, 32), (unsigned)cdiv(rest, 64)), 256, 0, st>>>(
+          A, n, k0, kb);
+      PLOM_CHECK_LAUNCH();
+    }
+  }
+  return PLOM_OK;
+}
+template int householder_signs<float>(const float*, int64_t, int, bool, double*, Arena&,
+                                      cudaStream_t);
+template int householder_signs<double>(const double*, int64_t, int, bool, double*, Arena&,
+                                       cudaStream_t);
+
+int sign_fold(double* W, double* R, const double* s, int n, cudaStream_t st) {
+  if (n < 1) return PLOM_OK;
+  sign_fold_kernel<<<grid1d((int64_t)n * n), 256, 0, st>>>(W, R, s, n);
+  PLOM_CHECK_LAUNCH();
+  return PLOM_OK;
+}
 
 }  // namespace plom
 

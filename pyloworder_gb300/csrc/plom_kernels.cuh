@@ -101,4 +101,14 @@ template <typename T>
 int complete_null_columns(const double* S, int n, T* U, int64_t m, int64_t ldu, const double* G,
                           const double* Mf, Arena& ws, cudaStream_t st);
 
+// Householder QR's column signs s (n values, +-1) for CholeskyQR factors Q, R
+// (R with a positive diagonal), from Q's top n x n block (ld ldq; square:
+// Q has exactly n rows): the factors LAPACK's geqrf returns are Q diag(s)
+// and diag(s) R.
+template <typename T>
+int householder_signs(const T* Qtop, int64_t ldq, int n, bool square, double* s, Arena& ws,
+                      cudaStream_t st);
+// W <- W diag(s) and R <- diag(s) R (n x n FP64, ld n; either may be null)
+int sign_fold(double* W, double* R, const double* s, int n, cudaStream_t st);
+
 }  // namespace plom

@@ -484,15 +484,29 @@ static int tsqr_svd_batched_packed(bool cplx, const float* X, int64_t batch, int
   return PLOM_OK;
 }
 
+// Q = Q2 R3^-1 and R = R3 R2 R1.  hh: with Householder QR's column signs
+// (LAPACK geqrf's factors, which the reference's qr/tsqr return): the signs
+// come from the top n rows of Q, computed first, and are folded into R3^-1
+// and R before the full product, so Q is written once.  Needs m >= n.
 static int tsqr_packed(const float* X, int64_t m, int n, int64_t ldx, float* Q, int64_t ldq,
-                       float* R, int* info, Arena& ws, cudaStream_t st) {
+                       float* R, int* info, Arena& ws, cudaStream_t st, bool hh = false) {
   PackedCore b;
   carve_packed_core(ws, b, m, n, p1_fits(ldq, n), Q);
   if (!ws.measuring()) PLOM_REQUIRE(!ws.overflow(), PLOM_ERR_WORKSPACE, "tsqr: workspace too small");
   const size_t mark = ws.off;
   PLOM_TRY(cholqr3_packed(false, X, m, n, ldx, b, info, ws, st));
-  const size_t need = ws.off;
+  size_t need = ws.off;
   ws.off = mark;
+  if (hh) {
+    float* T = ws.take<float>((size_t)n * n);
+    double* sg = ws.take<double>(n);
+    Packed top = packed_rows_view(b.P2, 0, n, n, b.P2.scale);
+    PLOM_TRY(apply_packed(top, b.W3, n, n, T, n, nullptr, info, ws, st, 0, 0, true));
+    PLOM_TRY(householder_signs<float>(T, n, n, m == n, sg, ws, st));
+    if (!ws.measuring()) PLOM_TRY(sign_fold(b.W3, b.Re, sg, n, st));
+    need = std::max(need, ws.off);
+    ws.off = mark;
+  }
   PLOM_TRY(apply_packed(b.P2, b.W3, n, n, Q, ldq, nullptr, info, ws, st, 0, 0, true));
   if (!ws.measuring()) PLOM_TRY((convert<double, float>(b.Re, R, (int64_t)n * n, st)));
   ws.off = std::max(need, ws.off);
@@ -584,18 +598,27 @@ static int tsqr_svd_impl(int prec, bool cplx, const TI* X, int64_t m, int n, int
 
 template <typename TI, typename TC>
 static int tsqr_impl(int prec, const TI* X, int64_t m, int n, int64_t ldx, TI* Q, int64_t ldq,
-                     TI* R, int* info, Arena& ws, cudaStream_t st) {
+                     TI* R, int* info, Arena& ws, cudaStream_t st, bool hh = false) {
   if constexpr (std::is_same<TI, float>::value && std::is_same<TC, float>::value) {
     if (prec == PLOM_PREC_MIXED && packed_ok(m))
-      return tsqr_packed(X, m, n, ldx, Q, ldq, R, info, ws, st);
+      return tsqr_packed(X, m, n, ldx, Q, ldq, R, info, ws, st, hh);
   }
   CoreBufs<TI, TC> b;
   const bool q1_in_q = std::is_same<TI, TC>::value && ldq == n;
   carve_core<TI, TC>(ws, b, m, n, !q1_in_q);
+  TI* T = hh ? ws.take<TI>((size_t)n * n) : nullptr;
+  double* sg = hh ? ws.take<double>(n) : nullptr;
   if (!ws.measuring()) PLOM_REQUIRE(!ws.overflow(), PLOM_ERR_WORKSPACE, "tsqr: workspace too small");
   PLOM_TRY((cholqr3<TI, TC>(prec, false, X, m, n, ldx, q1_in_q ? (TC*)(void*)Q : nullptr, n, b,
                             info, ws, st)));
   size_t need = ws.off;
+  if (hh) {
+    // signs from the top n rows of Q (see tsqr_packed), folded into R3^-1 and R
+    PLOM_TRY((tall_apply<TC, TI>(prec, b.Q2, n, n, n, b.W3, n, T, n, info, ws, st, true)));
+    PLOM_TRY(householder_signs<TI>(T, n, n, m == n, sg, ws, st));
+    if (!ws.measuring()) PLOM_TRY(sign_fold(b.W3, b.Re, sg, n, st));
+    need = std::max(need, ws.off);
+  }
   PLOM_TRY((tall_apply<TC, TI>(prec, b.Q2, n, m, n, b.W3, n, Q, ldq, info, ws, st, true)));
   if (!ws.measuring()) PLOM_TRY((convert<double, TI>(b.Re, R, (int64_t)n * n, st)));
   ws.off = std::max(need, ws.off);
@@ -607,8 +630,12 @@ static int tsqr_impl(int prec, const TI* X, int64_t m, int n, int64_t ldx, TI* Q
 // ---------------------------------------------------------------------------
 // Mixed form on FP32 data: A is packed once; the passes over it (A Omega,
 // A^T Q, A Q2, Q^T A) run on the tensor cores from the packed planes.
+// Two modes: randomized_svd (U, S, VT) and, with `qr`, randomized_qr (Q m x r
+// with Householder QR's column signs into Qout (ldq), B = Q^T A r x n into
+// Bout).  omega_in (n x r, or null): the test matrix instead of Philox(seed).
 static int rsvd_packed(const float* A, int64_t m, int64_t n, int64_t lda, int r, int q,
-                       uint64_t seed, float* U, int64_t ldu, float* S, float* VT, int* info,
+                       uint64_t seed, const float* omega_in, bool qr, float* U, int64_t ldu,
+                       float* S, float* VT, float* Qout, int64_t ldq, float* Bout, int* info,
                        Arena& ws, cudaStream_t st) {
   Packed Ap, Qp;
   packed_carve(ws, Ap, m, n);
@@ -616,13 +643,14 @@ static int rsvd_packed(const float* A, int64_t m, int64_t n, int64_t lda, int r,
   float* omega = ws.take<float>((size_t)n * r);
   double* om64 = ws.take<double>((size_t)n * r);
   float* Y = ws.take<float>((size_t)m * r);
-  float* Qm = ws.take<float>((size_t)m * r);
+  float* Qm = qr ? Qout : ws.take<float>((size_t)m * r);
+  const int64_t ldqm = qr ? ldq : r;
   float* Rq = ws.take<float>((size_t)r * r);
   double* Q2 = ws.take<double>((size_t)n * r);  // A^T Q (n x r); the last one is B^T
-  double* Ub = ws.take<double>((size_t)n * r);
-  double* Sb = ws.take<double>(r);
-  double* VbH = ws.take<double>((size_t)r * r);
-  double* Ur = ws.take<double>((size_t)r * r);
+  double* Ub = qr ? nullptr : ws.take<double>((size_t)n * r);
+  double* Sb = qr ? nullptr : ws.take<double>(r);
+  double* VbH = qr ? nullptr : ws.take<double>((size_t)r * r);
+  double* Ur = qr ? nullptr : ws.take<double>((size_t)r * r);
   double* Vo = ws.take<double>((size_t)r * n);
   const size_t mark = ws.off;
   size_t need = mark;
@@ -636,19 +664,33 @@ static int rsvd_packed(const float* A, int64_t m, int64_t n, int64_t lda, int r,
   const bool meas = ws.measuring();
   if (!meas) {
     PLOM_REQUIRE(!ws.overflow(), PLOM_ERR_WORKSPACE, "randomized_svd: workspace too small");
-    PLOM_TRY(fill_uniform_dispatch(PLOM_F32, omega, n * r, seed, st));
-    PLOM_TRY((convert<float, double>(omega, om64, n * r, st)));
+    if (omega_in)
+      PLOM_TRY((convert<float, double>(omega_in, om64, n * r, st)));
+    else {
+      PLOM_TRY(fill_uniform_dispatch(PLOM_F32, omega, n * r, seed, st));
+      PLOM_TRY((convert<float, double>(omega, om64, n * r, st)));
+    }
   }
   PLOM_TRY(sub([&] { return pack_f32(A, lda, m, n, Ap, ws, st); }));
   // Y = A Omega
   PLOM_TRY(sub([&] { return apply_packed(Ap, om64, r, r, Y, r, nullptr, info, ws, st); }));
   for (int j = 0; j <= q; ++j) {
-    PLOM_TRY(sub([&] { return tsqr_packed(Y, m, r, r, Qm, r, Rq, info, ws, st); }));
-    PLOM_TRY(sub([&] { return pack_f32(Qm, r, m, r, Qp, ws, st); }));
+    // only the final range basis needs Householder QR's signs
+    const bool hh = qr && j == q;
+    PLOM_TRY(sub([&] { return tsqr_packed(Y, m, r, r, Qm, ldqm, Rq, info, ws, st, hh); }));
+    PLOM_TRY(sub([&] { return pack_f32(Qm, ldqm, m, r, Qp, ws, st); }));
     // Q2 = A^T Q (n x r); after the last iteration this is B^T = (Q^T A)^T
     PLOM_TRY(sub([&] { return tn_packed(Ap, Qp, Q2, r, info, ws, st); }));
     if (j == q) break;
     PLOM_TRY(sub([&] { return apply_packed(Ap, Q2, r, r, Y, r, nullptr, info, ws, st); }));
+  }
+  if (qr) {
+    if (!meas) {
+      PLOM_TRY(transpose_f64(Q2, Vo, n, r, 1, st));  // B (r x n) = (B^T)^T
+      PLOM_TRY((convert<double, float>(Vo, Bout, (int64_t)r * n, st)));
+    }
+    ws.off = need;
+    return PLOM_OK;
   }
   // svd(B) through the tall n x r matrix B^T: B^T = Ub Sb VbH -> B = Vb Sb Ub^T
   PLOM_TRY(sub([&]() {
@@ -669,11 +711,13 @@ static int rsvd_packed(const float* A, int64_t m, int64_t n, int64_t lda, int r,
 
 template <typename TI, typename TC>
 static int rsvd_impl(int prec, const TI* A, int64_t m, int64_t n, int64_t lda, int r, int q,
-                     uint64_t seed, TI* U, int64_t ldu, TI* S, TI* VT, int* info, Arena& ws,
+                     uint64_t seed, const TI* omega_in, bool qr, TI* U, int64_t ldu, TI* S,
+                     TI* VT, TI* Qout, int64_t ldq, TI* Bout, int* info, Arena& ws,
                      cudaStream_t st) {
   if constexpr (std::is_same<TI, float>::value && std::is_same<TC, float>::value) {
     if (prec == PLOM_PREC_MIXED && packed_ok(m))
-      return rsvd_packed(A, m, n, lda, r, q, seed, U, ldu, S, VT, info, ws, st);
+      return rsvd_packed(A, m, n, lda, r, q, seed, omega_in, qr, U, ldu, S, VT, Qout, ldq, Bout,
+                         info, ws, st);
   }
   TI* omega = ws.take<TI>((size_t)n * r);
   TC* omc = ws.take<TC>((size_t)n * r);
@@ -689,6 +733,7 @@ static int rsvd_impl(int prec, const TI* A, int64_t m, int64_t n, int64_t lda, i
   double* Ur = ws.take<double>((size_t)r * r);
   double* Vo = ws.take<double>((size_t)r * n);
   TC* Rq = ws.take<TC>((size_t)r * r);
+  (void)Rr;
   size_t mark = ws.off;
   size_t need = mark;
   auto sub = [&](auto&& fn) -> int {
@@ -701,8 +746,12 @@ static int rsvd_impl(int prec, const TI* A, int64_t m, int64_t n, int64_t lda, i
   const bool meas = ws.measuring();
   if (!meas) {
     PLOM_REQUIRE(!ws.overflow(), PLOM_ERR_WORKSPACE, "randomized_svd: workspace too small");
-    PLOM_TRY(fill_uniform_dispatch(sizeof(TI) == 8 ? PLOM_F64 : PLOM_F32, omega, n * r, seed, st));
-    PLOM_TRY((convert<TI, TC>(omega, omc, n * r, st)));
+    if (omega_in)
+      PLOM_TRY((convert<TI, TC>(omega_in, omc, n * r, st)));
+    else {
+      PLOM_TRY(fill_uniform_dispatch(sizeof(TI) == 8 ? PLOM_F64 : PLOM_F32, omega, n * r, seed, st));
+      PLOM_TRY((convert<TI, TC>(omega, omc, n * r, st)));
+    }
   }
   // Y = A Omega
   auto apply_small = [&](const TC* Bm, TC* C) -> int {  // C(m x r) = A(m x n) Bm(n x r)
@@ -712,7 +761,9 @@ static int rsvd_impl(int prec, const TI* A, int64_t m, int64_t n, int64_t lda, i
   };
   if (!meas) PLOM_TRY(apply_small(omc, Y));
   for (int j = 0; j <= q; ++j) {
-    PLOM_TRY(sub([&]() { return tsqr_impl<TC, TC>(prec, Y, m, r, r, Qm, r, Rq, info, ws, st); }));
+    // only the final range basis needs Householder QR's signs
+    const bool hh = qr && j == q;
+    PLOM_TRY(sub([&]() { return tsqr_impl<TC, TC>(prec, Y, m, r, r, Qm, r, Rq, info, ws, st, hh); }));
     if (j == q) break;
     // Q2 = A^T Q  (n x r), then Y = A Q2
     PLOM_TRY(sub([&]() {
@@ -728,6 +779,14 @@ static int rsvd_impl(int prec, const TI* A, int64_t m, int64_t n, int64_t lda, i
       return gemm_tn<TC, TI, double, double>(Qm, r, A, lda, B, n, r, n, m, false, ws, st);
     return gemm_tn<TC, TI, float, double>(Qm, r, A, lda, B, n, r, n, m, false, ws, st);
   }));
+  if (qr) {
+    if (!meas) {
+      PLOM_TRY((copy2d<TC, TI>(Qm, r, Qout, ldq, m, r, st)));
+      PLOM_TRY((convert<double, TI>(B, Bout, (int64_t)r * n, st)));
+    }
+    ws.off = need;
+    return PLOM_OK;
+  }
   // svd(B) through the tall n x r matrix B^T: B^T = Ub Sb VbH -> B = Vb Sb Ub^T
   if (!meas) PLOM_TRY(transpose_f64(B, Bt, r, n, 1, st));
   PLOM_TRY(sub([&]() {
@@ -1106,13 +1165,13 @@ static int tsqr_dispatch(int dtype, int prec, const void* X, int64_t m, int64_t 
   if (dtype == PLOM_F32) {
     if (prec == PLOM_PREC_FP64)
       return tsqr_impl<float, double>(prec, (const float*)X, m, (int)n, ldx, (float*)Q, ldq,
-                                      (float*)R, info, ws, st);
+                                      (float*)R, info, ws, st, true);
     return tsqr_impl<float, float>(prec, (const float*)X, m, (int)n, ldx, (float*)Q, ldq,
-                                   (float*)R, info, ws, st);
+                                   (float*)R, info, ws, st, true);
   }
   if (dtype == PLOM_F64)
     return tsqr_impl<double, double>(PLOM_PREC_FP64, (const double*)X, m, (int)n, ldx, (double*)Q,
-                                     ldq, (double*)R, info, ws, st);
+                                     ldq, (double*)R, info, ws, st, true);
   set_error("tsqr: dtype must be F32 or F64");
   return PLOM_ERR_UNSUPPORTED;
 }
@@ -1130,7 +1189,7 @@ extern "C" int plom_tsqr(int dtype, int prec, const void* X, int64_t m, int64_t 
                          void* Q, int64_t ldq, void* R, void* ws, size_t ws_bytes, int* info,
                          void* stream) {
   PLOM_REQUIRE(prec_ok(prec), PLOM_ERR_ARG, "bad precision %d", prec);
-  PLOM_REQUIRE(m >= 1 && n >= 1 && n <= 4096, PLOM_ERR_ARG, "tsqr: bad sizes");
+  PLOM_REQUIRE(n >= 1 && m >= n && n <= 4096, PLOM_ERR_ARG, "tsqr: need 1 <= n <= min(m, 4096)");
   PLOM_REQUIRE(ldx >= n && ldq >= n, PLOM_ERR_ARG, "tsqr: leading dimension < n");
   PLOM_REQUIRE(X && Q && R && info && ws, PLOM_ERR_ARG, "tsqr: null pointer");
   size_t need = plom_tsqr_workspace(dtype, prec, m, n);
@@ -1143,18 +1202,22 @@ extern "C" int plom_tsqr(int dtype, int prec, const void* X, int64_t m, int64_t 
 }
 
 static int rsvd_dispatch(int dtype, int prec, const void* X, int64_t m, int64_t n, int64_t ldx,
-                         int64_t r, int q, uint64_t seed, void* U, int64_t ldu, void* S, void* VT,
-                         int* info, Arena& ws, cudaStream_t st) {
+                         int64_t r, int q, uint64_t seed, const void* omega, bool qr, void* U,
+                         int64_t ldu, void* S, void* VT, void* Q, int64_t ldq, void* B, int* info,
+                         Arena& ws, cudaStream_t st) {
   if (dtype == PLOM_F32) {
     if (prec == PLOM_PREC_FP64)
       return rsvd_impl<float, double>(prec, (const float*)X, m, n, ldx, (int)r, q, seed,
-                                      (float*)U, ldu, (float*)S, (float*)VT, info, ws, st);
-    return rsvd_impl<float, float>(prec, (const float*)X, m, n, ldx, (int)r, q, seed, (float*)U,
-                                   ldu, (float*)S, (float*)VT, info, ws, st);
+                                      (const float*)omega, qr, (float*)U, ldu, (float*)S,
+                                      (float*)VT, (float*)Q, ldq, (float*)B, info, ws, st);
+    return rsvd_impl<float, float>(prec, (const float*)X, m, n, ldx, (int)r, q, seed,
+                                   (const float*)omega, qr, (float*)U, ldu, (float*)S, (float*)VT,
+                                   (float*)Q, ldq, (float*)B, info, ws, st);
   }
   if (dtype == PLOM_F64)
     return rsvd_impl<double, double>(PLOM_PREC_FP64, (const double*)X, m, n, ldx, (int)r, q, seed,
-                                     (double*)U, ldu, (double*)S, (double*)VT, info, ws, st);
+                                     (const double*)omega, qr, (double*)U, ldu, (double*)S,
+                                     (double*)VT, (double*)Q, ldq, (double*)B, info, ws, st);
   set_error("randomized_svd: dtype must be F32 or F64");
   return PLOM_ERR_UNSUPPORTED;
 }
@@ -1164,8 +1227,8 @@ extern "C" size_t plom_randomized_svd_workspace(int dtype, int prec, int64_t m, 
   size_t bytes = 0;
   int dummy[PLOM_INFO_WORDS];
   run_measured(&bytes, [&](Arena& a) {
-    return rsvd_dispatch(dtype, prec, nullptr, m, n, n, r, 1, 0, nullptr, r, nullptr, nullptr,
-                         dummy, a, 0);
+    return rsvd_dispatch(dtype, prec, nullptr, m, n, n, r, 1, 0, nullptr, false, nullptr, r,
+                         nullptr, nullptr, nullptr, r, nullptr, dummy, a, 0);
   });
   return bytes;
 }
@@ -1185,8 +1248,38 @@ extern "C" int plom_randomized_svd(int dtype, int prec, const void* X, int64_t m
                ws_bytes, need);
   Arena a(ws, ws_bytes);
   PLOM_CHECK_CUDA(cudaMemsetAsync(info, 0, sizeof(int) * PLOM_INFO_WORDS, (cudaStream_t)stream));
-  return rsvd_dispatch(dtype, prec, X, m, n, ldx, r, q, seed, U, ldu, S, VT, info, a,
-                       (cudaStream_t)stream);
+  return rsvd_dispatch(dtype, prec, X, m, n, ldx, r, q, seed, nullptr, false, U, ldu, S, VT,
+                       nullptr, r, nullptr, info, a, (cudaStream_t)stream);
+}
+
+extern "C" size_t plom_randomized_qr_workspace(int dtype, int prec, int64_t m, int64_t n,
+                                               int64_t r) {
+  size_t bytes = 0;
+  int dummy[PLOM_INFO_WORDS];
+  run_measured(&bytes, [&](Arena& a) {
+    return rsvd_dispatch(dtype, prec, nullptr, m, n, n, r, 1, 0, nullptr, true, nullptr, r,
+                         nullptr, nullptr, nullptr, r, nullptr, dummy, a, 0);
+  });
+  return bytes;
+}
+
+extern "C" int plom_randomized_qr(int dtype, int prec, const void* X, int64_t m, int64_t n,
+                                  int64_t ldx, int64_t r, int q, uint64_t seed, const void* omega,
+                                  void* Q, int64_t ldq, void* B, void* ws, size_t ws_bytes,
+                                  int* info, void* stream) {
+  PLOM_REQUIRE(prec_ok(prec), PLOM_ERR_ARG, "bad precision %d", prec);
+  PLOM_REQUIRE(m >= 1 && n >= 1 && r >= 1 && r <= n && r <= m && r <= 4096 && q >= 0,
+               PLOM_ERR_ARG, "randomized_qr: need 1 <= r <= min(m, n, 4096), q >= 0");
+  PLOM_REQUIRE(ldx >= n && ldq >= r, PLOM_ERR_ARG, "randomized_qr: leading dimension too small");
+  PLOM_REQUIRE(X && Q && B && info && ws, PLOM_ERR_ARG, "randomized_qr: null pointer");
+  size_t need = plom_randomized_qr_workspace(dtype, prec, m, n, r);
+  PLOM_REQUIRE(need > 0, PLOM_ERR_ARG, "randomized_qr: workspace query failed");
+  PLOM_REQUIRE(ws_bytes >= need, PLOM_ERR_WORKSPACE, "randomized_qr: workspace %zu < %zu",
+               ws_bytes, need);
+  Arena a(ws, ws_bytes);
+  PLOM_CHECK_CUDA(cudaMemsetAsync(info, 0, sizeof(int) * PLOM_INFO_WORDS, (cudaStream_t)stream));
+  return rsvd_dispatch(dtype, prec, X, m, n, ldx, r, q, seed, omega, true, nullptr, r, nullptr,
+                       nullptr, Q, ldq, B, info, a, (cudaStream_t)stream);
 }
 
 // ---------------------------------------------------------------------------

@@ -24,7 +24,7 @@ from . import _lib as L
 __all__ = [
     "temporal_mean", "subtract_mean", "temporal_variance", "norm_variance",
     "matmul", "matmulp", "vecmat", "transpose", "tsqr", "tsqr_svd", "randomized_svd",
-    "randomized_qr", "init_qr_streaming", "update_qr_streaming", "compute_truncation_residual",
+    "randomized_qr", "randomized_qr2", "qr", "svd", "init_qr_streaming", "update_qr_streaming", "compute_truncation_residual",
     "energy", "hammwin", "RMSE",
 ]
 
@@ -315,15 +315,14 @@ def svd(A, method="gesdd", *, precision=None):
     return tsqr_svd(A, precision=precision)
 
 
-def tsqr(Ai, *, precision=None):
-    """Q, R = tsqr(A): Q m x n orthonormal columns, R n x n upper triangular
-    (pyLOM/vmmath/svd.py:50)."""
+def tsqr_device(x, ld, precision=None):
+    """Q, R of a tall CUDA tensor (m >= n) with Householder QR's column signs."""
     t = L.torch()
-    cv = L.to_device(Ai)
-    x, ld = L.as_rows(cv.t)
     m, n = x.shape
     if x.dtype not in (t.float32, t.float64):
         raise TypeError("tsqr takes float32 or float64 data")
+    if m < n:
+        raise ValueError(f"tsqr needs m >= n, got {m} x {n}")
     dt = L.dtype_code(x)
     prec = L.precision_code(precision, x)
     Q = t.empty((m, n), dtype=x.dtype, device="cuda")
@@ -333,12 +332,33 @@ def tsqr(Ai, *, precision=None):
     L.call("plom_tsqr", dt, prec, L.ptr(x), m, n, ld, L.ptr(Q), n, L.ptr(R), L.ptr(ws), ws.numel(),
            L.ptr(info), L.stream_ptr())
     L.check_info(info, "tsqr")
+    return Q, R
+
+
+def tsqr(Ai, *, precision=None):
+    """Q, R = tsqr(A): Q m x n orthonormal columns, R n x n upper triangular
+    (pyLOM/vmmath/svd.py:50).  On one rank pyLOM's tsqr is LAPACK's
+    Householder QR (svd.py:58 then QW = I), and so are these factors: R's
+    diagonal carries Householder's signs (minus the sign of each pivot)."""
+    cv = L.to_device(Ai)
+    x, ld = L.as_rows(cv.t)
+    Q, R = tsqr_device(x, ld, precision)
     return cv.back(Q), cv.back(R)
 
 
 def qr(A, *, precision=None):
-    """pyLOM/vmmath/svd.py:29."""
-    return tsqr(A, precision=precision)
+    """Reduced QR of any shape, numpy.linalg.qr's factors (pyLOM/vmmath/
+    svd.py:29): m >= n -> Q m x n, R n x n; m < n -> Q m x m, R m x n
+    (the QR of the leading m x m block, R's trailing columns Q^T A)."""
+    cv = L.to_device(A)
+    x, ld = L.as_rows(cv.t)
+    m, n = x.shape
+    if m >= n:
+        Q, R = tsqr_device(x, ld, precision)
+        return cv.back(Q), cv.back(R)
+    Q, R1 = tsqr_device(x[:, :m], ld, precision)
+    R2 = _matmul_dev(Q, m, 1, x[:, m:], ld, m, n - m, m, precision)
+    return cv.back(Q), cv.back(L.torch().cat([R1, R2], dim=1))
 
 
 def randomized_svd_device(x, ld, r, q, seed, precision=None):
@@ -371,14 +391,52 @@ def randomized_svd(Ai, r, q, seed=-1, *, precision=None):
     return cv.back(U), cv.back(S), cv.back(V)
 
 
-def randomized_qr(Ai, r, q, seed=-1, *, precision=None):
-    """Q (m x r), B = Q^T A (r x n) of the randomized range finder
-    (pyLOM/vmmath/svd.py:121), from the same device pipeline."""
-    U, S, V = randomized_svd(Ai, r, q, seed, precision=precision)
+def randomized_qr_device(x, ld, r, q, seed, omega=None, precision=None):
+    """Q (m x r), B = Q^T X (r x n) of the randomized range finder on a CUDA
+    tensor (plom_randomized_qr); omega: an n x r CUDA tensor of x's dtype or
+    None (Philox keyed by seed)."""
     t = L.torch()
-    if isinstance(U, t.Tensor):
-        return U, S.reshape(-1, 1) * V
-    return U, S.reshape(-1, 1) * V
+    m, n = x.shape
+    dt = L.dtype_code(x)
+    prec = L.precision_code(precision, x)
+    Q = t.empty((m, r), dtype=x.dtype, device="cuda")
+    B = t.empty((r, n), dtype=x.dtype, device="cuda")
+    if omega is not None:
+        omega = omega.to(device="cuda", dtype=x.dtype).contiguous()
+        if tuple(omega.shape) != (n, r):
+            raise ValueError(f"omega must be {n} x {r}, got {tuple(omega.shape)}")
+    ws = L.workspace(L.load().plom_randomized_qr_workspace(dt, prec, m, n, r))
+    info = L.new_info()
+    L.call("plom_randomized_qr", dt, prec, L.ptr(x), m, n, ld, r, q, seed & (2**64 - 1),
+           L.ptr(omega), L.ptr(Q), r, L.ptr(B), L.ptr(ws), ws.numel(), L.ptr(info),
+           L.stream_ptr())
+    L.check_info(info, "randomized_qr")
+    return Q, B
+
+
+def randomized_qr(Ai, r, q, seed=-1, *, omega=None, precision=None):
+    """Qi (m x r), B = Qi^T A (r x n) of the randomized range finder
+    (pyLOM/vmmath/svd.py:121-144): Omega uniform [0, 1) (n x r), Y = A Omega,
+    q times (Q = tsqr(Y); Y = A (A^T Q)), Q = tsqr(Y), B = Q^T A.  Q carries
+    Householder QR's column signs, as the reference's tsqr gives them.
+    Omega: the Philox4x32-10 stream keyed by ``seed`` (time-seeded when
+    seed < 0, as in pyLOM), or ``omega`` when given (e.g. the reference's own
+    numpy draw, for parity)."""
+    seed = int(time.time()) if seed < 0 else int(seed)
+    cv = L.to_device(Ai)
+    x, ld = L.as_rows(cv.t)
+    if x.dtype not in (L.torch().float32, L.torch().float64):
+        raise TypeError("randomized_qr takes float32 or float64 data")
+    om = None if omega is None else _device_like(omega, x.dtype)
+    Q, B = randomized_qr_device(x, ld, int(r), int(q), seed, om, precision)
+    return cv.back(Q), cv.back(B)
+
+
+def randomized_qr2(Ai, r, q, seed=-1, *, omega=None, precision=None):
+    """pyLOM/vmmath/svd.py:147-173: the same range finder as randomized_qr
+    (pyLOM runs its products on the host and only tsqr on the GPU; here every
+    step is on the GPU), the same factors."""
+    return randomized_qr(Ai, r, q, seed, omega=omega, precision=precision)
 
 
 # --------------------------------------------------------------------------
@@ -400,34 +458,12 @@ def _uniform_device(rows, cols, seed, dtype):
     return out
 
 
-def _householder_signs(Q):
-    """Signs s with Q diag(s) and diag(s) R the factors Householder QR (LAPACK
-    geqrf, m > n) returns for the matrix whose CholeskyQR factors (R with a
-    positive diagonal) are Q, R: s_k is minus the sign of the k-th pivot of
-    the LU of Q's top n x n block shifted by diag(s) -- the sign rule of
-    Householder reconstruction (Ballard, Demmel, Grigori, Jacquelin, Knight,
-    Nguyen, J. Parallel Distrib. Comput. 85, 2015), which is Householder's
-    own choice of the reflection that avoids cancellation.  Every pivot is
-    at least 1 in magnitude.  n x n work, on the host (n is the range size)."""
-    n = Q.shape[1]
-    Q1 = Q[:n, :n].double().cpu().numpy().copy()
-    s = np.empty(n)
-    for k in range(n):
-        s[k] = -1.0 if Q1[k, k] >= 0 else 1.0
-        Q1[k, k] -= s[k]
-        Q1[k + 1:, k] /= Q1[k, k]
-        Q1[k + 1:, k + 1:] -= np.outer(Q1[k + 1:, k], Q1[k, k + 1:])
-    return s
-
-
 def _tsqr_householder(Y, precision):
-    """tsqr of a tall device matrix with Householder QR's column signs, so
-    that sums of such factors across calls (the streaming update's Yo += Yn)
-    follow the reference."""
-    t = L.torch()
-    Q, R = tsqr(Y, precision=precision)
-    s = t.as_tensor(_householder_signs(Q), dtype=Q.dtype, device="cuda")
-    return Q * s, R * s[:, None]
+    """tsqr of a tall device matrix; its factors carry Householder QR's column
+    signs (computed on the device), so sums of such factors across calls (the
+    streaming update's Yo += Yn) follow the reference."""
+    Yr, ld = L.as_rows(Y)
+    return tsqr_device(Yr, ld, precision)
 
 
 def _pack_dev(x):

@@ -160,6 +160,35 @@ def main(refroot):
         U, S, V = pyLOM.math.tsqr_svd(A)
         np.savez_compressed(os.path.join(HERE, f"tsqr_svd_{tag}.npz"), A=A, U=U, S=S, V=V)
 
+    # qr (numpy.linalg.qr's Householder factors) and tsqr (one rank: the same
+    # factors), tall, square and wide; randomized_qr / randomized_qr2 with the
+    # Omega the reference draws (np.random.seed(seed); rand(n, r))
+    rq = np.random.default_rng(21)
+    cases = {"tall_f64": rq.standard_normal((300, 20)),
+             "tall_f32": rq.standard_normal((200, 12)).astype(np.float32),
+             "square_f64": rq.standard_normal((16, 16)),
+             "wide_f64": rq.standard_normal((12, 30))}
+    out = {}
+    for tag, A in cases.items():
+        Q, R = pyLOM.math.qr(A)
+        out[f"{tag}_A"], out[f"{tag}_Q"], out[f"{tag}_R"] = A, Q, R
+    for tag, A in [("tsqr_f64", rq.standard_normal((500, 30))),
+                   ("tsqr_f32", rq.standard_normal((400, 16)).astype(np.float32))]:
+        Q, R = pyLOM.math.tsqr(A)
+        out[f"{tag}_A"], out[f"{tag}_Q"], out[f"{tag}_R"] = A, Q, R
+    np.savez_compressed(os.path.join(HERE, "qr.npz"), **out)
+    out = {}
+    for tag, dt in [("f64", np.float64), ("f32", np.float32)]:
+        A = pod_field(16, 16, 48, 10, seed=1008, dtype=dt)
+        r, q, seed = 10, 2, 13
+        Q, B = pyLOM.math.randomized_qr(A, r, q, seed=seed)
+        Q2, B2 = pyLOM.math.randomized_qr2(A, r, q, seed=seed)
+        np.random.seed(seed=seed)
+        om = np.random.rand(A.shape[1], r).astype(A.dtype)
+        out.update({f"{tag}_A": A, f"{tag}_Q": Q, f"{tag}_B": B, f"{tag}_Q2": Q2, f"{tag}_B2": B2,
+                    f"{tag}_omega": om})
+    np.savez_compressed(os.path.join(HERE, "randomized_qr.npz"), r=10, q=2, seed=13, **out)
+
     # averaging
     X = pod_field(16, 16, 30, 5, seed=3)
     mean = pyLOM.math.temporal_mean(X)
@@ -241,4 +270,6 @@ def main(refroot):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if len(sys.argv) != 2:
+        sys.exit("usage: python tests/golden/make_golden.py <path to the pyLowOrder sources>")
+    main(sys.argv[1])

@@ -365,6 +365,97 @@ def test_tsqr(dtype):
     np.testing.assert_allclose(Q.astype(np.float64) @ R, X, atol=tol * 10 * np.abs(X).max())
 
 
+@pytest.mark.parametrize("tag", ["tall_f64", "tall_f32", "square_f64", "wide_f64", "tsqr_f64",
+                                 "tsqr_f32"])
+def test_qr_tsqr_reference_factors(golden, tag):
+    """qr / tsqr return the reference's own factors (LAPACK Householder QR,
+    pyLOM/vmmath/svd.py:29-36 and :50-118 on one rank), column by column with
+    no sign freedom: R's diagonal signs are Householder's, computed on the
+    device.  FP64 form 1e-10, mixed form (float32 data) 1e-5, both relative
+    to the largest entry."""
+    g = golden("qr")
+    A, Qr, Rr = g[f"{tag}_A"], g[f"{tag}_Q"], g[f"{tag}_R"]
+    Q, R = (P.math.tsqr if tag.startswith("tsqr") else P.math.qr)(A)
+    assert isinstance(Q, np.ndarray) and Q.dtype == A.dtype and Q.shape == Qr.shape
+    assert R.shape == Rr.shape
+    tol = 1e-5 if A.dtype == np.float32 else 1e-10
+    np.testing.assert_allclose(Q, Qr, rtol=0, atol=tol)
+    np.testing.assert_allclose(R, Rr, rtol=0, atol=tol * np.abs(Rr).max())
+
+
+@pytest.mark.parametrize("m,n", [(5000, 100), (3000, 300), (70, 70), (40000, 33)])
+@pytest.mark.parametrize("dtype", [np.float64, np.float32])
+def test_tsqr_householder_signs_multi_panel(m, n, dtype):
+    """The device sign rule past its first 32-column panel (n = 33 .. 300,
+    square included) gives numpy.linalg.qr's factors."""
+    rng = np.random.default_rng(m + n)
+    X = rng.standard_normal((m, n)).astype(dtype)
+    Q, R = P.math.tsqr(X)
+    Qr, Rr = O.qr(X.astype(np.float64))
+    tol = 1e-4 if dtype == np.float32 else 1e-10
+    assert np.array_equal(np.sign(np.diag(R)), np.sign(np.diag(Rr)))
+    np.testing.assert_allclose(Q, Qr, rtol=0, atol=tol)
+    np.testing.assert_allclose(R, Rr, rtol=0, atol=tol * np.abs(Rr).max())
+
+
+@pytest.mark.parametrize("tag", ["f64", "f32"])
+@pytest.mark.parametrize("fn", ["randomized_qr", "randomized_qr2"])
+def test_randomized_qr_reference_factors(golden, tag, fn):
+    """randomized_qr (pyLOM/vmmath/svd.py:121-144; randomized_qr2 at :147
+    computes the same factors) with the reference's own Omega returns its Q
+    (m x r, Householder signs) and B = Q^T A (r x n), column by column.  FP64:
+    1e-10.  float32 (mixed form): 1e-5 on the 9 signal columns; the 10th sits
+    on the noise floor (sigma_10 / sigma_11 = 1.03), where the reference's
+    own float32 result differs from an FP64 evaluation of the same steps by
+    1.3e-3, so it gets 5e-3."""
+    g = golden("randomized_qr")
+    r, q = int(g["r"]), int(g["q"])
+    A = g[f"{tag}_A"]
+    Q, B = getattr(P.math, fn)(A, r, q, omega=g[f"{tag}_omega"])
+    assert Q.shape == (A.shape[0], r) and B.shape == (r, A.shape[1]) and Q.dtype == A.dtype
+    Qr, Br = g[f"{tag}_Q"], g[f"{tag}_B"]
+    bmax = np.abs(Br).max()
+    if tag == "f64":
+        np.testing.assert_allclose(Q, Qr, rtol=0, atol=1e-10)
+        np.testing.assert_allclose(B, Br, rtol=0, atol=1e-10 * bmax)
+    else:
+        np.testing.assert_allclose(Q[:, :9], Qr[:, :9], rtol=0, atol=1e-5)
+        np.testing.assert_allclose(B[:9], Br[:9], rtol=0, atol=1e-5 * bmax)
+        np.testing.assert_allclose(Q[:, 9], Qr[:, 9], rtol=0, atol=5e-3)
+    # the seeded Philox draw matches the oracle on the same Omega
+    Qs, Bs = getattr(P.math, fn)(A, r, q, seed=77)
+    om = O.philox_uniform((A.shape[1], r), 77, A.dtype)
+    Qo, Bo = O.randomized_qr(A.astype(np.float64), r, q, omega=om.astype(np.float64))
+    k = 10 if tag == "f64" else 9
+    np.testing.assert_allclose(Qs[:, :k], Qo[:, :k], rtol=0, atol=1e-10 if tag == "f64" else 1e-5)
+
+
+@pytest.mark.parametrize("n", [1024, 1700])
+def test_mixed_repeated_calls_identical(n):
+    """The same mean-removed input three times: bitwise-identical sigma, U and
+    V.  The null direction of mean removal (sigma ~ 1e-8 sigma_1, below the
+    22-bit operand level) makes R3^-1 long in a few directions; the columns
+    renormalised for it are chosen by an ordered scan and every sum on that
+    path is taken in a fixed order, so no run differs from another.
+    ||I - U^T U|| is reported and held at the documented level: 1e-4 at
+    n = 1,024, 1e-3 at n = 1,700 (32,768 points, noise floor 5e-7 sigma_1)."""
+    from pyloworder_gb300 import datagen
+    m, k = 32768, 64
+    nx, ny = datagen.grid_for_points(m)
+    X = datagen.pod_field_device(nx, ny, n, k, seed=91, noise=1e-5, amp_pow=1.5, m=m)
+    Y, _, _ = P.vmmath.remove_mean_device(X, n)
+    runs = [P.vmmath.tsqr_svd_device(Y, n, "mixed") for _ in range(3)]
+    U0, S0, V0 = runs[0]
+    for U, S, V in runs[1:]:
+        assert torch.equal(S, S0)
+        assert torch.equal(U, U0)
+        assert torch.equal(V, V0)
+    Ud = U0.double()
+    orth = float((Ud.T @ Ud - torch.eye(n, dtype=torch.float64, device="cuda")).abs().max())
+    print(f"n = {n}: max |U^T U - I| = {orth:.2e}")
+    assert orth < (1e-4 if n <= 1600 else 1e-3)
+
+
 @pytest.mark.parametrize("m,n,ld", [(1, 1, 1), (5, 1, 1), (64, 64, 64), (1000, 33, 40),
                                     (2049, 129, 129), (300, 500, 500)])
 def test_tsqr_svd_shapes(m, n, ld):

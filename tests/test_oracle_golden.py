@@ -82,6 +82,41 @@ def test_randomized_numpy_omega(golden):
     _cols_match_up_to_sign(U, g["U"], 1e-8)
 
 
+@pytest.mark.parametrize("tag", ["tall_f64", "tall_f32", "square_f64", "wide_f64", "tsqr_f64",
+                                 "tsqr_f32"])
+def test_qr_and_tsqr(golden, tag):
+    """qr / tsqr reproduce the reference's Householder factors, signs
+    included; the sign rule applied to CholeskyQR-signed factors (positive
+    R diagonal) recovers them."""
+    g = golden("qr")
+    A, Qr, Rr = g[f"{tag}_A"], g[f"{tag}_Q"], g[f"{tag}_R"]
+    tol = 1e-5 if A.dtype == np.float32 else 1e-12
+    Q, R = (O.tsqr if tag.startswith("tsqr") else O.qr)(A)
+    np.testing.assert_allclose(Q, Qr, rtol=0, atol=tol)
+    np.testing.assert_allclose(R, Rr, rtol=0, atol=tol * np.abs(Rr).max())
+    if A.shape[0] >= A.shape[1]:
+        d = np.sign(np.diag(Rr))
+        Qc = Qr * d  # CholeskyQR's factor: R with a positive diagonal
+        s = O.householder_signs(Qc)
+        np.testing.assert_array_equal(s, d)
+
+
+@pytest.mark.parametrize("tag", ["f64", "f32"])
+def test_randomized_qr(golden, tag):
+    """randomized_qr with the reference's seed and with its Omega passed in;
+    randomized_qr2 returns the same factors."""
+    g = golden("randomized_qr")
+    r, q, seed = int(g["r"]), int(g["q"]), int(g["seed"])
+    A = g[f"{tag}_A"]
+    tol = 2e-4 if tag == "f32" else 1e-10
+    for kw in ({"seed": seed}, {"omega": g[f"{tag}_omega"]}):
+        Q, B = O.randomized_qr(A, r, q, **kw)
+        np.testing.assert_allclose(Q, g[f"{tag}_Q"], rtol=0, atol=tol)
+        np.testing.assert_allclose(B, g[f"{tag}_B"], rtol=0, atol=tol * np.abs(g[f"{tag}_B"]).max())
+    np.testing.assert_array_equal(g[f"{tag}_Q2"], g[f"{tag}_Q"])
+    np.testing.assert_array_equal(g[f"{tag}_B2"], g[f"{tag}_B"])
+
+
 def test_pca(golden):
     g = golden("pca")
     U, sc = O.pca_run(g["X"])
