@@ -41,7 +41,8 @@ M_FULL = 8_388_608
 N_FULL = 1024
 NMODES = 64
 SEED = 1002
-CPU_SAMPLE_ROWS = 131_072
+CPU_SAMPLE_ROWS = 65_536
+REF_SAMPLE_ROWS = 32_768
 FP64_SAMPLE_ROWS = 1_048_576
 
 
@@ -188,45 +189,82 @@ def max_over_ranks(x, world):
 
 
 # ---------------------------------------------------------------------------
-# CPU baseline (oracle port on the host cores, bounded sample)
+# CPU baseline: pyLOM's own compiled tsqr_svd (pyLOM/vmmath/src/svd.c, built
+# into oracle/_ref by oracle/build_ref.py) on the host cores, bounded sample;
+# the numpy restatement of the oracle only where that build is unavailable
 # ---------------------------------------------------------------------------
 
-def cpu_baseline(rows=CPU_SAMPLE_ROWS, reps=1):
-    from oracle import plom_oracle as O
+def _cpu_sample(rows):
     from pyloworder_gb300 import datagen
     nx, ny = datagen.grid_for_points(rows)
     X = datagen.pod_field_np(nx, ny, N_FULL, NMODES, seed=SEED, noise=1e-5, amp_pow=1.5,
-                             dtype=np.float32, distinct=True)
-    X = X - X.mean(axis=1, keepdims=True)
-    O.tsqr_svd(X[:4096])  # warm the BLAS threads
+                             dtype=np.float32, distinct=True)[:rows]
+    return np.ascontiguousarray(X - X.mean(axis=1, keepdims=True))
+
+
+def _reference_build():
+    """pyLOM's compiled path, built on this host if needed; (module, None) or
+    (None, reason)."""
+    try:
+        from oracle import build_ref, plom_ref
+        if not plom_ref.available():
+            build_ref.build()
+        plom_ref.load()
+        return plom_ref, None
+    except Exception as e:  # noqa: BLE001
+        return None, str(e).splitlines()[0][:200]
+
+
+def cpu_baseline(rows=CPU_SAMPLE_ROWS, reps=1, X=None):
+    cores = os.cpu_count()
+    X = _cpu_sample(rows) if X is None else X
+    R, why = _reference_build()
+    if R is not None:
+        R.set_threads(cores)
+        R.tsqr_svd(X[:4096])  # warm the BLAS threads
+        t0 = time.perf_counter()
+        for _ in range(reps):
+            R.tsqr_svd(X)
+        dt = (time.perf_counter() - t0) / reps
+        return {"value": algorithmic_bytes(rows, N_FULL) / dt / 1e9, "unit": "GB/s", "cores": cores,
+                "kind": "reference",
+                "sample": f"pyLOM's compiled stsqr_svd (pyLOM/vmmath/src/svd.c + vector_matrix.c, "
+                          f"LAPACKE/CBLAS on SciPy's bundled OpenBLAS) on {rows} x {N_FULL} FP32 rows "
+                          f"of the same field, mean removed; one process (no MPI on this host), "
+                          f"OpenBLAS threads = {cores}; {dt:.2f} s per call"}
+    from oracle import plom_oracle as O
+    O.tsqr_svd(X[:4096])
     t0 = time.perf_counter()
     for _ in range(reps):
         O.tsqr_svd(X)
     dt = (time.perf_counter() - t0) / reps
-    cores = os.cpu_count()
     return {"value": algorithmic_bytes(rows, N_FULL) / dt / 1e9, "unit": "GB/s", "cores": cores,
             "kind": "port",
-            "sample": f"oracle tsqr_svd (numpy/LAPACK, all {cores} host threads) on {rows} x {N_FULL} "
-                      f"FP32 rows of the same field, {dt:.2f} s per call"}
+            "sample": f"oracle tsqr_svd (numpy/LAPACK restatement, all {cores} host threads) on {rows} "
+                      f"x {N_FULL} FP32 rows of the same field, {dt:.2f} s per call; the compiled "
+                      f"reference was unavailable: {why}"}
 
 
 def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return 0
-    vals = []
+    rows = REF_SAMPLE_ROWS
+    X = _cpu_sample(rows)
     for _ in range(max(1, args.warmup)):
-        cpu_baseline(rows=CPU_SAMPLE_ROWS // 4)
-    for _ in range(args.steps):
-        vals.append(cpu_baseline(rows=CPU_SAMPLE_ROWS // 2))
+        cpu_baseline(rows=rows // 4, X=X[:rows // 4])
+    vals = [cpu_baseline(rows=rows, X=X) for _ in range(args.steps)]
     v = float(np.median([x["value"] for x in vals]))
-    ms = algorithmic_bytes(CPU_SAMPLE_ROWS // 2, N_FULL) / (v * 1e9) * 1e3
+    ms = algorithmic_bytes(rows, N_FULL) / (v * 1e9) * 1e3
     line = {"metric": "TSQR-SVD GB/s", "value": v, "unit": "GB/s", "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic", "impl": "reference",
-            "config": {"workload": f"tsqr_svd {M_FULL}x{N_FULL} f32 (sampled rows)",
-                       "sample_rows": CPU_SAMPLE_ROWS // 2},
+            "config": {"workload": f"tsqr_svd {M_FULL}x{N_FULL} f32 (POD config 2, mean removed; "
+                                   f"sampled rows)", "sample_rows": rows,
+                       "note": "the reference's C indexes with int, so m * n must stay below 2^31: "
+                               "the full 8,388,608 x 1,024 matrix is beyond it; the rate is per "
+                               "row-sample call"},
             "cpu_baseline": dict(vals[-1], value=v),
             "e2e": {"value": v, "unit": "GB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
@@ -369,6 +407,10 @@ def run_ours(args):
 
     hbm, bf16, how = peaks()
     cpu = cpu_baseline() if (rank == 0 and not args.quick and world == 1) else None
+    del Y
+    torch.cuda.synchronize()
+    torch.cuda.empty_cache()
+    others = side_legs() if (rank == 0 and not args.quick and world == 1) else None
     serve = serving_leg() if (rank == 0 and not args.quick) else None
     if rank == 0:
         roof = None
@@ -394,7 +436,8 @@ def run_ours(args):
                            "parallelism": "replicas" if world > 1 else "single"},
                 "clocks": clk.summary(), "gpu_launches": sum(k["launches"] for k in kernels.values()) if kernels else None,
                 "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "fp64_form": fp64,
-                "accuracy_vs_fp64": acc, "serving": serve, "kernels": kernels,
+                "accuracy_vs_fp64": acc, "serving": serve, "other_workloads": others,
+                "kernels": kernels,
                 "info": {"cholesky_shift_escalations": info_words[1] if info_words else None,
                          "jacobi_sweeps": info_words[2] if info_words else None,
                          "jacobi_fp32_sweeps": info_words[4] if info_words else None}}
@@ -410,30 +453,37 @@ def run_ours(args):
 # DMD (config 3), SPOD (config 4)
 # ---------------------------------------------------------------------------
 
-def run_other(args):
+def measure_workload(workload, steps, warmup, m=M_FULL):
+    """One of the other workloads (randomized SVD on the headline field, DMD,
+    SPOD, the streaming range finder): device-resident inputs, CUDA events
+    around `steps` calls after `warmup`, per-kernel timings, clocks, and the
+    algorithmic bytes and flops of the survey's definitions with the HBM
+    fraction of the call and of its dominant kernel."""
     import torch
     import pyloworder_gb300 as P
     from pyloworder_gb300 import _lib as L, datagen
     L.load()
     st = torch.cuda.current_stream()
-    out = {"n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "higher_is_better": True,
+    hbm, bf16, how = peaks()
+    out = {"n_gpus": 1, "steps": steps, "warmup": warmup, "higher_is_better": True,
            "scaling": "weak", "vs_baseline": None, "data": "synthetic", "dtype": "f32"}
-    if args.workload == "randomized":
-        m, n, r, q = args.m, N_FULL, 80, 2
+    if workload == "randomized":
+        m, n, r, q = m, N_FULL, 80, 2
         nx, ny = datagen.grid_for_points(m)
         X = datagen.pod_field_device(nx, ny, n, NMODES, seed=SEED, noise=1e-5, amp_pow=1.5, m=m)
         Y, _, _ = P.vmmath.remove_mean_device(X, n)
         del X
         step = lambda: P.vmmath.randomized_svd_device(Y, n, r, q, 7, "mixed")  # noqa: E731
         nbytes = 4 * m * n * (2 + 2 * q) + 4 * m * r
+        nflops = 2.0 * m * n * r * (2 + 2 * q)
         out.update(metric="randomized_svd GB/s", unit="GB/s",
                    config={"workload": f"randomized_svd {m}x{n} f32, r={r} (64+16), q={q}",
                            "precision": "mixed"})
-    elif args.workload == "streaming":
+    elif workload == "streaming":
         # the POD field of the headline workload arriving in 8 batches of 128
         # snapshots: init_qr_streaming on the first, update_qr_streaming on
         # the others (range r = 80, q = 2)
-        m, n, r, q, nb = args.m, N_FULL, 80, 2, 8
+        m, n, r, q, nb = m, N_FULL, 80, 2, 8
         nx, ny = datagen.grid_for_points(m)
         X = datagen.pod_field_device(nx, ny, n, NMODES, seed=SEED, noise=1e-5, amp_pow=1.5, m=m)
         Y, _, _ = P.vmmath.remove_mean_device(X, n)
@@ -448,26 +498,30 @@ def run_other(args):
             return Q, B, Yo
         # per batch: A Omega, q x (A^T Q, A O2), Q^T A and, in an update, Q2^T A
         nbytes = 4 * m * w * (2 + 2 * q + 1) * nb + 4 * m * r * (2 * nb)
+        nflops = 2.0 * m * w * r * (2 + 2 * q + 1) * nb
         out.update(metric="streaming QR GB/s", unit="GB/s",
                    config={"workload": f"init/update_qr_streaming {m}x{n} f32 in {nb} batches of {w} "
                                        f"snapshots, r={r}, q={q}", "precision": "mixed"})
-    elif args.workload == "dmd":
+    elif workload == "dmd":
         m, n, r = 2_097_152, 512, 32
         X, lam = datagen.dmd_field_device(m, n)
         step = lambda: P.DMD.run_device(X, n, r, remove_mean=False, precision="mixed")  # noqa: E731
+        # X read, TSQR-SVD of Y1 (read, write U), Phi (complex) written
         nbytes = 4 * m * n + 2 * 4 * m * (n - 1) + 8 * m * r
+        nflops = 4.0 * m * (n - 1) ** 2 + 2.0 * m * (n - 1) * r + 8.0 * m * (n - 1) * r
         out.update(metric="DMD GB/s", unit="GB/s",
                    config={"workload": f"DMD.run {m}x{n} f32, r={r}", "precision": "mixed"})
     else:
-        M, N = 1_048_576, 8192
+        M, N, nDFT, nB, nf = 1_048_576, 8192, 256, 63, 129
         X = datagen.spod_field_device(M, N)
         t = np.arange(N, dtype=np.float64)
-        step = lambda: P.SPOD.run_device(X, N, t, nDFT=256, nolap=128, precision="mixed")  # noqa: E731
-        nbytes = 4 * M * N + 4 * M * 63 * 129
+        step = lambda: P.SPOD.run_device(X, N, t, nDFT=nDFT, nolap=128, precision="mixed")  # noqa: E731
+        nbytes = 4 * M * N + 4 * M * nB * nf
+        nflops = nB * M * 2.5 * nDFT * np.log2(nDFT) + nf * (8.0 * M * nB ** 2 + 8.0 * M * nB ** 2)
         out.update(metric="SPOD GB/s", unit="GB/s",
-                   config={"workload": f"SPOD.run {M}x{N} f32, nDFT=256, nolap=128 (63 blocks, "
-                                       "129 frequencies), Hamming window", "precision": "mixed"})
-    for _ in range(args.warmup):
+                   config={"workload": f"SPOD.run {M}x{N} f32, nDFT={nDFT}, nolap=128 ({nB} blocks, "
+                                       f"{nf} frequencies), Hamming window", "precision": "mixed"})
+    for _ in range(warmup):
         res = step()
     torch.cuda.synchronize()
     prof = L.Profiler()
@@ -475,21 +529,53 @@ def run_other(args):
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     with ClockSampler(0) as clk:
         e0.record(st)
-        for _ in range(args.steps):
+        for _ in range(steps):
             res = step()
         e1.record(st)
         torch.cuda.synchronize()
-    ms = e0.elapsed_time(e1) / args.steps
+    ms = e0.elapsed_time(e1) / steps
     kernels = prof.stop()
-    out.update(value=nbytes / (ms * 1e-3) / 1e9, ms_per_step=ms, clocks=clk.summary(),
+    value = nbytes / (ms * 1e-3) / 1e9
+    top = max(kernels.values(), key=lambda k: k["ms_total"]) if kernels else None
+    roof = {"bound": "hbm", "achieved": value, "peak": hbm, "unit": "GB/s", "frac": value / hbm,
+            "peak_source": how, "algorithmic_bytes": nbytes, "algorithmic_flops": nflops,
+            "tensor_frac": nflops / (ms * 1e-3) / 1e12 / bf16,
+            "note": "call-level: algorithmic bytes / call time against the measured copy bandwidth"}
+    if top:
+        t_ms = top["ms_total"] / steps
+        roof["dominant_kernel"] = {"name": top["name"], "ms_per_call": t_ms,
+                                   "share": top["ms_total"] / (ms * steps),
+                                   "gbs": top["bytes"] / (top["ms_total"] * 1e-3) / 1e9,
+                                   "hbm_frac": top["bytes"] / (top["ms_total"] * 1e-3) / 1e9 / hbm,
+                                   "tflops": top["flops"] / (top["ms_total"] * 1e-3) / 1e12}
+    out.update(value=value, ms_per_step=ms, clocks=clk.summary(), roofline=roof,
                kernels=kernels, gpu_launches=sum(k["launches"] for k in kernels.values()))
-    if args.workload == "dmd":
+    if workload == "dmd":
         mu = (res[0].double() + 1j * res[1].double()).cpu().numpy()
         true = np.concatenate([lam, np.conj(lam)])
         out["max_abs_lambda_err"] = float(max(np.min(np.abs(mu - z)) for z in true))
-    if args.workload == "randomized":
+    if workload == "randomized":
         out["sigma_head"] = res[1][:4].double().cpu().numpy().tolist()
-    print(json.dumps(out), flush=True)
+    del res, step
+    torch.cuda.synchronize()
+    torch.cuda.empty_cache()
+    return out
+
+
+def side_legs(steps=3, warmup=2):
+    """The other configurations, each measured after the headline (outside
+    its timed region): randomized SVD on the headline field, DMD, SPOD."""
+    out = {}
+    for w in ("randomized", "dmd", "spod"):
+        try:
+            out[w] = measure_workload(w, steps, warmup)
+        except Exception as e:  # noqa: BLE001 - a failing side leg must not lose the headline
+            out[w] = {"error": str(e)[:300]}
+    return out
+
+
+def run_other(args):
+    print(json.dumps(measure_workload(args.workload, args.steps, args.warmup, args.m)), flush=True)
     return 0
 
 

@@ -264,9 +264,13 @@ int plom_packed_tn(const void* pa, int64_t Na, const void* pb, int64_t Nb, int64
    the process exits; larger results are rejected with PLOM_ERR_WORKSPACE
    before anything is launched.  The first call on each device looks up the
    array's device address (cudaGetSymbolAddress, with that device current):
-   make that first call before any stream capture.  All calls share the
-   array, so calls that overlap on the GPU race; serialise them (one stream,
-   or events).  Allocates nothing and calls no allocating routine. */
+   make that first call before any stream capture.  After a device reset
+   (cudaDeviceReset, or a reset of the primary context) the array lives at a
+   new address in the new context; the first call made in that context looks
+   it up again (the address is cached per device with the context's unique
+   ID), so that call, too, should come before any capture.  All calls share
+   the array, so calls that overlap on the GPU race; serialise them (one
+   stream, or events).  Allocates nothing and calls no allocating routine. */
 #define PLOM_STATIC_SCRATCH_BYTES (32u << 20)
 int plom_matmulp_static(int dtype, const void* A, int64_t lda, const void* B, int64_t ldb,
                         void* C, int64_t ldc, int64_t m, int64_t n, int64_t k, void* stream);

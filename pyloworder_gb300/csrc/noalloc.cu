@@ -8,9 +8,16 @@
 // The array is file-scope device memory of PLOM_STATIC_SCRATCH_BYTES; every
 // GPU that loads the library holds it until the process exits.  Host code
 // cannot use the array's name as a device address, so the device address is
-// looked up once per device with cudaGetSymbolAddress on the first call made
-// with that device current, and cached.  All calls share the array: calls
-// that overlap on the GPU (other streams, other host threads) race on it.
+// looked up with cudaGetSymbolAddress on the first call made with a device
+// current, and cached per device together with the unique ID of the context
+// it belongs to (cuCtxGetId).  A device reset (cudaDeviceReset, or a reset of
+// the primary context) ends that context; the library's module is loaded
+// again in the next one, so a call that finds a different context ID looks
+// the address up again instead of using the old one.  All calls share the
+// array: calls that overlap on the GPU (other streams, other host threads)
+// race on it.
+#include <cuda.h>
+
 #include <mutex>
 
 #include "plom_common.cuh"
@@ -21,17 +28,54 @@ static __device__ __align__(256) unsigned char g_plom_static_scratch[PLOM_STATIC
 namespace {
 constexpr int kMaxDevices = 128;
 std::mutex g_scratch_mutex;
-void* g_scratch_addr[kMaxDevices] = {};
+struct ScratchAddr {
+  void* ptr = nullptr;
+  unsigned long long ctx_id = 0;
+};
+ScratchAddr g_scratch_addr[kMaxDevices];
 
-// device address of the static scratch for the current device (set-up on the
-// first call per device)
+using CtxGetCurrentFn = CUresult (*)(CUcontext*);
+using CtxGetIdFn = CUresult (*)(CUcontext, unsigned long long*);
+
+// unique ID of the current context (0 when it cannot be read)
+unsigned long long current_ctx_id() {
+  static CtxGetCurrentFn get_current = nullptr;
+  static CtxGetIdFn get_id = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &p, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      get_current = reinterpret_cast<CtxGetCurrentFn>(p);
+    p = nullptr;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &p, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      get_id = reinterpret_cast<CtxGetIdFn>(p);
+  });
+  CUcontext ctx = nullptr;
+  unsigned long long id = 0;
+  if (get_current && get_id && get_current(&ctx) == CUDA_SUCCESS && ctx &&
+      get_id(ctx, &id) == CUDA_SUCCESS)
+    return id;
+  return 0;
+}
+
+// device address of the static scratch for the current device and context
+// (set-up on the first call per device, again after a device reset)
 int static_scratch(void** out) {
   int dev = 0;
   PLOM_CHECK_CUDA(cudaGetDevice(&dev));
   PLOM_REQUIRE(dev >= 0 && dev < kMaxDevices, PLOM_ERR_UNSUPPORTED, "device id %d out of range",
                dev);
+  // no context current on this thread yet reads as ID 0: the lookup below
+  // binds the device's primary context, whose ID is then recorded
+  const unsigned long long id = current_ctx_id();
   std::lock_guard<std::mutex> lock(g_scratch_mutex);
-  if (!g_scratch_addr[dev]) {
+  ScratchAddr& a = g_scratch_addr[dev];
+  if (!a.ptr || id == 0 || a.ctx_id != id) {
     void* p = nullptr;
     cudaError_t rc = cudaGetSymbolAddress(&p, g_plom_static_scratch);
     if (rc != cudaSuccess || p == nullptr) {
@@ -39,9 +83,10 @@ int static_scratch(void** out) {
                       cudaGetErrorString(rc));
       return PLOM_ERR_CUDA;
     }
-    g_scratch_addr[dev] = p;
+    a.ptr = p;
+    a.ctx_id = current_ctx_id();
   }
-  *out = g_scratch_addr[dev];
+  *out = a.ptr;
   return PLOM_OK;
 }
 }  // namespace
