@@ -42,7 +42,7 @@ N_FULL = 1024
 NMODES = 64
 SEED = 1002
 CPU_SAMPLE_ROWS = 65_536
-REF_SAMPLE_ROWS = 32_768
+REF_SAMPLE_ROWS = 65_536
 FP64_SAMPLE_ROWS = 1_048_576
 
 
@@ -252,7 +252,7 @@ def run_reference(args):
     rows = REF_SAMPLE_ROWS
     X = _cpu_sample(rows)
     for _ in range(max(1, args.warmup)):
-        cpu_baseline(rows=rows // 4, X=X[:rows // 4])
+        cpu_baseline(rows=rows // 16, X=X[:rows // 16])
     vals = [cpu_baseline(rows=rows, X=X) for _ in range(args.steps)]
     v = float(np.median([x["value"] for x in vals]))
     ms = algorithmic_bytes(rows, N_FULL) / (v * 1e9) * 1e3
