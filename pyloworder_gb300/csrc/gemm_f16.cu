@@ -153,6 +153,16 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&r)[32]) {
         "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
       : "r"(taddr));
 }
+// 32 lanes x 16 consecutive 32-bit columns
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t (&r)[16]) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 "
+      "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+        "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
+        "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr));
+}
 __device__ __forceinline__ void tmem_wait_ld() {
   asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 }
@@ -181,6 +191,20 @@ __device__ __forceinline__ uint64_t desc_sw128(uint32_t saddr, uint32_t lbo, uin
   d |= (uint64_t)((sbo >> 4) & 0x3FFFu) << 32;
   d |= (uint64_t)1 << 46;
   d |= (uint64_t)2 << 61;
+  return d;
+}
+// K-major tile of rows of `bk` fp16 (bk = 64: 128-byte rows, 128-byte swizzle;
+// bk = 32: 64-byte rows, 64-byte swizzle), 8-row core groups 8 * 2 bk bytes
+// apart (SBO); layout type 2 = SWIZZLE_128B, 4 = SWIZZLE_64B
+template <int BK>
+__device__ __forceinline__ uint64_t desc_kmajor(uint32_t saddr) {
+  static_assert(BK == 64 || BK == 32, "stage depth");
+  uint64_t d = 0;
+  d |= (uint64_t)((saddr >> 4) & 0x3FFFu);
+  d |= (uint64_t)1 << 16;  // LBO (unused for swizzled K-major tiles)
+  d |= (uint64_t)(((16u * BK) >> 4) & 0x3FFFu) << 32;
+  d |= (uint64_t)1 << 46;
+  d |= (uint64_t)(BK == 64 ? 2 : 4) << 61;
   return d;
 }
 // Instruction descriptor: kind::f16, D = F32, A = B = F16; a_mn/b_mn select
@@ -741,20 +765,375 @@ __global__ void gram16_reduce_kernel(const double* __restrict__ part, int N, int
 }
 
 // ---------------------------------------------------------------------------
-// apply: C (m x k) = Y W, persistent CTAs over 128 x 128 output tiles
+// wide gram: 128 x 256 tiles (one 128 x 256 x 16 UMMA per product), for
+// operands wider than 128 columns.  The 256-wide UMMA keeps the tensor pipe
+// busy through the stage ring (see ApplyCfg) and the A panel is received once
+// per 256 output columns instead of once per 128.  Stages of 32 rows (48 KiB,
+// four of them); the two accumulators (main 256 + correction 256 columns) fill
+// TMEM, so a sub-chunk's drain holds the next sub-chunk's products.
+// SYM tiles: for each 128-column block I of A and 256-column block J of B with
+// J + 256 > I (the tiles that meet the upper triangle); where I lies inside J
+// (the band tiles) A is the middle or first half of B and is not loaded, and
+// the Gram diagonal is summed on the CUDA cores as in gram16_kernel.
 // ---------------------------------------------------------------------------
-constexpr int A_BK = 64;                       // K per stage (one 128-byte row)
-constexpr uint32_t A_TILE = 128 * 128;         // 128 rows x 64 fp16 (16 KB)
-constexpr uint32_t A_STAGE = 4 * A_TILE;       // A hi, A lo, B hi, B lo
-constexpr int A_STAGES = 3;
+constexpr int GW_BK = 32;                      // rows per stage
+constexpr uint32_t GW_BOX = GW_BK * 128;       // GW_BK rows x 64 fp16
+constexpr uint32_t GW_STAGE = 12 * GW_BOX;     // A hi/lo (2 boxes each), B hi/lo (4 each)
+constexpr int GW_STAGES = 4;
+constexpr size_t GW_SMEM = (size_t)GW_STAGES * GW_STAGE + 1024;
+static_assert(G_KSUB % GW_BK == 0, "drain on stage boundaries");
+
+// SYM tile index -> (ti, tj): ti-major, tj from ti / 2 to tn2 - 1
+__host__ __device__ inline void gw_tile_sym(int tile, int tn2, int& ti, int& tj) {
+  int rem = tile, t = 0;
+  while (rem >= tn2 - (t >> 1)) {
+    rem -= tn2 - (t >> 1);
+    ++t;
+  }
+  ti = t;
+  tj = (t >> 1) + rem;
+}
+__host__ __device__ inline int gw_tiles_sym(int tn, int tn2) {
+  int c = 0;
+  for (int t = 0; t < tn; ++t) c += tn2 - (t >> 1);
+  return c;
+}
+
+template <bool SYM>
+__global__ void __launch_bounds__(320, 1)
+    gram16w_kernel(const __grid_constant__ CUtensorMap tmP, const __grid_constant__ CUtensorMap tmB,
+                   int64_t m, int tn, int tn2, int64_t rows_per_chunk, int chunks,
+                   double* __restrict__ part, int* err, int64_t mp) {
+  extern __shared__ uint8_t smem_raw[];
+  __shared__ uint64_t full_bar[GW_STAGES], empty_bar[GW_STAGES];
+  __shared__ uint64_t tfull, tempty, dfull[2];
+  __shared__ double diag_sh[2][2][128];  // [buffer][row half][column]
+  __shared__ uint32_t tmem_sh;
+  __shared__ int abort_sh;
+  const uint32_t base = (smem_u32(smem_raw) + 1023u) & ~1023u;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  // work item -> (problem, row chunk, tile): consecutive CTAs take different
+  // tiles of the same row chunk (L2 sharing of the panels)
+  const int ntiles = SYM ? gw_tiles_sym(tn, tn2) : tn * tn2;
+  const int per_problem = ntiles * chunks;
+  const int pb = (int)(blockIdx.x / per_problem);
+  const int rem_item = (int)(blockIdx.x % per_problem);
+  const int chunk = rem_item / ntiles, tile = rem_item % ntiles;
+  const int item = (pb * ntiles + tile) * chunks + chunk;  // partial slab index (tile-major)
+  int ti = 0, tj = 0;
+  if (SYM)
+    gw_tile_sym(tile, tn2, ti, tj);
+  else {
+    ti = tile / tn2;
+    tj = tile % tn2;
+  }
+  const int I0 = ti * 128, J0 = tj * 256;
+  const bool band = SYM && I0 >= J0 && I0 < J0 + 256;   // A = columns I0.. of the B tile
+  const uint32_t a_off = band ? (uint32_t)((I0 - J0) / 64) * GW_BOX : 0u;
+  const int dcol = I0 - J0;  // tile column of the Gram diagonal (band tiles)
+  const int64_t r_beg = (int64_t)chunk * rows_per_chunk;
+  const int64_t r_end = (r_beg + rows_per_chunk < m) ? r_beg + rows_per_chunk : m;
+  const int64_t nrows = (r_end > r_beg) ? r_end - r_beg : 0;
+  const int KB = (int)((nrows + GW_BK - 1) / GW_BK);
+  constexpr int KB_PER_SUB = G_KSUB / GW_BK;
+  const int nsub = (KB + KB_PER_SUB - 1) / KB_PER_SUB;
+  if (launch_aborted(err)) return;
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < GW_STAGES; ++s) {
+      mbar_init(&full_bar[s], 1);
+      mbar_init(&empty_bar[s], band ? 1 + 128 : 1);  // MMA commit (+ diagonal warps)
+    }
+    mbar_init(&tfull, 1);
+    mbar_init(&tempty, band ? 128 : 256);  // drain threads: 4 warps (band tiles) or 8
+    for (int b = 0; b < 2; ++b) mbar_init(&dfull[b], 128);
+    abort_sh = 0;
+    mbar_fence_init();
+  }
+  if (warp == 8) {
+    tmem_alloc(&tmem_sh, G_TMEM);
+    tmem_relinquish();
+  }
+  if (warp == 9 && lane == 0) {
+    tma_prefetch_map(&tmP);
+    if (!SYM) tma_prefetch_map(&tmB);
+  }
+  fence_before();
+  __syncthreads();
+  fence_after();
+  const uint32_t tmem = tmem_sh;
+  float2* P = reinterpret_cast<float2*>(part) + (int64_t)item * 128 * 256;
+  // stage layout: A hi (2 boxes), A lo (2), B hi (4), B lo (4)
+  constexpr uint32_t OFF_AL = 2 * GW_BOX, OFF_BH = 4 * GW_BOX, OFF_BL = 8 * GW_BOX;
+
+  if (warp == 9) {
+    // ---- TMA producer: GW_BK rows x (I block unless band, J block) of both planes
+    if (lane == 0) {
+      const uint32_t bytes = (band ? 8u : 12u) * GW_BOX;
+      const CUtensorMap* mb = SYM ? &tmP : &tmB;
+      for (int kb = 0; kb < KB; ++kb) {
+        const int s = kb % GW_STAGES;
+        const uint32_t ph = (uint32_t)(kb / GW_STAGES) & 1u;
+        if (!mbar_wait(&empty_bar[s], ph ^ 1u, &abort_sh, err)) break;
+        const uint32_t st = base + s * GW_STAGE;
+        const int y = (int)((int64_t)pb * mp + r_beg + (int64_t)kb * GW_BK);
+        mbar_expect_tx(&full_bar[s], bytes);
+#pragma unroll
+        for (int z = 0; z < 2; ++z) {
+          if (!band) {
+            tma_load_3d(st + z * OFF_AL, &tmP, I0, y, z, &full_bar[s]);
+            tma_load_3d(st + z * OFF_AL + GW_BOX, &tmP, I0 + 64, y, z, &full_bar[s]);
+          }
+#pragma unroll
+          for (int q = 0; q < 4; ++q)
+            tma_load_3d(st + OFF_BH + z * 4 * GW_BOX + q * GW_BOX, mb, J0 + 64 * q, y, z,
+                        &full_bar[s]);
+        }
+      }
+    }
+  } else if (warp >= 4 && warp < 8 && band) {
+    // ---- band tiles: compensated sums of (hi + lo)^2 of A's columns (as in
+    // gram16_kernel: two adjacent columns per thread, half of each stage's
+    // rows, four compensated chains)
+    {
+      const int t = threadIdx.x - 128;
+      const int c = 2 * (t & 63);                // first of the two columns of A
+      const int h = t >> 6;                      // row half of each stage
+      const uint32_t cb = OFF_BH + a_off + (uint32_t)(c >> 6) * GW_BOX;
+      const uint32_t w = (uint32_t)(c & 63);
+      const uint32_t ch = w >> 3, within = (w & 7u) * 2u;
+      const uint32_t k0 = (uint32_t)h * (GW_BK / 2), k1 = k0 + GW_BK / 2;
+      float sm[2][2] = {{0.f, 0.f}, {0.f, 0.f}}, cp[2][2] = {{0.f, 0.f}, {0.f, 0.f}};
+      for (int kb = 0; kb < KB; ++kb) {
+        const int s = kb % GW_STAGES;
+        const uint32_t ph = (uint32_t)(kb / GW_STAGES) & 1u;
+        if (!mbar_wait(&full_bar[s], ph, &abort_sh, err)) break;
+        const uint32_t st = base + s * GW_STAGE + cb;
+#pragma unroll 4
+        for (uint32_t k = k0; k < k1; k += 2) {
+#pragma unroll
+          for (uint32_t u = 0; u < 2; ++u) {
+            const uint32_t kk = k + u;
+            const uint32_t off = (kk >> 3) * 1024u + (kk & 7u) * 128u + (((ch ^ (kk & 7u)) << 4) | within);
+            const float2 hv = ld_shared_h2f(st + off);
+            const float2 lv = ld_shared_h2f(st + 4 * GW_BOX + off);  // B lo = B hi + 4 boxes
+            const float v[2] = {hv.x + lv.x, hv.y + lv.y};  // exact: 22 bits
+#pragma unroll
+            for (int q = 0; q < 2; ++q) {
+              const float y = fmaf(v[q], v[q], -cp[q][u]);
+              const float tt = sm[q][u] + y;
+              cp[q][u] = (tt - sm[q][u]) - y;
+              sm[q][u] = tt;
+            }
+          }
+        }
+        mbar_arrive(&empty_bar[s]);
+        if ((kb % KB_PER_SUB) == KB_PER_SUB - 1 || kb == KB - 1) {
+          const int b = (kb / KB_PER_SUB) & 1;
+#pragma unroll
+          for (int q = 0; q < 2; ++q) {
+            diag_sh[b][h][c + q] = ((double)sm[q][0] - (double)cp[q][0]) +
+                                   ((double)sm[q][1] - (double)cp[q][1]);
+            sm[q][0] = sm[q][1] = cp[q][0] = cp[q][1] = 0.f;
+          }
+          mbar_arrive(&dfull[b]);
+        }
+      }
+    }
+  } else if (warp == 8 && lane == 0) {
+    // ---- UMMA issuer: main += hi*hi, correction += hi*lo + lo*hi
+    constexpr uint32_t idesc = idesc_f16(128, 256, 1, 1);
+    bool ok = true;
+    int kb = 0;
+    for (int sub = 0; sub < nsub && ok; ++sub) {
+      if (!mbar_wait(&tempty, ((uint32_t)sub & 1u) ^ 1u, &abort_sh, err)) {
+        ok = false;
+        break;
+      }
+      fence_after();
+      const uint32_t dmain = tmem, dcorr = tmem + 256u;
+      const int kb_end = (kb + KB_PER_SUB < KB) ? kb + KB_PER_SUB : KB;
+      for (int kl = 0; kb < kb_end; ++kb, ++kl) {
+        const int s = kb % GW_STAGES;
+        const uint32_t ph = (uint32_t)(kb / GW_STAGES) & 1u;
+        if (!mbar_wait(&full_bar[s], ph, &abort_sh, err)) {
+          ok = false;
+          break;
+        }
+        fence_after();
+        const uint32_t st = base + s * GW_STAGE;
+        const uint32_t bH = st + OFF_BH, bL = st + OFF_BL;
+        const uint32_t aH = band ? bH + a_off : st, aL = band ? bL + a_off : st + OFF_AL;
+#pragma unroll
+        for (int kk = 0; kk < GW_BK / 16; ++kk) {
+          const uint32_t adv = (uint32_t)kk * 2048u;  // 16 rows of 128 bytes
+          const uint64_t dAH = desc_sw128(aH + adv, GW_BOX, 1024), dAL = desc_sw128(aL + adv, GW_BOX, 1024);
+          const uint64_t dBH = desc_sw128(bH + adv, GW_BOX, 1024), dBL = desc_sw128(bL + adv, GW_BOX, 1024);
+          const uint32_t first = (kl > 0 || kk > 0) ? 1u : 0u;
+          mma_f16(dmain, dAH, dBH, idesc, first);
+          mma_f16(dcorr, dAH, dBL, idesc, first);
+          mma_f16(dcorr, dAL, dBH, idesc, 1u);
+        }
+        mma_commit(&empty_bar[s]);
+      }
+      if (ok) mma_commit(&tfull);
+    }
+  } else if (warp < 8) {
+    // ---- epilogue: drain each finished sub-chunk into the double-float
+    // partial; warps 0-3 (TMEM lane quarters) take all 256 columns on band
+    // tiles, warps 0-7 take 128 columns each (half w / 4) elsewhere
+    const int rloc = (warp & 3) * 32 + lane;
+    const int cbeg = band ? 0 : (warp >> 2) * 128, ncc = band ? 8 : 4;
+    for (int sub = 0; sub < nsub; ++sub) {
+      const int b = sub & 1;
+      bool ready = mbar_wait(&tfull, (uint32_t)sub & 1u, &abort_sh, err);
+      if (band) ready = ready && mbar_wait(&dfull[b], ((uint32_t)sub >> 1) & 1u, &abort_sh, err);
+      __syncwarp();
+      if (!__all_sync(0xffffffffu, ready)) break;
+      fence_after();
+      const float2 dval =
+          band ? dw_from_double(diag_sh[b][0][rloc] + diag_sh[b][1][rloc]) : make_float2(0.f, 0.f);
+      const int dc = band ? dcol + rloc : -1;
+      float2* prow = P + (int64_t)rloc * 256;
+#pragma unroll 1
+      for (int c8 = 0; c8 < ncc; ++c8) {
+        const int cc = cbeg / 32 + c8;
+        uint32_t rm[32], rc[32];
+        const uint32_t ta = tmem + ((uint32_t)((warp & 3) * 32) << 16) + (uint32_t)(cc * 32);
+        tmem_ld32(ta, rm);
+        tmem_ld32(ta + 256, rc);
+        tmem_wait_ld();
+        float2* d = prow + cc * 32;
+#pragma unroll
+        for (int j = 0; j < 32; j += 2) {
+          float2 v0 = dw_two_sum(__uint_as_float(rm[j]), __uint_as_float(rc[j]));
+          float2 v1 = dw_two_sum(__uint_as_float(rm[j + 1]), __uint_as_float(rc[j + 1]));
+          if (cc * 32 + j == dc) v0 = dval;
+          if (cc * 32 + j + 1 == dc) v1 = dval;
+          float4* q = reinterpret_cast<float4*>(d + j);
+          if (sub == 0) {
+            *q = make_float4(v0.x, v0.y, v1.x, v1.y);
+          } else {
+            const float4 o = *q;
+            const float2 a0 = dw_add(make_float2(o.x, o.y), v0);
+            const float2 a1 = dw_add(make_float2(o.z, o.w), v1);
+            *q = make_float4(a0.x, a0.y, a1.x, a1.y);
+          }
+        }
+      }
+      fence_before();
+      mbar_arrive(&tempty);
+    }
+    if (nsub == 0) {  // empty chunk: the partial is zero
+      float2* prow = P + (int64_t)rloc * 256;
+      for (int j = cbeg; j < cbeg + 32 * ncc; ++j) prow[j] = make_float2(0.f, 0.f);
+    }
+  }
+  fence_before();
+  __syncthreads();
+  if (warp == 8) {
+    __syncwarp();
+    fence_after();
+    tmem_dealloc(tmem, G_TMEM);
+  }
+}
+
+// G[i][j] = sum over chunks of the 128 x 256 tile partials (fixed order) /
+// (s_i s_j), taken from the upper triangle (i <= j) and mirrored
+__global__ void gram16w_reduce_kernel(const double* __restrict__ part, int N, int tn, int tn2,
+                                      int chunks, const float* __restrict__ s,
+                                      double* __restrict__ G, int batch, int ld, int accumulate) {
+  const int64_t total = (int64_t)N * N * batch;
+  const int ntiles = gw_tiles_sym(tn, tn2);
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < total;
+       e += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t pb = e / ((int64_t)N * N);
+    const int64_t r = e - pb * N * N;
+    const int i = (int)(r / N), j = (int)(r % N);
+    const int a = min(i, j), b = max(i, j);
+    const int ti = a / 128, tj = b / 256;
+    int tile = 0;
+    for (int t = 0; t < ti; ++t) tile += tn2 - (t >> 1);
+    tile += tj - (ti >> 1);
+    const float2* p = reinterpret_cast<const float2*>(part) +
+                      ((pb * ntiles + tile) * chunks) * 128 * 256 + (int64_t)(a - ti * 128) * 256 +
+                      (b - tj * 256);
+    float2 acc = make_float2(0.f, 0.f);
+    for (int c = 0; c < chunks; ++c) acc = dw_add(acc, p[(int64_t)c * 128 * 256]);
+    const float* sp = s + pb * ld;
+    const double v = dw_value(acc) / ((double)sp[i] * (double)sp[j]);
+    G[e] = accumulate ? G[e] + v : v;
+  }
+}
+
+// C[i][j] (Na x Nb, ldc) = sum over chunks of the 128 x 256 tile partials / (sA_i sB_j)
+__global__ void tn16w_reduce_kernel(const double* __restrict__ part, int Na, int Nb, int tn2,
+                                    int chunks, const float* __restrict__ sa,
+                                    const float* __restrict__ sb, double* __restrict__ C,
+                                    int64_t ldc) {
+  const int64_t total = (int64_t)Na * Nb;
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < total;
+       e += (int64_t)gridDim.x * blockDim.x) {
+    const int i = (int)(e / Nb), j = (int)(e % Nb);
+    const int ti = i / 128, tj = j / 256;
+    const int tile = ti * tn2 + tj;
+    const float2* p = reinterpret_cast<const float2*>(part) + ((int64_t)tile * chunks) * 128 * 256 +
+                      (int64_t)(i - ti * 128) * 256 + (j - tj * 256);
+    float2 acc = make_float2(0.f, 0.f);
+    for (int c = 0; c < chunks; ++c) acc = dw_add(acc, p[(int64_t)c * 128 * 256]);
+    C[(int64_t)i * ldc + j] = dw_value(acc) / ((double)sa[i] * (double)sb[j]);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// apply: C (m x k) = Y W, persistent CTAs over 128 x TN output tiles.
+// TN = 256 (k > 128): one 128 x 256 x 16 UMMA per product.  A UMMA of N = 128
+// takes 64 cycles, too short for the per-stage barrier round trip of the
+// stage ring to hide (measured: a three-stage ring of 128 x 128 products runs
+// the tensor pipe at 0.80 of its rate, the same ring of 128 x 256 products at
+// 1.00), and a 256-wide tile also halves the A operand's share of the bytes
+// each SM must receive per product.  Its two accumulators fill TMEM (256 + 256
+// columns), so the epilogue of a tile does not overlap the next tile's
+// products; two 96 KiB stages.  TN = 128 (narrow k): three 64 KiB stages and
+// two accumulator buffers.
+// ---------------------------------------------------------------------------
+template <int TN>
+struct ApplyCfg {
+  // K per stage: 64 (128-byte rows, 128-byte swizzle) for TN = 128; 32 (64-byte
+  // rows, 64-byte swizzle) for TN = 256, so that four stages fit
+  static constexpr int BK = TN == 256 ? 32 : 64;
+  static constexpr uint32_t A_TILE = 128u * BK * 2;           // 128 rows x BK fp16
+  static constexpr uint32_t B_TILE = (uint32_t)TN * BK * 2;   // TN rows x BK fp16
+  static constexpr uint32_t STAGE = 2 * A_TILE + 2 * B_TILE;  // A hi, A lo, B hi, B lo
+  static constexpr int STAGES = TN == 256 ? 4 : 3;
+  static constexpr int NBUF = TN == 256 ? 1 : 2;   // TMEM accumulator buffers
+};
 // Warps: 0-7 epilogue (warp w drains TMEM lanes 32 (w % 4).. for the column
 // half w / 4 of the tile), 8 UMMA issuer (and TMEM owner), 9 TMA producer.
 // Eight epilogue warps keep short-K tiles (narrow problems, the first column
 // blocks of a triangular W) from being paced by the TMEM drain and stores.
-constexpr int A_EPI_WARPS = 8;
+// Eight epilogue warps (two per TMEM lane quarter); with TN = 256 each reads
+// its 128 columns out of TMEM into registers, releases the single accumulator
+// buffer and then stores them through its staging rows, so the stores overlap
+// the next tile's products.
+// TN = 256 epilogue: 1 = read the tile into registers and release TMEM before
+// the stores (the next tile's products overlap them), 0 = drain and store
+// 32 columns at a time, releasing TMEM at the end
+#ifndef PLOM_APPLY_HOLD
+#define PLOM_APPLY_HOLD 1
+#endif
+template <int TN>
+struct ApplyWarps {
+  static constexpr int EPI = 8;
+  static constexpr int THREADS = 32 * (EPI + 2);
+  static constexpr uint32_t STG = EPI * 4096u;  // staging: 32 rows x 128 bytes a warp
+};
+constexpr int A_EPI_WARPS = 8;                 // TN = 128
 constexpr int A_THREADS = 32 * (A_EPI_WARPS + 2);
-constexpr uint32_t A_STG = A_EPI_WARPS * 4096; // epilogue staging: 32 rows x 128 bytes per warp
-constexpr size_t A_SMEM = (size_t)A_STAGES * A_STAGE + A_STG + 1024;
+template <int TN>
+constexpr size_t apply_smem() {
+  return (size_t)ApplyCfg<TN>::STAGES * ApplyCfg<TN>::STAGE + ApplyWarps<TN>::STG + 1024;
+}
 
 struct ApplyOut {
   float* C;        // FP32 output (m x k, ldc) or nullptr
@@ -765,7 +1144,67 @@ struct ApplyOut {
   int ldo;
 };
 
-__global__ void __launch_bounds__(A_THREADS, 1)
+// one 32-column group of an apply tile (FP32 or packed output) through the
+// warp's staging rows: row r holds 8 chunks of 16 bytes, chunk q in slot
+// q ^ (r & 7); each row leaves as 128 contiguous bytes (fewer at the last
+// columns).  FP32 rows < m and columns < k; packed rows < mp (padding rows
+// get the zeros their zero input rows produce)
+__device__ __forceinline__ void apply_store_chunk(const float (&v)[32], int col0, uint4* stg,
+                                            int lane, const ApplyOut& out, int k, int64_t m,
+                                            int64_t mp, int64_t pb, int64_t row0,
+                                            bool c_vec) {
+
+  const bool staged = out.C ? (col0 < k) : (col0 < out.ldo);
+  if (!staged) return;
+  __syncwarp();
+  if (out.C) {
+#pragma unroll
+    for (int q = 0; q < 8; ++q)
+      stg[lane * 8 + (q ^ (lane & 7))] =
+          make_uint4(__float_as_uint(v[4 * q]), __float_as_uint(v[4 * q + 1]),
+                     __float_as_uint(v[4 * q + 2]), __float_as_uint(v[4 * q + 3]));
+  } else {
+#pragma unroll
+    for (int g = 0; g < 4; ++g) {
+      float w[8];
+#pragma unroll
+      for (int q = 0; q < 8; ++q) w[q] = v[8 * g + q];
+      uint4 h, l;
+      split8(w, h, l);
+      stg[lane * 8 + (g ^ (lane & 7))] = h;
+      stg[lane * 8 + ((4 + g) ^ (lane & 7))] = l;
+    }
+  }
+  __syncwarp();
+  const int q = lane & 7;
+#pragma unroll
+  for (int s8 = 0; s8 < 8; ++s8) {
+    const int rr = 4 * s8 + (lane >> 3);
+    const uint4 val = stg[rr * 8 + (q ^ (rr & 7))];
+    const int64_t r = row0 + rr;
+    if (out.C) {
+      const int c = col0 + 4 * q;
+      if (r < m && c < k) {
+        float* dst = out.C + pb * out.cstride + r * out.ldc + c;
+        if (c_vec && c + 4 <= k) {
+          *reinterpret_cast<uint4*>(dst) = val;
+        } else {
+          const float w4[4] = {__uint_as_float(val.x), __uint_as_float(val.y),
+                               __uint_as_float(val.z), __uint_as_float(val.w)};
+#pragma unroll
+          for (int e = 0; e < 4; ++e)
+            if (c + e < k) dst[e] = w4[e];
+        }
+      }
+    } else if (r < mp) {
+      __half* plane = q < 4 ? out.ohi : out.olo;
+      *reinterpret_cast<uint4*>(plane + (pb * mp + r) * out.ldo + col0 + 8 * (q & 3)) = val;
+    }
+  }
+}
+
+template <int TN>
+__global__ void __launch_bounds__(ApplyWarps<TN>::THREADS, 1)
     apply16_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
                    int64_t m, int kblocks, int k, int64_t col_tiles, int64_t tiles,
                    const float* __restrict__ f, ApplyOut out, int* err, int64_t mp,
@@ -773,14 +1212,18 @@ __global__ void __launch_bounds__(A_THREADS, 1)
   // tile t -> (problem pb, row block rb, column block cb); a problem's rows are
   // mp apart in the packed planes (input and packed output alike).  With an
   // upper-triangular W (upper != 0) column block cb needs only the first
-  // (cb + 1) 128 rows of W: the K blocks below 2 (cb + 1).
+  // (cb + 1) TN rows of W: the K blocks below (cb + 1) TN / 64.
   // by_rows: CTA x takes whole row blocks (every column tile of row blocks x,
   // x + G, ...), so the column tiles that re-read a row block's input follow
   // each other on one SM (L2 hits) and every CTA gets the same work per row
   // block.  Otherwise it takes single tiles, tile r G + x in even rounds r and
   // r G + (G - 1 - x) in odd ones.
+  constexpr int A_STAGES = ApplyCfg<TN>::STAGES, NBUF = ApplyCfg<TN>::NBUF, A_BK = ApplyCfg<TN>::BK;
+  constexpr uint32_t A_STAGE = ApplyCfg<TN>::STAGE, B_TILE = ApplyCfg<TN>::B_TILE;
+  constexpr uint32_t A_TILE = ApplyCfg<TN>::A_TILE;
+  constexpr int A_EPI_WARPS = ApplyWarps<TN>::EPI;
   extern __shared__ uint8_t smem_raw[];
-  __shared__ uint64_t full_bar[A_STAGES], empty_bar[A_STAGES], tfull[2], tempty[2];
+  __shared__ uint64_t full_bar[A_STAGES], empty_bar[A_STAGES], tfull[NBUF], tempty[NBUF];
   __shared__ uint32_t tmem_sh;
   __shared__ int abort_sh;
   const uint32_t base = (smem_u32(smem_raw) + 1023u) & ~1023u;
@@ -798,7 +1241,7 @@ __global__ void __launch_bounds__(A_THREADS, 1)
     return it * G + ((it & 1) ? G - 1 - blockIdx.x : (int64_t)blockIdx.x);
   };
   auto apply_kend = [&](int cb) -> int {
-    return upper ? min(kblocks, (cb + 1) * (128 / A_BK)) : kblocks;
+    return upper ? min(kblocks, (cb + 1) * (TN / A_BK)) : kblocks;
   };
   if (launch_aborted(err)) return;
 
@@ -807,7 +1250,7 @@ __global__ void __launch_bounds__(A_THREADS, 1)
       mbar_init(&full_bar[s], 1);
       mbar_init(&empty_bar[s], 1);
     }
-    for (int b = 0; b < 2; ++b) {
+    for (int b = 0; b < NBUF; ++b) {
       mbar_init(&tfull[b], 1);
       mbar_init(&tempty[b], 32 * A_EPI_WARPS);
     }
@@ -815,7 +1258,7 @@ __global__ void __launch_bounds__(A_THREADS, 1)
     mbar_fence_init();
   }
   if (warp == A_EPI_WARPS) {
-    tmem_alloc(&tmem_sh, 512);  // 2 buffers x (main 128 + correction 128)
+    tmem_alloc(&tmem_sh, 512);  // NBUF buffers x (main TN + correction TN)
     tmem_relinquish();
   }
   if (warp == A_EPI_WARPS + 1 && lane == 0) {
@@ -838,7 +1281,7 @@ __global__ void __launch_bounds__(A_THREADS, 1)
         const int64_t pb = t / (row_tiles * col_tiles);
         const int64_t rt = t - pb * row_tiles * col_tiles;
         const int rb = (int)(rt / col_tiles), cb = (int)(rt % col_tiles);
-        const int ya = (int)(pb * mp + (int64_t)rb * 128), yb = (int)(pb * k + (int64_t)cb * 128);
+        const int ya = (int)(pb * mp + (int64_t)rb * 128), yb = (int)(pb * k + (int64_t)cb * TN);
         const int kend = apply_kend(cb);
         for (int kb = 0; kb < kend; ++kb, ++g) {
           const int s = (int)(g % A_STAGES);
@@ -851,29 +1294,35 @@ __global__ void __launch_bounds__(A_THREADS, 1)
           mbar_expect_tx(&full_bar[s], A_STAGE);
           tma_load_3d(st, &tmA, kb * A_BK, ya, 0, &full_bar[s]);
           tma_load_3d(st + A_TILE, &tmA, kb * A_BK, ya, 1, &full_bar[s]);
-          tma_load_3d(st + 2 * A_TILE, &tmB, kb * A_BK, yb, 0, &full_bar[s]);
-          tma_load_3d(st + 3 * A_TILE, &tmB, kb * A_BK, yb, 1, &full_bar[s]);
+          // B: TN rows of the W copy in boxes of 128 rows (the K-major SW128
+          // layout of a 256-row tile is two 128-row tiles back to back)
+#pragma unroll
+          for (int h = 0; h < TN / 128; ++h) {
+            tma_load_3d(st + 2 * A_TILE + h * A_TILE, &tmB, kb * A_BK, yb + 128 * h, 0, &full_bar[s]);
+            tma_load_3d(st + 2 * A_TILE + B_TILE + h * A_TILE, &tmB, kb * A_BK, yb + 128 * h, 1,
+                        &full_bar[s]);
+          }
         }
       }
     }
   } else if (warp == A_EPI_WARPS) {
     // ---- UMMA issuer
     if (lane == 0) {
-      constexpr uint32_t idesc = idesc_f16(128, 128, 0, 0);
+      constexpr uint32_t idesc = idesc_f16(128, TN, 0, 0);
       int64_t g = 0;
       int i = 0;
       bool ok = true;
       for (int64_t it = 0; it < my_tiles && ok; ++it) {
         const int64_t t = apply_tile(it);
         if (t >= tiles) continue;
-        const int b = i & 1;
-        if (!mbar_wait(&tempty[b], (((uint32_t)i >> 1) & 1u) ^ 1u, &abort_sh, err)) {
+        const int b = i % NBUF;
+        if (!mbar_wait(&tempty[b], (((uint32_t)(i / NBUF)) & 1u) ^ 1u, &abort_sh, err)) {
           ok = false;
           break;
         }
         fence_after();
-        const uint32_t dmain = tmem + (uint32_t)(b * 256);
-        const uint32_t dcorr = dmain + 128u;
+        const uint32_t dmain = tmem + (uint32_t)(b * 2 * TN);
+        const uint32_t dcorr = dmain + (uint32_t)TN;
         const int kend = apply_kend((int)(t % col_tiles));
         for (int kb = 0; kb < kend; ++kb, ++g) {
           const int s = (int)(g % A_STAGES);
@@ -887,10 +1336,10 @@ __global__ void __launch_bounds__(A_THREADS, 1)
 #pragma unroll
           for (int kk = 0; kk < A_BK / 16; ++kk) {
             const uint32_t adv = (uint32_t)kk * 32u;  // 16 fp16 along K
-            const uint64_t dAH = desc_sw128(st + adv, 16, 1024);
-            const uint64_t dAL = desc_sw128(st + A_TILE + adv, 16, 1024);
-            const uint64_t dBH = desc_sw128(st + 2 * A_TILE + adv, 16, 1024);
-            const uint64_t dBL = desc_sw128(st + 3 * A_TILE + adv, 16, 1024);
+            const uint64_t dAH = desc_kmajor<A_BK>(st + adv);
+            const uint64_t dAL = desc_kmajor<A_BK>(st + A_TILE + adv);
+            const uint64_t dBH = desc_kmajor<A_BK>(st + 2 * A_TILE + adv);
+            const uint64_t dBL = desc_kmajor<A_BK>(st + 2 * A_TILE + B_TILE + adv);
             const uint32_t acc = (kb > 0 || kk > 0) ? 1u : 0u;
             mma_f16(dmain, dAH, dBH, idesc, acc);
             mma_f16(dcorr, dAH, dBL, idesc, acc);
@@ -911,8 +1360,8 @@ __global__ void __launch_bounds__(A_THREADS, 1)
     for (int64_t it = 0; it < my_tiles; ++it) {
       const int64_t t = apply_tile(it);
       if (t >= tiles) continue;
-      const int b = i & 1;
-      const bool ready = mbar_wait(&tfull[b], ((uint32_t)i >> 1) & 1u, &abort_sh, err);
+      const int b = i % NBUF;
+      const bool ready = mbar_wait(&tfull[b], ((uint32_t)(i / NBUF)) & 1u, &abort_sh, err);
       __syncwarp();
       if (!__all_sync(0xffffffffu, ready)) break;
       fence_after();
@@ -923,71 +1372,50 @@ __global__ void __launch_bounds__(A_THREADS, 1)
       const float* fp = f + pb * fstride;
       const bool c_vec = out.C && ((out.ldc & 3) == 0) && ((out.cstride & 3) == 0) &&
                          ((reinterpret_cast<uintptr_t>(out.C) & 15) == 0);
+      if constexpr (TN == 256 && PLOM_APPLY_HOLD) {
+        // one accumulator buffer: the warp's 128 columns are read out of TMEM
+        // into registers first and the buffer is released before the stores,
+        // so the next tile's products overlap them
+        float vv[4][32];
+#pragma unroll
+        for (int c4 = 0; c4 < 4; ++c4) {
+          const int col0 = (int)(cb * TN) + (4 * half + c4) * 32;
+#pragma unroll
+          for (int hh = 0; hh < 2; ++hh) {
+            uint32_t rm[16], rc[16];
+            const uint32_t ta = tmem + ((uint32_t)(quarter * 32) << 16) +
+                                (uint32_t)((4 * half + c4) * 32 + hh * 16);
+            tmem_ld16(ta, rm);
+            tmem_ld16(ta + TN, rc);
+            tmem_wait_ld();
+#pragma unroll
+            for (int j = 0; j < 16; ++j)
+              vv[c4][hh * 16 + j] = (__uint_as_float(rm[j]) + __uint_as_float(rc[j])) *
+                                    __ldg(fp + col0 + hh * 16 + j);
+          }
+        }
+        fence_before();
+        mbar_arrive(&tempty[b]);
+#pragma unroll
+        for (int c4 = 0; c4 < 4; ++c4)
+          apply_store_chunk(vv[c4], (int)(cb * TN) + (4 * half + c4) * 32, stg, lane, out, k, m, mp,
+                            pb, row0, c_vec);
+        ++i;
+        continue;
+      }
 #pragma unroll 1
-      for (int cc = 2 * half; cc < 2 * half + 2; ++cc) {
+      for (int cc = (TN / 64) * half; cc < (TN / 64) * (half + 1); ++cc) {
         uint32_t rm[32], rc[32];
-        const uint32_t ta = tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(b * 256 + cc * 32);
+        const uint32_t ta = tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(b * 2 * TN + cc * 32);
         tmem_ld32(ta, rm);
-        tmem_ld32(ta + 128, rc);
+        tmem_ld32(ta + TN, rc);
         tmem_wait_ld();
-        const int col0 = (int)(cb * 128) + cc * 32;
+        const int col0 = (int)(cb * TN) + cc * 32;
         float v[32];
 #pragma unroll
         for (int j = 0; j < 32; ++j)
           v[j] = (__uint_as_float(rm[j]) + __uint_as_float(rc[j])) * __ldg(fp + col0 + j);
-        // 32-column groups go through the warp's staging rows (row r: 8
-        // chunks of 16 bytes, chunk q in slot q ^ (r & 7)) and leave as 128
-        // contiguous bytes per row (fewer at the last columns); FP32 rows < m
-        // and columns < k, packed rows < mp (padding rows get the zeros their
-        // zero input rows produce)
-        const bool staged = out.C ? (col0 < k) : (col0 < out.ldo);
-        if (staged) {
-          __syncwarp();
-          if (out.C) {
-#pragma unroll
-            for (int q = 0; q < 8; ++q)
-              stg[lane * 8 + (q ^ (lane & 7))] =
-                  make_uint4(__float_as_uint(v[4 * q]), __float_as_uint(v[4 * q + 1]),
-                             __float_as_uint(v[4 * q + 2]), __float_as_uint(v[4 * q + 3]));
-          } else {
-#pragma unroll
-            for (int g = 0; g < 4; ++g) {
-              float w[8];
-#pragma unroll
-              for (int q = 0; q < 8; ++q) w[q] = v[8 * g + q];
-              uint4 h, l;
-              split8(w, h, l);
-              stg[lane * 8 + (g ^ (lane & 7))] = h;
-              stg[lane * 8 + ((4 + g) ^ (lane & 7))] = l;
-            }
-          }
-          __syncwarp();
-          const int q = lane & 7;
-#pragma unroll
-          for (int s8 = 0; s8 < 8; ++s8) {
-            const int rr = 4 * s8 + (lane >> 3);
-            const uint4 val = stg[rr * 8 + (q ^ (rr & 7))];
-            const int64_t r = row0 + rr;
-            if (out.C) {
-              const int c = col0 + 4 * q;
-              if (r < m && c < k) {
-                float* dst = out.C + pb * out.cstride + r * out.ldc + c;
-                if (c_vec && c + 4 <= k) {
-                  *reinterpret_cast<uint4*>(dst) = val;
-                } else {
-                  const float w4[4] = {__uint_as_float(val.x), __uint_as_float(val.y),
-                                       __uint_as_float(val.z), __uint_as_float(val.w)};
-#pragma unroll
-                  for (int e = 0; e < 4; ++e)
-                    if (c + e < k) dst[e] = w4[e];
-                }
-              }
-            } else if (r < mp) {
-              __half* plane = q < 4 ? out.ohi : out.olo;
-              *reinterpret_cast<uint4*>(plane + (pb * mp + r) * out.ldo + col0 + 8 * (q & 3)) = val;
-            }
-          }
-        }
+        apply_store_chunk(v, col0, stg, lane, out, k, m, mp, pb, row0, c_vec);
       }
       fence_before();
       mbar_arrive(&tempty[b]);
@@ -1200,7 +1628,7 @@ static PFN_cuTensorMapEncodeTiled_v12000 encode_fn16() {
 // lo plane (0: rows * ld, planes back to back)
 static bool make_map_planes(CUtensorMap* map, const __half* base, uint64_t inner, uint64_t rows,
                             uint64_t ld, uint32_t box_inner, uint32_t box_rows,
-                            uint64_t pstride = 0) {
+                            uint64_t pstride = 0, bool sw64 = false) {
   PFN_cuTensorMapEncodeTiled_v12000 fn = encode_fn16();
   if (!fn) return false;
   if (pstride == 0) pstride = ld * rows;
@@ -1210,7 +1638,8 @@ static bool make_map_planes(CUtensorMap* map, const __half* base, uint64_t inner
   cuuint32_t box[3] = {box_inner, box_rows, 1};
   cuuint32_t estr[3] = {1, 1, 1};
   CUresult r = fn(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 3, const_cast<__half*>(base), dims,
-                  strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                  strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                  sw64 ? CU_TENSOR_MAP_SWIZZLE_64B : CU_TENSOR_MAP_SWIZZLE_128B,
                   CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
   return r == CUDA_SUCCESS;
 }
@@ -1294,9 +1723,9 @@ int pack_f32(const float* Y, int64_t ld, int64_t m, int64_t N, Packed& p, Arena&
 // work items of the Gram: tiles x chunks, the fewest whole waves of the GPU
 // (one CTA per SM) that the tile count divides, with chunks of at least four
 // stages; fewer chunks keep the partial slabs (and their reduction) small
-static int gram16_chunks(int64_t m, int tiles) {
+static int gram16_chunks(int64_t m, int tiles, int bk = hp::G_BK) {
   const int64_t sms = num_sms();
-  const int64_t maxc = std::max<int64_t>(1, cdiv(m, 4 * hp::G_BK));
+  const int64_t maxc = std::max<int64_t>(1, cdiv(m, 4 * (int64_t)bk));
   for (int64_t waves = 1; waves <= 64; ++waves) {
     const int64_t items = waves * sms * PLOM_GRAM_WAVE_MULT;
     if (items % tiles) continue;
@@ -1305,8 +1734,52 @@ static int gram16_chunks(int64_t m, int tiles) {
   return (int)std::max<int64_t>(1, std::min<int64_t>(maxc, cdiv(2 * sms, tiles)));
 }
 
+// Gram of operands wider than 128 columns: 128 x 256 tiles (gram16w_kernel)
+static int gram_packed_wide(const Packed& p, double* G, int* err, Arena& ws, cudaStream_t st,
+                            bool accumulate) {
+  const int64_t m = p.m, N = p.N, batch = p.batch;
+  const int tn = (int)cdiv(p.ld, 128), tn2 = (int)cdiv(p.ld, 256);
+  const int tiles = hp::gw_tiles_sym(tn, tn2);
+  const int chunks = gram16_chunks(m, (int)std::min<int64_t>(tiles * batch, 1 << 20), hp::GW_BK);
+  int64_t rpc = cdiv(m, chunks);
+  rpc = cdiv(rpc, hp::GW_BK) * hp::GW_BK;  // chunk boundaries on stage boundaries
+  const int chunks_eff = (int)std::max<int64_t>(1, cdiv(m, rpc));
+  double* part = ws.take<double>((size_t)(batch * tiles * chunks_eff) * 128 * 256);
+  if (ws.measuring()) return PLOM_OK;
+  PLOM_REQUIRE(!ws.overflow(), PLOM_ERR_WORKSPACE, "gram16w: workspace too small");
+  PLOM_REQUIRE(p.hi && G && part && m >= 1 && batch * p.mp < (1ll << 31) &&
+                   batch * tiles * chunks_eff < (1ll << 31),
+               PLOM_ERR_ARG, "gram16w: bad arguments");
+  static bool attr = false;
+  if (!attr) {
+    PLOM_CHECK_CUDA(cudaFuncSetAttribute(hp::gram16w_kernel<true>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)hp::GW_SMEM));
+    PLOM_CHECK_CUDA(cudaFuncSetAttribute(hp::gram16w_kernel<false>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)hp::GW_SMEM));
+    attr = true;
+  }
+  CUtensorMap tm;
+  PLOM_REQUIRE(make_map_planes(&tm, p.hi, (uint64_t)p.ld, (uint64_t)(batch * p.mp),
+                               (uint64_t)p.ld, 64, hp::GW_BK, (uint64_t)p.pstride),
+               PLOM_ERR_CUDA, "gram16w: tensor map encoding failed");
+  ProfScope prof_g("tc_gram_f16x3", st, (double)m * N * N * batch, 4.0 * (double)m * p.ld * batch);
+  hp::gram16w_kernel<true><<<(unsigned)(batch * tiles * chunks_eff), 320, hp::GW_SMEM, st>>>(
+      tm, tm, m, tn, tn2, rpc, chunks_eff, part, err, p.mp);
+  PLOM_CHECK_LAUNCH();
+  const int64_t total = N * N * batch;
+  const int blocks = (int)std::min<int64_t>(cdiv(total, 256), (int64_t)num_sms() * 16);
+  ProfScope prof_r("gram_reduce", st, 0.0, 8.0 * (double)batch * tiles * chunks_eff * 128 * 256);
+  hp::gram16w_reduce_kernel<<<blocks, 256, 0, st>>>(part, (int)N, tn, tn2, chunks_eff, p.scale, G,
+                                                    (int)batch, (int)p.ld, accumulate ? 1 : 0);
+  PLOM_CHECK_LAUNCH();
+  return PLOM_OK;
+}
+
 int gram_packed(const Packed& p, double* G, int* err, Arena& ws, cudaStream_t st,
                 bool accumulate) {
+  if (p.ld > 128) return gram_packed_wide(p, G, err, ws, st, accumulate);
   const int64_t m = p.m, N = p.N, batch = p.batch;
   const int tn = (int)cdiv(p.ld, 128);
   const int tiles = tn * (tn + 1) / 2;
@@ -1347,8 +1820,53 @@ int gram_packed(const Packed& p, double* G, int* err, Arena& ws, cudaStream_t st
   return PLOM_OK;
 }
 
+// A^T B with B wider than 128 columns: 128 x 256 tiles (gram16w_kernel<false>)
+static int tn_packed_wide(const Packed& a, const Packed& b, double* C, int64_t ldc, int* err,
+                          Arena& ws, cudaStream_t st) {
+  const int64_t m = a.m;
+  const int tna = (int)cdiv(a.ld, 128), tn2 = (int)cdiv(b.ld, 256);
+  const int tiles = tna * tn2;
+  const int chunks = gram16_chunks(m, tiles, hp::GW_BK);
+  int64_t rpc = cdiv(m, chunks);
+  rpc = cdiv(rpc, hp::GW_BK) * hp::GW_BK;
+  const int chunks_eff = (int)std::max<int64_t>(1, cdiv(m, rpc));
+  double* part = ws.take<double>((size_t)tiles * chunks_eff * 128 * 256);
+  if (ws.measuring()) return PLOM_OK;
+  PLOM_REQUIRE(!ws.overflow(), PLOM_ERR_WORKSPACE, "tn16w: workspace too small");
+  PLOM_REQUIRE(a.hi && b.hi && C && part && m >= 1 && m < (1ll << 31) && b.m == m &&
+                   ldc >= b.N && a.batch == 1 && b.batch == 1,
+               PLOM_ERR_ARG, "tn16w: bad arguments");
+  static bool attr = false;
+  if (!attr) {
+    PLOM_CHECK_CUDA(cudaFuncSetAttribute(hp::gram16w_kernel<false>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)hp::GW_SMEM));
+    attr = true;
+  }
+  CUtensorMap ta, tb;
+  PLOM_REQUIRE(make_map_planes(&ta, a.hi, (uint64_t)a.ld, (uint64_t)m, (uint64_t)a.ld, 64,
+                               hp::GW_BK, (uint64_t)a.pstride) &&
+                   make_map_planes(&tb, b.hi, (uint64_t)b.ld, (uint64_t)m, (uint64_t)b.ld, 64,
+                                   hp::GW_BK, (uint64_t)b.pstride),
+               PLOM_ERR_CUDA, "tn16w: tensor map encoding failed");
+  {
+    ProfScope prof("tc_tn_f16x3", st, 2.0 * (double)m * a.N * b.N,
+                   4.0 * (double)m * (a.ld + b.ld));
+    hp::gram16w_kernel<false><<<tiles * chunks_eff, 320, hp::GW_SMEM, st>>>(
+        ta, tb, m, tna, tn2, rpc, chunks_eff, part, err, m);
+    PLOM_CHECK_LAUNCH();
+  }
+  const int64_t total = a.N * b.N;
+  const int blocks = (int)std::max<int64_t>(1, std::min<int64_t>(cdiv(total, 256), (int64_t)num_sms() * 16));
+  hp::tn16w_reduce_kernel<<<blocks, 256, 0, st>>>(part, (int)a.N, (int)b.N, tn2, chunks_eff,
+                                                  a.scale, b.scale, C, ldc);
+  PLOM_CHECK_LAUNCH();
+  return PLOM_OK;
+}
+
 int tn_packed(const Packed& a, const Packed& b, double* C, int64_t ldc, int* err, Arena& ws,
               cudaStream_t st) {
+  if (b.ld > 128) return tn_packed_wide(a, b, C, ldc, err, ws, st);
   const int64_t m = a.m;
   const int tna = (int)cdiv(a.ld, 128), tnb = (int)cdiv(b.ld, 128);
   const int tiles = tna * tnb;
@@ -1395,8 +1913,12 @@ int apply_packed(const Packed& p, const double* W, int64_t ldw, int64_t k, float
                  int64_t cstride, bool upper) {
   const int64_t m = p.m, batch = p.batch;
   const int64_t ldk = p.ld;  // K extent of the W copies (= packed pitch of the input)
-  const int64_t col_tiles = cdiv(k, 128);
-  const int fstride = (int)(col_tiles * 128);
+  // output tile width (see ApplyCfg): 256 for dense W wider than 128 columns;
+  // an upper-triangular W keeps 128-wide column tiles, whose K ranges follow
+  // the triangle more closely (256-wide ones do 11 % more products at k = 1024)
+  const int TN = (k > 128 && !(upper && k == p.N)) ? 256 : 128;
+  const int64_t col_tiles = cdiv(k, TN);
+  const int fstride = (int)(col_tiles * TN);
   __half* bhi = ws.take<__half>((size_t)(2 * batch * k * ldk));
   __half* blo = bhi ? bhi + batch * k * ldk : nullptr;
   float* f = ws.take<float>((size_t)(batch * fstride));
@@ -1412,9 +1934,12 @@ int apply_packed(const Packed& p, const double* W, int64_t ldw, int64_t k, float
                         PLOM_ERR_ARG, "apply16: bad packed output");
   static bool attr = false;
   if (!attr) {
-    PLOM_CHECK_CUDA(cudaFuncSetAttribute(hp::apply16_kernel,
+    PLOM_CHECK_CUDA(cudaFuncSetAttribute(hp::apply16_kernel<128>,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)hp::A_SMEM));
+                                         (int)hp::apply_smem<128>()));
+    PLOM_CHECK_CUDA(cudaFuncSetAttribute(hp::apply16_kernel<256>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)hp::apply_smem<256>()));
     attr = true;
   }
   const float out_scale = out ? (float)(1 << hp::PK_LOG2) : 1.0f;
@@ -1428,10 +1953,11 @@ int apply_packed(const Packed& p, const double* W, int64_t ldw, int64_t k, float
     PLOM_CHECK_LAUNCH();
   }
   CUtensorMap tmA, tmB;
+  const uint32_t bk = TN == 256 ? (uint32_t)hp::ApplyCfg<256>::BK : (uint32_t)hp::ApplyCfg<128>::BK;
   PLOM_REQUIRE(make_map_planes(&tmA, p.hi, (uint64_t)p.ld, (uint64_t)(batch * p.mp),
-                               (uint64_t)p.ld, 64, 128, (uint64_t)p.pstride) &&
+                               (uint64_t)p.ld, bk, 128, (uint64_t)p.pstride, bk == 32) &&
                    make_map_planes(&tmB, bhi, (uint64_t)ldk, (uint64_t)(batch * k), (uint64_t)ldk,
-                                   64, 128),
+                                   bk, 128, 0, bk == 32),
                PLOM_ERR_CUDA, "apply16: tensor map encoding failed");
   const int64_t row_tiles = cdiv(p.mp, 128);
   const int64_t tiles = batch * row_tiles * col_tiles;
@@ -1453,9 +1979,14 @@ int apply_packed(const Packed& p, const double* W, int64_t ldw, int64_t k, float
   const bool tri = tri_pre;
   const double flops = tri ? (double)m * p.N * (p.N + 1) * batch : 2.0 * m * p.N * k * batch;
   ProfScope prof("tc_apply_f16x3", st, flops, 4.0 * ((double)m * p.ld + (double)m * k) * batch);
-  hp::apply16_kernel<<<grid, hp::A_THREADS, hp::A_SMEM, st>>>(tmA, tmB, m, (int)(ldk / 64), (int)k,
-                                                    col_tiles, tiles, f, o, err, p.mp, row_tiles,
-                                                    fstride, tri ? 1 : 0, by_rows);
+  if (TN == 256)
+    hp::apply16_kernel<256><<<grid, hp::ApplyWarps<256>::THREADS, hp::apply_smem<256>(), st>>>(
+        tmA, tmB, m, (int)(ldk / hp::ApplyCfg<256>::BK), (int)k, col_tiles, tiles, f, o, err, p.mp,
+        row_tiles, fstride, tri ? 1 : 0, by_rows);
+  else
+    hp::apply16_kernel<128><<<grid, hp::ApplyWarps<128>::THREADS, hp::apply_smem<128>(), st>>>(
+        tmA, tmB, m, (int)(ldk / 64), (int)k, col_tiles, tiles, f, o, err, p.mp, row_tiles,
+        fstride, tri ? 1 : 0, by_rows);
   PLOM_CHECK_LAUNCH();
   return PLOM_OK;
 }

@@ -129,6 +129,9 @@ class Server:
         self.executor = executor
         self.footprint = footprint or (lambda j: footprint_bytes(j, self.precision))
         self._streams = {}
+        # (job id, stream index, start event, end event) of every GPU job, recorded
+        # on the job's stream: the device-side timeline of the mix (see timeline())
+        self.events = []
 
     def _gpu_execute(self, job, wid):
         torch = L.torch()
@@ -136,11 +139,23 @@ class Server:
         if stream is None:
             stream = self._streams[wid] = torch.cuda.Stream()
         with torch.cuda.stream(stream):
+            ev0 = torch.cuda.Event(enable_timing=True)
+            ev1 = torch.cuda.Event(enable_timing=True)
+            ev0.record(stream)
             X = generate(job)
             res = run_job(job, X, self.precision)
             del X
+            ev1.record(stream)
         stream.synchronize()
+        self.events.append((job.jid, wid, ev0, ev1))
         return res
+
+    def timeline(self, ref):
+        """[(job id, stream index, start ms, end ms)] of the GPU jobs, in ms
+        after the CUDA event `ref` (recorded before the run), from the events
+        each job recorded on its own stream."""
+        return sorted((jid, wid, ref.elapsed_time(a), ref.elapsed_time(b))
+                      for jid, wid, a, b in self.events)
 
     def _worker(self, wid, work_q, done_q, t0):
         execute = self.executor or self._gpu_execute

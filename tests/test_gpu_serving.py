@@ -36,3 +36,24 @@ def test_same_result_alone_and_in_mix():
             if key in ("f",):
                 continue
             _close(by[jid].result[key], res.result[key], key)
+
+
+def test_jobs_on_different_streams_overlap_on_the_device():
+    """Two admitted jobs run on their own streams at the same time: the
+    device-side intervals between the events each job records on its stream
+    intersect (the second starts before the first ends), and the two streams
+    are different."""
+    jobs = [serving.Job(0, "POD", 262144, 256, seed=1), serving.Job(1, "DMD", 262144, 200, seed=2),
+            serving.Job(2, "POD", 131072, 300, seed=3), serving.Job(3, "SPOD", 131072, 400, seed=4)]
+    srv = serving.Server(hbm_budget_bytes=40e9, slots=4)
+    warm = serving.Server(hbm_budget_bytes=40e9, slots=4)
+    warm.run([serving.Job(9, k, 65536, 96, seed=9) for k in ("POD", "DMD", "SPOD")], realtime=False)
+    ref = torch.cuda.Event(enable_timing=True)
+    ref.record()
+    done, summ = srv.run(jobs, realtime=False)
+    assert summ["completed"] == 4, [j.error for j in done if j.error]
+    tl = srv.timeline(ref)
+    assert len(tl) == 4 and len({w for _, w, _, _ in tl}) >= 2
+    overlaps = [(a, b) for a in tl for b in tl
+                if a[0] < b[0] and a[1] != b[1] and a[2] < b[3] and b[2] < a[3]]
+    assert overlaps, tl
