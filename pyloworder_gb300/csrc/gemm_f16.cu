@@ -770,7 +770,8 @@ __global__ void gram16_reduce_kernel(const double* __restrict__ part, int N, int
 // busy through the stage ring (see ApplyCfg) and the A panel is received once
 // per 256 output columns instead of once per 128.  Stages of 32 rows (48 KiB,
 // four of them); the two accumulators (main 256 + correction 256 columns) fill
-// TMEM, so a sub-chunk's drain holds the next sub-chunk's products.
+// TMEM, so a sub-chunk's drain holds the next sub-chunk's products: the drain
+// only reads TMEM and writes (no read-modify-write of a running partial).
 // SYM tiles: for each 128-column block I of A and 256-column block J of B with
 // J + 256 > I (the tiles that meet the upper triangle); where I lies inside J
 // (the band tiles) A is the middle or first half of B and is not loaded, and
@@ -803,7 +804,8 @@ template <bool SYM>
 __global__ void __launch_bounds__(320, 1)
     gram16w_kernel(const __grid_constant__ CUtensorMap tmP, const __grid_constant__ CUtensorMap tmB,
                    int64_t m, int tn, int tn2, int64_t rows_per_chunk, int chunks,
-                   double* __restrict__ part, int* err, int64_t mp) {
+                   int subs_per_chunk, int nsubs, float* __restrict__ part,
+                   double* __restrict__ diagp, int* err, int64_t mp) {
   extern __shared__ uint8_t smem_raw[];
   __shared__ uint64_t full_bar[GW_STAGES], empty_bar[GW_STAGES];
   __shared__ uint64_t tfull, tempty, dfull[2];
@@ -819,7 +821,8 @@ __global__ void __launch_bounds__(320, 1)
   const int pb = (int)(blockIdx.x / per_problem);
   const int rem_item = (int)(blockIdx.x % per_problem);
   const int chunk = rem_item / ntiles, tile = rem_item % ntiles;
-  const int item = (pb * ntiles + tile) * chunks + chunk;  // partial slab index (tile-major)
+  // sub-chunk slabs of this item: (problem, tile) major, then the sub-chunks of all rows
+  const int64_t slab0 = (int64_t)(pb * ntiles + tile) * nsubs + (int64_t)chunk * subs_per_chunk;
   int ti = 0, tj = 0;
   if (SYM)
     gw_tile_sym(tile, tn2, ti, tj);
@@ -845,7 +848,7 @@ __global__ void __launch_bounds__(320, 1)
       mbar_init(&empty_bar[s], band ? 1 + 128 : 1);  // MMA commit (+ diagonal warps)
     }
     mbar_init(&tfull, 1);
-    mbar_init(&tempty, band ? 128 : 256);  // drain threads: 4 warps (band tiles) or 8
+    mbar_init(&tempty, band ? 128 : 256);  // drain warps: 0-3 on band tiles, 0-7 elsewhere
     for (int b = 0; b < 2; ++b) mbar_init(&dfull[b], 128);
     abort_sh = 0;
     mbar_fence_init();
@@ -862,7 +865,6 @@ __global__ void __launch_bounds__(320, 1)
   __syncthreads();
   fence_after();
   const uint32_t tmem = tmem_sh;
-  float2* P = reinterpret_cast<float2*>(part) + (int64_t)item * 128 * 256;
   // stage layout: A hi (2 boxes), A lo (2), B hi (4), B lo (4)
   constexpr uint32_t OFF_AL = 2 * GW_BOX, OFF_BH = 4 * GW_BOX, OFF_BL = 8 * GW_BOX;
 
@@ -892,52 +894,50 @@ __global__ void __launch_bounds__(320, 1)
       }
     }
   } else if (warp >= 4 && warp < 8 && band) {
-    // ---- band tiles: compensated sums of (hi + lo)^2 of A's columns (as in
-    // gram16_kernel: two adjacent columns per thread, half of each stage's
-    // rows, four compensated chains)
-    {
-      const int t = threadIdx.x - 128;
-      const int c = 2 * (t & 63);                // first of the two columns of A
-      const int h = t >> 6;                      // row half of each stage
-      const uint32_t cb = OFF_BH + a_off + (uint32_t)(c >> 6) * GW_BOX;
-      const uint32_t w = (uint32_t)(c & 63);
-      const uint32_t ch = w >> 3, within = (w & 7u) * 2u;
-      const uint32_t k0 = (uint32_t)h * (GW_BK / 2), k1 = k0 + GW_BK / 2;
-      float sm[2][2] = {{0.f, 0.f}, {0.f, 0.f}}, cp[2][2] = {{0.f, 0.f}, {0.f, 0.f}};
-      for (int kb = 0; kb < KB; ++kb) {
-        const int s = kb % GW_STAGES;
-        const uint32_t ph = (uint32_t)(kb / GW_STAGES) & 1u;
-        if (!mbar_wait(&full_bar[s], ph, &abort_sh, err)) break;
-        const uint32_t st = base + s * GW_STAGE + cb;
+    // ---- band tiles: compensated sums of (hi + lo)^2 of A's columns on the
+    // CUDA cores, the Gram diagonal (as in gram16_kernel: two adjacent columns
+    // per thread, half of each stage's rows, four compensated chains)
+    const int t = threadIdx.x - 128;
+    const int c = 2 * (t & 63);                // first of the two columns of A
+    const int h = t >> 6;                      // row half of each stage
+    const uint32_t cbo = OFF_BH + a_off + (uint32_t)(c >> 6) * GW_BOX;
+    const uint32_t cw = (uint32_t)(c & 63);
+    const uint32_t ch = cw >> 3, within = (cw & 7u) * 2u;
+    const uint32_t k0 = (uint32_t)h * (GW_BK / 2), k1 = k0 + GW_BK / 2;
+    float sm[2][2] = {{0.f, 0.f}, {0.f, 0.f}}, cp[2][2] = {{0.f, 0.f}, {0.f, 0.f}};
+    for (int kb = 0; kb < KB; ++kb) {
+      const int s = kb % GW_STAGES;
+      const uint32_t ph = (uint32_t)(kb / GW_STAGES) & 1u;
+      if (!mbar_wait(&full_bar[s], ph, &abort_sh, err)) break;
+      const uint32_t st = base + s * GW_STAGE + cbo;
 #pragma unroll 4
-        for (uint32_t k = k0; k < k1; k += 2) {
+      for (uint32_t k = k0; k < k1; k += 2) {
 #pragma unroll
-          for (uint32_t u = 0; u < 2; ++u) {
-            const uint32_t kk = k + u;
-            const uint32_t off = (kk >> 3) * 1024u + (kk & 7u) * 128u + (((ch ^ (kk & 7u)) << 4) | within);
-            const float2 hv = ld_shared_h2f(st + off);
-            const float2 lv = ld_shared_h2f(st + 4 * GW_BOX + off);  // B lo = B hi + 4 boxes
-            const float v[2] = {hv.x + lv.x, hv.y + lv.y};  // exact: 22 bits
-#pragma unroll
-            for (int q = 0; q < 2; ++q) {
-              const float y = fmaf(v[q], v[q], -cp[q][u]);
-              const float tt = sm[q][u] + y;
-              cp[q][u] = (tt - sm[q][u]) - y;
-              sm[q][u] = tt;
-            }
-          }
-        }
-        mbar_arrive(&empty_bar[s]);
-        if ((kb % KB_PER_SUB) == KB_PER_SUB - 1 || kb == KB - 1) {
-          const int b = (kb / KB_PER_SUB) & 1;
+        for (uint32_t u = 0; u < 2; ++u) {
+          const uint32_t kk = k + u;
+          const uint32_t off = (kk >> 3) * 1024u + (kk & 7u) * 128u + (((ch ^ (kk & 7u)) << 4) | within);
+          const float2 hv = ld_shared_h2f(st + off);
+          const float2 lv = ld_shared_h2f(st + 4 * GW_BOX + off);  // B lo = B hi + 4 boxes
+          const float v[2] = {hv.x + lv.x, hv.y + lv.y};  // exact: 22 bits
 #pragma unroll
           for (int q = 0; q < 2; ++q) {
-            diag_sh[b][h][c + q] = ((double)sm[q][0] - (double)cp[q][0]) +
-                                   ((double)sm[q][1] - (double)cp[q][1]);
-            sm[q][0] = sm[q][1] = cp[q][0] = cp[q][1] = 0.f;
+            const float y = fmaf(v[q], v[q], -cp[q][u]);
+            const float tt = sm[q][u] + y;
+            cp[q][u] = (tt - sm[q][u]) - y;
+            sm[q][u] = tt;
           }
-          mbar_arrive(&dfull[b]);
         }
+      }
+      mbar_arrive(&empty_bar[s]);
+      if ((kb % KB_PER_SUB) == KB_PER_SUB - 1 || kb == KB - 1) {
+        const int b = (kb / KB_PER_SUB) & 1;
+#pragma unroll
+        for (int q = 0; q < 2; ++q) {
+          diag_sh[b][h][c + q] = ((double)sm[q][0] - (double)cp[q][0]) +
+                                 ((double)sm[q][1] - (double)cp[q][1]);
+          sm[q][0] = sm[q][1] = cp[q][0] = cp[q][1] = 0.f;
+        }
+        mbar_arrive(&dfull[b]);
       }
     }
   } else if (warp == 8 && lane == 0) {
@@ -979,9 +979,13 @@ __global__ void __launch_bounds__(320, 1)
       if (ok) mma_commit(&tfull);
     }
   } else if (warp < 8) {
-    // ---- epilogue: drain each finished sub-chunk into the double-float
-    // partial; warps 0-3 (TMEM lane quarters) take all 256 columns on band
-    // tiles, warps 0-7 take 128 columns each (half w / 4) elsewhere
+    // ---- drain warps (TMEM lane quarter w % 4): 0-3 take all 256 columns on
+    // band tiles, 0-7 take 128 columns each (half w / 4) elsewhere.  Each
+    // finished sub-chunk is written once, main + correction rounded to FP32
+    // (half an ulp of a 4,096-row partial), into its own slab; no slab is
+    // read back here, so the drain is a TMEM read and a stream of stores, and
+    // the reduction kernel sums the slabs in a fixed order.  Band tiles also
+    // write their rows' diagonal (the CUDA-core sums, FP64) per sub-chunk.
     const int rloc = (warp & 3) * 32 + lane;
     const int cbeg = band ? 0 : (warp >> 2) * 128, ncc = band ? 8 : 4;
     for (int sub = 0; sub < nsub; ++sub) {
@@ -991,42 +995,27 @@ __global__ void __launch_bounds__(320, 1)
       __syncwarp();
       if (!__all_sync(0xffffffffu, ready)) break;
       fence_after();
-      const float2 dval =
-          band ? dw_from_double(diag_sh[b][0][rloc] + diag_sh[b][1][rloc]) : make_float2(0.f, 0.f);
-      const int dc = band ? dcol + rloc : -1;
-      float2* prow = P + (int64_t)rloc * 256;
+      float* prow = part + ((slab0 + sub) * 128 + rloc) * 256 + cbeg;
 #pragma unroll 1
       for (int c8 = 0; c8 < ncc; ++c8) {
-        const int cc = cbeg / 32 + c8;
         uint32_t rm[32], rc[32];
-        const uint32_t ta = tmem + ((uint32_t)((warp & 3) * 32) << 16) + (uint32_t)(cc * 32);
+        const uint32_t ta = tmem + ((uint32_t)((warp & 3) * 32) << 16) + (uint32_t)(cbeg + 32 * c8);
         tmem_ld32(ta, rm);
         tmem_ld32(ta + 256, rc);
         tmem_wait_ld();
-        float2* d = prow + cc * 32;
-#pragma unroll
-        for (int j = 0; j < 32; j += 2) {
-          float2 v0 = dw_two_sum(__uint_as_float(rm[j]), __uint_as_float(rc[j]));
-          float2 v1 = dw_two_sum(__uint_as_float(rm[j + 1]), __uint_as_float(rc[j + 1]));
-          if (cc * 32 + j == dc) v0 = dval;
-          if (cc * 32 + j + 1 == dc) v1 = dval;
-          float4* q = reinterpret_cast<float4*>(d + j);
-          if (sub == 0) {
-            *q = make_float4(v0.x, v0.y, v1.x, v1.y);
-          } else {
-            const float4 o = *q;
-            const float2 a0 = dw_add(make_float2(o.x, o.y), v0);
-            const float2 a1 = dw_add(make_float2(o.z, o.w), v1);
-            *q = make_float4(a0.x, a0.y, a1.x, a1.y);
-          }
+        if (c8 == ncc - 1) {
+          fence_before();
+          mbar_arrive(&tempty);
         }
+        float4* d = reinterpret_cast<float4*>(prow + 32 * c8);
+#pragma unroll
+        for (int j = 0; j < 32; j += 4)
+          d[j / 4] = make_float4(__uint_as_float(rm[j]) + __uint_as_float(rc[j]),
+                                 __uint_as_float(rm[j + 1]) + __uint_as_float(rc[j + 1]),
+                                 __uint_as_float(rm[j + 2]) + __uint_as_float(rc[j + 2]),
+                                 __uint_as_float(rm[j + 3]) + __uint_as_float(rc[j + 3]));
       }
-      fence_before();
-      mbar_arrive(&tempty);
-    }
-    if (nsub == 0) {  // empty chunk: the partial is zero
-      float2* prow = P + (int64_t)rloc * 256;
-      for (int j = cbeg; j < cbeg + 32 * ncc; ++j) prow[j] = make_float2(0.f, 0.f);
+      if (band) diagp[(slab0 + sub) * 128 + rloc] = diag_sh[b][0][rloc] + diag_sh[b][1][rloc];
     }
   }
   fence_before();
@@ -1038,10 +1027,12 @@ __global__ void __launch_bounds__(320, 1)
   }
 }
 
-// G[i][j] = sum over chunks of the 128 x 256 tile partials (fixed order) /
-// (s_i s_j), taken from the upper triangle (i <= j) and mirrored
-__global__ void gram16w_reduce_kernel(const double* __restrict__ part, int N, int tn, int tn2,
-                                      int chunks, const float* __restrict__ s,
+// G[i][j] = sum over the 4,096-row sub-chunk slabs (fixed order, double-float)
+// / (s_i s_j), taken from the upper triangle (i <= j) and mirrored; the
+// diagonal from the band tiles' FP64 slabs
+__global__ void gram16w_reduce_kernel(const float* __restrict__ part,
+                                      const double* __restrict__ diagp, int N, int tn, int tn2,
+                                      int nsubs, const float* __restrict__ s,
                                       double* __restrict__ G, int batch, int ld, int accumulate) {
   const int64_t total = (int64_t)N * N * batch;
   const int ntiles = gw_tiles_sym(tn, tn2);
@@ -1050,25 +1041,36 @@ __global__ void gram16w_reduce_kernel(const double* __restrict__ part, int N, in
     const int64_t pb = e / ((int64_t)N * N);
     const int64_t r = e - pb * N * N;
     const int i = (int)(r / N), j = (int)(r % N);
-    const int a = min(i, j), b = max(i, j);
+    if (i > j) continue;  // the upper triangle, written to both halves
+    const int a = i, b = j;
     const int ti = a / 128, tj = b / 256;
     int tile = 0;
     for (int t = 0; t < ti; ++t) tile += tn2 - (t >> 1);
     tile += tj - (ti >> 1);
-    const float2* p = reinterpret_cast<const float2*>(part) +
-                      ((pb * ntiles + tile) * chunks) * 128 * 256 + (int64_t)(a - ti * 128) * 256 +
-                      (b - tj * 256);
-    float2 acc = make_float2(0.f, 0.f);
-    for (int c = 0; c < chunks; ++c) acc = dw_add(acc, p[(int64_t)c * 128 * 256]);
+    const int64_t slab = (pb * ntiles + tile) * (int64_t)nsubs;
+    double v;
+    if (a == b) {
+      const double* p = diagp + slab * 128 + (a - ti * 128);
+      float2 acc = make_float2(0.f, 0.f);
+      for (int c = 0; c < nsubs; ++c) acc = dw_add(acc, dw_from_double(p[(int64_t)c * 128]));
+      v = dw_value(acc);
+    } else {
+      const float* p = part + slab * 128 * 256 + (int64_t)(a - ti * 128) * 256 + (b - tj * 256);
+      float2 acc = make_float2(0.f, 0.f);
+      for (int c = 0; c < nsubs; ++c) acc = dw_add(acc, make_float2(p[(int64_t)c * 128 * 256], 0.f));
+      v = dw_value(acc);
+    }
     const float* sp = s + pb * ld;
-    const double v = dw_value(acc) / ((double)sp[i] * (double)sp[j]);
+    v /= ((double)sp[i] * (double)sp[j]);
+    const int64_t e2 = pb * N * N + (int64_t)j * N + i;
     G[e] = accumulate ? G[e] + v : v;
+    if (e2 != e) G[e2] = accumulate ? G[e2] + v : v;
   }
 }
 
-// C[i][j] (Na x Nb, ldc) = sum over chunks of the 128 x 256 tile partials / (sA_i sB_j)
-__global__ void tn16w_reduce_kernel(const double* __restrict__ part, int Na, int Nb, int tn2,
-                                    int chunks, const float* __restrict__ sa,
+// C[i][j] (Na x Nb, ldc) = sum over the sub-chunk slabs / (sA_i sB_j)
+__global__ void tn16w_reduce_kernel(const float* __restrict__ part, int Na, int Nb, int tn2,
+                                    int nsubs, const float* __restrict__ sa,
                                     const float* __restrict__ sb, double* __restrict__ C,
                                     int64_t ldc) {
   const int64_t total = (int64_t)Na * Nb;
@@ -1077,10 +1079,10 @@ __global__ void tn16w_reduce_kernel(const double* __restrict__ part, int Na, int
     const int i = (int)(e / Nb), j = (int)(e % Nb);
     const int ti = i / 128, tj = j / 256;
     const int tile = ti * tn2 + tj;
-    const float2* p = reinterpret_cast<const float2*>(part) + ((int64_t)tile * chunks) * 128 * 256 +
-                      (int64_t)(i - ti * 128) * 256 + (j - tj * 256);
+    const float* p = part + ((int64_t)tile * nsubs) * 128 * 256 + (int64_t)(i - ti * 128) * 256 +
+                     (j - tj * 256);
     float2 acc = make_float2(0.f, 0.f);
-    for (int c = 0; c < chunks; ++c) acc = dw_add(acc, p[(int64_t)c * 128 * 256]);
+    for (int c = 0; c < nsubs; ++c) acc = dw_add(acc, make_float2(p[(int64_t)c * 128 * 256], 0.f));
     C[(int64_t)i * ldc + j] = dw_value(acc) / ((double)sa[i] * (double)sb[j]);
   }
 }
@@ -1734,17 +1736,29 @@ static int gram16_chunks(int64_t m, int tiles, int bk = hp::G_BK) {
   return (int)std::max<int64_t>(1, std::min<int64_t>(maxc, cdiv(2 * sms, tiles)));
 }
 
-// Gram of operands wider than 128 columns: 128 x 256 tiles (gram16w_kernel)
+// Gram of operands wider than 128 columns: 128 x 256 tiles (gram16w_kernel);
+// row chunks are whole 4,096-row sub-chunks, each with its own FP32 slab
+static void wide_chunks(int64_t m, int items_per_chunk, int& chunks_eff, int64_t& rpc,
+                        int& subs_per_chunk, int& nsubs) {
+  const int chunks = gram16_chunks(m, items_per_chunk, hp::G_KSUB / 4);
+  rpc = cdiv(cdiv(m, chunks), hp::G_KSUB) * hp::G_KSUB;
+  chunks_eff = (int)std::max<int64_t>(1, cdiv(m, rpc));
+  subs_per_chunk = (int)(rpc / hp::G_KSUB);
+  nsubs = (int)std::max<int64_t>(1, cdiv(m, hp::G_KSUB));
+}
+
 static int gram_packed_wide(const Packed& p, double* G, int* err, Arena& ws, cudaStream_t st,
                             bool accumulate) {
   const int64_t m = p.m, N = p.N, batch = p.batch;
   const int tn = (int)cdiv(p.ld, 128), tn2 = (int)cdiv(p.ld, 256);
   const int tiles = hp::gw_tiles_sym(tn, tn2);
-  const int chunks = gram16_chunks(m, (int)std::min<int64_t>(tiles * batch, 1 << 20), hp::GW_BK);
-  int64_t rpc = cdiv(m, chunks);
-  rpc = cdiv(rpc, hp::GW_BK) * hp::GW_BK;  // chunk boundaries on stage boundaries
-  const int chunks_eff = (int)std::max<int64_t>(1, cdiv(m, rpc));
-  double* part = ws.take<double>((size_t)(batch * tiles * chunks_eff) * 128 * 256);
+  int chunks_eff, subs_per_chunk, nsubs;
+  int64_t rpc;
+  wide_chunks(m, (int)std::min<int64_t>(tiles * batch, 1 << 20), chunks_eff, rpc, subs_per_chunk,
+              nsubs);
+  const int64_t slabs = batch * tiles * (int64_t)nsubs;
+  float* part = ws.take<float>((size_t)slabs * 128 * 256);
+  double* diagp = ws.take<double>((size_t)slabs * 128);
   if (ws.measuring()) return PLOM_OK;
   PLOM_REQUIRE(!ws.overflow(), PLOM_ERR_WORKSPACE, "gram16w: workspace too small");
   PLOM_REQUIRE(p.hi && G && part && m >= 1 && batch * p.mp < (1ll << 31) &&
@@ -1766,13 +1780,13 @@ static int gram_packed_wide(const Packed& p, double* G, int* err, Arena& ws, cud
                PLOM_ERR_CUDA, "gram16w: tensor map encoding failed");
   ProfScope prof_g("tc_gram_f16x3", st, (double)m * N * N * batch, 4.0 * (double)m * p.ld * batch);
   hp::gram16w_kernel<true><<<(unsigned)(batch * tiles * chunks_eff), 320, hp::GW_SMEM, st>>>(
-      tm, tm, m, tn, tn2, rpc, chunks_eff, part, err, p.mp);
+      tm, tm, m, tn, tn2, rpc, chunks_eff, subs_per_chunk, nsubs, part, diagp, err, p.mp);
   PLOM_CHECK_LAUNCH();
   const int64_t total = N * N * batch;
   const int blocks = (int)std::min<int64_t>(cdiv(total, 256), (int64_t)num_sms() * 16);
-  ProfScope prof_r("gram_reduce", st, 0.0, 8.0 * (double)batch * tiles * chunks_eff * 128 * 256);
-  hp::gram16w_reduce_kernel<<<blocks, 256, 0, st>>>(part, (int)N, tn, tn2, chunks_eff, p.scale, G,
-                                                    (int)batch, (int)p.ld, accumulate ? 1 : 0);
+  ProfScope prof_r("gram_reduce", st, 0.0, 4.0 * (double)slabs * 128 * 256);
+  hp::gram16w_reduce_kernel<<<blocks, 256, 0, st>>>(part, diagp, (int)N, tn, tn2, nsubs, p.scale,
+                                                    G, (int)batch, (int)p.ld, accumulate ? 1 : 0);
   PLOM_CHECK_LAUNCH();
   return PLOM_OK;
 }
@@ -1826,11 +1840,11 @@ static int tn_packed_wide(const Packed& a, const Packed& b, double* C, int64_t l
   const int64_t m = a.m;
   const int tna = (int)cdiv(a.ld, 128), tn2 = (int)cdiv(b.ld, 256);
   const int tiles = tna * tn2;
-  const int chunks = gram16_chunks(m, tiles, hp::GW_BK);
-  int64_t rpc = cdiv(m, chunks);
-  rpc = cdiv(rpc, hp::GW_BK) * hp::GW_BK;
-  const int chunks_eff = (int)std::max<int64_t>(1, cdiv(m, rpc));
-  double* part = ws.take<double>((size_t)tiles * chunks_eff * 128 * 256);
+  int chunks_eff, subs_per_chunk, nsubs;
+  int64_t rpc;
+  wide_chunks(m, tiles, chunks_eff, rpc, subs_per_chunk, nsubs);
+  const int64_t slabs = tiles * (int64_t)nsubs;
+  float* part = ws.take<float>((size_t)slabs * 128 * 256);
   if (ws.measuring()) return PLOM_OK;
   PLOM_REQUIRE(!ws.overflow(), PLOM_ERR_WORKSPACE, "tn16w: workspace too small");
   PLOM_REQUIRE(a.hi && b.hi && C && part && m >= 1 && m < (1ll << 31) && b.m == m &&
@@ -1853,13 +1867,13 @@ static int tn_packed_wide(const Packed& a, const Packed& b, double* C, int64_t l
     ProfScope prof("tc_tn_f16x3", st, 2.0 * (double)m * a.N * b.N,
                    4.0 * (double)m * (a.ld + b.ld));
     hp::gram16w_kernel<false><<<tiles * chunks_eff, 320, hp::GW_SMEM, st>>>(
-        ta, tb, m, tna, tn2, rpc, chunks_eff, part, err, m);
+        ta, tb, m, tna, tn2, rpc, chunks_eff, subs_per_chunk, nsubs, part, nullptr, err, m);
     PLOM_CHECK_LAUNCH();
   }
   const int64_t total = a.N * b.N;
   const int blocks = (int)std::max<int64_t>(1, std::min<int64_t>(cdiv(total, 256), (int64_t)num_sms() * 16));
-  hp::tn16w_reduce_kernel<<<blocks, 256, 0, st>>>(part, (int)a.N, (int)b.N, tn2, chunks_eff,
-                                                  a.scale, b.scale, C, ldc);
+  hp::tn16w_reduce_kernel<<<blocks, 256, 0, st>>>(part, (int)a.N, (int)b.N, tn2, nsubs, a.scale,
+                                                  b.scale, C, ldc);
   PLOM_CHECK_LAUNCH();
   return PLOM_OK;
 }
