@@ -38,9 +38,11 @@ def test_workspace_queries():
     m, n = 8388608, 1024
     mixed = lib.plom_tsqr_svd_workspace(L.F32, L.PREC_MIXED, m, n)
     fp64 = lib.plom_tsqr_svd_workspace(L.F32, L.PREC_FP64, m, n)
-    # mixed: one FP32 m x n buffer (Q1 lives in U) plus the Gram's FP64 tile
-    # partials (36 tiles x 152 row chunks x 128 KiB); FP64: two FP64 buffers
-    assert 4 * m * n <= mixed < 4 * m * n + (2 << 30)
+    # mixed: one FP32 m x n buffer (Q1 lives in U) plus the Gram's FP32
+    # sub-chunk slabs (20 tiles of 128 x 256 x 2,048 sub-chunks of 4,096 rows x
+    # 128 KiB = 5 GiB) and their FP64 diagonals; FP64: two FP64 buffers
+    slabs = 20 * (m // 4096) * 128 * 256 * 4
+    assert 4 * m * n + slabs <= mixed < 4 * m * n + slabs + (2 << 30)
     assert 16 * m * n <= fp64 < 16 * m * n + (1 << 30)
     # mixed randomized: A packed once (4 m n bytes), Q packed (pitch 128), Y and
     # Q in FP32, and the packed CholeskyQR of the m x r sketch (two pitch-128
