@@ -68,31 +68,53 @@ def ncu_traffic(kernel):
     return None
 
 
-def serving_leg(njobs=48, seed=5, slots=4, budget=150e9):
-    """Serving mix (config 5 distribution, bounded sample): saturation
-    throughput and Poisson-arrival latency, mixed form; FP64 form on the
-    subset of small jobs for the speed ratio."""
+def serving_leg(njobs=2000, seed=5, slots=4, budget=150e9, max_sat_s=90.0, poisson_s=20.0,
+                cmp_jobs=64):
+    """The serving mix (config 5's distribution: POD / DMD / SPOD jobs, m
+    log-uniform 16,384-4,194,304, n log-uniform 32-1,024, FP32 data generated
+    per job seed on the device, 150 GB admission budget):
+    * saturation: all `njobs` jobs queued at t = 0, mixed form -> jobs/s,
+      p50 / p99 latency; `njobs` is lowered (and reported) only if a 200-job
+      prefix predicts more than `max_sat_s` seconds;
+    * Poisson arrivals at 0.5, 0.7 and 0.9 of the saturation rate, each on a
+      prefix of the mix sized for ~`poisson_s` seconds;
+    * mixed vs plain FP64 form on the same first `cmp_jobs` jobs of the mix
+      (the FP64 form of the largest jobs takes seconds each, so the whole mix
+      is out of reach in FP64)."""
     from pyloworder_gb300 import serving
-    jobs = serving.make_mix(njobs, seed=seed)
-    warm = serving.make_mix(3, seed=seed + 1, m_range=(16384, 65536), n_range=(32, 64))
+    warm = serving.make_mix(6, seed=seed + 1, m_range=(16384, 65536), n_range=(32, 96))
     serving.Server(budget, slots).run(warm, realtime=False)
-    _, sat = serving.Server(budget, slots).run(jobs, realtime=False)
-    rate = 0.7 * sat["jobs_per_s"]
-    jobs2 = serving.make_mix(njobs, seed=seed, rate=rate)
-    _, poi = serving.Server(budget, slots).run(jobs2, realtime=True)
-    small = [j for j in serving.make_mix(njobs, seed=seed) if j.m * j.n <= 2**24][:12]
-    for j in small:
-        j.arrival = 0.0
-    _, smx = serving.Server(budget, slots, precision="mixed").run(small, realtime=False)
-    _, s64 = serving.Server(budget, slots, precision="fp64").run(small, realtime=False)
-    return {"workload": f"{njobs} POD/DMD/SPOD jobs, m log-uniform 16384-4194304, n log-uniform "
-                        f"32-1024, FP32, {slots} streams, {budget / 1e9:.0f} GB admission budget",
-            "jobs_per_s": sat["jobs_per_s"], "saturation": sat,
-            "poisson_rate_jobs_per_s": rate, "p50_ms": poi["p50_ms"], "p99_ms": poi["p99_ms"],
-            "poisson": poi,
-            "mixed_vs_fp64_small_jobs": {"jobs": len(small), "mixed_wall_s": smx["wall_s"],
-                                         "fp64_wall_s": s64["wall_s"],
-                                         "speedup": s64["wall_s"] / smx["wall_s"]}}
+    serving.Server(budget, slots, precision="fp64").run(warm, realtime=False)
+    _, pre = serving.Server(budget, slots).run(serving.make_mix(200, seed=seed), realtime=False)
+    n_sat = njobs
+    if pre["jobs_per_s"] > 0 and njobs / pre["jobs_per_s"] > max_sat_s:
+        n_sat = max(200, int(pre["jobs_per_s"] * max_sat_s))
+    _, sat = serving.Server(budget, slots).run(serving.make_mix(n_sat, seed=seed), realtime=False)
+    poisson = []
+    for frac in (0.5, 0.7, 0.9):
+        rate = frac * sat["jobs_per_s"]
+        n_p = int(min(n_sat, max(50, rate * poisson_s)))
+        _, poi = serving.Server(budget, slots).run(serving.make_mix(n_p, seed=seed, rate=rate),
+                                                   realtime=True)
+        poisson.append({"rate_frac": frac, "rate_jobs_per_s": rate, "jobs": n_p,
+                        "jobs_per_s": poi["jobs_per_s"], "p50_ms": poi["p50_ms"],
+                        "p99_ms": poi["p99_ms"], "failed": poi["failed"]})
+    cmp = serving.make_mix(cmp_jobs, seed=seed)
+    _, cmx = serving.Server(budget, slots, precision="mixed").run(cmp, realtime=False)
+    cmp = serving.make_mix(cmp_jobs, seed=seed)
+    _, c64 = serving.Server(budget, slots, precision="fp64").run(cmp, realtime=False)
+    mid = poisson[1]
+    return {"workload": f"{n_sat} POD/DMD/SPOD jobs (of {njobs} asked), m log-uniform "
+                        f"16384-4194304, n log-uniform 32-1024, FP32 generated per job on the "
+                        f"device, {slots} streams, {budget / 1e9:.0f} GB admission budget",
+            "jobs": n_sat, "jobs_per_s": sat["jobs_per_s"], "saturation": sat,
+            "p50_ms": mid["p50_ms"], "p99_ms": mid["p99_ms"], "poisson_sweep": poisson,
+            "mixed_vs_fp64": {"jobs": cmp_jobs, "sample": f"the first {cmp_jobs} jobs of the mix",
+                              "mixed_jobs_per_s": cmx["jobs_per_s"],
+                              "fp64_jobs_per_s": c64["jobs_per_s"],
+                              "mixed_p50_ms": cmx["p50_ms"], "fp64_p50_ms": c64["p50_ms"],
+                              "mixed_p99_ms": cmx["p99_ms"], "fp64_p99_ms": c64["p99_ms"],
+                              "speedup": c64["wall_s"] / cmx["wall_s"]}}
 
 
 def peaks():
@@ -453,7 +475,7 @@ def run_ours(args):
 # DMD (config 3), SPOD (config 4)
 # ---------------------------------------------------------------------------
 
-def measure_workload(workload, steps, warmup, m=M_FULL):
+def measure_workload(workload, steps, warmup, m=M_FULL, rows=None):
     """One of the other workloads (randomized SVD on the headline field, DMD,
     SPOD, the streaming range finder): device-resident inputs, CUDA events
     around `steps` calls after `warmup`, per-kernel timings, clocks, and the
@@ -503,7 +525,7 @@ def measure_workload(workload, steps, warmup, m=M_FULL):
                    config={"workload": f"init/update_qr_streaming {m}x{n} f32 in {nb} batches of {w} "
                                        f"snapshots, r={r}, q={q}", "precision": "mixed"})
     elif workload == "dmd":
-        m, n, r = 2_097_152, 512, 32
+        m, n, r = rows or 2_097_152, 512, 32
         X, lam = datagen.dmd_field_device(m, n)
         step = lambda: P.DMD.run_device(X, n, r, remove_mean=False, precision="mixed")  # noqa: E731
         # X read, TSQR-SVD of Y1 (read, write U), Phi (complex) written
@@ -512,7 +534,7 @@ def measure_workload(workload, steps, warmup, m=M_FULL):
         out.update(metric="DMD GB/s", unit="GB/s",
                    config={"workload": f"DMD.run {m}x{n} f32, r={r}", "precision": "mixed"})
     else:
-        M, N, nDFT, nB, nf = 1_048_576, 8192, 256, 63, 129
+        M, N, nDFT, nB, nf = rows or 1_048_576, 8192, 256, 63, 129
         X = datagen.spod_field_device(M, N)
         t = np.arange(N, dtype=np.float64)
         step = lambda: P.SPOD.run_device(X, N, t, nDFT=nDFT, nolap=128, precision="mixed")  # noqa: E731
@@ -575,23 +597,30 @@ def side_legs(steps=3, warmup=2):
 
 
 def run_other(args):
-    print(json.dumps(measure_workload(args.workload, args.steps, args.warmup, args.m)), flush=True)
+    print(json.dumps(measure_workload(args.workload, args.steps, args.warmup, args.m, args.rows)),
+          flush=True)
     return 0
 
 
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--workload", default="tsqr_svd",
-                    choices=["tsqr_svd", "randomized", "dmd", "spod", "streaming"])
+                    choices=["tsqr_svd", "randomized", "dmd", "spod", "streaming", "serving"])
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--m", type=int, default=M_FULL)
+    ap.add_argument("--jobs", type=int, default=2000, help="jobs of the serving mix")
+    ap.add_argument("--rows", type=int, default=None,
+                    help="points of the DMD / SPOD workload (default: the configuration's)")
     ap.add_argument("--quick", action="store_true", help="skip accuracy / e2e / CPU legs")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
+    if args.workload == "serving":
+        print(json.dumps(serving_leg(njobs=args.jobs)), flush=True)
+        return 0
     if args.workload != "tsqr_svd":
         return run_other(args)
     return run_ours(args)

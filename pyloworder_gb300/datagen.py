@@ -59,12 +59,16 @@ def pod_field_np(nx, ny, nt, nmodes, seed, noise=1e-4, amp_pow=None, dtype=np.fl
 
 
 def pod_field_device(nx, ny, nt, nmodes, seed, noise=1e-5, amp_pow=1.5, dtype="float32",
-                     distinct=True, kmax=16, chunk_rows=1 << 20, m=None):
+                     distinct=True, kmax=16, chunk_rows=1 << 20, m=None, compute="float64"):
     """Config-2 style field generated in HBM (torch, row chunks).  With `m`
     given, the first m points of the nx x ny grid (row by row) are used, so
-    any point count fits a grid with nx * ny >= m."""
+    any point count fits a grid with nx * ny >= m.  `compute`: the arithmetic
+    of the generator (float64 by default; float32 makes the per-job fields of
+    the serving mix cheap to build, GB300 running FP64 at a small fraction of
+    its FP32 rate)."""
     import torch
     tdt = getattr(torch, dtype) if isinstance(dtype, str) else dtype
+    cdt = getattr(torch, compute) if isinstance(compute, str) else compute
     rng, kx, ky, w, th = _pod_params(nmodes, seed, distinct, kmax)
     if m is None:
         m = nx * ny
@@ -74,9 +78,9 @@ def pod_field_device(nx, ny, nt, nmodes, seed, noise=1e-5, amp_pow=1.5, dtype="f
                      for k in range(1, nmodes + 1)])
     t = np.arange(nt, dtype=np.float64)
     T = torch.tensor(amps[:, None] * np.cos(np.outer(w, t) + th[:, None]), device="cuda",
-                     dtype=torch.float64)
-    kxt = torch.tensor(kx, device="cuda", dtype=torch.float64)
-    kyt = torch.tensor(ky, device="cuda", dtype=torch.float64)
+                     dtype=cdt)
+    kxt = torch.tensor(kx, device="cuda", dtype=cdt)
+    kyt = torch.tensor(ky, device="cuda", dtype=cdt)
     X = torch.empty((m, nt), dtype=tdt, device="cuda")
     g = torch.Generator(device="cuda")
     g.manual_seed(int(seed))
@@ -85,11 +89,11 @@ def pod_field_device(nx, ny, nt, nmodes, seed, noise=1e-5, amp_pow=1.5, dtype="f
     for r0 in range(0, m, chunk_rows):
         r1 = min(m, r0 + chunk_rows)
         idx = torch.arange(r0, r1, device="cuda", dtype=torch.int64)
-        xs = (idx // ny).to(torch.float64) * hx
-        ys = (idx % ny).to(torch.float64) * hy
+        xs = (idx // ny).to(cdt) * hx
+        ys = (idx % ny).to(cdt) * hy
         Phi = torch.sin(xs[:, None] * kxt[None, :]) * torch.sin(ys[:, None] * kyt[None, :])
         blk = Phi @ T
-        blk += noise * torch.randn(blk.shape, device="cuda", dtype=torch.float64, generator=g)
+        blk += noise * torch.randn(blk.shape, device="cuda", dtype=cdt, generator=g)
         X[r0:r1].copy_(blk)
         del Phi, blk
     return X

@@ -90,7 +90,7 @@ def generate(job):
     as config 1, per-job seed)."""
     nx, ny = datagen.grid_for_points(job.m)
     return datagen.pod_field_device(nx, ny, job.n, 10, seed=job.seed, noise=1e-4, amp_pow=None,
-                                    dtype="float32", distinct=False, m=job.m)
+                                    dtype="float32", distinct=False, m=job.m, compute="float32")
 
 
 def run_job(job, X, precision="mixed"):
