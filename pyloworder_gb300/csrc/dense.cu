@@ -2002,11 +2002,13 @@ __global__ void pre32_operands_kernel(const float* __restrict__ J32, const float
        e += (int64_t)gridDim.x * blockDim.x) {
     const double jo = (double)J32[e] + 0.5 * (double)C[e];
     Jo[e] = jo;
-    const float jh = (float)jo;
-    const float jl = (float)(jo - (double)jh);
-    Jcat[e] = jh;
-    Jcat[nn + e] = jl;
-    Jcat[2 * nn + e] = jh;
+    if (Jcat) {
+      const float jh = (float)jo;
+      const float jl = (float)(jo - (double)jh);
+      Jcat[e] = jh;
+      Jcat[nn + e] = jl;
+      Jcat[2 * nn + e] = jh;
+    }
     const double a = ldexp(A[e], -ex);
     const float ah = (float)a;
     const float al = (float)(a - (double)ah);
@@ -2023,17 +2025,476 @@ __global__ void pre32_unscale_kernel(double* __restrict__ S, int n,
   for (int i = threadIdx.x; i < n; i += blockDim.x) S[i] = ldexp(S[i], ex);
 }
 
-// Only where the double-float finish runs in shared memory (the df16 block
-// kernel): larger n keeps the double-float-only path.
+// ---- refinement of the FP32 phase ----------------------------------------
+// The FP32 sweeps leave the rotation product Jo accurate to ~1e-5 with
+// respect to B itself.  B' = B Jo is formed once (double-float sums of exact
+// FP32 products, operands split x = xh + xl:  X^T Y ~ [Xh; Xh; Xl]^T
+// [Yh; Yl; Yh]), and its right singular vectors V' = I + D are found close
+// to the identity: with W = B' (I + D) and C = W^T W, the simultaneous
+// one-sided Jacobi angles of all pairs
+//     Om_ij = C_ij / (C_jj - C_ii)  (skew),   I + D <- (I + D)(I + Om),
+// followed by Newton-Schulz steps that keep I + D orthogonal
+// (E = I - (I + D)^T (I + D) = -(D + D^T) - D^T D,  D <- D + (I + D) E / 2).
+// Only D, Om and E are products of small matrices, so W = B' + B' D keeps
+// every column of B' to its own relative accuracy (the small singular
+// values included) and the iteration converges to the SVD of the fixed B'
+// (the same matrix a double-float Jacobi finish would decompose), the error
+// of a separated pair squaring at each step.  Pairs whose angle would
+// exceed 0.1 (singular values closer than the remaining error) and pairs of
+// columns both below JAC_REFINE_FLOOR of the largest are not rotated, and a
+// step whose angles have a Frobenius norm above 0.25 is shortened to it.
+// Finally V = Jo (I + D), sigma_k = ||W e_k||, and the columns of
+// Ut = W diag(sigma)^-1 are orthonormalised in descending sigma order
+// (graded: the leading, accurate columns keep their directions).
+// (T. Ogita and K. Aishima refine SVDs by matrix products in the same
+// spirit, J. Comput. Appl. Math. 369 (2020); this is a one-sided form.)
+constexpr int JAC_REFINE_STEPS = 3;
+constexpr int JAC_REFINE_NS = 2;           // Newton-Schulz steps per refinement step
+constexpr double JAC_REFINE_MAX_ANGLE = 0.1;
+constexpr double JAC_REFINE_NULL = 1e-8;   // sigma_k / sigma_1 below this: a null column
+constexpr double JAC_REFINE_FLOOR = 1e-5;  // pairs of columns both below this fraction: kept
+constexpr int JAC_REFINE_GS = 3;           // graded orthonormalisation steps of Ut
+
+// a3 = [Xh; Xh; Xl], b3 = [Xh; Xl; Xh] (3n x n FP32 each; either may be null)
+__global__ void rf_split3_kernel(const double* __restrict__ X, int64_t nn, float* __restrict__ a3,
+                                 float* __restrict__ b3) {
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < nn;
+       e += (int64_t)gridDim.x * blockDim.x) {
+    const double x = X[e];
+    const float h = (float)x;
+    const float l = (float)(x - (double)h);
+    if (a3) {
+      a3[e] = h;
+      a3[nn + e] = h;
+      a3[2 * nn + e] = l;
+    }
+    if (b3) {
+      b3[e] = h;
+      b3[nn + e] = l;
+      b3[2 * nn + e] = h;
+    }
+  }
+}
+
+// t = the transposed split of X (so that t^T Y = X Y): nparts = 2 gives
+// [Xh^T; Xl^T] (against [Y; Y]), nparts = 3 gives [Xh^T; Xh^T; Xl^T]
+// (against [Yh; Yl; Yh])
+__global__ void rf_tsplit_kernel(const double* __restrict__ X, int n, int nparts,
+                                 float* __restrict__ t) {
+  const int64_t nn = (int64_t)n * n;
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < nn;
+       e += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i = e / n, j = e % n;
+    const double x = X[j * n + i];
+    const float h = (float)x;
+    const float l = (float)(x - (double)h);
+    t[e] = h;
+    if (nparts == 2) {
+      t[nn + e] = l;
+    } else {
+      t[nn + e] = h;
+      t[2 * nn + e] = l;
+    }
+  }
+}
+
+// cmax[0] = max_i C_ii (one block)
+__global__ void rf_cmax_kernel(const double* __restrict__ C, int n, double* __restrict__ cmax) {
+  __shared__ double red[32];
+  double v = 0.0;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) v = fmax(v, C[(int64_t)i * n + i]);
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t = fmax(t, red[w]);
+    cmax[0] = t;
+  }
+}
+
+// om (FP32): Om_ij = C_ij / (C_jj - C_ii) with C symmetrised; 0 on the
+// diagonal, where |Om_ij| would exceed JAC_REFINE_MAX_ANGLE and for pairs of
+// columns both below JAC_REFINE_FLOOR of the largest
+__global__ void rf_omega_kernel(const double* __restrict__ C, int n, const double* __restrict__ cmax,
+                                float* __restrict__ om) {
+  const int64_t nn = (int64_t)n * n;
+  const double floor2 = JAC_REFINE_FLOOR * JAC_REFINE_FLOOR * cmax[0];
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < nn;
+       e += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i = e / n, j = e % n;
+    double o = 0.0;
+    const double ci = C[i * n + i], cj = C[j * n + j];
+    if (i != j && fmax(ci, cj) > floor2) {
+      const double c = 0.5 * (C[e] + C[j * n + i]);
+      const double d = cj - ci;
+      if (fabs(d) * JAC_REFINE_MAX_ANGLE > fabs(c)) o = c / d;
+    }
+    om[e] = (float)o;
+  }
+}
+
+// om *= min(1, JAC_REFINE_MAX_NORM / ||om||_F): a step that would leave
+// I + D far from orthogonal (many unresolved pairs at the angle bound at
+// once) is shortened so that the Newton-Schulz steps stay convergent.  One
+// block; the sum of squares in a fixed order.
+constexpr double JAC_REFINE_MAX_NORM = 0.25;
+__global__ void rf_omnorm_kernel(const float* __restrict__ om, int64_t nn, double* __restrict__ g) {
+  __shared__ double red[32];
+  double v = 0.0;
+  for (int64_t e = threadIdx.x; e < nn; e += blockDim.x) v = fma((double)om[e], (double)om[e], v);
+  v = warp_sum(v);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += red[w];
+    const double f = sqrt(t);
+    g[0] = (f > JAC_REFINE_MAX_NORM) ? JAC_REFINE_MAX_NORM / f : 1.0;
+  }
+}
+
+__global__ void rf_omscale_kernel(float* __restrict__ om, int64_t nn, const double* __restrict__ g) {
+  const float f = (float)g[0];
+  if (f == 1.f) return;
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < nn;
+       e += (int64_t)gridDim.x * blockDim.x)
+    om[e] *= f;
+}
+
+// D += om + P  ((I + D)(I + Om) - I with P = D Om)
+__global__ void rf_rotate_kernel(double* __restrict__ D, const float* __restrict__ om,
+                                 const double* __restrict__ P, int64_t nn) {
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < nn;
+       e += (int64_t)gridDim.x * blockDim.x)
+    D[e] += (double)om[e] + P[e];
+}
+
+// E = -(D + D^T) - G  (G = D^T D): FP64 and FP32 copies
+__global__ void rf_ns_residual_kernel(const double* __restrict__ D, const double* __restrict__ G,
+                                      int n, double* __restrict__ E, float* __restrict__ E32) {
+  const int64_t nn = (int64_t)n * n;
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < nn;
+       e += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i = e / n, j = e % n;
+    const double v = -(D[e] + D[j * n + i]) - G[e];
+    E[e] = v;
+    E32[e] = (float)v;
+  }
+}
+
+// D += (E + P) / 2  (P = D E)
+__global__ void rf_ns_update_kernel(double* __restrict__ D, const double* __restrict__ E,
+                                    const double* __restrict__ P, int64_t nn) {
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < nn;
+       e += (int64_t)gridDim.x * blockDim.x)
+    D[e] += 0.5 * (E[e] + P[e]);
+}
+
+// out = X + P
+__global__ void rf_add_kernel(double* __restrict__ out, const double* __restrict__ X,
+                              const double* __restrict__ P, int64_t nn) {
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < nn;
+       e += (int64_t)gridDim.x * blockDim.x)
+    out[e] = X[e] + P[e];
+}
+
+// f = strict upper triangle of G (the first-order Gram-Schmidt coefficients)
+__global__ void rf_upper_kernel(const double* __restrict__ G, int n, float* __restrict__ f) {
+  const int64_t nn = (int64_t)n * n;
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < nn;
+       e += (int64_t)gridDim.x * blockDim.x)
+    f[e] = (e % n > e / n) ? (float)G[e] : 0.f;
+}
+
+// X -= P, then (separately) columns to unit norm
+__global__ void rf_sub_kernel(double* __restrict__ X, const double* __restrict__ P, int64_t nn) {
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < nn;
+       e += (int64_t)gridDim.x * blockDim.x)
+    X[e] -= P[e];
+}
+
+// s[c] = ||X e_c|| (each thread sums one column down the rows: fixed order)
+__global__ void rf_colnorm_kernel(const double* __restrict__ W, int n, double* __restrict__ s) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= n) return;
+  double acc = 0.0;
+  for (int r = 0; r < n; ++r) {
+    const double w = W[(int64_t)r * n + c];
+    acc = fma(w, w, acc);
+  }
+  s[c] = sqrt(acc);
+}
+
+// columns of X to unit norm; a column whose norm fell below 1e-3 (it
+// depended on the earlier ones) becomes zero and is completed later
+__global__ void rf_colscale_kernel(double* __restrict__ X, int n, const double* __restrict__ s,
+                                   int* __restrict__ zero) {
+  const int64_t nn = (int64_t)n * n;
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < nn;
+       e += (int64_t)gridDim.x * blockDim.x) {
+    const double v = s[e % n];
+    X[e] = (v > 1e-3) ? X[e] / v : 0.0;
+    if (e < n && !(v > 1e-3)) zero[e] = 1;
+  }
+}
+
+// rank of column c in descending sigma (ties: lower index first)
+__global__ void rf_order_kernel(const double* __restrict__ s, int n, int* __restrict__ perm) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= n) return;
+  const double v = s[c];
+  int rank = 0;
+  for (int k = 0; k < n; ++k) rank += (s[k] > v) || (s[k] == v && k < c);
+  perm[rank] = c;
+}
+
+// sorted outputs: S[k] = s[p], Ut e_k = W e_p / s[p] (zero for a null
+// column, flagged for completion), VHt row k = V e_p (p = perm[k])
+__global__ void rf_output_kernel(const double* __restrict__ W, const double* __restrict__ V,
+                                 const double* __restrict__ s, const int* __restrict__ perm, int n,
+                                 double* __restrict__ S, double* __restrict__ Ut,
+                                 double* __restrict__ VHt, int* __restrict__ zero) {
+  const int64_t nn = (int64_t)n * n;
+  const double s1 = s[perm[0]];
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < nn;
+       e += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i = e / n, k = e % n;
+    const int p = perm[k];
+    const double sp = s[p];
+    const bool live = sp > JAC_REFINE_NULL * s1;
+    Ut[e] = live ? W[i * n + p] / sp : 0.0;
+    VHt[k * n + i] = V[i * n + p];
+    if (i == 0) {
+      S[k] = sp;
+      zero[k] = live ? 0 : 1;
+    }
+  }
+}
+
+// Orthonormal completion of the zero columns of Ut (null singular values, or
+// columns that the orthonormalisation found dependent): column k becomes
+// e_r - Ut (Ut^T e_r), twice, normalised, for the first row r (from k on,
+// cyclically) whose projection keeps at least half its norm.  One CTA; only
+// exactly rank-deficient problems have such columns.
+__global__ void __launch_bounds__(256) rf_complete_kernel(double* __restrict__ Ut, int n,
+                                                          const int* __restrict__ zero) {
+  extern __shared__ double cw[];  // [n] coefficients, [n] the new column
+  double* coef = cw;
+  double* col = cw + n;
+  __shared__ double red[8];
+  __shared__ double tot;
+  for (int k = 0; k < n; ++k) {
+    if (!zero[k]) continue;
+    for (int tries = 0; tries < n; ++tries) {
+      const int r = (k + tries) % n;
+      for (int i = threadIdx.x; i < n; i += blockDim.x) col[i] = (i == r) ? 1.0 : 0.0;
+      __syncthreads();
+      for (int pass = 0; pass < 2; ++pass) {
+        // coef_l = col . Ut e_l (the columns not yet completed are zero)
+        for (int l = threadIdx.x; l < n; l += blockDim.x) {
+          double a = 0.0;
+          for (int i = 0; i < n; ++i) a = fma(Ut[(int64_t)i * n + l], col[i], a);
+          coef[l] = a;
+        }
+        __syncthreads();
+        for (int i = threadIdx.x; i < n; i += blockDim.x) {
+          double a = col[i];
+          for (int l = 0; l < n; ++l) a = fma(-Ut[(int64_t)i * n + l], coef[l], a);
+          col[i] = a;
+        }
+        __syncthreads();
+      }
+      double q = 0.0;
+      for (int i = threadIdx.x; i < n; i += blockDim.x) q = fma(col[i], col[i], q);
+      q = warp_sum(q);
+      if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = q;
+      __syncthreads();
+      if (threadIdx.x == 0) {
+        double t = 0.0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += red[w];
+        tot = t;
+      }
+      __syncthreads();
+      if (tot >= 0.25) {
+        const double f = 1.0 / sqrt(tot);
+        for (int i = threadIdx.x; i < n; i += blockDim.x) Ut[(int64_t)i * n + k] = col[i] * f;
+        __syncthreads();
+        break;
+      }
+      __syncthreads();
+    }
+  }
+}
+
+__global__ void rf_info_kernel(int* info, int slot, int v) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) info[slot] = v;
+}
+
+struct RefineBufs {
+  double *Bp, *Dl, *W, *C, *P, *G, *E, *s, *cmax;
+  float *a3, *b3, *bt3, *t2, *om, *E32;
+  int* perm;
+  int* zero;  // [n] 1 = column of Ut to be completed
+};
+
+static void carve_refine(Arena& ws, RefineBufs& b, int n) {
+  const size_t nn = (size_t)n * n;
+  b.Bp = ws.take<double>(nn);
+  b.Dl = ws.take<double>(nn);
+  b.W = ws.take<double>(nn);
+  b.C = ws.take<double>(nn);
+  b.P = ws.take<double>(nn);
+  b.G = ws.take<double>(nn);
+  b.E = ws.take<double>(nn);
+  b.s = ws.take<double>(n);
+  b.cmax = ws.take<double>(2);  // max C_ii, the step's scale
+  b.a3 = ws.take<float>(3 * nn);
+  b.b3 = ws.take<float>(3 * nn);
+  b.bt3 = ws.take<float>(3 * nn);
+  b.t2 = ws.take<float>(2 * nn);
+  b.om = ws.take<float>(nn);
+  b.E32 = ws.take<float>(nn);
+  b.perm = ws.take<int>(n);
+  b.zero = ws.take<int>(n);
+}
+
+// gemm_tn_df (C = A^T B, K x n operands) whose row-chunk partials go back to
+// the arena after the call
+static int rf_prod(const float* A, const float* B, double* C, int n, int64_t K, Arena& ws,
+                   cudaStream_t st) {
+  const size_t mark = ws.off;
+  const int r = gemm_tn_df(A, n, B, n, C, n, n, n, K, ws, st);
+  ws.off = mark;
+  return r;
+}
+
+static int rf_grid(int64_t nn) {
+  return (int)std::max<int64_t>(1, std::min<int64_t>(cdiv(nn, 256), (int64_t)num_sms() * 16));
+}
+
+// Graded orthonormalisation of X's columns in their order: the first-order
+// Gram-Schmidt step X <- X - X triu(X^T X, 1) (column k loses its components
+// along the columns before it; the leading columns are not rotated), then
+// every column to unit norm.  Quadratic in the departure from
+// orthonormality, like Newton-Schulz, but the accurate leading columns keep
+// their directions (the symmetric polar step would spread the small columns'
+// errors onto them).
+static int rf_graded(double* X, int n, RefineBufs& b, Arena& ws, cudaStream_t st) {
+  const int64_t nn = (int64_t)n * n;
+  const int eg = rf_grid(nn);
+  rf_split3_kernel<<<eg, 256, 0, st>>>(X, nn, b.a3, b.b3);
+  PLOM_CHECK_LAUNCH();
+  PLOM_TRY(rf_prod(b.a3, b.b3, b.G, n, 3 * (int64_t)n, ws, st));  // X^T X
+  rf_upper_kernel<<<eg, 256, 0, st>>>(b.G, n, b.E32);
+  PLOM_CHECK_LAUNCH();
+  rf_tsplit_kernel<<<eg, 256, 0, st>>>(X, n, 2, b.t2);
+  PLOM_CHECK_LAUNCH();
+  PLOM_TRY(rf_prod(b.t2, b.E32, b.P, n, n, ws, st));  // X F (the coefficients are small)
+  rf_sub_kernel<<<eg, 256, 0, st>>>(X, b.P, nn);
+  PLOM_CHECK_LAUNCH();
+  rf_colnorm_kernel<<<(unsigned)cdiv(n, 128), 128, 0, st>>>(X, n, b.s);
+  PLOM_CHECK_LAUNCH();
+  rf_colscale_kernel<<<eg, 256, 0, st>>>(X, n, b.s, b.zero);
+  PLOM_CHECK_LAUNCH();
+  return PLOM_OK;
+}
+
+// SVD of the scaled B (Rcat = [Ah; Ah; Al], A = B^T) from the orthonormal
+// starting product Jo: S (scaled), Ut (columns = left vectors), VHt (rows =
+// right vectors)
+static int jacobi_refine(const float* Rcat, const double* Jo, int n, double* S, double* Ut,
+                         double* VHt, int* info, Arena& ws, cudaStream_t st) {
+  RefineBufs b;
+  carve_refine(ws, b, n);
+  const int64_t nn = (int64_t)n * n;
+  if (ws.measuring())  // the largest row-chunk partials of the products (K = 3n)
+    return gemm_tn_df(nullptr, n, nullptr, n, nullptr, n, n, n, 3 * (int64_t)n, ws, st);
+  PLOM_REQUIRE(!ws.overflow(), PLOM_ERR_WORKSPACE, "jacobi refine: workspace too small");
+  const int eg = rf_grid(nn);
+  const int64_t K3 = 3 * (int64_t)n;
+  ProfScope prof("jacobi_refine", st, 2.0 * (7.0 + 8.0 * JAC_REFINE_STEPS) * (double)nn * n, 0.0);
+  // B' = B Jo, fixed; its transposed split for the W updates
+  rf_split3_kernel<<<eg, 256, 0, st>>>(Jo, nn, nullptr, b.b3);
+  PLOM_CHECK_LAUNCH();
+  PLOM_TRY(rf_prod(Rcat, b.b3, b.Bp, n, K3, ws, st));
+  rf_tsplit_kernel<<<eg, 256, 0, st>>>(b.Bp, n, 3, b.bt3);
+  PLOM_CHECK_LAUNCH();
+  PLOM_CHECK_CUDA(cudaMemsetAsync(b.Dl, 0, sizeof(double) * nn, st));
+  PLOM_CHECK_CUDA(cudaMemcpyAsync(b.W, b.Bp, sizeof(double) * nn, cudaMemcpyDeviceToDevice, st));
+  for (int it = 0; it < JAC_REFINE_STEPS; ++it) {
+    // C = W^T W and the angles
+    rf_split3_kernel<<<eg, 256, 0, st>>>(b.W, nn, b.a3, b.b3);
+    PLOM_CHECK_LAUNCH();
+    PLOM_TRY(rf_prod(b.a3, b.b3, b.C, n, K3, ws, st));
+    rf_cmax_kernel<<<1, 256, 0, st>>>(b.C, n, b.cmax);
+    PLOM_CHECK_LAUNCH();
+    rf_omega_kernel<<<eg, 256, 0, st>>>(b.C, n, b.cmax, b.om);
+    PLOM_CHECK_LAUNCH();
+    rf_omnorm_kernel<<<1, 1024, 0, st>>>(b.om, nn, b.cmax + 1);
+    PLOM_CHECK_LAUNCH();
+    rf_omscale_kernel<<<eg, 256, 0, st>>>(b.om, nn, b.cmax + 1);
+    PLOM_CHECK_LAUNCH();
+    // D <- D + Om + D Om
+    rf_tsplit_kernel<<<eg, 256, 0, st>>>(b.Dl, n, 2, b.t2);
+    PLOM_CHECK_LAUNCH();
+    PLOM_TRY(rf_prod(b.t2, b.om, b.P, n, n, ws, st));
+    rf_rotate_kernel<<<eg, 256, 0, st>>>(b.Dl, b.om, b.P, nn);
+    PLOM_CHECK_LAUNCH();
+    for (int k = 0; k < JAC_REFINE_NS; ++k) {
+      // E = -(D + D^T) - D^T D;  D <- D + (E + D E) / 2
+      rf_split3_kernel<<<eg, 256, 0, st>>>(b.Dl, nn, b.a3, nullptr);
+      PLOM_CHECK_LAUNCH();
+      PLOM_TRY(rf_prod(b.a3, b.a3, b.G, n, n, ws, st));
+      rf_ns_residual_kernel<<<eg, 256, 0, st>>>(b.Dl, b.G, n, b.E, b.E32);
+      PLOM_CHECK_LAUNCH();
+      rf_tsplit_kernel<<<eg, 256, 0, st>>>(b.Dl, n, 2, b.t2);
+      PLOM_CHECK_LAUNCH();
+      PLOM_TRY(rf_prod(b.t2, b.E32, b.P, n, n, ws, st));
+      rf_ns_update_kernel<<<eg, 256, 0, st>>>(b.Dl, b.E, b.P, nn);
+      PLOM_CHECK_LAUNCH();
+    }
+    // W = B' + B' D
+    rf_split3_kernel<<<eg, 256, 0, st>>>(b.Dl, nn, nullptr, b.b3);
+    PLOM_CHECK_LAUNCH();
+    PLOM_TRY(rf_prod(b.bt3, b.b3, b.P, n, K3, ws, st));
+    rf_add_kernel<<<eg, 256, 0, st>>>(b.W, b.Bp, b.P, nn);
+    PLOM_CHECK_LAUNCH();
+  }
+  // V = Jo + Jo D (into C)
+  rf_tsplit_kernel<<<eg, 256, 0, st>>>(Jo, n, 3, b.bt3);
+  PLOM_CHECK_LAUNCH();
+  PLOM_TRY(rf_prod(b.bt3, b.b3, b.P, n, K3, ws, st));  // b3 still holds D's split
+  rf_add_kernel<<<eg, 256, 0, st>>>(b.C, Jo, b.P, nn);
+  PLOM_CHECK_LAUNCH();
+  rf_colnorm_kernel<<<(unsigned)cdiv(n, 128), 128, 0, st>>>(b.W, n, b.s);
+  PLOM_CHECK_LAUNCH();
+  rf_order_kernel<<<(unsigned)cdiv(n, 128), 128, 0, st>>>(b.s, n, b.perm);
+  PLOM_CHECK_LAUNCH();
+  rf_output_kernel<<<eg, 256, 0, st>>>(b.W, b.C, b.s, b.perm, n, S, Ut, VHt, b.zero);
+  PLOM_CHECK_LAUNCH();
+  for (int k = 0; k < JAC_REFINE_GS; ++k) PLOM_TRY(rf_graded(Ut, n, b, ws, st));
+  rf_complete_kernel<<<1, 256, sizeof(double) * 2 * n, st>>>(Ut, n, b.zero);
+  PLOM_CHECK_LAUNCH();
+  rf_info_kernel<<<1, 1, 0, st>>>(info, ST_REFINE, JAC_REFINE_STEPS);
+  PLOM_CHECK_LAUNCH();
+  return PLOM_OK;
+}
+
+// Real problems from n = 512 on at the mixed form's tolerance, up to the size
+// whose FP32 block kernel rows fit in shared memory (the double-float kernel's
+// bound, kept for the larger sizes' workspace estimates).
 static bool use_pre32(int n, double tol) {
   return n >= JAC_PRE32_MIN_N && tol >= JAC_DF_TOL &&
          (size_t)16 * jac_pitch(n, 0) * sizeof(double) <= JAC_BLOCK_SMEM_MAX;
 }
 
-// SVD of B = A^T (At holds B, A is B^T) through the FP32 pre-sweeps:
-// B = Ut diag(S) VHt, VHt = (Jo V')^T.
+// SVD of B = A^T (At holds B, A is B^T) through the FP32 pre-sweeps and the
+// refinement of their rotation product: B = Ut diag(S) VHt.
 static int jacobi_pre32(const double* A, const double* At, int n, double tol, double* S,
                         double* Ut, double* VHt, int* info, Arena& ws, cudaStream_t st) {
+  (void)tol;
   const size_t nn = (size_t)n * n;
   Jac32State j32;
   j32.pitch = ((int64_t)n + 3) / 4 * 4;
@@ -2047,14 +2508,15 @@ static int jacobi_pre32(const double* A, const double* At, int n, double tol, do
   float* C = ws.take<float>(nn);
   double* G = ws.take<double>(nn);
   double* Jo = ws.take<double>(nn);
-  float* Jcat = ws.take<float>(3 * nn);
   float* Rcat = ws.take<float>(3 * nn);
-  double* Bp = ws.take<double>(nn);
-  JacState js;
-  carve_jac(ws, js, n, 1, 0);
-  if (ws.measuring()) {  // the partials of the two double-float products
+  const size_t mark = ws.off;
+  if (ws.measuring()) {  // the partials of G's product, then the refinement's needs
     PLOM_TRY(gemm_tn_df(nullptr, n, nullptr, n, nullptr, n, n, n, n, ws, st));
-    return gemm_tn_df(nullptr, n, nullptr, n, nullptr, n, n, n, 3 * (int64_t)n, ws, st);
+    size_t need = ws.off;
+    ws.off = mark;
+    PLOM_TRY(jacobi_refine(nullptr, nullptr, n, nullptr, nullptr, nullptr, nullptr, ws, st));
+    ws.off = std::max(need, ws.off);
+    return PLOM_OK;
   }
   PLOM_REQUIRE(!ws.overflow(), PLOM_ERR_WORKSPACE, "jacobi: workspace too small");
   {
@@ -2074,15 +2536,13 @@ static int jacobi_pre32(const double* A, const double* At, int n, double tol, do
   }
   const int eg = (int)std::max<int64_t>(1, std::min<int64_t>(cdiv((int64_t)nn, 256),
                                                              (int64_t)num_sms() * 16));
-  PLOM_TRY(gemm_tn_df(J32, n, J32, n, G, n, n, n, n, ws, st));  // G = J32^T J32
+  PLOM_TRY(rf_prod(J32, J32, G, n, n, ws, st));  // G = J32^T J32
   pre32_residual_kernel<<<eg, 256, 0, st>>>(G, E, n);
   PLOM_CHECK_LAUNCH();
   PLOM_TRY((gemm_nn<float, float, float, float>(J32, n, E, n, C, n, n, n, n, st)));
-  pre32_operands_kernel<<<eg, 256, 0, st>>>(J32, C, A, j32.amax, Jo, Jcat, Rcat, n);
+  pre32_operands_kernel<<<eg, 256, 0, st>>>(J32, C, A, j32.amax, Jo, nullptr, Rcat, n);
   PLOM_CHECK_LAUNCH();
-  PLOM_TRY(gemm_tn_df(Rcat, n, Jcat, n, Bp, n, n, n, 3 * (int64_t)n, ws, st));  // B Jo, scaled
-  js.V0 = Jo;
-  PLOM_TRY(jacobi_launch(Bp, n, 1, 0, js, tol, S, Ut, VHt, info, st));
+  PLOM_TRY(jacobi_refine(Rcat, Jo, n, S, Ut, VHt, info, ws, st));
   pre32_unscale_kernel<<<1, 256, 0, st>>>(S, n, j32.amax);
   PLOM_CHECK_LAUNCH();
   return PLOM_OK;

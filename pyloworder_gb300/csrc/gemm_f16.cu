@@ -1029,42 +1029,88 @@ __global__ void __launch_bounds__(320, 1)
 
 // G[i][j] = sum over the 4,096-row sub-chunk slabs (fixed order, double-float)
 // / (s_i s_j), taken from the upper triangle (i <= j) and mirrored; the
-// diagonal from the band tiles' FP64 slabs
-__global__ void gram16w_reduce_kernel(const float* __restrict__ part,
-                                      const double* __restrict__ diagp, int N, int tn, int tn2,
-                                      int nsubs, const float* __restrict__ s,
-                                      double* __restrict__ G, int batch, int ld, int accumulate) {
-  const int64_t total = (int64_t)N * N * batch;
+// diagonal from the band tiles' FP64 slabs.  One thread per 4 consecutive
+// columns of a tile row: 16-byte loads down the slabs, eight in flight, each
+// of the 4 sums in sub-chunk order (the same order for every call).
+constexpr int GWR_UNROLL = 16;
+__global__ void __launch_bounds__(256) gram16w_reduce_kernel(const float* __restrict__ part,
+                                                             const double* __restrict__ diagp,
+                                                             int N, int tn, int tn2, int nsubs,
+                                                             const float* __restrict__ s,
+                                                             double* __restrict__ G, int batch,
+                                                             int ld, int accumulate) {
   const int ntiles = gw_tiles_sym(tn, tn2);
-  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < total;
-       e += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t pb = e / ((int64_t)N * N);
-    const int64_t r = e - pb * N * N;
-    const int i = (int)(r / N), j = (int)(r % N);
-    if (i > j) continue;  // the upper triangle, written to both halves
-    const int a = i, b = j;
-    const int ti = a / 128, tj = b / 256;
-    int tile = 0;
-    for (int t = 0; t < ti; ++t) tile += tn2 - (t >> 1);
-    tile += tj - (ti >> 1);
+  const int64_t units = (int64_t)batch * ntiles * 128 * 64;
+  const int64_t slab_elems = 128 * 256;
+  for (int64_t u = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; u < units;
+       u += (int64_t)gridDim.x * blockDim.x) {
+    const int q = (int)(u & 63);
+    const int row = (int)((u >> 6) & 127);
+    const int64_t tb = u >> 13;
+    const int tile = (int)(tb % ntiles);
+    const int64_t pb = tb / ntiles;
+    // tile -> (ti, tj): row block ti holds tn2 - ti / 2 tiles, from tj = ti / 2
+    int ti = 0, rest = tile;
+    while (rest >= tn2 - (ti >> 1)) {
+      rest -= tn2 - (ti >> 1);
+      ++ti;
+    }
+    const int tj = (ti >> 1) + rest;
+    const int a = ti * 128 + row, b0 = tj * 256 + 4 * q;
+    if (a >= N || b0 >= N || b0 + 3 < a) continue;
     const int64_t slab = (pb * ntiles + tile) * (int64_t)nsubs;
-    double v;
-    if (a == b) {
-      const double* p = diagp + slab * 128 + (a - ti * 128);
-      float2 acc = make_float2(0.f, 0.f);
-      for (int c = 0; c < nsubs; ++c) acc = dw_add(acc, dw_from_double(p[(int64_t)c * 128]));
-      v = dw_value(acc);
-    } else {
-      const float* p = part + slab * 128 * 256 + (int64_t)(a - ti * 128) * 256 + (b - tj * 256);
-      float2 acc = make_float2(0.f, 0.f);
-      for (int c = 0; c < nsubs; ++c) acc = dw_add(acc, make_float2(p[(int64_t)c * 128 * 256], 0.f));
-      v = dw_value(acc);
+    const float4* p = reinterpret_cast<const float4*>(part + slab * slab_elems + (int64_t)row * 256 +
+                                                      4 * q);
+    float2 acc[4];
+#pragma unroll
+    for (int e = 0; e < 4; ++e) acc[e] = make_float2(0.f, 0.f);
+    for (int c0 = 0; c0 < nsubs; c0 += GWR_UNROLL) {
+      float4 v[GWR_UNROLL];
+#pragma unroll
+      for (int k = 0; k < GWR_UNROLL; ++k)
+        v[k] = (c0 + k < nsubs) ? __ldcs(p + (int64_t)(c0 + k) * (slab_elems / 4))
+                                : make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+      for (int k = 0; k < GWR_UNROLL; ++k) {
+        if (c0 + k >= nsubs) break;
+        acc[0] = dw_add(acc[0], make_float2(v[k].x, 0.f));
+        acc[1] = dw_add(acc[1], make_float2(v[k].y, 0.f));
+        acc[2] = dw_add(acc[2], make_float2(v[k].z, 0.f));
+        acc[3] = dw_add(acc[3], make_float2(v[k].w, 0.f));
+      }
     }
     const float* sp = s + pb * ld;
-    v /= ((double)sp[i] * (double)sp[j]);
-    const int64_t e2 = pb * N * N + (int64_t)j * N + i;
-    G[e] = accumulate ? G[e] + v : v;
-    if (e2 != e) G[e2] = accumulate ? G[e2] + v : v;
+    const double sa = (double)sp[a];
+#pragma unroll
+    for (int e = 0; e < 4; ++e) {
+      const int b = b0 + e;
+      if (b >= N || b < a) continue;
+      double v;
+      if (b == a) {
+        // the diagonal's FP64 slabs, in the same order, loads batched
+        const double* dp = diagp + slab * 128 + row;
+        float2 d = make_float2(0.f, 0.f);
+        for (int c0 = 0; c0 < nsubs; c0 += GWR_UNROLL) {
+          double dv[GWR_UNROLL];
+#pragma unroll
+          for (int k = 0; k < GWR_UNROLL; ++k)
+            dv[k] = (c0 + k < nsubs) ? dp[(int64_t)(c0 + k) * 128] : 0.0;
+#pragma unroll
+          for (int k = 0; k < GWR_UNROLL; ++k) {
+            if (c0 + k >= nsubs) break;
+            d = dw_add(d, dw_from_double(dv[k]));
+          }
+        }
+        v = dw_value(d);
+      } else {
+        v = dw_value(acc[e]);
+      }
+      v /= sa * (double)sp[b];
+      const int64_t e1 = pb * N * N + (int64_t)a * N + b;
+      const int64_t e2 = pb * N * N + (int64_t)b * N + a;
+      G[e1] = accumulate ? G[e1] + v : v;
+      if (e2 != e1) G[e2] = accumulate ? G[e2] + v : v;
+    }
   }
 }
 
@@ -1245,6 +1291,13 @@ __global__ void __launch_bounds__(ApplyWarps<TN>::THREADS, 1)
   auto apply_kend = [&](int cb) -> int {
     return upper ? min(kblocks, (cb + 1) * (TN / A_BK)) : kblocks;
   };
+  // TN = 256 with an upper-triangular W: the W rows of the last 128 K of
+  // column block cb, [cb TN + 128, (cb + 1) TN), are zero left of the
+  // diagonal, so those K blocks run 128-wide products on the right half only
+  // (the triangle at 128-column granularity, as with TN = 128)
+  auto apply_khalf = [&](int cb) -> int {
+    return (TN == 256 && upper) ? (cb * TN + 128) / A_BK : 0x7fffffff;
+  };
   if (launch_aborted(err)) return;
 
   if (threadIdx.x == 0) {
@@ -1284,7 +1337,7 @@ __global__ void __launch_bounds__(ApplyWarps<TN>::THREADS, 1)
         const int64_t rt = t - pb * row_tiles * col_tiles;
         const int rb = (int)(rt / col_tiles), cb = (int)(rt % col_tiles);
         const int ya = (int)(pb * mp + (int64_t)rb * 128), yb = (int)(pb * k + (int64_t)cb * TN);
-        const int kend = apply_kend(cb);
+        const int kend = apply_kend(cb), khalf = apply_khalf(cb);
         for (int kb = 0; kb < kend; ++kb, ++g) {
           const int s = (int)(g % A_STAGES);
           const uint32_t ph = (uint32_t)(g / A_STAGES) & 1u;
@@ -1293,13 +1346,17 @@ __global__ void __launch_bounds__(ApplyWarps<TN>::THREADS, 1)
             break;
           }
           const uint32_t st = base + s * A_STAGE;
-          mbar_expect_tx(&full_bar[s], A_STAGE);
+          // K blocks from khalf on feed only the right 128 columns of the tile:
+          // the left half of their W rows is not loaded
+          const int h0 = kb >= khalf ? 1 : 0;
+          mbar_expect_tx(&full_bar[s], A_STAGE - 2u * (uint32_t)h0 * A_TILE);
           tma_load_3d(st, &tmA, kb * A_BK, ya, 0, &full_bar[s]);
           tma_load_3d(st + A_TILE, &tmA, kb * A_BK, ya, 1, &full_bar[s]);
-          // B: TN rows of the W copy in boxes of 128 rows (the K-major SW128
+          // B: TN rows of the W copy in boxes of 128 rows (the K-major swizzled
           // layout of a 256-row tile is two 128-row tiles back to back)
 #pragma unroll
           for (int h = 0; h < TN / 128; ++h) {
+            if (h < h0) continue;
             tma_load_3d(st + 2 * A_TILE + h * A_TILE, &tmB, kb * A_BK, yb + 128 * h, 0, &full_bar[s]);
             tma_load_3d(st + 2 * A_TILE + B_TILE + h * A_TILE, &tmB, kb * A_BK, yb + 128 * h, 1,
                         &full_bar[s]);
@@ -1325,7 +1382,7 @@ __global__ void __launch_bounds__(ApplyWarps<TN>::THREADS, 1)
         fence_after();
         const uint32_t dmain = tmem + (uint32_t)(b * 2 * TN);
         const uint32_t dcorr = dmain + (uint32_t)TN;
-        const int kend = apply_kend((int)(t % col_tiles));
+        const int kend = apply_kend((int)(t % col_tiles)), khalf = apply_khalf((int)(t % col_tiles));
         for (int kb = 0; kb < kend; ++kb, ++g) {
           const int s = (int)(g % A_STAGES);
           const uint32_t ph = (uint32_t)(g / A_STAGES) & 1u;
@@ -1335,6 +1392,24 @@ __global__ void __launch_bounds__(ApplyWarps<TN>::THREADS, 1)
           }
           fence_after();
           const uint32_t st = base + s * A_STAGE;
+          if (TN == 256 && kb >= khalf) {
+            // right half: B rows 128..255 (the second 128-row box of each
+            // plane), accumulators at column offset 128; kb > 0 here
+            constexpr uint32_t idesc_h = idesc_f16(128, 128, 0, 0);
+#pragma unroll
+            for (int kk = 0; kk < A_BK / 16; ++kk) {
+              const uint32_t adv = (uint32_t)kk * 32u;
+              const uint64_t dAH = desc_kmajor<A_BK>(st + adv);
+              const uint64_t dAL = desc_kmajor<A_BK>(st + A_TILE + adv);
+              const uint64_t dBH = desc_kmajor<A_BK>(st + 3 * A_TILE + adv);
+              const uint64_t dBL = desc_kmajor<A_BK>(st + 3 * A_TILE + B_TILE + adv);
+              mma_f16(dmain + 128u, dAH, dBH, idesc_h, 1u);
+              mma_f16(dcorr + 128u, dAH, dBL, idesc_h, 1u);
+              mma_f16(dcorr + 128u, dAL, dBH, idesc_h, 1u);
+            }
+            mma_commit(&empty_bar[s]);
+            continue;
+          }
 #pragma unroll
           for (int kk = 0; kk < A_BK / 16; ++kk) {
             const uint32_t adv = (uint32_t)kk * 32u;  // 16 fp16 along K
@@ -1782,8 +1857,9 @@ static int gram_packed_wide(const Packed& p, double* G, int* err, Arena& ws, cud
   hp::gram16w_kernel<true><<<(unsigned)(batch * tiles * chunks_eff), 320, hp::GW_SMEM, st>>>(
       tm, tm, m, tn, tn2, rpc, chunks_eff, subs_per_chunk, nsubs, part, diagp, err, p.mp);
   PLOM_CHECK_LAUNCH();
-  const int64_t total = N * N * batch;
-  const int blocks = (int)std::min<int64_t>(cdiv(total, 256), (int64_t)num_sms() * 16);
+  const int64_t units = (int64_t)batch * hp::gw_tiles_sym(tn, tn2) * 128 * 64;
+  // two resident blocks per SM (96 registers a thread), a grid-stride loop
+  const int blocks = (int)std::min<int64_t>(cdiv(units, 256), (int64_t)num_sms() * 2);
   ProfScope prof_r("gram_reduce", st, 0.0, 4.0 * (double)slabs * 128 * 256);
   hp::gram16w_reduce_kernel<<<blocks, 256, 0, st>>>(part, diagp, (int)N, tn, tn2, nsubs, p.scale,
                                                     G, (int)batch, (int)p.ld, accumulate ? 1 : 0);
@@ -1927,10 +2003,10 @@ int apply_packed(const Packed& p, const double* W, int64_t ldw, int64_t k, float
                  int64_t cstride, bool upper) {
   const int64_t m = p.m, batch = p.batch;
   const int64_t ldk = p.ld;  // K extent of the W copies (= packed pitch of the input)
-  // output tile width (see ApplyCfg): 256 for dense W wider than 128 columns;
-  // an upper-triangular W keeps 128-wide column tiles, whose K ranges follow
-  // the triangle more closely (256-wide ones do 11 % more products at k = 1024)
-  const int TN = (k > 128 && !(upper && k == p.N)) ? 256 : 128;
+  // output tile width (see ApplyCfg): 256 for W wider than 128 columns (an
+  // upper-triangular W follows its triangle at 128-column granularity in
+  // either width)
+  const int TN = k > 128 ? 256 : 128;
   const int64_t col_tiles = cdiv(k, TN);
   const int fstride = (int)(col_tiles * TN);
   __half* bhi = ws.take<__half>((size_t)(2 * batch * k * ldk));

@@ -129,9 +129,10 @@ def test_mixed_mean_removed_u_orthonormal():
 @pytest.mark.parametrize("n", [1024, 517])
 def test_mixed_large_n_fp32_presweeps(n):
     """512 <= n <= 1600 in the mixed form: the SVD of R starts with FP32 Jacobi sweeps,
-    re-orthonormalises their rotation product and finishes with double-float
-    sweeps from it.  The result must match the plain FP64 form within the
-    mixed-form tolerances, with orthonormal U and V (n = 517: odd row
+    re-orthonormalises their rotation product and refines it with matrix
+    products in double-float sums (simultaneous Jacobi angles plus
+    Newton-Schulz steps).  The result must match the plain FP64 form within
+    the mixed-form tolerances, with orthonormal U and V (n = 517: odd row
     quarters take the one-row-per-lane loops)."""
     from pyloworder_gb300 import _lib as L
     from pyloworder_gb300 import datagen
@@ -141,8 +142,8 @@ def test_mixed_large_n_fp32_presweeps(n):
     Y, _, _ = P.vmmath.remove_mean_device(X, n)
     U, S, V = P.vmmath.tsqr_svd_device(Y, n, "mixed")
     info = list(L.last_info)
-    print(f"FP32 sweeps {info[4]}, double-float sweeps {info[2]}")
-    assert info[4] > 0  # the FP32 phase ran
+    print(f"FP32 sweeps {info[4]}, refinement steps {info[5]}")
+    assert info[4] > 0 and info[5] > 0  # the FP32 phase and the refinement ran
     Ur, Sr, _ = P.vmmath.tsqr_svd_device(Y.double(), n, "fp64")
     S64, Sr64 = S.double().cpu().numpy(), Sr.cpu().numpy()
     assert sigma_rel(S64, Sr64, k) < 1e-5
