@@ -1515,19 +1515,31 @@ __global__ void __launch_bounds__(512, 1)
 }
 
 // ---------------------------------------------------------------------------
-// FP32 pre-sweeps of large real Jacobi problems at the mixed form's tolerance.
-// The block schedule of jacobi_block_df16_kernel (4-column blocks, one CTA
-// per block pair, 8 rows of At and Vt in shared memory, one grid barrier per
-// block step) on FP32 rows with explicit (c, s) rotations: a dot costs one
-// FMA per row instead of a double-float accumulation, a rotation four FMAs.
-// The sweeps stop when every pair is orthogonal to `tol` (at FP32 level, far
-// above the final tolerance) or after max_sweeps.  Output: the rotation
-// product J32 (n x n row-major FP32, J32 = the accumulated V); the host
-// re-orthonormalises it to Jo and hands B Jo to the double-float kernel,
-// whose accumulated rotations start from Jo (jacobi_pre32).
+// FP32 sweeps of large real Jacobi problems at the mixed form's tolerance.
+// Block schedule with 8-column blocks: one CTA per pair of blocks holds their
+// 16 rows of At and Vt in shared memory for one round-robin block step (the
+// 64 cross rotations in 8 rounds of 8 disjoint pairs, plus the 28 + 28
+// rotations inside the two blocks at the first step of a sweep), one grid
+// barrier per block step (127 per sweep at n = 1,024, half as many as with
+// 4-column blocks, for the same number of rounds); two warps per pair, each
+// over half the rows.  Explicit (c, s) rotations: a dot costs one FMA per
+// row, a rotation four FMAs.  The sweeps stop when every pair is orthogonal
+// to `tol`, when the pairs above the floor have converged (see
+// JAC_PRE32_TSTOP), or after max_sweeps.  Output: the rotation product J32
+// (n x n row-major FP32, J32 = the accumulated V); the host
+// re-orthonormalises it to Jo and refines the SVD of B Jo (jacobi_pre32).
 // ---------------------------------------------------------------------------
 constexpr int JAC_PRE32_MIN_N = 512;       // real, batch 1, n from here on (see use_pre32)
+constexpr int J32B = 8;                    // columns per block of the FP32 kernel
 constexpr float JAC_PRE32_TOL = 2e-6f;     // pair orthogonality of the FP32 phase
+// The FP32 phase also ends after a sweep in which every rotated pair with a
+// column above JAC_PRE32_FLOOR of the largest turned by less than
+// JAC_PRE32_TSTOP: those pairs are then well inside the refinement's
+// quadratic range, and the pairs of smaller columns (a noise floor, which
+// the Jacobi ordering keeps rotating for several more sweeps) are only used
+// at the FP32 phase's accuracy.  The floor matches the refinement's.
+constexpr float JAC_PRE32_FLOOR = 1e-5f;
+constexpr float JAC_PRE32_TSTOP = 1e-4f;
 constexpr int JAC_PRE32_MAX_SWEEPS = 30;
 
 struct Jac32State {
@@ -1535,6 +1547,8 @@ struct Jac32State {
   float* Vt;      // n x pitch: rows = columns of the rotation product
   float* nrm2;    // n squared column norms; < 0 = recompute
   int* counts;    // [JACOBI_MAX_SWEEPS] rotations per sweep
+  unsigned* cmax; // [JACOBI_MAX_SWEEPS] bits of the largest squared column norm (sweep start)
+  unsigned* tmax; // [JACOBI_MAX_SWEEPS] bits of the largest |t| of the pairs above the floor
   unsigned long long* amax;  // bits of max |b_ij|
   int64_t pitch;  // floats per row: n rounded up to 4 (16-byte bulk copies)
 };
@@ -1612,19 +1626,19 @@ __device__ __forceinline__ void f32_rotate(float* x, float* y, int h0, int h1, i
 __global__ void __launch_bounds__(512, 1)
     jacobi_block_f32_kernel(const double* __restrict__ B, int n, Jac32State js, float tol,
                             int max_sweeps, float* __restrict__ J, int* info) {
-  extern __shared__ __align__(16) float jsm32[];  // [8][pitch] At rows, [8][pitch] Vt rows
-  __shared__ float snrm[8];
-  __shared__ float red[4][4][3];  // [pair][quarter][g a2 b2]
-  __shared__ int scol[8];
+  extern __shared__ __align__(16) float jsm32[];  // [2 J32B][pitch] At rows, then Vt rows
+  __shared__ float snrm[2 * J32B];
+  __shared__ float red[J32B][2][3];  // [pair][row half][g a2 b2]
+  __shared__ int scol[2 * J32B];
   __shared__ __align__(8) uint64_t bar;
   __shared__ int abort_sh;
   cg::grid_group grid = cg::this_grid();
   const int64_t P = js.pitch;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const int pk = warp >> 2, qtr = warp & 3;  // pair slot, row quarter
-  const int h0 = n * qtr / 4, h1 = n * (qtr + 1) / 4;
+  const int pk = warp >> 1, qtr = warp & 1;  // pair slot, row half
+  const int h0 = n * qtr / 2, h1 = n * (qtr + 1) / 2;
   float* cA = jsm32;
-  float* cV = jsm32 + 8 * P;
+  float* cV = jsm32 + 2 * J32B * P;
   const uint32_t bar_s = (uint32_t)__cvta_generic_to_shared(&bar);
   if (threadIdx.x == 0) {
     asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar_s));
@@ -1635,7 +1649,11 @@ __global__ void __launch_bounds__(512, 1)
   const int64_t gtid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   const int64_t gthreads = (int64_t)gridDim.x * blockDim.x;
   if (gtid == 0) js.amax[0] = 0ull;
-  if (gtid < JACOBI_MAX_SWEEPS) js.counts[gtid] = 0;
+  if (gtid < JACOBI_MAX_SWEEPS) {
+    js.counts[gtid] = 0;
+    js.cmax[gtid] = 0u;
+    js.tmax[gtid] = 0u;
+  }
   grid.sync();
   {
     unsigned long long mx = 0ull;  // non-negative doubles order as their bits
@@ -1664,13 +1682,19 @@ __global__ void __launch_bounds__(512, 1)
   }
   grid.sync();
 
-  const int nb = (n + 3) / 4;
+  const int nb = (n + J32B - 1) / J32B;
   const int nbp = (nb + (nb & 1) < 2) ? 2 : nb + (nb & 1);  // even, >= 2
   const int bpairs = nbp / 2;
   uint32_t phase = 0;
   int sweep = 0;
   for (; sweep < max_sweeps; ++sweep) {
     int myrot = 0;
+    float mytmax = 0.f;  // |t| of this thread's rotated pairs above the floor
+    // floor from the previous sweep's largest squared column norm (none in
+    // the first sweep)
+    const float floor2 = sweep > 0 ? JAC_PRE32_FLOOR * JAC_PRE32_FLOOR *
+                                         __uint_as_float(js.cmax[sweep - 1])
+                                   : 3.0e38f;
     for (int step = 0; step < nbp - 1; ++step) {
       for (int task = blockIdx.x; task < bpairs; task += gridDim.x) {
         int bi, bj;
@@ -1680,13 +1704,13 @@ __global__ void __launch_bounds__(512, 1)
         if (threadIdx.x == 0 && !abort_sh) {
           asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
           uint32_t bytes = 0;
-          for (int s8 = 0; s8 < 8; ++s8)
-            if (4 * (s8 < 4 ? bi : bj) + (s8 & 3) < n) bytes += 2u * (uint32_t)(P * 4);
+          for (int s8 = 0; s8 < 2 * J32B; ++s8)
+            if (J32B * (s8 < J32B ? bi : bj) + (s8 % J32B) < n) bytes += 2u * (uint32_t)(P * 4);
           asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar_s),
                        "r"(bytes)
                        : "memory");
-          for (int s8 = 0; s8 < 8; ++s8) {
-            const int col = 4 * (s8 < 4 ? bi : bj) + (s8 & 3);
+          for (int s8 = 0; s8 < 2 * J32B; ++s8) {
+            const int col = J32B * (s8 < J32B ? bi : bj) + (s8 % J32B);
             if (col >= n) continue;
             bulk_load((uint32_t)__cvta_generic_to_shared(cA + s8 * P), js.At + (int64_t)col * P,
                       (uint32_t)(P * 4), bar_s);
@@ -1694,8 +1718,8 @@ __global__ void __launch_bounds__(512, 1)
                       (uint32_t)(P * 4), bar_s);
           }
         }
-        if (threadIdx.x < 8) {
-          const int col = 4 * (threadIdx.x < 4 ? bi : bj) + (threadIdx.x & 3);
+        if (threadIdx.x < 2 * J32B) {
+          const int col = J32B * (threadIdx.x < J32B ? bi : bj) + (threadIdx.x % J32B);
           const bool v = col < n;
           scol[threadIdx.x] = v ? col : -1;
           snrm[threadIdx.x] = v ? js.nrm2[col] : 0.f;
@@ -1729,35 +1753,37 @@ __global__ void __launch_bounds__(512, 1)
           continue;
         }
         if (step == 0) {
-          // exact squared norms once per sweep: 2 warps per row
-          const int s8 = warp >> 1, half = warp & 1;
+          // exact squared norms once per sweep: one warp per row
+          const int s16 = warp;
           float acc = 0.f;
-          if (scol[s8] >= 0) {
-            const float* x = cA + s8 * P;
-            for (int i = n * half / 2 + lane; i < n * (half + 1) / 2; i += 32)
-              acc = fmaf(x[i], x[i], acc);
+          if (scol[s16] >= 0) {
+            const float* x = cA + s16 * P;
+            for (int i = lane; i < n; i += 32) acc = fmaf(x[i], x[i], acc);
           }
           acc = warp_sum(acc);
-          if (lane == 0) red[s8 >> 1][(s8 & 1) * 2 + half][0] = acc;
-          __syncthreads();
-          if (threadIdx.x < 8) {
-            const int r8 = threadIdx.x;
-            snrm[r8] = red[r8 >> 1][(r8 & 1) * 2][0] + red[r8 >> 1][(r8 & 1) * 2 + 1][0];
+          if (lane == 0) {
+            snrm[s16] = acc;
+            if (scol[s16] >= 0) atomicMax(&js.cmax[sweep], __float_as_uint(acc));
           }
           __syncthreads();
         }
-        const int nrounds = (step == 0) ? 7 : 4;
+        // rounds: at a sweep's first step the 28 pairs inside each block (7
+        // rounds of the circle method, 4 + 4 pairs), then the 64 cross pairs
+        // (8 rounds of 8: column pk of the first block with column
+        // (pk + u) mod 8 of the second)
+        const int nintra = (step == 0) ? J32B - 1 : 0;
+        const int nrounds = nintra + J32B;
         for (int rd = 0; rd < nrounds; ++rd) {
           int a, c;
-          if (step == 0 && rd < 3) {
-            intra_pair(rd, pk & 1, a, c);
-            const int off = (pk >> 1) * 4;
+          if (rd < nintra) {
+            rr_pair(rd, pk % (J32B / 2), J32B, a, c);
+            const int off = (pk / (J32B / 2)) * J32B;
             a += off;
             c += off;
           } else {
-            const int u = (step == 0) ? rd - 3 : rd;
+            const int u = rd - nintra;
             a = pk;
-            c = 4 + ((pk + u) & 3);
+            c = J32B + ((pk + u) % J32B);
           }
           const bool live = scol[a] >= 0 && scol[c] >= 0;
           float al = snrm[a], be = snrm[c];  // read before the owner updates them
@@ -1772,18 +1798,20 @@ __global__ void __launch_bounds__(512, 1)
             }
           }
           __syncthreads();
-          // every lane of the pair's four warps derives the same (c, s) from
+          // every lane of the pair's two warps derives the same (c, s) from
           // the same sums in the same order; the first warp stores the norms
           float2 cs = make_float2(0.f, 0.f);
           if (live) {
-            const float g = (red[pk][0][0] + red[pk][1][0]) + (red[pk][2][0] + red[pk][3][0]);
-            if (al < 0.f) al = (red[pk][0][1] + red[pk][1][1]) + (red[pk][2][1] + red[pk][3][1]);
-            if (be < 0.f) be = (red[pk][0][2] + red[pk][1][2]) + (red[pk][2][2] + red[pk][3][2]);
+            const float g = red[pk][0][0] + red[pk][1][0];
+            if (al < 0.f) al = red[pk][0][1] + red[pk][1][1];
+            if (be < 0.f) be = red[pk][0][2] + red[pk][1][2];
+            const float big = fmaxf(al, be);
             cs = f32_params(al, be, g, tol);
             if (qtr == 0 && lane == 0) {
               snrm[a] = al;
               snrm[c] = be;
               myrot += cs.x > 0.f ? 1 : 0;
+              if (cs.x > 0.f && big > floor2) mytmax = fmaxf(mytmax, fabsf(cs.y / cs.x));
             }
           }
           if (cs.x > 0.f) {
@@ -1793,7 +1821,7 @@ __global__ void __launch_bounds__(512, 1)
           __syncthreads();
         }
         // rows out (16-byte vectors: the pitch is a multiple of 4 floats)
-        for (int s8 = 0; s8 < 8; ++s8) {
+        for (int s8 = 0; s8 < 2 * J32B; ++s8) {
           const int col = scol[s8];
           if (col < 0) continue;
           float4* ga = reinterpret_cast<float4*>(js.At + (int64_t)col * P);
@@ -1805,14 +1833,17 @@ __global__ void __launch_bounds__(512, 1)
             gv[i] = sv[i];
           }
         }
-        if (threadIdx.x < 8 && scol[threadIdx.x] >= 0) js.nrm2[scol[threadIdx.x]] = snrm[threadIdx.x];
+        if (threadIdx.x < 2 * J32B && scol[threadIdx.x] >= 0)
+          js.nrm2[scol[threadIdx.x]] = snrm[threadIdx.x];
         __syncthreads();
       }
       grid.sync();
     }
     if (lane == 0 && myrot) atomicAdd(&js.counts[sweep], myrot);
+    if (lane == 0 && mytmax > 0.f) atomicMax(&js.tmax[sweep], __float_as_uint(mytmax));
     grid.sync();
     if (js.counts[sweep] == 0) break;
+    if (sweep > 0 && __uint_as_float(js.tmax[sweep]) <= JAC_PRE32_TSTOP) break;
   }
   if (gtid == 0) info[ST_SWEEPS32] = sweep < max_sweeps ? sweep + 1 : sweep;
   // J32 (row-major): column k = row k of Vt
@@ -2117,10 +2148,13 @@ __global__ void rf_cmax_kernel(const double* __restrict__ C, int n, double* __re
 // om (FP32): Om_ij = C_ij / (C_jj - C_ii) with C symmetrised; 0 on the
 // diagonal, where |Om_ij| would exceed JAC_REFINE_MAX_ANGLE and for pairs of
 // columns both below JAC_REFINE_FLOOR of the largest
-__global__ void rf_omega_kernel(const double* __restrict__ C, int n, const double* __restrict__ cmax,
-                                float* __restrict__ om) {
+__global__ void __launch_bounds__(256) rf_omega_kernel(const double* __restrict__ C, int n,
+                                                       const double* __restrict__ cmax,
+                                                       float* __restrict__ om,
+                                                       double* __restrict__ part) {
   const int64_t nn = (int64_t)n * n;
   const double floor2 = JAC_REFINE_FLOOR * JAC_REFINE_FLOOR * cmax[0];
+  double sq = 0.0;
   for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < nn;
        e += (int64_t)gridDim.x * blockDim.x) {
     const int64_t i = e / n, j = e % n;
@@ -2131,19 +2165,33 @@ __global__ void rf_omega_kernel(const double* __restrict__ C, int n, const doubl
       const double d = cj - ci;
       if (fabs(d) * JAC_REFINE_MAX_ANGLE > fabs(c)) o = c / d;
     }
-    om[e] = (float)o;
+    const float of = (float)o;
+    om[e] = of;
+    sq = fma((double)of, (double)of, sq);
+  }
+  // this block's share of ||om||_F^2, warps in a fixed order
+  __shared__ double red[8];
+  sq = warp_sum(sq);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = sq;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int w = 0; w < 8; ++w) t += red[w];
+    part[blockIdx.x] = t;
   }
 }
 
 // om *= min(1, JAC_REFINE_MAX_NORM / ||om||_F): a step that would leave
 // I + D far from orthogonal (many unresolved pairs at the angle bound at
-// once) is shortened so that the Newton-Schulz steps stay convergent.  One
-// block; the sum of squares in a fixed order.
+// once) is shortened so that the Newton-Schulz steps stay convergent.  The
+// sum of squares: per-block partials (rf_omega_kernel), then one block sums
+// them, both in a fixed order.
 constexpr double JAC_REFINE_MAX_NORM = 0.25;
-__global__ void rf_omnorm_kernel(const float* __restrict__ om, int64_t nn, double* __restrict__ g) {
+__global__ void rf_omnorm_kernel(const double* __restrict__ part, int nparts,
+                                 double* __restrict__ g) {
   __shared__ double red[32];
   double v = 0.0;
-  for (int64_t e = threadIdx.x; e < nn; e += blockDim.x) v = fma((double)om[e], (double)om[e], v);
+  for (int e = threadIdx.x; e < nparts; e += blockDim.x) v += part[e];
   v = warp_sum(v);
   if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
   __syncthreads();
@@ -2215,16 +2263,27 @@ __global__ void rf_sub_kernel(double* __restrict__ X, const double* __restrict__
     X[e] -= P[e];
 }
 
-// s[c] = ||X e_c|| (each thread sums one column down the rows: fixed order)
-__global__ void rf_colnorm_kernel(const double* __restrict__ W, int n, double* __restrict__ s) {
-  const int c = blockIdx.x * blockDim.x + threadIdx.x;
-  if (c >= n) return;
+// s[c] = ||X e_c||: 32 columns per block, 8 row groups per column (each
+// thread sums every 8th row of its group in order), the 8 partials combined
+// in a fixed order
+__global__ void __launch_bounds__(256) rf_colnorm_kernel(const double* __restrict__ W, int n,
+                                                         double* __restrict__ s) {
+  __shared__ double red[8][33];
+  const int cl = threadIdx.x & 31, rg = threadIdx.x >> 5;
+  const int c = blockIdx.x * 32 + cl;
   double acc = 0.0;
-  for (int r = 0; r < n; ++r) {
-    const double w = W[(int64_t)r * n + c];
-    acc = fma(w, w, acc);
+  if (c < n)
+    for (int r = rg; r < n; r += 8) {
+      const double w = W[(int64_t)r * n + c];
+      acc = fma(w, w, acc);
+    }
+  red[rg][cl] = acc;
+  __syncthreads();
+  if (rg == 0 && c < n) {
+    double t = 0.0;
+    for (int g = 0; g < 8; ++g) t += red[g][cl];
+    s[c] = sqrt(t);
   }
-  s[c] = sqrt(acc);
 }
 
 // columns of X to unit norm; a column whose norm fell below 1e-3 (it
@@ -2333,7 +2392,7 @@ __global__ void rf_info_kernel(int* info, int slot, int v) {
 }
 
 struct RefineBufs {
-  double *Bp, *Dl, *W, *C, *P, *G, *E, *s, *cmax;
+  double *Bp, *Dl, *W, *C, *P, *G, *E, *s, *cmax, *part;
   float *a3, *b3, *bt3, *t2, *om, *E32;
   int* perm;
   int* zero;  // [n] 1 = column of Ut to be completed
@@ -2350,6 +2409,7 @@ static void carve_refine(Arena& ws, RefineBufs& b, int n) {
   b.E = ws.take<double>(nn);
   b.s = ws.take<double>(n);
   b.cmax = ws.take<double>(2);  // max C_ii, the step's scale
+  b.part = ws.take<double>((size_t)num_sms() * 16);  // per-block sums of squares of the angles
   b.a3 = ws.take<float>(3 * nn);
   b.b3 = ws.take<float>(3 * nn);
   b.bt3 = ws.take<float>(3 * nn);
@@ -2394,7 +2454,7 @@ static int rf_graded(double* X, int n, RefineBufs& b, Arena& ws, cudaStream_t st
   PLOM_TRY(rf_prod(b.t2, b.E32, b.P, n, n, ws, st));  // X F (the coefficients are small)
   rf_sub_kernel<<<eg, 256, 0, st>>>(X, b.P, nn);
   PLOM_CHECK_LAUNCH();
-  rf_colnorm_kernel<<<(unsigned)cdiv(n, 128), 128, 0, st>>>(X, n, b.s);
+  rf_colnorm_kernel<<<(unsigned)cdiv(n, 32), 256, 0, st>>>(X, n, b.s);
   PLOM_CHECK_LAUNCH();
   rf_colscale_kernel<<<eg, 256, 0, st>>>(X, n, b.s, b.zero);
   PLOM_CHECK_LAUNCH();
@@ -2430,9 +2490,9 @@ static int jacobi_refine(const float* Rcat, const double* Jo, int n, double* S, 
     PLOM_TRY(rf_prod(b.a3, b.b3, b.C, n, K3, ws, st));
     rf_cmax_kernel<<<1, 256, 0, st>>>(b.C, n, b.cmax);
     PLOM_CHECK_LAUNCH();
-    rf_omega_kernel<<<eg, 256, 0, st>>>(b.C, n, b.cmax, b.om);
+    rf_omega_kernel<<<eg, 256, 0, st>>>(b.C, n, b.cmax, b.om, b.part);
     PLOM_CHECK_LAUNCH();
-    rf_omnorm_kernel<<<1, 1024, 0, st>>>(b.om, nn, b.cmax + 1);
+    rf_omnorm_kernel<<<1, 1024, 0, st>>>(b.part, eg, b.cmax + 1);
     PLOM_CHECK_LAUNCH();
     rf_omscale_kernel<<<eg, 256, 0, st>>>(b.om, nn, b.cmax + 1);
     PLOM_CHECK_LAUNCH();
@@ -2468,7 +2528,7 @@ static int jacobi_refine(const float* Rcat, const double* Jo, int n, double* S, 
   PLOM_TRY(rf_prod(b.bt3, b.b3, b.P, n, K3, ws, st));  // b3 still holds D's split
   rf_add_kernel<<<eg, 256, 0, st>>>(b.C, Jo, b.P, nn);
   PLOM_CHECK_LAUNCH();
-  rf_colnorm_kernel<<<(unsigned)cdiv(n, 128), 128, 0, st>>>(b.W, n, b.s);
+  rf_colnorm_kernel<<<(unsigned)cdiv(n, 32), 256, 0, st>>>(b.W, n, b.s);
   PLOM_CHECK_LAUNCH();
   rf_order_kernel<<<(unsigned)cdiv(n, 128), 128, 0, st>>>(b.s, n, b.perm);
   PLOM_CHECK_LAUNCH();
@@ -2502,6 +2562,8 @@ static int jacobi_pre32(const double* A, const double* At, int n, double tol, do
   j32.Vt = ws.take<float>((size_t)n * j32.pitch);
   j32.nrm2 = ws.take<float>(n);
   j32.counts = ws.take<int>(JACOBI_MAX_SWEEPS);
+  j32.cmax = ws.take<unsigned>(JACOBI_MAX_SWEEPS);
+  j32.tmax = ws.take<unsigned>(JACOBI_MAX_SWEEPS);
   j32.amax = ws.take<unsigned long long>(1);
   float* J32 = ws.take<float>(nn);
   float* E = ws.take<float>(nn);
@@ -2521,9 +2583,9 @@ static int jacobi_pre32(const double* A, const double* At, int n, double tol, do
   PLOM_REQUIRE(!ws.overflow(), PLOM_ERR_WORKSPACE, "jacobi: workspace too small");
   {
     const void* k = (const void*)jacobi_block_f32_kernel;
-    const size_t smem = (size_t)16 * j32.pitch * sizeof(float);
+    const size_t smem = (size_t)4 * J32B * j32.pitch * sizeof(float);
     PLOM_CHECK_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    const int nb = (n + 3) / 4;
+    const int nb = (n + J32B - 1) / J32B;
     const int nbp = std::max(2, nb + (nb & 1));
     const int blocks = coop_blocks(k, 512, smem, nbp / 2);
     float tolf = JAC_PRE32_TOL;

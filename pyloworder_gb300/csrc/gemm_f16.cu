@@ -463,6 +463,11 @@ __device__ __forceinline__ float2 dw_add(float2 x, float2 y) {
   const float2 v = dw_fast_two_sum(s.x, s.y + t.x);
   return dw_fast_two_sum(v.x, t.y + v.y);
 }
+// x + y for a double-float x and an FP32 y
+__device__ __forceinline__ float2 dw_add_f(float2 x, float y) {
+  const float2 s = dw_two_sum(x.x, y);
+  return dw_fast_two_sum(s.x, s.y + x.y);
+}
 __device__ __forceinline__ float2 dw_from_double(double d) {
   const float h = __double2float_rn(d);
   return make_float2(h, __double2float_rn(d - (double)h));
@@ -1030,8 +1035,10 @@ __global__ void __launch_bounds__(320, 1)
 // G[i][j] = sum over the 4,096-row sub-chunk slabs (fixed order, double-float)
 // / (s_i s_j), taken from the upper triangle (i <= j) and mirrored; the
 // diagonal from the band tiles' FP64 slabs.  One thread per 4 consecutive
-// columns of a tile row: 16-byte loads down the slabs, eight in flight, each
-// of the 4 sums in sub-chunk order (the same order for every call).
+// columns of a tile row: 16-byte loads down the slabs, sixteen in flight;
+// each batch of 16 slabs is summed in FP32 and added to a double-float sum,
+// in sub-chunk order (the same order for every call; the slabs' own FP32
+// sums over 4,096 rows carry the larger error).
 constexpr int GWR_UNROLL = 16;
 __global__ void __launch_bounds__(256) gram16w_reduce_kernel(const float* __restrict__ part,
                                                              const double* __restrict__ diagp,
@@ -1070,14 +1077,19 @@ __global__ void __launch_bounds__(256) gram16w_reduce_kernel(const float* __rest
       for (int k = 0; k < GWR_UNROLL; ++k)
         v[k] = (c0 + k < nsubs) ? __ldcs(p + (int64_t)(c0 + k) * (slab_elems / 4))
                                 : make_float4(0.f, 0.f, 0.f, 0.f);
+      // the batch's slabs in FP32 (in order), then into the double-float sums
+      float4 bs = make_float4(0.f, 0.f, 0.f, 0.f);
 #pragma unroll
       for (int k = 0; k < GWR_UNROLL; ++k) {
-        if (c0 + k >= nsubs) break;
-        acc[0] = dw_add(acc[0], make_float2(v[k].x, 0.f));
-        acc[1] = dw_add(acc[1], make_float2(v[k].y, 0.f));
-        acc[2] = dw_add(acc[2], make_float2(v[k].z, 0.f));
-        acc[3] = dw_add(acc[3], make_float2(v[k].w, 0.f));
+        bs.x += v[k].x;
+        bs.y += v[k].y;
+        bs.z += v[k].z;
+        bs.w += v[k].w;
       }
+      acc[0] = dw_add_f(acc[0], bs.x);
+      acc[1] = dw_add_f(acc[1], bs.y);
+      acc[2] = dw_add_f(acc[2], bs.z);
+      acc[3] = dw_add_f(acc[3], bs.w);
     }
     const float* sp = s + pb * ld;
     const double sa = (double)sp[a];
@@ -1291,13 +1303,6 @@ __global__ void __launch_bounds__(ApplyWarps<TN>::THREADS, 1)
   auto apply_kend = [&](int cb) -> int {
     return upper ? min(kblocks, (cb + 1) * (TN / A_BK)) : kblocks;
   };
-  // TN = 256 with an upper-triangular W: the W rows of the last 128 K of
-  // column block cb, [cb TN + 128, (cb + 1) TN), are zero left of the
-  // diagonal, so those K blocks run 128-wide products on the right half only
-  // (the triangle at 128-column granularity, as with TN = 128)
-  auto apply_khalf = [&](int cb) -> int {
-    return (TN == 256 && upper) ? (cb * TN + 128) / A_BK : 0x7fffffff;
-  };
   if (launch_aborted(err)) return;
 
   if (threadIdx.x == 0) {
@@ -1337,7 +1342,7 @@ __global__ void __launch_bounds__(ApplyWarps<TN>::THREADS, 1)
         const int64_t rt = t - pb * row_tiles * col_tiles;
         const int rb = (int)(rt / col_tiles), cb = (int)(rt % col_tiles);
         const int ya = (int)(pb * mp + (int64_t)rb * 128), yb = (int)(pb * k + (int64_t)cb * TN);
-        const int kend = apply_kend(cb), khalf = apply_khalf(cb);
+        const int kend = apply_kend(cb);
         for (int kb = 0; kb < kend; ++kb, ++g) {
           const int s = (int)(g % A_STAGES);
           const uint32_t ph = (uint32_t)(g / A_STAGES) & 1u;
@@ -1346,17 +1351,13 @@ __global__ void __launch_bounds__(ApplyWarps<TN>::THREADS, 1)
             break;
           }
           const uint32_t st = base + s * A_STAGE;
-          // K blocks from khalf on feed only the right 128 columns of the tile:
-          // the left half of their W rows is not loaded
-          const int h0 = kb >= khalf ? 1 : 0;
-          mbar_expect_tx(&full_bar[s], A_STAGE - 2u * (uint32_t)h0 * A_TILE);
+          mbar_expect_tx(&full_bar[s], A_STAGE);
           tma_load_3d(st, &tmA, kb * A_BK, ya, 0, &full_bar[s]);
           tma_load_3d(st + A_TILE, &tmA, kb * A_BK, ya, 1, &full_bar[s]);
           // B: TN rows of the W copy in boxes of 128 rows (the K-major swizzled
           // layout of a 256-row tile is two 128-row tiles back to back)
 #pragma unroll
           for (int h = 0; h < TN / 128; ++h) {
-            if (h < h0) continue;
             tma_load_3d(st + 2 * A_TILE + h * A_TILE, &tmB, kb * A_BK, yb + 128 * h, 0, &full_bar[s]);
             tma_load_3d(st + 2 * A_TILE + B_TILE + h * A_TILE, &tmB, kb * A_BK, yb + 128 * h, 1,
                         &full_bar[s]);
@@ -1382,7 +1383,7 @@ __global__ void __launch_bounds__(ApplyWarps<TN>::THREADS, 1)
         fence_after();
         const uint32_t dmain = tmem + (uint32_t)(b * 2 * TN);
         const uint32_t dcorr = dmain + (uint32_t)TN;
-        const int kend = apply_kend((int)(t % col_tiles)), khalf = apply_khalf((int)(t % col_tiles));
+        const int kend = apply_kend((int)(t % col_tiles));
         for (int kb = 0; kb < kend; ++kb, ++g) {
           const int s = (int)(g % A_STAGES);
           const uint32_t ph = (uint32_t)(g / A_STAGES) & 1u;
@@ -1392,24 +1393,6 @@ __global__ void __launch_bounds__(ApplyWarps<TN>::THREADS, 1)
           }
           fence_after();
           const uint32_t st = base + s * A_STAGE;
-          if (TN == 256 && kb >= khalf) {
-            // right half: B rows 128..255 (the second 128-row box of each
-            // plane), accumulators at column offset 128; kb > 0 here
-            constexpr uint32_t idesc_h = idesc_f16(128, 128, 0, 0);
-#pragma unroll
-            for (int kk = 0; kk < A_BK / 16; ++kk) {
-              const uint32_t adv = (uint32_t)kk * 32u;
-              const uint64_t dAH = desc_kmajor<A_BK>(st + adv);
-              const uint64_t dAL = desc_kmajor<A_BK>(st + A_TILE + adv);
-              const uint64_t dBH = desc_kmajor<A_BK>(st + 3 * A_TILE + adv);
-              const uint64_t dBL = desc_kmajor<A_BK>(st + 3 * A_TILE + B_TILE + adv);
-              mma_f16(dmain + 128u, dAH, dBH, idesc_h, 1u);
-              mma_f16(dcorr + 128u, dAH, dBL, idesc_h, 1u);
-              mma_f16(dcorr + 128u, dAL, dBH, idesc_h, 1u);
-            }
-            mma_commit(&empty_bar[s]);
-            continue;
-          }
 #pragma unroll
           for (int kk = 0; kk < A_BK / 16; ++kk) {
             const uint32_t adv = (uint32_t)kk * 32u;  // 16 fp16 along K
@@ -2003,10 +1986,14 @@ int apply_packed(const Packed& p, const double* W, int64_t ldw, int64_t k, float
                  int64_t cstride, bool upper) {
   const int64_t m = p.m, batch = p.batch;
   const int64_t ldk = p.ld;  // K extent of the W copies (= packed pitch of the input)
-  // output tile width (see ApplyCfg): 256 for W wider than 128 columns (an
-  // upper-triangular W follows its triangle at 128-column granularity in
-  // either width)
-  const int TN = k > 128 ? 256 : 128;
+  // output tile width (see ApplyCfg): 256 for dense W wider than 128 columns.
+  // An upper-triangular W keeps 128-wide tiles: its short column tiles (the
+  // first K blocks only) finish their products faster than the single
+  // 256-wide accumulator is drained, while the 128-wide kernel's two
+  // accumulator buffers overlap them (measured: 0.70 of the dense product's
+  // time for 0.56 of its products, against 0.75 with 256-wide tiles and
+  // 128-wide products on the diagonal band)
+  const int TN = (k > 128 && !(upper && k == p.N)) ? 256 : 128;
   const int64_t col_tiles = cdiv(k, TN);
   const int fstride = (int)(col_tiles * TN);
   __half* bhi = ws.take<__half>((size_t)(2 * batch * k * ldk));
