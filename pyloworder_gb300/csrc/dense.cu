@@ -1516,21 +1516,24 @@ __global__ void __launch_bounds__(512, 1)
 
 // ---------------------------------------------------------------------------
 // FP32 sweeps of large real Jacobi problems at the mixed form's tolerance.
-// Block schedule with 8-column blocks: one CTA per pair of blocks holds their
-// 16 rows of At and Vt in shared memory for one round-robin block step (the
-// 64 cross rotations in 8 rounds of 8 disjoint pairs, plus the 28 + 28
-// rotations inside the two blocks at the first step of a sweep), one grid
-// barrier per block step (127 per sweep at n = 1,024, half as many as with
-// 4-column blocks, for the same number of rounds); two warps per pair, each
-// over half the rows.  Explicit (c, s) rotations: a dot costs one FMA per
-// row, a rotation four FMAs.  The sweeps stop when every pair is orthogonal
-// to `tol`, when the pairs above the floor have converged (see
-// JAC_PRE32_TSTOP), or after max_sweeps.  Output: the rotation product J32
-// (n x n row-major FP32, J32 = the accumulated V); the host
-// re-orthonormalises it to Jo and refines the SVD of B Jo (jacobi_pre32).
+// Block schedule with J32B-column blocks: one CTA per pair of blocks holds
+// their 2 J32B rows of At and Vt in shared memory for one round-robin block
+// step (the J32B^2 cross rotations in J32B rounds of J32B disjoint pairs,
+// plus the rotations inside the two blocks at the first step of a sweep),
+// one grid barrier per block step; 16 warps, 16 / J32B per pair, each over
+// a share of the rows.  J32B = 4 (255 steps a sweep at n = 1,024, 128 CTAs):
+// 8-column blocks halve the barriers but double each warp's rows per round
+// and halve the CTAs, 4.0 against 3.2 ms a sweep measured on the headline R.
+// Explicit (c, s) rotations: a dot costs one FMA per row, a rotation four
+// FMAs.  The sweeps stop when every pair is orthogonal to `tol`, when the
+// pairs above the floor have converged (see JAC_PRE32_TSTOP), or after
+// max_sweeps.  Output: the rotation product J32 (n x n row-major FP32, J32 =
+// the accumulated V); the host re-orthonormalises it to Jo and refines the
+// SVD of B Jo (jacobi_pre32).
 // ---------------------------------------------------------------------------
 constexpr int JAC_PRE32_MIN_N = 512;       // real, batch 1, n from here on (see use_pre32)
-constexpr int J32B = 8;                    // columns per block of the FP32 kernel
+constexpr int J32B = 4;                    // columns per block of the FP32 kernel
+constexpr int J32W = 16 / J32B;            // warps per column pair (of 16)
 constexpr float JAC_PRE32_TOL = 2e-6f;     // pair orthogonality of the FP32 phase
 // The FP32 phase also ends after a sweep in which every rotated pair with a
 // column above JAC_PRE32_FLOOR of the largest turned by less than
@@ -1628,15 +1631,15 @@ __global__ void __launch_bounds__(512, 1)
                             int max_sweeps, float* __restrict__ J, int* info) {
   extern __shared__ __align__(16) float jsm32[];  // [2 J32B][pitch] At rows, then Vt rows
   __shared__ float snrm[2 * J32B];
-  __shared__ float red[J32B][2][3];  // [pair][row half][g a2 b2]
+  __shared__ float red[J32B][J32W][3];  // [pair][row part][g a2 b2]
   __shared__ int scol[2 * J32B];
   __shared__ __align__(8) uint64_t bar;
   __shared__ int abort_sh;
   cg::grid_group grid = cg::this_grid();
   const int64_t P = js.pitch;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const int pk = warp >> 1, qtr = warp & 1;  // pair slot, row half
-  const int h0 = n * qtr / 2, h1 = n * (qtr + 1) / 2;
+  const int pk = warp / J32W, qtr = warp % J32W;  // pair slot, row part
+  const int h0 = n * qtr / J32W, h1 = n * (qtr + 1) / J32W;
   float* cA = jsm32;
   float* cV = jsm32 + 2 * J32B * P;
   const uint32_t bar_s = (uint32_t)__cvta_generic_to_shared(&bar);
@@ -1753,17 +1756,20 @@ __global__ void __launch_bounds__(512, 1)
           continue;
         }
         if (step == 0) {
-          // exact squared norms once per sweep: one warp per row
-          const int s16 = warp;
-          float acc = 0.f;
-          if (scol[s16] >= 0) {
-            const float* x = cA + s16 * P;
-            for (int i = lane; i < n; i += 32) acc = fmaf(x[i], x[i], acc);
-          }
-          acc = warp_sum(acc);
-          if (lane == 0) {
-            snrm[s16] = acc;
-            if (scol[s16] >= 0) atomicMax(&js.cmax[sweep], __float_as_uint(acc));
+          // exact squared norms once per sweep: one warp per row (warps
+          // 0 .. 2 J32B - 1)
+          if (warp < 2 * J32B) {
+            const int s16 = warp;
+            float acc = 0.f;
+            if (scol[s16] >= 0) {
+              const float* x = cA + s16 * P;
+              for (int i = lane; i < n; i += 32) acc = fmaf(x[i], x[i], acc);
+            }
+            acc = warp_sum(acc);
+            if (lane == 0) {
+              snrm[s16] = acc;
+              if (scol[s16] >= 0) atomicMax(&js.cmax[sweep], __float_as_uint(acc));
+            }
           }
           __syncthreads();
         }
@@ -1798,13 +1804,19 @@ __global__ void __launch_bounds__(512, 1)
             }
           }
           __syncthreads();
-          // every lane of the pair's two warps derives the same (c, s) from
-          // the same sums in the same order; the first warp stores the norms
+          // every lane of the pair's warps derives the same (c, s) from the
+          // same sums in the same order; the first warp stores the norms
           float2 cs = make_float2(0.f, 0.f);
           if (live) {
-            const float g = red[pk][0][0] + red[pk][1][0];
-            if (al < 0.f) al = red[pk][0][1] + red[pk][1][1];
-            if (be < 0.f) be = red[pk][0][2] + red[pk][1][2];
+            float g = 0.f, sa = 0.f, sb = 0.f;
+#pragma unroll
+            for (int w = 0; w < J32W; ++w) {
+              g += red[pk][w][0];
+              sa += red[pk][w][1];
+              sb += red[pk][w][2];
+            }
+            if (al < 0.f) al = sa;
+            if (be < 0.f) be = sb;
             const float big = fmaxf(al, be);
             cs = f32_params(al, be, g, tol);
             if (qtr == 0 && lane == 0) {

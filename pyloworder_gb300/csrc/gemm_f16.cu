@@ -1040,7 +1040,7 @@ __global__ void __launch_bounds__(320, 1)
 // in sub-chunk order (the same order for every call; the slabs' own FP32
 // sums over 4,096 rows carry the larger error).
 constexpr int GWR_UNROLL = 16;
-__global__ void __launch_bounds__(256) gram16w_reduce_kernel(const float* __restrict__ part,
+__global__ void __launch_bounds__(256, 3) gram16w_reduce_kernel(const float* __restrict__ part,
                                                              const double* __restrict__ diagp,
                                                              int N, int tn, int tn2, int nsubs,
                                                              const float* __restrict__ s,
@@ -1841,8 +1841,8 @@ static int gram_packed_wide(const Packed& p, double* G, int* err, Arena& ws, cud
       tm, tm, m, tn, tn2, rpc, chunks_eff, subs_per_chunk, nsubs, part, diagp, err, p.mp);
   PLOM_CHECK_LAUNCH();
   const int64_t units = (int64_t)batch * hp::gw_tiles_sym(tn, tn2) * 128 * 64;
-  // two resident blocks per SM (96 registers a thread), a grid-stride loop
-  const int blocks = (int)std::min<int64_t>(cdiv(units, 256), (int64_t)num_sms() * 2);
+  // three resident blocks per SM (80 registers a thread), a grid-stride loop
+  const int blocks = (int)std::min<int64_t>(cdiv(units, 256), (int64_t)num_sms() * 3);
   ProfScope prof_r("gram_reduce", st, 0.0, 4.0 * (double)slabs * 128 * 256);
   hp::gram16w_reduce_kernel<<<blocks, 256, 0, st>>>(part, diagp, (int)N, tn, tn2, nsubs, p.scale,
                                                     G, (int)batch, (int)p.ld, accumulate ? 1 : 0);
