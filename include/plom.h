@@ -61,6 +61,21 @@ extern "C" {
 const char* plom_last_error_string(void);
 int plom_version(void);
 
+/* Run-time schedule and tile parameters of the tall tensor-core kernels (no
+   counterpart in pyLOM, whose products are LAPACK/BLAS calls): the Gram's
+   work items per SM per wave ("gram_wave_mult", 1-32), the resident blocks
+   per SM of its slab reduction ("reduce_blocks_per_sm", 1-16), the output
+   tile width of dense products wider than 128 columns ("apply_dense_tn",
+   128 or 256) and whether such products give each CTA whole row blocks
+   ("apply_dense_by_rows", 0 or 1).  Process-wide; set them before the
+   workspace queries of the calls they are to govern.  The Python package
+   applies the values in its tuning file at load (pyloworder_gb300.autotune
+   measures and writes them).  plom_set_tuning returns PLOM_ERR_ARG for an
+   unknown key or a value outside the listed range; plom_get_tuning returns
+   -1 for an unknown key. */
+int plom_set_tuning(const char* key, double value);
+double plom_get_tuning(const char* key);
+
 /* Per-kernel device timing on the calling host thread, the device-side
    counterpart of pyLOM's named timing channels (pyLOM/utils/cr.py:199-246
    cr_start/cr_stop, cr_info).  plom_profile_begin starts recording CUDA

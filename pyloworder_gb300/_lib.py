@@ -36,6 +36,8 @@ c_sz = ctypes.c_size_t
 PROTOS = {
     "plom_last_error_string": (ctypes.c_char_p, []),
     "plom_version": (c_int, []),
+    "plom_set_tuning": (c_int, [ctypes.c_char_p, ctypes.c_double]),
+    "plom_get_tuning": (ctypes.c_double, [ctypes.c_char_p]),
     "plom_profile_begin": (c_int, []),
     "plom_profile_end": (c_int, [ctypes.c_char_p, c_sz]),
     "plom_temporal_mean": (c_int, [c_int, c_vp, c_i64, c_i64, c_i64, c_vp, c_vp]),
@@ -110,8 +112,28 @@ def load(build_if_missing: bool = True):
             fn = getattr(lib, name)
             fn.restype = res
             fn.argtypes = args
+        _apply_tuning(lib)
         _lib = lib
         return lib
+
+
+TUNING_FILE = os.path.join(HERE, "tuning", "gb300.json")
+
+
+def _apply_tuning(lib, path=None):
+    """Set the kernels' tuning parameters from the tuning file (written by
+    pyloworder_gb300.autotune); PLOM_TUNING names another file, and an empty
+    PLOM_TUNING keeps the library's defaults."""
+    import json
+    path = path or os.environ.get("PLOM_TUNING", TUNING_FILE)
+    if not path or not os.path.exists(path):
+        return {}
+    with open(path) as f:
+        params = json.load(f).get("params", {})
+    for key, value in params.items():
+        if lib.plom_set_tuning(key.encode(), float(value)) != 0:
+            raise PlomError(f"tuning file {path}: {lib.plom_last_error_string().decode()}")
+    return params
 
 
 def call(name, *args):

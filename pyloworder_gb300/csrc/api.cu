@@ -18,6 +18,11 @@ void set_error(const char* fmt, ...) {
 
 const char* last_error() { return g_err; }
 
+Tuning& tuning() {
+  static Tuning t;
+  return t;
+}
+
 static thread_local std::vector<ProfEntry>* g_prof = nullptr;
 bool prof_on() { return g_prof != nullptr; }
 void prof_push(const ProfEntry& e) {
@@ -76,4 +81,46 @@ extern "C" int plom_profile_end(char* buf, size_t cap) {
   }
   if (status != PLOM_OK) set_error("plom_profile_end: event timing failed");
   return status;
+}
+
+// tuning parameters by name (see plom::Tuning); values outside the allowed
+// set are rejected with PLOM_ERR_ARG
+extern "C" int plom_set_tuning(const char* key, double value) {
+  using namespace plom;
+  if (!key) {
+    set_error("plom_set_tuning: null key");
+    return PLOM_ERR_ARG;
+  }
+  const std::string k(key);
+  const int v = (int)value;
+  if ((double)v != value) {
+    set_error("plom_set_tuning: %s takes an integer", key);
+    return PLOM_ERR_ARG;
+  }
+  Tuning& t = tuning();
+  if (k == "gram_wave_mult" && v >= 1 && v <= 32) {
+    t.gram_wave_mult = v;
+  } else if (k == "reduce_blocks_per_sm" && v >= 1 && v <= 16) {
+    t.reduce_blocks_per_sm = v;
+  } else if (k == "apply_dense_tn" && (v == 128 || v == 256)) {
+    t.apply_dense_tn = v;
+  } else if (k == "apply_dense_by_rows" && (v == 0 || v == 1)) {
+    t.apply_dense_by_rows = v;
+  } else {
+    set_error("plom_set_tuning: unknown key or value out of range: %s = %g", key, value);
+    return PLOM_ERR_ARG;
+  }
+  return PLOM_OK;
+}
+
+extern "C" double plom_get_tuning(const char* key) {
+  using namespace plom;
+  if (!key) return -1.0;
+  const std::string k(key);
+  const Tuning& t = tuning();
+  if (k == "gram_wave_mult") return t.gram_wave_mult;
+  if (k == "reduce_blocks_per_sm") return t.reduce_blocks_per_sm;
+  if (k == "apply_dense_tn") return t.apply_dense_tn;
+  if (k == "apply_dense_by_rows") return t.apply_dense_by_rows;
+  return -1.0;
 }

@@ -66,6 +66,18 @@ struct Arena {
   bool overflow() const { return base != nullptr && off > cap; }
 };
 
+// Run-time schedule and tile parameters of the tall kernels, set through
+// plom_set_tuning (the package loads them from its tuning file, written by
+// pyloworder_gb300.autotune on the target GPU).  Defaults: the values tuned
+// on GB300.
+struct Tuning {
+  int gram_wave_mult = 4;        // Gram work items per SM per wave (row-chunk granularity)
+  int reduce_blocks_per_sm = 3;  // resident blocks of the Gram slab reduction
+  int apply_dense_tn = 256;      // output tile width of dense products wider than 128 (128 or 256)
+  int apply_dense_by_rows = 0;   // dense products: whole row blocks per CTA (1) or single tiles (0)
+};
+Tuning& tuning();
+
 inline int num_sms() {
   static int sms = -1;
   if (sms < 0) {

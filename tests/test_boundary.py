@@ -97,3 +97,34 @@ def test_workspace_dry_runs_launch_nothing(dtype, prec):
         assert lib.plom_randomized_svd_workspace(dtype, prec, 3000, 120, 16) > 0
         for tA in (0, 1):
             assert lib.plom_matmul_workspace(dtype, prec, tA, 100, 20, 30) > 0
+
+
+def test_tuning_parameters_round_trip_and_range():
+    lib = L.load()
+    keys = [b"gram_wave_mult", b"reduce_blocks_per_sm", b"apply_dense_tn", b"apply_dense_by_rows"]
+    old = {k: lib.plom_get_tuning(k) for k in keys}
+    try:
+        assert all(v >= 0 for v in old.values())
+        assert lib.plom_set_tuning(b"gram_wave_mult", 2.0) == 0
+        assert lib.plom_get_tuning(b"gram_wave_mult") == 2.0
+        assert lib.plom_set_tuning(b"apply_dense_tn", 192.0) != 0  # 128 or 256 only
+        assert lib.plom_set_tuning(b"gram_wave_mult", 2.5) != 0    # integers only
+        assert lib.plom_set_tuning(b"no_such_key", 1.0) != 0
+        assert lib.plom_get_tuning(b"no_such_key") == -1.0
+    finally:
+        for k, v in old.items():
+            lib.plom_set_tuning(k, v)
+
+
+def test_committed_tuning_file_is_valid():
+    import json
+    with open(L.TUNING_FILE) as f:
+        params = json.load(f)["params"]
+    lib = L.load()
+    old = {k: lib.plom_get_tuning(k.encode()) for k in params}
+    try:
+        for k, v in params.items():
+            assert lib.plom_set_tuning(k.encode(), float(v)) == 0, (k, v)
+    finally:
+        for k, v in old.items():
+            lib.plom_set_tuning(k.encode(), v)
