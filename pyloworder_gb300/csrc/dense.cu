@@ -1552,6 +1552,8 @@ struct Jac32State {
   int* counts;    // [JACOBI_MAX_SWEEPS] rotations per sweep
   unsigned* cmax; // [JACOBI_MAX_SWEEPS] bits of the largest squared column norm (sweep start)
   unsigned* tmax; // [JACOBI_MAX_SWEEPS] bits of the largest |t| of the pairs above the floor
+  int* bflag;     // [blocks] block steps through which a block's rows are final
+  int* abortf;    // set by a CTA whose wait ran out: every CTA stops waiting
   unsigned long long* amax;  // bits of max |b_ij|
   int64_t pitch;  // floats per row: n rounded up to 4 (16-byte bulk copies)
 };
@@ -1683,11 +1685,13 @@ __global__ void __launch_bounds__(512, 1)
     }
     for (int64_t e = gtid; e < n; e += gthreads) js.nrm2[e] = -1.f;
   }
-  grid.sync();
-
   const int nb = (n + J32B - 1) / J32B;
   const int nbp = (nb + (nb & 1) < 2) ? 2 : nb + (nb & 1);  // even, >= 2
   const int bpairs = nbp / 2;
+  for (int64_t e = gtid; e < nbp; e += gthreads) js.bflag[e] = 0;
+  if (gtid == 0) *js.abortf = 0;
+  grid.sync();
+  int gstep = 0;  // block steps since the first sweep
   uint32_t phase = 0;
   int sweep = 0;
   for (; sweep < max_sweeps; ++sweep) {
@@ -1702,9 +1706,39 @@ __global__ void __launch_bounds__(512, 1)
       for (int task = blockIdx.x; task < bpairs; task += gridDim.x) {
         int bi, bj;
         rr_pair(step, task, nbp, bi, bj);
+        // the two blocks' rows and norms are final once the CTAs that held
+        // them in the previous block step have released their flags (a
+        // release/acquire pair per block instead of a grid-wide barrier per
+        // step); threads 0 .. 2 J32B - 1 each acquire them, as they read
+        // the norms below, and thread 0 then issues the row loads
+        if (threadIdx.x < 2 * J32B && !abort_sh) {
+          uint64_t t0 = 0;
+          asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t0));
+          for (int q = 0; q < 2; ++q) {
+            const int* fl = js.bflag + (q ? bj : bi);
+            while (true) {
+              int v;
+              asm volatile("ld.acquire.gpu.global.b32 %0, [%1];" : "=r"(v) : "l"(fl) : "memory");
+              if (v >= gstep) break;
+              if (*(volatile int*)js.abortf) {
+                abort_sh = 1;
+                break;
+              }
+              uint64_t t1;
+              asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t1));
+              if (t1 - t0 > JAC_WAIT_NS) {
+                abort_sh = 1;
+                atomicExch(js.abortf, 1);
+                break;
+              }
+            }
+          }
+        }
+        __syncthreads();
         // the row loads go out first (their columns follow from the schedule
         // alone); the carried norms are read while they are in flight
         if (threadIdx.x == 0 && !abort_sh) {
+          asm volatile("fence.proxy.async.global;" ::: "memory");
           asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
           uint32_t bytes = 0;
           for (int s8 = 0; s8 < 2 * J32B; ++s8)
@@ -1744,6 +1778,7 @@ __global__ void __launch_bounds__(512, 1)
             asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t1));
             if (t1 - t0 > JAC_WAIT_NS) {
               abort_sh = 1;
+              atomicExch(js.abortf, 1);
               break;
             }
           }
@@ -1848,12 +1883,20 @@ __global__ void __launch_bounds__(512, 1)
         if (threadIdx.x < 2 * J32B && scol[threadIdx.x] >= 0)
           js.nrm2[scol[threadIdx.x]] = snrm[threadIdx.x];
         __syncthreads();
+        if (threadIdx.x == 0) {
+          __threadfence();
+          asm volatile("st.release.gpu.global.b32 [%0], %1;" ::"l"(js.bflag + bi), "r"(gstep + 1)
+                       : "memory");
+          asm volatile("st.release.gpu.global.b32 [%0], %1;" ::"l"(js.bflag + bj), "r"(gstep + 1)
+                       : "memory");
+        }
       }
-      grid.sync();
+      ++gstep;
     }
     if (lane == 0 && myrot) atomicAdd(&js.counts[sweep], myrot);
     if (lane == 0 && mytmax > 0.f) atomicMax(&js.tmax[sweep], __float_as_uint(mytmax));
     grid.sync();
+    if (*(volatile int*)js.abortf) break;
     if (js.counts[sweep] == 0) break;
     if (sweep > 0 && __uint_as_float(js.tmax[sweep]) <= JAC_PRE32_TSTOP) break;
   }
@@ -2473,6 +2516,22 @@ static int rf_graded(double* X, int n, RefineBufs& b, Arena& ws, cudaStream_t st
   return PLOM_OK;
 }
 
+// C = A B (n x n FP64): [Ah^T; Ah^T; Al^T]^T [Bh; Bl; Bh] by gemm_tn_df
+int gemm_nn_df(const double* A, const double* B, double* C, int n, Arena& ws, cudaStream_t st) {
+  const int64_t nn = (int64_t)n * n;
+  float* at = ws.take<float>((size_t)(3 * nn));
+  float* b3 = ws.take<float>((size_t)(3 * nn));
+  if (ws.measuring()) return gemm_tn_df(nullptr, n, nullptr, n, nullptr, n, n, n, 3 * (int64_t)n, ws, st);
+  PLOM_REQUIRE(!ws.overflow(), PLOM_ERR_WORKSPACE, "gemm_nn_df: workspace too small");
+  PLOM_REQUIRE(A && B && C && n >= 1, PLOM_ERR_ARG, "gemm_nn_df: bad arguments");
+  const int eg = rf_grid(nn);
+  rf_tsplit_kernel<<<eg, 256, 0, st>>>(A, n, 3, at);
+  PLOM_CHECK_LAUNCH();
+  rf_split3_kernel<<<eg, 256, 0, st>>>(B, nn, nullptr, b3);
+  PLOM_CHECK_LAUNCH();
+  return gemm_tn_df(at, n, b3, n, C, n, n, n, 3 * (int64_t)n, ws, st);
+}
+
 // SVD of the scaled B (Rcat = [Ah; Ah; Al], A = B^T) from the orthonormal
 // starting product Jo: S (scaled), Ut (columns = left vectors), VHt (rows =
 // right vectors)
@@ -2576,6 +2635,8 @@ static int jacobi_pre32(const double* A, const double* At, int n, double tol, do
   j32.counts = ws.take<int>(JACOBI_MAX_SWEEPS);
   j32.cmax = ws.take<unsigned>(JACOBI_MAX_SWEEPS);
   j32.tmax = ws.take<unsigned>(JACOBI_MAX_SWEEPS);
+  j32.bflag = ws.take<int>((size_t)n / J32B + 2);
+  j32.abortf = ws.take<int>(1);
   j32.amax = ws.take<unsigned long long>(1);
   float* J32 = ws.take<float>(nn);
   float* E = ws.take<float>(nn);

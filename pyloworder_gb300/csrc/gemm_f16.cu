@@ -426,9 +426,7 @@ __global__ void __launch_bounds__(256) split_w16_kernel(const double* __restrict
 // row chunks of the Gram: the fewest whole waves of CTAs that split evenly
 // into tiles, times this factor (shorter chunks keep the tiles that share a
 // row panel closer together in time, so more of the panel re-reads hit L2)
-#ifndef PLOM_GRAM_WAVE_MULT
-#define PLOM_GRAM_WAVE_MULT 4
-#endif
+
 constexpr int G_BK = PLOM_GRAM_BK;             // rows per stage (a multiple of 16)
 constexpr uint32_t G_BOX = G_BK * 128;         // G_BK rows x 64 fp16
 constexpr uint32_t G_TILE = 2 * G_BOX;         // G_BK rows x 128 columns of one plane
@@ -837,6 +835,10 @@ __global__ void __launch_bounds__(320, 1)
   }
   const int I0 = ti * 128, J0 = tj * 256;
   const bool band = SYM && I0 >= J0 && I0 < J0 + 256;   // A = columns I0.. of the B tile
+  // the second band tile of a column block (I0 = J0 + 128): its left 128
+  // columns lie below the diagonal, so only the 128 x 128 diagonal block is
+  // formed (128-wide products on the B panel's right half, which is A)
+  const bool half = band && I0 == J0 + 128;
   const uint32_t a_off = band ? (uint32_t)((I0 - J0) / 64) * GW_BOX : 0u;
   const int dcol = I0 - J0;  // tile column of the Gram diagonal (band tiles)
   const int64_t r_beg = (int64_t)chunk * rows_per_chunk;
@@ -876,7 +878,7 @@ __global__ void __launch_bounds__(320, 1)
   if (warp == 9) {
     // ---- TMA producer: GW_BK rows x (I block unless band, J block) of both planes
     if (lane == 0) {
-      const uint32_t bytes = (band ? 8u : 12u) * GW_BOX;
+      const uint32_t bytes = (half ? 4u : band ? 8u : 12u) * GW_BOX;
       const CUtensorMap* mb = SYM ? &tmP : &tmB;
       for (int kb = 0; kb < KB; ++kb) {
         const int s = kb % GW_STAGES;
@@ -892,9 +894,11 @@ __global__ void __launch_bounds__(320, 1)
             tma_load_3d(st + z * OFF_AL + GW_BOX, &tmP, I0 + 64, y, z, &full_bar[s]);
           }
 #pragma unroll
-          for (int q = 0; q < 4; ++q)
+          for (int q = 0; q < 4; ++q) {
+            if (half && q < 2) continue;
             tma_load_3d(st + OFF_BH + z * 4 * GW_BOX + q * GW_BOX, mb, J0 + 64 * q, y, z,
                         &full_bar[s]);
+          }
         }
       }
     }
@@ -969,6 +973,21 @@ __global__ void __launch_bounds__(320, 1)
         const uint32_t st = base + s * GW_STAGE;
         const uint32_t bH = st + OFF_BH, bL = st + OFF_BL;
         const uint32_t aH = band ? bH + a_off : st, aL = band ? bL + a_off : st + OFF_AL;
+        if (half) {
+          // accumulators at column 128: the slab keeps its column layout
+          constexpr uint32_t idesc_h = idesc_f16(128, 128, 1, 1);
+#pragma unroll
+          for (int kk = 0; kk < GW_BK / 16; ++kk) {
+            const uint32_t adv = (uint32_t)kk * 2048u;
+            const uint64_t dAH = desc_sw128(aH + adv, GW_BOX, 1024), dAL = desc_sw128(aL + adv, GW_BOX, 1024);
+            const uint32_t first = (kl > 0 || kk > 0) ? 1u : 0u;
+            mma_f16(dmain + 128u, dAH, dAH, idesc_h, first);
+            mma_f16(dcorr + 128u, dAH, dAL, idesc_h, first);
+            mma_f16(dcorr + 128u, dAL, dAH, idesc_h, 1u);
+          }
+          mma_commit(&empty_bar[s]);
+          continue;
+        }
 #pragma unroll
         for (int kk = 0; kk < GW_BK / 16; ++kk) {
           const uint32_t adv = (uint32_t)kk * 2048u;  // 16 rows of 128 bytes
@@ -992,7 +1011,7 @@ __global__ void __launch_bounds__(320, 1)
     // the reduction kernel sums the slabs in a fixed order.  Band tiles also
     // write their rows' diagonal (the CUDA-core sums, FP64) per sub-chunk.
     const int rloc = (warp & 3) * 32 + lane;
-    const int cbeg = band ? 0 : (warp >> 2) * 128, ncc = band ? 8 : 4;
+    const int cbeg = half ? 128 : band ? 0 : (warp >> 2) * 128, ncc = (band && !half) ? 8 : 4;
     for (int sub = 0; sub < nsub; ++sub) {
       const int b = sub & 1;
       bool ready = mbar_wait(&tfull, (uint32_t)sub & 1u, &abort_sh, err);
@@ -1787,7 +1806,7 @@ static int gram16_chunks(int64_t m, int tiles, int bk = hp::G_BK) {
   const int64_t sms = num_sms();
   const int64_t maxc = std::max<int64_t>(1, cdiv(m, 4 * (int64_t)bk));
   for (int64_t waves = 1; waves <= 64; ++waves) {
-    const int64_t items = waves * sms * PLOM_GRAM_WAVE_MULT;
+    const int64_t items = waves * sms * tuning().gram_wave_mult;
     if (items % tiles) continue;
     return (int)std::max<int64_t>(1, std::min(maxc, items / tiles));
   }
@@ -1841,8 +1860,9 @@ static int gram_packed_wide(const Packed& p, double* G, int* err, Arena& ws, cud
       tm, tm, m, tn, tn2, rpc, chunks_eff, subs_per_chunk, nsubs, part, diagp, err, p.mp);
   PLOM_CHECK_LAUNCH();
   const int64_t units = (int64_t)batch * hp::gw_tiles_sym(tn, tn2) * 128 * 64;
-  // three resident blocks per SM (80 registers a thread), a grid-stride loop
-  const int blocks = (int)std::min<int64_t>(cdiv(units, 256), (int64_t)num_sms() * 3);
+  // a few resident blocks per SM (80 registers a thread), a grid-stride loop
+  const int blocks = (int)std::min<int64_t>(
+      cdiv(units, 256), (int64_t)num_sms() * tuning().reduce_blocks_per_sm);
   ProfScope prof_r("gram_reduce", st, 0.0, 4.0 * (double)slabs * 128 * 256);
   hp::gram16w_reduce_kernel<<<blocks, 256, 0, st>>>(part, diagp, (int)N, tn, tn2, nsubs, p.scale,
                                                     G, (int)batch, (int)p.ld, accumulate ? 1 : 0);
@@ -1993,7 +2013,7 @@ int apply_packed(const Packed& p, const double* W, int64_t ldw, int64_t k, float
   // accumulator buffers overlap them (measured: 0.70 of the dense product's
   // time for 0.56 of its products, against 0.75 with 256-wide tiles and
   // 128-wide products on the diagonal band)
-  const int TN = (k > 128 && !(upper && k == p.N)) ? 256 : 128;
+  const int TN = (k > 128 && !(upper && k == p.N)) ? tuning().apply_dense_tn : 128;
   const int64_t col_tiles = cdiv(k, TN);
   const int fstride = (int)(col_tiles * TN);
   __half* bhi = ws.take<__half>((size_t)(2 * batch * k * ldk));
@@ -2042,7 +2062,8 @@ int apply_packed(const Packed& p, const double* W, int64_t ldw, int64_t k, float
   // different lengths); the dense case keeps concurrent tiles of one row
   // block on different SMs (fewer DRAM re-reads)
   const bool tri_pre = upper && k == p.N;
-  const int by_rows = (tri_pre && batch * row_tiles >= 2 * num_sms()) ? 1 : 0;
+  const int by_rows =
+      ((tri_pre || tuning().apply_dense_by_rows) && batch * row_tiles >= 2 * num_sms()) ? 1 : 0;
   const int grid = (int)std::min<int64_t>(by_rows ? batch * row_tiles : tiles, num_sms());
   hp::ApplyOut o;
   o.C = out ? nullptr : C;

@@ -47,6 +47,11 @@ size_t gemm_tn_workspace_batched(int64_t M, int64_t N, int64_t K, bool sym, size
                                  int batch);
 // C (M x N, FP64, ld ldc) = A^T B for FP32 A (K x M), B (K x N): exact products,
 // compensated double-float sums over row chunks, FP64 chunk reduction.
+// ---- dense.cu ----
+// C = A B for n x n FP64 operands as double-float sums of exact FP32 products
+// (~1e-9 relative to sum |a_ik b_kj|; the mixed form's n x n products, whose
+// factors carry FP32-level information), on the CUDA cores' FP32 pipe
+int gemm_nn_df(const double* A, const double* B, double* C, int n, Arena& ws, cudaStream_t st);
 int gemm_tn_df(const float* A, int64_t lda, const float* B, int64_t ldb, double* C, int64_t ldc,
                int64_t M, int64_t N, int64_t K, Arena& ws, cudaStream_t st);
 

@@ -35,6 +35,8 @@ namespace plom {
 
 static const double U64 = 1.1102230246251565e-16;  // 2^-53
 static const double U32 = 5.9604644775390625e-08;  // 2^-24 (the fp16-pair products are FP32-accurate)
+// n x n products of the mixed form in double-float sums from this size on
+static const int DF_PRODUCT_MIN_N = 256;
 
 // ---------------------------------------------------------------------------
 // tall operations, dispatched on precision
@@ -269,11 +271,16 @@ static int cholqr3_packed_passes23(bool cplx, int n, PackedCore& b, double relfa
   PLOM_TRY(sub([&] { return apply_packed(b.P1, F2, N, N, nullptr, 0, &b.P2, info, ws, st, 0, 0, true); }));
   // pass 3
   PLOM_TRY(sub([&] { return chol_pass_packed(cplx, n, b.P2, b, b.R3, b.W3, 0.0, relfail, info, ws, st); }));
-  ws.off = need;
-  if (!ws.measuring()) {
+  // Re = R3 R2 R1: double-float products from n = 256 on (the factors carry
+  // the 22-bit operands' information; FP64 runs at 1/64 of the FP32 rate)
+  if (N >= DF_PRODUCT_MIN_N) {
+    PLOM_TRY(sub([&] { return gemm_nn_df(b.R3, b.R2, b.Rp, N, ws, st); }));
+    PLOM_TRY(sub([&] { return gemm_nn_df(b.Rp, b.R1, b.Re, N, ws, st); }));
+  } else if (!ws.measuring()) {
     PLOM_TRY((gemm_sq_nn(b.R3, b.R2, b.Rp, N, 1, 3, st)));
     PLOM_TRY((gemm_sq_nn(b.Rp, b.R1, b.Re, N, 1, 3, st)));
   }
+  ws.off = need;
   return PLOM_OK;
 }
 
@@ -335,7 +342,13 @@ static int svd_tail_packed(bool cplx, int n, PackedCore& b, int64_t m, float* U,
   need = std::max(need, ws.off);
   ws.off = mark;
   const double* Mop = b.F;
-  if (!ws.measuring()) {
+  if (!cplx && N >= DF_PRODUCT_MIN_N) {
+    // M = R3^-1 Ur, the right operand of Q2 x M (double-float products)
+    PLOM_TRY(gemm_nn_df(b.W3, Ur, Me, N, ws, st));
+    need = std::max(need, ws.off);
+    ws.off = mark;
+    Mop = Me;
+  } else if (!ws.measuring()) {
     // M = R3^-1 Ur (embedded for complex), the right operand of Q2 x M
     if (cplx) {
       PLOM_TRY(complex_to_embed(Ur, Ue, n, 1, st));
