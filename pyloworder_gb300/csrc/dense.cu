@@ -1531,7 +1531,7 @@ __global__ void __launch_bounds__(512, 1)
 // the accumulated V); the host re-orthonormalises it to Jo and refines the
 // SVD of B Jo (jacobi_pre32).
 // ---------------------------------------------------------------------------
-constexpr int JAC_PRE32_MIN_N = 512;       // real, batch 1, n from here on (see use_pre32)
+constexpr int JAC_PRE32_MIN_N = 256;       // real, batch 1, n from here on (see use_pre32)
 constexpr int J32B = 4;                    // columns per block of the FP32 kernel
 constexpr int J32W = 16 / J32B;            // warps per column pair (of 16)
 constexpr float JAC_PRE32_TOL = 2e-6f;     // pair orthogonality of the FP32 phase
