@@ -2613,7 +2613,7 @@ static int jacobi_refine(const float* Rcat, const double* Jo, int n, double* S, 
   return PLOM_OK;
 }
 
-// Real problems from n = 512 on at the mixed form's tolerance, up to the size
+// Real problems from n = 256 on at the mixed form's tolerance, up to the size
 // whose FP32 block kernel rows fit in shared memory (the double-float kernel's
 // bound, kept for the larger sizes' workspace estimates).
 static bool use_pre32(int n, double tol) {

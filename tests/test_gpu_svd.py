@@ -128,7 +128,7 @@ def test_mixed_mean_removed_u_orthonormal():
 
 @pytest.mark.parametrize("n", [1024, 517])
 def test_mixed_large_n_fp32_presweeps(n):
-    """512 <= n <= 1600 in the mixed form: the SVD of R starts with FP32 Jacobi sweeps,
+    """256 <= n <= 1600 in the mixed form: the SVD of R starts with FP32 Jacobi sweeps,
     re-orthonormalises their rotation product and refines it with matrix
     products in double-float sums (simultaneous Jacobi angles plus
     Newton-Schulz steps).  The result must match the plain FP64 form within
