@@ -86,80 +86,86 @@ __global__ void __launch_bounds__(256) chol_coop_kernel(const double* __restrict
       R[e] = v;
     }
     grid.sync();
-    for (int k = 0; k < T; ++k) {
+    // (1) diagonal block of problem b at block step k, by one CTA: the factor
+    // and Z = R_kk^-T row by row in the same steps (forward substitution of
+    // R^T Z = I):
+    //   piv = sqrt(S_jj), R_j. = S_j. / piv, Z_j. = P_j. / piv,
+    //   S_ac -= R_ja R_jc (j < a <= c),  P_a. -= R_ja Z_j. (a > j),  P = I at start
+    // Block step k + 1's diagonal block is factored inside step k's trailing
+    // update, by the CTA that updates it (look-ahead: one grid barrier less
+    // per block step, and the factorisation overlaps the other CTAs' updates)
+    auto diag_block = [&](int b, int k) {
       const int k0 = k * NB, nbk = min(NB, n - k0);
-      // (1) diagonal block, one CTA per problem: the factor and Z = R_kk^-T
-      // row by row in the same steps (forward substitution of R^T Z = I):
-      //   piv = sqrt(S_jj), R_j. = S_j. / piv, Z_j. = P_j. / piv,
-      //   S_ac -= R_ja R_jc (j < a <= c),  P_a. -= R_ja Z_j. (a > j),  P = I at start
-      for (int b = blockIdx.x; b < batch; b += gridDim.x) {
-        if (stt.status[b] != 0) continue;
-        double* Rb = R + b * nn;
-        for (int e = tid; e < NB * NB; e += blockDim.x) {
-          int i = e / NB, j = e % NB;
-          S[i][j] = (i < nbk && j < nbk) ? Rb[(int64_t)(k0 + i) * n + k0 + j] : 0.0;
-          P[i][j] = (i == j) ? 1.0 : 0.0;
+      if (stt.status[b] != 0) return;
+      double* Rb = R + b * nn;
+      for (int e = tid; e < NB * NB; e += blockDim.x) {
+        int i = e / NB, j = e % NB;
+        S[i][j] = (i < nbk && j < nbk) ? Rb[(int64_t)(k0 + i) * n + k0 + j] : 0.0;
+        P[i][j] = (i == j) ? 1.0 : 0.0;
+      }
+      __syncthreads();
+      for (int j = 0; j < nbk; ++j) {
+        if (tid == 0) {
+          double d = S[j][j];
+          bool ok = (d > 0.0) && isfinite(d);
+          if (!ok && rel0 == 0.0 && isfinite(d)) {
+            // unshifted factorization (a CholeskyQR pass after the first):
+            // a non-positive pivot is a null direction of G, e.g. an exact
+            // zero column of the tall matrix.  Floor this pivot alone (its
+            // row's remaining entries are at the rounding level of G);
+            // a shift of the whole diagonal would bias every other column
+            d = relfail * stt.trace[b] / n;
+            ok = d > 0.0;
+          }
+          sflag = ok ? 1 : 0;
+          const double piv = ok ? sqrt(d) : 1.0;
+          S[j][j] = piv;
+          rpiv = 1.0 / piv;
         }
         __syncthreads();
-        for (int j = 0; j < nbk; ++j) {
-          if (tid == 0) {
-            double d = S[j][j];
-            bool ok = (d > 0.0) && isfinite(d);
-            if (!ok && rel0 == 0.0 && isfinite(d)) {
-              // unshifted factorization (a CholeskyQR pass after the first):
-              // a non-positive pivot is a null direction of G, e.g. an exact
-              // zero column of the tall matrix.  Floor this pivot alone (its
-              // row's remaining entries are at the rounding level of G);
-              // a shift of the whole diagonal would bias every other column
-              d = relfail * stt.trace[b] / n;
-              ok = d > 0.0;
-            }
-            sflag = ok ? 1 : 0;
-            const double piv = ok ? sqrt(d) : 1.0;
-            S[j][j] = piv;
-            rpiv = 1.0 / piv;
-          }
-          __syncthreads();
-          if (!sflag) break;
-          const double rp = rpiv;
-          for (int i = tid; i < nbk; i += blockDim.x) {
-            if (i > j) S[j][i] *= rp;
-            else P[j][i] *= rp;
-          }
-          __syncthreads();
-          const int w = nbk - j - 1;
-          const int ns = w * w, np = w * (j + 1);
-          for (int e = tid; e < ns + np; e += blockDim.x) {
-            if (e < ns) {
-              const int a = j + 1 + e / w, c = j + 1 + e % w;
-              if (a <= c) S[a][c] -= S[j][a] * S[j][c];
-            } else {
-              const int e2 = e - ns;
-              const int a = j + 1 + e2 / (j + 1), q = e2 % (j + 1);
-              P[a][q] -= S[j][a] * P[j][q];
-            }
-          }
-          __syncthreads();
+        if (!sflag) break;
+        const double rp = rpiv;
+        for (int i = tid; i < nbk; i += blockDim.x) {
+          if (i > j) S[j][i] *= rp;
+          else P[j][i] *= rp;
         }
-        if (!sflag) {
-          if (tid == 0) stt.status[b] = 2;
-          __syncthreads();
-          continue;
-        }
-        // write back upper block, zero strict lower part
-        for (int e = tid; e < nbk * nbk; e += blockDim.x) {
-          int i = e / nbk, j = e % nbk;
-          Rb[(int64_t)(k0 + i) * n + k0 + j] = (i <= j) ? S[i][j] : 0.0;
-        }
-        // R_kk^-1 = Z^T
-        double* Db = Dinv + (int64_t)b * NB * NB;
-        for (int e = tid; e < NB * NB; e += blockDim.x) {
-          int i = e / NB, c = e % NB;
-          Db[e] = (i <= c && c < nbk) ? P[c][i] : 0.0;
+        __syncthreads();
+        const int w = nbk - j - 1;
+        const int ns = w * w, np = w * (j + 1);
+        for (int e = tid; e < ns + np; e += blockDim.x) {
+          if (e < ns) {
+            const int a = j + 1 + e / w, c = j + 1 + e % w;
+            if (a <= c) S[a][c] -= S[j][a] * S[j][c];
+          } else {
+            const int e2 = e - ns;
+            const int a = j + 1 + e2 / (j + 1), q = e2 % (j + 1);
+            P[a][q] -= S[j][a] * P[j][q];
+          }
         }
         __syncthreads();
       }
-      grid.sync();
+      if (!sflag) {
+        if (tid == 0) stt.status[b] = 2;
+        __syncthreads();
+        return;
+      }
+      // write back upper block, zero strict lower part
+      for (int e = tid; e < nbk * nbk; e += blockDim.x) {
+        int i = e / nbk, j = e % nbk;
+        Rb[(int64_t)(k0 + i) * n + k0 + j] = (i <= j) ? S[i][j] : 0.0;
+      }
+      // R_kk^-1 = Z^T
+      double* Db = Dinv + (int64_t)b * NB * NB;
+      for (int e = tid; e < NB * NB; e += blockDim.x) {
+        int i = e / NB, c = e % NB;
+        Db[e] = (i <= c && c < nbk) ? P[c][i] : 0.0;
+      }
+      __syncthreads();
+    };
+    for (int b = blockIdx.x; b < batch; b += gridDim.x) diag_block(b, 0);
+    grid.sync();
+    for (int k = 0; k < T; ++k) {
+      const int k0 = k * NB, nbk = min(NB, n - k0);
       // (2) panel: R_kj = Dinv_k^T R_kj for j > k
       const int ntask_p = (T - k - 1) * batch;
       for (int t = blockIdx.x; t < ntask_p; t += gridDim.x) {
@@ -185,10 +191,21 @@ __global__ void __launch_bounds__(256) chol_coop_kernel(const double* __restrict
       grid.sync();
       // (3) trailing update R_ac -= R_ka^T R_kc for k < a <= c
       const int w = T - k - 1;
-      const int ntask_t = w * (w + 1) / 2 * batch;
+      const int per = w * (w + 1) / 2;
+      const int ntask_t = per * batch;
       for (int t = blockIdx.x; t < ntask_t; t += gridDim.x) {
-        int b = t / (w * (w + 1) / 2);
-        int r = t % (w * (w + 1) / 2);
+        // the problems' (k + 1, k + 1) blocks first (task b, so that the CTA
+        // of problem b's next diagonal block updates it), then the others
+        int b, r;
+        if (t < batch) {
+          b = t;
+          r = 0;
+        } else {
+          const int u = t - batch;
+          b = u / (per - 1);
+          r = 1 + u % (per - 1);
+        }
+        const int r_task = r;
         // map r -> (a, c) with 0 <= a <= c < w
         int a = 0;
         while (r >= w - a) {
@@ -215,6 +232,7 @@ __global__ void __launch_bounds__(256) chol_coop_kernel(const double* __restrict
           Rb[(int64_t)(a0 + r2) * n + c0 + s2] -= acc;
         }
         __syncthreads();
+        if (r_task == 0) diag_block(b, k + 1);  // look-ahead: final after this update
       }
       grid.sync();
     }
@@ -2125,7 +2143,8 @@ __global__ void pre32_unscale_kernel(double* __restrict__ S, int n,
 // every column of B' to its own relative accuracy (the small singular
 // values included) and the iteration converges to the SVD of the fixed B'
 // (the same matrix a double-float Jacobi finish would decompose), the error
-// of a separated pair squaring at each step.  Pairs whose angle would
+// of a separated pair squaring at each step (two steps from the FP32 phase's
+// end, where every pair above the floor turned by less than 1e-4).  Pairs whose angle would
 // exceed 0.1 (singular values closer than the remaining error) and pairs of
 // columns both below JAC_REFINE_FLOOR of the largest are not rotated, and a
 // step whose angles have a Frobenius norm above 0.25 is shortened to it.
@@ -2134,8 +2153,9 @@ __global__ void pre32_unscale_kernel(double* __restrict__ S, int n,
 // (graded: the leading, accurate columns keep their directions).
 // (T. Ogita and K. Aishima refine SVDs by matrix products in the same
 // spirit, J. Comput. Appl. Math. 369 (2020); this is a one-sided form.)
-constexpr int JAC_REFINE_STEPS = 3;
-constexpr int JAC_REFINE_NS = 2;           // Newton-Schulz steps per refinement step
+constexpr int JAC_REFINE_STEPS = 2;
+constexpr int JAC_REFINE_NS = 2;           // Newton-Schulz steps after the first refinement step
+                                           // (one after the later, smaller ones)
 constexpr double JAC_REFINE_MAX_ANGLE = 0.1;
 constexpr double JAC_REFINE_NULL = 1e-8;   // sigma_k / sigma_1 below this: a null column
 constexpr double JAC_REFINE_FLOOR = 1e-5;  // pairs of columns both below this fraction: kept
@@ -2573,7 +2593,7 @@ static int jacobi_refine(const float* Rcat, const double* Jo, int n, double* S, 
     PLOM_TRY(rf_prod(b.t2, b.om, b.P, n, n, ws, st));
     rf_rotate_kernel<<<eg, 256, 0, st>>>(b.Dl, b.om, b.P, nn);
     PLOM_CHECK_LAUNCH();
-    for (int k = 0; k < JAC_REFINE_NS; ++k) {
+    for (int k = 0; k < (it == 0 ? JAC_REFINE_NS : 1); ++k) {
       // E = -(D + D^T) - D^T D;  D <- D + (E + D E) / 2
       rf_split3_kernel<<<eg, 256, 0, st>>>(b.Dl, nn, b.a3, nullptr);
       PLOM_CHECK_LAUNCH();
