@@ -66,8 +66,10 @@ int plom_version(void);
    work items per SM per wave ("gram_wave_mult", 1-32), the resident blocks
    per SM of its slab reduction ("reduce_blocks_per_sm", 1-16), the output
    tile width of dense products wider than 128 columns ("apply_dense_tn",
-   128 or 256) and whether such products give each CTA whole row blocks
-   ("apply_dense_by_rows", 0 or 1).  Process-wide; set them before the
+   128 or 256), whether such products give each CTA whole row blocks
+   ("apply_dense_by_rows", 0 or 1) and the row chunks of a large FP32 input
+   packed on a second stream beside the first Gram ("pass1_chunks", 1, 2, 4
+   or 8; 1 packs it whole first).  Process-wide; set them before the
    workspace queries of the calls they are to govern.  The Python package
    applies the values in its tuning file at load (pyloworder_gb300.autotune
    measures and writes them).  plom_set_tuning returns PLOM_ERR_ARG for an

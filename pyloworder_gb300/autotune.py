@@ -3,11 +3,12 @@
 The parameters (plom_set_tuning, include/plom.h) are the Gram's work items
 per SM per wave (row-chunk granularity), the resident blocks per SM of the
 Gram's slab reduction, the output tile width of dense products wider than
-128 columns and whether those products give each CTA whole row blocks.
+128 columns, whether those products give each CTA whole row blocks and the
+row chunks of a large FP32 input packed beside the first Gram.
 On the GPU at hand the tuner times the mixed-form tsqr_svd with CUDA events
-on two snapshot fields of the POD benchmark's kind -- a wide one (n = 1,024,
-the 128 x 256 Gram and apply kernels) and a narrow one (n = 64, the
-128 x 128 kernels) -- and settles one parameter at a time (coordinate
+on two snapshot fields of the POD benchmark's kind -- a wide one (2 x rows
+points, n = 1,024: the 128 x 256 Gram and apply kernels) and a narrow one
+(rows points, n = 64: the 128 x 128 kernels) -- and settles one parameter at a time (coordinate
 descent from the current values, two passes), keeping a value only when it
 is faster on the sum of the two shapes' median times relative to the
 starting point.  The result is written as JSON, which the package applies
@@ -28,19 +29,21 @@ CANDIDATES = {
     "reduce_blocks_per_sm": [2, 3, 4],
     "apply_dense_tn": [128, 256],
     "apply_dense_by_rows": [0, 1],
+    "pass1_chunks": [1, 4, 8],
 }
 
 
 def _fields(rows):
     from . import datagen, vmmath
     out = []
-    for n in (1024, 64):
-        nx, ny = datagen.grid_for_points(rows)
+    for n, m in ((1024, 2 * rows), (64, rows)):
+        rows_n = m
+        nx, ny = datagen.grid_for_points(rows_n)
         X = datagen.pod_field_device(nx, ny, n, min(64, n // 2), seed=17 + n, noise=1e-5,
-                                     amp_pow=1.5, m=rows)
+                                     amp_pow=1.5, m=rows_n)
         Y, _, _ = vmmath.remove_mean_device(X, n)
         del X
-        out.append((f"tsqr_svd {rows}x{n} f32 mixed", Y, n))
+        out.append((f"tsqr_svd {rows_n}x{n} f32 mixed", Y, n))
     return out
 
 

@@ -808,7 +808,7 @@ __global__ void __launch_bounds__(320, 1)
     gram16w_kernel(const __grid_constant__ CUtensorMap tmP, const __grid_constant__ CUtensorMap tmB,
                    int64_t m, int tn, int tn2, int64_t rows_per_chunk, int chunks,
                    int subs_per_chunk, int nsubs, float* __restrict__ part,
-                   double* __restrict__ diagp, int* err, int64_t mp) {
+                   double* __restrict__ diagp, int* err, int64_t mp, int64_t slab_off) {
   extern __shared__ uint8_t smem_raw[];
   __shared__ uint64_t full_bar[GW_STAGES], empty_bar[GW_STAGES];
   __shared__ uint64_t tfull, tempty, dfull[2];
@@ -825,7 +825,8 @@ __global__ void __launch_bounds__(320, 1)
   const int rem_item = (int)(blockIdx.x % per_problem);
   const int chunk = rem_item / ntiles, tile = rem_item % ntiles;
   // sub-chunk slabs of this item: (problem, tile) major, then the sub-chunks of all rows
-  const int64_t slab0 = (int64_t)(pb * ntiles + tile) * nsubs + (int64_t)chunk * subs_per_chunk;
+  const int64_t slab0 =
+      (int64_t)(pb * ntiles + tile) * nsubs + (int64_t)chunk * subs_per_chunk + slab_off;
   int ti = 0, tj = 0;
   if (SYM)
     gw_tile_sym(tile, tn2, ti, tj);
@@ -1059,12 +1060,17 @@ __global__ void __launch_bounds__(320, 1)
 // in sub-chunk order (the same order for every call; the slabs' own FP32
 // sums over 4,096 rows carry the larger error).
 constexpr int GWR_UNROLL = 16;
+// subs_per_scale > 0: the slabs come from row chunks packed with their own
+// column scales (scale vector q = sub-chunk / subs_per_scale, a multiple of
+// GWR_UNROLL sub-chunks each): every batch is unscaled (exactly: powers of
+// two) before it is added
 __global__ void __launch_bounds__(256, 3) gram16w_reduce_kernel(const float* __restrict__ part,
                                                              const double* __restrict__ diagp,
                                                              int N, int tn, int tn2, int nsubs,
                                                              const float* __restrict__ s,
                                                              double* __restrict__ G, int batch,
-                                                             int ld, int accumulate) {
+                                                             int ld, int accumulate,
+                                                             int subs_per_scale) {
   const int ntiles = gw_tiles_sym(tn, tn2);
   const int64_t units = (int64_t)batch * ntiles * 128 * 64;
   const int64_t slab_elems = 128 * 256;
@@ -1088,15 +1094,25 @@ __global__ void __launch_bounds__(256, 3) gram16w_reduce_kernel(const float* __r
     const float4* p = reinterpret_cast<const float4*>(part + slab * slab_elems + (int64_t)row * 256 +
                                                       4 * q);
     float2 acc[4];
+    double vsum[4] = {0.0, 0.0, 0.0, 0.0};  // per-chunk-scale mode: the unscaled chunk sums
 #pragma unroll
     for (int e = 0; e < 4; ++e) acc[e] = make_float2(0.f, 0.f);
+    // whole batches: sixteen independent loads in flight, then the batch's
+    // slabs in FP32 (in order) and into the double-float sums; the last
+    // partial batch the same way, one slab at a time
+    const int nfull = nsubs - nsubs % GWR_UNROLL;
     for (int c0 = 0; c0 < nsubs; c0 += GWR_UNROLL) {
       float4 v[GWR_UNROLL];
+      const int cnt = c0 < nfull ? GWR_UNROLL : nsubs - c0;
+      if (cnt == GWR_UNROLL) {
 #pragma unroll
-      for (int k = 0; k < GWR_UNROLL; ++k)
-        v[k] = (c0 + k < nsubs) ? __ldcs(p + (int64_t)(c0 + k) * (slab_elems / 4))
-                                : make_float4(0.f, 0.f, 0.f, 0.f);
-      // the batch's slabs in FP32 (in order), then into the double-float sums
+        for (int k = 0; k < GWR_UNROLL; ++k) v[k] = __ldcs(p + (int64_t)(c0 + k) * (slab_elems / 4));
+      } else {
+#pragma unroll
+        for (int k = 0; k < GWR_UNROLL; ++k)
+          v[k] = k < cnt ? __ldcs(p + (int64_t)(c0 + k) * (slab_elems / 4))
+                         : make_float4(0.f, 0.f, 0.f, 0.f);
+      }
       float4 bs = make_float4(0.f, 0.f, 0.f, 0.f);
 #pragma unroll
       for (int k = 0; k < GWR_UNROLL; ++k) {
@@ -1109,6 +1125,17 @@ __global__ void __launch_bounds__(256, 3) gram16w_reduce_kernel(const float* __r
       acc[1] = dw_add_f(acc[1], bs.y);
       acc[2] = dw_add_f(acc[2], bs.z);
       acc[3] = dw_add_f(acc[3], bs.w);
+      if (subs_per_scale > 0 &&
+          ((c0 + GWR_UNROLL) % subs_per_scale == 0 || c0 + GWR_UNROLL >= nsubs)) {
+        // end of a row chunk: its sums unscaled in FP64 (any scale range)
+        const float* sq = s + (int64_t)(c0 / subs_per_scale) * ld;
+        const double sa_q = (double)sq[a];
+#pragma unroll
+        for (int e = 0; e < 4; ++e) {
+          vsum[e] += dw_value(acc[e]) / (sa_q * (double)sq[min(b0 + e, N - 1)]);
+          acc[e] = make_float2(0.f, 0.f);
+        }
+      }
     }
     const float* sp = s + pb * ld;
     const double sa = (double)sp[a];
@@ -1121,6 +1148,7 @@ __global__ void __launch_bounds__(256, 3) gram16w_reduce_kernel(const float* __r
         // the diagonal's FP64 slabs, in the same order, loads batched
         const double* dp = diagp + slab * 128 + row;
         float2 d = make_float2(0.f, 0.f);
+        double dsum = 0.0;
         for (int c0 = 0; c0 < nsubs; c0 += GWR_UNROLL) {
           double dv[GWR_UNROLL];
 #pragma unroll
@@ -1131,12 +1159,18 @@ __global__ void __launch_bounds__(256, 3) gram16w_reduce_kernel(const float* __r
             if (c0 + k >= nsubs) break;
             d = dw_add(d, dw_from_double(dv[k]));
           }
+          if (subs_per_scale > 0 &&
+              ((c0 + GWR_UNROLL) % subs_per_scale == 0 || c0 + GWR_UNROLL >= nsubs)) {
+            const double sa_q = (double)s[(int64_t)(c0 / subs_per_scale) * ld + a];
+            dsum += dw_value(d) / (sa_q * sa_q);
+            d = make_float2(0.f, 0.f);
+          }
         }
-        v = dw_value(d);
+        v = subs_per_scale > 0 ? dsum : dw_value(d);
       } else {
-        v = dw_value(acc[e]);
+        v = subs_per_scale > 0 ? vsum[e] : dw_value(acc[e]);
       }
-      v /= sa * (double)sp[b];
+      if (subs_per_scale == 0) v /= sa * (double)sp[b];
       const int64_t e1 = pb * N * N + (int64_t)a * N + b;
       const int64_t e2 = pb * N * N + (int64_t)b * N + a;
       G[e1] = accumulate ? G[e1] + v : v;
@@ -1857,7 +1891,7 @@ static int gram_packed_wide(const Packed& p, double* G, int* err, Arena& ws, cud
                PLOM_ERR_CUDA, "gram16w: tensor map encoding failed");
   ProfScope prof_g("tc_gram_f16x3", st, (double)m * N * N * batch, 4.0 * (double)m * p.ld * batch);
   hp::gram16w_kernel<true><<<(unsigned)(batch * tiles * chunks_eff), 320, hp::GW_SMEM, st>>>(
-      tm, tm, m, tn, tn2, rpc, chunks_eff, subs_per_chunk, nsubs, part, diagp, err, p.mp);
+      tm, tm, m, tn, tn2, rpc, chunks_eff, subs_per_chunk, nsubs, part, diagp, err, p.mp, 0);
   PLOM_CHECK_LAUNCH();
   const int64_t units = (int64_t)batch * hp::gw_tiles_sym(tn, tn2) * 128 * 64;
   // a few resident blocks per SM (80 registers a thread), a grid-stride loop
@@ -1865,7 +1899,57 @@ static int gram_packed_wide(const Packed& p, double* G, int* err, Arena& ws, cud
       cdiv(units, 256), (int64_t)num_sms() * tuning().reduce_blocks_per_sm);
   ProfScope prof_r("gram_reduce", st, 0.0, 4.0 * (double)slabs * 128 * 256);
   hp::gram16w_reduce_kernel<<<blocks, 256, 0, st>>>(part, diagp, (int)N, tn, tn2, nsubs, p.scale,
-                                                    G, (int)batch, (int)p.ld, accumulate ? 1 : 0);
+                                                    G, (int)batch, (int)p.ld, accumulate ? 1 : 0, 0);
+  PLOM_CHECK_LAUNCH();
+  return PLOM_OK;
+}
+
+// Gram of a matrix packed in C row chunks of mc rows (mc a multiple of
+// 16 x 4,096), chunk c with its own column scales (scales + c ld): one wide
+// Gram launch per chunk, each writing its sub-chunk slabs into one array,
+// and one reduction over all of them.  Before chunk c's products the stream
+// waits for ready[c] (when given), so that chunks packed on another stream
+// are taken as they come.
+int gram_packed_chunks(const Packed& p, int C, int64_t mc, const float* scales, double* G,
+                       const cudaEvent_t* ready, int* err, Arena& ws, cudaStream_t st) {
+  const int64_t N = p.N;
+  const int tn = (int)cdiv(p.ld, 128), tn2 = (int)cdiv(p.ld, 256);
+  const int tiles = hp::gw_tiles_sym(tn, tn2);
+  int chunks_eff, subs_per_chunk, nsubs_c;
+  int64_t rpc;
+  wide_chunks(mc, tiles, chunks_eff, rpc, subs_per_chunk, nsubs_c);
+  const int64_t nsubs = (int64_t)C * nsubs_c;
+  const int64_t slabs = tiles * nsubs;
+  float* part = ws.take<float>((size_t)slabs * 128 * 256);
+  double* diagp = ws.take<double>((size_t)slabs * 128);
+  if (ws.measuring()) return PLOM_OK;
+  PLOM_REQUIRE(!ws.overflow(), PLOM_ERR_WORKSPACE, "gram16w chunks: workspace too small");
+  PLOM_REQUIRE(p.hi && G && scales && p.batch == 1 && p.ld > 128 && C >= 1 &&
+                   mc % ((int64_t)hp::G_KSUB * hp::GWR_UNROLL) == 0 && p.mp >= (int64_t)C * mc &&
+                   nsubs < (1ll << 31),
+               PLOM_ERR_ARG, "gram16w chunks: bad arguments");
+  PLOM_CHECK_CUDA(cudaFuncSetAttribute(hp::gram16w_kernel<true>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)hp::GW_SMEM));
+  for (int c = 0; c < C; ++c) {
+    if (ready) PLOM_CHECK_CUDA(cudaStreamWaitEvent(st, ready[c], 0));
+    const Packed v = packed_rows_view(p, (int64_t)c * mc, mc, mc, nullptr);
+    CUtensorMap tm;
+    PLOM_REQUIRE(make_map_planes(&tm, v.hi, (uint64_t)v.ld, (uint64_t)mc, (uint64_t)v.ld, 64,
+                                 hp::GW_BK, (uint64_t)v.pstride),
+                 PLOM_ERR_CUDA, "gram16w chunks: tensor map encoding failed");
+    ProfScope prof_g("tc_gram_f16x3", st, (double)mc * N * N, 4.0 * (double)mc * p.ld);
+    hp::gram16w_kernel<true><<<(unsigned)(tiles * chunks_eff), 320, hp::GW_SMEM, st>>>(
+        tm, tm, mc, tn, tn2, rpc, chunks_eff, subs_per_chunk, (int)nsubs, part, diagp, err, mc,
+        (int64_t)c * nsubs_c);
+    PLOM_CHECK_LAUNCH();
+  }
+  const int64_t units = (int64_t)tiles * 128 * 64;
+  const int blocks = (int)std::min<int64_t>(
+      cdiv(units, 256), (int64_t)num_sms() * tuning().reduce_blocks_per_sm);
+  ProfScope prof_r("gram_reduce", st, 0.0, 4.0 * (double)slabs * 128 * 256);
+  hp::gram16w_reduce_kernel<<<blocks, 256, 0, st>>>(part, diagp, (int)N, tn, tn2, (int)nsubs, scales,
+                                                    G, 1, (int)p.ld, 0, nsubs_c);
   PLOM_CHECK_LAUNCH();
   return PLOM_OK;
 }
@@ -1946,7 +2030,7 @@ static int tn_packed_wide(const Packed& a, const Packed& b, double* C, int64_t l
     ProfScope prof("tc_tn_f16x3", st, 2.0 * (double)m * a.N * b.N,
                    4.0 * (double)m * (a.ld + b.ld));
     hp::gram16w_kernel<false><<<tiles * chunks_eff, 320, hp::GW_SMEM, st>>>(
-        ta, tb, m, tna, tn2, rpc, chunks_eff, subs_per_chunk, nsubs, part, nullptr, err, m);
+        ta, tb, m, tna, tn2, rpc, chunks_eff, subs_per_chunk, nsubs, part, nullptr, err, m, 0);
     PLOM_CHECK_LAUNCH();
   }
   const int64_t total = a.N * b.N;

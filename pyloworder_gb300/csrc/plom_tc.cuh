@@ -38,6 +38,10 @@ int pack_f32(const float* Y, int64_t ld, int64_t m, int64_t N, Packed& p, Arena&
 // G (N x N, FP64; a batch: batch x N x N) = Y^T Y
 int gram_packed(const Packed& p, double* G, int* err, Arena& ws, cudaStream_t st,
                 bool accumulate = false);
+// G = Y^T Y for Y packed in C row chunks of mc rows with per-chunk column
+// scales (scales: C x ld); chunk c's products start after ready[c] (if given)
+int gram_packed_chunks(const Packed& p, int C, int64_t mc, const float* scales, double* G,
+                       const cudaEvent_t* ready, int* err, Arena& ws, cudaStream_t st);
 // C (A.N x B.N, FP64, ldc) = A^T B for two packed operands with the same rows
 int tn_packed(const Packed& a, const Packed& b, double* C, int64_t ldc, int* err, Arena& ws,
               cudaStream_t st);

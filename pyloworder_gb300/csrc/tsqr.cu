@@ -284,9 +284,116 @@ static int cholqr3_packed_passes23(bool cplx, int n, PackedCore& b, double relfa
   return PLOM_OK;
 }
 
+// Large real FP32 inputs: pass 1 in row chunks, each packed with its own
+// column scales on a second stream while the previous chunk's Gram runs, so
+// that the packing (HBM-bound, ~15 ms at 8,388,608 x 1,024) overlaps the
+// tensor-core Gram; Q1 = X R1^-1 then treats the chunks as a batch (one W,
+// each chunk's input scales), as the host entry does.  The chunks must tile
+// the rows exactly (Q1 lives in the caller's U).
+constexpr int OVERLAP_CHUNKS = 8;
+constexpr int64_t OVERLAP_MIN_CHUNK_ROWS = 262144;
+static int overlap_chunks(bool cplx, int64_t m, int N) {
+  if (cplx || N <= 128) return 1;  // the chunked Gram is the wide (128 x 256 tile) kernel
+  const int64_t C = std::min(OVERLAP_CHUNKS, tuning().pass1_chunks);
+  if (C <= 1) return 1;
+  // whole chunks of 16 x 4,096-row sub-chunks (the slab reduction's batches)
+  if (m % (C * 65536) != 0 || m / C < OVERLAP_MIN_CHUNK_ROWS) return 1;
+  return (int)C;
+}
+
+// one non-blocking auxiliary stream per device (host copies, chunk packing),
+// created on first use
+static cudaStream_t host_copy_stream() {
+  static std::mutex mu;
+  static std::map<int, cudaStream_t> streams;
+  int dev = 0;
+  cudaGetDevice(&dev);
+  std::lock_guard<std::mutex> lock(mu);
+  auto it = streams.find(dev);
+  if (it != streams.end()) return it->second;
+  cudaStream_t s = nullptr;
+  if (cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking) != cudaSuccess) return nullptr;
+  streams[dev] = s;
+  return s;
+}
+
+
+struct ChunkEvents {
+  cudaEvent_t start = nullptr, packed[OVERLAP_CHUNKS] = {};
+  bool ok = false;
+  ChunkEvents() {
+    ok = cudaEventCreateWithFlags(&start, cudaEventDisableTiming) == cudaSuccess;
+    for (auto& e : packed) ok = ok && cudaEventCreateWithFlags(&e, cudaEventDisableTiming) == cudaSuccess;
+  }
+  ~ChunkEvents() {  // released once their pending work completes
+    if (start) cudaEventDestroy(start);
+    for (auto& e : packed)
+      if (e) cudaEventDestroy(e);
+  }
+};
+
+static int cholqr3_packed_chunked(const float* X, int64_t m, int n, int64_t ldx, int C,
+                                  PackedCore& b, int* info, Arena& ws, cudaStream_t st) {
+  const int N = n;
+  const int64_t mc = m / C, ldp = b.P0.ld;
+  const bool meas = ws.measuring();
+  float* xscale = ws.take<float>((size_t)C * ldp);
+  float* qscale = ws.take<float>((size_t)C * ldp);
+  const size_t pack_bytes = sizeof(unsigned) * (size_t)N + 1024;  // pack_f32's column maxima
+  uint8_t* pbuf = ws.take<uint8_t>(pack_bytes);
+  if (!meas) PLOM_REQUIRE(!ws.overflow(), PLOM_ERR_WORKSPACE, "tsqr_svd: workspace too small");
+  b.P1.scale = qscale;
+  double rel1, relfail;
+  shifts_for(PLOM_PREC_MIXED, m, N, rel1, relfail);
+  const size_t mark = ws.off;
+  size_t need = mark;
+  auto sub = [&](auto&& fn) -> int {
+    ws.off = mark;
+    const int s = fn();
+    need = std::max(need, ws.off);
+    ws.off = mark;
+    return s;
+  };
+  ChunkEvents ev;
+  cudaStream_t cs = nullptr;
+  if (!meas) {
+    cs = host_copy_stream();
+    PLOM_REQUIRE(cs && ev.ok, PLOM_ERR_CUDA, "tsqr_svd: packing stream or events unavailable");
+    PLOM_CHECK_CUDA(cudaEventRecord(ev.start, st));  // X and the planes are ready from here
+    PLOM_CHECK_CUDA(cudaStreamWaitEvent(cs, ev.start, 0));
+  }
+  for (int c = 0; c < C; ++c) {
+    const int64_t r0 = (int64_t)c * mc;
+    Packed v = packed_rows_view(b.P0, r0, mc, mc, xscale ? xscale + (int64_t)c * ldp : nullptr);
+    // the packing stream's own workspace (its launches run beside the Grams')
+    Arena pa(pbuf, meas ? 0 : pack_bytes);
+    PLOM_TRY(pack_f32(X + r0 * ldx, ldx, mc, N, v, pa, meas ? st : cs));
+    if (!meas) PLOM_CHECK_CUDA(cudaEventRecord(ev.packed[c], cs));
+  }
+  // the chunks' Grams as they are packed, one reduction over all of them
+  PLOM_TRY(sub([&] {
+    return gram_packed_chunks(b.P0, C, mc, xscale, b.G, meas ? nullptr : ev.packed, info, ws, st);
+  }));
+  PLOM_TRY(sub([&] { return chol_shifted(b.G, b.R1, N, 1, rel1, relfail, info, ws, st); }));
+  PLOM_TRY(sub([&] { return trtri_upper(b.R1, b.W1, N, 1, ws, st); }));
+  Packed P0b = b.P0, P1b = b.P1;
+  P0b.batch = P1b.batch = C;
+  P0b.m = P1b.m = mc;
+  P0b.mp = P1b.mp = mc;
+  P0b.scale = xscale;
+  P1b.scale = qscale;
+  PLOM_TRY(sub([&] { return apply_packed(P0b, b.W1, N, N, nullptr, 0, &P1b, info, ws, st, 0, 0, true); }));
+  PLOM_TRY(sub([&] { return cholqr3_packed_passes23(false, n, b, relfail, info, ws, st); }));
+  ws.off = need;
+  return PLOM_OK;
+}
+
 static int cholqr3_packed(bool cplx, const float* X, int64_t m, int n, int64_t ldx,
                           PackedCore& b, int* info, Arena& ws, cudaStream_t st) {
   const int N = cplx ? 2 * n : n;
+  const int C = overlap_chunks(cplx, m, N);
+  if (C > 1 && b.P0.mp == m && b.P1.mp == m)
+    return cholqr3_packed_chunked(X, m, n, ldx, C, b, info, ws, st);
   double rel1, relfail;
   shifts_for(PLOM_PREC_MIXED, m, N, rel1, relfail);
   const size_t mark = ws.off;
@@ -984,21 +1091,6 @@ static HostPlan host_plan(int64_t m) {
   h.C = (int)cdiv(m, h.mc);
   h.M = h.mc * h.C;
   return h;
-}
-
-// one non-blocking copy stream per device, created on first use
-static cudaStream_t host_copy_stream() {
-  static std::mutex mu;
-  static std::map<int, cudaStream_t> streams;
-  int dev = 0;
-  cudaGetDevice(&dev);
-  std::lock_guard<std::mutex> lock(mu);
-  auto it = streams.find(dev);
-  if (it != streams.end()) return it->second;
-  cudaStream_t s = nullptr;
-  if (cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking) != cudaSuccess) return nullptr;
-  streams[dev] = s;
-  return s;
 }
 
 struct HostEvents {
