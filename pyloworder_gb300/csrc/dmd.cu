@@ -56,6 +56,7 @@ struct DmdBufs {
   double* babs; // N
   int* order;   // N
   double* Vr;   // N x nt complex Vandermonde
+  int* flip;    // N conjugate-pair fix-up flags of the ordered modes
 };
 
 // -------------------------------------------------------------------------
@@ -393,14 +394,21 @@ __device__ void schur_vectors(const double* T, const double* Z, const double* wr
 }
 
 // -------------------------------------------------------------------------
-// the whole reduced stage (one CTA)
+// the reduced stage: Atilde, its eigenpairs (Hessenberg + Francis, the Schur
+// vectors) and the Vandermonde rows in one CTA; P, q and the mode matrix in
+// kernels spread over the GPU (their FP64 sums over the snapshots were 57 %
+// of the one-CTA version's cycles); the amplitude solve in one CTA
 // -------------------------------------------------------------------------
-__global__ void __launch_bounds__(256) dmd_reduced_kernel(const double* __restrict__ aux1,
+__global__ void __launch_bounds__(256) dmd_eig_kernel(const double* __restrict__ aux1,
                                                           const double* __restrict__ S,
                                                           const double* __restrict__ VT, int N,
                                                           int nt, DmdBufs B, double* muR,
                                                           double* muI, double* bJov, double* Mphi,
                                                           int* info) {
+  (void)muR;
+  (void)muI;
+  (void)bJov;
+  (void)Mphi;
   extern __shared__ double sh[];
   const int tid = threadIdx.x, nthr = blockDim.x;
   // Atilde[i][j] = sum_t aux1[i][t] VT[j][t] / S[j]
@@ -418,7 +426,6 @@ __global__ void __launch_bounds__(256) dmd_reduced_kernel(const double* __restri
   }
   __syncthreads();
   schur_vectors(B.A, B.Z, B.wr, B.wi, N, B.Y, B.Wv, sh);
-  const cplx* W = reinterpret_cast<const cplx*>(B.Wv);
   cplx* V = reinterpret_cast<cplx*>(B.Vr);
   // Vandermonde rows mu_i^t by repeated multiplication
   for (int i = tid; i < N; i += nthr) {
@@ -430,43 +437,81 @@ __global__ void __launch_bounds__(256) dmd_reduced_kernel(const double* __restri
     }
   }
   __syncthreads();
-  // P = (W^H W) o conj(Vand Vand^H)
-  cplx* P = reinterpret_cast<cplx*>(B.Pm);
-  for (int e = tid; e < N * N; e += nthr) {
+}
+
+// P = (W^H W) o conj(Vand Vand^H) (one warp per element) and
+// q_i = conj( sum_t Vand[i][t] sum_k S_k VT[k][t] W[k][i] ) (one block per i,
+// the blocks after the P warps'): FP64 sums over t and k spread over the GPU
+__global__ void __launch_bounds__(256) dmd_pq_kernel(const double* __restrict__ S,
+                                                     const double* __restrict__ VT, int N, int nt,
+                                                     DmdBufs B, const int* __restrict__ info) {
+  if (info[ST_FAIL]) return;
+  const cplx* W = reinterpret_cast<const cplx*>(B.Wv);
+  const cplx* V = reinterpret_cast<const cplx*>(B.Vr);
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int pblocks = (N * N + 7) / 8;
+  if ((int)blockIdx.x < pblocks) {
+    const int e = blockIdx.x * 8 + warp;
+    if (e >= N * N) return;
     const int i = e / N, j = e % N;
-    cplx g = {0.0, 0.0};
-    for (int k = 0; k < N; ++k) {
-      const cplx a = cconj(W[(size_t)k * N + i]), b = W[(size_t)k * N + j];
-      const cplx ab = cmul(a, b);
+    cplx g = {0.0, 0.0}, vv = {0.0, 0.0};
+    for (int k = lane; k < N; k += 32) {
+      const cplx ab = cmul(cconj(W[(size_t)k * N + i]), W[(size_t)k * N + j]);
       g.re += ab.re;
       g.im += ab.im;
     }
-    cplx vv = {0.0, 0.0};
-    for (int t = 0; t < nt; ++t) {
+    for (int t = lane; t < nt; t += 32) {
       const cplx ab = cmul(V[(size_t)i * nt + t], cconj(V[(size_t)j * nt + t]));
       vv.re += ab.re;
       vv.im += ab.im;
     }
-    P[e] = cmul(g, cconj(vv));
+    g.re = warp_sum(g.re);
+    g.im = warp_sum(g.im);
+    vv.re = warp_sum(vv.re);
+    vv.im = warp_sum(vv.im);
+    if (lane == 0) reinterpret_cast<cplx*>(B.Pm)[e] = cmul(g, cconj(vv));
+    return;
   }
-  // q_i = conj( sum_t Vand[i][t] sum_k S_k VT[k][t] W[k][i] )
-  cplx* q = reinterpret_cast<cplx*>(B.qv);
-  for (int i = tid; i < N; i += nthr) {
-    cplx acc = {0.0, 0.0};
-    for (int t = 0; t < nt; ++t) {
-      cplx gw = {0.0, 0.0};
-      for (int k = 0; k < N; ++k) {
-        const double g = S[k] * VT[(size_t)k * nt + t];
-        gw.re += g * W[(size_t)k * N + i].re;
-        gw.im += g * W[(size_t)k * N + i].im;
-      }
-      const cplx ab = cmul(V[(size_t)i * nt + t], gw);
-      acc.re += ab.re;
-      acc.im += ab.im;
+  const int i = (int)blockIdx.x - pblocks;
+  if (i >= N) return;
+  cplx acc = {0.0, 0.0};
+  for (int t = threadIdx.x; t < nt; t += blockDim.x) {
+    cplx gw = {0.0, 0.0};
+    for (int k = 0; k < N; ++k) {
+      const double gk = S[k] * VT[(size_t)k * nt + t];
+      gw.re += gk * W[(size_t)k * N + i].re;
+      gw.im += gk * W[(size_t)k * N + i].im;
     }
-    q[i] = cconj(acc);
+    const cplx ab = cmul(V[(size_t)i * nt + t], gw);
+    acc.re += ab.re;
+    acc.im += ab.im;
+  }
+  __shared__ double red[8][2];
+  acc.re = warp_sum(acc.re);
+  acc.im = warp_sum(acc.im);
+  if (lane == 0) {
+    red[warp][0] = acc.re;
+    red[warp][1] = acc.im;
   }
   __syncthreads();
+  if (threadIdx.x == 0) {
+    cplx t = {0.0, 0.0};
+    for (int w = 0; w < 8; ++w) {
+      t.re += red[w][0];
+      t.im += red[w][1];
+    }
+    reinterpret_cast<cplx*>(B.qv)[i] = cconj(t);
+  }
+}
+
+// Cholesky solve for the amplitudes, the ordering and the conjugate-pair
+// fix-up flags (one CTA)
+__global__ void __launch_bounds__(256) dmd_amp_kernel(int N, DmdBufs B, double* muR, double* muI,
+                                                      double* bJov, int* info) {
+  if (info[ST_FAIL]) return;
+  const int tid = threadIdx.x, nthr = blockDim.x;
+  cplx* P = reinterpret_cast<cplx*>(B.Pm);
+  cplx* q = reinterpret_cast<cplx*>(B.qv);
   // Cholesky P = L L^H (in place, lower), then solve L L^H b = q
   cplx* b = reinterpret_cast<cplx*>(B.bv);
   __shared__ int bad;
@@ -528,7 +573,7 @@ __global__ void __launch_bounds__(256) dmd_reduced_kernel(const double* __restri
   }
   __syncthreads();
   // ordered eigenvalues / amplitudes and the pair fix-up flags
-  __shared__ int flip_tab[1024];
+  int* flip_tab = B.flip;
   if (tid == 0) {
     for (int j = 0; j < N; ++j) {
       const int o = B.order[j];
@@ -558,31 +603,44 @@ __global__ void __launch_bounds__(256) dmd_reduced_kernel(const double* __restri
     }
   }
   __syncthreads();
-  // Mphi[t][j] = sum_k VT[k][t] / S_k * W[k][o_j] / mu_{o_j}  (+ the imag fix-up)
-  for (int e = tid; e < nt * N; e += nthr) {
-    const int t = e / N, j = e % N;
-    const int o = B.order[j];
-    const cplx mu = {B.wr[o], B.wi[o]};
-    cplx s = {0.0, 0.0};
-    for (int k = 0; k < N; ++k) {
-      const double g = VT[(size_t)k * nt + t] / S[k];
-      s.re += g * W[(size_t)k * N + o].re;
-      s.im += g * W[(size_t)k * N + o].im;
-    }
-    s = cdiv(s, mu);
-    Mphi[(size_t)t * 2 * N + 2 * j] = s.re;
-    Mphi[(size_t)t * 2 * N + 2 * j + 1] = s.im;
+}
+
+// Mphi[t][j] = sum_k VT[k][t] / S_k * W[k][o_j] / mu_{o_j} (one thread per
+// element), then the conjugate-pair fix-up of its imaginary parts per row
+__global__ void __launch_bounds__(256) dmd_mphi_kernel(const double* __restrict__ S,
+                                                       const double* __restrict__ VT, int N,
+                                                       int nt, DmdBufs B, double* Mphi,
+                                                       const int* __restrict__ info) {
+  if (info[ST_FAIL]) return;
+  const cplx* W = reinterpret_cast<const cplx*>(B.Wv);
+  const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= (int64_t)nt * N) return;
+  const int t = (int)(e / N), j = (int)(e % N);
+  const int o = B.order[j];
+  const cplx mu = {B.wr[o], B.wi[o]};
+  cplx s = {0.0, 0.0};
+  for (int k = 0; k < N; ++k) {
+    const double g = VT[(size_t)k * nt + t] / S[k];
+    s.re += g * W[(size_t)k * N + o].re;
+    s.im += g * W[(size_t)k * N + o].im;
   }
-  __syncthreads();
-  // Phi.imag[:, j] = Phi.imag[:, j+1]; Phi.imag[:, j+1] = -Phi.imag[:, j+1]
-  for (int t = tid; t < nt; t += nthr) {
-    for (int j = 0; j + 1 < N && j < 1024; ++j) {
-      if (!flip_tab[j]) continue;
-      double* row = Mphi + (size_t)t * 2 * N;
-      const double im1 = row[2 * (j + 1) + 1];
-      row[2 * j + 1] = im1;
-      row[2 * (j + 1) + 1] = -im1;
-    }
+  s = cdiv(s, mu);
+  Mphi[(size_t)t * 2 * N + 2 * j] = s.re;
+  Mphi[(size_t)t * 2 * N + 2 * j + 1] = s.im;
+}
+
+// Phi.imag[:, j] = Phi.imag[:, j+1]; Phi.imag[:, j+1] = -Phi.imag[:, j+1]
+__global__ void dmd_flip_kernel(int N, int nt, DmdBufs B, double* Mphi,
+                                const int* __restrict__ info) {
+  if (info[ST_FAIL]) return;
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= nt) return;
+  double* row = Mphi + (size_t)t * 2 * N;
+  for (int j = 0; j + 1 < N; ++j) {
+    if (!B.flip[j]) continue;
+    const double im1 = row[2 * (j + 1) + 1];
+    row[2 * j + 1] = im1;
+    row[2 * (j + 1) + 1] = -im1;
   }
 }
 
@@ -600,6 +658,7 @@ size_t dmd_reduced_workspace(int N, int nt) {
   a.take<double>(N);
   a.take<int>(N);
   a.take<double>((size_t)2 * N * nt);
+  a.take<int>(N);
   return a.off + 1024;
 }
 
@@ -636,13 +695,23 @@ extern "C" int plom_dmd_reduced(const double* aux1, const double* S, const doubl
   B.babs = a.take<double>(N);
   B.order = a.take<int>(N);
   B.Vr = a.take<double>((size_t)2 * N * T);
+  B.flip = a.take<int>(N);
   cudaStream_t st = (cudaStream_t)stream;
   PLOM_CHECK_CUDA(cudaMemsetAsync(info, 0, sizeof(int) * PLOM_INFO_WORDS, st));
   const size_t shbytes = sizeof(double) * (2 * (size_t)N + 16);
   PLOM_REQUIRE(shbytes <= 48 * 1024, PLOM_ERR_ARG, "dmd_reduced: r too large for one CTA");
-  ProfScope prof("dmd_reduced_fp64", st, 0.0, 0.0);
-  dmd_reduced_kernel<<<1, 256, shbytes, st>>>(aux1, S, VT, N, T, B, muReal, muImag, bJov, Mphi,
-                                              info);
+  ProfScope prof("dmd_reduced_fp64", st, 0.0, 0.0, 5);
+  // eigenpairs of Atilde and the Vandermonde rows (one CTA), P and q (spread
+  // over the GPU), the amplitude solve and ordering (one CTA), the mode matrix
+  dmd_eig_kernel<<<1, 256, shbytes, st>>>(aux1, S, VT, N, T, B, muReal, muImag, bJov, Mphi, info);
+  PLOM_CHECK_LAUNCH();
+  dmd_pq_kernel<<<(unsigned)((N * N + 7) / 8 + N), 256, 0, st>>>(S, VT, N, T, B, info);
+  PLOM_CHECK_LAUNCH();
+  dmd_amp_kernel<<<1, 256, 0, st>>>(N, B, muReal, muImag, bJov, info);
+  PLOM_CHECK_LAUNCH();
+  dmd_mphi_kernel<<<(unsigned)cdiv((int64_t)T * N, 256), 256, 0, st>>>(S, VT, N, T, B, Mphi, info);
+  PLOM_CHECK_LAUNCH();
+  dmd_flip_kernel<<<(unsigned)cdiv((int64_t)T, 256), 256, 0, st>>>(N, T, B, Mphi, info);
   PLOM_CHECK_LAUNCH();
   return PLOM_OK;
 }

@@ -131,3 +131,31 @@ def test_spod_field_row_reduced_vs_oracle():
     with _fp64_oracle():
         Lo, Po, fo, Uo = O.spod_run(Xh, t, nDFT=256, nolap=128, return_U=True)
     _spod_leading_checks(Lm, Pm, f, Lo, Uo, fo, M, 1e-4, 1e-3, nfreq_p=12)
+
+
+def test_tsqr_svd_chunked_first_pass_matches_whole():
+    """A large FP32 input takes the first pass in row chunks packed on a second
+    stream beside the Gram (per-chunk column scales, one slab reduction that
+    unscales each chunk in FP64); the result must match the whole-matrix
+    packing (pass1_chunks = 1) to the mixed form's tolerances."""
+    from pyloworder_gb300 import _lib as L
+    lib = L.load()
+    m, n, k = 2_097_152, 256, 32
+    nx, ny = datagen.grid_for_points(m)
+    X = datagen.pod_field_device(nx, ny, n, k, seed=1203, noise=1e-5, amp_pow=1.5, m=m)
+    Y, _, _ = P.vmmath.remove_mean_device(X, n)
+    del X
+    old = lib.plom_get_tuning(b"pass1_chunks")
+    try:
+        assert lib.plom_set_tuning(b"pass1_chunks", 8.0) == 0
+        Uc, Sc, Vc = P.vmmath.tsqr_svd_device(Y, n, "mixed")
+        assert lib.plom_set_tuning(b"pass1_chunks", 1.0) == 0
+        Uw, Sw, Vw = P.vmmath.tsqr_svd_device(Y, n, "mixed")
+    finally:
+        lib.plom_set_tuning(b"pass1_chunks", old)
+    Sc, Sw = Sc.double().cpu().numpy(), Sw.double().cpu().numpy()
+    assert sigma_rel(Sc, Sw, k) < 1e-5
+    assert sigma_normwise(Sc, Sw) < 1e-5
+    assert subspace_angle(Uc[:, :k].double().cpu().numpy(), Uw[:, :k].double().cpu().numpy()) < 1e-4
+    Ud = Uc.double()
+    assert float((Ud.T @ Ud - torch.eye(n, dtype=torch.float64, device="cuda")).abs().max()) < 1e-4
