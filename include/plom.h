@@ -69,7 +69,9 @@ int plom_version(void);
    128 or 256), whether such products give each CTA whole row blocks
    ("apply_dense_by_rows", 0 or 1) and the row chunks of a large FP32 input
    packed on a second stream beside the first Gram ("pass1_chunks", 1, 2, 4
-   or 8; 1 packs it whole first).  Process-wide; set them before the
+   or 8; 1 packs it whole first) and which products of one tall matrix wider
+   than 128 columns run on SM pairs with 256 x 256 tiles (2-SM UMMA,
+   "apply_pair": 0 none, 1 dense W, 2 dense and triangular W).  Process-wide; set them before the
    workspace queries of the calls they are to govern.  The Python package
    applies the values in its tuning file at load (pyloworder_gb300.autotune
    measures and writes them).  plom_set_tuning returns PLOM_ERR_ARG for an

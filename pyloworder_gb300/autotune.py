@@ -4,7 +4,8 @@ The parameters (plom_set_tuning, include/plom.h) are the Gram's work items
 per SM per wave (row-chunk granularity), the resident blocks per SM of the
 Gram's slab reduction, the output tile width of dense products wider than
 128 columns, whether those products give each CTA whole row blocks and the
-row chunks of a large FP32 input packed beside the first Gram.
+row chunks of a large FP32 input packed beside the first Gram and the
+products that run on SM pairs.
 On the GPU at hand the tuner times the mixed-form tsqr_svd with CUDA events
 on two snapshot fields of the POD benchmark's kind -- a wide one (2 x rows
 points, n = 1,024: the 128 x 256 Gram and apply kernels) and a narrow one
@@ -30,6 +31,7 @@ CANDIDATES = {
     "apply_dense_tn": [128, 256],
     "apply_dense_by_rows": [0, 1],
     "pass1_chunks": [1, 4, 8],
+    "apply_pair": [0, 1, 2],
 }
 
 

@@ -108,6 +108,8 @@ extern "C" int plom_set_tuning(const char* key, double value) {
     t.apply_dense_by_rows = v;
   } else if (k == "pass1_chunks" && (v == 1 || v == 2 || v == 4 || v == 8)) {
     t.pass1_chunks = v;
+  } else if (k == "apply_pair" && v >= 0 && v <= 2) {
+    t.apply_pair = v;
   } else {
     set_error("plom_set_tuning: unknown key or value out of range: %s = %g", key, value);
     return PLOM_ERR_ARG;
@@ -125,5 +127,6 @@ extern "C" double plom_get_tuning(const char* key) {
   if (k == "apply_dense_tn") return t.apply_dense_tn;
   if (k == "apply_dense_by_rows") return t.apply_dense_by_rows;
   if (k == "pass1_chunks") return t.pass1_chunks;
+  if (k == "apply_pair") return t.apply_pair;
   return -1.0;
 }

@@ -1545,6 +1545,322 @@ __global__ void __launch_bounds__(ApplyWarps<TN>::THREADS, 1)
 }
 
 // ---------------------------------------------------------------------------
+// apply on SM pairs: C (m x k) = Y W with 2-SM products (tcgen05 cta_group::2).
+// A cluster of two CTAs takes 256 x 256 output tiles: CTA r of the pair holds
+// rows 128 r .. 128 r + 127 of the tile's Y rows (A) and of its 256 W columns
+// (B) in its own shared memory, and the leader (r = 0) issues one
+// 256 x 256 x 16 UMMA per product that reads both halves of B; each CTA's TMEM
+// receives its 128 rows x 256 columns.  Per SM and per product this moves half
+// the B bytes of the single-SM 128 x 256 tile through shared memory (TMA
+// writes and tensor-core reads), which is what bounds that kernel; a stage is
+// 32 KiB (A hi/lo, B-half hi/lo at K = 32), six stages per CTA.
+// Barriers: the stage-full barrier of the leader counts both CTAs' TMA bytes
+// (the peer's loads signal it across the pair); stage-empty and tile-full
+// barriers live in both CTAs and are signalled by the leader's multicast
+// commits; the tile-empty barrier of the leader collects one arrival per
+// epilogue warp of both CTAs.  Every wait is bounded as in the other kernels;
+// both CTAs always reach the TMEM allocation and the closing cluster barrier.
+// ---------------------------------------------------------------------------
+struct PairCfg {
+  static constexpr int BK = 32;                      // K per stage (64-byte rows, 64-byte swizzle)
+  static constexpr uint32_t TILE = 128u * BK * 2;    // 128 rows x BK fp16
+  static constexpr uint32_t STAGE = 4 * TILE;        // A hi, A lo, B-half hi, B-half lo
+  static constexpr int STAGES = 6;
+  static constexpr int EPI = 8;                      // epilogue warps
+  static constexpr int THREADS = 32 * (EPI + 2);     // + UMMA issuer, TMA producer
+  static constexpr uint32_t STG = EPI * 4096u;
+};
+constexpr size_t pair_smem() {
+  return (size_t)PairCfg::STAGES * PairCfg::STAGE + PairCfg::STG + 1024;
+}
+
+__device__ __forceinline__ uint32_t cluster_rank() {
+  uint32_t r;
+  asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+  return r;
+}
+// shared::cluster address of this CTA's variable at `saddr` in CTA `rank`
+__device__ __forceinline__ uint32_t map_to_rank(uint32_t saddr, uint32_t rank) {
+  uint32_t d;
+  asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(d) : "r"(saddr), "r"(rank));
+  return d;
+}
+__device__ __forceinline__ void cluster_sync_all() {
+  asm volatile(
+      "barrier.cluster.arrive.release.aligned;\n\t"
+      "barrier.cluster.wait.acquire.aligned;" ::: "memory");
+}
+__device__ __forceinline__ void mbar_arrive_remote(uint32_t caddr) {
+  asm volatile("mbarrier.arrive.release.cluster.shared::cluster.b64 _, [%0];" ::"r"(caddr)
+               : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait_cl(uint64_t* bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.acquire.cluster.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+// bounded wait with cluster-scope acquire (arrivals from the other CTA)
+__device__ __forceinline__ bool mbar_wait_cl(uint64_t* bar, uint32_t parity,
+                                             volatile int* abort_flag, int* err) {
+  if (mbar_try_wait_cl(bar, parity)) return true;
+  const uint64_t t0 = gtimer();
+  uint32_t spins = 0;
+  while (true) {
+    if (mbar_try_wait_cl(bar, parity)) return true;
+    if (*abort_flag) return false;
+    if ((++spins & 1023u) == 0 && err && *(volatile int*)err == PLOM_NUM_TIMEOUT) {
+      *abort_flag = 1;
+      return false;
+    }
+    if (gtimer() - t0 > WAIT_NS) {
+      *abort_flag = 1;
+      if (err) atomicMax(err, PLOM_NUM_TIMEOUT);
+      return false;
+    }
+  }
+}
+// TMEM of both CTAs of the pair: one warp of each CTA takes part
+__device__ __forceinline__ void tmem_alloc_pair(uint32_t* dst, uint32_t ncols) {
+  asm volatile("tcgen05.alloc.cta_group::2.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                   smem_u32(dst)),
+               "r"(ncols)
+               : "memory");
+}
+__device__ __forceinline__ void tmem_relinquish_pair() {
+  asm volatile("tcgen05.relinquish_alloc_permit.cta_group::2.sync.aligned;" ::: "memory");
+}
+__device__ __forceinline__ void tmem_dealloc_pair(uint32_t taddr, uint32_t ncols) {
+  asm volatile("tcgen05.dealloc.cta_group::2.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(ncols)
+               : "memory");
+}
+__device__ __forceinline__ void mma_f16_pair(uint32_t d_tmem, uint64_t adesc, uint64_t bdesc,
+                                             uint32_t idesc, uint32_t accum) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "setp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::2.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(d_tmem),
+      "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accum)
+      : "memory");
+}
+// arrive on the barrier at the same offset in both CTAs of the pair once the
+// issuing thread's earlier products are done
+__device__ __forceinline__ void mma_commit_pair(uint64_t* bar) {
+  asm volatile(
+      "tcgen05.commit.cta_group::2.mbarrier::arrive::one.shared::cluster.multicast::cluster.b64 "
+      "[%0], %1;" ::"r"(smem_u32(bar)),
+      "h"((uint16_t)3)
+      : "memory");
+}
+// TMA load into this CTA's shared memory whose completion is counted on a
+// barrier of either CTA of the pair (`bar`: shared::cluster address)
+__device__ __forceinline__ void tma_load_3d_pair(uint32_t dst, const CUtensorMap* map, int x, int y,
+                                                 int z, uint32_t bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.3d.cta_group::2.shared::cluster.global.mbarrier::complete_tx::bytes "
+      "[%0], [%1, {%2, %3, %4}], [%5];" ::"r"(dst),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(z), "r"(bar)
+      : "memory");
+}
+
+// Tiles: 256-row pair blocks q x 256-column blocks cb (tiles = row_pairs x
+// col_tiles); one problem (no batch).  upper: W upper triangular, column block
+// cb takes the K blocks below (cb + 1) 256.  by_rows as in apply16_kernel, over
+// pairs.
+__global__ void __launch_bounds__(PairCfg::THREADS, 1)
+    apply16p_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
+                    int64_t m, int kblocks, int k, int64_t col_tiles, int64_t tiles,
+                    const float* __restrict__ f, ApplyOut out, int* err, int64_t mp, int upper,
+                    int by_rows) {
+  constexpr int S = PairCfg::STAGES, BK = PairCfg::BK, EPI = PairCfg::EPI;
+  constexpr uint32_t TILE = PairCfg::TILE, STAGE = PairCfg::STAGE;
+  extern __shared__ uint8_t smem_raw[];
+  __shared__ uint64_t full_bar[S], empty_bar[S], tfull, tempty;
+  __shared__ uint32_t tmem_sh;
+  __shared__ int abort_sh;
+  const uint32_t base = (smem_u32(smem_raw) + 1023u) & ~1023u;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const uint32_t rank = cluster_rank();  // 0: the pair's leader (issues the products)
+  const int64_t G = gridDim.x >> 1, pid = blockIdx.x >> 1;
+  const int64_t units = tiles / col_tiles;  // 256-row pair blocks
+  const int64_t my_tiles =
+      by_rows ? (pid < units ? ((units - 1 - pid) / G + 1) * col_tiles : 0) : (tiles + G - 1) / G;
+  auto pair_tile = [&](int64_t it) -> int64_t {
+    if (by_rows) return (pid + (it / col_tiles) * G) * col_tiles + it % col_tiles;
+    return it * G + ((it & 1) ? G - 1 - pid : pid);
+  };
+  auto pair_kend = [&](int cb) -> int {
+    return upper ? min(kblocks, (cb + 1) * (256 / BK)) : kblocks;
+  };
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < S; ++s) {
+      mbar_init(&full_bar[s], 1);
+      mbar_init(&empty_bar[s], 1);
+    }
+    mbar_init(&tfull, 1);
+    mbar_init(&tempty, 2 * EPI);
+    abort_sh = 0;
+    mbar_fence_init();
+  }
+  if (warp == EPI) {
+    tmem_alloc_pair(&tmem_sh, 512);  // main 256 + correction 256 columns
+    tmem_relinquish_pair();
+  }
+  if (warp == EPI + 1 && lane == 0) {
+    tma_prefetch_map(&tmA);
+    tma_prefetch_map(&tmB);
+  }
+  fence_before();
+  __syncthreads();
+  cluster_sync_all();  // both CTAs' barriers initialised and TMEM allocated
+  fence_after();
+  const uint32_t tmem = tmem_sh;
+
+  if (warp == EPI + 1) {
+    // ---- TMA producer of this CTA's halves; the bytes land on the leader's barrier
+    if (lane == 0) {
+      const uint32_t full0 = map_to_rank(smem_u32(&full_bar[0]), 0);
+      int64_t g = 0;
+      bool ok = true;
+      for (int64_t it = 0; it < my_tiles && ok; ++it) {
+        const int64_t t = pair_tile(it);
+        if (t >= tiles) continue;
+        const int64_t q = t / col_tiles;
+        const int cb = (int)(t - q * col_tiles);
+        const int ya = (int)(q * 256 + 128 * (int64_t)rank), yb = cb * 256 + 128 * (int)rank;
+        const int kend = pair_kend(cb);
+        for (int kb = 0; kb < kend; ++kb, ++g) {
+          const int s = (int)(g % S);
+          const uint32_t ph = (uint32_t)(g / S) & 1u;
+          if (!mbar_wait(&empty_bar[s], ph ^ 1u, &abort_sh, err)) {
+            ok = false;
+            break;
+          }
+          if (rank == 0) mbar_expect_tx(&full_bar[s], 2 * STAGE);
+          const uint32_t st = base + s * STAGE, fb = full0 + 8u * (uint32_t)s;
+          tma_load_3d_pair(st, &tmA, kb * BK, ya, 0, fb);
+          tma_load_3d_pair(st + TILE, &tmA, kb * BK, ya, 1, fb);
+          tma_load_3d_pair(st + 2 * TILE, &tmB, kb * BK, yb, 0, fb);
+          tma_load_3d_pair(st + 3 * TILE, &tmB, kb * BK, yb, 1, fb);
+        }
+      }
+      // the last commits on this CTA's stage barriers land before it may exit
+      for (int64_t u = (g > S ? g - S : 0); ok && u < g; ++u)
+        ok = mbar_wait(&empty_bar[u % S], (uint32_t)(u / S) & 1u, &abort_sh, err);
+    }
+  } else if (warp == EPI) {
+    // ---- UMMA issuer (leader only)
+    if (lane == 0 && rank == 0) {
+      constexpr uint32_t idesc = idesc_f16(256, 256, 0, 0);
+      const uint32_t dmain = tmem, dcorr = tmem + 256u;
+      int64_t g = 0;
+      int i = 0;
+      bool ok = true;
+      for (int64_t it = 0; it < my_tiles && ok; ++it) {
+        const int64_t t = pair_tile(it);
+        if (t >= tiles) continue;
+        if (!mbar_wait_cl(&tempty, ((uint32_t)i & 1u) ^ 1u, &abort_sh, err)) {
+          ok = false;
+          break;
+        }
+        fence_after();
+        const int kend = pair_kend((int)(t % col_tiles));
+        for (int kb = 0; kb < kend; ++kb, ++g) {
+          const int s = (int)(g % S);
+          const uint32_t ph = (uint32_t)(g / S) & 1u;
+          if (!mbar_wait(&full_bar[s], ph, &abort_sh, err)) {
+            ok = false;
+            break;
+          }
+          fence_after();
+          const uint32_t st = base + s * STAGE;
+#pragma unroll
+          for (int kk = 0; kk < BK / 16; ++kk) {
+            const uint32_t adv = (uint32_t)kk * 32u;  // 16 fp16 along K
+            const uint64_t dAH = desc_kmajor<BK>(st + adv);
+            const uint64_t dAL = desc_kmajor<BK>(st + TILE + adv);
+            const uint64_t dBH = desc_kmajor<BK>(st + 2 * TILE + adv);
+            const uint64_t dBL = desc_kmajor<BK>(st + 3 * TILE + adv);
+            const uint32_t acc = (kb > 0 || kk > 0) ? 1u : 0u;
+            mma_f16_pair(dmain, dAH, dBH, idesc, acc);
+            mma_f16_pair(dcorr, dAH, dBL, idesc, acc);
+            mma_f16_pair(dcorr, dAL, dBH, idesc, 1u);
+          }
+          mma_commit_pair(&empty_bar[s]);
+        }
+        if (ok) mma_commit_pair(&tfull);
+        ++i;
+      }
+    }
+  } else {
+    // ---- epilogue (warps 0-7) of this CTA's 128 rows: TMEM -> registers,
+    // release the accumulator to the leader, then scale and store
+    uint4* stg = reinterpret_cast<uint4*>(smem_raw + (base - smem_u32(smem_raw)) + S * STAGE +
+                                          warp * 4096);
+    const uint32_t tempty_leader = map_to_rank(smem_u32(&tempty), 0);
+    const int quarter = warp & 3, half = warp >> 2;
+    const bool c_vec = out.C && ((out.ldc & 3) == 0) &&
+                       ((reinterpret_cast<uintptr_t>(out.C) & 15) == 0);
+    int i = 0;
+    for (int64_t it = 0; it < my_tiles; ++it) {
+      const int64_t t = pair_tile(it);
+      if (t >= tiles) continue;
+      const bool ready = mbar_wait(&tfull, (uint32_t)i & 1u, &abort_sh, err);
+      __syncwarp();
+      if (!__all_sync(0xffffffffu, ready)) break;
+      fence_after();
+      const int64_t q = t / col_tiles, cb = t - q * col_tiles;
+      const int64_t row0 = q * 256 + 128 * (int64_t)rank + quarter * 32;
+      float vv[4][32];
+#pragma unroll
+      for (int c4 = 0; c4 < 4; ++c4) {
+        const int col0 = (int)(cb * 256) + (4 * half + c4) * 32;
+#pragma unroll
+        for (int hh = 0; hh < 2; ++hh) {
+          uint32_t rm[16], rc[16];
+          const uint32_t ta = tmem + ((uint32_t)(quarter * 32) << 16) +
+                              (uint32_t)((4 * half + c4) * 32 + hh * 16);
+          tmem_ld16(ta, rm);
+          tmem_ld16(ta + 256u, rc);
+          tmem_wait_ld();
+#pragma unroll
+          for (int j = 0; j < 16; ++j)
+            vv[c4][hh * 16 + j] = (__uint_as_float(rm[j]) + __uint_as_float(rc[j])) *
+                                  __ldg(f + col0 + hh * 16 + j);
+        }
+      }
+      fence_before();
+      __syncwarp();
+      if (lane == 0) {
+        if (rank == 0)
+          mbar_arrive(&tempty);
+        else
+          mbar_arrive_remote(tempty_leader);
+      }
+#pragma unroll
+      for (int c4 = 0; c4 < 4; ++c4)
+        apply_store_chunk(vv[c4], (int)(cb * 256) + (4 * half + c4) * 32, stg, lane, out, k, m, mp,
+                          0, row0, c_vec);
+      ++i;
+    }
+  }
+  fence_before();
+  __syncthreads();
+  cluster_sync_all();  // no arrival or load of the other CTA is still headed here
+  if (warp == EPI) {
+    __syncwarp();
+    fence_after();
+    tmem_dealloc_pair(tmem, 512);
+  }
+}
+
+// ---------------------------------------------------------------------------
 // renormalisation of long-factor columns of U = Q2 M (see renorm_long_columns).
 // Deterministic: the columns are chosen by an ordered scan (the RN_MAX longest
 // factor columns above the threshold, ties to the lower index, listed in index
@@ -1758,6 +2074,32 @@ static bool make_map_planes(CUtensorMap* map, const __half* base, uint64_t inner
 }
 
 int64_t packed_ld(int64_t N) { return cdiv(N, 64) * 64; }
+
+// two-CTA clusters of apply16p_kernel resident at once (0: not available)
+static int pair_clusters() {
+  static int n = -1;
+  if (n < 0) {
+    n = 0;
+    if (cudaFuncSetAttribute(hp::apply16p_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)hp::pair_smem()) == cudaSuccess) {
+      cudaLaunchConfig_t cfg = {};
+      cfg.gridDim = dim3(2 * (unsigned)num_sms());
+      cfg.blockDim = dim3(hp::PairCfg::THREADS);
+      cfg.dynamicSmemBytes = hp::pair_smem();
+      cudaLaunchAttribute at[1];
+      at[0].id = cudaLaunchAttributeClusterDimension;
+      at[0].val.clusterDim.x = 2;
+      at[0].val.clusterDim.y = 1;
+      at[0].val.clusterDim.z = 1;
+      cfg.attrs = at;
+      cfg.numAttrs = 1;
+      int c = 0;
+      if (cudaOccupancyMaxActiveClusters(&c, hp::apply16p_kernel, &cfg) == cudaSuccess) n = c;
+    }
+    cudaGetLastError();
+  }
+  return n;
+}
 
 // rows per problem in the planes: m for one problem; for a batch, m rounded
 // up to 128 so that no stage or output tile of one problem reaches the next
@@ -2097,7 +2439,13 @@ int apply_packed(const Packed& p, const double* W, int64_t ldw, int64_t k, float
   // accumulator buffers overlap them (measured: 0.70 of the dense product's
   // time for 0.56 of its products, against 0.75 with 256-wide tiles and
   // 128-wide products on the diagonal band)
-  const int TN = (k > 128 && !(upper && k == p.N)) ? tuning().apply_dense_tn : 128;
+  const bool tri_w = upper && k == p.N;
+  // SM pairs (apply16p_kernel) for one problem wider than 128 columns, when
+  // enabled for its kind of W and the device runs two-CTA clusters of it
+  const bool pair = batch == 1 && k > 128 &&
+                    (tuning().apply_pair == 2 || (tuning().apply_pair == 1 && !tri_w)) &&
+                    pair_clusters() > 0;
+  const int TN = pair ? 256 : (k > 128 && !tri_w) ? tuning().apply_dense_tn : 128;
   const int64_t col_tiles = cdiv(k, TN);
   const int fstride = (int)(col_tiles * TN);
   __half* bhi = ws.take<__half>((size_t)(2 * batch * k * ldk));
@@ -2135,6 +2483,7 @@ int apply_packed(const Packed& p, const double* W, int64_t ldw, int64_t k, float
   }
   CUtensorMap tmA, tmB;
   const uint32_t bk = TN == 256 ? (uint32_t)hp::ApplyCfg<256>::BK : (uint32_t)hp::ApplyCfg<128>::BK;
+  static_assert(hp::ApplyCfg<256>::BK == hp::PairCfg::BK, "pair tiles share the 256-wide maps");
   PLOM_REQUIRE(make_map_planes(&tmA, p.hi, (uint64_t)p.ld, (uint64_t)(batch * p.mp),
                                (uint64_t)p.ld, bk, 128, (uint64_t)p.pstride, bk == 32) &&
                    make_map_planes(&tmB, bhi, (uint64_t)ldk, (uint64_t)(batch * k), (uint64_t)ldk,
@@ -2160,7 +2509,30 @@ int apply_packed(const Packed& p, const double* W, int64_t ldw, int64_t k, float
   // columns j >= i only
   const bool tri = tri_pre;
   const double flops = tri ? (double)m * p.N * (p.N + 1) * batch : 2.0 * m * p.N * k * batch;
-  ProfScope prof("tc_apply_f16x3", st, flops, 4.0 * ((double)m * p.ld + (double)m * k) * batch);
+  ProfScope prof(pair ? "tc_apply_f16x3_pair" : "tc_apply_f16x3", st, flops,
+                 4.0 * ((double)m * p.ld + (double)m * k) * batch);
+  if (pair) {
+    const int64_t pairs = cdiv(p.mp, 256), ptiles = pairs * col_tiles;
+    const int pby_rows = (tri && pairs >= 2 * (int64_t)pair_clusters()) ? 1 : 0;
+    const int64_t clusters = std::min<int64_t>(pby_rows ? pairs : ptiles, pair_clusters());
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)(2 * clusters));
+    cfg.blockDim = dim3(hp::PairCfg::THREADS);
+    cfg.dynamicSmemBytes = hp::pair_smem();
+    cfg.stream = st;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = 2;
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    PLOM_CHECK_CUDA(cudaLaunchKernelEx(&cfg, hp::apply16p_kernel, tmA, tmB, m,
+                                       (int)(ldk / hp::PairCfg::BK), (int)k, col_tiles, ptiles,
+                                       (const float*)f, o, err, p.mp, tri ? 1 : 0, pby_rows));
+    PLOM_CHECK_LAUNCH();
+    return PLOM_OK;
+  }
   if (TN == 256)
     hp::apply16_kernel<256><<<grid, hp::ApplyWarps<256>::THREADS, hp::apply_smem<256>(), st>>>(
         tmA, tmB, m, (int)(ldk / hp::ApplyCfg<256>::BK), (int)k, col_tiles, tiles, f, o, err, p.mp,

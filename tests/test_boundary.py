@@ -102,7 +102,7 @@ def test_workspace_dry_runs_launch_nothing(dtype, prec):
 def test_tuning_parameters_round_trip_and_range():
     lib = L.load()
     keys = [b"gram_wave_mult", b"reduce_blocks_per_sm", b"apply_dense_tn", b"apply_dense_by_rows",
-            b"pass1_chunks"]
+            b"pass1_chunks", b"apply_pair"]
     old = {k: lib.plom_get_tuning(k) for k in keys}
     try:
         assert all(v >= 0 for v in old.values())
@@ -110,6 +110,7 @@ def test_tuning_parameters_round_trip_and_range():
         assert lib.plom_get_tuning(b"gram_wave_mult") == 2.0
         assert lib.plom_set_tuning(b"apply_dense_tn", 192.0) != 0  # 128 or 256 only
         assert lib.plom_set_tuning(b"gram_wave_mult", 2.5) != 0    # integers only
+        assert lib.plom_set_tuning(b"apply_pair", 3.0) != 0        # 0, 1 or 2
         assert lib.plom_set_tuning(b"no_such_key", 1.0) != 0
         assert lib.plom_get_tuning(b"no_such_key") == -1.0
     finally:
