@@ -63,7 +63,8 @@ int plom_version(void);
 
 /* Run-time schedule and tile parameters of the tall tensor-core kernels (no
    counterpart in pyLOM, whose products are LAPACK/BLAS calls): the Gram's
-   work items per SM per wave ("gram_wave_mult", 1-32), the resident blocks
+   work items per SM per wave ("gram_wave_mult", 1-32; "gram_wide_wave_mult",
+   1-256, for Grams wider than 128 columns), the resident blocks
    per SM of its slab reduction ("reduce_blocks_per_sm", 1-16), the output
    tile width of dense products wider than 128 columns ("apply_dense_tn",
    128 or 256), whether such products give each CTA whole row blocks

@@ -1,7 +1,8 @@
 """Autotuner of the tall tensor-core kernels' schedule and tile parameters.
 
 The parameters (plom_set_tuning, include/plom.h) are the Gram's work items
-per SM per wave (row-chunk granularity), the resident blocks per SM of the
+per SM per wave (row-chunk granularity; narrow and wide Grams each their
+own), the resident blocks per SM of the
 Gram's slab reduction, the output tile width of dense products wider than
 128 columns, whether those products give each CTA whole row blocks and the
 row chunks of a large FP32 input packed beside the first Gram and the
@@ -27,6 +28,7 @@ import time
 
 CANDIDATES = {
     "gram_wave_mult": [1, 2, 4, 8],
+    "gram_wide_wave_mult": [8, 16, 32, 64, 128],
     "reduce_blocks_per_sm": [2, 3, 4],
     "apply_dense_tn": [128, 256],
     "apply_dense_by_rows": [0, 1],

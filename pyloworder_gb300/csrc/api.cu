@@ -100,6 +100,8 @@ extern "C" int plom_set_tuning(const char* key, double value) {
   Tuning& t = tuning();
   if (k == "gram_wave_mult" && v >= 1 && v <= 32) {
     t.gram_wave_mult = v;
+  } else if (k == "gram_wide_wave_mult" && v >= 1 && v <= 256) {
+    t.gram_wide_wave_mult = v;
   } else if (k == "reduce_blocks_per_sm" && v >= 1 && v <= 16) {
     t.reduce_blocks_per_sm = v;
   } else if (k == "apply_dense_tn" && (v == 128 || v == 256)) {
@@ -123,6 +125,7 @@ extern "C" double plom_get_tuning(const char* key) {
   const std::string k(key);
   const Tuning& t = tuning();
   if (k == "gram_wave_mult") return t.gram_wave_mult;
+  if (k == "gram_wide_wave_mult") return t.gram_wide_wave_mult;
   if (k == "reduce_blocks_per_sm") return t.reduce_blocks_per_sm;
   if (k == "apply_dense_tn") return t.apply_dense_tn;
   if (k == "apply_dense_by_rows") return t.apply_dense_by_rows;

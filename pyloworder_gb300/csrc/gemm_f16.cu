@@ -2178,11 +2178,12 @@ int pack_f32(const float* Y, int64_t ld, int64_t m, int64_t N, Packed& p, Arena&
 // work items of the Gram: tiles x chunks, the fewest whole waves of the GPU
 // (one CTA per SM) that the tile count divides, with chunks of at least four
 // stages; fewer chunks keep the partial slabs (and their reduction) small
-static int gram16_chunks(int64_t m, int tiles, int bk = hp::G_BK) {
+static int gram16_chunks(int64_t m, int tiles, int bk = hp::G_BK, int wave_mult = 0) {
   const int64_t sms = num_sms();
   const int64_t maxc = std::max<int64_t>(1, cdiv(m, 4 * (int64_t)bk));
+  if (wave_mult <= 0) wave_mult = tuning().gram_wave_mult;
   for (int64_t waves = 1; waves <= 64; ++waves) {
-    const int64_t items = waves * sms * tuning().gram_wave_mult;
+    const int64_t items = waves * sms * wave_mult;
     if (items % tiles) continue;
     return (int)std::max<int64_t>(1, std::min(maxc, items / tiles));
   }
@@ -2190,10 +2191,14 @@ static int gram16_chunks(int64_t m, int tiles, int bk = hp::G_BK) {
 }
 
 // Gram of operands wider than 128 columns: 128 x 256 tiles (gram16w_kernel);
-// row chunks are whole 4,096-row sub-chunks, each with its own FP32 slab
+// row chunks are whole 4,096-row sub-chunks, each with its own FP32 slab.
+// Short chunks keep the tiles of one chunk that run at the same time close
+// together in the rows, so that they share its panels in L2 (the slabs do
+// not depend on the chunking)
 static void wide_chunks(int64_t m, int items_per_chunk, int& chunks_eff, int64_t& rpc,
                         int& subs_per_chunk, int& nsubs) {
-  const int chunks = gram16_chunks(m, items_per_chunk, hp::G_KSUB / 4);
+  const int chunks =
+      gram16_chunks(m, items_per_chunk, hp::G_KSUB / 4, tuning().gram_wide_wave_mult);
   rpc = cdiv(cdiv(m, chunks), hp::G_KSUB) * hp::G_KSUB;
   chunks_eff = (int)std::max<int64_t>(1, cdiv(m, rpc));
   subs_per_chunk = (int)(rpc / hp::G_KSUB);

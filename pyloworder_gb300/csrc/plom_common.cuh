@@ -72,11 +72,12 @@ struct Arena {
 // on GB300.
 struct Tuning {
   int gram_wave_mult = 4;        // Gram work items per SM per wave (row-chunk granularity)
+  int gram_wide_wave_mult = 32;  // the same for Grams wider than 128 columns (128 x 256 tiles)
   int reduce_blocks_per_sm = 3;  // resident blocks of the Gram slab reduction
   int apply_dense_tn = 256;      // output tile width of dense products wider than 128 (128 or 256)
   int apply_dense_by_rows = 0;   // dense products: whole row blocks per CTA (1) or single tiles (0)
   int pass1_chunks = 8;          // large FP32 inputs: row chunks packed beside the first Gram (1: off)
-  int apply_pair = 0;            // products on SM pairs (2-SM UMMA): 0 off, 1 dense, 2 dense + triangular
+  int apply_pair = 1;            // products on SM pairs (2-SM UMMA): 0 off, 1 dense, 2 dense + triangular
 };
 Tuning& tuning();
 
