@@ -1546,32 +1546,43 @@ __global__ void __launch_bounds__(ApplyWarps<TN>::THREADS, 1)
 
 // ---------------------------------------------------------------------------
 // apply on SM pairs: C (m x k) = Y W with 2-SM products (tcgen05 cta_group::2).
-// A cluster of two CTAs takes 256 x 256 output tiles: CTA r of the pair holds
-// rows 128 r .. 128 r + 127 of the tile's Y rows (A) and of its 256 W columns
-// (B) in its own shared memory, and the leader (r = 0) issues one
-// 256 x 256 x 16 UMMA per product that reads both halves of B; each CTA's TMEM
-// receives its 128 rows x 256 columns.  Per SM and per product this moves half
-// the B bytes of the single-SM 128 x 256 tile through shared memory (TMA
-// writes and tensor-core reads), which is what bounds that kernel; a stage is
-// 32 KiB (A hi/lo, B-half hi/lo at K = 32), six stages per CTA.
+// A cluster of two CTAs takes 256 x TN output tiles: CTA r of the pair holds
+// rows 128 r .. 128 r + 127 of the tile's 256 Y rows (A) and W columns
+// TN r / 2 .. TN (r + 1) / 2 - 1 of its TN (B) in its own shared memory, and
+// the leader (r = 0) issues one 256 x TN x 16 UMMA per product that reads both
+// halves of B; each CTA's TMEM receives its 128 rows x TN columns.  Per SM and
+// per product this moves half the B bytes of the single-SM 128 x TN tile
+// through shared memory (TMA writes and tensor-core reads).
+//  TN = 256 (dense W wider than 128 columns): K = 32 per stage (64-byte
+//    swizzle), 32 KiB stages x 6; the two accumulators fill TMEM, so the
+//    epilogue reads the tile into registers and releases TMEM before its stores.
+//  TN = 128 (upper-triangular W: column block cb takes exactly the K blocks
+//    below (cb + 1) 128): K = 64 per stage (128-byte swizzle), 48 KiB stages x
+//    4, two accumulator buffers, so the epilogue of one tile overlaps the
+//    products of the next.  Per SM it has the bytes-per-product ratio of the
+//    single-SM 128 x 256 tile instead of the 128 x 128 one.
 // Barriers: the stage-full barrier of the leader counts both CTAs' TMA bytes
 // (the peer's loads signal it across the pair); stage-empty and tile-full
 // barriers live in both CTAs and are signalled by the leader's multicast
-// commits; the tile-empty barrier of the leader collects one arrival per
+// commits; the tile-empty barriers of the leader collect one arrival per
 // epilogue warp of both CTAs.  Every wait is bounded as in the other kernels;
 // both CTAs always reach the TMEM allocation and the closing cluster barrier.
 // ---------------------------------------------------------------------------
+template <int TN>
 struct PairCfg {
-  static constexpr int BK = 32;                      // K per stage (64-byte rows, 64-byte swizzle)
-  static constexpr uint32_t TILE = 128u * BK * 2;    // 128 rows x BK fp16
-  static constexpr uint32_t STAGE = 4 * TILE;        // A hi, A lo, B-half hi, B-half lo
-  static constexpr int STAGES = 6;
-  static constexpr int EPI = 8;                      // epilogue warps
-  static constexpr int THREADS = 32 * (EPI + 2);     // + UMMA issuer, TMA producer
+  static constexpr int BK = TN == 256 ? 32 : 64;               // K per stage
+  static constexpr uint32_t A_TILE = 128u * BK * 2;            // 128 rows x BK fp16
+  static constexpr uint32_t B_HALF = (uint32_t)(TN / 2) * BK * 2;
+  static constexpr uint32_t STAGE = 2 * A_TILE + 2 * B_HALF;   // A hi, A lo, B-half hi, B-half lo
+  static constexpr int STAGES = TN == 256 ? 6 : 4;
+  static constexpr int NBUF = TN == 256 ? 1 : 2;               // TMEM accumulator buffers
+  static constexpr int EPI = 8;                                // epilogue warps
+  static constexpr int THREADS = 32 * (EPI + 2);               // + UMMA issuer, TMA producer
   static constexpr uint32_t STG = EPI * 4096u;
 };
+template <int TN>
 constexpr size_t pair_smem() {
-  return (size_t)PairCfg::STAGES * PairCfg::STAGE + PairCfg::STG + 1024;
+  return (size_t)PairCfg<TN>::STAGES * PairCfg<TN>::STAGE + PairCfg<TN>::STG + 1024;
 }
 
 __device__ __forceinline__ uint32_t cluster_rank() {
@@ -1668,19 +1679,21 @@ __device__ __forceinline__ void tma_load_3d_pair(uint32_t dst, const CUtensorMap
       : "memory");
 }
 
-// Tiles: 256-row pair blocks q x 256-column blocks cb (tiles = row_pairs x
+// Tiles: 256-row pair blocks q x TN-column blocks cb (tiles = row_pairs x
 // col_tiles); one problem (no batch).  upper: W upper triangular, column block
-// cb takes the K blocks below (cb + 1) 256.  by_rows as in apply16_kernel, over
+// cb takes the K blocks below (cb + 1) TN.  by_rows as in apply16_kernel, over
 // pairs.
-__global__ void __launch_bounds__(PairCfg::THREADS, 1)
+template <int TN>
+__global__ void __launch_bounds__(PairCfg<TN>::THREADS, 1)
     apply16p_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
                     int64_t m, int kblocks, int k, int64_t col_tiles, int64_t tiles,
                     const float* __restrict__ f, ApplyOut out, int* err, int64_t mp, int upper,
                     int by_rows) {
-  constexpr int S = PairCfg::STAGES, BK = PairCfg::BK, EPI = PairCfg::EPI;
-  constexpr uint32_t TILE = PairCfg::TILE, STAGE = PairCfg::STAGE;
+  using C = PairCfg<TN>;
+  constexpr int S = C::STAGES, BK = C::BK, EPI = C::EPI, NBUF = C::NBUF;
+  constexpr uint32_t A_TILE = C::A_TILE, B_HALF = C::B_HALF, STAGE = C::STAGE;
   extern __shared__ uint8_t smem_raw[];
-  __shared__ uint64_t full_bar[S], empty_bar[S], tfull, tempty;
+  __shared__ uint64_t full_bar[S], empty_bar[S], tfull[NBUF], tempty[NBUF];
   __shared__ uint32_t tmem_sh;
   __shared__ int abort_sh;
   const uint32_t base = (smem_u32(smem_raw) + 1023u) & ~1023u;
@@ -1695,7 +1708,7 @@ __global__ void __launch_bounds__(PairCfg::THREADS, 1)
     return it * G + ((it & 1) ? G - 1 - pid : pid);
   };
   auto pair_kend = [&](int cb) -> int {
-    return upper ? min(kblocks, (cb + 1) * (256 / BK)) : kblocks;
+    return upper ? min(kblocks, (cb + 1) * (TN / BK)) : kblocks;
   };
 
   if (threadIdx.x == 0) {
@@ -1703,13 +1716,15 @@ __global__ void __launch_bounds__(PairCfg::THREADS, 1)
       mbar_init(&full_bar[s], 1);
       mbar_init(&empty_bar[s], 1);
     }
-    mbar_init(&tfull, 1);
-    mbar_init(&tempty, 2 * EPI);
+    for (int b = 0; b < NBUF; ++b) {
+      mbar_init(&tfull[b], 1);
+      mbar_init(&tempty[b], 2 * EPI);
+    }
     abort_sh = 0;
     mbar_fence_init();
   }
   if (warp == EPI) {
-    tmem_alloc_pair(&tmem_sh, 512);  // main 256 + correction 256 columns
+    tmem_alloc_pair(&tmem_sh, 512);  // NBUF x (main TN + correction TN) columns
     tmem_relinquish_pair();
   }
   if (warp == EPI + 1 && lane == 0) {
@@ -1733,7 +1748,7 @@ __global__ void __launch_bounds__(PairCfg::THREADS, 1)
         if (t >= tiles) continue;
         const int64_t q = t / col_tiles;
         const int cb = (int)(t - q * col_tiles);
-        const int ya = (int)(q * 256 + 128 * (int64_t)rank), yb = cb * 256 + 128 * (int)rank;
+        const int ya = (int)(q * 256 + 128 * (int64_t)rank), yb = cb * TN + (TN / 2) * (int)rank;
         const int kend = pair_kend(cb);
         for (int kb = 0; kb < kend; ++kb, ++g) {
           const int s = (int)(g % S);
@@ -1745,9 +1760,9 @@ __global__ void __launch_bounds__(PairCfg::THREADS, 1)
           if (rank == 0) mbar_expect_tx(&full_bar[s], 2 * STAGE);
           const uint32_t st = base + s * STAGE, fb = full0 + 8u * (uint32_t)s;
           tma_load_3d_pair(st, &tmA, kb * BK, ya, 0, fb);
-          tma_load_3d_pair(st + TILE, &tmA, kb * BK, ya, 1, fb);
-          tma_load_3d_pair(st + 2 * TILE, &tmB, kb * BK, yb, 0, fb);
-          tma_load_3d_pair(st + 3 * TILE, &tmB, kb * BK, yb, 1, fb);
+          tma_load_3d_pair(st + A_TILE, &tmA, kb * BK, ya, 1, fb);
+          tma_load_3d_pair(st + 2 * A_TILE, &tmB, kb * BK, yb, 0, fb);
+          tma_load_3d_pair(st + 2 * A_TILE + B_HALF, &tmB, kb * BK, yb, 1, fb);
         }
       }
       // the last commits on this CTA's stage barriers land before it may exit
@@ -1757,19 +1772,20 @@ __global__ void __launch_bounds__(PairCfg::THREADS, 1)
   } else if (warp == EPI) {
     // ---- UMMA issuer (leader only)
     if (lane == 0 && rank == 0) {
-      constexpr uint32_t idesc = idesc_f16(256, 256, 0, 0);
-      const uint32_t dmain = tmem, dcorr = tmem + 256u;
+      constexpr uint32_t idesc = idesc_f16(256, TN, 0, 0);
       int64_t g = 0;
       int i = 0;
       bool ok = true;
       for (int64_t it = 0; it < my_tiles && ok; ++it) {
         const int64_t t = pair_tile(it);
         if (t >= tiles) continue;
-        if (!mbar_wait_cl(&tempty, ((uint32_t)i & 1u) ^ 1u, &abort_sh, err)) {
+        const int b = i % NBUF;
+        if (!mbar_wait_cl(&tempty[b], (((uint32_t)(i / NBUF)) & 1u) ^ 1u, &abort_sh, err)) {
           ok = false;
           break;
         }
         fence_after();
+        const uint32_t dmain = tmem + (uint32_t)(b * 2 * TN), dcorr = dmain + (uint32_t)TN;
         const int kend = pair_kend((int)(t % col_tiles));
         for (int kb = 0; kb < kend; ++kb, ++g) {
           const int s = (int)(g % S);
@@ -1784,9 +1800,9 @@ __global__ void __launch_bounds__(PairCfg::THREADS, 1)
           for (int kk = 0; kk < BK / 16; ++kk) {
             const uint32_t adv = (uint32_t)kk * 32u;  // 16 fp16 along K
             const uint64_t dAH = desc_kmajor<BK>(st + adv);
-            const uint64_t dAL = desc_kmajor<BK>(st + TILE + adv);
-            const uint64_t dBH = desc_kmajor<BK>(st + 2 * TILE + adv);
-            const uint64_t dBL = desc_kmajor<BK>(st + 3 * TILE + adv);
+            const uint64_t dAL = desc_kmajor<BK>(st + A_TILE + adv);
+            const uint64_t dBH = desc_kmajor<BK>(st + 2 * A_TILE + adv);
+            const uint64_t dBL = desc_kmajor<BK>(st + 2 * A_TILE + B_HALF + adv);
             const uint32_t acc = (kb > 0 || kk > 0) ? 1u : 0u;
             mma_f16_pair(dmain, dAH, dBH, idesc, acc);
             mma_f16_pair(dcorr, dAH, dBL, idesc, acc);
@@ -1794,16 +1810,16 @@ __global__ void __launch_bounds__(PairCfg::THREADS, 1)
           }
           mma_commit_pair(&empty_bar[s]);
         }
-        if (ok) mma_commit_pair(&tfull);
+        if (ok) mma_commit_pair(&tfull[b]);
         ++i;
       }
     }
   } else {
-    // ---- epilogue (warps 0-7) of this CTA's 128 rows: TMEM -> registers,
-    // release the accumulator to the leader, then scale and store
+    // ---- epilogue (warps 0-7) of this CTA's 128 rows: warp w drains TMEM
+    // lanes 32 (w % 4).. for the column half w / 4 of the tile
     uint4* stg = reinterpret_cast<uint4*>(smem_raw + (base - smem_u32(smem_raw)) + S * STAGE +
                                           warp * 4096);
-    const uint32_t tempty_leader = map_to_rank(smem_u32(&tempty), 0);
+    const uint32_t tempty0 = map_to_rank(smem_u32(&tempty[0]), 0);
     const int quarter = warp & 3, half = warp >> 2;
     const bool c_vec = out.C && ((out.ldc & 3) == 0) &&
                        ((reinterpret_cast<uintptr_t>(out.C) & 15) == 0);
@@ -1811,42 +1827,69 @@ __global__ void __launch_bounds__(PairCfg::THREADS, 1)
     for (int64_t it = 0; it < my_tiles; ++it) {
       const int64_t t = pair_tile(it);
       if (t >= tiles) continue;
-      const bool ready = mbar_wait(&tfull, (uint32_t)i & 1u, &abort_sh, err);
+      const int b = i % NBUF;
+      const bool ready = mbar_wait(&tfull[b], ((uint32_t)(i / NBUF)) & 1u, &abort_sh, err);
       __syncwarp();
       if (!__all_sync(0xffffffffu, ready)) break;
       fence_after();
       const int64_t q = t / col_tiles, cb = t - q * col_tiles;
       const int64_t row0 = q * 256 + 128 * (int64_t)rank + quarter * 32;
-      float vv[4][32];
-#pragma unroll
-      for (int c4 = 0; c4 < 4; ++c4) {
-        const int col0 = (int)(cb * 256) + (4 * half + c4) * 32;
-#pragma unroll
-        for (int hh = 0; hh < 2; ++hh) {
-          uint32_t rm[16], rc[16];
-          const uint32_t ta = tmem + ((uint32_t)(quarter * 32) << 16) +
-                              (uint32_t)((4 * half + c4) * 32 + hh * 16);
-          tmem_ld16(ta, rm);
-          tmem_ld16(ta + 256u, rc);
-          tmem_wait_ld();
-#pragma unroll
-          for (int j = 0; j < 16; ++j)
-            vv[c4][hh * 16 + j] = (__uint_as_float(rm[j]) + __uint_as_float(rc[j])) *
-                                  __ldg(f + col0 + hh * 16 + j);
+      // release of accumulator buffer b to the leader: one arrival per warp
+      auto release = [&]() {
+        fence_before();
+        __syncwarp();
+        if (lane == 0) {
+          if (rank == 0)
+            mbar_arrive(&tempty[b]);
+          else
+            mbar_arrive_remote(tempty0 + 8u * (uint32_t)b);
         }
-      }
-      fence_before();
-      __syncwarp();
-      if (lane == 0) {
-        if (rank == 0)
-          mbar_arrive(&tempty);
-        else
-          mbar_arrive_remote(tempty_leader);
-      }
+      };
+      if constexpr (TN == 256) {
+        // one accumulator buffer: read the warp's 128 columns into registers,
+        // release TMEM, then store (the next tile's products overlap the stores)
+        float vv[4][32];
 #pragma unroll
-      for (int c4 = 0; c4 < 4; ++c4)
-        apply_store_chunk(vv[c4], (int)(cb * 256) + (4 * half + c4) * 32, stg, lane, out, k, m, mp,
-                          0, row0, c_vec);
+        for (int c4 = 0; c4 < 4; ++c4) {
+          const int col0 = (int)(cb * TN) + (4 * half + c4) * 32;
+#pragma unroll
+          for (int hh = 0; hh < 2; ++hh) {
+            uint32_t rm[16], rc[16];
+            const uint32_t ta = tmem + ((uint32_t)(quarter * 32) << 16) +
+                                (uint32_t)((4 * half + c4) * 32 + hh * 16);
+            tmem_ld16(ta, rm);
+            tmem_ld16(ta + (uint32_t)TN, rc);
+            tmem_wait_ld();
+#pragma unroll
+            for (int j = 0; j < 16; ++j)
+              vv[c4][hh * 16 + j] = (__uint_as_float(rm[j]) + __uint_as_float(rc[j])) *
+                                    __ldg(f + col0 + hh * 16 + j);
+          }
+        }
+        release();
+#pragma unroll
+        for (int c4 = 0; c4 < 4; ++c4)
+          apply_store_chunk(vv[c4], (int)(cb * TN) + (4 * half + c4) * 32, stg, lane, out, k, m,
+                            mp, 0, row0, c_vec);
+      } else {
+        // two buffers: drain and store 32 columns at a time, release at the end
+#pragma unroll 1
+        for (int cc = 2 * half; cc < 2 * half + 2; ++cc) {
+          uint32_t rm[32], rc[32];
+          const uint32_t ta = tmem + ((uint32_t)(quarter * 32) << 16) +
+                              (uint32_t)(b * 2 * TN + cc * 32);
+          tmem_ld32(ta, rm);
+          tmem_ld32(ta + (uint32_t)TN, rc);
+          tmem_wait_ld();
+          const int col0 = (int)(cb * TN) + cc * 32;
+          float v[32];
+#pragma unroll
+          for (int j = 0; j < 32; ++j)
+            v[j] = (__uint_as_float(rm[j]) + __uint_as_float(rc[j])) * __ldg(f + col0 + j);
+          apply_store_chunk(v, col0, stg, lane, out, k, m, mp, 0, row0, c_vec);
+        }
+        release();
+      }
       ++i;
     }
   }
@@ -2075,26 +2118,35 @@ static bool make_map_planes(CUtensorMap* map, const __half* base, uint64_t inner
 
 int64_t packed_ld(int64_t N) { return cdiv(N, 64) * 64; }
 
-// two-CTA clusters of apply16p_kernel resident at once (0: not available)
+static void pair_launch_config(cudaLaunchConfig_t& cfg, cudaLaunchAttribute* at, unsigned grid,
+                               unsigned threads, size_t smem, cudaStream_t st) {
+  cfg = {};
+  cfg.gridDim = dim3(grid);
+  cfg.blockDim = dim3(threads);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = st;
+  at[0].id = cudaLaunchAttributeClusterDimension;
+  at[0].val.clusterDim.x = 2;
+  at[0].val.clusterDim.y = 1;
+  at[0].val.clusterDim.z = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+}
+
+// two-CTA clusters of apply16p_kernel<TN> resident at once (0: not available)
+template <int TN>
 static int pair_clusters() {
   static int n = -1;
   if (n < 0) {
     n = 0;
-    if (cudaFuncSetAttribute(hp::apply16p_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)hp::pair_smem()) == cudaSuccess) {
-      cudaLaunchConfig_t cfg = {};
-      cfg.gridDim = dim3(2 * (unsigned)num_sms());
-      cfg.blockDim = dim3(hp::PairCfg::THREADS);
-      cfg.dynamicSmemBytes = hp::pair_smem();
+    if (cudaFuncSetAttribute(hp::apply16p_kernel<TN>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)hp::pair_smem<TN>()) == cudaSuccess) {
+      cudaLaunchConfig_t cfg;
       cudaLaunchAttribute at[1];
-      at[0].id = cudaLaunchAttributeClusterDimension;
-      at[0].val.clusterDim.x = 2;
-      at[0].val.clusterDim.y = 1;
-      at[0].val.clusterDim.z = 1;
-      cfg.attrs = at;
-      cfg.numAttrs = 1;
+      pair_launch_config(cfg, at, 2 * (unsigned)num_sms(), hp::PairCfg<TN>::THREADS,
+                         hp::pair_smem<TN>(), 0);
       int c = 0;
-      if (cudaOccupancyMaxActiveClusters(&c, hp::apply16p_kernel, &cfg) == cudaSuccess) n = c;
+      if (cudaOccupancyMaxActiveClusters(&c, hp::apply16p_kernel<TN>, &cfg) == cudaSuccess) n = c;
     }
     cudaGetLastError();
   }
@@ -2446,11 +2498,14 @@ int apply_packed(const Packed& p, const double* W, int64_t ldw, int64_t k, float
   // 128-wide products on the diagonal band)
   const bool tri_w = upper && k == p.N;
   // SM pairs (apply16p_kernel) for one problem wider than 128 columns, when
-  // enabled for its kind of W and the device runs two-CTA clusters of it
-  const bool pair = batch == 1 && k > 128 &&
-                    (tuning().apply_pair == 2 || (tuning().apply_pair == 1 && !tri_w)) &&
-                    pair_clusters() > 0;
-  const int TN = pair ? 256 : (k > 128 && !tri_w) ? tuning().apply_dense_tn : 128;
+  // enabled for its kind of W and the device runs two-CTA clusters of it:
+  // 256 x 256 tiles for a dense W, 256 x 128 tiles for a triangular one
+  const int pair_tn = (batch != 1 || k <= 128) ? 0
+                      : (!tri_w && tuning().apply_pair >= 1 && pair_clusters<256>() > 0) ? 256
+                      : (tri_w && tuning().apply_pair == 2 && pair_clusters<128>() > 0) ? 128
+                                                                                      : 0;
+  const bool pair = pair_tn != 0;
+  const int TN = pair ? pair_tn : (k > 128 && !tri_w) ? tuning().apply_dense_tn : 128;
   const int64_t col_tiles = cdiv(k, TN);
   const int fstride = (int)(col_tiles * TN);
   __half* bhi = ws.take<__half>((size_t)(2 * batch * k * ldk));
@@ -2488,11 +2543,15 @@ int apply_packed(const Packed& p, const double* W, int64_t ldw, int64_t k, float
   }
   CUtensorMap tmA, tmB;
   const uint32_t bk = TN == 256 ? (uint32_t)hp::ApplyCfg<256>::BK : (uint32_t)hp::ApplyCfg<128>::BK;
-  static_assert(hp::ApplyCfg<256>::BK == hp::PairCfg::BK, "pair tiles share the 256-wide maps");
+  static_assert(hp::ApplyCfg<256>::BK == hp::PairCfg<256>::BK &&
+                    hp::ApplyCfg<128>::BK == hp::PairCfg<128>::BK,
+                "pair tiles use the single-SM kernels' K depth");
+  // B boxes: TN rows of W (single SM, in boxes of 128) or the CTA's half (pair)
+  const uint32_t b_rows = pair ? (uint32_t)(TN / 2) : 128u;
   PLOM_REQUIRE(make_map_planes(&tmA, p.hi, (uint64_t)p.ld, (uint64_t)(batch * p.mp),
                                (uint64_t)p.ld, bk, 128, (uint64_t)p.pstride, bk == 32) &&
                    make_map_planes(&tmB, bhi, (uint64_t)ldk, (uint64_t)(batch * k), (uint64_t)ldk,
-                                   bk, 128, 0, bk == 32),
+                                   bk, b_rows, 0, bk == 32),
                PLOM_ERR_CUDA, "apply16: tensor map encoding failed");
   const int64_t row_tiles = cdiv(p.mp, 128);
   const int64_t tiles = batch * row_tiles * col_tiles;
@@ -2517,24 +2576,27 @@ int apply_packed(const Packed& p, const double* W, int64_t ldw, int64_t k, float
   ProfScope prof(pair ? "tc_apply_f16x3_pair" : "tc_apply_f16x3", st, flops,
                  4.0 * ((double)m * p.ld + (double)m * k) * batch);
   if (pair) {
+    const int clusters_max = TN == 256 ? pair_clusters<256>() : pair_clusters<128>();
     const int64_t pairs = cdiv(p.mp, 256), ptiles = pairs * col_tiles;
-    const int pby_rows = (tri && pairs >= 2 * (int64_t)pair_clusters()) ? 1 : 0;
-    const int64_t clusters = std::min<int64_t>(pby_rows ? pairs : ptiles, pair_clusters());
-    cudaLaunchConfig_t cfg = {};
-    cfg.gridDim = dim3((unsigned)(2 * clusters));
-    cfg.blockDim = dim3(hp::PairCfg::THREADS);
-    cfg.dynamicSmemBytes = hp::pair_smem();
-    cfg.stream = st;
+    const int pby_rows = (tri && pairs >= 2 * (int64_t)clusters_max) ? 1 : 0;
+    const int64_t clusters = std::min<int64_t>(pby_rows ? pairs : ptiles, clusters_max);
+    cudaLaunchConfig_t cfg;
     cudaLaunchAttribute at[1];
-    at[0].id = cudaLaunchAttributeClusterDimension;
-    at[0].val.clusterDim.x = 2;
-    at[0].val.clusterDim.y = 1;
-    at[0].val.clusterDim.z = 1;
-    cfg.attrs = at;
-    cfg.numAttrs = 1;
-    PLOM_CHECK_CUDA(cudaLaunchKernelEx(&cfg, hp::apply16p_kernel, tmA, tmB, m,
-                                       (int)(ldk / hp::PairCfg::BK), (int)k, col_tiles, ptiles,
-                                       (const float*)f, o, err, p.mp, tri ? 1 : 0, pby_rows));
+    if (TN == 256) {
+      pair_launch_config(cfg, at, (unsigned)(2 * clusters), hp::PairCfg<256>::THREADS,
+                         hp::pair_smem<256>(), st);
+      PLOM_CHECK_CUDA(cudaLaunchKernelEx(&cfg, hp::apply16p_kernel<256>, tmA, tmB, m,
+                                         (int)(ldk / hp::PairCfg<256>::BK), (int)k, col_tiles,
+                                         ptiles, (const float*)f, o, err, p.mp, tri ? 1 : 0,
+                                         pby_rows));
+    } else {
+      pair_launch_config(cfg, at, (unsigned)(2 * clusters), hp::PairCfg<128>::THREADS,
+                         hp::pair_smem<128>(), st);
+      PLOM_CHECK_CUDA(cudaLaunchKernelEx(&cfg, hp::apply16p_kernel<128>, tmA, tmB, m,
+                                         (int)(ldk / hp::PairCfg<128>::BK), (int)k, col_tiles,
+                                         ptiles, (const float*)f, o, err, p.mp, tri ? 1 : 0,
+                                         pby_rows));
+    }
     PLOM_CHECK_LAUNCH();
     return PLOM_OK;
   }
