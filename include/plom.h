@@ -68,7 +68,8 @@ int plom_version(void);
    per SM of its slab reduction ("reduce_blocks_per_sm", 1-16), the output
    tile width of dense products wider than 128 columns ("apply_dense_tn",
    128 or 256), whether such products give each CTA whole row blocks
-   ("apply_dense_by_rows", 0 or 1) and the row chunks of a large FP32 input
+   ("apply_dense_by_rows", 0 or 1; "apply_tri_by_rows" for triangular W)
+   and the row chunks of a large FP32 input
    packed on a second stream beside the first Gram ("pass1_chunks", 1, 2, 4
    or 8; 1 packs it whole first) and which products of one tall matrix wider
    than 128 columns run on SM pairs with 256 x 256 tiles (2-SM UMMA,

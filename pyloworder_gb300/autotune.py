@@ -32,6 +32,7 @@ CANDIDATES = {
     "reduce_blocks_per_sm": [2, 3, 4],
     "apply_dense_tn": [128, 256],
     "apply_dense_by_rows": [0, 1],
+    "apply_tri_by_rows": [0, 1],
     "pass1_chunks": [1, 4, 8],
     "apply_pair": [0, 1, 2],
 }

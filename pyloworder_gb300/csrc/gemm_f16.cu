@@ -2559,8 +2559,10 @@ int apply_packed(const Packed& p, const double* W, int64_t ldw, int64_t k, float
   // different lengths); the dense case keeps concurrent tiles of one row
   // block on different SMs (fewer DRAM re-reads)
   const bool tri_pre = upper && k == p.N;
-  const int by_rows =
-      ((tri_pre || tuning().apply_dense_by_rows) && batch * row_tiles >= 2 * num_sms()) ? 1 : 0;
+  const int by_rows = ((tri_pre ? tuning().apply_tri_by_rows : tuning().apply_dense_by_rows) &&
+                       batch * row_tiles >= 2 * num_sms())
+                          ? 1
+                          : 0;
   const int grid = (int)std::min<int64_t>(by_rows ? batch * row_tiles : tiles, num_sms());
   hp::ApplyOut o;
   o.C = out ? nullptr : C;
@@ -2578,7 +2580,11 @@ int apply_packed(const Packed& p, const double* W, int64_t ldw, int64_t k, float
   if (pair) {
     const int clusters_max = TN == 256 ? pair_clusters<256>() : pair_clusters<128>();
     const int64_t pairs = cdiv(p.mp, 256), ptiles = pairs * col_tiles;
-    const int pby_rows = (tri && pairs >= 2 * (int64_t)clusters_max) ? 1 : 0;
+    const int pby_rows =
+        ((tri ? tuning().apply_tri_by_rows : tuning().apply_dense_by_rows) &&
+         pairs >= 2 * (int64_t)clusters_max)
+            ? 1
+            : 0;
     const int64_t clusters = std::min<int64_t>(pby_rows ? pairs : ptiles, clusters_max);
     cudaLaunchConfig_t cfg;
     cudaLaunchAttribute at[1];

@@ -76,6 +76,7 @@ struct Tuning {
   int reduce_blocks_per_sm = 3;  // resident blocks of the Gram slab reduction
   int apply_dense_tn = 256;      // output tile width of dense products wider than 128 (128 or 256)
   int apply_dense_by_rows = 0;   // dense products: whole row blocks per CTA (1) or single tiles (0)
+  int apply_tri_by_rows = 1;     // the same for triangular W
   int pass1_chunks = 8;          // large FP32 inputs: row chunks packed beside the first Gram (1: off)
   int apply_pair = 1;            // products on SM pairs (2-SM UMMA): 0 off, 1 dense, 2 dense + triangular
 };
