@@ -463,7 +463,8 @@ def run_ours(args):
                 "info": {"cholesky_shift_escalations": info_words[1] if info_words else None,
                          "jacobi_sweeps": info_words[2] if info_words else None,
                          "jacobi_fp32_sweeps": info_words[4] if info_words else None,
-                         "jacobi_refine_steps": info_words[5] if info_words else None}}
+                         "jacobi_refine_steps": info_words[5] if info_words else None,
+                         "cholesky_closed_form": info_words[6] if info_words else None}}
         print(json.dumps(line), flush=True)
     if world > 1:
         import torch.distributed as dist

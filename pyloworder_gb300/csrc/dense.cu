@@ -38,13 +38,22 @@ struct CholState {
   int* status;    // [batch]: 0 pending, 1 done, 2 failed in this round
   int* shifts_used;
   int* pending;   // [CHOL_ROUNDS] counters
+  double* colsq;  // [CHOL_NEAR_GROUPS x n]: partial column sums of the near-identity test
 };
+
+// Unshifted factorisation of one Gram close to the identity, G = I + E (the
+// later CholeskyQR passes): R = I + X with X = triu(E, 1) + diag(E) / 2 gives
+// R^T R = G + X^T X exactly, and |(X^T X)_ij| <= max_j ||X e_j||^2.  When the
+// caller allows a perturbation of G (near_tol > 0: the mixed form, whose
+// operands carry 22 bits) and that bound is at most near_tol, R is written
+// directly and the blocked factorisation is skipped.
+constexpr int CHOL_NEAR_GROUPS = 8;   // row groups of the column sums
 
 __global__ void __launch_bounds__(256) chol_coop_kernel(const double* __restrict__ G,
                                                         double* __restrict__ R,
                                                         double* __restrict__ Dinv, int n,
                                                         int batch, double rel0, double relfail,
-                                                        CholState stt, int* info) {
+                                                        double near_tol, CholState stt, int* info) {
   cg::grid_group grid = cg::this_grid();
   __shared__ double S[NB][NB + 1];
   __shared__ double P[NB][NB + 1];
@@ -72,6 +81,43 @@ __global__ void __launch_bounds__(256) chol_coop_kernel(const double* __restrict
     __syncthreads();
   }
   if (blockIdx.x == 0 && tid < CHOL_ROUNDS) stt.pending[tid] = 0;
+  if (batch == 1 && rel0 == 0.0 && stt.colsq) {
+    // near-identity test: partial sums of X's squared columns over
+    // CHOL_NEAR_GROUPS row groups (thread per column, coalesced rows), summed
+    // per column in group order and compared with the bound (every block
+    // reaches the same answer from the same partials)
+    const int rows_g = (n + CHOL_NEAR_GROUPS - 1) / CHOL_NEAR_GROUPS;
+    const int cblocks = (n + blockDim.x - 1) / blockDim.x;
+    for (int task = blockIdx.x; task < cblocks * CHOL_NEAR_GROUPS; task += gridDim.x) {
+      const int g = task / cblocks, j = (task % cblocks) * blockDim.x + tid;
+      if (j >= n) continue;
+      double acc = 0.0;
+      const int i1 = min(min(n, (g + 1) * rows_g), j + 1);
+      for (int i = g * rows_g; i < i1; ++i) {
+        const double e = G[(int64_t)i * n + j];
+        const double x = (i == j) ? 0.5 * (e - 1.0) : e;
+        acc = fma(x, x, acc);
+      }
+      stt.colsq[(int64_t)g * n + j] = acc;
+    }
+    grid.sync();
+    int ok = 1;
+    for (int j = tid; j < n; j += blockDim.x) {
+      double c = 0.0;
+      for (int g = 0; g < CHOL_NEAR_GROUPS; ++g) c += stt.colsq[(int64_t)g * n + j];
+      if (!(c <= near_tol)) ok = 0;  // (a NaN fails the test)
+    }
+    const bool near = __syncthreads_and(ok) && stt.status[0] == 0;
+    if (near) {
+      for (int64_t e = (int64_t)blockIdx.x * blockDim.x + tid; e < nn;
+           e += (int64_t)gridDim.x * blockDim.x) {
+        const int i = (int)(e / n), j = (int)(e % n);
+        R[e] = (i < j) ? G[e] : (i == j ? 1.0 + 0.5 * (G[e] - 1.0) : 0.0);
+      }
+      if (blockIdx.x == 0 && tid == 0) atomicAdd(&info[ST_NEAR], 1);
+      return;  // every block takes the same branch: no grid barrier follows
+    }
+  }
   grid.sync();
 
   for (int round = 0; round < CHOL_ROUNDS; ++round) {
@@ -270,13 +316,16 @@ static int coop_blocks(const void* kern, int threads, size_t smem, int want) {
 }
 
 int chol_shifted(const double* G, double* R, int n, int batch, double rel0, double relfail,
-                 int* info, Arena& ws, cudaStream_t st) {
+                 int* info, Arena& ws, cudaStream_t st, double near_tol) {
   CholState s;
   s.trace = ws.take<double>(batch);
   s.shift = ws.take<double>(batch);
   s.status = ws.take<int>(batch);
   s.shifts_used = ws.take<int>(1);
   s.pending = ws.take<int>(CHOL_ROUNDS);
+  s.colsq = (batch == 1 && rel0 == 0.0 && near_tol > 0.0)
+                ? ws.take<double>((size_t)CHOL_NEAR_GROUPS * n)
+                : nullptr;
   double* Dinv = ws.take<double>((size_t)batch * NB * NB);
   if (ws.measuring() || n == 0 || batch == 0) return PLOM_OK;
   PLOM_REQUIRE(!ws.overflow(), PLOM_ERR_WORKSPACE, "chol: workspace too small");
@@ -286,8 +335,9 @@ int chol_shifted(const double* G, double* R, int n, int batch, double rel0, doub
   int want = std::max(batch * std::max(1, T * (T + 1) / 2), 1);
   int blocks = coop_blocks((const void*)chol_coop_kernel, 256, 0, want);
   ProfScope prof("chol_fp64", st, (double)n * n * n / 3.0 * batch, 16.0 * n * n * batch);
-  void* args[] = {(void*)&G, (void*)&R, (void*)&Dinv, (void*)&n, (void*)&batch,
-                  (void*)&rel0, (void*)&relfail, (void*)&s, (void*)&info};
+  void* args[] = {(void*)&G,       (void*)&R,       (void*)&Dinv,     (void*)&n,
+                  (void*)&batch,   (void*)&rel0,    (void*)&relfail,  (void*)&near_tol,
+                  (void*)&s,       (void*)&info};
   PLOM_CHECK_CUDA(cudaLaunchCooperativeKernel((const void*)chol_coop_kernel, dim3(blocks),
                                               dim3(256), args, 0, st));
   return PLOM_OK;

@@ -150,8 +150,9 @@ struct ProfScope {
 // status words written by kernels (device side) and read back by the host.
 // Index 0: numerical failure code (0 = ok), 1: count of Cholesky shift
 // escalations, 2: Jacobi sweeps of the last small SVD, 3: non-finite input seen,
-// 4: FP32 Jacobi sweeps, 5: refinement steps after them.
+// 4: FP32 Jacobi sweeps, 5: refinement steps after them, 6: Cholesky
+// factorisations of a Gram next to the identity written in closed form.
 enum { ST_FAIL = 0, ST_SHIFTS = 1, ST_SWEEPS = 2, ST_NONFINITE = 3, ST_SWEEPS32 = 4, ST_REFINE = 5,
-       ST_WORDS = 8 };
+       ST_NEAR = 6, ST_WORDS = 8 };
 
 }  // namespace plom

@@ -61,9 +61,14 @@ int gemm_tn_df(const float* A, int64_t lda, const float* B, int64_t ldb, double*
 // factorization restarts with s = max(s*100, shift_rel_fail*trace/n).  With
 // shift_rel0 = 0 a non-positive pivot is instead floored alone at
 // shift_rel_fail*trace/n (a null direction of a positive semidefinite G).
-// info[ST_FAIL] = PLOM_NUM_CHOLESKY when all attempts fail.
+// info[ST_FAIL] = PLOM_NUM_CHOLESKY when all attempts fail.  near_tol > 0
+// (one unshifted problem): a G within that bound of the identity (the largest
+// squared column of triu(G - I, 1) + diag(G - I) / 2) is factored in closed
+// form, R = I + that matrix, which is the exact factor of G perturbed by at
+// most near_tol per element; info[ST_NEAR] counts such factorisations.
 int chol_shifted(const double* G, double* R, int n, int batch, double shift_rel0,
-                 double shift_rel_fail, int* info, Arena& ws, cudaStream_t st);
+                 double shift_rel_fail, int* info, Arena& ws, cudaStream_t st,
+                 double near_tol = 0.0);
 // W = R^{-1} for upper-triangular R (batch, stride n*n).
 int trtri_upper(const double* R, double* W, int n, int batch, Arena& ws, cudaStream_t st);
 // One-sided Jacobi SVD of `batch` square n x n matrices A (ld n, stride n*n),

@@ -241,7 +241,9 @@ static int chol_pass_packed(bool cplx, int n, const Packed& P, PackedCore& b, do
   need = std::max(need, ws.off);
   ws.off = mark;
   if (cplx && !ws.measuring()) PLOM_TRY(complexify_gram(b.H, b.G, n, 1, st));
-  PLOM_TRY(chol_shifted(b.G, R, N, 1, rel0, relfail, info, ws, st));
+  // the Gram of a factor next to orthonormal is factored in closed form when
+  // the implied perturbation of G is below 1e-10 (the operands carry 22 bits)
+  PLOM_TRY(chol_shifted(b.G, R, N, 1, rel0, relfail, info, ws, st, rel0 == 0.0 ? 1e-10 : 0.0));
   need = std::max(need, ws.off);
   ws.off = mark;
   PLOM_TRY(trtri_upper(R, W, N, 1, ws, st));

@@ -538,3 +538,26 @@ def test_tsqr_svd_batched(cplx, precision):
         assert orthogonality(U[p].astype(A64.dtype)) < tol * 10
         rec = (U[p].astype(A64.dtype) * S[p]) @ V[p].astype(A64.dtype)
         assert np.linalg.norm(rec - A64) / np.linalg.norm(A64) < tol * 10
+
+
+def test_mixed_cholesky_of_near_identity_gram_in_closed_form():
+    """The Gram of the last CholeskyQR factor sits next to the identity; its
+    factor is written in closed form (R = I + triu(E, 1) + diag(E) / 2, exact
+    for G perturbed by at most 1e-10 per element; info word 6 counts it) and
+    the SVD keeps the mixed form's accuracy against the FP64 form."""
+    from pyloworder_gb300 import _lib as L
+    m, n = 65536, 384
+    g = torch.Generator(device="cuda").manual_seed(4242)
+    X = torch.randn(m, n, device="cuda", generator=g, dtype=torch.float32)
+    X *= torch.logspace(0, -3, n, device="cuda")  # graded columns
+    U, S, V = P.vmmath.tsqr_svd_device(X, n, "mixed")
+    info = list(L.last_info)
+    assert info[6] >= 1, info
+    Ur, Sr, Vr = P.vmmath.tsqr_svd_device(X.double(), n, "fp64")
+    s, sr = S.double().cpu().numpy(), Sr.cpu().numpy()
+    assert sigma_normwise(s, sr) < 1e-6
+    assert sigma_rel(s, sr, 64) < 1e-5
+    Ud = U.double()
+    assert float((Ud.T @ Ud - torch.eye(n, dtype=torch.float64, device="cuda")).abs().max()) < 1e-5
+    R = (Ud * S.double()) @ V.double() - X.double()
+    assert float(R.abs().max()) / float(X.abs().max()) < 1e-5
