@@ -1210,15 +1210,17 @@ __global__ void tn16w_reduce_kernel(const float* __restrict__ part, int Na, int 
 // products; two 96 KiB stages.  TN = 128 (narrow k): three 64 KiB stages and
 // two accumulator buffers.
 // ---------------------------------------------------------------------------
-template <int TN>
+// K per stage (BKV): 64 (128-byte rows, 128-byte swizzle) or 32 (64-byte rows,
+// 64-byte swizzle); 192 KiB of stages either way, so 32-deep stages give the
+// ring twice as many, shorter stages (TN = 256 always takes 32: four stages)
+template <int TN, int BKV = (TN == 256 ? 32 : 64)>
 struct ApplyCfg {
-  // K per stage: 64 (128-byte rows, 128-byte swizzle) for TN = 128; 32 (64-byte
-  // rows, 64-byte swizzle) for TN = 256, so that four stages fit
-  static constexpr int BK = TN == 256 ? 32 : 64;
+  static_assert(BKV == 32 || BKV == 64, "stage depth");
+  static constexpr int BK = BKV;
   static constexpr uint32_t A_TILE = 128u * BK * 2;           // 128 rows x BK fp16
   static constexpr uint32_t B_TILE = (uint32_t)TN * BK * 2;   // TN rows x BK fp16
   static constexpr uint32_t STAGE = 2 * A_TILE + 2 * B_TILE;  // A hi, A lo, B hi, B lo
-  static constexpr int STAGES = TN == 256 ? 4 : 3;
+  static constexpr int STAGES = (int)(196608u / STAGE);
   static constexpr int NBUF = TN == 256 ? 1 : 2;   // TMEM accumulator buffers
 };
 // Warps: 0-7 epilogue (warp w drains TMEM lanes 32 (w % 4).. for the column
@@ -1243,9 +1245,9 @@ struct ApplyWarps {
 };
 constexpr int A_EPI_WARPS = 8;                 // TN = 128
 constexpr int A_THREADS = 32 * (A_EPI_WARPS + 2);
-template <int TN>
+template <int TN, int BKV = ApplyCfg<TN>::BK>
 constexpr size_t apply_smem() {
-  return (size_t)ApplyCfg<TN>::STAGES * ApplyCfg<TN>::STAGE + ApplyWarps<TN>::STG + 1024;
+  return (size_t)ApplyCfg<TN, BKV>::STAGES * ApplyCfg<TN, BKV>::STAGE + ApplyWarps<TN>::STG + 1024;
 }
 
 struct ApplyOut {
@@ -1316,7 +1318,7 @@ __device__ __forceinline__ void apply_store_chunk(const float (&v)[32], int col0
   }
 }
 
-template <int TN>
+template <int TN, int BKV = ApplyCfg<TN>::BK>
 __global__ void __launch_bounds__(ApplyWarps<TN>::THREADS, 1)
     apply16_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
                    int64_t m, int kblocks, int k, int64_t col_tiles, int64_t tiles,
@@ -1331,9 +1333,10 @@ __global__ void __launch_bounds__(ApplyWarps<TN>::THREADS, 1)
   // each other on one SM (L2 hits) and every CTA gets the same work per row
   // block.  Otherwise it takes single tiles, tile r G + x in even rounds r and
   // r G + (G - 1 - x) in odd ones.
-  constexpr int A_STAGES = ApplyCfg<TN>::STAGES, NBUF = ApplyCfg<TN>::NBUF, A_BK = ApplyCfg<TN>::BK;
-  constexpr uint32_t A_STAGE = ApplyCfg<TN>::STAGE, B_TILE = ApplyCfg<TN>::B_TILE;
-  constexpr uint32_t A_TILE = ApplyCfg<TN>::A_TILE;
+  using Cfg = ApplyCfg<TN, BKV>;
+  constexpr int A_STAGES = Cfg::STAGES, NBUF = Cfg::NBUF, A_BK = Cfg::BK;
+  constexpr uint32_t A_STAGE = Cfg::STAGE, B_TILE = Cfg::B_TILE;
+  constexpr uint32_t A_TILE = Cfg::A_TILE;
   constexpr int A_EPI_WARPS = ApplyWarps<TN>::EPI;
   extern __shared__ uint8_t smem_raw[];
   __shared__ uint64_t full_bar[A_STAGES], empty_bar[A_STAGES], tfull[NBUF], tempty[NBUF];
@@ -2526,6 +2529,9 @@ int apply_packed(const Packed& p, const double* W, int64_t ldw, int64_t k, float
     PLOM_CHECK_CUDA(cudaFuncSetAttribute(hp::apply16_kernel<128>,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)hp::apply_smem<128>()));
+    PLOM_CHECK_CUDA(cudaFuncSetAttribute(hp::apply16_kernel<128, 32>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)hp::apply_smem<128, 32>()));
     PLOM_CHECK_CUDA(cudaFuncSetAttribute(hp::apply16_kernel<256>,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)hp::apply_smem<256>()));
@@ -2542,7 +2548,9 @@ int apply_packed(const Packed& p, const double* W, int64_t ldw, int64_t k, float
     PLOM_CHECK_LAUNCH();
   }
   CUtensorMap tmA, tmB;
-  const uint32_t bk = TN == 256 ? (uint32_t)hp::ApplyCfg<256>::BK : (uint32_t)hp::ApplyCfg<128>::BK;
+  // single-SM 128-wide tiles: 64- or 32-deep stages (apply_narrow_bk)
+  const int nbk = (!pair && TN == 128 && tuning().apply_narrow_bk == 32) ? 32 : 64;
+  const uint32_t bk = TN == 256 ? (uint32_t)hp::ApplyCfg<256>::BK : (uint32_t)nbk;
   static_assert(hp::ApplyCfg<256>::BK == hp::PairCfg<256>::BK &&
                     hp::ApplyCfg<128>::BK == hp::PairCfg<128>::BK,
                 "pair tiles use the single-SM kernels' K depth");
@@ -2610,6 +2618,10 @@ int apply_packed(const Packed& p, const double* W, int64_t ldw, int64_t k, float
     hp::apply16_kernel<256><<<grid, hp::ApplyWarps<256>::THREADS, hp::apply_smem<256>(), st>>>(
         tmA, tmB, m, (int)(ldk / hp::ApplyCfg<256>::BK), (int)k, col_tiles, tiles, f, o, err, p.mp,
         row_tiles, fstride, tri ? 1 : 0, by_rows);
+  else if (nbk == 32)
+    hp::apply16_kernel<128, 32><<<grid, hp::ApplyWarps<128>::THREADS, hp::apply_smem<128, 32>(),
+                                  st>>>(tmA, tmB, m, (int)(ldk / 32), (int)k, col_tiles, tiles, f,
+                                        o, err, p.mp, row_tiles, fstride, tri ? 1 : 0, by_rows);
   else
     hp::apply16_kernel<128><<<grid, hp::ApplyWarps<128>::THREADS, hp::apply_smem<128>(), st>>>(
         tmA, tmB, m, (int)(ldk / 64), (int)k, col_tiles, tiles, f, o, err, p.mp, row_tiles,
