@@ -33,7 +33,6 @@ CANDIDATES = {
     "apply_dense_tn": [128, 256],
     "apply_dense_by_rows": [0, 1],
     "apply_tri_by_rows": [0, 1],
-    "apply_narrow_bk": [64, 32],
     "pass1_chunks": [1, 4, 8],
     "apply_pair": [0, 1, 2],
 }

@@ -110,8 +110,6 @@ extern "C" int plom_set_tuning(const char* key, double value) {
     t.apply_dense_by_rows = v;
   } else if (k == "apply_tri_by_rows" && (v == 0 || v == 1)) {
     t.apply_tri_by_rows = v;
-  } else if (k == "apply_narrow_bk" && (v == 32 || v == 64)) {
-    t.apply_narrow_bk = v;
   } else if (k == "pass1_chunks" && (v == 1 || v == 2 || v == 4 || v == 8)) {
     t.pass1_chunks = v;
   } else if (k == "apply_pair" && v >= 0 && v <= 2) {
@@ -134,7 +132,6 @@ extern "C" double plom_get_tuning(const char* key) {
   if (k == "apply_dense_tn") return t.apply_dense_tn;
   if (k == "apply_dense_by_rows") return t.apply_dense_by_rows;
   if (k == "apply_tri_by_rows") return t.apply_tri_by_rows;
-  if (k == "apply_narrow_bk") return t.apply_narrow_bk;
   if (k == "pass1_chunks") return t.pass1_chunks;
   if (k == "apply_pair") return t.apply_pair;
   return -1.0;

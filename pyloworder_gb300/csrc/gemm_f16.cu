@@ -1210,9 +1210,10 @@ __global__ void tn16w_reduce_kernel(const float* __restrict__ part, int Na, int 
 // products; two 96 KiB stages.  TN = 128 (narrow k): three 64 KiB stages and
 // two accumulator buffers.
 // ---------------------------------------------------------------------------
-// K per stage (BKV): 64 (128-byte rows, 128-byte swizzle) or 32 (64-byte rows,
-// 64-byte swizzle); 192 KiB of stages either way, so 32-deep stages give the
-// ring twice as many, shorter stages (TN = 256 always takes 32: four stages)
+// K per stage: 64 (128-byte rows, 128-byte swizzle) for TN = 128; 32 (64-byte
+// rows, 64-byte swizzle) for TN = 256, so that four stages fit in 192 KiB
+// (32-deep stages for TN = 128, six of 32 KiB, measured 15 % slower on the
+// triangular products than three of 64 KiB)
 template <int TN, int BKV = (TN == 256 ? 32 : 64)>
 struct ApplyCfg {
   static_assert(BKV == 32 || BKV == 64, "stage depth");
@@ -2529,9 +2530,6 @@ int apply_packed(const Packed& p, const double* W, int64_t ldw, int64_t k, float
     PLOM_CHECK_CUDA(cudaFuncSetAttribute(hp::apply16_kernel<128>,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)hp::apply_smem<128>()));
-    PLOM_CHECK_CUDA(cudaFuncSetAttribute(hp::apply16_kernel<128, 32>,
-                                         cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)hp::apply_smem<128, 32>()));
     PLOM_CHECK_CUDA(cudaFuncSetAttribute(hp::apply16_kernel<256>,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)hp::apply_smem<256>()));
@@ -2548,9 +2546,7 @@ int apply_packed(const Packed& p, const double* W, int64_t ldw, int64_t k, float
     PLOM_CHECK_LAUNCH();
   }
   CUtensorMap tmA, tmB;
-  // single-SM 128-wide tiles: 64- or 32-deep stages (apply_narrow_bk)
-  const int nbk = (!pair && TN == 128 && tuning().apply_narrow_bk == 32) ? 32 : 64;
-  const uint32_t bk = TN == 256 ? (uint32_t)hp::ApplyCfg<256>::BK : (uint32_t)nbk;
+  const uint32_t bk = TN == 256 ? (uint32_t)hp::ApplyCfg<256>::BK : (uint32_t)hp::ApplyCfg<128>::BK;
   static_assert(hp::ApplyCfg<256>::BK == hp::PairCfg<256>::BK &&
                     hp::ApplyCfg<128>::BK == hp::PairCfg<128>::BK,
                 "pair tiles use the single-SM kernels' K depth");
@@ -2618,10 +2614,6 @@ int apply_packed(const Packed& p, const double* W, int64_t ldw, int64_t k, float
     hp::apply16_kernel<256><<<grid, hp::ApplyWarps<256>::THREADS, hp::apply_smem<256>(), st>>>(
         tmA, tmB, m, (int)(ldk / hp::ApplyCfg<256>::BK), (int)k, col_tiles, tiles, f, o, err, p.mp,
         row_tiles, fstride, tri ? 1 : 0, by_rows);
-  else if (nbk == 32)
-    hp::apply16_kernel<128, 32><<<grid, hp::ApplyWarps<128>::THREADS, hp::apply_smem<128, 32>(),
-                                  st>>>(tmA, tmB, m, (int)(ldk / 32), (int)k, col_tiles, tiles, f,
-                                        o, err, p.mp, row_tiles, fstride, tri ? 1 : 0, by_rows);
   else
     hp::apply16_kernel<128><<<grid, hp::ApplyWarps<128>::THREADS, hp::apply_smem<128>(), st>>>(
         tmA, tmB, m, (int)(ldk / 64), (int)k, col_tiles, tiles, f, o, err, p.mp, row_tiles,

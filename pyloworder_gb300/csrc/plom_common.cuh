@@ -77,7 +77,6 @@ struct Tuning {
   int apply_dense_tn = 256;      // output tile width of dense products wider than 128 (128 or 256)
   int apply_dense_by_rows = 0;   // dense products: whole row blocks per CTA (1) or single tiles (0)
   int apply_tri_by_rows = 1;     // the same for triangular W
-  int apply_narrow_bk = 64;      // K depth of the 128-wide single-SM product's stages (64 or 32)
   int pass1_chunks = 8;          // large FP32 inputs: row chunks packed beside the first Gram (1: off)
   int apply_pair = 1;            // products on SM pairs (2-SM UMMA): 0 off, 1 dense, 2 dense + triangular
 };

@@ -102,7 +102,7 @@ def test_workspace_dry_runs_launch_nothing(dtype, prec):
 def test_tuning_parameters_round_trip_and_range():
     lib = L.load()
     keys = [b"gram_wave_mult", b"gram_wide_wave_mult", b"reduce_blocks_per_sm", b"apply_dense_tn", b"apply_dense_by_rows",
-            b"pass1_chunks", b"apply_pair", b"apply_tri_by_rows", b"apply_narrow_bk"]
+            b"pass1_chunks", b"apply_pair", b"apply_tri_by_rows"]
     old = {k: lib.plom_get_tuning(k) for k in keys}
     try:
         assert all(v >= 0 for v in old.values())

@@ -98,21 +98,3 @@ def test_tsqr_svd_pair_products_match_single_sm():
     Ud = U2.double()
     assert float((Ud.T @ Ud - torch.eye(n, dtype=torch.float64, device="cuda")).abs().max()) < 1e-4
 
-
-def test_narrow_stage_depth_variants_match():
-    """The 128-wide single-SM product with 32-deep stages (apply_narrow_bk = 32:
-    six stages of 32 KiB instead of three of 64 KiB) issues the same products
-    in the same K order as the 64-deep one: the factors agree to the last bits."""
-    from pyloworder_gb300 import datagen, vmmath
-    m, n = 262_144 + 128, 512
-    nx, ny = datagen.grid_for_points(m)
-    X = datagen.pod_field_device(nx, ny, n, 48, seed=78, noise=1e-5, amp_pow=1.5, m=m)
-    Y, _, _ = vmmath.remove_mean_device(X, n)
-    del X
-    with _Tuned("apply_narrow_bk", 64):
-        U1, S1, V1 = vmmath.tsqr_svd_device(Y, n, "mixed")
-    with _Tuned("apply_narrow_bk", 32):
-        U2, S2, V2 = vmmath.tsqr_svd_device(Y, n, "mixed")
-    s1, s2 = S1.double().cpu().numpy(), S2.double().cpu().numpy()
-    assert np.max(np.abs(s1 - s2)) <= 1e-6 * s1[0]
-    assert float((U1[:, :48].double() - U2[:, :48].double()).abs().max()) < 1e-5
