@@ -1609,8 +1609,10 @@ constexpr float JAC_PRE32_TOL = 2e-6f;     // pair orthogonality of the FP32 pha
 // quadratic range, and the pairs of smaller columns (a noise floor, which
 // the Jacobi ordering keeps rotating for several more sweeps) are only used
 // at the FP32 phase's accuracy.  The floor matches the refinement's.
+// (3e-4 against 1e-4: one sweep fewer on the 8,388,608 x 1,024 POD field, 9
+// instead of 10, with the same accuracy after the refinement.)
 constexpr float JAC_PRE32_FLOOR = 1e-5f;
-constexpr float JAC_PRE32_TSTOP = 1e-4f;
+constexpr float JAC_PRE32_TSTOP = 3e-4f;
 constexpr int JAC_PRE32_MAX_SWEEPS = 30;
 
 struct Jac32State {
