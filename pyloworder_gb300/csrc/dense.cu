@@ -333,6 +333,10 @@ int chol_shifted(const double* G, double* R, int n, int batch, double rel0, doub
   PLOM_CHECK_CUDA(cudaMemsetAsync(s.shifts_used, 0, sizeof(int), st));
   const int T = (n + NB - 1) / NB;
   int want = std::max(batch * std::max(1, T * (T + 1) / 2), 1);
+  // one problem: one CTA per SM (the FP64 pipe of an SM is shared by its
+  // CTAs, and fewer CTAs make each grid barrier cheaper: 9.8 -> 8.1 ms for the
+  // three factorisations of the 1,024 x 1,024 headline Grams)
+  if (batch == 1) want = std::min(want, num_sms());
   int blocks = coop_blocks((const void*)chol_coop_kernel, 256, 0, want);
   ProfScope prof("chol_fp64", st, (double)n * n * n / 3.0 * batch, 16.0 * n * n * batch);
   void* args[] = {(void*)&G,       (void*)&R,       (void*)&Dinv,     (void*)&n,
