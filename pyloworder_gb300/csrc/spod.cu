@@ -235,23 +235,28 @@ __global__ void __launch_bounds__(256) spod_fft32_kernel(
       for (int r = 0; r < E; ++r) z[r * 32 + lane] = make_float2(re[r], im[r]);
     }
     __syncthreads();
-    // Q[f][row][b]: one contiguous run of nBlks values per frequency.
+    // Q[f][row][b]: one contiguous run of nBlks values per frequency, a warp
+    // per frequency (its two spectrum slots and scale computed once), lanes
+    // along the blocks.
     // X_a[f] = (Z[f] + conj Z[N-f]) / 2,  X_b[f] = (Z[f] - conj Z[N-f]) / (2i)
     c2<float>* Qc = reinterpret_cast<c2<float>*>(Q);
-    for (int e = tid; e < nf * nBlks; e += blockDim.x) {
-      const int f = e / nBlks, b = e - f * nBlks;
-      const float2* z = zs + (size_t)(b >> 1) * ZP;
-      const float2 zk = z[slot(f)], zn = z[slot((N - f) & (N - 1))];
+    for (int f = warp; f < nf; f += 8) {
+      const int sk = slot(f), sn = slot((N - f) & (N - 1));
       const float g = 0.5f * ((f >= 1 && f <= nf - 2) ? 2.f * scale : scale);
-      c2<float> v;
-      if ((b & 1) == 0) {
-        v.re = (zk.x + zn.x) * g;
-        v.im = (zk.y - zn.y) * g;
-      } else {
-        v.re = (zk.y + zn.y) * g;
-        v.im = (zn.x - zk.x) * g;
+      c2<float>* qrow = Qc + ((int64_t)f * M + row) * nBlks;
+      for (int b = lane; b < nBlks; b += 32) {
+        const float2* z = zs + (size_t)(b >> 1) * ZP;
+        const float2 zk = z[sk], zn = z[sn];
+        c2<float> v;
+        if ((b & 1) == 0) {
+          v.re = (zk.x + zn.x) * g;
+          v.im = (zk.y - zn.y) * g;
+        } else {
+          v.re = (zk.y + zn.y) * g;
+          v.im = (zn.x - zk.x) * g;
+        }
+        qrow[b] = v;
       }
-      Qc[((int64_t)f * M + row) * nBlks + b] = v;
     }
     __syncthreads();
   }
@@ -328,35 +333,25 @@ static int spod_fft_impl(const T* Y, int64_t M, int64_t N, int64_t ldy, const T*
 // of one batched SVD (U_g: M x nBlks complex, interleaved, ustride complex
 // elements apart): pyLOM's column layout of the modes, real(U) flattened in
 // Fortran order into column ifreq of P (SPOD/wrapper.py:84).  A block stages
-// PB consecutive points' G x nBlks real parts per step (the PB points' values
-// of one frequency are contiguous in U) and writes them back
-// frequency-fastest (G contiguous values per point and block), so both the
-// reads and the writes are contiguous runs; PB points per step amortise the
-// two block barriers and keep several loads in flight per thread.
+// one point's G x nBlks real parts and writes them back frequency-fastest, so
+// both the reads (along b) and the writes (along f) are contiguous.
 template <typename T>
 __global__ void __launch_bounds__(256) spod_modes_kernel(const T* __restrict__ U, int64_t M,
                                                          int nBlks, int G, int64_t ustride,
                                                          T* __restrict__ P, int64_t nf, int64_t f0,
-                                                         int PB, int pitch) {
+                                                         int pitch) {
   extern __shared__ __align__(16) unsigned char modes_sm[];
-  T* tile = reinterpret_cast<T*>(modes_sm);  // [G][pitch]: point p, block b at p nBlks + b
-  const int per_g = PB * nBlks;
-  const int tot = G * per_g;
-  for (int64_t i0 = (int64_t)blockIdx.x * PB; i0 < M; i0 += (int64_t)gridDim.x * PB) {
-    const int np = (int)min((int64_t)PB, M - i0);
-    const int valid = np * nBlks;  // values per frequency in this step
-#pragma unroll 4
+  T* tile = reinterpret_cast<T*>(modes_sm);  // [G][pitch]
+  const int tot = G * nBlks;
+  for (int64_t i = blockIdx.x; i < M; i += gridDim.x) {
     for (int e = threadIdx.x; e < tot; e += blockDim.x) {
-      const int g = e / per_g, q = e - g * per_g;
-      if (q < valid) tile[g * pitch + q] = U[2 * ((int64_t)g * ustride + i0 * nBlks + q)];
+      const int g = e / nBlks, b = e - g * nBlks;
+      tile[g * pitch + b] = U[2 * ((int64_t)g * ustride + i * nBlks + b)];
     }
     __syncthreads();
-    const int per_b = np * G;
-#pragma unroll 4
-    for (int e = threadIdx.x; e < nBlks * per_b; e += blockDim.x) {
-      const int bb = e / per_b, r = e - bb * per_b;
-      const int pp = r / G, g = r - pp * G;
-      P[((int64_t)bb * M + i0 + pp) * nf + f0 + g] = tile[g * pitch + pp * nBlks + bb];
+    for (int e = threadIdx.x; e < tot; e += blockDim.x) {
+      const int b = e / G, g = e - b * G;
+      P[((int64_t)b * M + i) * nf + f0 + g] = tile[g * pitch + b];
     }
     __syncthreads();
   }
@@ -365,11 +360,7 @@ __global__ void __launch_bounds__(256) spod_modes_kernel(const T* __restrict__ U
 template <typename T>
 static int spod_modes_impl(const T* U, int64_t G, int64_t M, int64_t nBlks, int64_t ustride, T* P,
                            int64_t nf, int64_t f0, cudaStream_t st) {
-  // points per step: up to 8, within 96 KiB of staging (two blocks per SM)
-  const size_t cap = 96 * 1024;
-  int PB = 8;
-  while (PB > 1 && sizeof(T) * (size_t)G * (size_t)((PB * nBlks) | 1) > cap) --PB;
-  const int pitch = (int)((PB * nBlks) | 1);  // odd pitch: the frequency-fastest reads spread over banks
+  const int pitch = (int)(nBlks | 1);  // odd pitch: the frequency-fastest reads spread over banks
   const size_t smem = sizeof(T) * (size_t)G * pitch;
   PLOM_REQUIRE(smem <= 200 * 1024, PLOM_ERR_UNSUPPORTED,
                "spod_modes: %lld frequencies x %lld blocks do not fit in shared memory",
@@ -377,10 +368,10 @@ static int spod_modes_impl(const T* U, int64_t G, int64_t M, int64_t nBlks, int6
   if (smem > 48 * 1024)
     PLOM_CHECK_CUDA(cudaFuncSetAttribute(spod_modes_kernel<T>,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  const int64_t grid = std::min<int64_t>(cdiv(M, PB), (int64_t)num_sms() * 8);
+  const int64_t grid = std::min<int64_t>(M, (int64_t)num_sms() * 8);
   ProfScope prof("spod_modes", st, 0.0, (double)sizeof(T) * 3.0 * G * M * nBlks);
   spod_modes_kernel<T><<<(unsigned)grid, 256, smem, st>>>(U, M, (int)nBlks, (int)G, ustride, P, nf,
-                                                          f0, PB, pitch);
+                                                          f0, pitch);
   PLOM_CHECK_LAUNCH();
   return PLOM_OK;
 }

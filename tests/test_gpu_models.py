@@ -237,8 +237,7 @@ def test_spod_assemble(dt, rows, nf, G):
                                               (43, 1003, 63, 129, 43)])
 def test_spod_mode_layout(dt, G, M, nBlks, nf, f0):
     """P[(b M + i) nf + f0 + g] = Re U_g[i][b] (pyLOM's Fortran-order columns).
-    (43, 1003, 63, 129, 43): a group of SPOD's 129 frequencies with 63 blocks,
-    staged 8 points a step in FP32 and 4 in FP64, with a ragged last step."""
+    (43, 1003, 63, 129, 43): a group of SPOD's 129 frequencies with 63 blocks."""
     from pyloworder_gb300 import _lib as L
     g = torch.Generator(device="cuda")
     g.manual_seed(G * 1000 + M)
