@@ -1612,11 +1612,12 @@ constexpr float JAC_PRE32_TOL = 2e-6f;     // pair orthogonality of the FP32 pha
 // JAC_PRE32_TSTOP: those pairs are then well inside the refinement's
 // quadratic range, and the pairs of smaller columns (a noise floor, which
 // the Jacobi ordering keeps rotating for several more sweeps) are only used
-// at the FP32 phase's accuracy.  The floor matches the refinement's.
-// (3e-4 against 1e-4: one sweep fewer on the 8,388,608 x 1,024 POD field, 9
-// instead of 10, with the same accuracy after the refinement.)
+// at the FP32 phase's accuracy.  The floor matches the refinement's, and the
+// refinement's first step takes angles of 3e-3 down to ~1e-5 (measured on two
+// 8,388,608 x 1,024 POD fields: 8 and 9 sweeps with 3e-3, 10 with 1e-4, the
+// same sigma, subspace angle and orthogonality after the refinement).
 constexpr float JAC_PRE32_FLOOR = 1e-5f;
-constexpr float JAC_PRE32_TSTOP = 3e-4f;
+constexpr float JAC_PRE32_TSTOP = 3e-3f;
 constexpr int JAC_PRE32_MAX_SWEEPS = 30;
 
 struct Jac32State {
