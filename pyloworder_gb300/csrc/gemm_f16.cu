@@ -2560,10 +2560,10 @@ int apply_packed(const Packed& p, const double* W, int64_t ldw, int64_t k, float
   const int64_t row_tiles = cdiv(p.mp, 128);
   const int64_t tiles = batch * row_tiles * col_tiles;
   // whole row blocks per CTA pay for the triangular case (column tiles of very
-  // different lengths); the dense case keeps concurrent tiles of one row
-  // block on different SMs (fewer DRAM re-reads)
-  const bool tri_pre = upper && k == p.N;
-  const int by_rows = ((tri_pre ? tuning().apply_tri_by_rows : tuning().apply_dense_by_rows) &&
+  // different lengths; interleaved single tiles measured 10 % slower there);
+  // the dense case keeps concurrent tiles of one row block on different SMs
+  // (fewer DRAM re-reads)
+  const int by_rows = ((tri_w ? tuning().apply_tri_by_rows : tuning().apply_dense_by_rows) &&
                        batch * row_tiles >= 2 * num_sms())
                           ? 1
                           : 0;
@@ -2577,7 +2577,7 @@ int apply_packed(const Packed& p, const double* W, int64_t ldw, int64_t k, float
   o.ldo = out ? (int)out->ld : 0;
   // an upper-triangular W (k = N) needs m N (N + 1) flops: row i of W meets
   // columns j >= i only
-  const bool tri = tri_pre;
+  const bool tri = tri_w;
   const double flops = tri ? (double)m * p.N * (p.N + 1) * batch : 2.0 * m * p.N * k * batch;
   ProfScope prof(pair ? "tc_apply_f16x3_pair" : "tc_apply_f16x3", st, flops,
                  4.0 * ((double)m * p.ld + (double)m * k) * batch);
