@@ -52,7 +52,8 @@ def _profiled(fn):
     return out, names
 
 
-@pytest.mark.parametrize("m,N,k", [(262_344, 320, 300), (131_072, 1024, 1024), (70_000, 192, 1000)])
+@pytest.mark.parametrize("m,N,k", [(262_344, 320, 300), (131_072, 1024, 1024), (70_000, 192, 1000),
+                                   (100, 320, 300), (1, 192, 200)])
 def test_packed_apply_pair_matches_single_sm(m, N, k):
     from pyloworder_gb300 import vmmath
     g = torch.Generator(device="cuda").manual_seed(m + N + k)
